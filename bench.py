@@ -1,0 +1,357 @@
+"""Benchmark: 2.5D space-charge macroparticle-kicks/s on the FODO workload
+(1e6 protons at 1 GeV, 128x128x64 grid, 40 TEAPOT FODO cells with 4 SC
+nodes each = 160 SC kicks per turn), plain FP64 form by default.
+
+One step = one turn of the lattice over the whole bunch (160 kicks).
+  value  : device-timed throughput with the bunch resident in HBM; the L2
+           (129 MB > the 48 MB bunch) is flushed by writing a 512 MiB buffer
+           before every timed step.
+  e2e    : the same metric through the reference-facing API with host
+           buffers: per step, upload the coordinates from pinned host memory,
+           Lattice.trackBunch, download the coordinates to pinned memory.
+  --impl reference : the CPU restatement of the reference algorithm
+           (oracle/, all host threads as MPI-rank-like slices) on a bounded
+           sample of the same workload.
+Multi-GPU (torchrun): independent replicas, one bunch per rank (the path
+has no data-path collective in a one-GPU-per-bunch layout).
+"""
+from __future__ import annotations
+
+import argparse
+import contextlib
+import io
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "py-orbit_gb300"))
+
+N_PARTICLES = 1_000_000
+GRID = (128, 128, 64)
+CELLS = 40
+METRIC = "2.5D SC macroparticle-kicks/s, 1M particles 128x128 grid, vs FP64 plain form"
+CPU_SAMPLE_N = 250_000
+
+# Algorithmic work per particle for the roofline (counted from the restated
+# formulas): HBM bytes of each particle kernel.
+ALG_BYTES = {"pass_kick_maps": 96, "pass_maps": 96, "deposit": 24, "extrema": 24, "kick": 56}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--form", default="plain", choices=["plain", "fp32"])
+    ap.add_argument("--n", type=int, default=N_PARTICLES)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def quiet():
+    return contextlib.redirect_stdout(io.StringIO())
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+# FP64 FMA throughput measured on this machine's GB300 with a DFMA-chain kernel
+# (profiles/fp64_pipe_peak.md): 593 G DFMA/s = 1.186 TFLOP/s.
+FP64_PEAK_TFLOPS = 1.186
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                          "-i", str(self.index), "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_workload(n, form, seed):
+    from orbit_gb300 import workloads as W
+    from spacecharge import SpaceChargeCalc2p5D
+    soa = W.c2_coords(n, seed=seed)
+    bunch = W.make_bunch(soa, W.C2_MACROSIZE * (N_PARTICLES / n))
+    calc = SpaceChargeCalc2p5D(*GRID, form=form)
+    with quiet():
+        lat = W.fodo_lattice(calc, cells=CELLS)
+    return soa, bunch, calc, lat
+
+
+def cpu_reference_rate(n_sample, turns, warmup, threads):
+    """Times the CPU restatement of the reference (oracle) on a sample of the
+    FODO workload; returns (kicks/s, seconds per turn, kicks per turn)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from orbit_gb300 import workloads as W
+    from orbit.teapot.recording import BunchRecorder
+    from orbit.lattice import AccActionsContainer
+    soa = W.c2_coords(n_sample, seed=99)
+
+    class _Calc:  # records SC nodes without a GPU calculator
+        def trackBunch(self, bunch, length, boundary=None):
+            bunch._record_sc(self, length)
+
+    with quiet():
+        lat = W.fodo_lattice(_Calc(), cells=CELLS)
+    bunch = W.make_bunch(soa, W.C2_MACROSIZE * (N_PARTICLES / n_sample))
+    rec = BunchRecorder(bunch)
+    cont = AccActionsContainer()
+    cont.addAction(lambda p: p["node"].track(p), AccActionsContainer.BODY)
+    lat.trackActions(cont, {"bunch": rec, "useCharge": 1})
+    ops = rec.ops
+    kicks_per_turn = sum(1 for o in ops if o[0] == 32)
+    s = bunch.getSyncParticle()
+    sync = O.make_sync(beta=s.beta(), gamma=s.gamma(), momentum=s.momentum(), macrosize=bunch.macroSize())
+    sc = [O.OracleSC(*GRID)]
+    a = soa.copy()
+    for _ in range(warmup):
+        O.run_program(ops, 1, a, sync, sc, nthreads=threads)
+    times = []
+    for _ in range(turns):
+        t0 = time.perf_counter()
+        rc = O.run_program(ops, 1, a, sync, sc, nthreads=threads)
+        times.append(time.perf_counter() - t0)
+        if rc != 0:
+            raise RuntimeError("oracle status %d" % rc)
+    total = sum(times)
+    return n_sample * kicks_per_turn * turns / total, total / turns, kicks_per_turn
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    rate, per_turn, kpt = cpu_reference_rate(CPU_SAMPLE_N, args.steps, args.warmup, threads)
+    ms_per_step = per_turn * 1e3
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": "macroparticle-kicks/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded 4D waterbag, Gaussian z/dE)",
+        "config": {"workload": "FODO 40 cells, 160 SC kicks/turn, grid 128x128x64, sample %d particles"
+                   % CPU_SAMPLE_N, "particles": CPU_SAMPLE_N, "grid": list(GRID), "kicks_per_step": kpt},
+        "cpu_baseline": {"value": rate, "unit": "macroparticle-kicks/s", "cores": threads, "kind": "port",
+                         "sample": "%d particles x 1 turn (%d SC kicks) per step, %d threads as rank slices"
+                                   % (CPU_SAMPLE_N, kpt, threads)},
+        "e2e": {"value": rate, "unit": "macroparticle-kicks/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    rank, world, local = dist_env()
+    dist = None
+    if world > 1:
+        import torch.distributed as tdist
+        torch.cuda.set_device(local)
+        tdist.init_process_group("nccl")
+        dist = tdist
+    os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("CUDA_VISIBLE_DEVICES", ""))
+    torch.cuda.init()
+    n = args.n
+    soa, bunch, calc, lat = build_workload(n, args.form, seed=1000 + rank)
+    prog = lat.fusedProgram(bunch)
+    dev = bunch._device_bunch()
+    stream = torch.cuda.ExternalStream(dev.stream_ptr())
+    kicks_per_turn = sum(1 for o in prog.ops if o[0] == 32)
+    launches_per_turn = None
+    for _ in range(max(args.warmup, 1)):
+        prog.run(bunch, 1)
+    launches_per_turn = prog.launches_per_turn()
+    # per-kernel times of one eager turn (CUDA events on the bunch's stream)
+    prof = prog.device.profile(dev)
+    bunch._device_modified()
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        torch.cuda.synchronize()
+        dev.sync()
+        if dist is not None:
+            dist.barrier()
+
+    clocks = ClockSampler(local)
+    barrier()
+    clocks.start()
+    step_ms = []
+    wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        prog.device.enqueue(dev, 1)
+        e1.record(stream)
+        dev.sync()
+        step_ms.append(e0.elapsed_time(e1))
+    wall = time.perf_counter() - wall0
+    barrier()
+    clk = clocks.stop()
+    bunch._device_modified()
+    total_ms = sum(step_ms)
+    if dist is not None:
+        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    kicks = world * n * kicks_per_turn * args.steps
+    value = kicks / (total_ms * 1e-3)
+
+    # ---- end to end through the public API with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        pin_in = torch.empty((6, n), dtype=torch.float64, pin_memory=True).numpy()
+        pin_out = torch.empty((6, n), dtype=torch.float64, pin_memory=True).numpy()
+        pin_in[...] = soa
+        e2e_ms = []
+        for i in range(args.steps + 1):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            bunch.setCoordinates(pin_in, copy=False)
+            lat.trackBunch(bunch)
+            bunch.getCoordinates(out=pin_out)
+            t1 = time.perf_counter()
+            if i > 0:  # the first call re-records and re-captures the graphs
+                e2e_ms.append((t1 - t0) * 1e3)
+        tot = sum(e2e_ms)
+        if dist is not None:
+            t = torch.tensor([tot], dtype=torch.float64, device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            tot = float(t.item())
+        e2e = {"value": world * n * kicks_per_turn * len(e2e_ms) / (tot * 1e-3), "unit": "macroparticle-kicks/s",
+               "h2d_bytes_per_step": int(pin_in.nbytes), "d2h_bytes_per_step": int(pin_out.nbytes),
+               "ms_per_step": tot / len(e2e_ms)}
+
+    if rank != 0:
+        return
+    # ---- roofline of the dominant kernel (largest share of the eager turn)
+    hbm_peak, peak_kind = measured_peaks()
+    turn_ms = sum(v[0] for v in prof.values())
+    dom = max(prof.items(), key=lambda kv: kv[1][0])
+    name, (dom_ms, dom_launches) = dom
+    per_launch_ms = dom_ms / dom_launches
+    alg_bytes = ALG_BYTES.get(name, 0) * n
+    achieved = alg_bytes / (per_launch_ms * 1e-3) / 1e9 if alg_bytes else None
+    roofline = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": (achieved / hbm_peak) if achieved else None, "traffic": TRAFFIC.get((args.form, name)),
+                "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_kind if peak_kind == "measured"
+                else "fallback 6.8 TB/s",
+                "kernel_ms_per_launch": per_launch_ms, "share_of_turn": dom_ms / turn_ms,
+                "kernels": {k: {"ms": v[0], "launches": v[1], "share": v[0] / turn_ms} for k, v in prof.items()}}
+    fl = FP64_OPS.get((args.form, name))
+    if fl:
+        tf = fl * n / (per_launch_ms * 1e-3) / 1e12
+        roofline["fp64_pipe"] = {"achieved_tflops": tf, "peak_tflops": FP64_PEAK_TFLOPS, "frac": tf / FP64_PEAK_TFLOPS,
+                                 "fp64_ops_per_particle": fl,
+                                 "peak_source": "measured DFMA-chain peak, profiles/fp64_pipe_peak.md"}
+    cpu = None
+    if not args.no_cpu:
+        threads = os.cpu_count() or 1
+        rate, per_turn, kpt = cpu_reference_rate(CPU_SAMPLE_N, 1, 0, threads)
+        cpu = {"value": rate, "unit": "macroparticle-kicks/s", "cores": threads, "kind": "port",
+               "sample": "%d particles x 1 turn (%d SC kicks), %d threads as rank slices" % (CPU_SAMPLE_N, kpt,
+                                                                                         threads)}
+    line = {
+        "metric": METRIC, "value": value, "unit": "macroparticle-kicks/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if args.form == "plain" else "f32-field/f64-coords",
+        "data": "synthetic (seeded 4D waterbag rms 4 mm/0.8 mrad, z~N(0,10 m), dE~N(0,1 MeV))",
+        "config": {"workload": "FODO 40 cells x 4 SC nodes, %d particles, grid %dx%dx%d, one turn per step"
+                   % (n, *GRID), "form": args.form, "particles": n, "grid": list(GRID),
+                   "kicks_per_step": kicks_per_turn, "l2": "flushed (512 MiB write) before each timed step",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+        "gpu_launches": launches_per_turn * args.steps, "wall_s": wall,
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+# DRAM traffic per launch from ncu (dram__bytes_read.sum + dram__bytes_write.sum),
+# filled from the committed summaries under profiles/ once captured.
+TRAFFIC = {}
+# FP64-pipe operations per particle for the fused pass and deposit kernels of
+# the plain form, counted from the restated formulas.
+FP64_OPS = {}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,198 @@
+/*
+ * orbit_gb300 -- C ABI of the GB300-native PyORBIT 2.5D space-charge and
+ * TEAPOT tracking hot path.
+ *
+ * One shared library (liborbit_gb300.so) exports these entry points.  All
+ * signatures use plain C types and pointers; no framework types cross the
+ * boundary.  Every function returns an int status (ORBIT_OK == 0, negative on
+ * error) and records a message retrievable with orbit_last_error().  The
+ * reference aborts the process on these conditions (ORBIT_MPI_Finalize, e.g.
+ * src/spacecharge/SpaceChargeCalc2p5D.cc:131-143, Grid2D.cc:38-52,
+ * PoissonSolverFFT2D.cc:30-42); this library reports them instead.
+ *
+ * Execution model: each bunch owns one CUDA stream.  Compute calls enqueue
+ * work on the bunch's stream and return; orbit_bunch_sync() and the
+ * download calls wait for it and report any error the kernels recorded in
+ * the bunch's device status word.  Coordinates stay resident in HBM as six
+ * FP64 arrays (x, xp, y, yp, z, dE) between calls.
+ */
+#ifndef ORBIT_GB300_H
+#define ORBIT_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ */
+/* status codes                                                        */
+/* ------------------------------------------------------------------ */
+#define ORBIT_OK 0
+#define ORBIT_ERR_ARG (-1)      /* bad handle, size or parameter */
+#define ORBIT_ERR_EXTENT (-2)   /* zero beam extent (SpaceChargeCalc2p5D.cc:131-143) */
+#define ORBIT_ERR_GRID (-3)     /* grid too small (Grid2D.cc:40-51, Grid1D.cc:70-82) */
+#define ORBIT_ERR_CUDA (-4)     /* CUDA runtime error */
+#define ORBIT_ERR_NAN (-5)      /* non-finite coordinate met by the extrema scan */
+#define ORBIT_ERR_DEVICE (-6)   /* device-side range check failed */
+#define ORBIT_ERR_NOMEM (-8)    /* device allocation failed */
+#define ORBIT_ERR_UNSUPPORTED (-9)
+
+/* Copies the calling thread's last error message (NUL terminated) into buf.
+ * Returns the message length. */
+int orbit_last_error(char* buf, int len);
+
+/* Library version string, e.g. "orbit_gb300 0.1 sm_103a". */
+const char* orbit_version(void);
+
+/* ------------------------------------------------------------------ */
+/* Bunch: device-resident SoA macroparticle container                 */
+/* replaces Bunch (src/orbit/Bunch.hh:60-136, AoS double[6] rows) and  */
+/* SyncPart kinematics (src/orbit/SyncPart.cc:236-306)                 */
+/* ------------------------------------------------------------------ */
+typedef struct orbit_bunch orbit_bunch_t;
+
+/* Reference-particle data the maps and the SC kick read. `time` is advanced
+ * by drift/quad1/bend1 exactly as SyncPart::setTime is in teapotbase.cc:164-165,
+ * 638-642, 1109-1113. */
+typedef struct {
+  double beta, gamma, momentum, mass, charge, classical_radius, macrosize, time;
+} orbit_sync_t;
+
+int orbit_bunch_create(orbit_bunch_t** out, int capacity);
+int orbit_bunch_destroy(orbit_bunch_t* b);
+/* Host SoA -> device: soa[c] points at n doubles for c = x,xp,y,yp,z,dE. */
+int orbit_bunch_upload(orbit_bunch_t* b, const double* const* soa, int n);
+/* Device -> host, same layout; waits for pending work. */
+int orbit_bunch_download(orbit_bunch_t* b, double* const* soa);
+/* Device SoA -> device: for callers that already hold device arrays. */
+int orbit_bunch_upload_device(orbit_bunch_t* b, const double* const* dev_soa, int n);
+int orbit_bunch_size(const orbit_bunch_t* b, int* n);
+int orbit_bunch_set_sync(orbit_bunch_t* b, const orbit_sync_t* s);
+int orbit_bunch_get_sync(const orbit_bunch_t* b, orbit_sync_t* s);
+/* Per-particle "macrosize" attribute (Grid2D.cc:123-131); NULL removes it. */
+int orbit_bunch_set_macrosizes(orbit_bunch_t* b, const double* m, int n);
+/* The six device coordinate arrays (valid until the next upload/resize). */
+int orbit_bunch_device_coords(orbit_bunch_t* b, double** dev_soa);
+/* Waits for the bunch's stream and reports device-side errors. */
+int orbit_bunch_sync(orbit_bunch_t* b);
+/* The bunch's CUDA stream as an opaque pointer (cudaStream_t). */
+int orbit_bunch_stream(orbit_bunch_t* b, void** stream);
+
+/* ------------------------------------------------------------------ */
+/* SpaceChargeCalc2p5D (src/spacecharge/SpaceChargeCalc2p5D.cc:25-234) */
+/* ------------------------------------------------------------------ */
+typedef struct orbit_sc2p5d orbit_sc2p5d_t;
+
+#define ORBIT_FORM_PLAIN 0   /* FP64 throughout: the drop-in */
+#define ORBIT_FORM_FP32 1    /* deposit/FFT/gradient FP32, coordinates and kick FP64 */
+
+/* SpaceChargeCalc2p5D(xSize, ySize, zSize[, xy_ratio]); xy_ratio <= 0 means
+ * the 3-argument constructor (wrap_spacechargecalc2p5d.cc:38-52). */
+int orbit_sc2p5d_create(orbit_sc2p5d_t** out, int nx, int ny, int nz, double xy_ratio, int form);
+int orbit_sc2p5d_destroy(orbit_sc2p5d_t* c);
+/* trackBunch(bunch, length) without a boundary (SpaceChargeCalc2p5D.cc:77-120).
+ * Enqueued on the bunch's stream. */
+int orbit_sc2p5d_track(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length);
+
+#define ORBIT_GRID_RHO 0
+#define ORBIT_GRID_PHI 1
+#define ORBIT_GRID_LONG 2
+/* getRhoGrid / getPhiGrid (nx*ny, row-major [ix][iy]) and getLongGrid (nz)
+ * copied to host (wrap_spacechargecalc2p5d.cc:55-115).  Waits for the last
+ * stream the calculator ran on. */
+int orbit_sc2p5d_get_grid(orbit_sc2p5d_t* c, int which, double* host_out);
+/* lim = {xmin,xmax,ymin,ymax,zmin,zmax,dx,dy,dz,xy_ratio,total_macrosize} */
+int orbit_sc2p5d_get_limits(orbit_sc2p5d_t* c, double* lim);
+int orbit_sc2p5d_get_sizes(const orbit_sc2p5d_t* c, int* nx, int* ny, int* nz, int* form);
+/* Grid2D::calcGradient + Grid1D::getValue at n host points with the current
+ * grids (Grid2D.cc:212-256, Grid1D.cc:191-211). */
+int orbit_sc2p5d_fields(orbit_sc2p5d_t* c, int n, const double* x, const double* y, const double* z,
+                        double* ex, double* ey, double* lam);
+
+/* ------------------------------------------------------------------ */
+/* teapot_base maps (src/teapot/teapotbase.cc; Python names in         */
+/* src/teapot/wrap_teapotbase.cc:488-512).  The useCharge argument of  */
+/* the reference is accepted by the Python layer and ignored there too */
+/* ------------------------------------------------------------------ */
+int orbit_tpb_rotatexy(orbit_bunch_t* b, double angle);
+int orbit_tpb_drift(orbit_bunch_t* b, double length);
+int orbit_tpb_wrapbunch(orbit_bunch_t* b, double length);
+int orbit_tpb_kick(orbit_bunch_t* b, double kx, double ky, double kE);
+int orbit_tpb_multp(orbit_bunch_t* b, int pole, double kl, int skew);
+int orbit_tpb_multpfringeIN(orbit_bunch_t* b, int pole, double kl, int skew);
+int orbit_tpb_multpfringeOUT(orbit_bunch_t* b, int pole, double kl, int skew);
+int orbit_tpb_quad1(orbit_bunch_t* b, double length, double kq);
+int orbit_tpb_quad2(orbit_bunch_t* b, double length);
+int orbit_tpb_quadfringeIN(orbit_bunch_t* b, double kq);
+int orbit_tpb_quadfringeOUT(orbit_bunch_t* b, double kq);
+int orbit_tpb_wedgerotate(orbit_bunch_t* b, double e, int frinout);
+int orbit_tpb_wedgedrift(orbit_bunch_t* b, double e, int inout);
+int orbit_tpb_wedgebend(orbit_bunch_t* b, double e, int inout, double rho, int nsteps);
+int orbit_tpb_bend1(orbit_bunch_t* b, double length, double th);
+int orbit_tpb_bend2(orbit_bunch_t* b, double length);
+int orbit_tpb_bend3(orbit_bunch_t* b, double th);
+int orbit_tpb_bend4(orbit_bunch_t* b, double th);
+int orbit_tpb_bendfringeIN(orbit_bunch_t* b, double rho);
+int orbit_tpb_bendfringeOUT(orbit_bunch_t* b, double rho);
+
+/* ------------------------------------------------------------------ */
+/* Lattice programs: a recorded node sequence replayed on the device   */
+/* (AccNode.trackActions order, py/orbit/lattice/AccNode.py:302-350)   */
+/* ------------------------------------------------------------------ */
+#define ORBIT_OP_DRIFT 1      /* d0 = length */
+#define ORBIT_OP_QUAD1 2      /* d0 = length, d1 = kq */
+#define ORBIT_OP_QUAD2 3      /* d0 = length */
+#define ORBIT_OP_QFRIN 4      /* d0 = kq */
+#define ORBIT_OP_QFROUT 5     /* d0 = kq */
+#define ORBIT_OP_BEND1 6      /* d0 = length, d1 = theta */
+#define ORBIT_OP_BEND2 7      /* d0 = length */
+#define ORBIT_OP_BEND3 8      /* d0 = theta */
+#define ORBIT_OP_BEND4 9      /* d0 = theta */
+#define ORBIT_OP_BFRIN 10     /* d0 = rho */
+#define ORBIT_OP_BFROUT 11    /* d0 = rho */
+#define ORBIT_OP_MULTP 12     /* i0 = pole, i1 = skew, d0 = kl */
+#define ORBIT_OP_MPFRIN 13    /* i0 = pole, i1 = skew, d0 = kl */
+#define ORBIT_OP_MPFROUT 14   /* i0 = pole, i1 = skew, d0 = kl */
+#define ORBIT_OP_ROTXY 15     /* d0 = angle */
+#define ORBIT_OP_WRAP 16      /* d0 = ring length */
+#define ORBIT_OP_KICK 17      /* d0 = kx, d1 = ky, d2 = kE */
+#define ORBIT_OP_WEDGEROT 18  /* d0 = e, i0 = frinout */
+#define ORBIT_OP_WEDGEDRIFT 19 /* d0 = e, i0 = inout */
+#define ORBIT_OP_WEDGEBEND 20 /* d0 = e, i0 = inout, d1 = rho, i1 = nsteps */
+#define ORBIT_OP_SC 32        /* i0 = calculator index, d0 = sc length */
+
+typedef struct {
+  int32_t code, i0, i1, i2;
+  double d[6];
+} orbit_op_t;
+
+typedef struct orbit_program orbit_program_t;
+
+/* Compiles ops into fused device passes: all maps between two SC kicks run
+ * in one particle pass together with the previous kick and the next extrema
+ * scan.  calcs[i] serves ORBIT_OP_SC ops with i0 == i. */
+int orbit_program_create(orbit_program_t** out, const orbit_op_t* ops, int nops,
+                         orbit_sc2p5d_t* const* calcs, int ncalcs);
+int orbit_program_destroy(orbit_program_t* p);
+/* Runs the program `turns` times on the bunch (captured once per bunch as a
+ * CUDA graph and replayed) and advances the bunch's sync time. Waits for
+ * completion and reports device errors. */
+int orbit_program_run(orbit_program_t* p, orbit_bunch_t* b, int turns);
+/* As orbit_program_run, but only enqueues the graphs on the bunch's stream;
+ * orbit_bunch_sync() waits and reports device errors. */
+int orbit_program_enqueue(orbit_program_t* p, orbit_bunch_t* b, int turns);
+/* Number of kernel launches one pass of the program issues. */
+int orbit_program_launches(const orbit_program_t* p, int* launches);
+/* Runs one turn without graph capture, timing every launch with CUDA events
+ * on the bunch's stream; per kernel kind k < *nkinds: names[32*k] (NUL
+ * terminated), total milliseconds and launch count.  Advances the bunch like
+ * orbit_program_run(p, b, 1). */
+int orbit_program_profile(orbit_program_t* p, orbit_bunch_t* b, int max_kinds, char* names, double* total_ms,
+                          int* launches, int* nkinds);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

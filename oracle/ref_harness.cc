@@ -1,0 +1,150 @@
+// ORACLE / TEST INFRASTRUCTURE ONLY.
+//
+// C-ABI harness over the UNMODIFIED reference C++ (PyORBIT src/orbit,
+// src/spacecharge, src/teapot), compiled in place from the reference tree by
+// oracle/build_ref.sh into oracle/_ref/.  It replaces the Python-2 wrappers
+// (src/spacecharge/wrap_spacechargecalc2p5d.cc, src/teapot/wrap_teapotbase.cc,
+// src/orbit/wrap_bunch.cc, src/orbit/wrap_syncpart.cc) so that ctypes can
+// drive the reference's own hot path from Python 3.  It is used only to pin
+// the CPU restatement (oracle/orbit_oracle.c) and to generate golden vectors;
+// it never ships in the product library and cannot run on the GPU host
+// (the reference tree is not there).
+#include "Bunch.hh"
+#include "SyncPart.hh"
+#include "SpaceChargeCalc2p5D.hh"
+#include "Grid1D.hh"
+#include "Grid2D.hh"
+#include "teapotbase.hh"
+
+#include <cstdlib>
+
+// The reference's Bunch() asks the Python MPI-comm wrapper for a
+// communicator (src/orbit/Bunch.cc:59,107).  Without MPI and without the
+// Python-2 wrapper module, a heap object holding MPI_COMM_WORLD stands in.
+namespace wrap_orbit_mpi_comm {
+pyORBIT_MPI_Comm* newMPI_Comm() {
+  pyORBIT_MPI_Comm* c = (pyORBIT_MPI_Comm*)calloc(1, sizeof(pyORBIT_MPI_Comm));
+  c->comm = MPI_COMM_WORLD;
+  return c;
+}
+void freeMPI_Comm(pyORBIT_MPI_Comm* c) { free(c); }
+}  // namespace wrap_orbit_mpi_comm
+
+extern "C" {
+
+void* ref_bunch_new() {
+  teapot_base::init_factorial();
+  return new Bunch();
+}
+void ref_bunch_free(void* b) { delete (Bunch*)b; }
+
+// Same steps as SyncPart_kinEnergy(value) (src/orbit/wrap_syncpart.cc:70-93).
+double ref_bunch_set_kin_energy(void* b, double ek) {
+  SyncPart* s = ((Bunch*)b)->getSyncPart();
+  double p = s->energyToMomentum(ek);
+  s->setMomentum(p);
+  return s->momentumToEnergy(p);
+}
+void ref_bunch_set_macrosize(void* b, double m) { ((Bunch*)b)->setMacroSize(m); }
+void ref_bunch_set_mass(void* b, double m) { ((Bunch*)b)->setMass(m); }
+void ref_bunch_set_charge(void* b, double c) { ((Bunch*)b)->setCharge(c); }
+int ref_bunch_size(void* b) { return ((Bunch*)b)->getSize(); }
+
+// kin[0..6] = beta, gamma, momentum, kinetic energy, mass, classical radius, time
+void ref_bunch_kinematics(void* b, double* kin) {
+  Bunch* bb = (Bunch*)b;
+  SyncPart* s = bb->getSyncPart();
+  kin[0] = s->getBeta();
+  kin[1] = s->getGamma();
+  kin[2] = s->getMomentum();
+  kin[3] = s->getEnergy();
+  kin[4] = bb->getMass();
+  kin[5] = bb->getClassicalRadius();
+  kin[6] = s->getTime();
+}
+
+// soa: x[n], xp[n], y[n], yp[n], z[n], dE[n]
+void ref_bunch_add(void* b, int n, const double* soa) {
+  Bunch* bb = (Bunch*)b;
+  for (int i = 0; i < n; ++i)
+    bb->addParticle(soa[i], soa[n + i], soa[2 * n + i], soa[3 * n + i], soa[4 * n + i], soa[5 * n + i]);
+}
+void ref_bunch_get(void* b, double* soa) {
+  Bunch* bb = (Bunch*)b;
+  int n = bb->getSize();
+  double** a = bb->coordArr();
+  for (int i = 0; i < n; ++i)
+    for (int c = 0; c < 6; ++c) soa[c * n + i] = a[i][c];
+}
+void ref_bunch_set(void* b, const double* soa) {
+  Bunch* bb = (Bunch*)b;
+  int n = bb->getSize();
+  double** a = bb->coordArr();
+  for (int i = 0; i < n; ++i)
+    for (int c = 0; c < 6; ++c) a[i][c] = soa[c * n + i];
+}
+
+// Same constructor choice as SpaceChargeCalc2p5D_init
+// (src/spacecharge/wrap_spacechargecalc2p5d.cc:38-52).
+void* ref_sc_new(int nx, int ny, int nz, double xy_ratio) {
+  if (xy_ratio > 0.) return new SpaceChargeCalc2p5D(nx, ny, nz, xy_ratio);
+  return new SpaceChargeCalc2p5D(nx, ny, nz);
+}
+void ref_sc_free(void* sc) { delete (SpaceChargeCalc2p5D*)sc; }
+void ref_sc_track(void* sc, void* b, double length) {
+  ((SpaceChargeCalc2p5D*)sc)->trackBunch((Bunch*)b, length, NULL);
+}
+// rho/phi: nx*ny row-major [ix][iy]; zg: nz; lim: xmin,xmax,ymin,ymax,zmin,zmax,dx,dy,dz
+void ref_sc_grids(void* sc, double* rho, double* phi, double* zg, double* lim) {
+  SpaceChargeCalc2p5D* c = (SpaceChargeCalc2p5D*)sc;
+  Grid2D* r = c->getRhoGrid();
+  Grid2D* p = c->getPhiGrid();
+  Grid1D* z = c->getLongGrid();
+  int nx = r->getSizeX(), ny = r->getSizeY();
+  for (int i = 0; i < nx; ++i)
+    for (int j = 0; j < ny; ++j) {
+      rho[i * ny + j] = r->getValueOnGrid(i, j);
+      phi[i * ny + j] = p->getValueOnGrid(i, j);
+    }
+  for (int k = 0; k < z->getSizeZ(); ++k) zg[k] = z->getValueOnGrid(k);
+  lim[0] = r->getMinX(); lim[1] = r->getMaxX();
+  lim[2] = r->getMinY(); lim[3] = r->getMaxY();
+  lim[4] = z->getMinZ(); lim[5] = z->getMaxZ();
+  lim[6] = r->getStepX(); lim[7] = r->getStepY(); lim[8] = z->getStepZ();
+}
+// Per-particle gradient of the current phi grid and lambda(z), as the kick
+// loop evaluates them (src/spacecharge/SpaceChargeCalc2p5D.cc:104-119).
+void ref_sc_fields(void* sc, int n, const double* x, const double* y, const double* z,
+                   double* ex, double* ey, double* lam) {
+  SpaceChargeCalc2p5D* c = (SpaceChargeCalc2p5D*)sc;
+  Grid2D* p = c->getPhiGrid();
+  Grid1D* zg = c->getLongGrid();
+  for (int i = 0; i < n; ++i) {
+    p->calcGradient(x[i], y[i], ex[i], ey[i]);
+    lam[i] = zg->getValue(z[i]);
+  }
+}
+
+// ---- teapot_base maps (src/teapot/teapotbase.cc) ----
+void ref_tpb_rotatexy(void* b, double a) { teapot_base::rotatexy((Bunch*)b, a); }
+void ref_tpb_drift(void* b, double L) { teapot_base::drift((Bunch*)b, L); }
+void ref_tpb_wrapbunch(void* b, double L) { teapot_base::wrapbunch((Bunch*)b, L); }
+void ref_tpb_kick(void* b, double kx, double ky, double kE) { teapot_base::kick((Bunch*)b, kx, ky, kE, 1); }
+void ref_tpb_multp(void* b, int pole, double kl, int skew) { teapot_base::multp((Bunch*)b, pole, kl, skew, 1); }
+void ref_tpb_multpfringeIN(void* b, int pole, double kl, int skew) { teapot_base::multpfringeIN((Bunch*)b, pole, kl, skew, 1); }
+void ref_tpb_multpfringeOUT(void* b, int pole, double kl, int skew) { teapot_base::multpfringeOUT((Bunch*)b, pole, kl, skew, 1); }
+void ref_tpb_quad1(void* b, double L, double kq) { teapot_base::quad1((Bunch*)b, L, kq, 1); }
+void ref_tpb_quad2(void* b, double L) { teapot_base::quad2((Bunch*)b, L); }
+void ref_tpb_quadfringeIN(void* b, double kq) { teapot_base::quadfringeIN((Bunch*)b, kq, 1); }
+void ref_tpb_quadfringeOUT(void* b, double kq) { teapot_base::quadfringeOUT((Bunch*)b, kq, 1); }
+void ref_tpb_wedgerotate(void* b, double e, int fr) { teapot_base::wedgerotate((Bunch*)b, e, fr); }
+void ref_tpb_wedgedrift(void* b, double e, int io) { teapot_base::wedgedrift((Bunch*)b, e, io); }
+void ref_tpb_wedgebend(void* b, double e, int io, double rho, int ns) { teapot_base::wedgebend((Bunch*)b, e, io, rho, ns); }
+void ref_tpb_bend1(void* b, double L, double th) { teapot_base::bend1((Bunch*)b, L, th); }
+void ref_tpb_bend2(void* b, double L) { teapot_base::bend2((Bunch*)b, L); }
+void ref_tpb_bend3(void* b, double th) { teapot_base::bend3((Bunch*)b, th); }
+void ref_tpb_bend4(void* b, double th) { teapot_base::bend4((Bunch*)b, th); }
+void ref_tpb_bendfringeIN(void* b, double rho) { teapot_base::bendfringeIN((Bunch*)b, rho); }
+void ref_tpb_bendfringeOUT(void* b, double rho) { teapot_base::bendfringeOUT((Bunch*)b, rho); }
+
+}  // extern "C"

@@ -1,0 +1,617 @@
+"""Module ``bunch``: the PyORBIT ``Bunch`` / ``SyncPart`` /
+``BunchTwissAnalysis`` interface (src/orbit/wrap_bunch.cc,
+src/orbit/wrap_syncpart.cc, src/orbit/BunchDiagnostics/) over a
+device-resident bunch.
+
+The coordinates live in HBM as six FP64 arrays once any GPU map or
+space-charge kick has touched the bunch; per-particle accessors such as
+``x(i)`` download them on demand, and host-side edits are uploaded before
+the next device operation.  Host-only use (building a bunch, reading it
+back) needs no GPU.
+"""
+from __future__ import annotations
+
+import math
+import os
+
+import numpy as np
+
+_COORDS = ("x", "xp", "y", "yp", "z", "dE")
+
+# OrbitConst.cc:34-36
+MASS_PROTON = 0.938272013
+CLASSICAL_RADIUS_PROTON = 1.534698e-18
+CHARGE_PROTON = 1.0
+
+
+class SyncPart:
+    """Synchronous (reference) particle: momentum vector, kinetic energy,
+    beta, gamma and time (src/orbit/SyncPart.cc)."""
+
+    def __init__(self, bunch: "Bunch"):
+        self._bunch = bunch
+        self._time = 0.0
+        self._xyz = [0.0, 0.0, 0.0]
+        self._pxyz = [0.0, 0.0, 0.0]
+        self._p_abs = 0.0
+        self._energy = 0.0
+        self._beta = 0.0
+        self._gamma = 1.0
+
+    # SyncPart::updateKinematics (SyncPart.cc:236-306), kinematics part
+    def _update(self):
+        p2 = self._pxyz[0] * self._pxyz[0] + self._pxyz[1] * self._pxyz[1] + self._pxyz[2] * self._pxyz[2]
+        self._p_abs = math.sqrt(p2)
+        m = self._bunch.mass()
+        m2 = m * m
+        w = math.sqrt(m2 + p2)
+        self._energy = p2 / (math.sqrt(m2 + p2) + m)
+        self._beta = self._p_abs / w
+        self._gamma = w / m
+        self._bunch._sync_changed()
+
+    def energyToMomentum(self, ek: float) -> float:  # SyncPart.cc:314-317
+        m = self._bunch.mass()
+        return math.sqrt(ek * (ek + 2.0 * m))
+
+    def momentumToEnergy(self, p: float) -> float:  # SyncPart.cc:308-312
+        m = self._bunch.mass()
+        return p * p / (math.sqrt(m * m + p * p) + m)
+
+    def kinEnergy(self, value=None) -> float:
+        """kinEnergy() -> GeV; kinEnergy(ek) sets pz (wrap_syncpart.cc:70-93)."""
+        if value is None:
+            return self._energy
+        p = self.energyToMomentum(float(value))
+        self._pxyz = [0.0, 0.0, p]
+        self._update()
+        return self.momentumToEnergy(p)
+
+    def momentum(self, value=None) -> float:
+        if value is None:
+            return self._p_abs
+        self._pxyz = [0.0, 0.0, float(value)]
+        self._update()
+        return self._p_abs
+
+    def beta(self) -> float:
+        return self._beta
+
+    def gamma(self) -> float:
+        return self._gamma
+
+    def mass(self) -> float:
+        return self._bunch.mass()
+
+    def time(self, value=None) -> float:
+        if value is not None:
+            self._bunch._sync_changed()
+            self._time = float(value)
+        else:
+            self._bunch._pull_time()
+        return self._time
+
+    def _coord(self, arr, i, value):
+        if value is not None:
+            arr[i] = float(value)
+            if arr is self._pxyz:
+                self._update()
+        return arr[i]
+
+    def x(self, v=None): return self._coord(self._xyz, 0, v)
+    def y(self, v=None): return self._coord(self._xyz, 1, v)
+    def z(self, v=None): return self._coord(self._xyz, 2, v)
+    def px(self, v=None): return self._coord(self._pxyz, 0, v)
+    def py(self, v=None): return self._coord(self._pxyz, 1, v)
+    def pz(self, v=None): return self._coord(self._pxyz, 2, v)
+
+    def pVector(self, v=None):
+        if v is not None:
+            self._pxyz = [float(a) for a in v]
+            self._update()
+        return tuple(self._pxyz)
+
+    def rVector(self, v=None):
+        if v is not None:
+            self._xyz = [float(a) for a in v]
+        return tuple(self._xyz)
+
+
+class Bunch:
+    """Macroparticle bunch with the reference's Python interface."""
+
+    def __init__(self):
+        self._n = 0
+        self._host = np.zeros((6, 16), dtype=np.float64)
+        self._flag = np.ones(16, dtype=np.int8)
+        self._host_ok = True     # host copy holds the current coordinates
+        self._dev_ok = False     # device copy holds the current coordinates
+        self._dev = None         # orbit_gb300.DeviceBunch, created on first device use
+        self._mass = MASS_PROTON
+        self._charge = CHARGE_PROTON
+        self._classical_radius = CLASSICAL_RADIUS_PROTON
+        self._macrosize = 0.0
+        self._attr_double = {"mass": self._mass, "charge": self._charge,
+                             "classical_radius": self._classical_radius, "macro_size": 0.0}
+        self._attr_int = {}
+        self._part_attr = {}     # name -> (n, k) array
+        self._part_attr_dict = {}
+        self._sync = SyncPart(self)
+        self._sync_dirty = True
+
+    # ------------------------------------------------------------ storage
+    def _ensure_host(self):
+        if not self._host_ok:
+            if self._host.shape[1] < self._n:
+                self._host = np.zeros((6, max(self._n, 16)), dtype=np.float64)
+            rows = [self._host[c, : self._n] for c in range(6)]
+            rows = [np.ascontiguousarray(r) for r in rows]
+            self._dev.download_rows(rows)
+            for c in range(6):
+                self._host[c, : self._n] = rows[c]
+            self._host_ok = True
+
+    def _grow(self, need):
+        cap = self._host.shape[1]
+        if need <= cap:
+            return
+        newcap = max(need, 2 * cap)
+        h = np.zeros((6, newcap), dtype=np.float64)
+        h[:, : self._n] = self._host[:, : self._n]
+        f = np.ones(newcap, dtype=np.int8)
+        f[: self._n] = self._flag[: self._n]
+        self._host, self._flag = h, f
+        for name, arr in list(self._part_attr.items()):
+            a = np.zeros((newcap, arr.shape[1]))
+            a[: self._n] = arr[: self._n]
+            self._part_attr[name] = a
+
+    def _device_bunch(self):
+        """Device copy with current coordinates and reference-particle data."""
+        from orbit_gb300 import DeviceBunch, Sync  # noqa: WPS433
+        if self._dev is None:
+            self._dev = DeviceBunch()
+            self._dev_ok = False
+            self._sync_dirty = True
+        if not self._dev_ok:
+            self.compress()
+            rows = [np.ascontiguousarray(self._host[c, : self._n]) for c in range(6)]
+            self._dev.upload_rows(rows, self._n)
+            self._upload_keepalive = rows
+            if "macrosize" in self._part_attr:
+                self._dev.set_macrosizes(self._part_attr["macrosize"][: self._n, 0])
+            else:
+                self._dev.set_macrosizes(None)
+            self._dev.sync()
+            self._dev_ok = True
+        if self._sync_dirty:
+            s = self._sync
+            self._dev.set_sync(Sync(s._beta, s._gamma, s._p_abs, self._mass, self._charge,
+                                    self._classical_radius, self._macrosize, s._time))
+            self._sync_dirty = False
+        return self._dev
+
+    def _device_modified(self):
+        """Called after a device operation changed coordinates."""
+        self._host_ok = False
+
+    def _sync_changed(self):
+        # keep the time the device maps advanced before the host copy wins
+        if self._dev is not None and not self._sync_dirty:
+            self._sync._time = self._dev.get_sync().time
+        self._sync_dirty = True
+
+    def _pull_time(self):
+        if self._dev is not None and not self._sync_dirty:
+            self._sync._time = self._dev.get_sync().time
+
+    def _host_modified(self):
+        self._dev_ok = False
+
+    # -------------------------------------------------------- particles
+    def addParticle(self, x, xp, y, yp, z, dE) -> int:
+        self._ensure_host()
+        self._grow(self._n + 1)
+        i = self._n
+        self._host[:, i] = (x, xp, y, yp, z, dE)
+        self._flag[i] = 1
+        for arr in self._part_attr.values():
+            arr[i] = 0.0
+        self._n += 1
+        self._host_modified()
+        return self._n
+
+    def deleteParticleFast(self, index: int):
+        self._ensure_host()
+        self._flag[index] = 0
+        self._host_modified()
+
+    def deleteParticle(self, index: int):
+        self.deleteParticleFast(index)
+        self.compress()
+
+    def deleteAllParticles(self):
+        self._n = 0
+        self._host_ok = True
+        self._host_modified()
+
+    def compress(self):
+        """Removes particles flagged dead (Bunch.cc:704-770)."""
+        if self._n == 0 or bool(np.all(self._flag[: self._n] == 1)):
+            return
+        self._ensure_host()
+        keep = np.nonzero(self._flag[: self._n] == 1)[0]
+        m = keep.shape[0]
+        self._host[:, :m] = self._host[:, keep]
+        for name, arr in self._part_attr.items():
+            arr[:m] = arr[keep]
+        self._flag[:] = 1
+        self._n = m
+        self._host_modified()
+
+    def flag(self, index: int) -> int:
+        return int(self._flag[index])
+
+    def _coord(self, c, index, value):
+        self._ensure_host()
+        if index < 0 or index >= self._n:
+            raise IndexError("particle index %d out of range [0, %d)" % (index, self._n))
+        if value is not None:
+            self._host[c, index] = float(value)
+            self._host_modified()
+        return float(self._host[c, index])
+
+    def x(self, i, v=None): return self._coord(0, i, v)
+    def xp(self, i, v=None): return self._coord(1, i, v)
+    def px(self, i, v=None): return self._coord(1, i, v)
+    def y(self, i, v=None): return self._coord(2, i, v)
+    def yp(self, i, v=None): return self._coord(3, i, v)
+    def py(self, i, v=None): return self._coord(3, i, v)
+    def z(self, i, v=None): return self._coord(4, i, v)
+    def dE(self, i, v=None): return self._coord(5, i, v)
+    def pz(self, i, v=None): return self._coord(5, i, v)
+
+    # numpy extensions
+    def getCoordinates(self, out=None) -> np.ndarray:
+        """(6, n) copy of x, xp, y, yp, z, dE (into ``out`` if given)."""
+        if out is not None and not self._host_ok and out.shape == (6, self._n) and out.dtype == np.float64 \
+                and out.flags.c_contiguous:
+            self._dev.download_rows([out[c] for c in range(6)])
+            return out
+        self._ensure_host()
+        if out is None:
+            return self._host[:, : self._n].copy()
+        out[...] = self._host[:, : self._n]
+        return out
+
+    def setCoordinates(self, soa, copy=True):
+        """Replaces all particles by the (6, n) array.  With copy=False a
+        C-contiguous float64 array (e.g. in pinned memory) becomes the host
+        storage itself, so uploads read it directly."""
+        soa = np.asarray(soa, dtype=np.float64)
+        if soa.ndim != 2 or soa.shape[0] != 6:
+            raise ValueError("expected a (6, n) array")
+        n = soa.shape[1]
+        if copy or not soa.flags.c_contiguous:
+            self._host = np.array(soa, dtype=np.float64, order="C", copy=True)
+        else:
+            self._host = soa
+        if n == 0:
+            self._host = np.zeros((6, 16))
+        self._flag = np.ones(max(n, 16), dtype=np.int8)
+        for name, arr in list(self._part_attr.items()):
+            self._part_attr[name] = np.zeros((max(n, 16), arr.shape[1]))
+        self._n = n
+        self._host_ok = True
+        self._host_modified()
+
+    def ringwrap(self, ring_length: float):
+        from orbit.teapot_base import TPB
+        TPB.wrapbunch(self, ring_length)
+
+    # --------------------------------------------------------- sizes
+    def getSize(self) -> int:
+        return self._n
+
+    def getSizeGlobal(self) -> int:
+        return self._n
+
+    def getSizeGlobalFromMemory(self) -> int:
+        return self._n
+
+    def getTotalCount(self) -> int:
+        return self._n
+
+    def getCapacity(self) -> int:
+        return self._host.shape[1]
+
+    # --------------------------------------------------- bunch params
+    def mass(self, value=None) -> float:
+        if value is not None:  # Bunch::setMass (Bunch.cc:789-794)
+            self._mass = float(value)
+            self._attr_double["mass"] = self._mass
+            self._update_classical_radius_attr()
+            self._sync._update()
+        return self._mass
+
+    def charge(self, value=None) -> float:
+        if value is not None:
+            self._charge = float(value)
+            self._attr_double["charge"] = self._charge
+            self._update_classical_radius_attr()
+            self._sync_changed()
+        return self._charge
+
+    def _update_classical_radius_attr(self):
+        # Bunch::updateClassicalRadius (Bunch.cc:804-812) updates the
+        # attribute only; the value the calculators read is unchanged.
+        v = CLASSICAL_RADIUS_PROTON * MASS_PROTON / self._mass * self._charge * self._charge
+        self._attr_double["classical_radius"] = v
+
+    def classicalRadius(self) -> float:
+        return self._classical_radius
+
+    def macroSize(self, value=None) -> float:
+        if value is not None:
+            self._macrosize = float(value)
+            self._attr_double["macro_size"] = self._macrosize
+            self._sync_changed()
+        return self._macrosize
+
+    def B_Rho(self) -> float:  # Bunch.cc:781-787
+        if self._charge != 0.0:
+            return 3.335640952 * self._sync.momentum() / self._charge
+        return 1.0e36
+
+    def getSyncParticle(self) -> SyncPart:
+        return self._sync
+
+    # ---------------------------------------------- bunch attributes
+    def bunchAttrDouble(self, name, value=None):
+        if value is not None:
+            self._attr_double[name] = float(value)
+            if name == "mass":
+                self._mass = float(value)
+            elif name == "charge":
+                self._charge = float(value)
+            elif name == "classical_radius":
+                self._classical_radius = float(value)
+            elif name == "macro_size":
+                self._macrosize = float(value)
+            self._sync_changed()
+        return self._attr_double[name]
+
+    def bunchAttrInt(self, name, value=None):
+        if value is not None:
+            self._attr_int[name] = int(value)
+        return self._attr_int[name]
+
+    def bunchAttrDoubleNames(self):
+        return tuple(self._attr_double.keys())
+
+    def bunchAttrIntNames(self):
+        return tuple(self._attr_int.keys())
+
+    def hasBunchAttrDouble(self, name) -> int:
+        return 1 if name in self._attr_double else 0
+
+    def hasBunchAttrInt(self, name) -> int:
+        return 1 if name in self._attr_int else 0
+
+    # --------------------------------------- particle attributes
+    _PART_ATTR_SIZES = {"macrosize": 1, "ParticleIdNumber": 1, "TurnNumber": 1}
+
+    def addPartAttr(self, name, params=None):
+        if name in self._part_attr:
+            return
+        k = self._PART_ATTR_SIZES.get(name, 1)
+        if params and "size" in params:
+            k = int(params["size"])
+        self._part_attr[name] = np.zeros((self._host.shape[1], k))
+        self._part_attr_dict[name] = dict(params or {})
+        if name == "macrosize":
+            self._host_modified()
+
+    def removePartAttr(self, name):
+        self._part_attr.pop(name, None)
+        self._part_attr_dict.pop(name, None)
+        if name == "macrosize":
+            self._host_modified()
+
+    def removeAllPartAttr(self):
+        for name in list(self._part_attr):
+            self.removePartAttr(name)
+
+    def hasPartAttr(self, name) -> int:
+        return 1 if name in self._part_attr else 0
+
+    def getPartAttrNames(self):
+        return tuple(self._part_attr.keys())
+
+    def getPartAttrSize(self, name) -> int:
+        return self._part_attr[name].shape[1]
+
+    def partAttrValue(self, name, index, attr_index, value=None):
+        arr = self._part_attr[name]
+        if value is not None:
+            arr[index, attr_index] = float(value)
+            if name == "macrosize":
+                self._host_modified()
+        return float(arr[index, attr_index])
+
+    # ----------------------------------------------------- copies
+    def copyEmptyBunchTo(self, other: "Bunch"):
+        other._mass, other._charge = self._mass, self._charge
+        other._classical_radius, other._macrosize = self._classical_radius, self._macrosize
+        other._attr_double = dict(self._attr_double)
+        other._attr_int = dict(self._attr_int)
+        other._sync._pxyz = list(self._sync._pxyz)
+        other._sync._xyz = list(self._sync._xyz)
+        other._sync._time = self._sync.time()
+        other._sync._update()
+        for name in self._part_attr:
+            other.addPartAttr(name, self._part_attr_dict.get(name))
+
+    def copyBunchTo(self, other: "Bunch"):
+        self.copyEmptyBunchTo(other)
+        other.deleteAllParticles()
+        self.addParticlesTo(other)
+
+    def addParticlesTo(self, other: "Bunch"):
+        self._ensure_host()
+        other._ensure_host()
+        m = self._n
+        base = other._n
+        other._grow(base + m)
+        other._host[:, base:base + m] = self._host[:, :m]
+        other._flag[base:base + m] = self._flag[:m]
+        for name, arr in self._part_attr.items():
+            if name in other._part_attr:
+                other._part_attr[name][base:base + m] = arr[:m]
+        other._n = base + m
+        other._host_modified()
+
+    # ----------------------------------------------------- I/O
+    def dumpBunch(self, fileName=None):
+        """Text dump in the layout of Bunch::print (Bunch.cc:894-980)."""
+        self._ensure_host()
+        lines = ["% PARTICLE_ATTRIBUTES_CONTROLLERS_NAMES " + " ".join(self._part_attr.keys()) + " "]
+        for name, v in self._attr_int.items():
+            lines.append("%% BUNCH_ATTRIBUTE_INT %s   %d " % (name, v))
+        for name, v in self._attr_double.items():
+            lines.append("%% BUNCH_ATTRIBUTE_DOUBLE %s   %.8g " % (name, v))
+        s = self._sync
+        lines.append("% SYNC_PART_COORDS " + " ".join("%.8g" % v for v in s._xyz) + "  x, y, z positions in [m]")
+        lines.append("% SYNC_PART_MOMENTUM " + " ".join("%.8g" % v for v in s._pxyz) + "  px, py, pz momentum component in GeV/c")
+        lines.append("% SYNC_PART_X_AXIS 1 0 0  nxx, nxy, nxz - x-axis ort coordinates")
+        lines.append("% info only: energy of the synchronous particle [GeV] = %.8g" % s.kinEnergy())
+        lines.append("% info only: momentum of the synchronous particle [GeV/c] = %.8g" % s.momentum())
+        lines.append("% info only: beta of the synchronous particle = %.8g" % s.beta())
+        lines.append("% info only: gamma of the synchronous particle = %.8g" % s.gamma())
+        lines.append("% SYNC_PART_TIME %.8g  time in [sec]" % s.time())
+        lines.append("% x[m] px[rad] y[m] py[rad] z[m]  (pz or dE [GeV]) ")
+        body = []
+        attrs = [self._part_attr[k] for k in self._part_attr]
+        for i in range(self._n):
+            if self._flag[i] > 0:
+                vals = ["%.8g" % v for v in self._host[:, i]]
+                for a in attrs:
+                    vals += ["%.8g" % v for v in a[i]]
+                body.append(" ".join(vals) + " ")
+        text = "\n".join(lines + body) + "\n"
+        if fileName is None:
+            print(text, end="")
+        else:
+            with open(fileName, "w") as f:
+                f.write(text)
+
+    def readBunch(self, fileName, nParts=-1):
+        """Reads a file written by dumpBunch (Bunch.cc:1116-1300)."""
+        rows = []
+        attr_names = []
+        with open(fileName) as f:
+            for line in f:
+                line = line.strip()
+                if not line:
+                    continue
+                if line.startswith("%"):
+                    tok = line.split()
+                    if len(tok) >= 2 and tok[1] == "PARTICLE_ATTRIBUTES_CONTROLLERS_NAMES":
+                        attr_names = tok[2:]
+                    elif len(tok) >= 4 and tok[1] == "BUNCH_ATTRIBUTE_DOUBLE":
+                        self.bunchAttrDouble(tok[2], float(tok[3]))
+                    elif len(tok) >= 4 and tok[1] == "BUNCH_ATTRIBUTE_INT":
+                        self.bunchAttrInt(tok[2], int(tok[3]))
+                    elif len(tok) >= 5 and tok[1] == "SYNC_PART_MOMENTUM":
+                        self._sync.pVector([float(t) for t in tok[2:5]])
+                    elif len(tok) >= 5 and tok[1] == "SYNC_PART_COORDS":
+                        self._sync.rVector([float(t) for t in tok[2:5]])
+                    elif len(tok) >= 3 and tok[1] == "SYNC_PART_TIME":
+                        self._sync.time(float(tok[2]))
+                    continue
+                rows.append([float(t) for t in line.split()])
+                if 0 < nParts <= len(rows):
+                    break
+        for name in attr_names:
+            self.addPartAttr(name)
+        arr = np.array(rows, dtype=np.float64).reshape(-1, max(6, len(rows[0]) if rows else 6))
+        self.setCoordinates(arr[:, :6].T)
+        col = 6
+        for name in attr_names:
+            k = self._part_attr[name].shape[1]
+            self._part_attr[name][: self._n] = arr[:, col:col + k]
+            col += k
+        return self._n
+
+
+class BunchTwissAnalysis:
+    """Second moments, rms emittances and Twiss parameters
+    (src/orbit/BunchDiagnostics/BunchTwissAnalysis.cc:49-140, 344-420)."""
+
+    def __init__(self):
+        self._avg = np.zeros(6)
+        self._corr = np.zeros((6, 6))
+        self._count = 0
+        self._total_m = 0.0
+        self._beta = 0.0
+        self._gamma = 1.0
+
+    def analyzeBunch(self, bunch: Bunch):
+        bunch.compress()
+        c = bunch.getCoordinates()
+        n = c.shape[1]
+        self._count = n
+        if "macrosize" in bunch._part_attr:
+            m = bunch._part_attr["macrosize"][:n, 0]
+        else:
+            m = np.ones(n)
+        self._total_m = float(m.sum())
+        if self._total_m != 0.0:
+            self._avg = (c * m).sum(axis=1) / self._total_m
+            self._corr = (c * m) @ c.T / self._total_m
+        s = bunch.getSyncParticle()
+        self._beta, self._gamma = s.beta(), s.gamma()
+
+    def getCorrelation(self, i, j):
+        return float(self._corr[i, j] - self._avg[i] * self._avg[j])
+
+    def getAverage(self, i):
+        return float(self._avg[i])
+
+    def getGlobalCount(self):
+        return self._count
+
+    def getGlobalMacrosize(self):
+        return self._total_m
+
+    def getEmittance(self, ic):
+        if ic < 0 or ic > 2:
+            return 0.0
+        C = self.getCorrelation
+        x2, xp2 = abs(C(2 * ic, 2 * ic)), abs(C(2 * ic + 1, 2 * ic + 1))
+        xxp, xdE, xpdE = C(2 * ic, 2 * ic + 1), C(2 * ic, 5), C(2 * ic + 1, 5)
+        dE2 = abs(C(5, 5))
+        if ic == 2 or dE2 == 0:
+            return math.sqrt(abs(x2 * xp2 - xxp * xxp))
+        return math.sqrt(abs((x2 - xdE * xdE / dE2) * (xp2 - xpdE * xpdE / dE2)
+                             - (xxp - xdE * xpdE / dE2) ** 2))
+
+    def getEmittanceNormalized(self, ic):
+        if ic == 2:
+            return self.getEmittance(ic)
+        return self.getEmittance(ic) * self._gamma * self._beta
+
+    def getBeta(self, ic):
+        e = self.getEmittance(ic)
+        return abs(self.getCorrelation(2 * ic, 2 * ic)) / e if e else 0.0
+
+    def getAlpha(self, ic):
+        e = self.getEmittance(ic)
+        return -self.getCorrelation(2 * ic, 2 * ic + 1) / e if e else 0.0
+
+    def getGamma(self, ic):
+        e = self.getEmittance(ic)
+        return abs(self.getCorrelation(2 * ic + 1, 2 * ic + 1)) / e if e else 0.0
+
+
+__all__ = ["Bunch", "SyncPart", "BunchTwissAnalysis"]

@@ -1,0 +1,102 @@
+// Block-cooperative mixed-radix Stockham FFT in shared memory.
+//
+// Used for the Hockney open-boundary convolution of the 2D Poisson solve
+// (the role FFTW plays in src/spacecharge/PoissonSolverFFT2D.cc:57-59, 162,
+// 228, 245).  One thread block transforms one length-N sequence held in
+// shared memory; stage s with radix p maps
+//   b[k*L*p + j + r*L] = sum_q (a[k*L + j + q*N/p] * W_{Lp}^{j q}) W_p^{q r}
+// (L = product of the radices before s), so the result is in natural order
+// after the last stage.  Twiddles come from a table W_N^e = exp(-2 pi i e/N)
+// computed on the host; supported radices are 2, 3, 4, 5 and any prime up
+// to 13.
+#pragma once
+
+#include "common.cuh"
+#include "sc2p5d.cuh"
+
+namespace orbit {
+
+template <typename T> struct CT;
+template <> struct CT<double> { typedef double2 t; };
+template <> struct CT<float> { typedef float2 t; };
+
+template <typename C>
+__device__ __forceinline__ C c_mul(C a, C b) {
+  C r;
+  r.x = a.x * b.x - a.y * b.y;
+  r.y = a.x * b.y + a.y * b.x;
+  return r;
+}
+template <typename C>
+__device__ __forceinline__ C c_add(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <typename C>
+__device__ __forceinline__ C c_sub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+template <typename C>
+__device__ __forceinline__ C c_conj(C a) { a.y = -a.y; return a; }
+
+// a: input buffer, b: scratch; returns the buffer holding the result.
+// `inv` selects the backward (+i) transform; unnormalised.
+template <typename T>
+__device__ typename CT<T>::t* block_fft(typename CT<T>::t* a, typename CT<T>::t* b, const FftPlan& pl,
+                                        const typename CT<T>::t* __restrict__ tw, bool inv) {
+  typedef typename CT<T>::t C;
+  const int N = pl.n;
+  int L = 1;
+  for (int s = 0; s < pl.nst; ++s) {
+    const int p = pl.rad[s];
+    const int Np = N / p;
+    const int Lp = L * p;
+    const int tws = N / Lp;
+    for (int t = threadIdx.x; t < Np; t += blockDim.x) {
+      const int j = t % L;
+      const int k = t / L;
+      C x[13];
+#pragma unroll 4
+      for (int q = 0; q < p; ++q) x[q] = a[k * L + j + q * Np];
+      if (j != 0) {
+        for (int q = 1; q < p; ++q) {
+          C w = tw[j * q * tws];
+          if (inv) w.y = -w.y;
+          x[q] = c_mul(x[q], w);
+        }
+      }
+      C* out = b + k * Lp + j;
+      if (p == 2) {
+        out[0] = c_add(x[0], x[1]);
+        out[L] = c_sub(x[0], x[1]);
+      } else if (p == 4) {
+        C a0 = c_add(x[0], x[2]), a1 = c_sub(x[0], x[2]);
+        C b0 = c_add(x[1], x[3]), b1 = c_sub(x[1], x[3]);
+        C c;  // (-i or +i) * b1
+        if (inv) { c.x = -b1.y; c.y = b1.x; } else { c.x = b1.y; c.y = -b1.x; }
+        out[0] = c_add(a0, b0);
+        out[L] = c_add(a1, c);
+        out[2 * L] = c_sub(a0, b0);
+        out[3 * L] = c_sub(a1, c);
+      } else {
+        const int twp = N / p;  // W_p^e = tw[e * twp]
+        for (int r = 0; r < p; ++r) {
+          C acc = x[0];
+          for (int q = 1; q < p; ++q) {
+            C w = tw[((q * r) % p) * twp];
+            if (inv) w.y = -w.y;
+            C m = c_mul(x[q], w);
+            acc = c_add(acc, m);
+          }
+          out[r * L] = acc;
+        }
+      }
+    }
+    __syncthreads();
+    C* tmp = a;
+    a = b;
+    b = tmp;
+    L = Lp;
+  }
+  return a;
+}
+
+// Host: factor N into supported radices (4s first, then 2, 3, 5, 7, 11, 13).
+bool make_fft_plan(int n, FftPlan& pl);
+
+}  // namespace orbit

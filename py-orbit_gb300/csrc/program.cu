@@ -1,0 +1,419 @@
+// Lattice programs: a recorded node sequence (the order AccNode.trackActions
+// produces, py/orbit/lattice/AccNode.py:302-350) compiled into fused device
+// passes and replayed from a CUDA graph.
+//
+// A turn with SC kicks S_0..S_{m-1} between map segments M_0..M_m runs as
+//   [P_0]  solve(S_0) P_1 solve(S_1) ... solve(S_{m-1}) P_m
+// where P_0 = M_0 + extrema(S_0), P_i = kick(S_{i-1}) + M_i + extrema(S_i) and
+// the last pass of a turn that is followed by another turn also applies M_0
+// of the next turn and the extrema scan for its first kick.  Every pass reads
+// and writes the six coordinates once; the deposit reads x, y, z once more.
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+#include "sc2p5d.cuh"
+#include "sc_device.cuh"
+#include "teapot.cuh"
+
+namespace orbit {
+
+int check_status(orbit_bunch_t* b);
+
+static const int kPassSmem = 220 * 1024;
+
+// KF: 0 no kick, 1 plain kick, 2 fp32 kick.  EXT: accumulate extrema.
+template <int KF, bool EXT, bool KSMEM>
+__global__ void __launch_bounds__(512) k_pass(double* __restrict__ cx, double* __restrict__ cxp,
+                                              double* __restrict__ cy, double* __restrict__ cyp,
+                                              double* __restrict__ cz, double* __restrict__ cdE, int n,
+                                              const DevOp* __restrict__ ops, int a, int b, MapCtx m,
+                                              KickArgs kick, ScState* ext_st, unsigned* status) {
+  KickConst k;
+  const double* P = kick.phi;
+  const double* Lm = kick.lam;
+  const float* Pf = kick.phi_f;
+  const float* Lf = kick.lam_f;
+  extern __shared__ unsigned char s_raw[];
+  if (KF != 0) {
+    load_kick_const(k, kick.st, kick.host_factor, kick.nx, kick.ny, kick.nz);
+    if (KSMEM) {
+      int ng = kick.nx * kick.ny;
+      if (KF == 1) {
+        double* s = reinterpret_cast<double*>(s_raw);
+        for (int i = threadIdx.x; i < ng; i += blockDim.x) s[i] = kick.phi[i];
+        for (int i = threadIdx.x; i < kick.nz; i += blockDim.x) s[ng + i] = kick.lam[i];
+        P = s;
+        Lm = s + ng;
+      } else {
+        float* s = reinterpret_cast<float*>(s_raw);
+        for (int i = threadIdx.x; i < ng; i += blockDim.x) s[i] = kick.phi_f[i];
+        for (int i = threadIdx.x; i < kick.nz; i += blockDim.x) s[ng + i] = kick.lam_f[i];
+        Pf = s;
+        Lf = s + ng;
+      }
+      __syncthreads();
+    }
+  }
+  ExtAcc acc;
+  if (EXT) acc.init();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    Part p;
+    p.x = cx[i]; p.xp = cxp[i]; p.y = cy[i]; p.yp = cyp[i]; p.z = cz[i]; p.dE = cdE[i];
+    p.knl_ok = false;
+    if (KF == 1 && !k.skip) kick_plain(k, P, Lm, p.x, p.y, p.z, p.xp, p.yp);
+    if (KF == 2 && !k.skip) kick_fp32(k, Pf, Lf, p.x, p.y, p.z, p.xp, p.yp);
+    apply_ops(p, ops, a, b, m);
+    if (EXT) acc.add(p.x, p.y, p.z);
+    cx[i] = p.x; cxp[i] = p.xp; cy[i] = p.y; cyp[i] = p.yp; cz[i] = p.z; cdE[i] = p.dE;
+  }
+  if (EXT) ext_block_commit(acc, ext_st, status);
+}
+
+// Shared-memory limits are raised once, outside any stream capture.
+static int init_pass_attrs() {
+  static bool done = false;
+  if (done) return ORBIT_OK;
+  ORBIT_CUDA(cudaFuncSetAttribute(k_pass<1, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kPassSmem));
+  ORBIT_CUDA(cudaFuncSetAttribute(k_pass<1, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kPassSmem));
+  ORBIT_CUDA(cudaFuncSetAttribute(k_pass<2, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kPassSmem));
+  ORBIT_CUDA(cudaFuncSetAttribute(k_pass<2, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kPassSmem));
+  done = true;
+  return ORBIT_OK;
+}
+
+template <int KF, bool EXT, bool KSMEM>
+static int launch_pass(orbit_bunch_t* bu, cudaStream_t s, size_t smem, const DevOp* ops, int a, int b,
+                       const MapCtx& m, const KickArgs& ka, ScState* ext) {
+  int threads = 512;
+  int bps = KSMEM ? (int)(kPassSmem / (smem > 0 ? smem : 1)) : 4;
+  if (bps < 1) bps = 1;
+  if (bps > 4) bps = 4;
+  int blocks = num_sms() * bps;
+  int need = (bu->n + threads - 1) / threads;
+  if (need < blocks) blocks = need < 1 ? 1 : need;
+  ORBIT_PB(KF == 0 ? "pass_maps" : "pass_kick_maps", s);
+  k_pass<KF, EXT, KSMEM><<<blocks, threads, KSMEM ? smem : 0, s>>>(
+      bu->coord(0), bu->coord(1), bu->coord(2), bu->coord(3), bu->coord(4), bu->coord(5), bu->n, ops, a, b, m, ka,
+      ext, bu->d_status);
+  ORBIT_PE(s);
+  ORBIT_LAUNCH_CHECK("k_pass");
+  return ORBIT_OK;
+}
+
+}  // namespace orbit
+
+using namespace orbit;
+
+struct orbit_program {
+  std::vector<orbit_op_t> ops;
+  std::vector<orbit_sc2p5d_t*> calcs;
+  // compiled for one bunch configuration
+  orbit_bunch_t* key_bunch = nullptr;
+  int key_n = -1;
+  double* key_coords = nullptr;
+  orbit_sync_t key_sync{};
+  int key_msize = -1;
+  DevOp* d_ops = nullptr;
+  int n_devops = 0;
+  cudaGraphExec_t g_first = nullptr;  // prologue + turn ending with the wrap pass
+  cudaGraphExec_t g_mid = nullptr;    // turn ending with the wrap pass
+  cudaGraphExec_t g_last = nullptr;   // turn ending without the wrap
+  cudaGraphExec_t g_single = nullptr; // prologue + turn without wrap (one-turn runs)
+  std::vector<double> time_adv;       // per-op SyncPart time increments
+  int launches_per_turn = 0;
+};
+
+namespace orbit {
+
+struct Seg { int a, b; };
+
+struct Plan {
+  std::vector<Seg> segs;      // m+1 map segments in the device op array
+  std::vector<int> sc_idx;    // op index of each SC op
+  Seg wrap;                   // M_m ++ M_0 in the device op array
+};
+
+static void free_graphs(orbit_program_t* p) {
+  cudaGraphExec_t* gs[] = {&p->g_first, &p->g_mid, &p->g_last, &p->g_single};
+  for (auto g : gs)
+    if (*g) { cudaGraphExecDestroy(*g); *g = nullptr; }
+}
+
+static bool sync_equal(const orbit_sync_t& a, const orbit_sync_t& b) {
+  return a.beta == b.beta && a.gamma == b.gamma && a.momentum == b.momentum && a.charge == b.charge &&
+         a.classical_radius == b.classical_radius && a.macrosize == b.macrosize && a.mass == b.mass;
+}
+
+static KickArgs kick_args(orbit_sc2p5d_t* c, const orbit_sync_t& s, double length) {
+  KickArgs ka;
+  ka.st = c->d_st;
+  ka.phi = c->d_phi;
+  ka.lam = c->d_lam;
+  ka.phi_f = c->d_phi_f;
+  ka.lam_f = c->d_lam_f;
+  ka.host_factor = sc_host_factor(s, length);
+  ka.nx = c->nx; ka.ny = c->ny; ka.nz = c->nz; ka.form = c->form;
+  return ka;
+}
+
+// One fused pass: optional kick of calculator kc, maps [a,b), optional
+// extrema for calculator ec.
+static int enqueue_pass(orbit_bunch_t* bu, cudaStream_t s, const DevOp* ops, Seg seg, const MapCtx& m,
+                        orbit_sc2p5d_t* kc, double klen, orbit_sc2p5d_t* ec, int* nl) {
+  KickArgs ka;
+  std::memset(&ka, 0, sizeof(ka));
+  int kf = 0;
+  size_t smem = 0;
+  bool ksm = false;
+  if (kc) {
+    ka = kick_args(kc, bu->sync, klen);
+    kf = kc->form == ORBIT_FORM_PLAIN ? 1 : 2;
+    smem = (kf == 1 ? 8 : 4) * ((size_t)kc->nx * kc->ny + kc->nz);
+    ksm = smem <= (size_t)kPassSmem;
+  }
+  if (!kc && !ec && seg.a == seg.b) return ORBIT_OK;  // nothing to do
+  ScState* ext = ec ? ec->d_st : nullptr;
+  bool e = ext != nullptr;
+  int rc;
+  if (kf == 0) rc = e ? launch_pass<0, true, false>(bu, s, 0, ops, seg.a, seg.b, m, ka, ext)
+                      : launch_pass<0, false, false>(bu, s, 0, ops, seg.a, seg.b, m, ka, ext);
+  else if (kf == 1) {
+    if (ksm) rc = e ? launch_pass<1, true, true>(bu, s, smem, ops, seg.a, seg.b, m, ka, ext)
+                    : launch_pass<1, false, true>(bu, s, smem, ops, seg.a, seg.b, m, ka, ext);
+    else rc = e ? launch_pass<1, true, false>(bu, s, 0, ops, seg.a, seg.b, m, ka, ext)
+                : launch_pass<1, false, false>(bu, s, 0, ops, seg.a, seg.b, m, ka, ext);
+  } else {
+    if (ksm) rc = e ? launch_pass<2, true, true>(bu, s, smem, ops, seg.a, seg.b, m, ka, ext)
+                    : launch_pass<2, false, true>(bu, s, smem, ops, seg.a, seg.b, m, ka, ext);
+    else rc = e ? launch_pass<2, true, false>(bu, s, 0, ops, seg.a, seg.b, m, ka, ext)
+                : launch_pass<2, false, false>(bu, s, 0, ops, seg.a, seg.b, m, ka, ext);
+  }
+  if (rc == ORBIT_OK) ++*nl;
+  return rc;
+}
+
+// Builds the device op array: all non-SC ops of the turn in order, then the
+// wrap segment (last segment followed by the first).
+static int compile(orbit_program_t* p, orbit_bunch_t* bu, Plan& plan) {
+  std::vector<DevOp> dev;
+  p->time_adv.assign(p->ops.size(), 0.0);
+  int start = 0;
+  std::vector<std::pair<int, int>> seg_ops;  // [first op, last op) in p->ops for each segment
+  for (size_t k = 0; k < p->ops.size(); ++k) {
+    if (p->ops[k].code == ORBIT_OP_SC) {
+      seg_ops.push_back({start, (int)k});
+      plan.sc_idx.push_back((int)k);
+      start = (int)k + 1;
+    }
+  }
+  seg_ops.push_back({start, (int)p->ops.size()});
+  auto emit = [&](int a, int b) -> Seg {
+    Seg s;
+    s.a = (int)dev.size();
+    for (int k = a; k < b; ++k) {
+      DevOp d;
+      double adv = 0.0;
+      if (!compile_op(p->ops[k], bu->sync, d, &adv)) return Seg{-1, -1};
+      p->time_adv[k] = adv;
+      if (d.code != 0) dev.push_back(d);
+    }
+    s.b = (int)dev.size();
+    return s;
+  };
+  for (auto& so : seg_ops) {
+    Seg s = emit(so.first, so.second);
+    if (s.a < 0) return set_error(ORBIT_ERR_ARG, "orbit_program: bad op parameters");
+    plan.segs.push_back(s);
+  }
+  Seg w;
+  w.a = (int)dev.size();
+  {
+    Seg s1 = emit(seg_ops.back().first, seg_ops.back().second);
+    Seg s2 = emit(seg_ops.front().first, seg_ops.front().second);
+    if (s1.a < 0 || s2.a < 0) return set_error(ORBIT_ERR_ARG, "orbit_program: bad op parameters");
+  }
+  w.b = (int)dev.size();
+  plan.wrap = w;
+  if (p->d_ops) { cudaFree(p->d_ops); p->d_ops = nullptr; }
+  p->n_devops = (int)dev.size();
+  if (!dev.empty()) {
+    ORBIT_CUDA(cudaMalloc(&p->d_ops, sizeof(DevOp) * dev.size()));
+    ORBIT_CUDA(cudaMemcpy(p->d_ops, dev.data(), sizeof(DevOp) * dev.size(), cudaMemcpyHostToDevice));
+  }
+  return ORBIT_OK;
+}
+
+// Enqueues one turn.  prologue: run P_0 first.  wrap: end with the pass
+// that also applies M_0 of the next turn and its extrema scan.
+static int enqueue_turn(orbit_program_t* p, orbit_bunch_t* bu, cudaStream_t s, const Plan& plan, bool prologue,
+                        bool wrap, int* nl) {
+  const DevOp* ops = p->d_ops;
+  MapCtx m = make_ctx(bu->sync);
+  int nsc = (int)plan.sc_idx.size();
+  bool sc_active = bu->n >= 2;  // SpaceChargeCalc2p5D.cc:79-80
+  auto calc_of = [&](int i) -> orbit_sc2p5d_t* { return p->calcs[p->ops[plan.sc_idx[i]].i0]; };
+  auto len_of = [&](int i) -> double { return p->ops[plan.sc_idx[i]].d[0]; };
+  int rc;
+  if (nsc == 0 || !sc_active) {
+    // no kicks: one pass over all maps of the turn
+    for (size_t i = 0; i < plan.segs.size(); ++i) {
+      rc = enqueue_pass(bu, s, ops, plan.segs[i], m, nullptr, 0.0, nullptr, nl);
+      if (rc) return rc;
+    }
+    return ORBIT_OK;
+  }
+  if (prologue) {
+    rc = enqueue_pass(bu, s, ops, plan.segs[0], m, nullptr, 0.0, calc_of(0), nl);
+    if (rc) return rc;
+  }
+  for (int i = 0; i < nsc; ++i) {
+    rc = sc_enqueue_kick(calc_of(i), bu, len_of(i), s, false, false, nl);
+    if (rc) return rc;
+    bool last = (i == nsc - 1);
+    if (!last) {
+      rc = enqueue_pass(bu, s, ops, plan.segs[i + 1], m, calc_of(i), len_of(i), calc_of(i + 1), nl);
+    } else if (wrap) {
+      rc = enqueue_pass(bu, s, ops, plan.wrap, m, calc_of(i), len_of(i), calc_of(0), nl);
+    } else {
+      rc = enqueue_pass(bu, s, ops, plan.segs[nsc], m, calc_of(i), len_of(i), nullptr, nl);
+    }
+    if (rc) return rc;
+  }
+  return ORBIT_OK;
+}
+
+static int capture(orbit_program_t* p, orbit_bunch_t* bu, const Plan& plan, bool prologue, bool wrap,
+                   cudaGraphExec_t* out, int* nl) {
+  cudaStream_t s = bu->stream;
+  ORBIT_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  int rc = enqueue_turn(p, bu, s, plan, prologue, wrap, nl);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(s, &g);
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return cuda_error(e, "cudaStreamEndCapture");
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_error(e, "cudaGraphInstantiate");
+  return ORBIT_OK;
+}
+
+static int prepare(orbit_program_t* p, orbit_bunch_t* bu) {
+  bool same = p->key_bunch == bu && p->key_n == bu->n && p->key_coords == bu->d_coords &&
+              p->key_msize == bu->has_msize && sync_equal(p->key_sync, bu->sync) && p->g_mid;
+  if (same) return ORBIT_OK;
+  free_graphs(p);
+  Plan plan;
+  int rc = compile(p, bu, plan);
+  if (rc) return rc;
+  int nl = 0;
+  rc = capture(p, bu, plan, true, true, &p->g_first, &nl);
+  if (!rc) { nl = 0; rc = capture(p, bu, plan, false, true, &p->g_mid, &nl); }
+  if (!rc) { p->launches_per_turn = nl; nl = 0; rc = capture(p, bu, plan, false, false, &p->g_last, &nl); }
+  if (!rc) { nl = 0; rc = capture(p, bu, plan, true, false, &p->g_single, &nl); }
+  if (rc) { free_graphs(p); return rc; }
+  p->key_bunch = bu;
+  p->key_n = bu->n;
+  p->key_coords = bu->d_coords;
+  p->key_sync = bu->sync;
+  p->key_msize = bu->has_msize;
+  return ORBIT_OK;
+}
+
+}  // namespace orbit
+
+extern "C" {
+
+int orbit_program_create(orbit_program_t** out, const orbit_op_t* ops, int nops, orbit_sc2p5d_t* const* calcs,
+                         int ncalcs) {
+  if (!out || nops < 0 || (nops > 0 && !ops) || ncalcs < 0 || (ncalcs > 0 && !calcs))
+    return set_error(ORBIT_ERR_ARG, "orbit_program_create: bad argument");
+  int arc = init_pass_attrs();
+  if (arc) return arc;
+  num_sms();
+  orbit_program_t* p = new orbit_program_t();
+  p->ops.assign(ops, ops + nops);
+  p->calcs.assign(calcs, calcs + ncalcs);
+  for (auto& o : p->ops) {
+    if (o.code == ORBIT_OP_SC && (o.i0 < 0 || o.i0 >= ncalcs || !p->calcs[o.i0])) {
+      delete p;
+      return set_error(ORBIT_ERR_ARG, "orbit_program_create: SC op refers to a missing calculator");
+    }
+  }
+  *out = p;
+  return ORBIT_OK;
+}
+
+int orbit_program_destroy(orbit_program_t* p) {
+  if (!p) return ORBIT_OK;
+  if (p->key_bunch && p->key_bunch->stream) cudaStreamSynchronize(p->key_bunch->stream);
+  free_graphs(p);
+  if (p->d_ops) cudaFree(p->d_ops);
+  delete p;
+  return ORBIT_OK;
+}
+
+int orbit_program_run(orbit_program_t* p, orbit_bunch_t* b, int turns) {
+  int rc = orbit_program_enqueue(p, b, turns);
+  if (rc) return rc;
+  return check_status(b);
+}
+
+int orbit_program_enqueue(orbit_program_t* p, orbit_bunch_t* b, int turns) {
+  if (!p || !b || turns < 0) return set_error(ORBIT_ERR_ARG, "orbit_program_enqueue: bad argument");
+  if (turns == 0) return ORBIT_OK;
+  // calculators last used on another stream must be idle first
+  for (auto c : p->calcs)
+    if (c->last_stream && c->last_stream != b->stream) ORBIT_CUDA(cudaStreamSynchronize(c->last_stream));
+  int rc = prepare(p, b);
+  if (rc) return rc;
+  if (turns == 1) {
+    ORBIT_CUDA(cudaGraphLaunch(p->g_single, b->stream));
+  } else {
+    ORBIT_CUDA(cudaGraphLaunch(p->g_first, b->stream));
+    for (int t = 1; t < turns - 1; ++t) ORBIT_CUDA(cudaGraphLaunch(p->g_mid, b->stream));
+    ORBIT_CUDA(cudaGraphLaunch(p->g_last, b->stream));
+  }
+  for (auto c : p->calcs) c->last_stream = b->stream;
+  // SyncPart time, advanced in op order as each map would (teapotbase.cc:165)
+  for (int t = 0; t < turns; ++t)
+    for (double a : p->time_adv)
+      if (a != 0.0) b->sync.time = b->sync.time + a;
+  return ORBIT_OK;
+}
+
+int orbit_program_profile(orbit_program_t* p, orbit_bunch_t* b, int max_kinds, char* names, double* total_ms,
+                          int* launches, int* nkinds) {
+  if (!p || !b || max_kinds <= 0 || !names || !total_ms || !launches || !nkinds)
+    return set_error(ORBIT_ERR_ARG, "orbit_program_profile: bad argument");
+  for (auto c : p->calcs)
+    if (c->last_stream && c->last_stream != b->stream) ORBIT_CUDA(cudaStreamSynchronize(c->last_stream));
+  // an eager (uncaptured) turn; the captured graphs are rebuilt on the next run
+  ORBIT_CUDA(cudaStreamSynchronize(b->stream));
+  free_graphs(p);
+  p->key_bunch = nullptr;
+  Plan plan;
+  int rc = compile(p, b, plan);
+  if (rc) return rc;
+  Profiler* prof = prof_install();
+  int nl = 0;
+  rc = enqueue_turn(p, b, b->stream, plan, true, false, &nl);
+  int rc2 = prof_collect(prof, max_kinds, names, total_ms, launches, nkinds);
+  for (auto c : p->calcs) c->last_stream = b->stream;
+  for (double a : p->time_adv)
+    if (a != 0.0) b->sync.time = b->sync.time + a;
+  if (rc) return rc;
+  if (rc2) return rc2;
+  return check_status(b);
+}
+
+int orbit_program_launches(const orbit_program_t* p, int* launches) {
+  if (!p || !launches) return set_error(ORBIT_ERR_ARG, "orbit_program_launches: bad argument");
+  *launches = p->launches_per_turn;
+  return ORBIT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,904 @@
+// SpaceChargeCalc2p5D on the GPU: extrema, grid set-up, deposit, FFT Poisson
+// solve and kick as a chain of kernels on the bunch's stream with no host
+// round trip (src/spacecharge/SpaceChargeCalc2p5D.cc:77-234,
+// PoissonSolverFFT2D.cc:115-256, Grid2D.cc, Grid1D.cc).
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+#include "fft.cuh"
+#include "sc2p5d.cuh"
+#include "sc_device.cuh"
+
+namespace orbit {
+
+static const int kMaxSmem = 220 * 1024;
+
+bool make_fft_plan(int n, FftPlan& pl) {
+  pl.n = n;
+  pl.nst = 0;
+  int m = n;
+  while (m % 4 == 0 && pl.nst < 24) { pl.rad[pl.nst++] = 4; m /= 4; }
+  const int primes[] = {2, 3, 5, 7, 11, 13};
+  for (int p : primes)
+    while (m % p == 0 && pl.nst < 24) { pl.rad[pl.nst++] = p; m /= p; }
+  return m == 1;
+}
+
+double sc_host_factor(const orbit_sync_t& s, double length) {
+  return 2 * length * s.classical_radius / (std::pow(s.beta, 2) * std::pow(s.gamma, 3));
+}
+
+// ---------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------
+__global__ void k_extrema(const double* __restrict__ x, const double* __restrict__ y,
+                          const double* __restrict__ z, int n, ScState* st, unsigned* status) {
+  ExtAcc a;
+  a.init();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) a.add(x[i], y[i], z[i]);
+  ext_block_commit(a, st, status);
+}
+
+// Grid set-up of bunchAnalysis (SpaceChargeCalc2p5D.cc:126-216) in one
+// thread with explicitly rounded operations (no contraction), so that the
+// grid limits and the persistent xy_ratio evolve exactly as the reference's,
+// then all threads clear the accumulation grids.
+template <typename G>
+__global__ void k_setup(ScState* st, unsigned* status, int nx, int ny, int nz, double inv_qscale,
+                        G* rho_acc, G* z_acc) {
+  __shared__ int s_skip;
+  if (threadIdx.x == 0) {
+    double xMin = dkey_inv(st->key[0]), xMax = dkey_inv(st->key[1]);
+    double yMin = dkey_inv(st->key[2]), yMax = dkey_inv(st->key[3]);
+    double zMin = dkey_inv(st->key[4]), zMax = dkey_inv(st->key[5]);
+    for (int c = 0; c < 3; ++c) { st->key[2 * c] = ~0ull; st->key[2 * c + 1] = 0ull; }
+    int skip = 0;
+    if (*status & ST_NAN) {
+      // a non-finite coordinate was met by the extrema scan: no kick
+      skip = 1;
+    } else if (!(xMin < xMax) || !(yMin < yMax) || !(zMin < zMax)) {  // :131 (also catches an empty scan)
+      skip = 1;
+      atomicOr(status, (unsigned)ST_EXTENT);
+    } else {
+      double xy = st->xy_ratio;
+      double ratio_beam = __ddiv_rn(__dsub_rn(xMax, xMin), __dsub_rn(yMax, yMin));
+      int set_solver = 0;
+      if (fabs(__dsub_rn(ratio_beam, xy)) < __dmul_rn(0.25, xy)) {  // :152-168
+        double width, center;
+        if (ratio_beam > xy) {
+          center = __ddiv_rn(__dadd_rn(yMax, yMin), 2.0);
+          width = __ddiv_rn(__dmul_rn(__dsub_rn(yMax, yMin), __ddiv_rn(ratio_beam, xy)), 2.0);
+          yMin = __dsub_rn(center, width);
+          yMax = __dadd_rn(center, width);
+        } else {
+          center = __ddiv_rn(__dadd_rn(xMax, xMin), 2.0);
+          width = __ddiv_rn(__ddiv_rn(__dsub_rn(xMax, xMin), __ddiv_rn(ratio_beam, xy)), 2.0);
+          xMin = __dsub_rn(center, width);
+          xMax = __dadd_rn(center, width);
+        }
+        xy = __ddiv_rn(__dsub_rn(xMax, xMin), __dsub_rn(yMax, yMin));
+      } else {  // :169-173
+        xy = ratio_beam;
+        set_solver = 1;
+      }
+      // Grid2D::setGridX/Y (Grid2D.cc:422-433), Grid1D::setGridZ (Grid1D.cc:89-94)
+      double dx = __ddiv_rn(__dsub_rn(xMax, xMin), (double)(nx - 1));
+      double dy = __ddiv_rn(__dsub_rn(yMax, yMin), (double)(ny - 1));
+      double dz = __ddiv_rn(__dsub_rn(zMax, zMin), (double)nz);
+      st->xmin = xMin; st->xmax = xMax; st->ymin = yMin; st->ymax = yMax;
+      st->dx = dx; st->dy = dy; st->inv_dx = __drcp_rn(dx); st->inv_dy = __drcp_rn(dy);
+      st->zmin = zMin; st->zmax = zMax; st->dz = dz; st->inv_dz = __drcp_rn(dz);
+      st->xy_ratio = xy;
+      // solver-shape check (SpaceChargeCalc2p5D.cc:208-216)
+      if (!set_solver) {
+        double sr = __ddiv_rn(__dsub_rn(st->sxmax, st->sxmin), __dsub_rn(st->symax, st->symin));
+        if (fabs(__dsub_rn(sr, xy)) > 0.00000001) set_solver = 1;
+      }
+      if (set_solver) {  // PoissonSolverFFT2D::setGridXY (PoissonSolverFFT2D.cc:103-111)
+        st->sxmin = xMin; st->sxmax = xMax; st->symin = yMin; st->symax = yMax;
+        st->sdx = dx; st->sdy = dy;
+        st->green_dirty = 1;
+      }
+      st->scale = log(__ddiv_rn(st->sdx, dx));  // PoissonSolverFFT2D.cc:213
+      st->inv_qscale = inv_qscale;
+    }
+    st->skip = skip;
+    s_skip = skip;
+  }
+  __syncthreads();
+  if (s_skip) return;
+  for (int i = threadIdx.x; i < nx * ny; i += blockDim.x) rho_acc[i] = (G)0;
+  for (int i = threadIdx.x; i < nz; i += blockDim.x) z_acc[i] = (G)0;
+}
+
+// Green function of the doubled grid (PoissonSolverFFT2D.cc:115-152); the
+// mirrored entries are recomputed with the identical expression, which gives
+// the same values the reference copies.
+__global__ void k_green_fill(const ScState* st, double* g, int nx2, int ny2) {
+  if (!st->green_dirty || st->skip) return;
+  double sdx = st->sdx, sdy = st->sdy;
+  int tot = nx2 * ny2;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < tot; idx += gridDim.x * blockDim.x) {
+    int iX = idx / ny2, iY = idx % ny2;
+    int ex = iX <= nx2 / 2 ? iX : nx2 - iX;
+    int ey = iY <= ny2 / 2 ? iY : ny2 - iY;
+    double v = 0.0;
+    if (ex != 0 || ey != 0) {
+      double rX = __dmul_rn((double)ex, sdx), rY = __dmul_rn((double)ey, sdy);
+      double r2 = __dadd_rn(__dmul_rn(rX, rX), __dmul_rn(rY, rY));
+      v = __ddiv_rn(-log(r2), 2.0);
+    }
+    g[idx] = v;
+  }
+}
+
+// Row transforms along y (length N = ny2) of two real rows per block:
+// z = a + i b, Z = FFT(z), A_k = (Z_k + conj Z_{N-k})/2, B_k = (Z_k - conj Z_{N-k})/(2i).
+// SRC 0: Green rows (double, full length, all nx2 rows, only when dirty)
+// SRC 1: plain rho from the fixed-point grid (first ny columns, first nx rows)
+// SRC 2: fp32 rho
+template <typename T, int SRC>
+__global__ void k_rows_fwd(const ScState* st, const void* src, double* rho_out, typename CT<T>::t* hat,
+                           const typename CT<T>::t* __restrict__ tw, FftPlan pl, int nrows, int ncols, int H) {
+  typedef typename CT<T>::t C;
+  if (SRC == 0 && !st->green_dirty) return;
+  if (st->skip) return;
+  extern __shared__ unsigned char smem_raw[];
+  C* a = reinterpret_cast<C*>(smem_raw);
+  C* b = a + pl.n;
+  const int N = pl.n;
+  int r0 = 2 * blockIdx.x, r1 = r0 + 1;
+  double iq = st->inv_qscale;
+  for (int j = threadIdx.x; j < N; j += blockDim.x) {
+    T va = (T)0, vb = (T)0;
+    if (j < ncols) {
+      if (SRC == 0) {
+        const double* g = (const double*)src;
+        va = (T)g[(size_t)r0 * N + j];
+        if (r1 < nrows) vb = (T)g[(size_t)r1 * N + j];
+      } else if (SRC == 1) {
+        const long long* q = (const long long*)src;
+        double da = (double)q[(size_t)r0 * ncols + j] * iq;
+        rho_out[(size_t)r0 * ncols + j] = da;
+        va = (T)da;
+        if (r1 < nrows) {
+          double db = (double)q[(size_t)r1 * ncols + j] * iq;
+          rho_out[(size_t)r1 * ncols + j] = db;
+          vb = (T)db;
+        }
+      } else {
+        const float* q = (const float*)src;
+        float fa = q[(size_t)r0 * ncols + j];
+        rho_out[(size_t)r0 * ncols + j] = (double)fa;
+        va = (T)fa;
+        if (r1 < nrows) {
+          float fb = q[(size_t)r1 * ncols + j];
+          rho_out[(size_t)r1 * ncols + j] = (double)fb;
+          vb = (T)fb;
+        }
+      }
+    }
+    C v;
+    v.x = va;
+    v.y = vb;
+    a[j] = v;
+  }
+  __syncthreads();
+  C* Z = block_fft<T>(a, b, pl, tw, false);
+  for (int k = threadIdx.x; k < H; k += blockDim.x) {
+    C zk = Z[k], zc = c_conj(Z[(N - k) % N]);
+    C A, B;
+    A.x = (zk.x + zc.x) * (T)0.5;
+    A.y = (zk.y + zc.y) * (T)0.5;
+    // (zk - zc) / (2i) = -i/2 (zk - zc)
+    B.x = (zk.y - zc.y) * (T)0.5;
+    B.y = -(zk.x - zc.x) * (T)0.5;
+    hat[(size_t)r0 * H + k] = A;
+    if (r1 < nrows) hat[(size_t)r1 * H + k] = B;
+  }
+}
+
+// Column transforms along x (length N = nx2), one column k per block.
+// MODE 0: forward transform of the Green columns in place (when dirty).
+// MODE 1: forward, multiply by the Green spectrum with the log-scale
+//         correction (PoissonSolverFFT2D.cc:212-242), backward; rows >= nin
+//         are zero on input and only rows < nin are kept on output.
+template <typename T, int MODE>
+__global__ void k_cols(const ScState* st, typename CT<T>::t* hat, const typename CT<T>::t* __restrict__ green,
+                       const typename CT<T>::t* __restrict__ tw, FftPlan pl, int nin, int H, int ny2) {
+  typedef typename CT<T>::t C;
+  if (MODE == 0 && !st->green_dirty) return;
+  if (st->skip) return;
+  extern __shared__ unsigned char smem_raw[];
+  C* a = reinterpret_cast<C*>(smem_raw);
+  C* b = a + pl.n;
+  const int N = pl.n;
+  const int k = blockIdx.x;
+  for (int r = threadIdx.x; r < N; r += blockDim.x) {
+    C v;
+    if (r < nin) v = hat[(size_t)r * H + k];
+    else { v.x = (T)0; v.y = (T)0; }
+    a[r] = v;
+  }
+  __syncthreads();
+  C* F = block_fft<T>(a, b, pl, tw, false);
+  if (MODE == 0) {
+    for (int r = threadIdx.x; r < N; r += blockDim.x) hat[(size_t)r * H + k] = F[r];
+    return;
+  }
+  double s = st->scale;
+  for (int r = threadIdx.x; r < N; r += blockDim.x) {
+    C g = green[(size_t)r * H + k];
+    T gr;
+    if (r == 0 && k == 0) {
+      double re00 = (double)g.x;
+      gr = (T)((re00 + s * (double)(N * ny2)) - s);
+    } else {
+      gr = (T)((double)g.x - s);
+    }
+    T gi = g.y;
+    C o = F[r], res;
+    res.x = o.x * gr - o.y * gi;
+    res.y = o.x * gi + o.y * gr;
+    F[r] = res;
+  }
+  __syncthreads();
+  C* other = (F == a) ? b : a;
+  C* R = block_fft<T>(F, other, pl, tw, true);
+  for (int r = threadIdx.x; r < nin; r += blockDim.x) hat[(size_t)r * H + k] = R[r];
+}
+
+// Backward row transforms (c2r, two rows per block) and the 1/(4 nx ny)
+// normalisation onto the nx x ny potential (PoissonSolverFFT2D.cc:244-255).
+// Imaginary parts at the self-conjugate k = 0 and k = N/2 are ignored.
+template <typename T>
+__global__ void k_rows_inv(const ScState* st, const typename CT<T>::t* __restrict__ hat,
+                           const typename CT<T>::t* __restrict__ tw, FftPlan pl, int nrows, int ny, int H,
+                           double denom, double* phi, float* phi_f) {
+  typedef typename CT<T>::t C;
+  if (st->skip) return;
+  extern __shared__ unsigned char smem_raw[];
+  C* a = reinterpret_cast<C*>(smem_raw);
+  C* b = a + pl.n;
+  const int N = pl.n;
+  int r0 = 2 * blockIdx.x, r1 = r0 + 1;
+  bool has1 = r1 < nrows;
+  for (int k = threadIdx.x; k < N; k += blockDim.x) {
+    C A, B;
+    if (k < H) {
+      A = hat[(size_t)r0 * H + k];
+      B = has1 ? hat[(size_t)r1 * H + k] : C{(T)0, (T)0};
+      if (k == 0 || 2 * k == N) { A.y = (T)0; B.y = (T)0; }
+    } else {
+      A = c_conj(hat[(size_t)r0 * H + (N - k)]);
+      B = has1 ? c_conj(hat[(size_t)r1 * H + (N - k)]) : C{(T)0, (T)0};
+    }
+    C z;  // A + i B
+    z.x = A.x - B.y;
+    z.y = A.y + B.x;
+    a[k] = z;
+  }
+  __syncthreads();
+  C* R = block_fft<T>(a, b, pl, tw, true);
+  for (int j = threadIdx.x; j < ny; j += blockDim.x) {
+    double va = denom * (double)R[j].x;
+    phi[(size_t)r0 * ny + j] = va;
+    if (phi_f) phi_f[(size_t)r0 * ny + j] = (float)va;
+    if (has1) {
+      double vb = denom * (double)R[j].y;
+      phi[(size_t)r1 * ny + j] = vb;
+      if (phi_f) phi_f[(size_t)r1 * ny + j] = (float)vb;
+    }
+  }
+}
+
+// Line density to doubles, total macrosize, and the Green-rebuild flag reset.
+template <typename G>
+__global__ void k_finalize(ScState* st, const G* zacc, int nz, double* lam, float* lam_f) {
+  if (st->skip) return;
+  if (threadIdx.x == 0) st->green_dirty = 0;
+  __shared__ double s_part[32];
+  double iq = st->inv_qscale;
+  double acc = 0.0;
+  long long iacc = 0;
+  for (int k = threadIdx.x; k < nz; k += blockDim.x) {
+    double v;
+    if (sizeof(G) == 8) {
+      long long q = (long long)zacc[k];
+      iacc += q;
+      v = (double)q * iq;
+    } else {
+      v = (double)zacc[k];
+      acc += v;
+    }
+    lam[k] = v;
+    if (lam_f) lam_f[k] = (float)v;
+  }
+  if (sizeof(G) == 8) {
+    // exact integer sum, one rounding
+    __shared__ long long s_i[32];
+    for (int off = 16; off > 0; off >>= 1) iacc += __shfl_xor_sync(0xffffffffu, iacc, off);
+    if ((threadIdx.x & 31) == 0) s_i[threadIdx.x >> 5] = iacc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      long long t = 0;
+      for (int w = 0; w < (int)((blockDim.x + 31) >> 5); ++w) t += s_i[w];
+      st->total_m = (double)t * iq;
+    }
+  } else {
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+    if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0;
+      for (int w = 0; w < (int)((blockDim.x + 31) >> 5); ++w) t += s_part[w];
+      st->total_m = t;
+    }
+  }
+}
+
+// Deposit, plain form.  SMEM: block-private fixed-point grids in shared
+// memory, flushed with one 64-bit atomic per non-zero cell.
+template <bool SMEM>
+__global__ void k_deposit_plain(const double* __restrict__ x, const double* __restrict__ y,
+                                const double* __restrict__ z, const double* __restrict__ msize, int n,
+                                const ScState* st, unsigned long long* g_rho, unsigned long long* g_z,
+                                double ms_uniform, double qscale, int nx, int ny, int nz) {
+  DepConst d;
+  load_dep_const(d, st, nx, ny, nz);
+  if (d.skip) return;
+  extern __shared__ unsigned long long s_acc[];
+  unsigned long long* rho = g_rho;
+  unsigned long long* zg = g_z;
+  if (SMEM) {
+    rho = s_acc;
+    zg = s_acc + nx * ny;
+    for (int i = threadIdx.x; i < nx * ny + nz; i += blockDim.x) s_acc[i] = 0ull;
+    __syncthreads();
+  }
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double ms = msize ? msize[i] * qscale : ms_uniform;
+    deposit_plain(d, rho, zg, x[i], y[i], z[i], ms);
+  }
+  if (SMEM) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < nx * ny; i += blockDim.x) {
+      unsigned long long v = s_acc[i];
+      if (v) atomicAdd(g_rho + i, v);
+    }
+    for (int i = threadIdx.x; i < nz; i += blockDim.x) {
+      unsigned long long v = s_acc[nx * ny + i];
+      if (v) atomicAdd(g_z + i, v);
+    }
+  }
+}
+
+template <bool SMEM>
+__global__ void k_deposit_fp32(const double* __restrict__ x, const double* __restrict__ y,
+                               const double* __restrict__ z, const double* __restrict__ msize, int n,
+                               const ScState* st, float* g_rho, float* g_z, float m_uniform, int nx, int ny,
+                               int nz) {
+  DepConst d;
+  load_dep_const(d, st, nx, ny, nz);
+  if (d.skip) return;
+  extern __shared__ float s_accf[];
+  float* rho = g_rho;
+  float* zg = g_z;
+  if (SMEM) {
+    rho = s_accf;
+    zg = s_accf + nx * ny;
+    for (int i = threadIdx.x; i < nx * ny + nz; i += blockDim.x) s_accf[i] = 0.0f;
+    __syncthreads();
+  }
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float m = msize ? (float)msize[i] : m_uniform;
+    deposit_fp32(d, rho, zg, x[i], y[i], z[i], m);
+  }
+  if (SMEM) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < nx * ny; i += blockDim.x) {
+      float v = s_accf[i];
+      if (v != 0.0f) atomicAdd(g_rho + i, v);
+    }
+    for (int i = threadIdx.x; i < nz; i += blockDim.x) {
+      float v = s_accf[nx * ny + i];
+      if (v != 0.0f) atomicAdd(g_z + i, v);
+    }
+  }
+}
+
+// Kick (SpaceChargeCalc2p5D.cc:104-119).
+template <bool SMEM>
+__global__ void k_kick_plain(const double* __restrict__ x, double* __restrict__ xp, const double* __restrict__ y,
+                             double* __restrict__ yp, const double* __restrict__ z, int n, const ScState* st,
+                             const double* __restrict__ phi, const double* __restrict__ lam, double host_factor,
+                             int nx, int ny, int nz) {
+  KickConst k;
+  load_kick_const(k, st, host_factor, nx, ny, nz);
+  if (k.skip) return;
+  extern __shared__ double s_phi[];
+  const double* P = phi;
+  const double* Lm = lam;
+  if (SMEM) {
+    for (int i = threadIdx.x; i < nx * ny; i += blockDim.x) s_phi[i] = phi[i];
+    for (int i = threadIdx.x; i < nz; i += blockDim.x) s_phi[nx * ny + i] = lam[i];
+    __syncthreads();
+    P = s_phi;
+    Lm = s_phi + nx * ny;
+  }
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double a = xp[i], b = yp[i];
+    kick_plain(k, P, Lm, x[i], y[i], z[i], a, b);
+    xp[i] = a;
+    yp[i] = b;
+  }
+}
+
+template <bool SMEM>
+__global__ void k_kick_fp32(const double* __restrict__ x, double* __restrict__ xp, const double* __restrict__ y,
+                            double* __restrict__ yp, const double* __restrict__ z, int n, const ScState* st,
+                            const float* __restrict__ phi, const float* __restrict__ lam, double host_factor,
+                            int nx, int ny, int nz) {
+  KickConst k;
+  load_kick_const(k, st, host_factor, nx, ny, nz);
+  if (k.skip) return;
+  extern __shared__ float s_phif[];
+  const float* P = phi;
+  const float* Lm = lam;
+  if (SMEM) {
+    for (int i = threadIdx.x; i < nx * ny; i += blockDim.x) s_phif[i] = phi[i];
+    for (int i = threadIdx.x; i < nz; i += blockDim.x) s_phif[nx * ny + i] = lam[i];
+    __syncthreads();
+    P = s_phif;
+    Lm = s_phif + nx * ny;
+  }
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double a = xp[i], b = yp[i];
+    kick_fp32(k, P, Lm, x[i], y[i], z[i], a, b);
+    xp[i] = a;
+    yp[i] = b;
+  }
+}
+
+// Field evaluation at arbitrary points (Grid2D::calcGradient, Grid1D::getValue).
+__global__ void k_fields(const ScState* st, const double* __restrict__ phi, const double* __restrict__ lam,
+                         int nx, int ny, int nz, int n, const double* x, const double* y, const double* z,
+                         double* ex, double* ey, double* lv) {
+  KickConst k;
+  load_kick_const(k, st, 0.0, nx, ny, nz);
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  // With fac = -1 the kick adds gx/dx * lambda... evaluate the pieces directly.
+  int ix, iy;
+  double fx, fy;
+  tsc_index<double>((x[i] - k.xmin) * k.inv_dx, nx, ix, fx);
+  tsc_index<double>((y[i] - k.ymin) * k.inv_dy, ny, iy, fy);
+  double wxm, wx0, wxp, wym, wy0, wyp;
+  tsc_weights<double>(fx, wxm, wx0, wxp);
+  tsc_weights<double>(fy, wym, wy0, wyp);
+  double dxw[3] = {fx - 0.5, -2.0 * fx, 0.5 + fx};
+  double dyw[3] = {fy - 0.5, -2.0 * fy, 0.5 + fy};
+  double wxw[3] = {wxm, wx0, wxp}, wyw[3] = {wym, wy0, wyp};
+  double gx = 0, gy = 0;
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) {
+      double v = phi[(ix - 1 + a) * ny + (iy - 1 + b)];
+      gx += dxw[a] * wyw[b] * v;
+      gy += wxw[a] * dyw[b] * v;
+    }
+  ex[i] = gx * k.inv_dx;
+  ey[i] = gy * k.inv_dy;
+  double l = 0.0;
+  if (!(z[i] < k.zmin || z[i] > k.zmax)) {
+    int i0, ip;
+    double w0, wp;
+    g1_index<double>(z[i], k.zmin, k.inv_dz, nz, i0, ip, w0, wp);
+    l = (nz > 1) ? (w0 * lam[i0] + wp * lam[ip]) : lam[0];
+  }
+  lv[i] = l;
+}
+
+// ---------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------
+template <typename T>
+static void* make_twiddles(int n, cudaError_t* err) {
+  typedef typename CT<T>::t C;
+  std::vector<C> h(n);
+  for (int e = 0; e < n; ++e) {
+    long double a = 2.0L * 3.141592653589793238462643383279502884L * (long double)e / (long double)n;
+    h[e].x = (T)cosl(a);
+    h[e].y = (T)(-sinl(a));
+  }
+  if (n % 4 == 0) {  // exact quadrant points
+    h[0].x = 1; h[0].y = 0;
+    h[n / 4].x = 0; h[n / 4].y = -1;
+    h[n / 2].x = -1; h[n / 2].y = 0;
+    h[3 * n / 4].x = 0; h[3 * n / 4].y = 1;
+  } else if (n % 2 == 0) {
+    h[n / 2].x = -1; h[n / 2].y = 0;
+  }
+  void* d = nullptr;
+  *err = cudaMalloc(&d, sizeof(C) * n);
+  if (*err == cudaSuccess) *err = cudaMemcpy(d, h.data(), sizeof(C) * n, cudaMemcpyHostToDevice);
+  return d;
+}
+
+static int fft_threads(int n) { return n >= 1024 ? 512 : (n >= 256 ? 256 : 128); }
+
+template <typename T>
+static size_t fft_smem(int n) { return 2 * sizeof(typename CT<T>::t) * (size_t)n; }
+
+template <typename T>
+static int set_fft_attrs(int nmax) {
+  int bytes = (int)fft_smem<T>(nmax);
+  if (bytes <= 48 * 1024) return ORBIT_OK;
+  ORBIT_CUDA(cudaFuncSetAttribute(k_rows_fwd<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  ORBIT_CUDA(cudaFuncSetAttribute(k_rows_fwd<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  ORBIT_CUDA(cudaFuncSetAttribute(k_rows_fwd<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  ORBIT_CUDA(cudaFuncSetAttribute(k_cols<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  ORBIT_CUDA(cudaFuncSetAttribute(k_cols<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  ORBIT_CUDA(cudaFuncSetAttribute(k_rows_inv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  return ORBIT_OK;
+}
+
+static int ext_blocks(int n) {
+  int b = (n + 255) / 256;
+  int cap = num_sms() * 4;
+  return b < 1 ? 1 : (b > cap ? cap : b);
+}
+
+// launch geometry for particle kernels that keep a grid copy in shared memory
+static void particle_geometry(size_t smem, int n, int* blocks, int* threads) {
+  int bps = smem > 0 ? (int)(kMaxSmem / smem) : 8;
+  if (bps < 1) bps = 1;
+  if (bps > 4) bps = 4;
+  *threads = (bps == 1) ? 1024 : 512;
+  int b = num_sms() * bps;
+  int need = (n + *threads - 1) / *threads;
+  *blocks = need < b ? (need < 1 ? 1 : need) : b;
+}
+
+template <typename T>
+static int enqueue_solve(orbit_sc2p5d_t* c, cudaStream_t s, int* nl) {
+  typedef typename CT<T>::t C;
+  C* hat = (C*)c->d_hat;
+  C* green = (C*)c->d_green;
+  const C* twx = (const C*)c->d_tw_x;
+  const C* twy = (const C*)c->d_tw_y;
+  int thx = fft_threads(c->nx2), thy = fft_threads(c->ny2);
+  size_t smx = fft_smem<T>(c->nx2), smy = fft_smem<T>(c->ny2);
+  double denom = 1.0 / (c->nx2 * c->ny2);
+  ORBIT_PB("fft_rows_fwd", s);
+  if (c->form == ORBIT_FORM_PLAIN) {
+    k_rows_fwd<T, 1><<<(c->nx + 1) / 2, thy, smy, s>>>(c->d_st, c->d_rho_q, c->d_rho, hat, twy, c->plan_y, c->nx,
+                                                        c->ny, c->H);
+  } else {
+    k_rows_fwd<T, 2><<<(c->nx + 1) / 2, thy, smy, s>>>(c->d_st, c->d_rho_f, c->d_rho, hat, twy, c->plan_y, c->nx,
+                                                        c->ny, c->H);
+  }
+  ORBIT_PE(s);
+  ORBIT_PB("fft_cols_conv", s);
+  k_cols<T, 1><<<c->H, thx, smx, s>>>(c->d_st, hat, green, twx, c->plan_x, c->nx, c->H, c->ny2);
+  ORBIT_PE(s);
+  ORBIT_PB("fft_rows_inv", s);
+  k_rows_inv<T><<<(c->nx + 1) / 2, thy, smy, s>>>(c->d_st, hat, twy, c->plan_y, c->nx, c->ny, c->H, denom,
+                                                   c->d_phi, c->d_phi_f);
+  ORBIT_PE(s);
+  *nl += 3;
+  ORBIT_LAUNCH_CHECK("sc2p5d solve");
+  return ORBIT_OK;
+}
+
+template <typename T>
+static int enqueue_green(orbit_sc2p5d_t* c, cudaStream_t s, int* nl) {
+  typedef typename CT<T>::t C;
+  C* green = (C*)c->d_green;
+  const C* twx = (const C*)c->d_tw_x;
+  const C* twy = (const C*)c->d_tw_y;
+  int thx = fft_threads(c->nx2), thy = fft_threads(c->ny2);
+  size_t smx = fft_smem<T>(c->nx2), smy = fft_smem<T>(c->ny2);
+  int tot = c->nx2 * c->ny2;
+  int gb = (tot + 255) / 256;
+  if (gb > num_sms() * 4) gb = num_sms() * 4;
+  ORBIT_PB("green_fill", s);
+  k_green_fill<<<gb, 256, 0, s>>>(c->d_st, c->d_gbuf, c->nx2, c->ny2);
+  ORBIT_PE(s);
+  ORBIT_PB("green_rows", s);
+  k_rows_fwd<T, 0><<<c->nx2 / 2, thy, smy, s>>>(c->d_st, c->d_gbuf, nullptr, green, twy, c->plan_y, c->nx2,
+                                                 c->ny2, c->H);
+  ORBIT_PE(s);
+  ORBIT_PB("green_cols", s);
+  k_cols<T, 0><<<c->H, thx, smx, s>>>(c->d_st, green, nullptr, twx, c->plan_x, c->nx2, c->H, c->ny2);
+  ORBIT_PE(s);
+  *nl += 3;
+  ORBIT_LAUNCH_CHECK("sc2p5d green");
+  return ORBIT_OK;
+}
+
+static double qscale_for(double msum_abs) {
+  double M = msum_abs;
+  if (!(M > 0.0) || !std::isfinite(M)) return 1.0;
+  int e = 0;
+  std::frexp(M, &e);  // M < 2^e
+  return std::ldexp(1.0, 61 - e);
+}
+
+int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStream_t s, bool do_extrema,
+                    bool do_kick, int* launches) {
+  int nl = 0;
+  const int n = b->n;
+  if (do_extrema) {
+    ORBIT_PB("extrema", s);
+    k_extrema<<<ext_blocks(n), 256, 0, s>>>(b->coord(0), b->coord(2), b->coord(4), n, c->d_st, b->d_status);
+    ORBIT_PE(s);
+    ++nl;
+  }
+  // fixed-point scale from the total |macrosize|
+  double msum = b->has_msize ? b->msize_abs_sum : std::fabs(b->sync.macrosize) * (double)n;
+  double S = qscale_for(msum);
+  const double* msz = b->has_msize ? b->d_msize : nullptr;
+  const bool plain = c->form == ORBIT_FORM_PLAIN;
+  ORBIT_PB("setup", s);
+  if (plain)
+    k_setup<unsigned long long><<<1, 256, 0, s>>>(c->d_st, b->d_status, c->nx, c->ny, c->nz, 1.0 / S, c->d_rho_q,
+                                                  c->d_z_q);
+  else
+    k_setup<float><<<1, 256, 0, s>>>(c->d_st, b->d_status, c->nx, c->ny, c->nz, 1.0, c->d_rho_f, c->d_z_f);
+  ORBIT_PE(s);
+  ++nl;
+  int rc = plain ? enqueue_green<double>(c, s, &nl) : enqueue_green<float>(c, s, &nl);
+  if (rc) return rc;
+  size_t esz = plain ? sizeof(unsigned long long) : sizeof(float);
+  size_t sm = esz * ((size_t)c->nx * c->ny + c->nz);
+  int blocks, threads;
+  particle_geometry(c->smem_deposit ? sm : 0, n, &blocks, &threads);
+  ORBIT_PB("deposit", s);
+  if (plain) {
+    if (c->smem_deposit)
+      k_deposit_plain<true><<<blocks, threads, sm, s>>>(b->coord(0), b->coord(2), b->coord(4), msz, n, c->d_st,
+                                                        c->d_rho_q, c->d_z_q, b->sync.macrosize * S, S, c->nx,
+                                                        c->ny, c->nz);
+    else
+      k_deposit_plain<false><<<blocks, threads, 0, s>>>(b->coord(0), b->coord(2), b->coord(4), msz, n, c->d_st,
+                                                        c->d_rho_q, c->d_z_q, b->sync.macrosize * S, S, c->nx,
+                                                        c->ny, c->nz);
+  } else {
+    if (c->smem_deposit)
+      k_deposit_fp32<true><<<blocks, threads, sm, s>>>(b->coord(0), b->coord(2), b->coord(4), msz, n, c->d_st,
+                                                       c->d_rho_f, c->d_z_f, (float)b->sync.macrosize, c->nx,
+                                                       c->ny, c->nz);
+    else
+      k_deposit_fp32<false><<<blocks, threads, 0, s>>>(b->coord(0), b->coord(2), b->coord(4), msz, n, c->d_st,
+                                                       c->d_rho_f, c->d_z_f, (float)b->sync.macrosize, c->nx,
+                                                       c->ny, c->nz);
+  }
+  ORBIT_PE(s);
+  ORBIT_PB("finalize", s);
+  if (plain)
+    k_finalize<unsigned long long><<<1, 256, 0, s>>>(c->d_st, c->d_z_q, c->nz, c->d_lam, nullptr);
+  else
+    k_finalize<float><<<1, 256, 0, s>>>(c->d_st, c->d_z_f, c->nz, c->d_lam, c->d_lam_f);
+  ORBIT_PE(s);
+  nl += 2;
+  ORBIT_LAUNCH_CHECK("sc2p5d deposit");
+  rc = plain ? enqueue_solve<double>(c, s, &nl) : enqueue_solve<float>(c, s, &nl);
+  if (rc) return rc;
+  if (do_kick) {
+    double hf = sc_host_factor(b->sync, length);
+    size_t smk = (plain ? sizeof(double) : sizeof(float)) * ((size_t)c->nx * c->ny + c->nz);
+    particle_geometry(c->smem_kick ? smk : 0, n, &blocks, &threads);
+    ORBIT_PB("kick", s);
+    if (plain) {
+      if (c->smem_kick)
+        k_kick_plain<true><<<blocks, threads, smk, s>>>(b->coord(0), b->coord(1), b->coord(2), b->coord(3),
+                                                        b->coord(4), n, c->d_st, c->d_phi, c->d_lam, hf, c->nx,
+                                                        c->ny, c->nz);
+      else
+        k_kick_plain<false><<<blocks, threads, 0, s>>>(b->coord(0), b->coord(1), b->coord(2), b->coord(3),
+                                                       b->coord(4), n, c->d_st, c->d_phi, c->d_lam, hf, c->nx,
+                                                       c->ny, c->nz);
+    } else {
+      if (c->smem_kick)
+        k_kick_fp32<true><<<blocks, threads, smk, s>>>(b->coord(0), b->coord(1), b->coord(2), b->coord(3),
+                                                       b->coord(4), n, c->d_st, c->d_phi_f, c->d_lam_f, hf, c->nx,
+                                                       c->ny, c->nz);
+      else
+        k_kick_fp32<false><<<blocks, threads, 0, s>>>(b->coord(0), b->coord(1), b->coord(2), b->coord(3),
+                                                      b->coord(4), n, c->d_st, c->d_phi_f, c->d_lam_f, hf, c->nx,
+                                                      c->ny, c->nz);
+    }
+    ORBIT_PE(s);
+    ++nl;
+    ORBIT_LAUNCH_CHECK("sc2p5d kick");
+  }
+  c->last_stream = s;
+  if (launches) *launches += nl;
+  return ORBIT_OK;
+}
+
+static int init_attrs(orbit_sc2p5d_t* c) {
+  size_t dep = (c->form == ORBIT_FORM_PLAIN ? 8 : 4) * ((size_t)c->nx * c->ny + c->nz);
+  size_t kick = (c->form == ORBIT_FORM_PLAIN ? 8 : 4) * ((size_t)c->nx * c->ny + c->nz);
+  c->smem_deposit = dep <= (size_t)kMaxSmem;
+  c->smem_kick = kick <= (size_t)kMaxSmem;
+  if (c->form == ORBIT_FORM_PLAIN) {
+    if (c->smem_deposit && dep > 48 * 1024)
+      ORBIT_CUDA(cudaFuncSetAttribute(k_deposit_plain<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem));
+    if (c->smem_kick && kick > 48 * 1024)
+      ORBIT_CUDA(cudaFuncSetAttribute(k_kick_plain<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem));
+    int nmax = c->nx2 > c->ny2 ? c->nx2 : c->ny2;
+    return set_fft_attrs<double>(nmax);
+  }
+  if (c->smem_deposit && dep > 48 * 1024)
+    ORBIT_CUDA(cudaFuncSetAttribute(k_deposit_fp32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem));
+  if (c->smem_kick && kick > 48 * 1024)
+    ORBIT_CUDA(cudaFuncSetAttribute(k_kick_fp32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem));
+  int nmax = c->nx2 > c->ny2 ? c->nx2 : c->ny2;
+  return set_fft_attrs<float>(nmax);
+}
+
+}  // namespace orbit
+
+using namespace orbit;
+
+extern "C" {
+
+int orbit_sc2p5d_create(orbit_sc2p5d_t** out, int nx, int ny, int nz, double xy_ratio, int form) {
+  if (!out) return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_create: null output");
+  if (nx < 3 || ny < 3)
+    return set_error(ORBIT_ERR_GRID, "Grid2D: the grid size too small (should be more than 3)");
+  if (nz < 1) return set_error(ORBIT_ERR_GRID, "Grid1D: the grid size is too small (should be more than 0)");
+  if (form != ORBIT_FORM_PLAIN && form != ORBIT_FORM_FP32)
+    return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_create: unknown form");
+  if (nx > 2048 || ny > 2048)
+    return set_error(ORBIT_ERR_UNSUPPORTED, "orbit_sc2p5d_create: nx, ny above 2048 are not supported");
+  orbit_sc2p5d_t* c = new orbit_sc2p5d_t();
+  c->nx = nx; c->ny = ny; c->nz = nz; c->form = form;
+  c->nx2 = 2 * nx; c->ny2 = 2 * ny; c->H = ny + 1;
+  c->xy_ratio0 = xy_ratio > 0. ? xy_ratio : 1.0;
+  if (!make_fft_plan(c->nx2, c->plan_x) || !make_fft_plan(c->ny2, c->plan_y)) {
+    delete c;
+    return set_error(ORBIT_ERR_UNSUPPORTED, "orbit_sc2p5d_create: grid sizes must have no prime factor above 13");
+  }
+  size_t ng = (size_t)nx * ny;
+  size_t nhat = (size_t)c->nx2 * c->H;
+  cudaError_t e = cudaSuccess;
+  auto A = [&](void** p, size_t bytes) {
+    if (e == cudaSuccess) e = cudaMalloc(p, bytes);
+    if (e == cudaSuccess) e = cudaMemset(*p, 0, bytes);
+  };
+  A((void**)&c->d_st, sizeof(ScState));
+  A((void**)&c->d_rho, sizeof(double) * ng);
+  A((void**)&c->d_phi, sizeof(double) * ng);
+  A((void**)&c->d_lam, sizeof(double) * nz);
+  A((void**)&c->d_gbuf, sizeof(double) * (size_t)c->nx2 * c->ny2);
+  if (form == ORBIT_FORM_PLAIN) {
+    A((void**)&c->d_rho_q, sizeof(unsigned long long) * ng);
+    A((void**)&c->d_z_q, sizeof(unsigned long long) * nz);
+    A(&c->d_hat, sizeof(double2) * nhat);
+    A(&c->d_green, sizeof(double2) * nhat);
+    if (e == cudaSuccess) c->d_tw_x = make_twiddles<double>(c->nx2, &e);
+    if (e == cudaSuccess) c->d_tw_y = make_twiddles<double>(c->ny2, &e);
+  } else {
+    A((void**)&c->d_rho_f, sizeof(float) * ng);
+    A((void**)&c->d_z_f, sizeof(float) * nz);
+    A((void**)&c->d_phi_f, sizeof(float) * ng);
+    A((void**)&c->d_lam_f, sizeof(float) * nz);
+    A(&c->d_hat, sizeof(float2) * nhat);
+    A(&c->d_green, sizeof(float2) * nhat);
+    if (e == cudaSuccess) c->d_tw_x = make_twiddles<float>(c->nx2, &e);
+    if (e == cudaSuccess) c->d_tw_y = make_twiddles<float>(c->ny2, &e);
+  }
+  if (e != cudaSuccess) {
+    orbit_sc2p5d_destroy(c);
+    return cuda_error(e, "orbit_sc2p5d_create");
+  }
+  // constructor state (SpaceChargeCalc2p5D.cc:25-43): solver on (-r,r,-1,1),
+  // grids on (-1,1)^2 and (-0.5,0.5); the Green spectrum is built lazily on
+  // the first kick (green_dirty).
+  ScState h;
+  std::memset(&h, 0, sizeof(h));
+  double r = c->xy_ratio0;
+  h.xy_ratio = r;
+  h.sxmin = -r; h.sxmax = r; h.symin = -1.0; h.symax = 1.0;
+  h.sdx = (r - (-r)) / (nx - 1);
+  h.sdy = (1.0 - (-1.0)) / (ny - 1);
+  h.xmin = -1.0; h.xmax = 1.0; h.ymin = -1.0; h.ymax = 1.0;
+  h.dx = 2.0 / (nx - 1); h.dy = 2.0 / (ny - 1); h.inv_dx = 1.0 / h.dx; h.inv_dy = 1.0 / h.dy;
+  h.zmin = -0.5; h.zmax = 0.5; h.dz = 1.0 / nz; h.inv_dz = 1.0 / h.dz;
+  h.green_dirty = 1;
+  h.skip = 0;
+  for (int k = 0; k < 3; ++k) { h.key[2 * k] = ~0ull; h.key[2 * k + 1] = 0ull; }
+  e = cudaMemcpy(c->d_st, &h, sizeof(h), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    orbit_sc2p5d_destroy(c);
+    return cuda_error(e, "orbit_sc2p5d_create");
+  }
+  int rc = init_attrs(c);
+  if (rc) {
+    orbit_sc2p5d_destroy(c);
+    return rc;
+  }
+  *out = c;
+  return ORBIT_OK;
+}
+
+int orbit_sc2p5d_destroy(orbit_sc2p5d_t* c) {
+  if (!c) return ORBIT_OK;
+  if (c->last_stream) cudaStreamSynchronize(c->last_stream);
+  void* ptrs[] = {c->d_st, c->d_rho_q, c->d_z_q, c->d_rho_f, c->d_z_f, c->d_rho, c->d_phi, c->d_lam,
+                  c->d_phi_f, c->d_lam_f, c->d_hat, c->d_green, c->d_gbuf, c->d_tw_x, c->d_tw_y};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  delete c;
+  return ORBIT_OK;
+}
+
+int orbit_sc2p5d_track(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length) {
+  if (!c || !b) return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_track: null handle");
+  if (b->n < 2) return ORBIT_OK;  // SpaceChargeCalc2p5D.cc:79-80
+  if (c->last_stream && c->last_stream != b->stream) {
+    // the calculator's buffers were last used on another bunch's stream
+    ORBIT_CUDA(cudaStreamSynchronize(c->last_stream));
+  }
+  return sc_enqueue_kick(c, b, length, b->stream, true, true, nullptr);
+}
+
+int orbit_sc2p5d_get_grid(orbit_sc2p5d_t* c, int which, double* host_out) {
+  if (!c || !host_out) return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_get_grid: bad argument");
+  if (c->last_stream) ORBIT_CUDA(cudaStreamSynchronize(c->last_stream));
+  size_t ng = (size_t)c->nx * c->ny;
+  if (which == ORBIT_GRID_RHO) ORBIT_CUDA(cudaMemcpy(host_out, c->d_rho, sizeof(double) * ng, cudaMemcpyDeviceToHost));
+  else if (which == ORBIT_GRID_PHI) ORBIT_CUDA(cudaMemcpy(host_out, c->d_phi, sizeof(double) * ng, cudaMemcpyDeviceToHost));
+  else if (which == ORBIT_GRID_LONG) ORBIT_CUDA(cudaMemcpy(host_out, c->d_lam, sizeof(double) * c->nz, cudaMemcpyDeviceToHost));
+  else return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_get_grid: unknown grid");
+  return ORBIT_OK;
+}
+
+int orbit_sc2p5d_get_limits(orbit_sc2p5d_t* c, double* lim) {
+  if (!c || !lim) return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_get_limits: bad argument");
+  if (c->last_stream) ORBIT_CUDA(cudaStreamSynchronize(c->last_stream));
+  ScState h;
+  ORBIT_CUDA(cudaMemcpy(&h, c->d_st, sizeof(h), cudaMemcpyDeviceToHost));
+  lim[0] = h.xmin; lim[1] = h.xmax; lim[2] = h.ymin; lim[3] = h.ymax; lim[4] = h.zmin; lim[5] = h.zmax;
+  lim[6] = h.dx; lim[7] = h.dy; lim[8] = h.dz; lim[9] = h.xy_ratio; lim[10] = h.total_m;
+  return ORBIT_OK;
+}
+
+int orbit_sc2p5d_get_sizes(const orbit_sc2p5d_t* c, int* nx, int* ny, int* nz, int* form) {
+  if (!c) return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_get_sizes: null handle");
+  if (nx) *nx = c->nx;
+  if (ny) *ny = c->ny;
+  if (nz) *nz = c->nz;
+  if (form) *form = c->form;
+  return ORBIT_OK;
+}
+
+int orbit_sc2p5d_fields(orbit_sc2p5d_t* c, int n, const double* x, const double* y, const double* z, double* ex,
+                        double* ey, double* lam) {
+  if (!c || n < 0 || (n > 0 && (!x || !y || !z || !ex || !ey || !lam)))
+    return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_fields: bad argument");
+  if (n == 0) return ORBIT_OK;
+  if (c->last_stream) ORBIT_CUDA(cudaStreamSynchronize(c->last_stream));
+  double* d = nullptr;
+  ORBIT_CUDA(cudaMalloc(&d, sizeof(double) * 6 * (size_t)n));
+  cudaError_t e = cudaMemcpy(d, x, sizeof(double) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d + n, y, sizeof(double) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d + 2 * (size_t)n, z, sizeof(double) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    k_fields<<<(n + 255) / 256, 256>>>(c->d_st, c->d_phi, c->d_lam, c->nx, c->ny, c->nz, n, d, d + n,
+                                        d + 2 * (size_t)n, d + 3 * (size_t)n, d + 4 * (size_t)n, d + 5 * (size_t)n);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(ex, d + 3 * (size_t)n, sizeof(double) * n, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(ey, d + 4 * (size_t)n, sizeof(double) * n, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(lam, d + 5 * (size_t)n, sizeof(double) * n, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_error(e, "orbit_sc2p5d_fields");
+  return ORBIT_OK;
+}
+
+}  // extern "C"

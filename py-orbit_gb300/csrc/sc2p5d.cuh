@@ -1,0 +1,84 @@
+// 2.5D space-charge calculator: device state and kernel entry points shared
+// by the eager trackBunch path (sc2p5d.cu) and the lattice programs
+// (program.cu).
+#pragma once
+
+#include "common.cuh"
+
+namespace orbit {
+
+// Device-resident per-calculator state, written by the setup kernel so
+// that a whole kick runs without a host round trip (and can be captured in
+// a CUDA graph).  Field meanings follow SpaceChargeCalc2p5D::bunchAnalysis
+// (src/spacecharge/SpaceChargeCalc2p5D.cc:122-234) and PoissonSolverFFT2D.
+struct ScState {
+  double xmin, xmax, ymin, ymax, dx, dy, inv_dx, inv_dy;  // rho/phi grid (Grid2D)
+  double zmin, zmax, dz, inv_dz;                          // line-density grid (Grid1D)
+  double xy_ratio;                                        // calculator's xy_ratio (persists)
+  double sxmin, sxmax, symin, symax, sdx, sdy;            // Poisson-solver grid
+  double re00;                                            // Re G~[0][0] (PoissonSolverFFT2D.cc:164)
+  double scale;                                           // log(dx_solver/dx_rho) (:213)
+  double total_m;                                         // sum of the line density (:229-233)
+  double inv_qscale;                                      // 1/S of the fixed-point deposit
+  int green_dirty;                                        // Green spectrum must be rebuilt
+  int skip;                                               // this kick is skipped (zero extent)
+  unsigned long long key[6];                              // extrema accumulators (ordered keys)
+};
+
+struct FftPlan {
+  int n;
+  int nst;
+  int rad[24];
+};
+
+}  // namespace orbit
+
+struct orbit_sc2p5d {
+  int nx = 0, ny = 0, nz = 0, form = 0;
+  int nx2 = 0, ny2 = 0, H = 0;   // doubled grid, H = ny2/2 + 1
+  double xy_ratio0 = 1.0;
+  orbit::ScState* d_st = nullptr;
+  unsigned long long* d_rho_q = nullptr;  // fixed-point deposit (plain form)
+  unsigned long long* d_z_q = nullptr;
+  float* d_rho_f = nullptr;               // FP32 deposit (fp32 form)
+  float* d_z_f = nullptr;
+  double* d_rho = nullptr;                // user-visible rho (nx*ny)
+  double* d_phi = nullptr;                // user-visible phi (nx*ny)
+  double* d_lam = nullptr;                // user-visible line density (nz)
+  float* d_phi_f = nullptr;               // fp32-form phi
+  float* d_lam_f = nullptr;
+  void* d_hat = nullptr;                  // nx2 * H complex work spectrum (T = double or float)
+  void* d_green = nullptr;                // nx2 * H complex Green spectrum
+  double* d_gbuf = nullptr;               // nx2 * ny2 real Green function
+  void* d_tw_x = nullptr;                 // twiddles for N = nx2
+  void* d_tw_y = nullptr;                 // twiddles for N = ny2
+  orbit::FftPlan plan_x{}, plan_y{};
+  cudaStream_t last_stream = nullptr;
+  bool smem_deposit = false, smem_kick = false;
+  int dep_threads = 512, kick_threads = 512;
+};
+
+namespace orbit {
+
+// Enqueues one full trackBunch (extrema .. kick) for the bunch on `st`.
+// `do_extrema` = false when the extrema keys were already accumulated by a
+// fused pass; `do_kick` = false when the kick is deferred to the next fused
+// pass.  Returns the number of kernel launches added through *launches.
+int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStream_t st,
+                    bool do_extrema, bool do_kick, int* launches);
+// Kick factor 2 L r_c / (beta^2 gamma^3) computed on the host exactly as
+// SpaceChargeCalc2p5D.cc:96 does (libm pow).
+double sc_host_factor(const orbit_sync_t& s, double length);
+
+// Per-particle SC kick and extrema helpers used inside fused passes.
+struct KickArgs {
+  const ScState* st;
+  const double* phi;      // plain form
+  const double* lam;
+  const float* phi_f;     // fp32 form
+  const float* lam_f;
+  double host_factor;
+  int nx, ny, nz, form;
+};
+
+}  // namespace orbit

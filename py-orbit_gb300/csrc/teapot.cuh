@@ -1,0 +1,298 @@
+// TEAPOT symplectic maps as per-particle device functions.
+//
+// Each map restates one function of src/teapot/teapotbase.cc (cited per
+// case).  The per-element constants the reference computes once per call
+// (matrix elements, 1/factorial, cos/sin of the element angle) are computed
+// on the host in the same way (compile_op in teapot.cu) and carried in
+// DevOp::c; the per-particle arithmetic runs here in FP64 with fused
+// multiply-add allowed.  Per particle, dp_p = dE/(p*beta) and
+// KNL = 1/(1+dp_p) are computed once and reused by every map until a map
+// changes dE, which gives exactly the values each map would recompute.
+#pragma once
+
+#include "common.cuh"
+
+namespace orbit {
+
+struct DevOp {
+  int code, i0, i1, i2;
+  double c[12];
+};
+
+struct MapCtx {
+  double dp_p_coeff;  // 1/(p*beta)   (e.g. teapotbase.cc:168)
+  double gamma2i;     // 1/gamma^2    (teapotbase.cc:167)
+  double charge;      // bunch charge
+};
+
+struct Part {
+  double x, xp, y, yp, z, dE;
+  double dp_p, knl;
+  bool knl_ok;
+};
+
+__device__ __forceinline__ void ensure_knl(Part& p, const MapCtx& m) {
+  if (!p.knl_ok) {
+    p.dp_p = p.dE * m.dp_p_coeff;
+    p.knl = __drcp_rn(1.0 + p.dp_p);
+    p.knl_ok = true;
+  }
+}
+
+// drifti body (teapotbase.cc:132-139)
+__device__ __forceinline__ void drift_body(Part& p, const MapCtx& m, double L) {
+  ensure_knl(p, m);
+  double dp_p = p.dp_p, knl = p.knl;
+  double kl = knl * L;
+  p.x += kl * p.xp;
+  p.y += kl * p.yp;
+  double phifac = (p.xp * p.xp + p.yp * p.yp + dp_p * dp_p * m.gamma2i) * 0.5;
+  phifac = (phifac * knl - dp_p * m.gamma2i) * knl;
+  p.z -= L * phifac;
+}
+
+// complex helpers
+struct dcx { double re, im; };
+__device__ __forceinline__ dcx cmul(dcx a, dcx b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+__device__ __forceinline__ dcx cadd(dcx a, dcx b) { return {a.re + b.re, a.im + b.im}; }
+__device__ __forceinline__ dcx csub(dcx a, dcx b) { return {a.re - b.re, a.im - b.im}; }
+
+// multpfringeIN/OUT body (teapotbase.cc:436-486, 549-599); the sign of
+// kterm (IN: -kterm, OUT: +kterm) is folded into c[0], c[1] on the host.
+__device__ __forceinline__ void multpfringe_body(Part& p, const MapCtx& m, int pole, double ktre, double ktim) {
+  ensure_knl(p, m);
+  double x = p.x, y = p.y, px = p.xp, py = p.yp, KNL = p.knl;
+  dcx z = {x, y};
+  int l = pole + 1, lp2 = pole + 3;
+  dcx zlm1 = {1.0, 0.0};
+  for (int k = 0; k < pole; k++) zlm1 = cmul(zlm1, z);
+  dcx zl = cmul(zlm1, z);
+  double dl = (double)l, dlp2 = (double)lp2;
+  dcx fxterm = {dl * x, -dlp2 * y};
+  dcx dxfxterm = {dl * (fxterm.re + x), dl * (fxterm.im + y)};
+  // i * (l*fxterm - lp2*z)
+  dcx tq = {dl * fxterm.re - dlp2 * x, dl * fxterm.im - dlp2 * y};
+  dcx dyfxterm = {-tq.im, tq.re};
+  dcx fyterm = {dl * y, dlp2 * x};
+  // l*fyterm + i*lp2*z
+  dcx dxfyterm = {dl * fyterm.re - dlp2 * y, dl * fyterm.im + dlp2 * x};
+  // l*(i*fyterm + z)
+  dcx dyfyterm = {dl * (-fyterm.im + x), dl * (fyterm.re + y)};
+  dcx kt = {ktre, ktim};
+  dcx kzl = cmul(kt, zl), kzm = cmul(kt, zlm1);
+  double fxcx = cmul(kzl, fxterm).re;
+  double dxfxcx = cmul(kzm, dxfxterm).re;
+  double dyfxcx = cmul(kzm, dyfxterm).re;
+  double fycx = cmul(kzl, fyterm).re;
+  double dxfycx = cmul(kzm, dxfyterm).re;
+  double dyfycx = cmul(kzm, dyfyterm).re;
+  p.x -= fxcx * KNL;
+  p.y -= fycx * KNL;
+  double M11 = 1.0 - dxfxcx * KNL;
+  double M12 = -dxfycx * KNL;
+  double M21 = -dyfxcx * KNL;
+  double M22 = 1.0 - dyfycx * KNL;
+  double detM = M11 * M22 - M12 * M21;
+  double pxnew = (M22 * px - M12 * py) / detM;
+  double pynew = (-M21 * px + M11 * py) / detM;
+  p.xp = pxnew;
+  p.yp = pynew;
+  p.z -= (pxnew * fxcx + pynew * fycx) * KNL * KNL;
+}
+
+// Applies ops[a..b) to one particle.
+__device__ __forceinline__ void apply_ops(Part& p, const DevOp* __restrict__ ops, int a, int b,
+                                          const MapCtx& m) {
+  for (int k = a; k < b; ++k) {
+    const DevOp& o = ops[k];
+    switch (o.code) {
+      case ORBIT_OP_DRIFT:  // drift (teapotbase.cc:158-184)
+        drift_body(p, m, o.c[0]);
+        break;
+      case ORBIT_OP_QUAD1: {  // quad1 (teapotbase.cc:620-701); c = m11,m12,m21,m22,m33,m34,m43,m44,g2i*L
+        ensure_knl(p, m);
+        double x0 = p.x, xp0 = p.xp, y0 = p.y, yp0 = p.yp;
+        p.x = x0 * o.c[0] + xp0 * o.c[1];
+        p.xp = x0 * o.c[2] + xp0 * o.c[3];
+        p.y = y0 * o.c[4] + yp0 * o.c[5];
+        p.yp = y0 * o.c[6] + yp0 * o.c[7];
+        p.z += p.dp_p * o.c[8];
+        break;
+      }
+      case ORBIT_OP_QUAD2:
+      case ORBIT_OP_BEND2: {  // quad2 / bend2 (teapotbase.cc:719-744, 1164-1189); c0 = L
+        ensure_knl(p, m);
+        double L = o.c[0], dp_p = p.dp_p, knl = p.knl;
+        double kld = knl * L * dp_p;
+        p.x -= kld * p.xp;
+        p.y -= kld * p.yp;
+        double d2g = dp_p * dp_p * m.gamma2i;
+        double phifac = (p.xp * p.xp + p.yp * p.yp + d2g) * 0.5;
+        phifac = (phifac * knl + d2g) * knl;
+        p.z -= L * phifac;
+        break;
+      }
+      case ORBIT_OP_QFRIN:
+      case ORBIT_OP_QFROUT: {  // quadfringeIN/OUT (teapotbase.cc:784-904); c0 = kq, c1 = +1 IN / -1 OUT
+        ensure_knl(p, m);
+        double kq = o.c[0], s = o.c[1], KNL = p.knl;
+        double x0 = p.x, xp0 = p.xp, y0 = p.y, yp0 = p.yp;
+        double x2 = x0 * x0, y2 = y0 * y0;
+        double k4 = kq * KNL * 0.25, k12 = kq * KNL * (1.0 / 12.);
+        double t = k4 * (x2 - y2);
+        double detM = 1.0 - t * t;
+        double rdet = __drcp_rn(detM);
+        double x2p3y2 = x2 + 3. * y2, y2p3x2 = y2 + 3. * x2, r2 = x2 + y2;
+        p.x = x0 + s * (k12 * x0 * x2p3y2);
+        p.xp = (xp0 - s * (k4 * (xp0 * r2 - 2. * yp0 * x0 * y0))) * rdet;
+        p.y = y0 - s * (k12 * y0 * y2p3x2);
+        p.yp = (yp0 - s * (k4 * (-yp0 * r2 + 2. * xp0 * x0 * y0))) * rdet;
+        p.z += s * ((kq * KNL * KNL * (1.0 / 12.)) * (xp0 * x0 * x2p3y2 - yp0 * y0 * y2p3x2));
+        break;
+      }
+      case ORBIT_OP_BEND1: {  // bend1 (teapotbase.cc:1099-1146); c = m11,m12,m16,m21,m22,m26,m51,m52,m56,L
+        ensure_knl(p, m);
+        double x0 = p.x, xp0 = p.xp, dp_p = p.dp_p;
+        p.x = x0 * o.c[0] + xp0 * o.c[1] + dp_p * o.c[2];
+        p.xp = x0 * o.c[3] + xp0 * o.c[4] + dp_p * o.c[5];
+        p.y += o.c[9] * p.yp;
+        p.z += x0 * o.c[6] + xp0 * o.c[7] + dp_p * o.c[8];
+        break;
+      }
+      case ORBIT_OP_BEND3: {  // bend3 (teapotbase.cc:1208-1232); c0 = th
+        ensure_knl(p, m);
+        double th = o.c[0], dp_p = p.dp_p, KNL = p.knl;
+        double phifac = (p.yp * p.yp + dp_p * dp_p * m.gamma2i) * 0.5;
+        p.xp -= phifac * KNL * th;
+        p.y += KNL * p.yp * p.x * th;
+        phifac = (phifac * KNL - dp_p * m.gamma2i) * KNL;
+        p.z -= th * phifac * p.x;
+        break;
+      }
+      case ORBIT_OP_BEND4: {  // bend4 (teapotbase.cc:1251-1274); c0 = th
+        ensure_knl(p, m);
+        double th = o.c[0], KNL = p.knl;
+        double xfac = 1.0 + KNL * p.xp * th * 0.5;
+        double phifac = KNL * KNL * p.xp * p.xp * 0.5;
+        p.x *= xfac * xfac;
+        p.xp /= xfac;
+        p.z -= th * phifac * p.x;
+        break;
+      }
+      case ORBIT_OP_BFRIN:
+      case ORBIT_OP_BFROUT: {  // bendfringeIN/OUT (teapotbase.cc:1292-1348); c0 = +-1/(2 rho), c1 = +-1/rho
+        ensure_knl(p, m);
+        double KNL = p.knl, y2 = p.y * p.y;
+        p.x += KNL * y2 * o.c[0];
+        p.yp -= KNL * p.xp * p.y * o.c[1];
+        p.z += KNL * KNL * p.xp * y2 * o.c[0];
+        break;
+      }
+      case ORBIT_OP_MULTP: {  // multp (teapotbase.cc:336-374); i0 = pole, i1 = skew, c0 = kl/pole!
+        if (m.charge == 0.) break;
+        dcx z = {p.x, p.y};
+        dcx zn = {1.0, 0.0};
+        for (int q = 0; q < o.i0; q++) zn = cmul(zn, z);
+        double kl1 = o.c[0];
+        if (o.i1) {
+          p.xp += kl1 * zn.im;
+          p.yp += kl1 * zn.re;
+        } else {
+          p.xp -= kl1 * zn.re;
+          p.yp += kl1 * zn.im;
+        }
+        break;
+      }
+      case ORBIT_OP_MPFRIN:
+      case ORBIT_OP_MPFROUT:  // c0, c1 = signed kterm (re, im)
+        if (m.charge == 0.) break;
+        multpfringe_body(p, m, o.i0, o.c[0], o.c[1]);
+        break;
+      case ORBIT_OP_ROTXY: {  // rotatexy (teapotbase.cc:80-101); c0 = cos, c1 = sin
+        double cs = o.c[0], sn = o.c[1];
+        double xt = p.x, pxt = p.xp, yt = p.y, pyt = p.yp;
+        p.x = cs * xt - sn * yt;
+        p.xp = cs * pxt - sn * pyt;
+        p.y = sn * xt + cs * yt;
+        p.yp = sn * pxt + cs * pyt;
+        break;
+      }
+      case ORBIT_OP_WRAP:  // wrapbunch (teapotbase.cc:202-212); c0 = L, c1 = L/2
+        if (p.z < -o.c[1]) p.z += o.c[0];
+        if (p.z > o.c[1]) p.z -= o.c[0];
+        break;
+      case ORBIT_OP_KICK:  // kick (teapotbase.cc:232-258)
+        if (o.c[0] != 0.) p.xp += o.c[0];
+        if (o.c[1] != 0.) p.yp += o.c[1];
+        if (o.c[2] != 0.) { p.dE += o.c[2]; p.knl_ok = false; }
+        break;
+      case ORBIT_OP_WEDGEROT: {  // wedgerotate (teapotbase.cc:923-967); c0 = cos, c1 = sin, i0 = frinout
+        double cs = o.c[0], sn = o.c[1], dp_p;
+        double dpc = m.dp_p_coeff;
+        if (o.i0 == 0) {
+          dp_p = p.dE * dpc;
+          double xp_t = p.xp, p0_t = 1.0 + dp_p;
+          p.x /= cs;
+          p.xp = xp_t * cs + p0_t * sn;
+          double p0 = -xp_t * sn + p0_t * cs;
+          dp_p = p0 - 1.0;
+          p.z = (-p.x * sn + p.z) * cs;
+        } else {
+          dp_p = p.dE * dpc;
+          double p0 = 1.0 + dp_p;
+          p.z = p.x * sn + p.z / cs;
+          p.x *= cs;
+          double xp_t = p.xp * cs - p0 * sn;
+          double p0_t = p.xp * sn + p0 * cs;
+          p.xp = xp_t;
+          dp_p = p0_t - 1.0;
+        }
+        p.dE = dp_p / dpc;
+        p.knl_ok = false;
+        break;
+      }
+      case ORBIT_OP_WEDGEDRIFT: {  // wedgedrift (teapotbase.cc:986-1016); c0 = ct, i0 = inout
+        double s;
+        if (o.i0 == 0) {
+          ensure_knl(p, m);
+          double tn = p.xp / (1.0 + p.dp_p);
+          s = p.x / (o.c[0] - tn);
+        } else {
+          s = p.x / o.c[0];
+        }
+        drift_body(p, m, s);
+        break;
+      }
+      case ORBIT_OP_WEDGEBEND: {  // wedgebend (teapotbase.cc:1037-1080); c0 = ct, c1 = rho, i0 = inout, i1 = nst
+        double s;
+        if (o.i0 == 0) {
+          s = -p.x / o.c[0];
+        } else {
+          ensure_knl(p, m);
+          double tn = p.xp / (1.0 + p.dp_p);
+          s = -p.x / (o.c[0] + tn);
+        }
+        int nst = o.i1;
+        double sm = s / nst, sm2 = sm / 2.0;
+        drift_body(p, m, sm2);
+        p.xp -= sm / o.c[1];
+        for (int j = 1; j < nst; j++) {
+          drift_body(p, m, sm);
+          p.xp -= sm / o.c[1];
+        }
+        drift_body(p, m, sm2);
+        break;
+      }
+      default:
+        break;
+    }
+  }
+}
+
+// Host: compiles a reference op into a DevOp with the per-element constants
+// computed as the reference computes them; returns false for an unknown code.
+// `time_adv` receives length/v for maps that advance SyncPart time, or 0.
+bool compile_op(const orbit_op_t& in, const orbit_sync_t& s, DevOp& out, double* time_adv);
+MapCtx make_ctx(const orbit_sync_t& s);
+
+}  // namespace orbit

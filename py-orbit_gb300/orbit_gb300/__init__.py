@@ -1,0 +1,200 @@
+"""orbit_gb300: GB300-native (sm_103a) PyORBIT 2.5D space-charge and TEAPOT
+tracking hot path behind the C ABI of include/orbit_gb300.h.
+
+The reference-compatible Python modules live beside this package
+(``bunch``, ``spacecharge``, ``orbit.*``); this package holds the thin
+native layer they call.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _native
+from ._native import (FORM_FP32, FORM_PLAIN, OP, OrbitError, SpaceChargeError, Sync, call, load,
+                      library_path)
+
+__all__ = ["DeviceBunch", "DeviceSC2p5D", "DeviceProgram", "OrbitError", "SpaceChargeError", "load",
+           "FORM_PLAIN", "FORM_FP32", "OP", "library_path", "version"]
+
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+def version() -> str:
+    return load().orbit_version().decode()
+
+
+def _ptr_array(arrs):
+    return (_dp * 6)(*[a.ctypes.data_as(_dp) for a in arrs])
+
+
+class DeviceBunch:
+    """A device-resident SoA bunch (six FP64 arrays in HBM)."""
+
+    def __init__(self, capacity: int = 0):
+        h = ctypes.c_void_p()
+        call("orbit_bunch_create", ctypes.byref(h), int(capacity))
+        self.h = h
+        self._n = 0
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h is not None and h.value and _native._lib is not None:
+            _native._lib.orbit_bunch_destroy(h)
+            self.h = None
+
+    @property
+    def n(self) -> int:
+        return self._n
+
+    def upload(self, soa: np.ndarray):
+        soa = np.ascontiguousarray(soa, dtype=np.float64)
+        if soa.ndim != 2 or soa.shape[0] != 6:
+            raise ValueError("expected a (6, n) array")
+        n = soa.shape[1]
+        rows = [np.ascontiguousarray(soa[c]) for c in range(6)]
+        call("orbit_bunch_upload", self.h, _ptr_array(rows), n)
+        self._n = n
+        # the upload is asynchronous from pinned or pageable memory; make the
+        # host arrays' lifetime irrelevant by waiting here
+        call("orbit_bunch_sync", self.h)
+
+    def upload_rows(self, rows, n: int):
+        """Upload from six host arrays without copying them into one block."""
+        call("orbit_bunch_upload", self.h, _ptr_array(rows), int(n))
+        self._n = int(n)
+
+    def download(self, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty((6, self._n), dtype=np.float64)
+        rows = [out[c] for c in range(6)]
+        if not all(r.flags.c_contiguous for r in rows):
+            raise ValueError("output rows must be contiguous")
+        call("orbit_bunch_download", self.h, _ptr_array(rows))
+        return out
+
+    def download_rows(self, rows):
+        call("orbit_bunch_download", self.h, _ptr_array(rows))
+
+    def set_sync(self, s: Sync):
+        call("orbit_bunch_set_sync", self.h, ctypes.byref(s))
+
+    def get_sync(self) -> Sync:
+        s = Sync()
+        call("orbit_bunch_get_sync", self.h, ctypes.byref(s))
+        return s
+
+    def set_macrosizes(self, m):
+        if m is None:
+            call("orbit_bunch_set_macrosizes", self.h, None, 0)
+        else:
+            m = np.ascontiguousarray(m, dtype=np.float64)
+            call("orbit_bunch_set_macrosizes", self.h, m.ctypes.data_as(_dp), m.shape[0])
+
+    def sync(self):
+        call("orbit_bunch_sync", self.h)
+
+    def stream_ptr(self) -> int:
+        """The bunch's cudaStream_t as an integer."""
+        v = ctypes.c_void_p()
+        call("orbit_bunch_stream", self.h, ctypes.byref(v))
+        return v.value or 0
+
+    def device_pointers(self):
+        ptrs = (_dp * 6)()
+        call("orbit_bunch_device_coords", self.h, ptrs)
+        return [ctypes.cast(p, ctypes.c_void_p).value for p in ptrs]
+
+    def tpb(self, name: str, *args):
+        conv = [int if t is ctypes.c_int else float for t in _native.TPB_SIGS[name]]
+        call("orbit_tpb_" + name, self.h, *[c(a) for c, a in zip(conv, args)])
+
+
+class DeviceSC2p5D:
+    """The device SpaceChargeCalc2p5D (FP64 plain or FP32 form)."""
+
+    def __init__(self, nx: int, ny: int, nz: int, xy_ratio: float = -1.0, form: int = FORM_PLAIN):
+        h = ctypes.c_void_p()
+        call("orbit_sc2p5d_create", ctypes.byref(h), int(nx), int(ny), int(nz), float(xy_ratio), int(form))
+        self.h = h
+        self.nx, self.ny, self.nz, self.form = int(nx), int(ny), int(nz), int(form)
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h is not None and h.value and _native._lib is not None:
+            _native._lib.orbit_sc2p5d_destroy(h)
+            self.h = None
+
+    def track(self, bunch: DeviceBunch, length: float):
+        call("orbit_sc2p5d_track", self.h, bunch.h, float(length))
+
+    def grid(self, which: int) -> np.ndarray:
+        n = self.nz if which == _native.GRID_LONG else self.nx * self.ny
+        out = np.empty(n, dtype=np.float64)
+        call("orbit_sc2p5d_get_grid", self.h, int(which), out.ctypes.data_as(_dp))
+        return out if which == _native.GRID_LONG else out.reshape(self.nx, self.ny)
+
+    def limits(self) -> np.ndarray:
+        lim = np.empty(11, dtype=np.float64)
+        call("orbit_sc2p5d_get_limits", self.h, lim.ctypes.data_as(_dp))
+        return lim
+
+    def fields(self, x, y, z):
+        x, y, z = (np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z))
+        n = x.shape[0]
+        ex, ey, lam = np.empty(n), np.empty(n), np.empty(n)
+        call("orbit_sc2p5d_fields", self.h, n, *[a.ctypes.data_as(_dp) for a in (x, y, z, ex, ey, lam)])
+        return ex, ey, lam
+
+
+class DeviceProgram:
+    """A compiled lattice program: ops (code, (i0,i1,i2), (d0..d5)) plus calculators."""
+
+    def __init__(self, ops, calcs):
+        arr = (_native.Op * max(1, len(ops)))()
+        for k, (code, iv, dv) in enumerate(ops):
+            arr[k].code = int(code)
+            iv = list(iv) + [0, 0, 0]
+            arr[k].i0, arr[k].i1, arr[k].i2 = int(iv[0]), int(iv[1]), int(iv[2])
+            dv = list(dv) + [0.0] * 6
+            for j in range(6):
+                arr[k].d[j] = float(dv[j])
+        hs = (ctypes.c_void_p * max(1, len(calcs)))(*[c.h.value for c in calcs])
+        h = ctypes.c_void_p()
+        call("orbit_program_create", ctypes.byref(h), arr, len(ops), hs, len(calcs))
+        self.h = h
+        self.calcs = list(calcs)  # keep the calculators alive
+        self.nops = len(ops)
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h is not None and h.value and _native._lib is not None:
+            _native._lib.orbit_program_destroy(h)
+            self.h = None
+
+    def run(self, bunch: DeviceBunch, turns: int = 1):
+        call("orbit_program_run", self.h, bunch.h, int(turns))
+
+    def enqueue(self, bunch: DeviceBunch, turns: int = 1):
+        """Enqueue without waiting; bunch.sync() waits and reports errors."""
+        call("orbit_program_enqueue", self.h, bunch.h, int(turns))
+
+    def launches_per_turn(self) -> int:
+        v = ctypes.c_int()
+        call("orbit_program_launches", self.h, ctypes.byref(v))
+        return v.value
+
+    def profile(self, bunch: DeviceBunch, max_kinds: int = 32):
+        """One eager turn with every launch timed by CUDA events:
+        {kernel kind: (total ms, launches)}."""
+        names = ctypes.create_string_buffer(32 * max_kinds)
+        ms = (ctypes.c_double * max_kinds)()
+        cnt = (ctypes.c_int * max_kinds)()
+        nk = ctypes.c_int()
+        call("orbit_program_profile", self.h, bunch.h, max_kinds, names, ms, cnt, ctypes.byref(nk))
+        out = {}
+        for k in range(nk.value):
+            nm = names.raw[32 * k: 32 * k + 32].split(b"\0", 1)[0].decode()
+            out[nm] = (ms[k], cnt[k])
+        return out

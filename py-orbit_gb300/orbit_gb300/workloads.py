@@ -1,0 +1,96 @@
+"""Synthetic workloads of the benchmark configurations, built through the
+reference-compatible API.  All inputs are seeded (numpy PCG64); the
+reference publishes no datasets for this path.
+
+C1  plain FP64, CPU-runnable: 1e5 protons at 1 GeV, macrosize 1e9,
+    x, y ~ N(0, 5 mm), x', y' ~ N(0, 1 mrad), z ~ U(-100, 100) m, dE = 0;
+    grid 64x64x1; lattice (0.5 m drift + SC kick) x 10.
+C2  FODO tracking: 1e6 protons at 1 GeV, 4D waterbag with rms 4 mm /
+    0.8 mrad, z ~ N(0, 10 m), dE ~ N(0, 1 MeV); grid 128x128x64; 40 FODO
+    cells (quads k1 = +-0.5 m^-2, 0.5 m long; 2 m drifts; 4 SC nodes per
+    cell).  The configuration names no intensity; 1e14 protons
+    (macrosize 1e8 at 1e6 particles) is used.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from orbit.bunch_generators import WaterBagDist2D, twiss_for_rms
+
+KIN_ENERGY = 1.0  # GeV
+
+
+def c1_coords(n=100_000, seed=20240601):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    soa = np.empty((6, n))
+    soa[0] = rng.normal(0.0, 5e-3, n)
+    soa[1] = rng.normal(0.0, 1e-3, n)
+    soa[2] = rng.normal(0.0, 5e-3, n)
+    soa[3] = rng.normal(0.0, 1e-3, n)
+    soa[4] = rng.uniform(-100.0, 100.0, n)
+    soa[5] = 0.0
+    return soa
+
+
+def c2_coords(n=1_000_000, seed=20240602):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    tw = twiss_for_rms(4e-3, 0.8e-3)
+    dist = WaterBagDist2D(tw, tw)
+    x, xp, y, yp = dist.generate(n, rng)
+    soa = np.empty((6, n))
+    soa[0], soa[1], soa[2], soa[3] = x, xp, y, yp
+    soa[4] = rng.normal(0.0, 10.0, n)
+    soa[5] = rng.normal(0.0, 1e-3, n)
+    return soa
+
+
+C1_MACROSIZE = 1e9
+C2_MACROSIZE = 1e8
+
+
+def make_bunch(soa, macrosize, kin_energy=KIN_ENERGY):
+    from bunch import Bunch
+    b = Bunch()
+    b.getSyncParticle().kinEnergy(kin_energy)
+    b.macroSize(macrosize)
+    b.setCoordinates(soa)
+    return b
+
+
+def c1_lattice(calc, cells=10, drift=0.5):
+    """(drift + SC kick) x cells as a TEAPOT lattice with 2.5D SC nodes."""
+    from orbit.space_charge.sc2p5d import setSC2p5DAccNodes
+    from orbit.teapot import DriftTEAPOT, TEAPOT_Lattice
+    lat = TEAPOT_Lattice("c1")
+    for i in range(cells):
+        d = DriftTEAPOT("d%d" % i)
+        d.setLength(drift)
+        lat.addNode(d)
+    lat.initialize()
+    setSC2p5DAccNodes(lat, 0.4 * drift, calc)
+    return lat
+
+
+def fodo_lattice(calc, cells=40, kq=0.5, lq=0.5, ld=2.0, sc_min=0.3):
+    """FODO cells QF-D-QD-D with quads of 2 parts (fringes on, the
+    reference default) and 2.5D SC nodes every ~0.5 / 2 m (4 per cell)."""
+    from orbit.space_charge.sc2p5d import setSC2p5DAccNodes
+    from orbit.teapot import DriftTEAPOT, QuadTEAPOT, TEAPOT_Lattice
+    lat = TEAPOT_Lattice("fodo")
+    for c in range(cells):
+        qf = QuadTEAPOT("qf%d" % c)
+        qf.setLength(lq)
+        qf.addParam("kq", kq)
+        d1 = DriftTEAPOT("d1_%d" % c)
+        d1.setLength(ld)
+        qd = QuadTEAPOT("qd%d" % c)
+        qd.setLength(lq)
+        qd.addParam("kq", -kq)
+        d2 = DriftTEAPOT("d2_%d" % c)
+        d2.setLength(ld)
+        for node in (qf, d1, qd, d2):
+            lat.addNode(node)
+    lat.initialize()
+    if calc is not None:
+        setSC2p5DAccNodes(lat, sc_min, calc)
+    return lat

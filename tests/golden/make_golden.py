@@ -1,0 +1,120 @@
+"""Generates the golden vectors in tests/golden/*.npz by running the
+REFERENCE's own C++ (compiled from the reference tree by oracle/build_ref.sh,
+FFT = project shim because FFTW is unavailable) on seeded inputs.
+
+Run here, where the reference tree exists:
+    python tests/golden/make_golden.py
+The fixtures are committed; nothing reads the reference tree at test time.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import oracle as O  # noqa: E402
+
+
+def gaussian(n, seed, sx=5e-3, sxp=1e-3, sy=4e-3, syp=1e-3, sz=10.0, sde=1e-3):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    soa = np.empty((6, n))
+    soa[0] = rng.normal(0, sx, n)
+    soa[1] = rng.normal(0, sxp, n)
+    soa[2] = rng.normal(0, sy, n)
+    soa[3] = rng.normal(0, syp, n)
+    soa[4] = rng.normal(0, sz, n)
+    soa[5] = rng.normal(0, sde, n)
+    return soa
+
+
+MAPS = [
+    ("drift", (0.7,)), ("drift", (-0.3,)), ("quad1", (0.25, 0.5)), ("quad1", (0.25, -0.5)), ("quad1", (0.3, 0.0)),
+    ("quad2", (0.25,)), ("quadfringeIN", (0.5,)), ("quadfringeOUT", (-0.5,)), ("bend1", (0.5, 0.1)),
+    ("bend2", (0.5,)), ("bend3", (0.05,)), ("bend4", (0.05,)), ("bendfringeIN", (5.0,)),
+    ("bendfringeOUT", (5.0,)), ("multp", (2, 0.3, 0)), ("multp", (1, -0.2, 1)), ("multp", (3, 5.0, 0)),
+    ("multpfringeIN", (2, 0.4, 0)), ("multpfringeOUT", (2, 0.4, 1)), ("multpfringeIN", (1, 0.3, 0)),
+    ("rotatexy", (0.1,)), ("wrapbunch", (20.0,)), ("kick", (1e-4, -2e-4, 1e-5)),
+    ("wedgerotate", (0.05, 0)), ("wedgerotate", (0.05, 1)), ("wedgedrift", (0.3, 0)), ("wedgedrift", (0.3, 1)),
+    ("wedgebend", (0.3, 0, 10.0, 4)), ("wedgebend", (0.3, 1, 10.0, 5)),
+]
+
+
+def sc_case(name, soa, nx, ny, nz, xy_ratio, seq, ek=1.0, msize=1e9):
+    """seq: list of ("sc", L) or (map, args) applied in order; records the
+    grids after each SC kick and the coordinates at the end."""
+    b = O.RefBunch(soa, ek, msize)
+    sc = O.RefSC(nx, ny, nz, xy_ratio)
+    out = {"init": soa, "nx": nx, "ny": ny, "nz": nz, "xy_ratio": xy_ratio, "ek": ek, "macrosize": msize}
+    k = 0
+    seq_txt = []
+    for step in seq:
+        if step[0] == "sc":
+            sc.track(b, step[1])
+            rho, phi, zg, lim = sc.grids()
+            c = b.coords()
+            ex, ey, lam = sc.fields(c[0], c[2], c[4])
+            out["rho_%d" % k] = rho
+            out["phi_%d" % k] = phi
+            out["zg_%d" % k] = zg
+            out["lim_%d" % k] = lim
+            if k == 0:
+                out["ex_0"] = ex
+                out["ey_0"] = ey
+                out["lam_0"] = lam
+                out["coords_0"] = c
+            k += 1
+            seq_txt.append("sc:%r" % (step[1],))
+        else:
+            b.tpb(step[0], *step[1])
+            seq_txt.append("%s:%r" % (step[0], tuple(step[1])))
+    out["final"] = b.coords()
+    out["nkicks"] = k
+    out["sequence"] = np.array(seq_txt)
+    out["kin"] = np.array([b.kinematics()[q] for q in ("beta", "gamma", "momentum", "kin_energy", "mass",
+                                                      "classical_radius", "time")])
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print("wrote", name, "kicks", k)
+
+
+def main():
+    if not O.ref_available():
+        if not O.build_reference():
+            raise SystemExit("the compiled reference is not available")
+    # 1) every TEAPOT map in sequence, 256 particles
+    soa = gaussian(256, 11)
+    b = O.RefBunch(soa, 1.0, 1e9)
+    out = {"init": soa}
+    for k, (name, args) in enumerate(MAPS):
+        b.tpb(name, *args)
+        out["after_%02d" % k] = b.coords()
+    out["kin"] = np.array([b.kinematics()[q] for q in ("beta", "gamma", "momentum", "kin_energy", "mass",
+                                                      "classical_radius", "time")])
+    out["names"] = np.array([m[0] for m in MAPS])
+    out["args"] = np.array([repr(tuple(m[1])) for m in MAPS])
+    np.savez_compressed(os.path.join(HERE, "maps.npz"), **out)
+    print("wrote maps")
+    # 2) one kick, round beam, 32x32x8
+    sc_case("sc_round_32x32x8", gaussian(4096, 21, sy=5e-3), 32, 32, 8, -1.0, [("sc", 0.5)])
+    # 3) C1-like: nz = 1, 64x64x1, drift + kick x 5
+    rng = np.random.Generator(np.random.PCG64(31))
+    c1 = gaussian(3000, 31, sy=5e-3, sde=0.0)
+    c1[4] = rng.uniform(-100, 100, 3000)
+    c1[5] = 0.0
+    sc_case("c1_64x64x1", c1, 64, 64, 1, -1.0, [("drift", (0.5,)), ("sc", 0.5)] * 5)
+    # 4) flat beam (aspect ratio far from 1: the Green function is rebuilt),
+    #    odd sizes (40 x 24 -> doubled 80 x 48), per-kick maps between
+    flat = gaussian(3000, 41, sx=8e-3, sy=2e-3)
+    sc_case("flat_40x24x16", flat, 40, 24, 16, -1.0,
+            [("sc", 0.4), ("quad1", (0.25, 0.5)), ("sc", 0.4), ("drift", (1.0,)), ("sc", 0.4)])
+    # 5) explicit xy_ratio and nz = 2
+    sc_case("ratio2_16x16x2", gaussian(2048, 51, sx=6e-3, sy=3e-3), 16, 16, 2, 2.0,
+            [("sc", 1.0), ("drift", (0.5,)), ("sc", 1.0)])
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,71 @@
+"""The C restatement (oracle) against golden vectors produced by the
+reference's own C++ (tests/golden/make_golden.py).  This pins the oracle
+before it is trusted as the GPU checker."""
+import numpy as np
+import pytest
+
+import oracle as O
+from helpers import golden_maps, kin_sync, load_golden, parse_sequence, rel_err
+
+# On the x86 build host the oracle reproduces the reference bit for bit; on
+# another host libm (log, cos, cosh) may differ in the last bit.
+TOL = 1e-13
+
+
+def test_maps_sequence():
+    g = load_golden("maps")
+    soa = np.ascontiguousarray(g["init"].copy())
+    s = kin_sync(g["kin"], 1e9)
+    s.time = 0.0
+    for k, (name, args) in enumerate(golden_maps(g)):
+        O.tpb(name, soa, s, *args)
+        ref = g["after_%02d" % k]
+        for c in range(6):
+            assert rel_err(soa[c], ref[c]) <= TOL, (k, name, c, rel_err(soa[c], ref[c]))
+    assert abs(s.time - g["kin"][6]) <= 1e-15 * abs(g["kin"][6])
+
+
+@pytest.mark.parametrize("case", ["sc_round_32x32x8", "c1_64x64x1", "flat_40x24x16", "ratio2_16x16x2"])
+def test_sc_cases(case):
+    g = load_golden(case)
+    nx, ny, nz = int(g["nx"]), int(g["ny"]), int(g["nz"])
+    sc = O.OracleSC(nx, ny, nz, float(g["xy_ratio"]))
+    s = kin_sync(g["kin"], float(g["macrosize"]))
+    soa = np.ascontiguousarray(g["init"].copy())
+    k = 0
+    for step in parse_sequence(g["sequence"]):
+        if step[0] == "sc":
+            assert sc.track(soa, s, step[1]) == 0
+            rho, phi, zg, lim = sc.grids()
+            assert rel_err(rho, g["rho_%d" % k]) <= TOL
+            assert rel_err(phi, g["phi_%d" % k]) <= TOL
+            assert rel_err(zg, g["zg_%d" % k]) <= TOL
+            assert np.allclose(lim[:9], g["lim_%d" % k], rtol=1e-15, atol=0)
+            if k == 0:
+                ex, ey, lam = sc.fields(soa[0], soa[2], soa[4])
+                assert rel_err(ex, g["ex_0"]) <= TOL
+                assert rel_err(ey, g["ey_0"]) <= TOL
+                assert rel_err(lam, g["lam_0"]) <= TOL
+                for c in range(6):
+                    assert rel_err(soa[c], g["coords_0"][c]) <= TOL
+            k += 1
+        else:
+            O.tpb(step[0], soa, s, *step[1])
+    assert k == int(g["nkicks"])
+    for c in range(6):
+        assert rel_err(soa[c], g["final"][c]) <= TOL, (case, c)
+
+
+def test_multithreaded_slices_match_within_summation_order():
+    """The rank-sliced oracle differs from one slice only by the order of the
+    grid sums (the reference's MPI decomposition)."""
+    g = load_golden("sc_round_32x32x8")
+    s = kin_sync(g["kin"], float(g["macrosize"]))
+    a = np.ascontiguousarray(g["init"].copy())
+    b = a.copy()
+    s1 = O.OracleSC(32, 32, 8)
+    s2 = O.OracleSC(32, 32, 8)
+    s1.track(a, s, 0.5, nthreads=1)
+    s2.track(b, s, 0.5, nthreads=7)
+    assert rel_err(s2.grids()[1], s1.grids()[1]) <= 1e-14
+    assert rel_err(b[1] - g["init"][1], a[1] - g["init"][1]) <= 1e-12
