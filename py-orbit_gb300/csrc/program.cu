@@ -122,6 +122,8 @@ struct orbit_program {
   cudaGraphExec_t g_single = nullptr; // prologue + turn without wrap (one-turn runs)
   std::vector<double> time_adv;       // per-op SyncPart time increments
   int launches_per_turn = 0;
+  cudaEvent_t done = nullptr;         // recorded after the last enqueued run
+  bool used = false;
 };
 
 namespace orbit {
@@ -343,13 +345,19 @@ int orbit_program_create(orbit_program_t** out, const orbit_op_t* ops, int nops,
       return set_error(ORBIT_ERR_ARG, "orbit_program_create: SC op refers to a missing calculator");
     }
   }
+  cudaError_t e = cudaEventCreateWithFlags(&p->done, cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    delete p;
+    return cuda_error(e, "orbit_program_create");
+  }
   *out = p;
   return ORBIT_OK;
 }
 
 int orbit_program_destroy(orbit_program_t* p) {
   if (!p) return ORBIT_OK;
-  if (p->key_bunch && p->key_bunch->stream) cudaStreamSynchronize(p->key_bunch->stream);
+  if (p->used) cudaEventSynchronize(p->done);  // graphs in flight read d_ops
+  if (p->done) cudaEventDestroy(p->done);
   free_graphs(p);
   if (p->d_ops) cudaFree(p->d_ops);
   delete p;
@@ -365,9 +373,9 @@ int orbit_program_run(orbit_program_t* p, orbit_bunch_t* b, int turns) {
 int orbit_program_enqueue(orbit_program_t* p, orbit_bunch_t* b, int turns) {
   if (!p || !b || turns < 0) return set_error(ORBIT_ERR_ARG, "orbit_program_enqueue: bad argument");
   if (turns == 0) return ORBIT_OK;
-  // calculators last used on another stream must be idle first
+  // work already queued on a calculator by another bunch comes first
   for (auto c : p->calcs)
-    if (c->last_stream && c->last_stream != b->stream) ORBIT_CUDA(cudaStreamSynchronize(c->last_stream));
+    ORBIT_CUDA(sc_order_before(c, b->stream));
   int rc = prepare(p, b);
   if (rc) return rc;
   if (turns == 1) {
@@ -377,7 +385,9 @@ int orbit_program_enqueue(orbit_program_t* p, orbit_bunch_t* b, int turns) {
     for (int t = 1; t < turns - 1; ++t) ORBIT_CUDA(cudaGraphLaunch(p->g_mid, b->stream));
     ORBIT_CUDA(cudaGraphLaunch(p->g_last, b->stream));
   }
-  for (auto c : p->calcs) c->last_stream = b->stream;
+  for (auto c : p->calcs) ORBIT_CUDA(sc_mark_used(c, b->stream));
+  p->used = true;
+  ORBIT_CUDA(cudaEventRecord(p->done, b->stream));
   // SyncPart time, advanced in op order as each map would (teapotbase.cc:165)
   for (int t = 0; t < turns; ++t)
     for (double a : p->time_adv)
@@ -390,7 +400,7 @@ int orbit_program_profile(orbit_program_t* p, orbit_bunch_t* b, int max_kinds, c
   if (!p || !b || max_kinds <= 0 || !names || !total_ms || !launches || !nkinds)
     return set_error(ORBIT_ERR_ARG, "orbit_program_profile: bad argument");
   for (auto c : p->calcs)
-    if (c->last_stream && c->last_stream != b->stream) ORBIT_CUDA(cudaStreamSynchronize(c->last_stream));
+    ORBIT_CUDA(sc_order_before(c, b->stream));
   // an eager (uncaptured) turn; the captured graphs are rebuilt on the next run
   ORBIT_CUDA(cudaStreamSynchronize(b->stream));
   free_graphs(p);
@@ -402,7 +412,7 @@ int orbit_program_profile(orbit_program_t* p, orbit_bunch_t* b, int max_kinds, c
   int nl = 0;
   rc = enqueue_turn(p, b, b->stream, plan, true, false, &nl);
   int rc2 = prof_collect(prof, max_kinds, names, total_ms, launches, nkinds);
-  for (auto c : p->calcs) c->last_stream = b->stream;
+  for (auto c : p->calcs) ORBIT_CUDA(sc_mark_used(c, b->stream));
   for (double a : p->time_adv)
     if (a != 0.0) b->sync.time = b->sync.time + a;
   if (rc) return rc;

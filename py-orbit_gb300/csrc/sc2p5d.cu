@@ -714,9 +714,18 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
     ++nl;
     ORBIT_LAUNCH_CHECK("sc2p5d kick");
   }
-  c->last_stream = s;
+
   if (launches) *launches += nl;
   return ORBIT_OK;
+}
+
+cudaError_t sc_order_before(orbit_sc2p5d_t* c, cudaStream_t s) {
+  return c->used ? cudaStreamWaitEvent(s, c->done, 0) : cudaSuccess;
+}
+
+cudaError_t sc_mark_used(orbit_sc2p5d_t* c, cudaStream_t s) {
+  c->used = true;
+  return cudaEventRecord(c->done, s);
 }
 
 static int init_attrs(orbit_sc2p5d_t* c) {
@@ -770,6 +779,7 @@ int orbit_sc2p5d_create(orbit_sc2p5d_t** out, int nx, int ny, int nz, double xy_
     if (e == cudaSuccess) e = cudaMalloc(p, bytes);
     if (e == cudaSuccess) e = cudaMemset(*p, 0, bytes);
   };
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->done, cudaEventDisableTiming);
   A((void**)&c->d_st, sizeof(ScState));
   A((void**)&c->d_rho, sizeof(double) * ng);
   A((void**)&c->d_phi, sizeof(double) * ng);
@@ -828,7 +838,8 @@ int orbit_sc2p5d_create(orbit_sc2p5d_t** out, int nx, int ny, int nz, double xy_
 
 int orbit_sc2p5d_destroy(orbit_sc2p5d_t* c) {
   if (!c) return ORBIT_OK;
-  if (c->last_stream) cudaStreamSynchronize(c->last_stream);
+  if (c->used) cudaEventSynchronize(c->done);
+  if (c->done) cudaEventDestroy(c->done);
   void* ptrs[] = {c->d_st, c->d_rho_q, c->d_z_q, c->d_rho_f, c->d_z_f, c->d_rho, c->d_phi, c->d_lam,
                   c->d_phi_f, c->d_lam_f, c->d_hat, c->d_green, c->d_gbuf, c->d_tw_x, c->d_tw_y};
   for (void* p : ptrs)
@@ -840,16 +851,16 @@ int orbit_sc2p5d_destroy(orbit_sc2p5d_t* c) {
 int orbit_sc2p5d_track(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length) {
   if (!c || !b) return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_track: null handle");
   if (b->n < 2) return ORBIT_OK;  // SpaceChargeCalc2p5D.cc:79-80
-  if (c->last_stream && c->last_stream != b->stream) {
-    // the calculator's buffers were last used on another bunch's stream
-    ORBIT_CUDA(cudaStreamSynchronize(c->last_stream));
-  }
-  return sc_enqueue_kick(c, b, length, b->stream, true, true, nullptr);
+  ORBIT_CUDA(sc_order_before(c, b->stream));
+  int rc = sc_enqueue_kick(c, b, length, b->stream, true, true, nullptr);
+  if (rc) return rc;
+  ORBIT_CUDA(sc_mark_used(c, b->stream));
+  return ORBIT_OK;
 }
 
 int orbit_sc2p5d_get_grid(orbit_sc2p5d_t* c, int which, double* host_out) {
   if (!c || !host_out) return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_get_grid: bad argument");
-  if (c->last_stream) ORBIT_CUDA(cudaStreamSynchronize(c->last_stream));
+  if (c->used) ORBIT_CUDA(cudaEventSynchronize(c->done));
   size_t ng = (size_t)c->nx * c->ny;
   if (which == ORBIT_GRID_RHO) ORBIT_CUDA(cudaMemcpy(host_out, c->d_rho, sizeof(double) * ng, cudaMemcpyDeviceToHost));
   else if (which == ORBIT_GRID_PHI) ORBIT_CUDA(cudaMemcpy(host_out, c->d_phi, sizeof(double) * ng, cudaMemcpyDeviceToHost));
@@ -860,7 +871,7 @@ int orbit_sc2p5d_get_grid(orbit_sc2p5d_t* c, int which, double* host_out) {
 
 int orbit_sc2p5d_get_limits(orbit_sc2p5d_t* c, double* lim) {
   if (!c || !lim) return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_get_limits: bad argument");
-  if (c->last_stream) ORBIT_CUDA(cudaStreamSynchronize(c->last_stream));
+  if (c->used) ORBIT_CUDA(cudaEventSynchronize(c->done));
   ScState h;
   ORBIT_CUDA(cudaMemcpy(&h, c->d_st, sizeof(h), cudaMemcpyDeviceToHost));
   lim[0] = h.xmin; lim[1] = h.xmax; lim[2] = h.ymin; lim[3] = h.ymax; lim[4] = h.zmin; lim[5] = h.zmax;
@@ -882,7 +893,7 @@ int orbit_sc2p5d_fields(orbit_sc2p5d_t* c, int n, const double* x, const double*
   if (!c || n < 0 || (n > 0 && (!x || !y || !z || !ex || !ey || !lam)))
     return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_fields: bad argument");
   if (n == 0) return ORBIT_OK;
-  if (c->last_stream) ORBIT_CUDA(cudaStreamSynchronize(c->last_stream));
+  if (c->used) ORBIT_CUDA(cudaEventSynchronize(c->done));
   double* d = nullptr;
   ORBIT_CUDA(cudaMalloc(&d, sizeof(double) * 6 * (size_t)n));
   cudaError_t e = cudaMemcpy(d, x, sizeof(double) * n, cudaMemcpyHostToDevice);

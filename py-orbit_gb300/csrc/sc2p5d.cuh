@@ -53,7 +53,8 @@ struct orbit_sc2p5d {
   void* d_tw_x = nullptr;                 // twiddles for N = nx2
   void* d_tw_y = nullptr;                 // twiddles for N = ny2
   orbit::FftPlan plan_x{}, plan_y{};
-  cudaStream_t last_stream = nullptr;
+  cudaEvent_t done = nullptr;    // recorded after the last work that used the buffers
+  bool used = false;
   bool smem_deposit = false, smem_kick = false;
   int dep_threads = 512, kick_threads = 512;
 };
@@ -66,6 +67,10 @@ namespace orbit {
 // pass.  Returns the number of kernel launches added through *launches.
 int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStream_t st,
                     bool do_extrema, bool do_kick, int* launches);
+// Cross-stream ordering of a calculator's buffers: work on stream s waits
+// for the last recorded use, then records a new one.
+cudaError_t sc_order_before(orbit_sc2p5d_t* c, cudaStream_t s);
+cudaError_t sc_mark_used(orbit_sc2p5d_t* c, cudaStream_t s);
 // Kick factor 2 L r_c / (beta^2 gamma^3) computed on the host exactly as
 // SpaceChargeCalc2p5D.cc:96 does (libm pow).
 double sc_host_factor(const orbit_sync_t& s, double length);
