@@ -227,25 +227,27 @@ __device__ __forceinline__ void apply_ops(Part& p, const DevOp* __restrict__ ops
         if (o.c[2] != 0.) { p.dE += o.c[2]; p.knl_ok = false; }
         break;
       case ORBIT_OP_WEDGEROT: {  // wedgerotate (teapotbase.cc:923-967); c0 = cos, c1 = sin, i0 = frinout
+        // dE = (p0 - 1)/coeff cancels, so this rare map keeps the
+        // reference's unfused rounding (explicit _rn operations).
         double cs = o.c[0], sn = o.c[1], dp_p;
         double dpc = m.dp_p_coeff;
         if (o.i0 == 0) {
-          dp_p = p.dE * dpc;
-          double xp_t = p.xp, p0_t = 1.0 + dp_p;
+          dp_p = __dmul_rn(p.dE, dpc);
+          double xp_t = p.xp, p0_t = __dadd_rn(1.0, dp_p);
           p.x /= cs;
-          p.xp = xp_t * cs + p0_t * sn;
-          double p0 = -xp_t * sn + p0_t * cs;
-          dp_p = p0 - 1.0;
-          p.z = (-p.x * sn + p.z) * cs;
+          p.xp = __dadd_rn(__dmul_rn(xp_t, cs), __dmul_rn(p0_t, sn));
+          double p0 = __dadd_rn(__dmul_rn(-xp_t, sn), __dmul_rn(p0_t, cs));
+          dp_p = __dsub_rn(p0, 1.0);
+          p.z = __dmul_rn(__dadd_rn(__dmul_rn(-p.x, sn), p.z), cs);
         } else {
-          dp_p = p.dE * dpc;
-          double p0 = 1.0 + dp_p;
-          p.z = p.x * sn + p.z / cs;
-          p.x *= cs;
-          double xp_t = p.xp * cs - p0 * sn;
-          double p0_t = p.xp * sn + p0 * cs;
+          dp_p = __dmul_rn(p.dE, dpc);
+          double p0 = __dadd_rn(1.0, dp_p);
+          p.z = __dadd_rn(__dmul_rn(p.x, sn), p.z / cs);
+          p.x = __dmul_rn(p.x, cs);
+          double xp_t = __dsub_rn(__dmul_rn(p.xp, cs), __dmul_rn(p0, sn));
+          double p0_t = __dadd_rn(__dmul_rn(p.xp, sn), __dmul_rn(p0, cs));
           p.xp = xp_t;
-          dp_p = p0_t - 1.0;
+          dp_p = __dsub_rn(p0_t, 1.0);
         }
         p.dE = dp_p / dpc;
         p.knl_ok = false;

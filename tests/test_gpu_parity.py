@@ -41,7 +41,7 @@ def test_maps_against_golden():
         getattr(TPB, name)(b, *args)
         got = b.getCoordinates()
         err = coord_err(got, g["after_%02d" % k])
-        assert err <= 1e-13, (k, name, err)
+        assert err <= TOL_FIELD, (k, name, err)
     assert abs(b.getSyncParticle().time() - g["kin"][6]) <= 1e-15 * abs(g["kin"][6])
 
 
