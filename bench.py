@@ -37,8 +37,9 @@ CELLS = 40
 METRIC = "2.5D SC macroparticle-kicks/s, 1M particles 128x128 grid, vs FP64 plain form"
 CPU_SAMPLE_N = 250_000
 
-# Algorithmic work per particle for the roofline (counted from the restated
-# formulas): HBM bytes of each particle kernel.
+# Algorithmic HBM bytes per particle of each particle kernel: the fused pass
+# reads and writes x, xp, y, yp, z, dE; the deposit and the extrema scan
+# read x, y, z; the stand-alone kick reads x, y, z, xp, yp and writes xp, yp.
 ALG_BYTES = {"pass_kick_maps": 96, "pass_maps": 96, "deposit": 24, "extrema": 24, "kick": 56}
 
 
@@ -75,9 +76,34 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-# FP64 FMA throughput measured on this machine's GB300 with a DFMA-chain kernel
-# (profiles/fp64_pipe_peak.md): 593 G DFMA/s = 1.186 TFLOP/s.
-FP64_PEAK_TFLOPS = 1.186
+# Algorithmic FP64 operations per particle, counted from the reference
+# formulas (each +, -, *, / is one operation; per-element constants that the
+# reference computes once per call are not counted):
+#   SC kick (SpaceChargeCalc2p5D.cc:104-119 with Grid2D::calcGradient and
+#   Grid1D::getValue): indices and fractions 14, weights 16, derivative
+#   weights 12, two 9-point sums 54, line density 12, factor 1, kicks 4 = 113
+#   deposit (Grid2D::binValue + Grid1D::binValue): 14 + 16 + 27 + 12 = 69
+#   maps (teapotbase.cc): drift 22, quad1 16, quad2/bend2 25, quad fringe 70,
+#   bend1 18, bend3 20, bend4 14, bend fringe 16, multp 4 + 3 per pole,
+#   rotatexy 12, wrap 2, kick 3
+SC_KICK_FLOPS = 113
+DEPOSIT_FLOPS = 69
+MAP_FLOPS = {1: 22, 2: 16, 3: 25, 4: 70, 5: 70, 6: 18, 7: 25, 8: 20, 9: 14, 10: 16, 11: 16, 12: 7, 13: 60,
+             14: 60, 15: 12, 16: 2, 17: 3, 18: 20, 19: 30, 20: 60}
+
+
+def pass_flops_per_turn(ops):
+    """FP64 operations per particle of all fused passes of one turn."""
+    total = 0
+    for code, ints, dbls in ops:
+        if code == 32:
+            total += SC_KICK_FLOPS
+        else:
+            f = MAP_FLOPS.get(code, 0)
+            if code == 12 and ints:
+                f = 4 + 3 * int(ints[0])
+            total += f
+    return total
 
 
 class ClockSampler:
@@ -218,6 +244,7 @@ def run_ours(args):
     os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("CUDA_VISIBLE_DEVICES", ""))
     torch.cuda.init()
     n = args.n
+    TRAFFIC.n = n
     soa, bunch, calc, lat = build_workload(n, args.form, seed=1000 + rank)
     prog = lat.fusedProgram(bunch)
     dev = bunch._device_bunch()
@@ -230,6 +257,8 @@ def run_ours(args):
     # per-kernel times of one eager turn (CUDA events on the bunch's stream)
     prof = prog.device.profile(dev)
     bunch._device_modified()
+    from orbit_gb300 import device_peaks
+    fp64_peak, copy_gbs = device_peaks()
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     def barrier():
@@ -307,12 +336,19 @@ def run_ours(args):
                 else "fallback 6.8 TB/s",
                 "kernel_ms_per_launch": per_launch_ms, "share_of_turn": dom_ms / turn_ms,
                 "kernels": {k: {"ms": v[0], "launches": v[1], "share": v[0] / turn_ms} for k, v in prof.items()}}
-    fl = FP64_OPS.get((args.form, name))
-    if fl:
-        tf = fl * n / (per_launch_ms * 1e-3) / 1e12
-        roofline["fp64_pipe"] = {"achieved_tflops": tf, "peak_tflops": FP64_PEAK_TFLOPS, "frac": tf / FP64_PEAK_TFLOPS,
-                                 "fp64_ops_per_particle": fl,
-                                 "peak_source": "measured DFMA-chain peak, profiles/fp64_pipe_peak.md"}
+    if args.form == "plain":
+        # the plain form is bound by the FP64 pipe: algorithmic FP64 rate of
+        # the fused passes and of the deposit against the live DFMA peak
+        pass_ms = sum(v[0] for k, v in prof.items() if k.startswith("pass"))
+        pf = pass_flops_per_turn(prog.ops) * n
+        dep_ms, dep_l = prof.get("deposit", (0.0, 1))
+        roofline["fp64_pipe"] = {
+            "peak_tflops": fp64_peak, "peak_source": "measured in this run (orbit_device_peaks: DFMA chains)",
+            "pass_achieved_tflops": pf / (pass_ms * 1e-3) / 1e12,
+            "pass_frac": pf / (pass_ms * 1e-3) / 1e12 / fp64_peak,
+            "deposit_achieved_tflops": DEPOSIT_FLOPS * n * dep_l / (dep_ms * 1e-3) / 1e12,
+            "deposit_frac": DEPOSIT_FLOPS * n * dep_l / (dep_ms * 1e-3) / 1e12 / fp64_peak,
+            "flops_per_particle_turn": pass_flops_per_turn(prog.ops) + DEPOSIT_FLOPS * kicks_per_turn}
     cpu = None
     if not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -337,12 +373,21 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-# DRAM traffic per launch from ncu (dram__bytes_read.sum + dram__bytes_write.sum),
-# filled from the committed summaries under profiles/ once captured.
-TRAFFIC = {}
-# FP64-pipe operations per particle for the fused pass and deposit kernels of
-# the plain form, counted from the restated formulas.
-FP64_OPS = {}
+# DRAM traffic per particle per launch, dram__bytes_read.sum +
+# dram__bytes_write.sum from one ncu capture of a 4e6-particle run of this
+# benchmark (bunch larger than L2); scaled to the bench's particle count.
+TRAFFIC_PER_PARTICLE = {("plain", "pass_kick_maps"): 80.57, ("plain", "deposit"): 24.66}
+
+
+class _Traffic(dict):
+    n = N_PARTICLES
+
+    def get(self, key, default=None):
+        v = TRAFFIC_PER_PARTICLE.get(key)
+        return None if v is None else v * self.n
+
+
+TRAFFIC = _Traffic()
 
 
 def main():

@@ -45,6 +45,11 @@ int orbit_last_error(char* buf, int len);
 /* Library version string, e.g. "orbit_gb300 0.1 sm_103a". */
 const char* orbit_version(void);
 
+/* Measures this GPU's FP64 FMA throughput (TFLOP/s, independent DFMA
+ * chains) and streaming copy bandwidth (GB/s, read + write), the roofs the
+ * benchmark reports against.  No counterpart in the reference. */
+int orbit_device_peaks(double* fp64_tflops, double* copy_gbs);
+
 /* ------------------------------------------------------------------ */
 /* Bunch: device-resident SoA macroparticle container                 */
 /* replaces Bunch (src/orbit/Bunch.hh:60-136, AoS double[6] rows) and  */

@@ -191,7 +191,14 @@ _ref = None
 
 
 def ref_available() -> bool:
-    return os.path.exists(REF_SO)
+    """True where the compiled reference exists and loads on this host."""
+    if not os.path.exists(REF_SO):
+        return False
+    try:
+        ref()
+    except OSError:
+        return False
+    return True
 
 
 def ref():

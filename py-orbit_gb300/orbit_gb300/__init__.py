@@ -25,6 +25,13 @@ def version() -> str:
     return load().orbit_version().decode()
 
 
+def device_peaks():
+    """(FP64 FMA TFLOP/s, copy GB/s) measured on the current GPU."""
+    f, g = ctypes.c_double(), ctypes.c_double()
+    call("orbit_device_peaks", ctypes.byref(f), ctypes.byref(g))
+    return f.value, g.value
+
+
 def _ptr_array(arrs):
     return (_dp * 6)(*[a.ctypes.data_as(_dp) for a in arrs])
 

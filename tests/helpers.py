@@ -7,7 +7,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, "golden")
 
-# the benchmark spec tolerances (max-norm relative): potential and kicks 1e-12,
+# Required parity (max-norm relative): potential and kicks 1e-12,
 # coordinates after 100 kicks 1e-10.
 TOL_FIELD = 1e-12
 TOL_COORD = 1e-10
