@@ -115,6 +115,25 @@ int orbit_sc2p5d_get_sizes(const orbit_sc2p5d_t* c, int* nx, int* ny, int* nz, i
 int orbit_sc2p5d_fields(orbit_sc2p5d_t* c, int n, const double* x, const double* y, const double* z,
                         double* ex, double* ey, double* lam);
 
+/* No counterpart in the reference.  One trackBunch of a freshly constructed
+ * plain FP64 calculator (the result of orbit_sc2p5d_create + _track on the
+ * same inputs) that allocates nothing: for callers that cannot call
+ * cudaMalloc -- code running inside another framework's memory pool or
+ * under a fixed memory budget, loops that must not allocate after start-up,
+ * hosts that cannot afford the device synchronisation an allocation or free
+ * can cause.  All scratch (solver state, grids, FFT spectra, Green
+ * function) lives in one static device array of about 2.1 MB that every GPU
+ * loading the library holds until the process exits; grids are limited to
+ * nx, ny <= 128 and nz <= 256 (larger sizes return ORBIT_ERR_UNSUPPORTED).
+ * dev_coords: device SoA, coordinate c (x, xp, y, yp, z, dE) at
+ * dev_coords + c*stride, stride >= n; xp and yp are updated in place.
+ * stream: a cudaStream_t (NULL = default stream); the call waits for it.
+ * The first call on a device looks up the array's device address, so make
+ * that first call before any stream capture.  Calls share the array:
+ * calls that overlap on the GPU race. */
+int orbit_sc2p5d_track_static(double* dev_coords, int n, int stride, int nx, int ny, int nz, double xy_ratio,
+                              double length, const orbit_sync_t* sync, void* stream);
+
 /* ------------------------------------------------------------------ */
 /* teapot_base maps (src/teapot/teapotbase.cc; Python names in         */
 /* src/teapot/wrap_teapotbase.cc:488-512).  The useCharge argument of  */

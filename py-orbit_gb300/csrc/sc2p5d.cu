@@ -913,3 +913,154 @@ int orbit_sc2p5d_fields(orbit_sc2p5d_t* c, int n, const double* x, const double*
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------
+// No-allocation variant of trackBunch.
+//
+// Some callers cannot allocate device memory: code that runs inside another
+// framework's memory pool or arena (where a cudaMalloc would bypass its
+// accounting or fail under a fixed budget), real-time or embedded loops
+// that must not allocate after start-up, and hosts that forbid the implicit
+// device synchronisation a cudaMalloc/cudaFree can cause.  For them
+// orbit_sc2p5d_track_static runs one kick of a freshly constructed plain
+// FP64 calculator with every scratch buffer (solver state, fixed-point
+// grids, potential, FFT spectra, Green function, twiddles, status word)
+// carved from one file-scope __device__ array of kStaticScratchBytes.
+// ---------------------------------------------------------------------
+namespace orbit {
+
+static const int kStaticMaxNxy = 128;  // nx, ny <= 128
+static const int kStaticMaxNz = 256;   // nz <= 256
+
+static constexpr size_t al256(size_t v) { return (v + 255) & ~(size_t)255; }
+static constexpr size_t kStaticScratchBytes =
+    al256(sizeof(ScState)) + al256(sizeof(unsigned)) +                              // state, status
+    al256(8ull * kStaticMaxNxy * kStaticMaxNxy) + al256(8ull * kStaticMaxNz) +       // fixed-point grids
+    2 * al256(8ull * kStaticMaxNxy * kStaticMaxNxy) + al256(8ull * kStaticMaxNz) +   // rho, phi, lambda
+    2 * al256(16ull * 2 * kStaticMaxNxy * (kStaticMaxNxy + 1)) +                     // spectrum, Green spectrum
+    al256(8ull * 4 * kStaticMaxNxy * kStaticMaxNxy) +                                // Green function
+    2 * al256(16ull * 2 * kStaticMaxNxy);                                            // twiddles x, y
+
+// Held by every GPU that loads the library, until the process exits
+// (about 2.1 MB).  Shared by all calls: calls that overlap on the GPU race.
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+static unsigned char* g_static_ptr[256];  // device address per device ordinal, set up once
+
+static int static_scratch_ptr(unsigned char** out) {
+  int dev = 0;
+  ORBIT_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 256) return set_error(ORBIT_ERR_UNSUPPORTED, "orbit_sc2p5d_track_static: device ordinal");
+  if (!g_static_ptr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (e != cudaSuccess) return cuda_error(e, "orbit_sc2p5d_track_static: cudaGetSymbolAddress");
+    g_static_ptr[dev] = (unsigned char*)p;
+  }
+  *out = g_static_ptr[dev];
+  return ORBIT_OK;
+}
+
+template <typename T>
+static void fill_twiddles_host(int n, typename CT<T>::t* h) {
+  for (int e = 0; e < n; ++e) {
+    long double a = 2.0L * 3.141592653589793238462643383279502884L * (long double)e / (long double)n;
+    h[e].x = (T)cosl(a);
+    h[e].y = (T)(-sinl(a));
+  }
+  if (n % 4 == 0) {
+    h[0].x = 1; h[0].y = 0;
+    h[n / 4].x = 0; h[n / 4].y = -1;
+    h[n / 2].x = -1; h[n / 2].y = 0;
+    h[3 * n / 4].x = 0; h[3 * n / 4].y = 1;
+  } else if (n % 2 == 0) {
+    h[n / 2].x = -1; h[n / 2].y = 0;
+  }
+}
+
+}  // namespace orbit
+
+extern "C" int orbit_sc2p5d_track_static(double* dev_coords, int n, int stride, int nx, int ny, int nz,
+                                         double xy_ratio, double length, const orbit_sync_t* sync, void* stream) {
+  using namespace orbit;
+  if (!sync || n < 0 || (n > 0 && (!dev_coords || stride < n)))
+    return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_track_static: bad argument");
+  if (nx < 3 || ny < 3) return set_error(ORBIT_ERR_GRID, "Grid2D: the grid size too small (should be more than 3)");
+  if (nz < 1) return set_error(ORBIT_ERR_GRID, "Grid1D: the grid size is too small (should be more than 0)");
+  if (nx > kStaticMaxNxy || ny > kStaticMaxNxy || nz > kStaticMaxNz)
+    return set_error(ORBIT_ERR_UNSUPPORTED,
+                     "orbit_sc2p5d_track_static: grid above the static scratch limit (nx, ny <= 128, nz <= 256)");
+  orbit_sc2p5d_t c;
+  c.nx = nx; c.ny = ny; c.nz = nz; c.form = ORBIT_FORM_PLAIN;
+  c.nx2 = 2 * nx; c.ny2 = 2 * ny; c.H = ny + 1;
+  c.xy_ratio0 = xy_ratio > 0. ? xy_ratio : 1.0;
+  if (!make_fft_plan(c.nx2, c.plan_x) || !make_fft_plan(c.ny2, c.plan_y))
+    return set_error(ORBIT_ERR_UNSUPPORTED, "orbit_sc2p5d_track_static: grid sizes must have no prime factor above 13");
+  if (n < 2) return ORBIT_OK;  // SpaceChargeCalc2p5D.cc:79-80
+  unsigned char* base = nullptr;
+  int rc = static_scratch_ptr(&base);
+  if (rc) return rc;
+  // carve the buffers
+  size_t off = 0;
+  auto take = [&](size_t bytes) { unsigned char* p = base + off; off += al256(bytes); return (void*)p; };
+  size_t ng = (size_t)nx * ny, nhat = (size_t)c.nx2 * c.H;
+  c.d_st = (ScState*)take(sizeof(ScState));
+  unsigned* d_status = (unsigned*)take(sizeof(unsigned));
+  c.d_rho_q = (unsigned long long*)take(8 * ng);
+  c.d_z_q = (unsigned long long*)take(8 * (size_t)nz);
+  c.d_rho = (double*)take(8 * ng);
+  c.d_phi = (double*)take(8 * ng);
+  c.d_lam = (double*)take(8 * (size_t)nz);
+  c.d_hat = take(16 * nhat);
+  c.d_green = take(16 * nhat);
+  c.d_gbuf = (double*)take(8 * (size_t)c.nx2 * c.ny2);
+  c.d_tw_x = take(16 * (size_t)c.nx2);
+  c.d_tw_y = take(16 * (size_t)c.ny2);
+  if (off > kStaticScratchBytes) return set_error(ORBIT_ERR_DEVICE, "orbit_sc2p5d_track_static: scratch layout");
+  cudaStream_t s = (cudaStream_t)stream;
+  // state of a freshly constructed calculator (SpaceChargeCalc2p5D.cc:25-43);
+  // everything else is fully written by the kernels before it is read
+  ScState h;
+  std::memset(&h, 0, sizeof(h));
+  double r = c.xy_ratio0;
+  h.xy_ratio = r;
+  h.sxmin = -r; h.sxmax = r; h.symin = -1.0; h.symax = 1.0;
+  h.sdx = (r - (-r)) / (nx - 1);
+  h.sdy = (1.0 - (-1.0)) / (ny - 1);
+  h.xmin = -1.0; h.xmax = 1.0; h.ymin = -1.0; h.ymax = 1.0;
+  h.dx = 2.0 / (nx - 1); h.dy = 2.0 / (ny - 1); h.inv_dx = 1.0 / h.dx; h.inv_dy = 1.0 / h.dy;
+  h.zmin = -0.5; h.zmax = 0.5; h.dz = 1.0 / nz; h.inv_dz = 1.0 / h.dz;
+  h.green_dirty = 1;
+  for (int k = 0; k < 3; ++k) { h.key[2 * k] = ~0ull; h.key[2 * k + 1] = 0ull; }
+  double2 twx[2 * kStaticMaxNxy], twy[2 * kStaticMaxNxy];
+  fill_twiddles_host<double>(c.nx2, twx);
+  fill_twiddles_host<double>(c.ny2, twy);
+  ORBIT_CUDA(cudaMemcpyAsync(c.d_st, &h, sizeof(h), cudaMemcpyHostToDevice, s));
+  ORBIT_CUDA(cudaMemsetAsync(d_status, 0, sizeof(unsigned), s));
+  ORBIT_CUDA(cudaMemcpyAsync(c.d_tw_x, twx, sizeof(double2) * c.nx2, cudaMemcpyHostToDevice, s));
+  ORBIT_CUDA(cudaMemcpyAsync(c.d_tw_y, twy, sizeof(double2) * c.ny2, cudaMemcpyHostToDevice, s));
+  rc = init_attrs(&c);
+  if (rc) return rc;
+  orbit_bunch_t b;
+  b.n = n;
+  b.cap = stride;
+  b.d_coords = dev_coords;
+  b.d_status = d_status;
+  b.stream = s;
+  b.sync = *sync;
+  b.has_msize = 0;
+  rc = sc_enqueue_kick(&c, &b, length, s, true, true, nullptr);
+  b.d_coords = nullptr;  // the caller owns the coordinates
+  b.d_status = nullptr;
+  b.stream = nullptr;
+  if (rc) return rc;
+  unsigned st = 0;
+  ORBIT_CUDA(cudaMemcpyAsync(&st, d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  ORBIT_CUDA(cudaStreamSynchronize(s));
+  if (st & ST_NAN) return set_error(ORBIT_ERR_NAN, "non-finite particle coordinate found by the extrema scan");
+  if (st & ST_EXTENT)
+    return set_error(ORBIT_ERR_EXTENT,
+                     "SpaceChargeCalc2p5D: the bunch min and max sizes are wrong (zero extent); kick skipped");
+  if (st) return set_error(ORBIT_ERR_DEVICE, "device-side range check failed");
+  return ORBIT_OK;
+}

@@ -82,6 +82,9 @@ _SIGS = {
     "orbit_sc2p5d_get_limits": (ctypes.c_int, [_vp, _dp]),
     "orbit_sc2p5d_get_sizes": (ctypes.c_int, [_vp] + [ctypes.POINTER(ctypes.c_int)] * 4),
     "orbit_sc2p5d_fields": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _dp]),
+    "orbit_sc2p5d_track_static": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                 ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                                 ctypes.POINTER(Sync), _vp]),
     "orbit_program_create": (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.POINTER(Op), ctypes.c_int,
                                             ctypes.POINTER(_vp), ctypes.c_int]),
     "orbit_program_destroy": (ctypes.c_int, [_vp]),
