@@ -21,7 +21,7 @@ __global__ void k_dfma_chain(double* out, int iters, double a, double b) {
   if (s == 123456.789) out[0] = s;  // keeps the chains alive
 }
 
-__global__ void k_copy(const double4* __restrict__ a, double4* __restrict__ b, size_t n) {
+__global__ void k_copy(const double2* __restrict__ a, double2* __restrict__ b, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     b[i] = a[i];
 }
@@ -52,11 +52,11 @@ extern "C" int orbit_device_peaks(double* fp64_tflops, double* copy_gbs) {
   }
   *fp64_tflops = 2.0 * 8.0 * (double)blocks * threads * iters / (best * 1e-3) / 1e12;
   cudaFree(out);
-  size_t n = (size_t)1 << 25;  // 32 Mi double4 = 1 GiB per buffer
-  double4 *a = nullptr, *b = nullptr;
-  cudaError_t e = cudaMalloc(&a, n * sizeof(double4));
-  if (e == cudaSuccess) e = cudaMalloc(&b, n * sizeof(double4));
-  if (e == cudaSuccess) e = cudaMemset(a, 0, n * sizeof(double4));
+  size_t n = (size_t)1 << 26;  // 64 Mi double2 = 1 GiB per buffer
+  double2 *a = nullptr, *b = nullptr;
+  cudaError_t e = cudaMalloc(&a, n * sizeof(double2));
+  if (e == cudaSuccess) e = cudaMalloc(&b, n * sizeof(double2));
+  if (e == cudaSuccess) e = cudaMemset(a, 0, n * sizeof(double2));
   if (e != cudaSuccess) {
     if (a) cudaFree(a);
     if (b) cudaFree(b);
@@ -74,7 +74,7 @@ extern "C" int orbit_device_peaks(double* fp64_tflops, double* copy_gbs) {
     cudaEventElapsedTime(&ms, e0, e1);
     if (rep > 0 && ms < best) best = ms;
   }
-  *copy_gbs = 2.0 * n * sizeof(double4) / (best * 1e-3) / 1e9;
+  *copy_gbs = 2.0 * n * sizeof(double2) / (best * 1e-3) / 1e9;
   cudaFree(a);
   cudaFree(b);
   cudaEventDestroy(e0);

@@ -30,19 +30,21 @@ __global__ void __launch_bounds__(512) k_pass(double* __restrict__ cx, double* _
                                               const DevOp* __restrict__ ops, int a, int b, MapCtx m,
                                               KickArgs kick, ScState* ext_st, unsigned* status) {
   KickConst k;
-  const double* P = kick.phi;
-  const double* Lm = kick.lam;
+  KickFix kf;
+  const long long* P = kick.phi_fix;
+  const long long* Lm = kick.lam_fix;
   const float* Pf = kick.phi_f;
   const float* Lf = kick.lam_f;
   extern __shared__ unsigned char s_raw[];
   if (KF != 0) {
     load_kick_const(k, kick.st, kick.host_factor, kick.nx, kick.ny, kick.nz);
+    if (KF == 1) load_kick_fix(kf, kick.st, kick.host_factor, kick.nx, kick.ny, kick.nz);
     if (KSMEM) {
       int ng = kick.nx * kick.ny;
       if (KF == 1) {
-        double* s = reinterpret_cast<double*>(s_raw);
-        for (int i = threadIdx.x; i < ng; i += blockDim.x) s[i] = kick.phi[i];
-        for (int i = threadIdx.x; i < kick.nz; i += blockDim.x) s[ng + i] = kick.lam[i];
+        long long* s = reinterpret_cast<long long*>(s_raw);
+        for (int i = threadIdx.x; i < ng; i += blockDim.x) s[i] = kick.phi_fix[i];
+        for (int i = threadIdx.x; i < kick.nz; i += blockDim.x) s[ng + i] = kick.lam_fix[i];
         P = s;
         Lm = s + ng;
       } else {
@@ -61,7 +63,8 @@ __global__ void __launch_bounds__(512) k_pass(double* __restrict__ cx, double* _
     Part p;
     p.x = cx[i]; p.xp = cxp[i]; p.y = cy[i]; p.yp = cyp[i]; p.z = cz[i]; p.dE = cdE[i];
     p.knl_ok = false;
-    if (KF == 1 && !k.skip) kick_plain(k, P, Lm, p.x, p.y, p.z, p.xp, p.yp);
+    if (KF == 1 && !k.skip && !kick_fixed(kf, P, Lm, p.x, p.y, p.z, p.xp, p.yp))
+      kick_plain(k, kick.phi, kick.lam, p.x, p.y, p.z, p.xp, p.yp);
     if (KF == 2 && !k.skip) kick_fp32(k, Pf, Lf, p.x, p.y, p.z, p.xp, p.yp);
     apply_ops(p, ops, a, b, m);
     if (EXT) acc.add(p.x, p.y, p.z);
@@ -154,6 +157,8 @@ static KickArgs kick_args(orbit_sc2p5d_t* c, const orbit_sync_t& s, double lengt
   ka.lam = c->d_lam;
   ka.phi_f = c->d_phi_f;
   ka.lam_f = c->d_lam_f;
+  ka.phi_fix = c->d_phi_fix;
+  ka.lam_fix = c->d_lam_fix;
   ka.host_factor = sc_host_factor(s, length);
   ka.nx = c->nx; ka.ny = c->ny; ka.nz = c->nz; ka.form = c->form;
   return ka;

@@ -103,6 +103,8 @@ __global__ void k_setup(ScState* st, unsigned* status, int nx, int ny, int nz, d
       }
       st->scale = log(__ddiv_rn(st->sdx, dx));  // PoissonSolverFFT2D.cc:213
       st->inv_qscale = inv_qscale;
+      st->phi_absmax = 0ull;
+      st->lam_absmax = 0ull;
     }
     st->skip = skip;
     s_skip = skip;
@@ -254,7 +256,7 @@ __global__ void k_cols(const ScState* st, typename CT<T>::t* hat, const typename
 // normalisation onto the nx x ny potential (PoissonSolverFFT2D.cc:244-255).
 // Imaginary parts at the self-conjugate k = 0 and k = N/2 are ignored.
 template <typename T>
-__global__ void k_rows_inv(const ScState* st, const typename CT<T>::t* __restrict__ hat,
+__global__ void k_rows_inv(ScState* st, const typename CT<T>::t* __restrict__ hat,
                            const typename CT<T>::t* __restrict__ tw, FftPlan pl, int nrows, int ny, int H,
                            double denom, double* phi, float* phi_f) {
   typedef typename CT<T>::t C;
@@ -282,16 +284,38 @@ __global__ void k_rows_inv(const ScState* st, const typename CT<T>::t* __restric
   }
   __syncthreads();
   C* R = block_fft<T>(a, b, pl, tw, true);
+  unsigned long long amax = 0ull;  // bits of max |phi| (non-negative doubles order like their bits)
   for (int j = threadIdx.x; j < ny; j += blockDim.x) {
     double va = denom * (double)R[j].x;
     phi[(size_t)r0 * ny + j] = va;
     if (phi_f) phi_f[(size_t)r0 * ny + j] = (float)va;
+    unsigned long long ba = (unsigned long long)__double_as_longlong(fabs(va));
+    amax = ba > amax ? ba : amax;
     if (has1) {
       double vb = denom * (double)R[j].y;
       phi[(size_t)r1 * ny + j] = vb;
       if (phi_f) phi_f[(size_t)r1 * ny + j] = (float)vb;
+      unsigned long long bb = (unsigned long long)__double_as_longlong(fabs(vb));
+      amax = bb > amax ? bb : amax;
     }
   }
+  for (int off = 16; off > 0; off >>= 1) {
+    unsigned long long o = __shfl_xor_sync(0xffffffffu, amax, off);
+    amax = o > amax ? o : amax;
+  }
+  if ((threadIdx.x & 31) == 0 && amax) atomicMax(&st->phi_absmax, amax);
+}
+
+// Plain form: phi and lambda as 64-bit integers phi * 2^sphi, lambda *
+// 2^slam with the scales chosen from their maxima (below 2^61), read by the
+// fixed-point kick.
+__global__ void k_phi_fix(const ScState* st, const double* __restrict__ phi, const double* __restrict__ lam,
+                          long long* phi_fix, long long* lam_fix, int ng, int nz) {
+  if (st->skip) return;
+  int sphi = scale_bits(st->phi_absmax), slam = scale_bits(st->lam_absmax);
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < ng) phi_fix[i] = phi_fixed(phi[i], sphi);
+  if (i < nz) lam_fix[i] = phi_fixed(lam[i], slam);
 }
 
 // Line density to doubles, total macrosize, and the Green-rebuild flag reset.
@@ -303,6 +327,7 @@ __global__ void k_finalize(ScState* st, const G* zacc, int nz, double* lam, floa
   double iq = st->inv_qscale;
   double acc = 0.0;
   long long iacc = 0;
+  unsigned long long amax = 0ull;
   for (int k = threadIdx.x; k < nz; k += blockDim.x) {
     double v;
     if (sizeof(G) == 8) {
@@ -315,7 +340,14 @@ __global__ void k_finalize(ScState* st, const G* zacc, int nz, double* lam, floa
     }
     lam[k] = v;
     if (lam_f) lam_f[k] = (float)v;
+    unsigned long long bv = (unsigned long long)__double_as_longlong(fabs(v));
+    amax = bv > amax ? bv : amax;
   }
+  for (int off = 16; off > 0; off >>= 1) {
+    unsigned long long o = __shfl_xor_sync(0xffffffffu, amax, off);
+    amax = o > amax ? o : amax;
+  }
+  if ((threadIdx.x & 31) == 0 && amax) atomicMax(&st->lam_absmax, amax);
   if (sizeof(G) == 8) {
     // exact integer sum, one rounding
     __shared__ long long s_i[32];
@@ -340,15 +372,20 @@ __global__ void k_finalize(ScState* st, const G* zacc, int nz, double* lam, floa
 }
 
 // Deposit, plain form.  SMEM: block-private fixed-point grids in shared
-// memory, flushed with one 64-bit atomic per non-zero cell.
+// memory, flushed with one 64-bit atomic per non-zero cell.  With K > 0
+// (uniform macrosize) each particle deposits unit weight in units of 2^-K
+// through the integer path (deposit_fixed); otherwise, and for the rare
+// particle the integer path declines, macrosize * qscale through FP64.
 template <bool SMEM>
 __global__ void k_deposit_plain(const double* __restrict__ x, const double* __restrict__ y,
                                 const double* __restrict__ z, const double* __restrict__ msize, int n,
                                 const ScState* st, unsigned long long* g_rho, unsigned long long* g_z,
-                                double ms_uniform, double qscale, int nx, int ny, int nz) {
+                                double ms_uniform, double qscale, int nx, int ny, int nz, int K) {
   DepConst d;
   load_dep_const(d, st, nx, ny, nz);
   if (d.skip) return;
+  DepFix df;
+  if (K > 0) load_dep_fix(df, st, nx, ny, nz, K);
   extern __shared__ unsigned long long s_acc[];
   unsigned long long* rho = g_rho;
   unsigned long long* zg = g_z;
@@ -359,8 +396,10 @@ __global__ void k_deposit_plain(const double* __restrict__ x, const double* __re
     __syncthreads();
   }
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double xi = x[i], yi = y[i], zi = z[i];
+    if (K > 0 && deposit_fixed(df, rho, zg, xi, yi, zi)) continue;
     double ms = msize ? msize[i] * qscale : ms_uniform;
-    deposit_plain(d, rho, zg, x[i], y[i], z[i], ms);
+    deposit_plain(d, rho, zg, xi, yi, zi, ms);
   }
   if (SMEM) {
     __syncthreads();
@@ -409,28 +448,33 @@ __global__ void k_deposit_fp32(const double* __restrict__ x, const double* __res
   }
 }
 
-// Kick (SpaceChargeCalc2p5D.cc:104-119).
+// Kick (SpaceChargeCalc2p5D.cc:104-119): fixed-point gradient and line
+// density (kick_fixed), FP64 routine for the particles it declines.
 template <bool SMEM>
 __global__ void k_kick_plain(const double* __restrict__ x, double* __restrict__ xp, const double* __restrict__ y,
                              double* __restrict__ yp, const double* __restrict__ z, int n, const ScState* st,
-                             const double* __restrict__ phi, const double* __restrict__ lam, double host_factor,
-                             int nx, int ny, int nz) {
+                             const double* __restrict__ phi, const double* __restrict__ lam,
+                             const long long* __restrict__ phi_fix, const long long* __restrict__ lam_fix,
+                             double host_factor, int nx, int ny, int nz) {
   KickConst k;
   load_kick_const(k, st, host_factor, nx, ny, nz);
   if (k.skip) return;
-  extern __shared__ double s_phi[];
-  const double* P = phi;
-  const double* Lm = lam;
+  KickFix kf;
+  load_kick_fix(kf, st, host_factor, nx, ny, nz);
+  extern __shared__ long long s_phix[];
+  const long long* P = phi_fix;
+  const long long* Lm = lam_fix;
   if (SMEM) {
-    for (int i = threadIdx.x; i < nx * ny; i += blockDim.x) s_phi[i] = phi[i];
-    for (int i = threadIdx.x; i < nz; i += blockDim.x) s_phi[nx * ny + i] = lam[i];
+    for (int i = threadIdx.x; i < nx * ny; i += blockDim.x) s_phix[i] = phi_fix[i];
+    for (int i = threadIdx.x; i < nz; i += blockDim.x) s_phix[nx * ny + i] = lam_fix[i];
     __syncthreads();
-    P = s_phi;
-    Lm = s_phi + nx * ny;
+    P = s_phix;
+    Lm = s_phix + nx * ny;
   }
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     double a = xp[i], b = yp[i];
-    kick_plain(k, P, Lm, x[i], y[i], z[i], a, b);
+    double xi = x[i], yi = y[i], zi = z[i];
+    if (!kick_fixed(kf, P, Lm, xi, yi, zi, a, b)) kick_plain(k, phi, lam, xi, yi, zi, a, b);
     xp[i] = a;
     yp[i] = b;
   }
@@ -636,14 +680,28 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
     ORBIT_PE(s);
     ++nl;
   }
-  // fixed-point scale from the total |macrosize|
-  double msum = b->has_msize ? b->msize_abs_sum : std::fabs(b->sync.macrosize) * (double)n;
-  double S = qscale_for(msum);
+  // Fixed-point units of the plain deposit.  Uniform macrosize: unit weight
+  // in units of 2^-K with 4 n 2^K < 2^62 (a particle's |weights| sum to at
+  // most 4), the macrosize multiplies the grid afterwards.  Per-particle
+  // macrosizes: macrosize * S with S * sum|m| <= 2^61.
   const double* msz = b->has_msize ? b->d_msize : nullptr;
   const bool plain = c->form == ORBIT_FORM_PLAIN;
+  int K = 0;
+  double S = 1.0, inv_q = 1.0, ms_uniform = 0.0;
+  if (!b->has_msize) {
+    int e = 0;
+    std::frexp(4.0 * (double)(n > 0 ? n : 1), &e);  // 4n < 2^e
+    K = 62 - e;
+    if (K > 55) K = 55;
+    ms_uniform = std::ldexp(1.0, K);
+    inv_q = std::ldexp(b->sync.macrosize, -K);
+  } else {
+    S = qscale_for(b->msize_abs_sum);
+    inv_q = 1.0 / S;
+  }
   ORBIT_PB("setup", s);
   if (plain)
-    k_setup<unsigned long long><<<1, 256, 0, s>>>(c->d_st, b->d_status, c->nx, c->ny, c->nz, 1.0 / S, c->d_rho_q,
+    k_setup<unsigned long long><<<1, 256, 0, s>>>(c->d_st, b->d_status, c->nx, c->ny, c->nz, inv_q, c->d_rho_q,
                                                   c->d_z_q);
   else
     k_setup<float><<<1, 256, 0, s>>>(c->d_st, b->d_status, c->nx, c->ny, c->nz, 1.0, c->d_rho_f, c->d_z_f);
@@ -659,12 +717,12 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
   if (plain) {
     if (c->smem_deposit)
       k_deposit_plain<true><<<blocks, threads, sm, s>>>(b->coord(0), b->coord(2), b->coord(4), msz, n, c->d_st,
-                                                        c->d_rho_q, c->d_z_q, b->sync.macrosize * S, S, c->nx,
-                                                        c->ny, c->nz);
+                                                        c->d_rho_q, c->d_z_q, ms_uniform, S, c->nx, c->ny, c->nz,
+                                                        K);
     else
       k_deposit_plain<false><<<blocks, threads, 0, s>>>(b->coord(0), b->coord(2), b->coord(4), msz, n, c->d_st,
-                                                        c->d_rho_q, c->d_z_q, b->sync.macrosize * S, S, c->nx,
-                                                        c->ny, c->nz);
+                                                        c->d_rho_q, c->d_z_q, ms_uniform, S, c->nx, c->ny, c->nz,
+                                                        K);
   } else {
     if (c->smem_deposit)
       k_deposit_fp32<true><<<blocks, threads, sm, s>>>(b->coord(0), b->coord(2), b->coord(4), msz, n, c->d_st,
@@ -686,6 +744,15 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
   ORBIT_LAUNCH_CHECK("sc2p5d deposit");
   rc = plain ? enqueue_solve<double>(c, s, &nl) : enqueue_solve<float>(c, s, &nl);
   if (rc) return rc;
+  if (plain) {
+    int ng = c->nx * c->ny;
+    int m = ng > c->nz ? ng : c->nz;
+    ORBIT_PB("phi_fix", s);
+    k_phi_fix<<<(m + 255) / 256, 256, 0, s>>>(c->d_st, c->d_phi, c->d_lam, c->d_phi_fix, c->d_lam_fix, ng, c->nz);
+    ORBIT_PE(s);
+    ++nl;
+    ORBIT_LAUNCH_CHECK("sc2p5d phi_fix");
+  }
   if (do_kick) {
     double hf = sc_host_factor(b->sync, length);
     size_t smk = (plain ? sizeof(double) : sizeof(float)) * ((size_t)c->nx * c->ny + c->nz);
@@ -694,12 +761,12 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
     if (plain) {
       if (c->smem_kick)
         k_kick_plain<true><<<blocks, threads, smk, s>>>(b->coord(0), b->coord(1), b->coord(2), b->coord(3),
-                                                        b->coord(4), n, c->d_st, c->d_phi, c->d_lam, hf, c->nx,
-                                                        c->ny, c->nz);
+                                                        b->coord(4), n, c->d_st, c->d_phi, c->d_lam, c->d_phi_fix,
+                                                        c->d_lam_fix, hf, c->nx, c->ny, c->nz);
       else
         k_kick_plain<false><<<blocks, threads, 0, s>>>(b->coord(0), b->coord(1), b->coord(2), b->coord(3),
-                                                       b->coord(4), n, c->d_st, c->d_phi, c->d_lam, hf, c->nx,
-                                                       c->ny, c->nz);
+                                                       b->coord(4), n, c->d_st, c->d_phi, c->d_lam, c->d_phi_fix,
+                                                       c->d_lam_fix, hf, c->nx, c->ny, c->nz);
     } else {
       if (c->smem_kick)
         k_kick_fp32<true><<<blocks, threads, smk, s>>>(b->coord(0), b->coord(1), b->coord(2), b->coord(3),
@@ -788,6 +855,8 @@ int orbit_sc2p5d_create(orbit_sc2p5d_t** out, int nx, int ny, int nz, double xy_
   if (form == ORBIT_FORM_PLAIN) {
     A((void**)&c->d_rho_q, sizeof(unsigned long long) * ng);
     A((void**)&c->d_z_q, sizeof(unsigned long long) * nz);
+    A((void**)&c->d_phi_fix, sizeof(long long) * ng);
+    A((void**)&c->d_lam_fix, sizeof(long long) * nz);
     A(&c->d_hat, sizeof(double2) * nhat);
     A(&c->d_green, sizeof(double2) * nhat);
     if (e == cudaSuccess) c->d_tw_x = make_twiddles<double>(c->nx2, &e);
@@ -841,7 +910,8 @@ int orbit_sc2p5d_destroy(orbit_sc2p5d_t* c) {
   if (c->used) cudaEventSynchronize(c->done);
   if (c->done) cudaEventDestroy(c->done);
   void* ptrs[] = {c->d_st, c->d_rho_q, c->d_z_q, c->d_rho_f, c->d_z_f, c->d_rho, c->d_phi, c->d_lam,
-                  c->d_phi_f, c->d_lam_f, c->d_hat, c->d_green, c->d_gbuf, c->d_tw_x, c->d_tw_y};
+                  c->d_phi_f, c->d_lam_f, c->d_hat, c->d_green, c->d_gbuf, c->d_tw_x, c->d_tw_y,
+                  c->d_phi_fix, c->d_lam_fix};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete c;
@@ -939,7 +1009,8 @@ static constexpr size_t kStaticScratchBytes =
     2 * al256(8ull * kStaticMaxNxy * kStaticMaxNxy) + al256(8ull * kStaticMaxNz) +   // rho, phi, lambda
     2 * al256(16ull * 2 * kStaticMaxNxy * (kStaticMaxNxy + 1)) +                     // spectrum, Green spectrum
     al256(8ull * 4 * kStaticMaxNxy * kStaticMaxNxy) +                                // Green function
-    2 * al256(16ull * 2 * kStaticMaxNxy);                                            // twiddles x, y
+    2 * al256(16ull * 2 * kStaticMaxNxy) +                                           // twiddles x, y
+    al256(8ull * kStaticMaxNxy * kStaticMaxNxy) + al256(8ull * kStaticMaxNz);       // fixed-point phi, lambda
 
 // Held by every GPU that loads the library, until the process exits
 // (about 2.1 MB).  Shared by all calls: calls that overlap on the GPU race.
@@ -1016,6 +1087,8 @@ extern "C" int orbit_sc2p5d_track_static(double* dev_coords, int n, int stride, 
   c.d_gbuf = (double*)take(8 * (size_t)c.nx2 * c.ny2);
   c.d_tw_x = take(16 * (size_t)c.nx2);
   c.d_tw_y = take(16 * (size_t)c.ny2);
+  c.d_phi_fix = (long long*)take(8 * ng);
+  c.d_lam_fix = (long long*)take(8 * (size_t)nz);
   if (off > kStaticScratchBytes) return set_error(ORBIT_ERR_DEVICE, "orbit_sc2p5d_track_static: scratch layout");
   cudaStream_t s = (cudaStream_t)stream;
   // state of a freshly constructed calculator (SpaceChargeCalc2p5D.cc:25-43);

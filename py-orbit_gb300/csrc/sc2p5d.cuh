@@ -19,10 +19,13 @@ struct ScState {
   double re00;                                            // Re G~[0][0] (PoissonSolverFFT2D.cc:164)
   double scale;                                           // log(dx_solver/dx_rho) (:213)
   double total_m;                                         // sum of the line density (:229-233)
-  double inv_qscale;                                      // 1/S of the fixed-point deposit
+  double inv_qscale;                                      // macrosize per unit of the fixed-point deposit
   int green_dirty;                                        // Green spectrum must be rebuilt
   int skip;                                               // this kick is skipped (zero extent)
   unsigned long long key[6];                              // extrema accumulators (ordered keys)
+  unsigned long long phi_absmax;                          // bits of max |phi| (non-negative doubles
+  unsigned long long lam_absmax;                          //  order like their bit patterns), max |lambda|
+  int dep_k;                                              // fraction bits of the integer deposit (0: FP64 path)
 };
 
 struct FftPlan {
@@ -47,6 +50,8 @@ struct orbit_sc2p5d {
   double* d_lam = nullptr;                // user-visible line density (nz)
   float* d_phi_f = nullptr;               // fp32-form phi
   float* d_lam_f = nullptr;
+  long long* d_phi_fix = nullptr;         // plain form: phi, lambda as scaled 64-bit integers
+  long long* d_lam_fix = nullptr;
   void* d_hat = nullptr;                  // nx2 * H complex work spectrum (T = double or float)
   void* d_green = nullptr;                // nx2 * H complex Green spectrum
   double* d_gbuf = nullptr;               // nx2 * ny2 real Green function
@@ -82,6 +87,8 @@ struct KickArgs {
   const double* lam;
   const float* phi_f;     // fp32 form
   const float* lam_f;
+  const long long* phi_fix;  // plain form, fixed point
+  const long long* lam_fix;
   double host_factor;
   int nx, ny, nz, form;
 };

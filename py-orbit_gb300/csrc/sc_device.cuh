@@ -265,6 +265,244 @@ __device__ __forceinline__ void deposit_plain(const DepConst& d, unsigned long l
   }
 }
 
+// ---------------------------------------------------------------------
+// Exact fixed-point arithmetic on the integer pipe (plain form).
+//
+// After one FP64 fused multiply-add per coordinate, v = t + 0.5 with
+// t = (x - xmin)/dx in cell units, the index, the fraction and the 9-point
+// weights are computed as 64-bit fixed-point integers: the fraction
+// f = t - ind exactly as rounded into v (Q56), the weights W = (f -+ 0.5)^2/2
+// and 0.75 - f^2 in Q58 (absolute error below 2^-58), the derivative
+// weights exactly.  GB300 issues two FP64 FMAs per SM per cycle but dozens
+// of integer operations, so this keeps the FP64 pipe for the coordinates.
+// ---------------------------------------------------------------------
+
+// v * 2^F truncated toward zero; false when |v| * 2^F could reach 2^63 or v
+// is not finite.
+__device__ __forceinline__ bool fix_of(double v, int F, long long& out) {
+  long long u = __double_as_longlong(v);
+  int e = (int)((u >> 52) & 0x7ff);
+  long long m = (u & 0x000FFFFFFFFFFFFFll) | 0x0010000000000000ll;
+  int sh = e - 1075 + F;
+  long long r;
+  if (e == 0) {
+    r = 0;
+  } else if (sh >= 0) {
+    if (sh > 10) return false;
+    r = m << sh;
+  } else {
+    r = (sh > -63) ? (m >> (-sh)) : 0;
+  }
+  out = (u < 0) ? -r : r;
+  return true;
+}
+
+// Fraction bits F for values below n + 1 (n >= 2): v * 2^F < 2^63.
+__host__ __device__ __forceinline__ int fix_bits(int n) {
+  int b = 0;
+  while ((1 << b) < n + 2) ++b;
+  int F = 63 - b;
+  return F > 60 ? 60 : F;
+}
+
+// g in Q56 with |g| <= 2^57: g^2 in Q58.
+__device__ __forceinline__ long long sq_q58(long long g) {
+  unsigned long long a = (unsigned long long)(g < 0 ? -g : g) << 5;
+  return (long long)__umul64hi(a, a);
+}
+
+// Grid2D::getIndAndFracX/Y on v = t + 0.5: ind = floor(v) clamped to
+// [1, n-2], f = t - ind in Q56.  False outside 0 <= floor(v) <= n-1.
+__device__ __forceinline__ bool tsc_fixed(double v, int n, int F, int& ind, long long& f56) {
+  long long V;
+  // |f| <= 1.25 keeps every product below 2^63; particles inside the grid
+  // limits have 0.5 <= v <= n - 0.5
+  if (!fix_of(v, F, V) || V < (1ll << (F - 2)) || V > ((long long)n << F) - (1ll << (F - 2))) return false;
+  long long i = V >> F;
+  long long fr = V - (i << F) - (1ll << (F - 1));
+  long long f = (F <= 56) ? (fr << (56 - F)) : (fr >> (F - 56));
+  if (i < 1) { f -= (1ll << 56); i = 1; }
+  if (i > n - 2) { f += (1ll << 56); i = n - 2; }
+  ind = (int)i;
+  f56 = f;
+  return true;
+}
+
+// 9-point weights Wm, W0, Wp (Q58) and derivative weights (Q58).
+__device__ __forceinline__ void tsc_w_fixed(long long f, long long w[3]) {
+  w[0] = sq_q58(f - (1ll << 55)) >> 1;
+  w[1] = (3ll << 56) - sq_q58(f);
+  w[2] = sq_q58(f + (1ll << 55)) >> 1;
+}
+__device__ __forceinline__ void tsc_dw_fixed(long long f, long long dw[3]) {
+  dw[0] = (f - (1ll << 55)) << 2;  // f - 1/2
+  dw[1] = -(f << 3);               // -2 f
+  dw[2] = (f + (1ll << 55)) << 2;  // f + 1/2
+}
+
+// Grid1D index on u = (z - zmin)/dz + 0.5 (nz > 1): floor semantics with
+// periodic neighbours reproduce every wrap rule of Grid1D::getIndAndWZ;
+// wp (weight of ip) in Q56.
+__device__ __forceinline__ bool g1_fixed(double u, int nz, int F, int& i0, int& ip, long long& wp56) {
+  long long V;
+  if (!fix_of(u, F, V) || V < 0) return false;
+  long long i = V >> F;
+  if (i > nz) return false;
+  long long fr = V - (i << F);
+  wp56 = (F <= 56) ? (fr << (56 - F)) : (fr >> (F - 56));
+  int a = (int)i - 1;
+  i0 = a < 0 ? nz - 1 : a;
+  ip = (int)i >= nz ? 0 : (int)i;
+  return true;
+}
+
+struct DepFix {
+  unsigned long long kxmin, kxmax, kymin, kymax, kzmin, kzmax;  // ordered keys of the limits
+  double ax, cx, ay, cy, az, cz;   // v = x * ax + cx etc.
+  int nx, ny, nz, Fx, Fy, Fz, K;
+  int skip;
+};
+
+__device__ __forceinline__ void load_dep_fix(DepFix& d, const ScState* st, int nx, int ny, int nz, int K) {
+  d.kxmin = dkey(st->xmin); d.kxmax = dkey(st->xmax);
+  d.kymin = dkey(st->ymin); d.kymax = dkey(st->ymax);
+  d.kzmin = dkey(st->zmin); d.kzmax = dkey(st->zmax);
+  d.ax = st->inv_dx; d.cx = 0.5 - st->xmin * st->inv_dx;
+  d.ay = st->inv_dy; d.cy = 0.5 - st->ymin * st->inv_dy;
+  d.az = st->inv_dz; d.cz = 0.5 - st->zmin * st->inv_dz;
+  d.nx = nx; d.ny = ny; d.nz = nz;
+  d.Fx = fix_bits(nx); d.Fy = fix_bits(ny); d.Fz = fix_bits(nz);
+  d.K = K;
+  d.skip = st->skip;
+}
+
+// Integer deposit of one particle with unit weight scaled by 2^K (the
+// macrosize multiplies the grid afterwards).  Returns false when the
+// particle needs the FP64 path (never for finite coordinates in range).
+__device__ __forceinline__ bool deposit_fixed(const DepFix& d, unsigned long long* rho, unsigned long long* zg,
+                                              double x, double y, double z) {
+  unsigned long long kx = dkey(x), ky = dkey(y), kz = dkey(z);
+  bool in2 = kx >= d.kxmin && kx <= d.kxmax && ky >= d.kymin && ky <= d.kymax;
+  bool in1 = kz >= d.kzmin && kz <= d.kzmax;
+  int ix = 0, iy = 0, i0 = 0, ip = 0;
+  long long fx = 0, fy = 0, wp = 0;
+  if (in2) {
+    if (!tsc_fixed(fma(x, d.ax, d.cx), d.nx, d.Fx, ix, fx)) return false;
+    if (!tsc_fixed(fma(y, d.ay, d.cy), d.ny, d.Fy, iy, fy)) return false;
+  }
+  if (in1 && d.nz > 1) {
+    if (!g1_fixed(fma(z, d.az, d.cz), d.nz, d.Fz, i0, ip, wp)) return false;
+  }
+  if (in2) {
+    long long wx[3], wy[3];
+    tsc_w_fixed(fx, wx);
+    tsc_w_fixed(fy, wy);
+    const int sh = 60 - d.K;
+    const long long half = 1ll << (sh - 1);
+    unsigned long long* base = rho + (ix - 1) * d.ny + (iy - 1);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      long long a = wx[i] << 4;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        long long p = __mul64hi(a, wy[j] << 4);  // Wx Wy in Q60
+        atomicAdd(base + i * d.ny + j, (unsigned long long)((p + half) >> sh));
+      }
+    }
+  }
+  if (in1) {
+    const int sh = 56 - d.K;
+    const long long half = 1ll << (sh - 1);
+    if (d.nz > 1) {
+      atomicAdd(zg + i0, (unsigned long long)((((1ll << 56) - wp) + half) >> sh));
+      atomicAdd(zg + ip, (unsigned long long)((wp + half) >> sh));
+    } else {
+      atomicAdd(zg, (unsigned long long)(1ll << d.K));
+    }
+  }
+  return true;
+}
+
+// Fixed-point kick: phi and lambda as 64-bit integers with per-kick scales
+// (phi * 2^sphi, lambda * 2^slam, both below 2^61).
+struct KickFix {
+  double ax, cx, ay, cy, az, cz;
+  unsigned long long kzmin, kzmax;
+  double gxs, gys;   // inv_dx * 2^-(sphi-5), inv_dy * 2^-(sphi-5)
+  double lfs;        // -factor * 2^-(slam-2)
+  int nx, ny, nz, Fx, Fy, Fz;
+  int sphi, slam;
+  int skip;
+};
+
+__device__ __forceinline__ int scale_bits(unsigned long long absmax_bits) {
+  int e = (int)((absmax_bits >> 52) & 0x7ff);
+  return absmax_bits == 0 ? 0 : 1083 - e;  // max * 2^s < 2^61
+}
+
+__device__ __forceinline__ void load_kick_fix(KickFix& k, const ScState* st, double host_factor, int nx, int ny,
+                                              int nz) {
+  k.ax = st->inv_dx; k.cx = 0.5 - st->xmin * st->inv_dx;
+  k.ay = st->inv_dy; k.cy = 0.5 - st->ymin * st->inv_dy;
+  k.az = st->inv_dz; k.cz = 0.5 - st->zmin * st->inv_dz;
+  k.kzmin = dkey(st->zmin); k.kzmax = dkey(st->zmax);
+  k.sphi = scale_bits(st->phi_absmax);
+  k.slam = scale_bits(st->lam_absmax);
+  k.gxs = ldexp(st->inv_dx, 5 - k.sphi);
+  k.gys = ldexp(st->inv_dy, 5 - k.sphi);
+  double fac = host_factor / (st->dz * st->total_m);
+  k.lfs = ldexp(-fac, 2 - k.slam);
+  k.nx = nx; k.ny = ny; k.nz = nz;
+  k.Fx = fix_bits(nx); k.Fy = fix_bits(ny); k.Fz = fix_bits(nz);
+  k.skip = st->skip;
+}
+
+__device__ __forceinline__ long long phi_fixed(double v, int s) {
+  long long r;
+  return fix_of(v, s, r) ? r : 0;
+}
+
+// Returns false when the particle needs the FP64 path.
+__device__ __forceinline__ bool kick_fixed(const KickFix& k, const long long* __restrict__ P,
+                                           const long long* __restrict__ Lm, double x, double y, double z,
+                                           double& xp, double& yp) {
+  int ix, iy;
+  long long fx, fy;
+  if (!tsc_fixed(fma(x, k.ax, k.cx), k.nx, k.Fx, ix, fx)) return false;
+  if (!tsc_fixed(fma(y, k.ay, k.cy), k.ny, k.Fy, iy, fy)) return false;
+  long long lv = 0;
+  unsigned long long kz = dkey(z);
+  if (kz >= k.kzmin && kz <= k.kzmax) {
+    if (k.nz > 1) {
+      int i0, ip;
+      long long wp;
+      if (!g1_fixed(fma(z, k.az, k.cz), k.nz, k.Fz, i0, ip, wp)) return false;
+      lv = __mul64hi(((1ll << 56) - wp) << 6, Lm[i0]) + __mul64hi(wp << 6, Lm[ip]);  // Q(slam-2)
+    } else {
+      lv = Lm[0] >> 2;
+    }
+  }
+  long long wx[3], wy[3], dwx[3], dwy[3];
+  tsc_w_fixed(fx, wx);
+  tsc_w_fixed(fy, wy);
+  tsc_dw_fixed(fx, dwx);
+  tsc_dw_fixed(fy, dwy);
+  long long gx = 0, gy = 0;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const long long* r = P + (ix - 1 + i) * k.ny + (iy - 1);
+    long long a0 = r[0], a1 = r[1], a2 = r[2];
+    long long s = __mul64hi(wy[0] << 4, a0) + __mul64hi(wy[1] << 4, a1) + __mul64hi(wy[2] << 4, a2);     // Q(sphi-2)
+    long long t = __mul64hi(dwy[0] << 3, a0) + __mul64hi(dwy[1] << 3, a1) + __mul64hi(dwy[2] << 3, a2);  // Q(sphi-3)
+    gx += __mul64hi(dwx[i] << 3, s);  // Q(sphi-5)
+    gy += __mul64hi(wx[i] << 4, t);   // Q(sphi-5)
+  }
+  double lf = (double)lv * k.lfs;  // -lambda(z) * factor
+  xp = fma((double)gx, k.gxs * lf, xp);
+  yp = fma((double)gy, k.gys * lf, yp);
+  return true;
+}
+
 __device__ __forceinline__ void deposit_fp32(const DepConst& d, float* rho, float* zg, double x, double y,
                                              double z, float m) {
   if (!(x < d.xmin || x > d.xmax || y < d.ymin || y > d.ymax)) {
