@@ -595,11 +595,12 @@ static int ext_blocks(int n) {
 }
 
 // launch geometry for particle kernels that keep a grid copy in shared memory
-static void particle_geometry(size_t smem, int n, int* blocks, int* threads) {
+static void particle_geometry(size_t smem, int n, int max_threads, int* blocks, int* threads) {
   int bps = smem > 0 ? (int)(kMaxSmem / smem) : 8;
   if (bps < 1) bps = 1;
   if (bps > 4) bps = 4;
   *threads = (bps == 1) ? 1024 : 512;
+  if (*threads > max_threads) *threads = max_threads & ~31;  // register-limited kernels
   int b = num_sms() * bps;
   int need = (n + *threads - 1) / *threads;
   *blocks = need < b ? (need < 1 ? 1 : need) : b;
@@ -662,6 +663,25 @@ static int enqueue_green(orbit_sc2p5d_t* c, cudaStream_t s, int* nl) {
   return ORBIT_OK;
 }
 
+// Largest block the kernel can launch with (its registers per thread).
+template <typename K>
+static int max_threads_of(K kernel) {
+  cudaFuncAttributes a;
+  if (cudaFuncGetAttributes(&a, (const void*)kernel) != cudaSuccess) return 256;
+  return a.maxThreadsPerBlock;
+}
+
+// Block-size limits of the particle kernels: deposit plain (shared, global),
+// deposit fp32 (shared, global), kick plain (shared, global), kick fp32.
+// Queried once, outside any stream capture (init_attrs).
+static const int* particle_kernel_threads() {
+  static const int mt[8] = {max_threads_of(k_deposit_plain<true>), max_threads_of(k_deposit_plain<false>),
+                            max_threads_of(k_deposit_fp32<true>), max_threads_of(k_deposit_fp32<false>),
+                            max_threads_of(k_kick_plain<true>), max_threads_of(k_kick_plain<false>),
+                            max_threads_of(k_kick_fp32<true>), max_threads_of(k_kick_fp32<false>)};
+  return mt;
+}
+
 static double qscale_for(double msum_abs) {
   double M = msum_abs;
   if (!(M > 0.0) || !std::isfinite(M)) return 1.0;
@@ -712,7 +732,9 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
   size_t esz = plain ? sizeof(unsigned long long) : sizeof(float);
   size_t sm = esz * ((size_t)c->nx * c->ny + c->nz);
   int blocks, threads;
-  particle_geometry(c->smem_deposit ? sm : 0, n, &blocks, &threads);
+  const int* mt_dep = particle_kernel_threads();
+  particle_geometry(c->smem_deposit ? sm : 0, n, mt_dep[(plain ? 0 : 2) + (c->smem_deposit ? 0 : 1)], &blocks,
+                    &threads);
   ORBIT_PB("deposit", s);
   if (plain) {
     if (c->smem_deposit)
@@ -756,7 +778,9 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
   if (do_kick) {
     double hf = sc_host_factor(b->sync, length);
     size_t smk = (plain ? sizeof(double) : sizeof(float)) * ((size_t)c->nx * c->ny + c->nz);
-    particle_geometry(c->smem_kick ? smk : 0, n, &blocks, &threads);
+    const int* mt_kick = particle_kernel_threads() + 4;
+    particle_geometry(c->smem_kick ? smk : 0, n, mt_kick[(plain ? 0 : 2) + (c->smem_kick ? 0 : 1)], &blocks,
+                      &threads);
     ORBIT_PB("kick", s);
     if (plain) {
       if (c->smem_kick)
@@ -796,6 +820,7 @@ cudaError_t sc_mark_used(orbit_sc2p5d_t* c, cudaStream_t s) {
 }
 
 static int init_attrs(orbit_sc2p5d_t* c) {
+  particle_kernel_threads();
   size_t dep = (c->form == ORBIT_FORM_PLAIN ? 8 : 4) * ((size_t)c->nx * c->ny + c->nz);
   size_t kick = (c->form == ORBIT_FORM_PLAIN ? 8 : 4) * ((size_t)c->nx * c->ny + c->nz);
   c->smem_deposit = dep <= (size_t)kMaxSmem;

@@ -131,6 +131,32 @@ def test_hundred_kicks_fodo():
     assert rel_err(got[1], soa[1]) > 1e-3
 
 
+def test_benchmark_grid_fused_program():
+    """The benchmark's grid (128x128x64): shared-memory grids of 128 KiB, one
+    block per SM, register-limited block sizes; fused program vs oracle."""
+    from orbit_gb300 import workloads as W
+    from spacecharge import SpaceChargeCalc2p5D
+    soa = W.c2_coords(100_000, seed=21)
+    b = gpu_bunch(soa, 1e9)
+    calc = SpaceChargeCalc2p5D(128, 128, 64)
+    lat = W.fodo_lattice(calc, cells=2)
+    prog = lat.fusedProgram(b)
+    lat.trackBunchTurns(b, 2)
+    got = b.getCoordinates()
+    ref, ocalcs = run_oracle_program(prog.ops, soa, oracle_sync_of(b), [(128, 128, 64)], turns=2)
+    assert coord_err(got, ref) <= TOL_COORD
+    rho, phi, zg, lim = ocalcs[0].grids()
+    assert rel_err(calc.getPhiGrid().getArray(), phi) <= TOL_FIELD
+    # the eager path on the same grid (stand-alone kernels with 1024-thread blocks)
+    b2 = gpu_bunch(soa, 1e9)
+    c2 = SpaceChargeCalc2p5D(128, 128, 64)
+    c2.trackBunch(b2, 0.5)
+    s2 = O.OracleSC(128, 128, 64)
+    a = np.ascontiguousarray(soa.copy())
+    assert s2.track(a, oracle_sync_of(b2), 0.5, nthreads=8) == 0
+    assert rel_err(b2.getCoordinates()[1] - soa[1], a[1] - soa[1]) <= TOL_FIELD * 10
+
+
 def test_fused_equals_eager():
     from orbit_gb300 import workloads as W
     from spacecharge import SpaceChargeCalc2p5D
