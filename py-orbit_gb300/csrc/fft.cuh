@@ -7,8 +7,9 @@
 //   b[k*L*p + j + r*L] = sum_q (a[k*L + j + q*N/p] * W_{Lp}^{j q}) W_p^{q r}
 // (L = product of the radices before s), so the result is in natural order
 // after the last stage.  Twiddles come from a table W_N^e = exp(-2 pi i e/N)
-// computed on the host; supported radices are 2, 3, 4, 5 and any prime up
-// to 13.
+// computed on the host and staged in shared memory; supported radices are
+// 2, 3, 4, 5 and any prime up to 13, with fixed-radix butterflies in
+// registers for power-of-two lengths.
 #pragma once
 
 #include "common.cuh"
@@ -34,12 +35,81 @@ __device__ __forceinline__ C c_sub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y -
 template <typename C>
 __device__ __forceinline__ C c_conj(C a) { a.y = -a.y; return a; }
 
-// a: input buffer, b: scratch; returns the buffer holding the result.
-// `inv` selects the backward (+i) transform; unnormalised.
+// Radix-P stage of a power-of-two length (P = 2 or 4) with compile-time
+// butterflies: t = k*L + j, inputs a[t + q*N/P], outputs b[k*L*P + j + r*L],
+// twiddles W_{LP}^{jq} = tw[(j*q) << lgtw] read from shared memory.
+template <typename T, int P, bool INV>
+__device__ __forceinline__ void fft_stage_pow2(const typename CT<T>::t* __restrict__ a,
+                                               typename CT<T>::t* __restrict__ b, int N, int L, int lgL,
+                                               int lgtw, const typename CT<T>::t* __restrict__ tw) {
+  typedef typename CT<T>::t C;
+  const int Np = N / P;
+  for (int t = threadIdx.x; t < Np; t += blockDim.x) {
+    const int j = t & (L - 1);
+    C x[P];
+#pragma unroll
+    for (int q = 0; q < P; ++q) x[q] = a[t + q * Np];
+    if (L > 1) {  // the first stage has only W^0 = 1
+#pragma unroll
+      for (int q = 1; q < P; ++q) {
+        C w = tw[(j * q) << lgtw];
+        if (INV) w.y = -w.y;
+        x[q] = c_mul(x[q], w);
+      }
+    }
+    C* out = b + ((t - j) * P) + j;
+    if (P == 2) {
+      out[0] = c_add(x[0], x[1]);
+      out[L] = c_sub(x[0], x[1]);
+    } else {
+      C a0 = c_add(x[0], x[2]), a1 = c_sub(x[0], x[2]);
+      C b0 = c_add(x[1], x[3]), b1 = c_sub(x[1], x[3]);
+      C c;  // (-i or +i) * b1
+      if (INV) { c.x = -b1.y; c.y = b1.x; } else { c.x = b1.y; c.y = -b1.x; }
+      out[0] = c_add(a0, b0);
+      out[L] = c_add(a1, c);
+      out[2 * L] = c_sub(a0, b0);
+      out[3 * L] = c_sub(a1, c);
+    }
+  }
+}
+
+template <typename T, bool INV>
+__device__ typename CT<T>::t* block_fft_pow2(typename CT<T>::t* a, typename CT<T>::t* b, const FftPlan& pl,
+                                             const typename CT<T>::t* __restrict__ tw) {
+  typedef typename CT<T>::t C;
+  // FP64 runs at a fraction of a lane per cycle per SM sub-partition, so the
+  // transform is bound by how many warps share it: with N/2 threads every
+  // stage is radix 2 (one butterfly per thread); with fewer, radix 4 while
+  // possible, then one radix 2.
+  const int N = pl.n;
+  const int lgN = 31 - __clz(N);
+  const bool wide = (int)blockDim.x >= N / 2;
+  int L = 1, lgL = 0;
+  while (lgL < lgN) {
+    if (!wide && lgL + 2 <= lgN) {
+      fft_stage_pow2<T, 4, INV>(a, b, N, L, lgL, lgN - lgL - 2, tw);
+      L *= 4; lgL += 2;
+    } else {
+      fft_stage_pow2<T, 2, INV>(a, b, N, L, lgL, lgN - lgL - 1, tw);
+      L *= 2; lgL += 1;
+    }
+    __syncthreads();
+    C* tmp = a;
+    a = b;
+    b = tmp;
+  }
+  return a;
+}
+
+// a: input buffer, b: scratch, tw: the W_N table (shared memory); returns
+// the buffer holding the result.  `inv` selects the backward (+i)
+// transform; unnormalised.
 template <typename T>
 __device__ typename CT<T>::t* block_fft(typename CT<T>::t* a, typename CT<T>::t* b, const FftPlan& pl,
                                         const typename CT<T>::t* __restrict__ tw, bool inv) {
   typedef typename CT<T>::t C;
+  if (pl.pow2) return inv ? block_fft_pow2<T, true>(a, b, pl, tw) : block_fft_pow2<T, false>(a, b, pl, tw);
   const int N = pl.n;
   int L = 1;
   for (int s = 0; s < pl.nst; ++s) {
@@ -94,6 +164,12 @@ __device__ typename CT<T>::t* block_fft(typename CT<T>::t* a, typename CT<T>::t*
     L = Lp;
   }
   return a;
+}
+
+// Copies the W_N twiddle table to shared memory (the caller synchronises).
+template <typename C>
+__device__ __forceinline__ void load_twiddles(C* s_tw, const C* __restrict__ tw, int N) {
+  for (int e = threadIdx.x; e < N; e += blockDim.x) s_tw[e] = tw[e];
 }
 
 // Host: factor N into supported radices (4s first, then 2, 3, 5, 7, 11, 13).

@@ -28,7 +28,7 @@ __global__ void __launch_bounds__(512) k_pass(double* __restrict__ cx, double* _
                                               double* __restrict__ cy, double* __restrict__ cyp,
                                               double* __restrict__ cz, double* __restrict__ cdE, int n,
                                               const DevOp* __restrict__ ops, int a, int b, MapCtx m,
-                                              KickArgs kick, ScState* ext_st, unsigned* status) {
+                                              KickArgs kick, ScState* ext_st, unsigned* status, SetupArgs sa) {
   KickConst k;
   KickFix kf;
   const long long* P = kick.phi_fix;
@@ -42,9 +42,10 @@ __global__ void __launch_bounds__(512) k_pass(double* __restrict__ cx, double* _
     if (KSMEM) {
       int ng = kick.nx * kick.ny;
       if (KF == 1) {
+        // fixed-point copy converted here from the FP64 potential
         long long* s = reinterpret_cast<long long*>(s_raw);
-        for (int i = threadIdx.x; i < ng; i += blockDim.x) s[i] = kick.phi_fix[i];
-        for (int i = threadIdx.x; i < kick.nz; i += blockDim.x) s[ng + i] = kick.lam_fix[i];
+        for (int i = threadIdx.x; i < ng; i += blockDim.x) s[i] = phi_fixed(kick.phi[i], kf.sphi);
+        for (int i = threadIdx.x; i < kick.nz; i += blockDim.x) s[ng + i] = phi_fixed(kick.lam[i], kf.slam);
         P = s;
         Lm = s + ng;
       } else {
@@ -70,7 +71,8 @@ __global__ void __launch_bounds__(512) k_pass(double* __restrict__ cx, double* _
     if (EXT) acc.add(p.x, p.y, p.z);
     cx[i] = p.x; cxp[i] = p.xp; cy[i] = p.y; cyp[i] = p.yp; cz[i] = p.z; cdE[i] = p.dE;
   }
-  if (EXT) ext_block_commit(acc, ext_st, status);
+  // the last block sets up the grids of the next kick
+  if (EXT) ext_commit_and_setup(acc, ext_st, status, sa);
 }
 
 // Shared-memory limits are raised once, outside any stream capture.
@@ -87,7 +89,7 @@ static int init_pass_attrs() {
 
 template <int KF, bool EXT, bool KSMEM>
 static int launch_pass(orbit_bunch_t* bu, cudaStream_t s, size_t smem, const DevOp* ops, int a, int b,
-                       const MapCtx& m, const KickArgs& ka, ScState* ext) {
+                       const MapCtx& m, const KickArgs& ka, ScState* ext, const SetupArgs& sa) {
   int threads = 512;
   int bps = KSMEM ? (int)(kPassSmem / (smem > 0 ? smem : 1)) : 4;
   if (bps < 1) bps = 1;
@@ -98,7 +100,7 @@ static int launch_pass(orbit_bunch_t* bu, cudaStream_t s, size_t smem, const Dev
   ORBIT_PB(KF == 0 ? "pass_maps" : "pass_kick_maps", s);
   k_pass<KF, EXT, KSMEM><<<blocks, threads, KSMEM ? smem : 0, s>>>(
       bu->coord(0), bu->coord(1), bu->coord(2), bu->coord(3), bu->coord(4), bu->coord(5), bu->n, ops, a, b, m, ka,
-      ext, bu->d_status);
+      ext, bu->d_status, sa);
   ORBIT_PE(s);
   ORBIT_LAUNCH_CHECK("k_pass");
   return ORBIT_OK;
@@ -177,24 +179,27 @@ static int enqueue_pass(orbit_bunch_t* bu, cudaStream_t s, const DevOp* ops, Seg
     ka = kick_args(kc, bu->sync, klen);
     kf = kc->form == ORBIT_FORM_PLAIN ? 1 : 2;
     smem = (kf == 1 ? 8 : 4) * ((size_t)kc->nx * kc->ny + kc->nz);
-    ksm = smem <= (size_t)kPassSmem;
+    ksm = kc->smem_kick && smem <= (size_t)kPassSmem;  // else the kick reads phi_fix, converted by the solve
   }
   if (!kc && !ec && seg.a == seg.b) return ORBIT_OK;  // nothing to do
   ScState* ext = ec ? ec->d_st : nullptr;
   bool e = ext != nullptr;
+  SetupArgs sa;
+  std::memset(&sa, 0, sizeof(sa));
+  if (ec) sa = sc_setup_args(ec, sc_dep_scales(ec, bu));
   int rc;
-  if (kf == 0) rc = e ? launch_pass<0, true, false>(bu, s, 0, ops, seg.a, seg.b, m, ka, ext)
-                      : launch_pass<0, false, false>(bu, s, 0, ops, seg.a, seg.b, m, ka, ext);
+  if (kf == 0) rc = e ? launch_pass<0, true, false>(bu, s, 0, ops, seg.a, seg.b, m, ka, ext, sa)
+                      : launch_pass<0, false, false>(bu, s, 0, ops, seg.a, seg.b, m, ka, ext, sa);
   else if (kf == 1) {
-    if (ksm) rc = e ? launch_pass<1, true, true>(bu, s, smem, ops, seg.a, seg.b, m, ka, ext)
-                    : launch_pass<1, false, true>(bu, s, smem, ops, seg.a, seg.b, m, ka, ext);
-    else rc = e ? launch_pass<1, true, false>(bu, s, 0, ops, seg.a, seg.b, m, ka, ext)
-                : launch_pass<1, false, false>(bu, s, 0, ops, seg.a, seg.b, m, ka, ext);
+    if (ksm) rc = e ? launch_pass<1, true, true>(bu, s, smem, ops, seg.a, seg.b, m, ka, ext, sa)
+                    : launch_pass<1, false, true>(bu, s, smem, ops, seg.a, seg.b, m, ka, ext, sa);
+    else rc = e ? launch_pass<1, true, false>(bu, s, 0, ops, seg.a, seg.b, m, ka, ext, sa)
+                : launch_pass<1, false, false>(bu, s, 0, ops, seg.a, seg.b, m, ka, ext, sa);
   } else {
-    if (ksm) rc = e ? launch_pass<2, true, true>(bu, s, smem, ops, seg.a, seg.b, m, ka, ext)
-                    : launch_pass<2, false, true>(bu, s, smem, ops, seg.a, seg.b, m, ka, ext);
-    else rc = e ? launch_pass<2, true, false>(bu, s, 0, ops, seg.a, seg.b, m, ka, ext)
-                : launch_pass<2, false, false>(bu, s, 0, ops, seg.a, seg.b, m, ka, ext);
+    if (ksm) rc = e ? launch_pass<2, true, true>(bu, s, smem, ops, seg.a, seg.b, m, ka, ext, sa)
+                    : launch_pass<2, false, true>(bu, s, smem, ops, seg.a, seg.b, m, ka, ext, sa);
+    else rc = e ? launch_pass<2, true, false>(bu, s, 0, ops, seg.a, seg.b, m, ka, ext, sa)
+                : launch_pass<2, false, false>(bu, s, 0, ops, seg.a, seg.b, m, ka, ext, sa);
   }
   if (rc == ORBIT_OK) ++*nl;
   return rc;

@@ -23,6 +23,7 @@ bool make_fft_plan(int n, FftPlan& pl) {
   const int primes[] = {2, 3, 5, 7, 11, 13};
   for (int p : primes)
     while (m % p == 0 && pl.nst < 24) { pl.rad[pl.nst++] = p; m /= p; }
+  pl.pow2 = (n & (n - 1)) == 0;
   return m == 1;
 }
 
@@ -33,309 +34,72 @@ double sc_host_factor(const orbit_sync_t& s, double length) {
 // ---------------------------------------------------------------------
 // kernels
 // ---------------------------------------------------------------------
+// Extrema scan; the last block sets up the grids for the kick.  The
+// accumulation grids start at zero: the kernels that read them clear them.
 __global__ void k_extrema(const double* __restrict__ x, const double* __restrict__ y,
-                          const double* __restrict__ z, int n, ScState* st, unsigned* status) {
+                          const double* __restrict__ z, int n, ScState* st, unsigned* status, SetupArgs sa) {
   ExtAcc a;
   a.init();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) a.add(x[i], y[i], z[i]);
-  ext_block_commit(a, st, status);
+  ext_commit_and_setup(a, st, status, sa);
 }
 
-// Grid set-up of bunchAnalysis (SpaceChargeCalc2p5D.cc:126-216) in one
-// thread with explicitly rounded operations (no contraction), so that the
-// grid limits and the persistent xy_ratio evolve exactly as the reference's,
-// then all threads clear the accumulation grids.
-template <typename G>
-__global__ void k_setup(ScState* st, unsigned* status, int nx, int ny, int nz, double inv_qscale,
-                        G* rho_acc, G* z_acc) {
-  __shared__ int s_skip;
-  if (threadIdx.x == 0) {
-    double xMin = dkey_inv(st->key[0]), xMax = dkey_inv(st->key[1]);
-    double yMin = dkey_inv(st->key[2]), yMax = dkey_inv(st->key[3]);
-    double zMin = dkey_inv(st->key[4]), zMax = dkey_inv(st->key[5]);
-    for (int c = 0; c < 3; ++c) { st->key[2 * c] = ~0ull; st->key[2 * c + 1] = 0ull; }
-    int skip = 0;
-    if (*status & ST_NAN) {
-      // a non-finite coordinate was met by the extrema scan: no kick
-      skip = 1;
-    } else if (!(xMin < xMax) || !(yMin < yMax) || !(zMin < zMax)) {  // :131 (also catches an empty scan)
-      skip = 1;
-      atomicOr(status, (unsigned)ST_EXTENT);
-    } else {
-      double xy = st->xy_ratio;
-      double ratio_beam = __ddiv_rn(__dsub_rn(xMax, xMin), __dsub_rn(yMax, yMin));
-      int set_solver = 0;
-      if (fabs(__dsub_rn(ratio_beam, xy)) < __dmul_rn(0.25, xy)) {  // :152-168
-        double width, center;
-        if (ratio_beam > xy) {
-          center = __ddiv_rn(__dadd_rn(yMax, yMin), 2.0);
-          width = __ddiv_rn(__dmul_rn(__dsub_rn(yMax, yMin), __ddiv_rn(ratio_beam, xy)), 2.0);
-          yMin = __dsub_rn(center, width);
-          yMax = __dadd_rn(center, width);
-        } else {
-          center = __ddiv_rn(__dadd_rn(xMax, xMin), 2.0);
-          width = __ddiv_rn(__ddiv_rn(__dsub_rn(xMax, xMin), __ddiv_rn(ratio_beam, xy)), 2.0);
-          xMin = __dsub_rn(center, width);
-          xMax = __dadd_rn(center, width);
-        }
-        xy = __ddiv_rn(__dsub_rn(xMax, xMin), __dsub_rn(yMax, yMin));
-      } else {  // :169-173
-        xy = ratio_beam;
-        set_solver = 1;
-      }
-      // Grid2D::setGridX/Y (Grid2D.cc:422-433), Grid1D::setGridZ (Grid1D.cc:89-94)
-      double dx = __ddiv_rn(__dsub_rn(xMax, xMin), (double)(nx - 1));
-      double dy = __ddiv_rn(__dsub_rn(yMax, yMin), (double)(ny - 1));
-      double dz = __ddiv_rn(__dsub_rn(zMax, zMin), (double)nz);
-      st->xmin = xMin; st->xmax = xMax; st->ymin = yMin; st->ymax = yMax;
-      st->dx = dx; st->dy = dy; st->inv_dx = __drcp_rn(dx); st->inv_dy = __drcp_rn(dy);
-      st->zmin = zMin; st->zmax = zMax; st->dz = dz; st->inv_dz = __drcp_rn(dz);
-      st->xy_ratio = xy;
-      // solver-shape check (SpaceChargeCalc2p5D.cc:208-216)
-      if (!set_solver) {
-        double sr = __ddiv_rn(__dsub_rn(st->sxmax, st->sxmin), __dsub_rn(st->symax, st->symin));
-        if (fabs(__dsub_rn(sr, xy)) > 0.00000001) set_solver = 1;
-      }
-      if (set_solver) {  // PoissonSolverFFT2D::setGridXY (PoissonSolverFFT2D.cc:103-111)
-        st->sxmin = xMin; st->sxmax = xMax; st->symin = yMin; st->symax = yMax;
-        st->sdx = dx; st->sdy = dy;
-        st->green_dirty = 1;
-      }
-      st->scale = log(__ddiv_rn(st->sdx, dx));  // PoissonSolverFFT2D.cc:213
-      st->inv_qscale = inv_qscale;
-      st->phi_absmax = 0ull;
-      st->lam_absmax = 0ull;
-    }
-    st->skip = skip;
-    s_skip = skip;
-  }
-  __syncthreads();
-  if (s_skip) return;
-  for (int i = threadIdx.x; i < nx * ny; i += blockDim.x) rho_acc[i] = (G)0;
-  for (int i = threadIdx.x; i < nz; i += blockDim.x) z_acc[i] = (G)0;
-}
-
-// Green function of the doubled grid (PoissonSolverFFT2D.cc:115-152); the
-// mirrored entries are recomputed with the identical expression, which gives
-// the same values the reference copies.
-__global__ void k_green_fill(const ScState* st, double* g, int nx2, int ny2) {
-  if (!st->green_dirty || st->skip) return;
+// Green function of the doubled grid (PoissonSolverFFT2D.cc:115-152): the
+// quadrant 0 <= iX <= nx2/2, 0 <= iY <= ny2/2 is evaluated and written to
+// its mirror images, as the reference copies it.  gate: run only when the
+// Green spectrum is marked dirty (0 inside a graph branch taken on that
+// flag).
+__global__ void k_green_fill(const ScState* st, double* g, int nx2, int ny2, int gate) {
+  if ((gate && !st->green_dirty) || st->skip) return;
   double sdx = st->sdx, sdy = st->sdy;
-  int tot = nx2 * ny2;
+  const int hx = nx2 / 2, hy = ny2 / 2;
+  const int qy = hy + 1;
+  int tot = (hx + 1) * qy;
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < tot; idx += gridDim.x * blockDim.x) {
-    int iX = idx / ny2, iY = idx % ny2;
-    int ex = iX <= nx2 / 2 ? iX : nx2 - iX;
-    int ey = iY <= ny2 / 2 ? iY : ny2 - iY;
+    int iX = idx / qy, iY = idx % qy;
     double v = 0.0;
-    if (ex != 0 || ey != 0) {
-      double rX = __dmul_rn((double)ex, sdx), rY = __dmul_rn((double)ey, sdy);
+    if (iX != 0 || iY != 0) {
+      double rX = __dmul_rn((double)iX, sdx), rY = __dmul_rn((double)iY, sdy);
       double r2 = __dadd_rn(__dmul_rn(rX, rX), __dmul_rn(rY, rY));
       v = __ddiv_rn(-log(r2), 2.0);
     }
-    g[idx] = v;
-  }
-}
-
-// Row transforms along y (length N = ny2) of two real rows per block:
-// z = a + i b, Z = FFT(z), A_k = (Z_k + conj Z_{N-k})/2, B_k = (Z_k - conj Z_{N-k})/(2i).
-// SRC 0: Green rows (double, full length, all nx2 rows, only when dirty)
-// SRC 1: plain rho from the fixed-point grid (first ny columns, first nx rows)
-// SRC 2: fp32 rho
-template <typename T, int SRC>
-__global__ void k_rows_fwd(const ScState* st, const void* src, double* rho_out, typename CT<T>::t* hat,
-                           const typename CT<T>::t* __restrict__ tw, FftPlan pl, int nrows, int ncols, int H) {
-  typedef typename CT<T>::t C;
-  if (SRC == 0 && !st->green_dirty) return;
-  if (st->skip) return;
-  extern __shared__ unsigned char smem_raw[];
-  C* a = reinterpret_cast<C*>(smem_raw);
-  C* b = a + pl.n;
-  const int N = pl.n;
-  int r0 = 2 * blockIdx.x, r1 = r0 + 1;
-  double iq = st->inv_qscale;
-  for (int j = threadIdx.x; j < N; j += blockDim.x) {
-    T va = (T)0, vb = (T)0;
-    if (j < ncols) {
-      if (SRC == 0) {
-        const double* g = (const double*)src;
-        va = (T)g[(size_t)r0 * N + j];
-        if (r1 < nrows) vb = (T)g[(size_t)r1 * N + j];
-      } else if (SRC == 1) {
-        const long long* q = (const long long*)src;
-        double da = (double)q[(size_t)r0 * ncols + j] * iq;
-        rho_out[(size_t)r0 * ncols + j] = da;
-        va = (T)da;
-        if (r1 < nrows) {
-          double db = (double)q[(size_t)r1 * ncols + j] * iq;
-          rho_out[(size_t)r1 * ncols + j] = db;
-          vb = (T)db;
-        }
-      } else {
-        const float* q = (const float*)src;
-        float fa = q[(size_t)r0 * ncols + j];
-        rho_out[(size_t)r0 * ncols + j] = (double)fa;
-        va = (T)fa;
-        if (r1 < nrows) {
-          float fb = q[(size_t)r1 * ncols + j];
-          rho_out[(size_t)r1 * ncols + j] = (double)fb;
-          vb = (T)fb;
-        }
-      }
-    }
-    C v;
-    v.x = va;
-    v.y = vb;
-    a[j] = v;
-  }
-  __syncthreads();
-  C* Z = block_fft<T>(a, b, pl, tw, false);
-  for (int k = threadIdx.x; k < H; k += blockDim.x) {
-    C zk = Z[k], zc = c_conj(Z[(N - k) % N]);
-    C A, B;
-    A.x = (zk.x + zc.x) * (T)0.5;
-    A.y = (zk.y + zc.y) * (T)0.5;
-    // (zk - zc) / (2i) = -i/2 (zk - zc)
-    B.x = (zk.y - zc.y) * (T)0.5;
-    B.y = -(zk.x - zc.x) * (T)0.5;
-    hat[(size_t)r0 * H + k] = A;
-    if (r1 < nrows) hat[(size_t)r1 * H + k] = B;
-  }
-}
-
-// Column transforms along x (length N = nx2), one column k per block.
-// MODE 0: forward transform of the Green columns in place (when dirty).
-// MODE 1: forward, multiply by the Green spectrum with the log-scale
-//         correction (PoissonSolverFFT2D.cc:212-242), backward; rows >= nin
-//         are zero on input and only rows < nin are kept on output.
-template <typename T, int MODE>
-__global__ void k_cols(const ScState* st, typename CT<T>::t* hat, const typename CT<T>::t* __restrict__ green,
-                       const typename CT<T>::t* __restrict__ tw, FftPlan pl, int nin, int H, int ny2) {
-  typedef typename CT<T>::t C;
-  if (MODE == 0 && !st->green_dirty) return;
-  if (st->skip) return;
-  extern __shared__ unsigned char smem_raw[];
-  C* a = reinterpret_cast<C*>(smem_raw);
-  C* b = a + pl.n;
-  const int N = pl.n;
-  const int k = blockIdx.x;
-  for (int r = threadIdx.x; r < N; r += blockDim.x) {
-    C v;
-    if (r < nin) v = hat[(size_t)r * H + k];
-    else { v.x = (T)0; v.y = (T)0; }
-    a[r] = v;
-  }
-  __syncthreads();
-  C* F = block_fft<T>(a, b, pl, tw, false);
-  if (MODE == 0) {
-    for (int r = threadIdx.x; r < N; r += blockDim.x) hat[(size_t)r * H + k] = F[r];
-    return;
-  }
-  double s = st->scale;
-  for (int r = threadIdx.x; r < N; r += blockDim.x) {
-    C g = green[(size_t)r * H + k];
-    T gr;
-    if (r == 0 && k == 0) {
-      double re00 = (double)g.x;
-      gr = (T)((re00 + s * (double)(N * ny2)) - s);
-    } else {
-      gr = (T)((double)g.x - s);
-    }
-    T gi = g.y;
-    C o = F[r], res;
-    res.x = o.x * gr - o.y * gi;
-    res.y = o.x * gi + o.y * gr;
-    F[r] = res;
-  }
-  __syncthreads();
-  C* other = (F == a) ? b : a;
-  C* R = block_fft<T>(F, other, pl, tw, true);
-  for (int r = threadIdx.x; r < nin; r += blockDim.x) hat[(size_t)r * H + k] = R[r];
-}
-
-// Backward row transforms (c2r, two rows per block) and the 1/(4 nx ny)
-// normalisation onto the nx x ny potential (PoissonSolverFFT2D.cc:244-255).
-// Imaginary parts at the self-conjugate k = 0 and k = N/2 are ignored.
-template <typename T>
-__global__ void k_rows_inv(ScState* st, const typename CT<T>::t* __restrict__ hat,
-                           const typename CT<T>::t* __restrict__ tw, FftPlan pl, int nrows, int ny, int H,
-                           double denom, double* phi, float* phi_f) {
-  typedef typename CT<T>::t C;
-  if (st->skip) return;
-  extern __shared__ unsigned char smem_raw[];
-  C* a = reinterpret_cast<C*>(smem_raw);
-  C* b = a + pl.n;
-  const int N = pl.n;
-  int r0 = 2 * blockIdx.x, r1 = r0 + 1;
-  bool has1 = r1 < nrows;
-  for (int k = threadIdx.x; k < N; k += blockDim.x) {
-    C A, B;
-    if (k < H) {
-      A = hat[(size_t)r0 * H + k];
-      B = has1 ? hat[(size_t)r1 * H + k] : C{(T)0, (T)0};
-      if (k == 0 || 2 * k == N) { A.y = (T)0; B.y = (T)0; }
-    } else {
-      A = c_conj(hat[(size_t)r0 * H + (N - k)]);
-      B = has1 ? c_conj(hat[(size_t)r1 * H + (N - k)]) : C{(T)0, (T)0};
-    }
-    C z;  // A + i B
-    z.x = A.x - B.y;
-    z.y = A.y + B.x;
-    a[k] = z;
-  }
-  __syncthreads();
-  C* R = block_fft<T>(a, b, pl, tw, true);
-  unsigned long long amax = 0ull;  // bits of max |phi| (non-negative doubles order like their bits)
-  for (int j = threadIdx.x; j < ny; j += blockDim.x) {
-    double va = denom * (double)R[j].x;
-    phi[(size_t)r0 * ny + j] = va;
-    if (phi_f) phi_f[(size_t)r0 * ny + j] = (float)va;
-    unsigned long long ba = (unsigned long long)__double_as_longlong(fabs(va));
-    amax = ba > amax ? ba : amax;
-    if (has1) {
-      double vb = denom * (double)R[j].y;
-      phi[(size_t)r1 * ny + j] = vb;
-      if (phi_f) phi_f[(size_t)r1 * ny + j] = (float)vb;
-      unsigned long long bb = (unsigned long long)__double_as_longlong(fabs(vb));
-      amax = bb > amax ? bb : amax;
+    int mX = nx2 - iX, mY = ny2 - iY;
+    g[(size_t)iX * ny2 + iY] = v;
+    if (iY > 0 && mY != iY) g[(size_t)iX * ny2 + mY] = v;
+    if (iX > 0 && mX != iX) {
+      g[(size_t)mX * ny2 + iY] = v;
+      if (iY > 0 && mY != iY) g[(size_t)mX * ny2 + mY] = v;
     }
   }
-  for (int off = 16; off > 0; off >>= 1) {
-    unsigned long long o = __shfl_xor_sync(0xffffffffu, amax, off);
-    amax = o > amax ? o : amax;
-  }
-  if ((threadIdx.x & 31) == 0 && amax) atomicMax(&st->phi_absmax, amax);
 }
 
-// Plain form: phi and lambda as 64-bit integers phi * 2^sphi, lambda *
-// 2^slam with the scales chosen from their maxima (below 2^61), read by the
-// fixed-point kick.
-__global__ void k_phi_fix(const ScState* st, const double* __restrict__ phi, const double* __restrict__ lam,
-                          long long* phi_fix, long long* lam_fix, int ng, int nz) {
-  if (st->skip) return;
-  int sphi = scale_bits(st->phi_absmax), slam = scale_bits(st->lam_absmax);
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < ng) phi_fix[i] = phi_fixed(phi[i], sphi);
-  if (i < nz) lam_fix[i] = phi_fixed(lam[i], slam);
-}
-
-// Line density to doubles, total macrosize, and the Green-rebuild flag reset.
+// Line density to doubles, total macrosize and the Green-rebuild flag
+// reset, run by one extra block of the forward row transforms (the deposit
+// is complete).  Inside a graph the old flag selects the branch that
+// rebuilds the Green spectrum (cond); the line density accumulator is
+// cleared for the next deposit.
 template <typename G>
-__global__ void k_finalize(ScState* st, const G* zacc, int nz, double* lam, float* lam_f) {
-  if (st->skip) return;
-  if (threadIdx.x == 0) st->green_dirty = 0;
+__device__ __noinline__ void finalize_block(ScState* st, G* zacc, int nz, double* lam, float* lam_f,
+                               cudaGraphConditionalHandle cond) {
+  if (threadIdx.x == 0) {
+    if (cond) cudaGraphSetConditional(cond, st->green_dirty ? 1u : 0u);
+    st->green_dirty = 0;
+  }
   __shared__ double s_part[32];
   double iq = st->inv_qscale;
   double acc = 0.0;
   long long iacc = 0;
   unsigned long long amax = 0ull;
   for (int k = threadIdx.x; k < nz; k += blockDim.x) {
+    G g = zacc[k];
+    zacc[k] = (G)0;
     double v;
     if (sizeof(G) == 8) {
-      long long q = (long long)zacc[k];
+      long long q = (long long)g;
       iacc += q;
       v = (double)q * iq;
     } else {
-      v = (double)zacc[k];
+      v = (double)g;
       acc += v;
     }
     lam[k] = v;
@@ -371,13 +135,226 @@ __global__ void k_finalize(ScState* st, const G* zacc, int nz, double* lam, floa
   }
 }
 
+// Row transforms along y (length N = ny2) of two real rows per block:
+// z = a + i b, Z = FFT(z), A_k = (Z_k + conj Z_{N-k})/2, B_k = (Z_k - conj Z_{N-k})/(2i).
+// SRC 0: Green rows (double, full length; rows 0..nx2/2 transformed, the
+//        rest mirrored; nrows = nx2/2 + 1)
+// SRC 1: plain rho from the fixed-point grid (first ny columns, first nx rows)
+// SRC 2: fp32 rho
+// The deposit grid (SRC 1, 2) is cleared as it is read, ready for the next
+// deposit, and one extra block (the last) finalizes the line density.
+// gate (SRC 0): as for k_green_fill.
+template <typename T, int SRC>
+__global__ void k_rows_fwd(ScState* st, void* src, double* rho_out, typename CT<T>::t* hat,
+                           const typename CT<T>::t* __restrict__ tw, FftPlan pl, int nrows, int ncols, int H,
+                           int gate, void* zacc, int nz, double* lam, float* lam_f,
+                           cudaGraphConditionalHandle cond) {
+  typedef typename CT<T>::t C;
+  if (SRC == 0 && gate && !st->green_dirty) return;
+  if (st->skip) return;
+  if (SRC != 0 && blockIdx.x == gridDim.x - 1) {
+    if (SRC == 1) finalize_block(st, (unsigned long long*)zacc, nz, lam, (float*)nullptr, cond);
+    else finalize_block(st, (float*)zacc, nz, lam, lam_f, cond);
+    return;
+  }
+  extern __shared__ unsigned char smem_raw[];
+  C* a = reinterpret_cast<C*>(smem_raw);
+  C* b = a + pl.n;
+  const int N = pl.n;
+  C* stw = b + N;
+  load_twiddles(stw, tw, N);
+  int r0 = 2 * blockIdx.x, r1 = r0 + 1;
+  double iq = st->inv_qscale;
+  for (int j = threadIdx.x; j < N; j += blockDim.x) {
+    T va = (T)0, vb = (T)0;
+    if (j < ncols) {
+      if (SRC == 0) {
+        const double* g = (const double*)src;
+        va = (T)g[(size_t)r0 * N + j];
+        if (r1 < nrows) vb = (T)g[(size_t)r1 * N + j];
+      } else if (SRC == 1) {
+        long long* q = (long long*)src;
+        double da = (double)q[(size_t)r0 * ncols + j] * iq;
+        q[(size_t)r0 * ncols + j] = 0;
+        rho_out[(size_t)r0 * ncols + j] = da;
+        va = (T)da;
+        if (r1 < nrows) {
+          double db = (double)q[(size_t)r1 * ncols + j] * iq;
+          q[(size_t)r1 * ncols + j] = 0;
+          rho_out[(size_t)r1 * ncols + j] = db;
+          vb = (T)db;
+        }
+      } else {
+        float* q = (float*)src;
+        float fa = q[(size_t)r0 * ncols + j];
+        q[(size_t)r0 * ncols + j] = 0.0f;
+        rho_out[(size_t)r0 * ncols + j] = (double)fa;
+        va = (T)fa;
+        if (r1 < nrows) {
+          float fb = q[(size_t)r1 * ncols + j];
+          q[(size_t)r1 * ncols + j] = 0.0f;
+          rho_out[(size_t)r1 * ncols + j] = (double)fb;
+          vb = (T)fb;
+        }
+      }
+    }
+    C v;
+    v.x = va;
+    v.y = vb;
+    a[j] = v;
+  }
+  __syncthreads();
+  C* Z = block_fft<T>(a, b, pl, stw, false);
+  for (int k = threadIdx.x; k < H; k += blockDim.x) {
+    C zk = Z[k], zc = c_conj(Z[(N - k) % N]);
+    C A, B;
+    A.x = (zk.x + zc.x) * (T)0.5;
+    A.y = (zk.y + zc.y) * (T)0.5;
+    // (zk - zc) / (2i) = -i/2 (zk - zc)
+    B.x = (zk.y - zc.y) * (T)0.5;
+    B.y = -(zk.x - zc.x) * (T)0.5;
+    hat[(size_t)r0 * H + k] = A;
+    if (r1 < nrows) hat[(size_t)r1 * H + k] = B;
+    if (SRC == 0) {
+      // Green rows 0..nrows-1 = 0..nx2/2; row nx2 - r repeats row r
+      const int nfull = 2 * (nrows - 1);
+      if (r0 > 0 && r0 < nrows - 1) hat[(size_t)(nfull - r0) * H + k] = A;
+      if (r1 < nrows - 1) hat[(size_t)(nfull - r1) * H + k] = B;
+    }
+  }
+}
+
+// Column transforms along x (length N = nx2), one column k per block.
+// The Green spectrum is stored column by column (green[k * N + r]).
+// MODE 0: forward transform of the Green columns (when dirty), hat -> green.
+// MODE 1: forward, multiply by the Green spectrum with the log-scale
+//         correction (PoissonSolverFFT2D.cc:212-242), backward; rows >= nin
+//         are zero on input and only rows < nin are kept on output.
+template <typename T, int MODE>
+__global__ void k_cols(const ScState* st, typename CT<T>::t* hat, typename CT<T>::t* __restrict__ green,
+                       const typename CT<T>::t* __restrict__ tw, FftPlan pl, int nin, int H, int ny2, int gate) {
+  typedef typename CT<T>::t C;
+  if (MODE == 0 && gate && !st->green_dirty) return;
+  if (st->skip) return;
+  extern __shared__ unsigned char smem_raw[];
+  C* a = reinterpret_cast<C*>(smem_raw);
+  C* b = a + pl.n;
+  const int N = pl.n;
+  C* stw = b + N;
+  load_twiddles(stw, tw, N);
+  const int k = blockIdx.x;
+  for (int r = threadIdx.x; r < N; r += blockDim.x) {
+    C v;
+    if (r < nin) v = hat[(size_t)r * H + k];
+    else { v.x = (T)0; v.y = (T)0; }
+    a[r] = v;
+  }
+  __syncthreads();
+  C* F = block_fft<T>(a, b, pl, stw, false);
+  if (MODE == 0) {
+    for (int r = threadIdx.x; r < N; r += blockDim.x) green[(size_t)k * N + r] = F[r];
+    return;
+  }
+  double s = st->scale;
+  for (int r = threadIdx.x; r < N; r += blockDim.x) {
+    C g = green[(size_t)k * N + r];
+    T gr;
+    if (r == 0 && k == 0) {
+      double re00 = (double)g.x;
+      gr = (T)((re00 + s * (double)(N * ny2)) - s);
+    } else {
+      gr = (T)((double)g.x - s);
+    }
+    T gi = g.y;
+    C o = F[r], res;
+    res.x = o.x * gr - o.y * gi;
+    res.y = o.x * gi + o.y * gr;
+    F[r] = res;
+  }
+  __syncthreads();
+  C* other = (F == a) ? b : a;
+  C* R = block_fft<T>(F, other, pl, stw, true);
+  for (int r = threadIdx.x; r < nin; r += blockDim.x) hat[(size_t)r * H + k] = R[r];
+}
+
+// Backward row transforms (c2r, two rows per block) and the 1/(4 nx ny)
+// normalisation onto the nx x ny potential (PoissonSolverFFT2D.cc:244-255).
+// Imaginary parts at the self-conjugate k = 0 and k = N/2 are ignored.
+template <typename T>
+__global__ void k_rows_inv(ScState* st, const typename CT<T>::t* __restrict__ hat,
+                           const typename CT<T>::t* __restrict__ tw, FftPlan pl, int nrows, int ny, int H,
+                           double denom, double* phi, float* phi_f) {
+  typedef typename CT<T>::t C;
+  if (st->skip) return;
+  extern __shared__ unsigned char smem_raw[];
+  C* a = reinterpret_cast<C*>(smem_raw);
+  C* b = a + pl.n;
+  const int N = pl.n;
+  C* stw = b + N;
+  load_twiddles(stw, tw, N);
+  int r0 = 2 * blockIdx.x, r1 = r0 + 1;
+  bool has1 = r1 < nrows;
+  for (int k = threadIdx.x; k < N; k += blockDim.x) {
+    C A, B;
+    if (k < H) {
+      A = hat[(size_t)r0 * H + k];
+      B = has1 ? hat[(size_t)r1 * H + k] : C{(T)0, (T)0};
+      if (k == 0 || 2 * k == N) { A.y = (T)0; B.y = (T)0; }
+    } else {
+      A = c_conj(hat[(size_t)r0 * H + (N - k)]);
+      B = has1 ? c_conj(hat[(size_t)r1 * H + (N - k)]) : C{(T)0, (T)0};
+    }
+    C z;  // A + i B
+    z.x = A.x - B.y;
+    z.y = A.y + B.x;
+    a[k] = z;
+  }
+  __syncthreads();
+  C* R = block_fft<T>(a, b, pl, stw, true);
+  unsigned long long amax = 0ull;  // bits of max |phi| (non-negative doubles order like their bits)
+  for (int j = threadIdx.x; j < ny; j += blockDim.x) {
+    double va = denom * (double)R[j].x;
+    phi[(size_t)r0 * ny + j] = va;
+    if (phi_f) phi_f[(size_t)r0 * ny + j] = (float)va;
+    unsigned long long ba = (unsigned long long)__double_as_longlong(fabs(va));
+    amax = ba > amax ? ba : amax;
+    if (has1) {
+      double vb = denom * (double)R[j].y;
+      phi[(size_t)r1 * ny + j] = vb;
+      if (phi_f) phi_f[(size_t)r1 * ny + j] = (float)vb;
+      unsigned long long bb = (unsigned long long)__double_as_longlong(fabs(vb));
+      amax = bb > amax ? bb : amax;
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    unsigned long long o = __shfl_xor_sync(0xffffffffu, amax, off);
+    amax = o > amax ? o : amax;
+  }
+  if ((threadIdx.x & 31) == 0 && amax) atomicMax(&st->phi_absmax, amax);
+}
+
+// Plain form: phi and lambda as 64-bit integers phi * 2^sphi, lambda *
+// 2^slam with the scales chosen from their maxima (below 2^61), read by the
+// fixed-point kick.
+__global__ void k_phi_fix(const ScState* st, const double* __restrict__ phi, const double* __restrict__ lam,
+                          long long* phi_fix, long long* lam_fix, int ng, int nz) {
+  if (st->skip) return;
+  int sphi = scale_bits(st->phi_absmax), slam = scale_bits(st->lam_absmax);
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < ng) phi_fix[i] = phi_fixed(phi[i], sphi);
+  if (i < nz) lam_fix[i] = phi_fixed(lam[i], slam);
+}
+
 // Deposit, plain form.  SMEM: block-private fixed-point grids in shared
 // memory, flushed with one 64-bit atomic per non-zero cell.  With K > 0
 // (uniform macrosize) each particle deposits unit weight in units of 2^-K
 // through the integer path (deposit_fixed); otherwise, and for the rare
 // particle the integer path declines, macrosize * qscale through FP64.
+// Blocks of up to 768 threads (80 registers: 24 warps per SM) cover the
+// latency of the shared-memory atomics; 1024 threads at 64 registers spill
+// and ran slower.
 template <bool SMEM>
-__global__ void k_deposit_plain(const double* __restrict__ x, const double* __restrict__ y,
+__global__ void __launch_bounds__(768) k_deposit_plain(const double* __restrict__ x, const double* __restrict__ y,
                                 const double* __restrict__ z, const double* __restrict__ msize, int n,
                                 const ScState* st, unsigned long long* g_rho, unsigned long long* g_z,
                                 double ms_uniform, double qscale, int nx, int ny, int nz, int K) {
@@ -465,8 +442,9 @@ __global__ void k_kick_plain(const double* __restrict__ x, double* __restrict__ 
   const long long* P = phi_fix;
   const long long* Lm = lam_fix;
   if (SMEM) {
-    for (int i = threadIdx.x; i < nx * ny; i += blockDim.x) s_phix[i] = phi_fix[i];
-    for (int i = threadIdx.x; i < nz; i += blockDim.x) s_phix[nx * ny + i] = lam_fix[i];
+    // the shared copy is converted here; phi_fix, lam_fix are not read
+    for (int i = threadIdx.x; i < nx * ny; i += blockDim.x) s_phix[i] = phi_fixed(phi[i], kf.sphi);
+    for (int i = threadIdx.x; i < nz; i += blockDim.x) s_phix[nx * ny + i] = phi_fixed(lam[i], kf.slam);
     __syncthreads();
     P = s_phix;
     Lm = s_phix + nx * ny;
@@ -570,10 +548,17 @@ static void* make_twiddles(int n, cudaError_t* err) {
   return d;
 }
 
-static int fft_threads(int n) { return n >= 1024 ? 512 : (n >= 256 ? 256 : 128); }
+// Power-of-two lengths: one thread per radix-2 butterfly (N/2, at least a
+// warp, at most 1024, above which the stages are radix 4); other lengths: a
+// fixed block for the generic stages.
+static int fft_threads(const FftPlan& pl) {
+  int n = pl.n;
+  if (pl.pow2) return n / 2 >= 32 ? (n / 2 > 1024 ? 1024 : n / 2) : 32;
+  return n >= 1024 ? 512 : (n >= 256 ? 256 : 128);
+}
 
 template <typename T>
-static size_t fft_smem(int n) { return 2 * sizeof(typename CT<T>::t) * (size_t)n; }
+static size_t fft_smem(int n) { return 3 * sizeof(typename CT<T>::t) * (size_t)n; }  // a, b, twiddles
 
 template <typename T>
 static int set_fft_attrs(int nmax) {
@@ -606,57 +591,80 @@ static void particle_geometry(size_t smem, int n, int max_threads, int* blocks, 
   *blocks = need < b ? (need < 1 ? 1 : need) : b;
 }
 
+// Forward row transforms of the deposit (plus one block finalizing the line
+// density; inside a graph it sets `cond`, the Green-rebuild branch).
 template <typename T>
-static int enqueue_solve(orbit_sc2p5d_t* c, cudaStream_t s, int* nl) {
+static int enqueue_rows_fwd(orbit_sc2p5d_t* c, cudaStream_t s, cudaGraphConditionalHandle cond, int* nl) {
+  typedef typename CT<T>::t C;
+  C* hat = (C*)c->d_hat;
+  const C* twy = (const C*)c->d_tw_y;
+  int thy = fft_threads(c->plan_y);
+  size_t smy = fft_smem<T>(c->ny2);
+  int blocks = (c->nx + 1) / 2 + 1;
+  ORBIT_PB("fft_rows_fwd", s);
+  if (c->form == ORBIT_FORM_PLAIN) {
+    k_rows_fwd<T, 1><<<blocks, thy, smy, s>>>(c->d_st, c->d_rho_q, c->d_rho, hat, twy, c->plan_y, c->nx, c->ny,
+                                              c->H, 1, c->d_z_q, c->nz, c->d_lam, nullptr, cond);
+  } else {
+    k_rows_fwd<T, 2><<<blocks, thy, smy, s>>>(c->d_st, c->d_rho_f, c->d_rho, hat, twy, c->plan_y, c->nx, c->ny,
+                                              c->H, 1, c->d_z_f, c->nz, c->d_lam, c->d_lam_f, cond);
+  }
+  ORBIT_PE(s);
+  ++*nl;
+  ORBIT_LAUNCH_CHECK("sc2p5d rows");
+  return ORBIT_OK;
+}
+
+// Column transforms with the Green multiply, then the backward rows.
+template <typename T>
+static int enqueue_conv(orbit_sc2p5d_t* c, cudaStream_t s, int* nl) {
   typedef typename CT<T>::t C;
   C* hat = (C*)c->d_hat;
   C* green = (C*)c->d_green;
   const C* twx = (const C*)c->d_tw_x;
   const C* twy = (const C*)c->d_tw_y;
-  int thx = fft_threads(c->nx2), thy = fft_threads(c->ny2);
+  int thx = fft_threads(c->plan_x), thy = fft_threads(c->plan_y);
   size_t smx = fft_smem<T>(c->nx2), smy = fft_smem<T>(c->ny2);
   double denom = 1.0 / (c->nx2 * c->ny2);
-  ORBIT_PB("fft_rows_fwd", s);
-  if (c->form == ORBIT_FORM_PLAIN) {
-    k_rows_fwd<T, 1><<<(c->nx + 1) / 2, thy, smy, s>>>(c->d_st, c->d_rho_q, c->d_rho, hat, twy, c->plan_y, c->nx,
-                                                        c->ny, c->H);
-  } else {
-    k_rows_fwd<T, 2><<<(c->nx + 1) / 2, thy, smy, s>>>(c->d_st, c->d_rho_f, c->d_rho, hat, twy, c->plan_y, c->nx,
-                                                        c->ny, c->H);
-  }
-  ORBIT_PE(s);
   ORBIT_PB("fft_cols_conv", s);
-  k_cols<T, 1><<<c->H, thx, smx, s>>>(c->d_st, hat, green, twx, c->plan_x, c->nx, c->H, c->ny2);
+  k_cols<T, 1><<<c->H, thx, smx, s>>>(c->d_st, hat, green, twx, c->plan_x, c->nx, c->H, c->ny2, 1);
   ORBIT_PE(s);
   ORBIT_PB("fft_rows_inv", s);
   k_rows_inv<T><<<(c->nx + 1) / 2, thy, smy, s>>>(c->d_st, hat, twy, c->plan_y, c->nx, c->ny, c->H, denom,
                                                    c->d_phi, c->d_phi_f);
   ORBIT_PE(s);
-  *nl += 3;
+  *nl += 2;
   ORBIT_LAUNCH_CHECK("sc2p5d solve");
   return ORBIT_OK;
 }
 
+// Green spectrum rebuild.  gate = 1: the kernels return unless the spectrum
+// is marked dirty (eager calls); 0: unconditional (the body of a graph
+// branch taken on the flag).  `scratch` (nx2 x H complex) holds the row
+// spectra.  The Green function is even in x and y: one quadrant is
+// evaluated and mirrored, and rows 0..nx are transformed and mirrored.
 template <typename T>
-static int enqueue_green(orbit_sc2p5d_t* c, cudaStream_t s, int* nl) {
+static int enqueue_green(orbit_sc2p5d_t* c, cudaStream_t s, int gate, void* scratch, int* nl) {
   typedef typename CT<T>::t C;
   C* green = (C*)c->d_green;
   const C* twx = (const C*)c->d_tw_x;
   const C* twy = (const C*)c->d_tw_y;
-  int thx = fft_threads(c->nx2), thy = fft_threads(c->ny2);
+  int thx = fft_threads(c->plan_x), thy = fft_threads(c->plan_y);
   size_t smx = fft_smem<T>(c->nx2), smy = fft_smem<T>(c->ny2);
-  int tot = c->nx2 * c->ny2;
-  int gb = (tot + 255) / 256;
+  int quad = (c->nx + 1) * (c->ny + 1);
+  int gb = (quad + 255) / 256;
   if (gb > num_sms() * 4) gb = num_sms() * 4;
   ORBIT_PB("green_fill", s);
-  k_green_fill<<<gb, 256, 0, s>>>(c->d_st, c->d_gbuf, c->nx2, c->ny2);
+  k_green_fill<<<gb, 256, 0, s>>>(c->d_st, c->d_gbuf, c->nx2, c->ny2, gate);
   ORBIT_PE(s);
   ORBIT_PB("green_rows", s);
-  k_rows_fwd<T, 0><<<c->nx2 / 2, thy, smy, s>>>(c->d_st, c->d_gbuf, nullptr, green, twy, c->plan_y, c->nx2,
-                                                 c->ny2, c->H);
+  C* hat = (C*)scratch;
+  k_rows_fwd<T, 0><<<(c->nx + 2) / 2, thy, smy, s>>>(c->d_st, c->d_gbuf, nullptr, hat, twy, c->plan_y,
+                                                      c->nx + 1, c->ny2, c->H, gate, nullptr, 0, nullptr, nullptr,
+                                                      0);
   ORBIT_PE(s);
   ORBIT_PB("green_cols", s);
-  k_cols<T, 0><<<c->H, thx, smx, s>>>(c->d_st, green, nullptr, twx, c->plan_x, c->nx2, c->H, c->ny2);
+  k_cols<T, 0><<<c->H, thx, smx, s>>>(c->d_st, hat, green, twx, c->plan_x, c->nx2, c->H, c->ny2, gate);
   ORBIT_PE(s);
   *nl += 3;
   ORBIT_LAUNCH_CHECK("sc2p5d green");
@@ -690,45 +698,98 @@ static double qscale_for(double msum_abs) {
   return std::ldexp(1.0, 61 - e);
 }
 
+// Fixed-point units of the plain deposit.  Uniform macrosize: unit weight
+// in units of 2^-K with 4 n 2^K < 2^62 (a particle's |weights| sum to at
+// most 4), the macrosize multiplies the grid afterwards.  Per-particle
+// macrosizes: macrosize * S with S * sum|m| <= 2^61.
+DepScales sc_dep_scales(const orbit_sc2p5d_t* c, const orbit_bunch_t* b) {
+  (void)c;
+  DepScales d;
+  d.K = 0;
+  d.S = 1.0;
+  d.inv_q = 1.0;
+  d.ms_uniform = 0.0;
+  if (!b->has_msize) {
+    int e = 0;
+    std::frexp(4.0 * (double)(b->n > 0 ? b->n : 1), &e);  // 4n < 2^e
+    d.K = 62 - e;
+    if (d.K > 55) d.K = 55;
+    d.ms_uniform = std::ldexp(1.0, d.K);
+    d.inv_q = std::ldexp(b->sync.macrosize, -d.K);
+  } else {
+    d.S = qscale_for(b->msize_abs_sum);
+    d.inv_q = 1.0 / d.S;
+  }
+  return d;
+}
+
+SetupArgs sc_setup_args(const orbit_sc2p5d_t* c, const DepScales& d) {
+  SetupArgs sa;
+  sa.inv_qscale = c->form == ORBIT_FORM_PLAIN ? d.inv_q : 1.0;
+  sa.nx = c->nx;
+  sa.ny = c->ny;
+  sa.nz = c->nz;
+  return sa;
+}
+
+// Inside a stream capture: a conditional graph node after the forward row
+// transforms whose body rebuilds the Green spectrum (into its own scratch:
+// the work spectrum is in use); their finalizing block takes it when the
+// spectrum is dirty.  The body is captured on the calculator's own stream.
+static int add_green_branch(orbit_sc2p5d_t* c, cudaStream_t s, cudaGraphConditionalHandle cond) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  ORBIT_CUDA(cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, &deps, nullptr, &nd));
+  cudaGraphNodeParams p = {};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = cond;
+  p.conditional.type = cudaGraphCondTypeIf;
+  p.conditional.size = 1;
+  cudaGraphNode_t node;
+  ORBIT_CUDA(cudaGraphAddNode(&node, g, deps, nullptr, nd, &p));
+  cudaGraph_t body = p.conditional.phGraph_out[0];
+  ORBIT_CUDA(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  ORBIT_CUDA(cudaStreamBeginCaptureToGraph(c->aux, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  int bl = 0;
+  int rc = c->form == ORBIT_FORM_PLAIN ? enqueue_green<double>(c, c->aux, 0, c->d_gscratch, &bl)
+                                       : enqueue_green<float>(c, c->aux, 0, c->d_gscratch, &bl);
+  cudaGraph_t out = nullptr;
+  cudaError_t e = cudaStreamEndCapture(c->aux, &out);
+  if (rc) return rc;
+  if (e != cudaSuccess) return cuda_error(e, "sc2p5d: Green branch capture");
+  return ORBIT_OK;
+}
+
 int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStream_t s, bool do_extrema,
                     bool do_kick, int* launches) {
   int nl = 0;
   const int n = b->n;
+  const double* msz = b->has_msize ? b->d_msize : nullptr;
+  const bool plain = c->form == ORBIT_FORM_PLAIN;
+  const DepScales ds = sc_dep_scales(c, b);
   if (do_extrema) {
+    // the grid set-up runs in the scan's last block
     ORBIT_PB("extrema", s);
-    k_extrema<<<ext_blocks(n), 256, 0, s>>>(b->coord(0), b->coord(2), b->coord(4), n, c->d_st, b->d_status);
+    k_extrema<<<ext_blocks(n), 256, 0, s>>>(b->coord(0), b->coord(2), b->coord(4), n, c->d_st, b->d_status,
+                                            sc_setup_args(c, ds));
     ORBIT_PE(s);
     ++nl;
   }
-  // Fixed-point units of the plain deposit.  Uniform macrosize: unit weight
-  // in units of 2^-K with 4 n 2^K < 2^62 (a particle's |weights| sum to at
-  // most 4), the macrosize multiplies the grid afterwards.  Per-particle
-  // macrosizes: macrosize * S with S * sum|m| <= 2^61.
-  const double* msz = b->has_msize ? b->d_msize : nullptr;
-  const bool plain = c->form == ORBIT_FORM_PLAIN;
-  int K = 0;
-  double S = 1.0, inv_q = 1.0, ms_uniform = 0.0;
-  if (!b->has_msize) {
-    int e = 0;
-    std::frexp(4.0 * (double)(n > 0 ? n : 1), &e);  // 4n < 2^e
-    K = 62 - e;
-    if (K > 55) K = 55;
-    ms_uniform = std::ldexp(1.0, K);
-    inv_q = std::ldexp(b->sync.macrosize, -K);
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaGraph_t cg = nullptr;
+  ORBIT_CUDA(cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg, nullptr, nullptr, nullptr));
+  const bool branch = cs == cudaStreamCaptureStatusActive && c->aux != nullptr && c->d_gscratch != nullptr;
+  cudaGraphConditionalHandle cond = 0;
+  int rc;
+  if (branch) {
+    ORBIT_CUDA(cudaGraphConditionalHandleCreate(&cond, cg, 0, cudaGraphCondAssignDefault));
   } else {
-    S = qscale_for(b->msize_abs_sum);
-    inv_q = 1.0 / S;
+    // before the deposit: the work spectrum is free to hold the row spectra
+    rc = plain ? enqueue_green<double>(c, s, 1, c->d_hat, &nl) : enqueue_green<float>(c, s, 1, c->d_hat, &nl);
+    if (rc) return rc;
   }
-  ORBIT_PB("setup", s);
-  if (plain)
-    k_setup<unsigned long long><<<1, 256, 0, s>>>(c->d_st, b->d_status, c->nx, c->ny, c->nz, inv_q, c->d_rho_q,
-                                                  c->d_z_q);
-  else
-    k_setup<float><<<1, 256, 0, s>>>(c->d_st, b->d_status, c->nx, c->ny, c->nz, 1.0, c->d_rho_f, c->d_z_f);
-  ORBIT_PE(s);
-  ++nl;
-  int rc = plain ? enqueue_green<double>(c, s, &nl) : enqueue_green<float>(c, s, &nl);
-  if (rc) return rc;
   size_t esz = plain ? sizeof(unsigned long long) : sizeof(float);
   size_t sm = esz * ((size_t)c->nx * c->ny + c->nz);
   int blocks, threads;
@@ -739,12 +800,12 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
   if (plain) {
     if (c->smem_deposit)
       k_deposit_plain<true><<<blocks, threads, sm, s>>>(b->coord(0), b->coord(2), b->coord(4), msz, n, c->d_st,
-                                                        c->d_rho_q, c->d_z_q, ms_uniform, S, c->nx, c->ny, c->nz,
-                                                        K);
+                                                        c->d_rho_q, c->d_z_q, ds.ms_uniform, ds.S, c->nx, c->ny,
+                                                        c->nz, ds.K);
     else
       k_deposit_plain<false><<<blocks, threads, 0, s>>>(b->coord(0), b->coord(2), b->coord(4), msz, n, c->d_st,
-                                                        c->d_rho_q, c->d_z_q, ms_uniform, S, c->nx, c->ny, c->nz,
-                                                        K);
+                                                        c->d_rho_q, c->d_z_q, ds.ms_uniform, ds.S, c->nx, c->ny,
+                                                        c->nz, ds.K);
   } else {
     if (c->smem_deposit)
       k_deposit_fp32<true><<<blocks, threads, sm, s>>>(b->coord(0), b->coord(2), b->coord(4), msz, n, c->d_st,
@@ -756,17 +817,19 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
                                                        c->ny, c->nz);
   }
   ORBIT_PE(s);
-  ORBIT_PB("finalize", s);
-  if (plain)
-    k_finalize<unsigned long long><<<1, 256, 0, s>>>(c->d_st, c->d_z_q, c->nz, c->d_lam, nullptr);
-  else
-    k_finalize<float><<<1, 256, 0, s>>>(c->d_st, c->d_z_f, c->nz, c->d_lam, c->d_lam_f);
-  ORBIT_PE(s);
-  nl += 2;
+  ++nl;
   ORBIT_LAUNCH_CHECK("sc2p5d deposit");
-  rc = plain ? enqueue_solve<double>(c, s, &nl) : enqueue_solve<float>(c, s, &nl);
+  rc = plain ? enqueue_rows_fwd<double>(c, s, cond, &nl) : enqueue_rows_fwd<float>(c, s, cond, &nl);
   if (rc) return rc;
-  if (plain) {
+  if (branch) {
+    rc = add_green_branch(c, s, cond);
+    if (rc) return rc;
+  }
+  rc = plain ? enqueue_conv<double>(c, s, &nl) : enqueue_conv<float>(c, s, &nl);
+  if (rc) return rc;
+  if (plain && !c->smem_kick) {
+    // kicks that read the potential from global memory take it converted
+    // once; the shared-memory kicks convert their own copy
     int ng = c->nx * c->ny;
     int m = ng > c->nz ? ng : c->nz;
     ORBIT_PB("phi_fix", s);
@@ -872,6 +935,7 @@ int orbit_sc2p5d_create(orbit_sc2p5d_t** out, int nx, int ny, int nz, double xy_
     if (e == cudaSuccess) e = cudaMemset(*p, 0, bytes);
   };
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->done, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking);
   A((void**)&c->d_st, sizeof(ScState));
   A((void**)&c->d_rho, sizeof(double) * ng);
   A((void**)&c->d_phi, sizeof(double) * ng);
@@ -884,6 +948,7 @@ int orbit_sc2p5d_create(orbit_sc2p5d_t** out, int nx, int ny, int nz, double xy_
     A((void**)&c->d_lam_fix, sizeof(long long) * nz);
     A(&c->d_hat, sizeof(double2) * nhat);
     A(&c->d_green, sizeof(double2) * nhat);
+    A(&c->d_gscratch, sizeof(double2) * nhat);
     if (e == cudaSuccess) c->d_tw_x = make_twiddles<double>(c->nx2, &e);
     if (e == cudaSuccess) c->d_tw_y = make_twiddles<double>(c->ny2, &e);
   } else {
@@ -893,6 +958,7 @@ int orbit_sc2p5d_create(orbit_sc2p5d_t** out, int nx, int ny, int nz, double xy_
     A((void**)&c->d_lam_f, sizeof(float) * nz);
     A(&c->d_hat, sizeof(float2) * nhat);
     A(&c->d_green, sizeof(float2) * nhat);
+    A(&c->d_gscratch, sizeof(float2) * nhat);
     if (e == cudaSuccess) c->d_tw_x = make_twiddles<float>(c->nx2, &e);
     if (e == cudaSuccess) c->d_tw_y = make_twiddles<float>(c->ny2, &e);
   }
@@ -934,8 +1000,9 @@ int orbit_sc2p5d_destroy(orbit_sc2p5d_t* c) {
   if (!c) return ORBIT_OK;
   if (c->used) cudaEventSynchronize(c->done);
   if (c->done) cudaEventDestroy(c->done);
+  if (c->aux) cudaStreamDestroy(c->aux);
   void* ptrs[] = {c->d_st, c->d_rho_q, c->d_z_q, c->d_rho_f, c->d_z_f, c->d_rho, c->d_phi, c->d_lam,
-                  c->d_phi_f, c->d_lam_f, c->d_hat, c->d_green, c->d_gbuf, c->d_tw_x, c->d_tw_y,
+                  c->d_phi_f, c->d_lam_f, c->d_hat, c->d_green, c->d_gbuf, c->d_gscratch, c->d_tw_x, c->d_tw_y,
                   c->d_phi_fix, c->d_lam_fix};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -1135,6 +1202,10 @@ extern "C" int orbit_sc2p5d_track_static(double* dev_coords, int n, int stride, 
   fill_twiddles_host<double>(c.ny2, twy);
   ORBIT_CUDA(cudaMemcpyAsync(c.d_st, &h, sizeof(h), cudaMemcpyHostToDevice, s));
   ORBIT_CUDA(cudaMemsetAsync(d_status, 0, sizeof(unsigned), s));
+  // the deposit grids start at zero (a kick leaves them cleared, an
+  // interrupted one might not)
+  ORBIT_CUDA(cudaMemsetAsync(c.d_rho_q, 0, 8 * ng, s));
+  ORBIT_CUDA(cudaMemsetAsync(c.d_z_q, 0, 8 * (size_t)nz, s));
   ORBIT_CUDA(cudaMemcpyAsync(c.d_tw_x, twx, sizeof(double2) * c.nx2, cudaMemcpyHostToDevice, s));
   ORBIT_CUDA(cudaMemcpyAsync(c.d_tw_y, twy, sizeof(double2) * c.ny2, cudaMemcpyHostToDevice, s));
   rc = init_attrs(&c);

@@ -26,11 +26,26 @@ struct ScState {
   unsigned long long phi_absmax;                          // bits of max |phi| (non-negative doubles
   unsigned long long lam_absmax;                          //  order like their bit patterns), max |lambda|
   int dep_k;                                              // fraction bits of the integer deposit (0: FP64 path)
+  unsigned ext_count;                                     // blocks done with the extrema scan (last one sets up)
+};
+
+// Arguments of the grid set-up run at the end of the extrema scan.
+struct SetupArgs {
+  double inv_qscale;  // macrosize per unit of the fixed-point deposit (1 for the fp32 form)
+  int nx, ny, nz;
+};
+
+// Units of the plain-form deposit for one bunch: K > 0 (uniform macrosize)
+// deposits unit weights in units of 2^-K, else macrosize * S through FP64.
+struct DepScales {
+  int K;
+  double S, inv_q, ms_uniform;
 };
 
 struct FftPlan {
   int n;
   int nst;
+  int pow2;  // n is a power of two: radix-4 stages and at most one radix-2
   int rad[24];
 };
 
@@ -55,11 +70,13 @@ struct orbit_sc2p5d {
   void* d_hat = nullptr;                  // nx2 * H complex work spectrum (T = double or float)
   void* d_green = nullptr;                // nx2 * H complex Green spectrum
   double* d_gbuf = nullptr;               // nx2 * ny2 real Green function
+  void* d_gscratch = nullptr;             // nx2 * H complex: Green row spectra inside a graph
   void* d_tw_x = nullptr;                 // twiddles for N = nx2
   void* d_tw_y = nullptr;                 // twiddles for N = ny2
   orbit::FftPlan plan_x{}, plan_y{};
   cudaEvent_t done = nullptr;    // recorded after the last work that used the buffers
   bool used = false;
+  cudaStream_t aux = nullptr;    // captures the Green-rebuild graph branch
   bool smem_deposit = false, smem_kick = false;
   int dep_threads = 512, kick_threads = 512;
 };
@@ -76,6 +93,8 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
 // for the last recorded use, then records a new one.
 cudaError_t sc_order_before(orbit_sc2p5d_t* c, cudaStream_t s);
 cudaError_t sc_mark_used(orbit_sc2p5d_t* c, cudaStream_t s);
+DepScales sc_dep_scales(const orbit_sc2p5d_t* c, const orbit_bunch_t* b);
+SetupArgs sc_setup_args(const orbit_sc2p5d_t* c, const DepScales& d);
 // Kick factor 2 L r_c / (beta^2 gamma^3) computed on the host exactly as
 // SpaceChargeCalc2p5D.cc:96 does (libm pow).
 double sc_host_factor(const orbit_sync_t& s, double length);

@@ -63,6 +63,102 @@ __device__ __forceinline__ void ext_block_commit(ExtAcc& a, ScState* st, unsigne
 }
 
 // ---------------------------------------------------------------------
+// Grid set-up of bunchAnalysis (SpaceChargeCalc2p5D.cc:126-216), run by
+// one thread of the last block of the kernel that scanned the extrema.
+// ---------------------------------------------------------------------
+// Explicitly rounded operations (no contraction), so that the grid limits
+// and the persistent xy_ratio evolve exactly as the reference's.  The keys
+// and the status word were written by atomics of other blocks: they are
+// read from L2.
+static __device__ __noinline__ void sc_setup_scalar(ScState* st, unsigned* status, SetupArgs sa) {
+  unsigned long long key[6];
+  for (int c = 0; c < 6; ++c) key[c] = __ldcg(&st->key[c]);
+  double xMin = dkey_inv(key[0]), xMax = dkey_inv(key[1]);
+  double yMin = dkey_inv(key[2]), yMax = dkey_inv(key[3]);
+  double zMin = dkey_inv(key[4]), zMax = dkey_inv(key[5]);
+  for (int c = 0; c < 3; ++c) { st->key[2 * c] = ~0ull; st->key[2 * c + 1] = 0ull; }
+  int skip = 0;
+  if (__ldcg(status) & ST_NAN) {
+    // a non-finite coordinate was met by the extrema scan: no kick
+    skip = 1;
+  } else if (!(xMin < xMax) || !(yMin < yMax) || !(zMin < zMax)) {  // :131 (also catches an empty scan)
+    skip = 1;
+    atomicOr(status, (unsigned)ST_EXTENT);
+  } else {
+    double xy = st->xy_ratio;
+    double ratio_beam = __ddiv_rn(__dsub_rn(xMax, xMin), __dsub_rn(yMax, yMin));
+    int set_solver = 0;
+    if (fabs(__dsub_rn(ratio_beam, xy)) < __dmul_rn(0.25, xy)) {  // :152-168
+      double width, center;
+      if (ratio_beam > xy) {
+        center = __ddiv_rn(__dadd_rn(yMax, yMin), 2.0);
+        width = __ddiv_rn(__dmul_rn(__dsub_rn(yMax, yMin), __ddiv_rn(ratio_beam, xy)), 2.0);
+        yMin = __dsub_rn(center, width);
+        yMax = __dadd_rn(center, width);
+      } else {
+        center = __ddiv_rn(__dadd_rn(xMax, xMin), 2.0);
+        width = __ddiv_rn(__ddiv_rn(__dsub_rn(xMax, xMin), __ddiv_rn(ratio_beam, xy)), 2.0);
+        xMin = __dsub_rn(center, width);
+        xMax = __dadd_rn(center, width);
+      }
+      xy = __ddiv_rn(__dsub_rn(xMax, xMin), __dsub_rn(yMax, yMin));
+    } else {  // :169-173
+      xy = ratio_beam;
+      set_solver = 1;
+    }
+    // Grid2D::setGridX/Y (Grid2D.cc:422-433), Grid1D::setGridZ (Grid1D.cc:89-94)
+    double dx = __ddiv_rn(__dsub_rn(xMax, xMin), (double)(sa.nx - 1));
+    double dy = __ddiv_rn(__dsub_rn(yMax, yMin), (double)(sa.ny - 1));
+    double dz = __ddiv_rn(__dsub_rn(zMax, zMin), (double)sa.nz);
+    st->xmin = xMin; st->xmax = xMax; st->ymin = yMin; st->ymax = yMax;
+    st->dx = dx; st->dy = dy; st->inv_dx = __drcp_rn(dx); st->inv_dy = __drcp_rn(dy);
+    st->zmin = zMin; st->zmax = zMax; st->dz = dz; st->inv_dz = __drcp_rn(dz);
+    st->xy_ratio = xy;
+    // solver-shape check (SpaceChargeCalc2p5D.cc:208-216)
+    if (!set_solver) {
+      double sr = __ddiv_rn(__dsub_rn(st->sxmax, st->sxmin), __dsub_rn(st->symax, st->symin));
+      if (fabs(__dsub_rn(sr, xy)) > 0.00000001) set_solver = 1;
+    }
+    if (set_solver) {  // PoissonSolverFFT2D::setGridXY (PoissonSolverFFT2D.cc:103-111)
+      st->sxmin = xMin; st->sxmax = xMax; st->symin = yMin; st->symax = yMax;
+      st->sdx = dx; st->sdy = dy;
+      st->green_dirty = 1;
+    }
+    st->scale = log(__ddiv_rn(st->sdx, dx));  // PoissonSolverFFT2D.cc:213
+    st->inv_qscale = sa.inv_qscale;
+    st->phi_absmax = 0ull;
+    st->lam_absmax = 0ull;
+  }
+  st->skip = skip;
+}
+
+// True in exactly one block of the grid: the last to call it.  Every
+// thread's earlier global writes and atomics are fenced before the block
+// is counted; `counter` is left at zero for the next launch.
+__device__ __forceinline__ bool last_block_done(unsigned* counter) {
+  __shared__ int s_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned prev = atomicAdd(counter, 1u);
+    s_last = prev == gridDim.x - 1;
+    if (s_last) {
+      *counter = 0u;
+      __threadfence();
+    }
+  }
+  __syncthreads();
+  return s_last != 0;
+}
+
+// Extrema commit followed, in the last block, by the grid set-up.
+__device__ __forceinline__ void ext_commit_and_setup(ExtAcc& a, ScState* st, unsigned* status,
+                                                     const SetupArgs& sa) {
+  ext_block_commit(a, st, status);
+  if (last_block_done(&st->ext_count) && threadIdx.x == 0) sc_setup_scalar(st, status, sa);
+}
+
+// ---------------------------------------------------------------------
 // 9-point TSC weights (Grid2D.cc:147-156, 220-233)
 // ---------------------------------------------------------------------
 template <typename T>

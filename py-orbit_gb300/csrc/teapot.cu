@@ -75,8 +75,13 @@ bool compile_op(const orbit_op_t& in, const orbit_sync_t& s, DevOp& o, double* t
     case ORBIT_OP_QFRIN:
     case ORBIT_OP_QFROUT:
       if (s.charge == 0.) { o.code = 0; return true; }
-      o.c[0] = d[0];
-      o.c[1] = (in.code == ORBIT_OP_QFRIN) ? 1.0 : -1.0;
+      {
+        // the OUT map is the IN map with kq -> -kq (teapotbase.cc:784-904);
+        // both factors scale exactly under the sign flip
+        double sg = (in.code == ORBIT_OP_QFRIN) ? 1.0 : -1.0;
+        o.c[0] = sg * (d[0] / 4.);
+        o.c[1] = sg * (d[0] / 12.);
+      }
       return true;
     case ORBIT_OP_BEND1: {  // teapotbase.cc:1099-1131
       double length = d[0], th = d[1];

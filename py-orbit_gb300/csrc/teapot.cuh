@@ -133,21 +133,30 @@ __device__ __forceinline__ void apply_ops(Part& p, const DevOp* __restrict__ ops
         break;
       }
       case ORBIT_OP_QFRIN:
-      case ORBIT_OP_QFROUT: {  // quadfringeIN/OUT (teapotbase.cc:784-904); c0 = kq, c1 = +1 IN / -1 OUT
+      case ORBIT_OP_QFROUT: {  // quadfringeIN/OUT (teapotbase.cc:784-904); c0 = +-kq/4, c1 = +-kq/12
         ensure_knl(p, m);
-        double kq = o.c[0], s = o.c[1], KNL = p.knl;
+        double KNL = p.knl;
         double x0 = p.x, xp0 = p.xp, y0 = p.y, yp0 = p.yp;
-        double x2 = x0 * x0, y2 = y0 * y0;
-        double k4 = kq * KNL * 0.25, k12 = kq * KNL * (1.0 / 12.);
+        double x2 = x0 * x0, y2 = y0 * y0, xy = x0 * y0;
+        double k4 = o.c[0] * KNL, k12 = o.c[1] * KNL;
+        double a = fma(3., y2, x2), b = fma(3., x2, y2), r2 = x2 + y2;  // x^2+3y^2, y^2+3x^2
         double t = k4 * (x2 - y2);
-        double detM = 1.0 - t * t;
-        double rdet = __drcp_rn(detM);
-        double x2p3y2 = x2 + 3. * y2, y2p3x2 = y2 + 3. * x2, r2 = x2 + y2;
-        p.x = x0 + s * (k12 * x0 * x2p3y2);
-        p.xp = (xp0 - s * (k4 * (xp0 * r2 - 2. * yp0 * x0 * y0))) * rdet;
-        p.y = y0 - s * (k12 * y0 * y2p3x2);
-        p.yp = (yp0 - s * (k4 * (-yp0 * r2 + 2. * xp0 * x0 * y0))) * rdet;
-        p.z += s * ((kq * KNL * KNL * (1.0 / 12.)) * (xp0 * x0 * x2p3y2 - yp0 * y0 * y2p3x2));
+        double u = t * t;  // detM = 1 - u
+        double nxp = fma(-k4, fma(xp0, r2, -2. * (yp0 * xy)), xp0);
+        double nyp = fma(-k4, fma(-yp0, r2, 2. * (xp0 * xy)), yp0);
+        if (u < 0x1p-20) {
+          // 1/(1-u) = 1 + u + u^2 + O(2^-60): one rounding instead of two
+          double w = fma(u, u, u);
+          p.xp = fma(nxp, w, nxp);
+          p.yp = fma(nyp, w, nyp);
+        } else {
+          double detM = 1.0 - u;
+          p.xp = nxp / detM;
+          p.yp = nyp / detM;
+        }
+        p.x = fma(k12 * x0, a, x0);
+        p.y = fma(-k12 * y0, b, y0);
+        p.z = fma(k12 * KNL, fma(xp0 * x0, a, -(yp0 * y0) * b), p.z);
         break;
       }
       case ORBIT_OP_BEND1: {  // bend1 (teapotbase.cc:1099-1146); c = m11,m12,m16,m21,m22,m26,m51,m52,m56,L
