@@ -92,6 +92,17 @@ MAP_FLOPS = {1: 22, 2: 16, 3: 25, 4: 70, 5: 70, 6: 18, 7: 25, 8: 20, 9: 14, 10: 
              14: 60, 15: 12, 16: 2, 17: 3, 18: 20, 19: 30, 20: 60}
 
 
+# FP64 instructions per particle (DFMA + DMUL + DADD, thread level) that the
+# kernels execute on this workload, counted by ncu
+# (smsp__sass_thread_inst_executed_op_{dfma,dmul,dadd}_pred_on, 4e6
+# particles): the fused pass alternates the {kick, quad1, quad2, quad2,
+# quad1, fringe-out} segment (92.6) and the {kick, drift, fringe-in} segment
+# (60.6); the deposit runs 6.3 (one FMA per coordinate and the fixed-point
+# conversions; weights and sums are integer).  Conversions and compares also
+# occupy the FP64 pipe and are not in these counts.
+FP64_INST_PER_PARTICLE = {"pass_kick_maps": (92.6 + 60.6) / 2, "deposit": 6.26}
+
+
 def pass_flops_per_turn(ops):
     """FP64 operations per particle of all fused passes of one turn."""
     total = 0
@@ -337,18 +348,21 @@ def run_ours(args):
                 "kernel_ms_per_launch": per_launch_ms, "share_of_turn": dom_ms / turn_ms,
                 "kernels": {k: {"ms": v[0], "launches": v[1], "share": v[0] / turn_ms} for k, v in prof.items()}}
     if args.form == "plain":
-        # the plain form is bound by the FP64 pipe: algorithmic FP64 rate of
-        # the fused passes and of the deposit against the live DFMA peak
-        pass_ms = sum(v[0] for k, v in prof.items() if k.startswith("pass"))
-        pf = pass_flops_per_turn(prog.ops) * n
-        dep_ms, dep_l = prof.get("deposit", (0.0, 1))
-        roofline["fp64_pipe"] = {
-            "peak_tflops": fp64_peak, "peak_source": "measured in this run (orbit_device_peaks: DFMA chains)",
-            "pass_achieved_tflops": pf / (pass_ms * 1e-3) / 1e12,
-            "pass_frac": pf / (pass_ms * 1e-3) / 1e12 / fp64_peak,
-            "deposit_achieved_tflops": DEPOSIT_FLOPS * n * dep_l / (dep_ms * 1e-3) / 1e12,
-            "deposit_frac": DEPOSIT_FLOPS * n * dep_l / (dep_ms * 1e-3) / 1e12 / fp64_peak,
-            "flops_per_particle_turn": pass_flops_per_turn(prog.ops) + DEPOSIT_FLOPS * kicks_per_turn}
+        # the plain form is bound by the FP64 pipe: counted FP64 instructions
+        # of the fused passes and of the deposit against the live DFMA peak
+        peak_inst = fp64_peak / 2 * 1e12
+        fp = {"peak_tflops": fp64_peak, "peak_source": "measured in this run (orbit_device_peaks: DFMA chains)",
+              "peak_inst_per_s": peak_inst,
+              "reference_flops_per_particle_turn": pass_flops_per_turn(prog.ops) + DEPOSIT_FLOPS * kicks_per_turn}
+        for kname, ipp in FP64_INST_PER_PARTICLE.items():
+            k_ms, k_l = prof.get(kname, (0.0, 0))
+            if k_ms > 0:
+                rate = ipp * n * k_l / (k_ms * 1e-3)
+                fp[kname] = {"fp64_inst_per_particle": ipp, "achieved_inst_per_s": rate, "frac": rate / peak_inst}
+        roofline["fp64_pipe"] = fp
+    # how often the Poisson solver grid was reshaped (Green spectrum rebuilt)
+    kicks_done, green_done = calc._calc.counters()
+    green_rate = green_done / kicks_done if kicks_done else None
     cpu = None
     if not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -364,7 +378,8 @@ def run_ours(args):
         "config": {"workload": "FODO 40 cells x 4 SC nodes, %d particles, grid %dx%dx%d, one turn per step"
                    % (n, *GRID), "form": args.form, "particles": n, "grid": list(GRID),
                    "kicks_per_step": kicks_per_turn, "l2": "flushed (512 MiB write) before each timed step",
-                   "parallelism": "replicas" if world > 1 else "single"},
+                   "parallelism": "replicas" if world > 1 else "single",
+                   "green_rebuilds_per_kick": green_rate},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
         "gpu_launches": launches_per_turn * args.steps, "wall_s": wall,
     }
@@ -376,7 +391,7 @@ def run_ours(args):
 # DRAM traffic per particle per launch, dram__bytes_read.sum +
 # dram__bytes_write.sum from one ncu capture of a 4e6-particle run of this
 # benchmark (bunch larger than L2); scaled to the bench's particle count.
-TRAFFIC_PER_PARTICLE = {("plain", "pass_kick_maps"): 80.57, ("plain", "deposit"): 24.66}
+TRAFFIC_PER_PARTICLE = {("plain", "pass_kick_maps"): 88.9, ("plain", "deposit"): 24.75}
 
 
 class _Traffic(dict):

@@ -110,6 +110,11 @@ int orbit_sc2p5d_get_grid(orbit_sc2p5d_t* c, int which, double* host_out);
 /* lim = {xmin,xmax,ymin,ymax,zmin,zmax,dx,dy,dz,xy_ratio,total_macrosize} */
 int orbit_sc2p5d_get_limits(orbit_sc2p5d_t* c, double* lim);
 int orbit_sc2p5d_get_sizes(const orbit_sc2p5d_t* c, int* nx, int* ny, int* nz, int* form);
+/* No counterpart in the reference (diagnostic).  Kicks solved and Green
+ * spectra rebuilt (PoissonSolverFFT2D::setGridXY followed by the Green
+ * transform, PoissonSolverFFT2D.cc:103-172) since the calculator was
+ * created.  Waits for the last stream the calculator ran on. */
+int orbit_sc2p5d_counters(orbit_sc2p5d_t* c, long long* kicks, long long* green_rebuilds);
 /* Grid2D::calcGradient + Grid1D::getValue at n host points with the current
  * grids (Grid2D.cc:212-256, Grid1D.cc:191-211). */
 int orbit_sc2p5d_fields(orbit_sc2p5d_t* c, int n, const double* x, const double* y, const double* z,

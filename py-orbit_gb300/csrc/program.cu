@@ -22,13 +22,19 @@ int check_status(orbit_bunch_t* b);
 
 static const int kPassSmem = 220 * 1024;
 
+// Per-particle 1/(1+dp_p) kept between the passes of one program run
+// (it changes only with dE): km & KNL_STORE writes it at the end of the
+// pass, km & KNL_LOAD reads it instead of dividing.
+enum { KNL_LOAD = 1, KNL_STORE = 2 };
+
 // KF: 0 no kick, 1 plain kick, 2 fp32 kick.  EXT: accumulate extrema.
 template <int KF, bool EXT, bool KSMEM>
 __global__ void __launch_bounds__(512) k_pass(double* __restrict__ cx, double* __restrict__ cxp,
                                               double* __restrict__ cy, double* __restrict__ cyp,
                                               double* __restrict__ cz, double* __restrict__ cdE, int n,
                                               const DevOp* __restrict__ ops, int a, int b, MapCtx m,
-                                              KickArgs kick, ScState* ext_st, unsigned* status, SetupArgs sa) {
+                                              KickArgs kick, ScState* ext_st, unsigned* status, SetupArgs sa,
+                                              double* __restrict__ knl_buf, int km) {
   KickConst k;
   KickFix kf;
   const long long* P = kick.phi_fix;
@@ -64,11 +70,20 @@ __global__ void __launch_bounds__(512) k_pass(double* __restrict__ cx, double* _
     Part p;
     p.x = cx[i]; p.xp = cxp[i]; p.y = cy[i]; p.yp = cyp[i]; p.z = cz[i]; p.dE = cdE[i];
     p.knl_ok = false;
+    if (km & KNL_LOAD) {  // 1/(1+dp_p) as an earlier pass of this run computed it from the same dE
+      p.dp_p = p.dE * m.dp_p_coeff;
+      p.knl = knl_buf[i];
+      p.knl_ok = true;
+    }
     if (KF == 1 && !k.skip && !kick_fixed(kf, P, Lm, p.x, p.y, p.z, p.xp, p.yp))
       kick_plain(k, kick.phi, kick.lam, p.x, p.y, p.z, p.xp, p.yp);
     if (KF == 2 && !k.skip) kick_fp32(k, Pf, Lf, p.x, p.y, p.z, p.xp, p.yp);
     apply_ops(p, ops, a, b, m);
     if (EXT) acc.add(p.x, p.y, p.z);
+    if (km & KNL_STORE) {
+      ensure_knl(p, m);
+      knl_buf[i] = p.knl;
+    }
     cx[i] = p.x; cxp[i] = p.xp; cy[i] = p.y; cyp[i] = p.yp; cz[i] = p.z; cdE[i] = p.dE;
   }
   // the last block sets up the grids of the next kick
@@ -89,7 +104,8 @@ static int init_pass_attrs() {
 
 template <int KF, bool EXT, bool KSMEM>
 static int launch_pass(orbit_bunch_t* bu, cudaStream_t s, size_t smem, const DevOp* ops, int a, int b,
-                       const MapCtx& m, const KickArgs& ka, ScState* ext, const SetupArgs& sa) {
+                       const MapCtx& m, const KickArgs& ka, ScState* ext, const SetupArgs& sa, double* knl_buf,
+                       int km) {
   int threads = 512;
   int bps = KSMEM ? (int)(kPassSmem / (smem > 0 ? smem : 1)) : 4;
   if (bps < 1) bps = 1;
@@ -100,7 +116,7 @@ static int launch_pass(orbit_bunch_t* bu, cudaStream_t s, size_t smem, const Dev
   ORBIT_PB(KF == 0 ? "pass_maps" : "pass_kick_maps", s);
   k_pass<KF, EXT, KSMEM><<<blocks, threads, KSMEM ? smem : 0, s>>>(
       bu->coord(0), bu->coord(1), bu->coord(2), bu->coord(3), bu->coord(4), bu->coord(5), bu->n, ops, a, b, m, ka,
-      ext, bu->d_status, sa);
+      ext, bu->d_status, sa, knl_buf, km);
   ORBIT_PE(s);
   ORBIT_LAUNCH_CHECK("k_pass");
   return ORBIT_OK;
@@ -121,6 +137,8 @@ struct orbit_program {
   int key_msize = -1;
   DevOp* d_ops = nullptr;
   int n_devops = 0;
+  double* d_knl = nullptr;            // per-particle 1/(1+dp_p) between passes
+  size_t knl_n = 0;
   cudaGraphExec_t g_first = nullptr;  // prologue + turn ending with the wrap pass
   cudaGraphExec_t g_mid = nullptr;    // turn ending with the wrap pass
   cudaGraphExec_t g_last = nullptr;   // turn ending without the wrap
@@ -133,7 +151,10 @@ struct orbit_program {
 
 namespace orbit {
 
-struct Seg { int a, b; };
+struct Seg {
+  int a, b;
+  bool dE;  // an op of the segment changes dE (kick with dE, wedgerotate)
+};
 
 struct Plan {
   std::vector<Seg> segs;      // m+1 map segments in the device op array
@@ -168,8 +189,11 @@ static KickArgs kick_args(orbit_sc2p5d_t* c, const orbit_sync_t& s, double lengt
 
 // One fused pass: optional kick of calculator kc, maps [a,b), optional
 // extrema for calculator ec.
+// ec_here: the kick of ec is enqueued next in this same stream (and graph),
+// so a graph branch for its Green rebuild can be set up by this pass.
 static int enqueue_pass(orbit_bunch_t* bu, cudaStream_t s, const DevOp* ops, Seg seg, const MapCtx& m,
-                        orbit_sc2p5d_t* kc, double klen, orbit_sc2p5d_t* ec, int* nl) {
+                        orbit_sc2p5d_t* kc, double klen, orbit_sc2p5d_t* ec, bool ec_here, double* knl_buf, int km,
+                        int* nl) {
   KickArgs ka;
   std::memset(&ka, 0, sizeof(ka));
   int kf = 0;
@@ -186,20 +210,23 @@ static int enqueue_pass(orbit_bunch_t* bu, cudaStream_t s, const DevOp* ops, Seg
   bool e = ext != nullptr;
   SetupArgs sa;
   std::memset(&sa, 0, sizeof(sa));
-  if (ec) sa = sc_setup_args(ec, sc_dep_scales(ec, bu));
+  if (ec) {
+    sa = sc_setup_args(ec, sc_dep_scales(ec, bu));
+    if (ec_here) sa.cond = sc_green_cond(ec, s, true);
+  }
   int rc;
-  if (kf == 0) rc = e ? launch_pass<0, true, false>(bu, s, 0, ops, seg.a, seg.b, m, ka, ext, sa)
-                      : launch_pass<0, false, false>(bu, s, 0, ops, seg.a, seg.b, m, ka, ext, sa);
+  if (kf == 0) rc = e ? launch_pass<0, true, false>(bu, s, 0, ops, seg.a, seg.b, m, ka, ext, sa, knl_buf, km)
+                      : launch_pass<0, false, false>(bu, s, 0, ops, seg.a, seg.b, m, ka, ext, sa, knl_buf, km);
   else if (kf == 1) {
-    if (ksm) rc = e ? launch_pass<1, true, true>(bu, s, smem, ops, seg.a, seg.b, m, ka, ext, sa)
-                    : launch_pass<1, false, true>(bu, s, smem, ops, seg.a, seg.b, m, ka, ext, sa);
-    else rc = e ? launch_pass<1, true, false>(bu, s, 0, ops, seg.a, seg.b, m, ka, ext, sa)
-                : launch_pass<1, false, false>(bu, s, 0, ops, seg.a, seg.b, m, ka, ext, sa);
+    if (ksm) rc = e ? launch_pass<1, true, true>(bu, s, smem, ops, seg.a, seg.b, m, ka, ext, sa, knl_buf, km)
+                    : launch_pass<1, false, true>(bu, s, smem, ops, seg.a, seg.b, m, ka, ext, sa, knl_buf, km);
+    else rc = e ? launch_pass<1, true, false>(bu, s, 0, ops, seg.a, seg.b, m, ka, ext, sa, knl_buf, km)
+                : launch_pass<1, false, false>(bu, s, 0, ops, seg.a, seg.b, m, ka, ext, sa, knl_buf, km);
   } else {
-    if (ksm) rc = e ? launch_pass<2, true, true>(bu, s, smem, ops, seg.a, seg.b, m, ka, ext, sa)
-                    : launch_pass<2, false, true>(bu, s, smem, ops, seg.a, seg.b, m, ka, ext, sa);
-    else rc = e ? launch_pass<2, true, false>(bu, s, 0, ops, seg.a, seg.b, m, ka, ext, sa)
-                : launch_pass<2, false, false>(bu, s, 0, ops, seg.a, seg.b, m, ka, ext, sa);
+    if (ksm) rc = e ? launch_pass<2, true, true>(bu, s, smem, ops, seg.a, seg.b, m, ka, ext, sa, knl_buf, km)
+                    : launch_pass<2, false, true>(bu, s, smem, ops, seg.a, seg.b, m, ka, ext, sa, knl_buf, km);
+    else rc = e ? launch_pass<2, true, false>(bu, s, 0, ops, seg.a, seg.b, m, ka, ext, sa, knl_buf, km)
+                : launch_pass<2, false, false>(bu, s, 0, ops, seg.a, seg.b, m, ka, ext, sa, knl_buf, km);
   }
   if (rc == ORBIT_OK) ++*nl;
   return rc;
@@ -223,11 +250,13 @@ static int compile(orbit_program_t* p, orbit_bunch_t* bu, Plan& plan) {
   auto emit = [&](int a, int b) -> Seg {
     Seg s;
     s.a = (int)dev.size();
+    s.dE = false;
     for (int k = a; k < b; ++k) {
       DevOp d;
       double adv = 0.0;
-      if (!compile_op(p->ops[k], bu->sync, d, &adv)) return Seg{-1, -1};
+      if (!compile_op(p->ops[k], bu->sync, d, &adv)) return Seg{-1, -1, false};
       p->time_adv[k] = adv;
+      if (d.code == ORBIT_OP_WEDGEROT || (d.code == ORBIT_OP_KICK && d.c[2] != 0.)) s.dE = true;
       if (d.code != 0) dev.push_back(d);
     }
     s.b = (int)dev.size();
@@ -246,7 +275,16 @@ static int compile(orbit_program_t* p, orbit_bunch_t* bu, Plan& plan) {
     if (s1.a < 0 || s2.a < 0) return set_error(ORBIT_ERR_ARG, "orbit_program: bad op parameters");
   }
   w.b = (int)dev.size();
+  w.dE = plan.segs.back().dE || plan.segs.front().dE;
   plan.wrap = w;
+  if (p->knl_n < (size_t)bu->n) {
+    if (p->d_knl) { cudaFree(p->d_knl); p->d_knl = nullptr; }
+    p->knl_n = 0;
+    if (bu->n > 0) {
+      ORBIT_CUDA(cudaMalloc(&p->d_knl, sizeof(double) * (size_t)bu->n));
+      p->knl_n = (size_t)bu->n;
+    }
+  }
   if (p->d_ops) { cudaFree(p->d_ops); p->d_ops = nullptr; }
   p->n_devops = (int)dev.size();
   if (!dev.empty()) {
@@ -267,16 +305,28 @@ static int enqueue_turn(orbit_program_t* p, orbit_bunch_t* bu, cudaStream_t s, c
   auto calc_of = [&](int i) -> orbit_sc2p5d_t* { return p->calcs[p->ops[plan.sc_idx[i]].i0]; };
   auto len_of = [&](int i) -> double { return p->ops[plan.sc_idx[i]].d[0]; };
   int rc;
+  // the first pass of the run stores 1/(1+dp_p); later passes load it and
+  // store it again only when their ops change dE
+  bool first = true;
+  auto km_of = [&](const Seg& sg, bool sc) -> int {
+    if (!sc && sg.a == sg.b) return 0;  // enqueue_pass launches nothing
+    int km = first ? (int)KNL_STORE : (KNL_LOAD | (sg.dE ? KNL_STORE : 0));
+    first = false;
+    return km;
+  };
+  double* kb = p->d_knl;
   if (nsc == 0 || !sc_active) {
     // no kicks: one pass over all maps of the turn
     for (size_t i = 0; i < plan.segs.size(); ++i) {
-      rc = enqueue_pass(bu, s, ops, plan.segs[i], m, nullptr, 0.0, nullptr, nl);
+      rc = enqueue_pass(bu, s, ops, plan.segs[i], m, nullptr, 0.0, nullptr, false, kb, km_of(plan.segs[i], false),
+                        nl);
       if (rc) return rc;
     }
     return ORBIT_OK;
   }
   if (prologue) {
-    rc = enqueue_pass(bu, s, ops, plan.segs[0], m, nullptr, 0.0, calc_of(0), nl);
+    rc = enqueue_pass(bu, s, ops, plan.segs[0], m, nullptr, 0.0, calc_of(0), true, kb, km_of(plan.segs[0], true),
+                      nl);
     if (rc) return rc;
   }
   for (int i = 0; i < nsc; ++i) {
@@ -284,11 +334,14 @@ static int enqueue_turn(orbit_program_t* p, orbit_bunch_t* bu, cudaStream_t s, c
     if (rc) return rc;
     bool last = (i == nsc - 1);
     if (!last) {
-      rc = enqueue_pass(bu, s, ops, plan.segs[i + 1], m, calc_of(i), len_of(i), calc_of(i + 1), nl);
+      rc = enqueue_pass(bu, s, ops, plan.segs[i + 1], m, calc_of(i), len_of(i), calc_of(i + 1), true, kb,
+                        km_of(plan.segs[i + 1], true), nl);
     } else if (wrap) {
-      rc = enqueue_pass(bu, s, ops, plan.wrap, m, calc_of(i), len_of(i), calc_of(0), nl);
+      rc = enqueue_pass(bu, s, ops, plan.wrap, m, calc_of(i), len_of(i), calc_of(0), false, kb,
+                        km_of(plan.wrap, true), nl);
     } else {
-      rc = enqueue_pass(bu, s, ops, plan.segs[nsc], m, calc_of(i), len_of(i), nullptr, nl);
+      rc = enqueue_pass(bu, s, ops, plan.segs[nsc], m, calc_of(i), len_of(i), nullptr, false, kb,
+                        km_of(plan.segs[nsc], true), nl);
     }
     if (rc) return rc;
   }
@@ -298,8 +351,10 @@ static int enqueue_turn(orbit_program_t* p, orbit_bunch_t* bu, cudaStream_t s, c
 static int capture(orbit_program_t* p, orbit_bunch_t* bu, const Plan& plan, bool prologue, bool wrap,
                    cudaGraphExec_t* out, int* nl) {
   cudaStream_t s = bu->stream;
+  for (auto c : p->calcs) sc_clear_pending(c);
   ORBIT_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   int rc = enqueue_turn(p, bu, s, plan, prologue, wrap, nl);
+  for (auto c : p->calcs) sc_clear_pending(c);
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaStreamEndCapture(s, &g);
   if (rc) {
@@ -370,6 +425,7 @@ int orbit_program_destroy(orbit_program_t* p) {
   if (p->done) cudaEventDestroy(p->done);
   free_graphs(p);
   if (p->d_ops) cudaFree(p->d_ops);
+  if (p->d_knl) cudaFree(p->d_knl);
   delete p;
   return ORBIT_OK;
 }

@@ -75,15 +75,13 @@ __global__ void k_green_fill(const ScState* st, double* g, int nx2, int ny2, int
 
 // Line density to doubles, total macrosize and the Green-rebuild flag
 // reset, run by one extra block of the forward row transforms (the deposit
-// is complete).  Inside a graph the old flag selects the branch that
-// rebuilds the Green spectrum (cond); the line density accumulator is
-// cleared for the next deposit.
+// is complete; an eager Green rebuild ran before it, a graph branch reads
+// no flag).  The line density accumulator is cleared for the next deposit.
 template <typename G>
-__device__ __noinline__ void finalize_block(ScState* st, G* zacc, int nz, double* lam, float* lam_f,
-                               cudaGraphConditionalHandle cond) {
+__device__ __noinline__ void finalize_block(ScState* st, G* zacc, int nz, double* lam, float* lam_f) {
   if (threadIdx.x == 0) {
-    if (cond) cudaGraphSetConditional(cond, st->green_dirty ? 1u : 0u);
     st->green_dirty = 0;
+    st->n_kicks += 1;
   }
   __shared__ double s_part[32];
   double iq = st->inv_qscale;
@@ -147,14 +145,13 @@ __device__ __noinline__ void finalize_block(ScState* st, G* zacc, int nz, double
 template <typename T, int SRC>
 __global__ void k_rows_fwd(ScState* st, void* src, double* rho_out, typename CT<T>::t* hat,
                            const typename CT<T>::t* __restrict__ tw, FftPlan pl, int nrows, int ncols, int H,
-                           int gate, void* zacc, int nz, double* lam, float* lam_f,
-                           cudaGraphConditionalHandle cond) {
+                           int gate, void* zacc, int nz, double* lam, float* lam_f) {
   typedef typename CT<T>::t C;
   if (SRC == 0 && gate && !st->green_dirty) return;
   if (st->skip) return;
   if (SRC != 0 && blockIdx.x == gridDim.x - 1) {
-    if (SRC == 1) finalize_block(st, (unsigned long long*)zacc, nz, lam, (float*)nullptr, cond);
-    else finalize_block(st, (float*)zacc, nz, lam, lam_f, cond);
+    if (SRC == 1) finalize_block(st, (unsigned long long*)zacc, nz, lam, (float*)nullptr);
+    else finalize_block(st, (float*)zacc, nz, lam, lam_f);
     return;
   }
   extern __shared__ unsigned char smem_raw[];
@@ -231,7 +228,7 @@ __global__ void k_rows_fwd(ScState* st, void* src, double* rho_out, typename CT<
 //         correction (PoissonSolverFFT2D.cc:212-242), backward; rows >= nin
 //         are zero on input and only rows < nin are kept on output.
 template <typename T, int MODE>
-__global__ void k_cols(const ScState* st, typename CT<T>::t* hat, typename CT<T>::t* __restrict__ green,
+__global__ void k_cols(ScState* st, typename CT<T>::t* hat, typename CT<T>::t* __restrict__ green,
                        const typename CT<T>::t* __restrict__ tw, FftPlan pl, int nin, int H, int ny2, int gate) {
   typedef typename CT<T>::t C;
   if (MODE == 0 && gate && !st->green_dirty) return;
@@ -253,6 +250,7 @@ __global__ void k_cols(const ScState* st, typename CT<T>::t* hat, typename CT<T>
   C* F = block_fft<T>(a, b, pl, stw, false);
   if (MODE == 0) {
     for (int r = threadIdx.x; r < N; r += blockDim.x) green[(size_t)k * N + r] = F[r];
+    if (k == 0 && threadIdx.x == 0) st->n_green += 1;
     return;
   }
   double s = st->scale;
@@ -363,30 +361,32 @@ __global__ void __launch_bounds__(768) k_deposit_plain(const double* __restrict_
   if (d.skip) return;
   DepFix df;
   if (K > 0) load_dep_fix(df, st, nx, ny, nz, K);
-  extern __shared__ unsigned long long s_acc[];
-  unsigned long long* rho = g_rho;
-  unsigned long long* zg = g_z;
-  if (SMEM) {
-    rho = s_acc;
-    zg = s_acc + nx * ny;
-    for (int i = threadIdx.x; i < nx * ny + nz; i += blockDim.x) s_acc[i] = 0ull;
+  // shared: low words of the nx*ny + nz cells, then their high words
+  extern __shared__ unsigned s_acc32[];
+  const int ncell = nx * ny + nz;
+  GridAcc<SMEM> rho, zg;
+  if constexpr (SMEM) {
+    rho.lo = s_acc32;
+    rho.hi_off = ncell;
+    zg.lo = s_acc32 + nx * ny;
+    zg.hi_off = ncell;
+    for (int i = threadIdx.x; i < 2 * ncell; i += blockDim.x) s_acc32[i] = 0u;
     __syncthreads();
+  } else {
+    rho.p = g_rho;
+    zg.p = g_z;
   }
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     double xi = x[i], yi = y[i], zi = z[i];
-    if (K > 0 && deposit_fixed(df, rho, zg, xi, yi, zi)) continue;
+    if (K > 0 && deposit_fixed<SMEM>(df, rho, zg, xi, yi, zi)) continue;
     double ms = msize ? msize[i] * qscale : ms_uniform;
-    deposit_plain(d, rho, zg, xi, yi, zi, ms);
+    deposit_plain<SMEM>(d, rho, zg, xi, yi, zi, ms);
   }
-  if (SMEM) {
+  if constexpr (SMEM) {
     __syncthreads();
-    for (int i = threadIdx.x; i < nx * ny; i += blockDim.x) {
-      unsigned long long v = s_acc[i];
-      if (v) atomicAdd(g_rho + i, v);
-    }
-    for (int i = threadIdx.x; i < nz; i += blockDim.x) {
-      unsigned long long v = s_acc[nx * ny + i];
-      if (v) atomicAdd(g_z + i, v);
+    for (int i = threadIdx.x; i < ncell; i += blockDim.x) {
+      unsigned long long v = rho.get(i);
+      if (v) atomicAdd(i < nx * ny ? g_rho + i : g_z + (i - nx * ny), v);
     }
   }
 }
@@ -592,9 +592,9 @@ static void particle_geometry(size_t smem, int n, int max_threads, int* blocks, 
 }
 
 // Forward row transforms of the deposit (plus one block finalizing the line
-// density; inside a graph it sets `cond`, the Green-rebuild branch).
+// density).
 template <typename T>
-static int enqueue_rows_fwd(orbit_sc2p5d_t* c, cudaStream_t s, cudaGraphConditionalHandle cond, int* nl) {
+static int enqueue_rows_fwd(orbit_sc2p5d_t* c, cudaStream_t s, int* nl) {
   typedef typename CT<T>::t C;
   C* hat = (C*)c->d_hat;
   const C* twy = (const C*)c->d_tw_y;
@@ -604,10 +604,10 @@ static int enqueue_rows_fwd(orbit_sc2p5d_t* c, cudaStream_t s, cudaGraphConditio
   ORBIT_PB("fft_rows_fwd", s);
   if (c->form == ORBIT_FORM_PLAIN) {
     k_rows_fwd<T, 1><<<blocks, thy, smy, s>>>(c->d_st, c->d_rho_q, c->d_rho, hat, twy, c->plan_y, c->nx, c->ny,
-                                              c->H, 1, c->d_z_q, c->nz, c->d_lam, nullptr, cond);
+                                              c->H, 1, c->d_z_q, c->nz, c->d_lam, nullptr);
   } else {
     k_rows_fwd<T, 2><<<blocks, thy, smy, s>>>(c->d_st, c->d_rho_f, c->d_rho, hat, twy, c->plan_y, c->nx, c->ny,
-                                              c->H, 1, c->d_z_f, c->nz, c->d_lam, c->d_lam_f, cond);
+                                              c->H, 1, c->d_z_f, c->nz, c->d_lam, c->d_lam_f);
   }
   ORBIT_PE(s);
   ++*nl;
@@ -660,8 +660,7 @@ static int enqueue_green(orbit_sc2p5d_t* c, cudaStream_t s, int gate, void* scra
   ORBIT_PB("green_rows", s);
   C* hat = (C*)scratch;
   k_rows_fwd<T, 0><<<(c->nx + 2) / 2, thy, smy, s>>>(c->d_st, c->d_gbuf, nullptr, hat, twy, c->plan_y,
-                                                      c->nx + 1, c->ny2, c->H, gate, nullptr, 0, nullptr, nullptr,
-                                                      0);
+                                                      c->nx + 1, c->ny2, c->H, gate, nullptr, 0, nullptr, nullptr);
   ORBIT_PE(s);
   ORBIT_PB("green_cols", s);
   k_cols<T, 0><<<c->H, thx, smx, s>>>(c->d_st, hat, green, twx, c->plan_x, c->nx2, c->H, c->ny2, gate);
@@ -729,14 +728,38 @@ SetupArgs sc_setup_args(const orbit_sc2p5d_t* c, const DepScales& d) {
   sa.nx = c->nx;
   sa.ny = c->ny;
   sa.nz = c->nz;
+  sa.cond = 0;
   return sa;
 }
 
-// Inside a stream capture: a conditional graph node after the forward row
-// transforms whose body rebuilds the Green spectrum (into its own scratch:
-// the work spectrum is in use); their finalizing block takes it when the
-// spectrum is dirty.  The body is captured on the calculator's own stream.
-static int add_green_branch(orbit_sc2p5d_t* c, cudaStream_t s, cudaGraphConditionalHandle cond) {
+cudaGraphConditionalHandle sc_green_cond(orbit_sc2p5d_t* c, cudaStream_t s, bool pending) {
+  if (!c->aux || !c->d_gscratch) return 0;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaGraph_t g = nullptr;
+  if (cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, nullptr, nullptr, nullptr) != cudaSuccess) return 0;
+  if (cs != cudaStreamCaptureStatusActive) return 0;
+  cudaGraphConditionalHandle h = 0;
+  if (cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault) != cudaSuccess) return 0;
+  if (pending) {
+    c->pending_cond = h;
+    c->pending_graph = g;
+  }
+  return h;
+}
+
+void sc_clear_pending(orbit_sc2p5d_t* c) {
+  c->pending_cond = 0;
+  c->pending_graph = nullptr;
+}
+
+// Inside a stream capture: a conditional graph node, depending on what the
+// stream's next work would depend on (the deposit), whose body rebuilds the
+// Green spectrum into its own scratch.  The set-up took the branch when the
+// spectrum is dirty; the stream's dependencies are left as they were, so
+// the forward rows run beside the branch and the caller joins it before
+// the column transforms.
+static int add_green_branch(orbit_sc2p5d_t* c, cudaStream_t s, cudaGraphConditionalHandle cond,
+                            cudaGraphNode_t* node_out) {
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   cudaGraph_t g = nullptr;
   const cudaGraphNode_t* deps = nullptr;
@@ -750,7 +773,6 @@ static int add_green_branch(orbit_sc2p5d_t* c, cudaStream_t s, cudaGraphConditio
   cudaGraphNode_t node;
   ORBIT_CUDA(cudaGraphAddNode(&node, g, deps, nullptr, nd, &p));
   cudaGraph_t body = p.conditional.phGraph_out[0];
-  ORBIT_CUDA(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
   ORBIT_CUDA(cudaStreamBeginCaptureToGraph(c->aux, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
   int bl = 0;
   int rc = c->form == ORBIT_FORM_PLAIN ? enqueue_green<double>(c, c->aux, 0, c->d_gscratch, &bl)
@@ -759,6 +781,7 @@ static int add_green_branch(orbit_sc2p5d_t* c, cudaStream_t s, cudaGraphConditio
   cudaError_t e = cudaStreamEndCapture(c->aux, &out);
   if (rc) return rc;
   if (e != cudaSuccess) return cuda_error(e, "sc2p5d: Green branch capture");
+  *node_out = node;
   return ORBIT_OK;
 }
 
@@ -769,23 +792,28 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
   const double* msz = b->has_msize ? b->d_msize : nullptr;
   const bool plain = c->form == ORBIT_FORM_PLAIN;
   const DepScales ds = sc_dep_scales(c, b);
+  // Inside a graph the Green rebuild is a conditional branch beside the
+  // forward rows, taken by the set-up (run by the extrema scan here, or by
+  // the fused pass that created the pending handle); otherwise its kernels
+  // run first and return unless the spectrum is dirty.
+  cudaGraphConditionalHandle cond = 0;
   if (do_extrema) {
-    // the grid set-up runs in the scan's last block
+    SetupArgs sa = sc_setup_args(c, ds);
+    sa.cond = cond = sc_green_cond(c, s, false);
     ORBIT_PB("extrema", s);
-    k_extrema<<<ext_blocks(n), 256, 0, s>>>(b->coord(0), b->coord(2), b->coord(4), n, c->d_st, b->d_status,
-                                            sc_setup_args(c, ds));
+    k_extrema<<<ext_blocks(n), 256, 0, s>>>(b->coord(0), b->coord(2), b->coord(4), n, c->d_st, b->d_status, sa);
     ORBIT_PE(s);
     ++nl;
+  } else if (c->pending_cond) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaGraph_t cg = nullptr;
+    ORBIT_CUDA(cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg, nullptr, nullptr, nullptr));
+    if (cs == cudaStreamCaptureStatusActive && cg == c->pending_graph) cond = c->pending_cond;
   }
-  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-  cudaGraph_t cg = nullptr;
-  ORBIT_CUDA(cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg, nullptr, nullptr, nullptr));
-  const bool branch = cs == cudaStreamCaptureStatusActive && c->aux != nullptr && c->d_gscratch != nullptr;
-  cudaGraphConditionalHandle cond = 0;
+  sc_clear_pending(c);
+  cudaGraphNode_t branch_node = nullptr;
   int rc;
-  if (branch) {
-    ORBIT_CUDA(cudaGraphConditionalHandleCreate(&cond, cg, 0, cudaGraphCondAssignDefault));
-  } else {
+  if (!cond) {
     // before the deposit: the work spectrum is free to hold the row spectra
     rc = plain ? enqueue_green<double>(c, s, 1, c->d_hat, &nl) : enqueue_green<float>(c, s, 1, c->d_hat, &nl);
     if (rc) return rc;
@@ -819,12 +847,15 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
   ORBIT_PE(s);
   ++nl;
   ORBIT_LAUNCH_CHECK("sc2p5d deposit");
-  rc = plain ? enqueue_rows_fwd<double>(c, s, cond, &nl) : enqueue_rows_fwd<float>(c, s, cond, &nl);
-  if (rc) return rc;
-  if (branch) {
-    rc = add_green_branch(c, s, cond);
+  if (cond) {
+    // beside the forward rows, which leave most SMs free (the deposit fills them)
+    rc = add_green_branch(c, s, cond, &branch_node);
     if (rc) return rc;
   }
+  rc = plain ? enqueue_rows_fwd<double>(c, s, &nl) : enqueue_rows_fwd<float>(c, s, &nl);
+  if (rc) return rc;
+  if (branch_node)  // the column transforms read the Green spectrum
+    ORBIT_CUDA(cudaStreamUpdateCaptureDependencies(s, &branch_node, nullptr, 1, cudaStreamAddCaptureDependencies));
   rc = plain ? enqueue_conv<double>(c, s, &nl) : enqueue_conv<float>(c, s, &nl);
   if (rc) return rc;
   if (plain && !c->smem_kick) {
@@ -1038,6 +1069,16 @@ int orbit_sc2p5d_get_limits(orbit_sc2p5d_t* c, double* lim) {
   ORBIT_CUDA(cudaMemcpy(&h, c->d_st, sizeof(h), cudaMemcpyDeviceToHost));
   lim[0] = h.xmin; lim[1] = h.xmax; lim[2] = h.ymin; lim[3] = h.ymax; lim[4] = h.zmin; lim[5] = h.zmax;
   lim[6] = h.dx; lim[7] = h.dy; lim[8] = h.dz; lim[9] = h.xy_ratio; lim[10] = h.total_m;
+  return ORBIT_OK;
+}
+
+int orbit_sc2p5d_counters(orbit_sc2p5d_t* c, long long* kicks, long long* green_rebuilds) {
+  if (!c || !kicks || !green_rebuilds) return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_counters: bad argument");
+  if (c->used) ORBIT_CUDA(cudaEventSynchronize(c->done));
+  ScState h;
+  ORBIT_CUDA(cudaMemcpy(&h, c->d_st, sizeof(h), cudaMemcpyDeviceToHost));
+  *kicks = (long long)h.n_kicks;
+  *green_rebuilds = (long long)h.n_green;
   return ORBIT_OK;
 }
 

@@ -27,12 +27,14 @@ struct ScState {
   unsigned long long lam_absmax;                          //  order like their bit patterns), max |lambda|
   int dep_k;                                              // fraction bits of the integer deposit (0: FP64 path)
   unsigned ext_count;                                     // blocks done with the extrema scan (last one sets up)
+  unsigned long long n_kicks, n_green;                    // kicks solved, Green spectra rebuilt
 };
 
 // Arguments of the grid set-up run at the end of the extrema scan.
 struct SetupArgs {
   double inv_qscale;  // macrosize per unit of the fixed-point deposit (1 for the fp32 form)
   int nx, ny, nz;
+  cudaGraphConditionalHandle cond;  // inside a graph: the Green-rebuild branch of this kick (0: none)
 };
 
 // Units of the plain-form deposit for one bunch: K > 0 (uniform macrosize)
@@ -77,6 +79,10 @@ struct orbit_sc2p5d {
   cudaEvent_t done = nullptr;    // recorded after the last work that used the buffers
   bool used = false;
   cudaStream_t aux = nullptr;    // captures the Green-rebuild graph branch
+  // branch handle created with the set-up of the next kick while a graph is
+  // captured, and the graph it belongs to
+  cudaGraphConditionalHandle pending_cond = 0;
+  cudaGraph_t pending_graph = nullptr;
   bool smem_deposit = false, smem_kick = false;
   int dep_threads = 512, kick_threads = 512;
 };
@@ -95,6 +101,13 @@ cudaError_t sc_order_before(orbit_sc2p5d_t* c, cudaStream_t s);
 cudaError_t sc_mark_used(orbit_sc2p5d_t* c, cudaStream_t s);
 DepScales sc_dep_scales(const orbit_sc2p5d_t* c, const orbit_bunch_t* b);
 SetupArgs sc_setup_args(const orbit_sc2p5d_t* c, const DepScales& d);
+// While s is being captured into a graph (and the calculator can branch):
+// a conditional handle on that graph for the Green rebuild of the kick
+// whose set-up is about to be enqueued; with `pending` it is kept for that
+// kick's sc_enqueue_kick.  0 otherwise.
+cudaGraphConditionalHandle sc_green_cond(orbit_sc2p5d_t* c, cudaStream_t s, bool pending);
+// Forgets a pending handle (start of a new capture).
+void sc_clear_pending(orbit_sc2p5d_t* c);
 // Kick factor 2 L r_c / (beta^2 gamma^3) computed on the host exactly as
 // SpaceChargeCalc2p5D.cc:96 does (libm pow).
 double sc_host_factor(const orbit_sync_t& s, double length);

@@ -128,6 +128,7 @@ static __device__ __noinline__ void sc_setup_scalar(ScState* st, unsigned* statu
     st->inv_qscale = sa.inv_qscale;
     st->phi_absmax = 0ull;
     st->lam_absmax = 0ull;
+    if (sa.cond) cudaGraphSetConditional(sa.cond, st->green_dirty ? 1u : 0u);
   }
   st->skip = skip;
 }
@@ -326,11 +327,39 @@ __device__ __forceinline__ void load_dep_const(DepConst& d, const ScState* st, i
   d.skip = st->skip;
 }
 
+// 64-bit accumulation grids.  Global: native 64-bit atomics.  Shared: each
+// cell is a low and a high 32-bit word in two separate arrays (so that
+// random cells spread over all 32 banks), added with native 32-bit atomics:
+// the low word wraps modulo 2^32 and the add that wraps carries 1 into the
+// high word, so hi * 2^32 + lo, read once all adds are done, is the exact
+// sum modulo 2^64.
+template <bool SHARED> struct GridAcc;
+
+template <> struct GridAcc<false> {
+  unsigned long long* p;
+  __device__ __forceinline__ void add(int i, unsigned long long v) const { atomicAdd(p + i, v); }
+};
+
+template <> struct GridAcc<true> {
+  unsigned* lo;  // low words; the high words are at lo + hi_off
+  int hi_off;
+  __device__ __forceinline__ void add(int i, unsigned long long v) const {
+    unsigned l = (unsigned)v, h = (unsigned)(v >> 32);
+    unsigned old = atomicAdd(lo + i, l);
+    h += (old + l < old) ? 1u : 0u;
+    if (h) atomicAdd(lo + hi_off + i, h);
+  }
+  __device__ __forceinline__ unsigned long long get(int i) const {
+    return ((unsigned long long)lo[hi_off + i] << 32) | lo[i];
+  }
+};
+
 // Plain form: contributions are rounded to a fixed-point grid of step 1/S
 // (S a power of two with S * total macrosize <= 2^62) and summed as 64-bit
 // integers, so the deposit is exact and independent of summation order.
-__device__ __forceinline__ void deposit_plain(const DepConst& d, unsigned long long* rho, unsigned long long* zg,
-                                              double x, double y, double z, double ms) {
+template <bool SHARED>
+__device__ __forceinline__ void deposit_plain(const DepConst& d, const GridAcc<SHARED>& rho,
+                                              const GridAcc<SHARED>& zg, double x, double y, double z, double ms) {
   if (!(x < d.xmin || x > d.xmax || y < d.ymin || y > d.ymax)) {
     int ix, iy;
     double fx, fy;
@@ -341,22 +370,21 @@ __device__ __forceinline__ void deposit_plain(const DepConst& d, unsigned long l
     tsc_weights<double>(fy, wym, wy0, wyp);
     double ax[3] = {wxm * ms, wx0 * ms, wxp * ms};
     double wy[3] = {wym, wy0, wyp};
-    unsigned long long* base = rho + (ix - 1) * d.ny + (iy - 1);
+    const int base = (ix - 1) * d.ny + (iy - 1);
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
-      for (int j = 0; j < 3; ++j)
-        atomicAdd(base + i * d.ny + j, (unsigned long long)__double2ll_rn(ax[i] * wy[j]));
+      for (int j = 0; j < 3; ++j) rho.add(base + i * d.ny + j, (unsigned long long)__double2ll_rn(ax[i] * wy[j]));
   }
   if (!(z < d.zmin || z > d.zmax)) {
     int i0, ip;
     double w0, wp;
     g1_index<double>(z, d.zmin, d.inv_dz, d.nz, i0, ip, w0, wp);
     if (d.nz > 1) {
-      atomicAdd(zg + i0, (unsigned long long)__double2ll_rn(w0 * ms));
-      atomicAdd(zg + ip, (unsigned long long)__double2ll_rn(wp * ms));
+      zg.add(i0, (unsigned long long)__double2ll_rn(w0 * ms));
+      zg.add(ip, (unsigned long long)__double2ll_rn(wp * ms));
     } else {
-      atomicAdd(zg, (unsigned long long)__double2ll_rn(ms));
+      zg.add(0, (unsigned long long)__double2ll_rn(ms));
     }
   }
 }
@@ -475,8 +503,10 @@ __device__ __forceinline__ void load_dep_fix(DepFix& d, const ScState* st, int n
 // Integer deposit of one particle with unit weight scaled by 2^K (the
 // macrosize multiplies the grid afterwards).  Returns false when the
 // particle needs the FP64 path (never for finite coordinates in range).
-__device__ __forceinline__ bool deposit_fixed(const DepFix& d, unsigned long long* rho, unsigned long long* zg,
-                                              double x, double y, double z) {
+// SHARED: the grids are block-private shared memory.
+template <bool SHARED>
+__device__ __forceinline__ bool deposit_fixed(const DepFix& d, const GridAcc<SHARED>& rho,
+                                              const GridAcc<SHARED>& zg, double x, double y, double z) {
   unsigned long long kx = dkey(x), ky = dkey(y), kz = dkey(z);
   bool in2 = kx >= d.kxmin && kx <= d.kxmax && ky >= d.kymin && ky <= d.kymax;
   bool in1 = kz >= d.kzmin && kz <= d.kzmax;
@@ -495,14 +525,14 @@ __device__ __forceinline__ bool deposit_fixed(const DepFix& d, unsigned long lon
     tsc_w_fixed(fy, wy);
     const int sh = 60 - d.K;
     const long long half = 1ll << (sh - 1);
-    unsigned long long* base = rho + (ix - 1) * d.ny + (iy - 1);
+    const int base = (ix - 1) * d.ny + (iy - 1);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
       long long a = wx[i] << 4;
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
         long long p = __mul64hi(a, wy[j] << 4);  // Wx Wy in Q60
-        atomicAdd(base + i * d.ny + j, (unsigned long long)((p + half) >> sh));
+        rho.add(base + i * d.ny + j, (unsigned long long)((p + half) >> sh));
       }
     }
   }
@@ -510,10 +540,10 @@ __device__ __forceinline__ bool deposit_fixed(const DepFix& d, unsigned long lon
     const int sh = 56 - d.K;
     const long long half = 1ll << (sh - 1);
     if (d.nz > 1) {
-      atomicAdd(zg + i0, (unsigned long long)((((1ll << 56) - wp) + half) >> sh));
-      atomicAdd(zg + ip, (unsigned long long)((wp + half) >> sh));
+      zg.add(i0, (unsigned long long)((((1ll << 56) - wp) + half) >> sh));
+      zg.add(ip, (unsigned long long)((wp + half) >> sh));
     } else {
-      atomicAdd(zg, (unsigned long long)(1ll << d.K));
+      zg.add(0, (unsigned long long)(1ll << d.K));
     }
   }
   return true;

@@ -147,6 +147,12 @@ class DeviceSC2p5D:
         call("orbit_sc2p5d_get_limits", self.h, lim.ctypes.data_as(_dp))
         return lim
 
+    def counters(self):
+        """(kicks solved, Green spectra rebuilt) since creation."""
+        k, g = ctypes.c_longlong(), ctypes.c_longlong()
+        call("orbit_sc2p5d_counters", self.h, ctypes.byref(k), ctypes.byref(g))
+        return k.value, g.value
+
     def fields(self, x, y, z):
         x, y, z = (np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z))
         n = x.shape[0]

@@ -81,6 +81,7 @@ _SIGS = {
     "orbit_sc2p5d_get_grid": (ctypes.c_int, [_vp, ctypes.c_int, _dp]),
     "orbit_sc2p5d_get_limits": (ctypes.c_int, [_vp, _dp]),
     "orbit_sc2p5d_get_sizes": (ctypes.c_int, [_vp] + [ctypes.POINTER(ctypes.c_int)] * 4),
+    "orbit_sc2p5d_counters": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]),
     "orbit_sc2p5d_fields": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _dp]),
     "orbit_sc2p5d_track_static": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                  ctypes.c_int, ctypes.c_double, ctypes.c_double,

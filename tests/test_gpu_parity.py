@@ -173,6 +173,53 @@ def test_fused_equals_eager():
         l2.trackBunch(b2)
     assert coord_err(b1.getCoordinates(), b2.getCoordinates()) <= 1e-13
     assert abs(b1.getSyncParticle().time() - b2.getSyncParticle().time()) <= 1e-15 * b2.getSyncParticle().time()
+    # the captured program rebuilds the Green spectrum (a conditional graph
+    # branch) exactly when node-by-node tracking does
+    k1, g1 = c1._calc.counters()
+    k2, g2 = c2._calc.counters()
+    assert k1 == k2 == 3 * 8 and g1 == g2 and 1 <= g1 <= k1
+
+
+def test_fused_with_energy_kicks_equals_eager():
+    """Kickers that change dE inside the fused program: the passes after
+    them must use the new 1/(1+dp_p), not the one kept from the start of
+    the run, and the next run starts from the bunch's current dE."""
+    from orbit.teapot import KickTEAPOT, QuadTEAPOT
+    from orbit.space_charge.sc2p5d import setSC2p5DAccNodes
+    from orbit.teapot import DriftTEAPOT, TEAPOT_Lattice
+    from orbit_gb300 import workloads as W
+    from spacecharge import SpaceChargeCalc2p5D
+
+    def lattice(calc):
+        lat = TEAPOT_Lattice("kicked")
+        for c in range(3):
+            q = QuadTEAPOT("q%d" % c)
+            q.setLength(0.5)
+            q.addParam("kq", 0.5 if c % 2 == 0 else -0.5)
+            k = KickTEAPOT("k%d" % c)
+            k.setLength(0.4)
+            k.addParam("kx", 1e-5)
+            k.addParam("dE", 2e-4 * (c + 1))
+            d = DriftTEAPOT("d%d" % c)
+            d.setLength(1.0)
+            for node in (q, k, d):
+                lat.addNode(node)
+        lat.initialize()
+        setSC2p5DAccNodes(lat, 0.3, calc)
+        return lat
+
+    soa = W.c2_coords(10_000, seed=21)
+    b1 = gpu_bunch(soa, 1e10)
+    b2 = gpu_bunch(soa, 1e10)
+    l1 = lattice(SpaceChargeCalc2p5D(32, 32, 8))
+    l2 = lattice(SpaceChargeCalc2p5D(32, 32, 8))
+    l2.setFusedTracking(False)
+    for _ in range(3):
+        l1.trackBunch(b1)
+        l2.trackBunch(b2)
+    got, ref = b1.getCoordinates(), b2.getCoordinates()
+    assert np.max(np.abs(got[5] - soa[5])) > 1e-4  # the kickers acted
+    assert coord_err(got, ref) <= 1e-13
 
 
 def test_large_grid_global_path():
