@@ -103,6 +103,7 @@ int orbit_sc2p5d_track(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length);
 #define ORBIT_GRID_RHO 0
 #define ORBIT_GRID_PHI 1
 #define ORBIT_GRID_LONG 2
+#define ORBIT_GRID_LONG_DERIV 3 /* 2.5Drb only: getLongDerivativeGrid */
 /* getRhoGrid / getPhiGrid (nx*ny, row-major [ix][iy]) and getLongGrid (nz)
  * copied to host (wrap_spacechargecalc2p5d.cc:55-115).  Waits for the last
  * stream the calculator ran on. */
@@ -110,6 +111,24 @@ int orbit_sc2p5d_get_grid(orbit_sc2p5d_t* c, int which, double* host_out);
 /* lim = {xmin,xmax,ymin,ymax,zmin,zmax,dx,dy,dz,xy_ratio,total_macrosize} */
 int orbit_sc2p5d_get_limits(orbit_sc2p5d_t* c, double* lim);
 int orbit_sc2p5d_get_sizes(const orbit_sc2p5d_t* c, int* nx, int* ny, int* nz, int* form);
+/* SpaceChargeCalc2p5Drb(xSize, ySize, zSize[, xy_ratio]), plain FP64 form
+ * (src/spacecharge/wrap_spacechargecalc2p5d_rb.cc:37-50): the 2.5D kick
+ * plus a longitudinal kick of dE from the smoothed derivative of the line
+ * density and a pipe radius; the grid keeps the calculator's ratio and the
+ * Poisson solver grid is never reshaped (SpaceChargeCalc2p5Drb.cc:107-306).
+ * Destroyed with orbit_sc2p5d_destroy; grids, limits and counters through
+ * the orbit_sc2p5d_* calls (lim[10] is the rho-grid sum the kick divides
+ * by), the derivative grid as ORBIT_GRID_LONG_DERIV. */
+int orbit_sc2p5drb_create(orbit_sc2p5d_t** out, int nx, int ny, int nz, double xy_ratio);
+/* trackBunch(bunch, length, pipe_radius) (SpaceChargeCalc2p5Drb.cc:107-155) */
+int orbit_sc2p5drb_track(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, double pipe_radius);
+/* setLongAveragingPointsN / getLongAveragingPointsN (:309-318) */
+int orbit_sc2p5drb_set_long_avg(orbit_sc2p5d_t* c, int n);
+int orbit_sc2p5drb_get_long_avg(const orbit_sc2p5d_t* c, int* n);
+/* No counterpart in the reference (its values stay local to trackBunch):
+ * abx = {a_bunch, x_center, y_center} of the last kick. */
+int orbit_sc2p5drb_beam(orbit_sc2p5d_t* c, double* abx);
+
 /* No counterpart in the reference (diagnostic).  Kicks solved and Green
  * spectra rebuilt (PoissonSolverFFT2D::setGridXY followed by the Green
  * transform, PoissonSolverFFT2D.cc:103-172) since the calculator was
@@ -189,7 +208,7 @@ int orbit_tpb_bendfringeOUT(orbit_bunch_t* b, double rho);
 #define ORBIT_OP_WEDGEROT 18  /* d0 = e, i0 = frinout */
 #define ORBIT_OP_WEDGEDRIFT 19 /* d0 = e, i0 = inout */
 #define ORBIT_OP_WEDGEBEND 20 /* d0 = e, i0 = inout, d1 = rho, i1 = nsteps */
-#define ORBIT_OP_SC 32        /* i0 = calculator index, d0 = sc length */
+#define ORBIT_OP_SC 32        /* i0 = calculator index, d0 = sc length, d1 = pipe radius (2.5Drb calculators) */
 
 typedef struct {
   int32_t code, i0, i1, i2;

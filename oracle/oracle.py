@@ -91,6 +91,13 @@ def lib():
                                          ctypes.c_int, _dp, ctypes.POINTER(OracleSync),
                                          ctypes.POINTER(_vp), ctypes.c_int]
         L.oracle_rms_emittance.argtypes = [_dp, ctypes.c_int, _dp, _dp]
+        L.oracle_scrb_new.restype = _vp
+        L.oracle_scrb_new.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double]
+        L.oracle_scrb_set_long_avg.argtypes = [_vp, ctypes.c_int]
+        L.oracle_scrb_track.restype = ctypes.c_int
+        L.oracle_scrb_track.argtypes = [_vp, _dp, ctypes.c_int, _dp, ctypes.POINTER(OracleSync), ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_int]
+        L.oracle_scrb_extra.argtypes = [_vp, _dp, _dp]
         _lib = L
     return _lib
 
@@ -134,6 +141,33 @@ class OracleSC:
         x, y, z = (np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z))
         lib().oracle_sc_fields(self.h, n, _P(x), _P(y), _P(z), _P(ex), _P(ey), _P(lam))
         return ex, ey, lam
+
+
+class OracleSCrb(OracleSC):
+    """SpaceChargeCalc2p5Drb restated in C."""
+
+    def __init__(self, nx, ny, nz, xy_ratio=-1.0):
+        self.nx, self.ny, self.nz = nx, ny, nz
+        self.h = lib().oracle_scrb_new(nx, ny, nz, float(xy_ratio))
+        if not self.h:
+            raise ValueError("bad grid size")
+
+    def setLongAveragingPointsN(self, n):
+        lib().oracle_scrb_set_long_avg(self.h, int(n))
+
+    def track(self, soa: np.ndarray, sync: OracleSync, length: float, pipe_radius: float, msize=None,
+              nthreads=1) -> int:
+        assert soa.dtype == np.float64 and soa.flags.c_contiguous and soa.shape[0] == 6
+        m = None if msize is None else _P(np.ascontiguousarray(msize, dtype=np.float64))
+        return lib().oracle_scrb_track(self.h, _P(soa), soa.shape[1], m, ctypes.byref(sync), float(length),
+                                       float(pipe_radius), int(nthreads))
+
+    def extra(self):
+        """(derivative grid [nz], a_bunch, x_center, y_center)."""
+        zd = np.zeros(self.nz)
+        abx = np.zeros(3)
+        lib().oracle_scrb_extra(self.h, _P(zd), _P(abx))
+        return zd, abx[0], abx[1], abx[2]
 
 
 def tpb(name: str, soa: np.ndarray, sync: OracleSync, *args):
@@ -222,6 +256,12 @@ def ref():
         L.ref_sc_track.argtypes = [_vp, _vp, ctypes.c_double]
         L.ref_sc_grids.argtypes = [_vp, _dp, _dp, _dp, _dp]
         L.ref_sc_fields.argtypes = [_vp, ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.ref_scrb_new.restype = _vp
+        L.ref_scrb_new.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double]
+        L.ref_scrb_free.argtypes = [_vp]
+        L.ref_scrb_set_long_avg.argtypes = [_vp, ctypes.c_int]
+        L.ref_scrb_track.argtypes = [_vp, _vp, ctypes.c_double, ctypes.c_double]
+        L.ref_scrb_grids.argtypes = [_vp, _dp, _dp, _dp, _dp, _dp]
         _ref = L
     return _ref
 
@@ -298,3 +338,31 @@ class RefSC:
         x, y, z = (np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z))
         ref().ref_sc_fields(self.h, n, _P(x), _P(y), _P(z), _P(ex), _P(ey), _P(lam))
         return ex, ey, lam
+
+
+class RefSCrb:
+    """A reference ``SpaceChargeCalc2p5Drb`` driven through the harness."""
+
+    def __init__(self, nx, ny, nz, xy_ratio=-1.0):
+        self.nx, self.ny, self.nz = nx, ny, nz
+        self.h = ref().ref_scrb_new(nx, ny, nz, float(xy_ratio))
+
+    def __del__(self):
+        if getattr(self, "h", None) and _ref is not None:
+            _ref.ref_scrb_free(self.h)
+            self.h = None
+
+    def setLongAveragingPointsN(self, n):
+        ref().ref_scrb_set_long_avg(self.h, int(n))
+
+    def track(self, bunch: RefBunch, length: float, pipe_radius: float):
+        ref().ref_scrb_track(self.h, bunch.h, float(length), float(pipe_radius))
+
+    def grids(self):
+        rho = np.zeros(self.nx * self.ny)
+        phi = np.zeros(self.nx * self.ny)
+        zg = np.zeros(self.nz)
+        zd = np.zeros(self.nz)
+        lim = np.zeros(9)
+        ref().ref_scrb_grids(self.h, _P(rho), _P(phi), _P(zg), _P(zd), _P(lim))
+        return rho.reshape(self.nx, self.ny), phi.reshape(self.nx, self.ny), zg, zd, lim

@@ -173,6 +173,11 @@ struct oracle_sc {
   double* phi;
   double* zarr;
   double total_macrosize;
+  /* SpaceChargeCalc2p5Drb only (SpaceChargeCalc2p5Drb.cc:31-60) */
+  int rb;
+  int n_long_avg;
+  double* zderiv;
+  double a_bunch, x_c, y_c;
 };
 
 /* _defineGreenF (PoissonSolverFFT2D.cc:115-172) */
@@ -253,9 +258,23 @@ oracle_sc_t* oracle_sc_new(int nx, int ny, int nz, double xy_ratio) {
 void oracle_sc_free(oracle_sc_t* s) {
   if (!s) return;
   free(s->green_hat); free(s->work_hat); free(s->work_in);
-  free(s->rho); free(s->phi); free(s->zarr);
+  free(s->rho); free(s->phi); free(s->zarr); free(s->zderiv);
   free(s);
 }
+
+/* SpaceChargeCalc2p5Drb constructors (SpaceChargeCalc2p5Drb.cc:31-60): the
+ * same solver and grids as the 2.5D calculator plus the derivative grid;
+ * three smoothing points. */
+oracle_sc_t* oracle_scrb_new(int nx, int ny, int nz, double xy_ratio) {
+  oracle_sc_t* s = oracle_sc_new(nx, ny, nz, xy_ratio);
+  if (!s) return NULL;
+  s->rb = 1;
+  s->n_long_avg = 3;
+  s->zderiv = (double*)calloc((size_t)nz, sizeof(double));
+  return s;
+}
+
+void oracle_scrb_set_long_avg(oracle_sc_t* s, int n) { s->n_long_avg = n; }
 
 /* ------------------------------------------------------------------ */
 /* trackBunch                                                         */
@@ -272,6 +291,8 @@ typedef struct {
   double* zarr;
   double factor;
   int phase;
+  /* 2.5Drb longitudinal kick */
+  double lsf, lsf_in, lsf_out, a2, xc, yc;
 } slice_t;
 
 /* BunchExtremaCalculator::getExtremaXYZ loop (BunchExtremaCalculator.cc:47-62) */
@@ -324,11 +345,34 @@ static void slice_kick(slice_t* t) {
   }
 }
 
+/* kick loop of SpaceChargeCalc2p5Drb::trackBunch (SpaceChargeCalc2p5Drb.cc:132-154) */
+static void slice_kick_rb(slice_t* t) {
+  const oracle_sc_t* s = t->s;
+  double* x = t->soa;
+  double* xp = t->soa + (size_t)t->n;
+  double* y = t->soa + 2 * (size_t)t->n;
+  double* yp = t->soa + 3 * (size_t)t->n;
+  double* z = t->soa + 4 * (size_t)t->n;
+  double* dE = t->soa + 5 * (size_t)t->n;
+  for (int i = t->i0; i < t->i1; i++) {
+    double r2 = (x[i] - t->xc) * (x[i] - t->xc) + (y[i] - t->yc) * (y[i] - t->yc);
+    double ex, ey;
+    g2_grad(&s->grho, s->phi, x[i], y[i], &ex, &ey);
+    double ez = g1_value(&s->gz, s->zderiv, z[i]);
+    double Lfactor = -g1_value(&s->gz, s->zarr, z[i]) * t->factor;
+    xp[i] += ex * Lfactor;
+    yp[i] += ey * Lfactor;
+    double coeff = (r2 <= t->a2) ? t->lsf_in - r2 / t->a2 : t->lsf_out - log(r2);
+    dE[i] += ez * t->lsf * coeff;
+  }
+}
+
 static void* slice_worker(void* arg) {
   slice_t* t = (slice_t*)arg;
   if (t->phase == 0) slice_extrema(t);
   else if (t->phase == 1) slice_bin(t);
-  else slice_kick(t);
+  else if (t->phase == 2) slice_kick(t);
+  else slice_kick_rb(t);
   return NULL;
 }
 
@@ -417,6 +461,172 @@ int oracle_sc_track(oracle_sc_t* s, double* soa, int n, const double* msize,
   run_phase(sl, nt, 2);
   free(sl);
   return 0;
+}
+
+/* SpaceChargeCalc2p5Drb::calculateLongDerivative
+ * (SpaceChargeCalc2p5Drb.cc:257-306): quadratic least-squares fit over
+ * n_long_avg neighbouring cells, derivative at the cell centre. */
+static void rb_long_derivative(oracle_sc_t* s) {
+  const int nZ = s->nz;
+  const double z_step = s->gz.dz;
+  if (nZ == 1) {
+    s->zderiv[0] = 0.;
+    return;
+  }
+  if (nZ == 2) {
+    /* Grid1D::calcGradient at the midpoint (Grid1D.cc:520-534) */
+    double zm = (g1_gridz(&s->gz, 0) + g1_gridz(&s->gz, 1)) * 0.5;
+    double d = 0.;
+    if (!(zm < s->gz.zmin || zm > s->gz.zmax)) {
+      int i0, ip;
+      double w0, wp;
+      g1_ind(&s->gz, zm, &i0, &ip, &w0, &wp);
+      d = (s->zarr[ip] - s->zarr[i0]) / s->gz.dz;
+    }
+    s->zderiv[0] = d / z_step;
+    s->zderiv[1] = d / z_step;
+    return;
+  }
+  int nAvg = s->n_long_avg;
+  if (nZ < nAvg) nAvg = nZ;
+  for (int iz = 0; iz < nZ; iz++) {
+    double zc = g1_gridz(&s->gz, iz);
+    int i0 = iz - nAvg / 2;
+    if (i0 < 0) i0 = 0;
+    if (i0 + nAvg >= nZ) i0 = nZ - nAvg;
+    /* power sums: m[j] = sum t^j, q[j] = sum t^j y, t = 1..nAvg */
+    double m[5], q[5];
+    for (int j = 0; j < 5; j++) {
+      m[j] = 0.;
+      q[j] = 0.;
+      for (int i = i0; i < i0 + nAvg; i++) {
+        double t = 1.0 * (i - i0 + 1), y = s->zarr[i];
+        m[j] += pow(t, j) * pow(y, 0);
+        q[j] += pow(t, j) * pow(y, 1);
+      }
+    }
+    /* normal equations of y = a t^2 + b t + c by Cramer's rule */
+    double det = (m[0] * m[2] * m[4] - m[1] * m[1] * m[4] - m[0] * m[3] * m[3] + 2 * m[1] * m[2] * m[3] -
+                  m[2] * m[2] * m[2]);
+    double a = (q[0] * m[1] * m[3] - q[1] * m[0] * m[3] - q[0] * m[2] * m[2] + q[1] * m[1] * m[2] +
+                q[2] * m[0] * m[2] - q[2] * m[1] * m[1]) / det;
+    double b = (q[1] * m[0] * m[4] - q[0] * m[1] * m[4] + q[0] * m[2] * m[3] - q[2] * m[0] * m[3] -
+                q[1] * m[2] * m[2] + q[2] * m[1] * m[2]) / det;
+    double dy = 2 * a * (zc - g1_gridz(&s->gz, i0) + z_step) / z_step + b;
+    dy = dy / z_step;
+    s->zderiv[iz] = dy / z_step;
+  }
+}
+
+/* SpaceChargeCalc2p5Drb::trackBunch + bunchAnalysis
+ * (SpaceChargeCalc2p5Drb.cc:107-255). */
+int oracle_scrb_track(oracle_sc_t* s, double* soa, int n, const double* msize, const oracle_sync_t* sync,
+                      double length, double pipe_radius, int nthreads) {
+  if (n < 2) return 0; /* SpaceChargeCalc2p5Drb.cc:109-110 */
+  int nt = nthreads < 1 ? 1 : nthreads;
+  if (nt > n) nt = n;
+  slice_t* sl = (slice_t*)calloc((size_t)nt, sizeof(slice_t));
+  for (int k = 0; k < nt; k++) {
+    sl[k].s = s; sl[k].soa = soa; sl[k].msize = msize; sl[k].m0 = sync->macrosize; sl[k].n = n;
+    sl[k].i0 = (int)((long)n * k / nt);
+    sl[k].i1 = (int)((long)n * (k + 1) / nt);
+  }
+  run_phase(sl, nt, 0);
+  double xMin = sl[0].lim[0], xMax = sl[0].lim[1], yMin = sl[0].lim[2], yMax = sl[0].lim[3],
+         zMin = sl[0].lim[4], zMax = sl[0].lim[5];
+  for (int k = 1; k < nt; k++) {
+    if (sl[k].lim[0] < xMin) xMin = sl[k].lim[0];
+    if (sl[k].lim[1] > xMax) xMax = sl[k].lim[1];
+    if (sl[k].lim[2] < yMin) yMin = sl[k].lim[2];
+    if (sl[k].lim[3] > yMax) yMax = sl[k].lim[3];
+    if (sl[k].lim[4] < zMin) zMin = sl[k].lim[4];
+    if (sl[k].lim[5] > zMax) zMax = sl[k].lim[5];
+  }
+  if (xMin >= xMax || yMin >= yMax || zMin >= zMax) { free(sl); return -2; } /* :172-186 */
+  /* always stretched to the calculator's fixed ratio (:188-203) */
+  double xy_ratio_beam = (xMax - xMin) / (yMax - yMin);
+  double width, center;
+  if (xy_ratio_beam > s->xy_ratio) {
+    center = (yMax + yMin) / 2.0;
+    width = ((yMax - yMin) * (xy_ratio_beam / s->xy_ratio)) / 2.0;
+    yMin = center - width;
+    yMax = center + width;
+  } else {
+    center = (xMax + xMin) / 2.0;
+    width = ((xMax - xMin) / (xy_ratio_beam / s->xy_ratio)) / 2.0;
+    xMin = center - width;
+    xMax = center + width;
+  }
+  g2_setx(&s->grho, xMin, xMax);
+  g2_sety(&s->grho, yMin, yMax);
+  g1_set(&s->gz, zMin, zMax);
+  size_t ng = (size_t)s->nx * s->ny;
+  for (int k = 0; k < nt; k++) {
+    sl[k].rho = (k == 0) ? s->rho : (double*)calloc(ng, sizeof(double));
+    sl[k].zarr = (k == 0) ? s->zarr : (double*)calloc((size_t)s->nz, sizeof(double));
+  }
+  memset(s->rho, 0, sizeof(double) * ng);
+  memset(s->zarr, 0, sizeof(double) * (size_t)s->nz);
+  memset(s->zderiv, 0, sizeof(double) * (size_t)s->nz);
+  run_phase(sl, nt, 1);
+  for (int k = 1; k < nt; k++) {
+    for (size_t q = 0; q < ng; q++) s->rho[q] += sl[k].rho[q];
+    for (int q = 0; q < s->nz; q++) s->zarr[q] += sl[k].zarr[q];
+    free(sl[k].rho);
+    free(sl[k].zarr);
+  }
+  rb_long_derivative(s);
+  /* moments of the rho grid (:226-254); the reference takes y from the
+   * x grid (getGridX(iy)), kept for identical results */
+  double x_avg = 0., x2_avg = 0., y_avg = 0., y2_avg = 0., total = 0.;
+  for (int ix = 0; ix < s->nx; ix++) {
+    for (int iy = 0; iy < s->ny; iy++) {
+      double val = s->rho[(size_t)ix * s->ny + iy];
+      double x = s->grho.xmin + ix * s->grho.dx;
+      double y = s->grho.xmin + iy * s->grho.dx;
+      total += val;
+      x_avg += x * val;
+      x2_avg += x * x * val;
+      y_avg += y * val;
+      y2_avg += y * y * val;
+    }
+  }
+  x_avg /= total;
+  x2_avg /= total;
+  y_avg /= total;
+  y2_avg /= total;
+  s->x_c = x_avg;
+  s->y_c = y_avg;
+  x2_avg = fabs(x2_avg - x_avg * x_avg);
+  y2_avg = fabs(y2_avg - y_avg * y_avg);
+  s->a_bunch = sqrt(2 * (x2_avg + y2_avg));
+  s->total_macrosize = total;
+  double z_step = s->gz.dz;
+  find_potential(s);
+  double factor = 2 * length * sync->classical_radius / (pow(sync->beta, 2) * pow(sync->gamma, 3));
+  factor = factor / (z_step * total);
+  double a2 = s->a_bunch * s->a_bunch;
+  for (int k = 0; k < nt; k++) {
+    sl[k].factor = factor;
+    sl[k].lsf_in = 1.0 + 2 * log(pipe_radius / s->a_bunch);
+    sl[k].lsf_out = 2 * log(pipe_radius);
+    sl[k].a2 = a2;
+    sl[k].lsf = -length * sync->classical_radius * sync->mass / (pow(sync->gamma, 2));
+    sl[k].xc = s->x_c;
+    sl[k].yc = s->y_c;
+  }
+  run_phase(sl, nt, 3);
+  free(sl);
+  return 0;
+}
+
+void oracle_scrb_extra(const oracle_sc_t* s, double* zderiv, double* abx) {
+  if (zderiv && s->zderiv) memcpy(zderiv, s->zderiv, sizeof(double) * (size_t)s->nz);
+  if (abx) {
+    abx[0] = s->a_bunch;
+    abx[1] = s->x_c;
+    abx[2] = s->y_c;
+  }
 }
 
 void oracle_sc_grids(const oracle_sc_t* s, double* rho, double* phi, double* zg, double* lim) {
@@ -856,7 +1066,9 @@ int oracle_run_program(const oracle_op_t* ops, int nops, int turns, double* soa,
         case OP_WEDGEDRIFT: oracle_wedgedrift(soa, n, s, o->d[0], o->i0); break;
         case OP_WEDGEBEND: oracle_wedgebend(soa, n, s, o->d[0], o->i0, o->d[1], o->i1); break;
         case OP_SC: {
-          int rc = oracle_sc_track(calcs[o->i0], soa, n, msize, s, o->d[0], nthreads);
+          int rc = calcs[o->i0]->rb
+                       ? oracle_scrb_track(calcs[o->i0], soa, n, msize, s, o->d[0], o->d[1], nthreads)
+                       : oracle_sc_track(calcs[o->i0], soa, n, msize, s, o->d[0], nthreads);
           if (rc != 0) return rc;
           break;
         }

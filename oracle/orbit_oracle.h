@@ -54,6 +54,18 @@ void oracle_sc_grids(const oracle_sc_t* sc, double* rho, double* phi, double* zg
 void oracle_sc_fields(const oracle_sc_t* sc, int n, const double* x, const double* y,
                       const double* z, double* ex, double* ey, double* lam);
 
+/* SpaceChargeCalc2p5Drb(xSize, ySize, zSize[, xy_ratio]) -- 2.5D transverse
+ * kick plus the longitudinal kick from the smoothed derivative of the line
+ * density and a pipe radius (src/spacecharge/SpaceChargeCalc2p5Drb.cc).
+ * Freed with oracle_sc_free; grids read with oracle_sc_grids (lim[10] is
+ * the rho-grid sum the kick uses). */
+oracle_sc_t* oracle_scrb_new(int nx, int ny, int nz, double xy_ratio);
+void oracle_scrb_set_long_avg(oracle_sc_t* sc, int n);
+int oracle_scrb_track(oracle_sc_t* sc, double* soa, int n, const double* msize, const oracle_sync_t* sync,
+                      double length, double pipe_radius, int nthreads);
+/* derivative grid [nz]; abx = {a_bunch, x_center, y_center} */
+void oracle_scrb_extra(const oracle_sc_t* sc, double* zderiv, double* abx);
+
 /* ---- TEAPOT maps (src/teapot/teapotbase.cc) ---- */
 void oracle_rotatexy(double* soa, int n, double angle);
 void oracle_drift(double* soa, int n, oracle_sync_t* s, double length);

@@ -12,6 +12,7 @@
 #include "Bunch.hh"
 #include "SyncPart.hh"
 #include "SpaceChargeCalc2p5D.hh"
+#include "SpaceChargeCalc2p5Drb.hh"
 #include "Grid1D.hh"
 #include "Grid2D.hh"
 #include "teapotbase.hh"
@@ -123,6 +124,41 @@ void ref_sc_fields(void* sc, int n, const double* x, const double* y, const doub
     p->calcGradient(x[i], y[i], ex[i], ey[i]);
     lam[i] = zg->getValue(z[i]);
   }
+}
+
+// ---- SpaceChargeCalc2p5Drb (src/spacecharge/SpaceChargeCalc2p5Drb.cc) ----
+// Same constructor choice as SpaceChargeCalc2p5Drb_init
+// (src/spacecharge/wrap_spacechargecalc2p5d_rb.cc:37-50).
+void* ref_scrb_new(int nx, int ny, int nz, double xy_ratio) {
+  if (xy_ratio > 0.) return new SpaceChargeCalc2p5Drb(nx, ny, nz, xy_ratio);
+  return new SpaceChargeCalc2p5Drb(nx, ny, nz);
+}
+void ref_scrb_free(void* sc) { delete (SpaceChargeCalc2p5Drb*)sc; }
+void ref_scrb_set_long_avg(void* sc, int n) { ((SpaceChargeCalc2p5Drb*)sc)->setLongAveragingPointsN(n); }
+void ref_scrb_track(void* sc, void* b, double length, double pipe_radius) {
+  ((SpaceChargeCalc2p5Drb*)sc)->trackBunch((Bunch*)b, length, pipe_radius);
+}
+// rho, phi [nx*ny], zg, zderiv [nz], lim as ref_sc_grids
+void ref_scrb_grids(void* sc, double* rho, double* phi, double* zg, double* zd, double* lim) {
+  SpaceChargeCalc2p5Drb* c = (SpaceChargeCalc2p5Drb*)sc;
+  Grid2D* r = c->getRhoGrid();
+  Grid2D* p = c->getPhiGrid();
+  Grid1D* z = c->getLongGrid();
+  Grid1D* d = c->getLongDerivativeGrid();
+  int nx = r->getSizeX(), ny = r->getSizeY();
+  for (int i = 0; i < nx; ++i)
+    for (int j = 0; j < ny; ++j) {
+      rho[i * ny + j] = r->getValueOnGrid(i, j);
+      phi[i * ny + j] = p->getValueOnGrid(i, j);
+    }
+  for (int k = 0; k < z->getSizeZ(); ++k) {
+    zg[k] = z->getValueOnGrid(k);
+    zd[k] = d->getValueOnGrid(k);
+  }
+  lim[0] = r->getMinX(); lim[1] = r->getMaxX();
+  lim[2] = r->getMinY(); lim[3] = r->getMaxY();
+  lim[4] = z->getMinZ(); lim[5] = z->getMaxZ();
+  lim[6] = r->getStepX(); lim[7] = r->getStepY(); lim[8] = z->getStepZ();
 }
 
 // ---- teapot_base maps (src/teapot/teapotbase.cc) ----

@@ -75,8 +75,15 @@ __global__ void __launch_bounds__(512) k_pass(double* __restrict__ cx, double* _
       p.knl = knl_buf[i];
       p.knl_ok = true;
     }
-    if (KF == 1 && !k.skip && !kick_fixed(kf, P, Lm, p.x, p.y, p.z, p.xp, p.yp))
-      kick_plain(k, kick.phi, kick.lam, p.x, p.y, p.z, p.xp, p.yp);
+    if (KF == 1 && !k.skip) {
+      if (!kick_fixed(kf, P, Lm, p.x, p.y, p.z, p.xp, p.yp)) kick_plain(k, kick.phi, kick.lam, p.x, p.y, p.z, p.xp, p.yp);
+      if (kick.lamd) {  // 2.5Drb: longitudinal kick; dE changed
+        RbConst r;
+        load_rb_const(r, kick.st, kick.rb_lsf);
+        kick_rb_long(k, r, kick.lamd, p.x, p.y, p.z, p.dE);
+        p.knl_ok = false;
+      }
+    }
     if (KF == 2 && !k.skip) kick_fp32(k, Pf, Lf, p.x, p.y, p.z, p.xp, p.yp);
     apply_ops(p, ops, a, b, m);
     if (EXT) acc.add(p.x, p.y, p.z);
@@ -184,6 +191,8 @@ static KickArgs kick_args(orbit_sc2p5d_t* c, const orbit_sync_t& s, double lengt
   ka.lam_fix = c->d_lam_fix;
   ka.host_factor = sc_host_factor(s, length);
   ka.nx = c->nx; ka.ny = c->ny; ka.nz = c->nz; ka.form = c->form;
+  ka.lamd = c->rb ? c->d_lamd : nullptr;
+  ka.rb_lsf = c->rb ? sc_rb_long_factor(s, length) : 0.0;
   return ka;
 }
 
@@ -304,13 +313,16 @@ static int enqueue_turn(orbit_program_t* p, orbit_bunch_t* bu, cudaStream_t s, c
   bool sc_active = bu->n >= 2;  // SpaceChargeCalc2p5D.cc:79-80
   auto calc_of = [&](int i) -> orbit_sc2p5d_t* { return p->calcs[p->ops[plan.sc_idx[i]].i0]; };
   auto len_of = [&](int i) -> double { return p->ops[plan.sc_idx[i]].d[0]; };
+  auto pipe_of = [&](int i) -> double { return p->ops[plan.sc_idx[i]].d[1]; };
   int rc;
   // the first pass of the run stores 1/(1+dp_p); later passes load it and
   // store it again only when their ops change dE
   bool first = true;
-  auto km_of = [&](const Seg& sg, bool sc) -> int {
+  // (a 2.5Drb kick at the start of a pass also changes dE)
+  auto km_of = [&](const Seg& sg, bool sc, orbit_sc2p5d_t* kc = nullptr) -> int {
     if (!sc && sg.a == sg.b) return 0;  // enqueue_pass launches nothing
-    int km = first ? (int)KNL_STORE : (KNL_LOAD | (sg.dE ? KNL_STORE : 0));
+    bool dE = sg.dE || (kc && kc->rb);
+    int km = first ? (int)KNL_STORE : (KNL_LOAD | (dE ? KNL_STORE : 0));
     first = false;
     return km;
   };
@@ -330,18 +342,18 @@ static int enqueue_turn(orbit_program_t* p, orbit_bunch_t* bu, cudaStream_t s, c
     if (rc) return rc;
   }
   for (int i = 0; i < nsc; ++i) {
-    rc = sc_enqueue_kick(calc_of(i), bu, len_of(i), s, false, false, nl);
+    rc = sc_enqueue_kick(calc_of(i), bu, len_of(i), s, false, false, nl, pipe_of(i));
     if (rc) return rc;
     bool last = (i == nsc - 1);
     if (!last) {
       rc = enqueue_pass(bu, s, ops, plan.segs[i + 1], m, calc_of(i), len_of(i), calc_of(i + 1), true, kb,
-                        km_of(plan.segs[i + 1], true), nl);
+                        km_of(plan.segs[i + 1], true, calc_of(i)), nl);
     } else if (wrap) {
       rc = enqueue_pass(bu, s, ops, plan.wrap, m, calc_of(i), len_of(i), calc_of(0), false, kb,
-                        km_of(plan.wrap, true), nl);
+                        km_of(plan.wrap, true, calc_of(i)), nl);
     } else {
       rc = enqueue_pass(bu, s, ops, plan.segs[nsc], m, calc_of(i), len_of(i), nullptr, false, kb,
-                        km_of(plan.segs[nsc], true), nl);
+                        km_of(plan.segs[nsc], true, calc_of(i)), nl);
     }
     if (rc) return rc;
   }

@@ -31,6 +31,11 @@ double sc_host_factor(const orbit_sync_t& s, double length) {
   return 2 * length * s.classical_radius / (std::pow(s.beta, 2) * std::pow(s.gamma, 3));
 }
 
+// -L r_c m / gamma^2 (SpaceChargeCalc2p5Drb.cc:128), libm pow as the reference.
+double sc_rb_long_factor(const orbit_sync_t& s, double length) {
+  return -length * s.classical_radius * s.mass / (std::pow(s.gamma, 2));
+}
+
 // ---------------------------------------------------------------------
 // kernels
 // ---------------------------------------------------------------------
@@ -343,6 +348,120 @@ __global__ void k_phi_fix(const ScState* st, const double* __restrict__ phi, con
   if (i < nz) lam_fix[i] = phi_fixed(lam[i], slam);
 }
 
+// 2.5Drb: one cell of the smoothed line-density derivative
+// (SpaceChargeCalc2p5Drb::calculateLongDerivative, SpaceChargeCalc2p5Drb.cc:257-306),
+// a quadratic least-squares fit over navg cells solved by Cramer's rule,
+// with the reference's operation order and explicit rounding.
+__device__ double rb_deriv_cell(const double* lam, int nz, int navg, double zmin, double dz, int iz) {
+  if (nz < navg) navg = nz;
+  double zc = __dadd_rn(zmin, __dmul_rn(iz + 0.5, dz));
+  int i0 = iz - navg / 2;
+  if (i0 < 0) i0 = 0;
+  if (i0 + navg >= nz) i0 = nz - navg;
+  double m[5], q[5];
+  for (int j = 0; j < 5; ++j) {
+    m[j] = 0.0;
+    q[j] = 0.0;
+    for (int i = i0; i < i0 + navg; ++i) {
+      double t = (double)(i - i0 + 1), tj = 1.0;
+      for (int e = 0; e < j; ++e) tj = __dmul_rn(tj, t);  // t^j, exact for these small integers
+      m[j] = __dadd_rn(m[j], tj);
+      q[j] = __dadd_rn(q[j], __dmul_rn(tj, lam[i]));
+    }
+  }
+#define M(a, b) __dmul_rn(a, b)
+  double det = __dsub_rn(__dadd_rn(__dsub_rn(__dsub_rn(M(M(m[0], m[2]), m[4]), M(M(m[1], m[1]), m[4])),
+                                             M(M(m[0], m[3]), m[3])),
+                                   M(M(M(2.0, m[1]), m[2]), m[3])),
+                         M(M(m[2], m[2]), m[2]));
+  double an = __dsub_rn(__dadd_rn(__dadd_rn(__dsub_rn(__dsub_rn(M(M(q[0], m[1]), m[3]), M(M(q[1], m[0]), m[3])),
+                                                      M(M(q[0], m[2]), m[2])),
+                                            M(M(q[1], m[1]), m[2])),
+                                  M(M(q[2], m[0]), m[2])),
+                        M(M(q[2], m[1]), m[1]));
+  double bn = __dadd_rn(__dsub_rn(__dsub_rn(__dadd_rn(__dsub_rn(M(M(q[1], m[0]), m[4]), M(M(q[0], m[1]), m[4])),
+                                                      M(M(q[0], m[2]), m[3])),
+                                            M(M(q[2], m[0]), m[3])),
+                                  M(M(q[1], m[2]), m[2])),
+                        M(M(q[2], m[1]), m[2]));
+#undef M
+  double a = __ddiv_rn(an, det), b = __ddiv_rn(bn, det);
+  double z0 = __dadd_rn(zmin, __dmul_rn(i0 + 0.5, dz));
+  double y = __dadd_rn(__ddiv_rn(__dmul_rn(__dmul_rn(2.0, a), __dadd_rn(__dsub_rn(zc, z0), dz)), dz), b);
+  y = __ddiv_rn(y, dz);
+  return __ddiv_rn(y, dz);
+}
+
+// 2.5Drb analysis on the finished grids (one block): the rho-grid moments
+// that give the beam centre and a_bunch = sqrt(2 (<x^2> + <y^2>))
+// (SpaceChargeCalc2p5Drb.cc:226-254; the reference takes y from the x grid,
+// kept), the total macrosize the kick divides by, the pipe-radius terms of
+// the longitudinal kick (:124-136) and the derivative grid.
+__global__ void k_rb_analysis(ScState* st, const double* __restrict__ rho, const double* __restrict__ lam,
+                              double* lamd, int nx, int ny, int nz, int navg, double pipe_radius) {
+  if (st->skip) return;
+  const double xmin = st->xmin, dx = st->dx;
+  double s[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int idx = threadIdx.x; idx < nx * ny; idx += blockDim.x) {
+    int ix = idx / ny, iy = idx - ix * ny;
+    double val = rho[idx];
+    double x = __dadd_rn(xmin, __dmul_rn((double)ix, dx));
+    double y = __dadd_rn(xmin, __dmul_rn((double)iy, dx));
+    s[0] += val;
+    s[1] += x * val;
+    s[2] += x * x * val;
+    s[3] += y * val;
+    s[4] += y * y * val;
+  }
+  __shared__ double red[32][5];
+  for (int c = 0; c < 5; ++c)
+    for (int off = 16; off > 0; off >>= 1) s[c] += __shfl_xor_sync(0xffffffffu, s[c], off);
+  if ((threadIdx.x & 31) == 0)
+    for (int c = 0; c < 5; ++c) red[threadIdx.x >> 5][c] = s[c];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+      for (int c = 0; c < 5; ++c) t[c] += red[w][c];
+    double total = t[0];
+    double xa = t[1] / total, x2 = t[2] / total, ya = t[3] / total, y2 = t[4] / total;
+    x2 = fabs(x2 - xa * xa);
+    y2 = fabs(y2 - ya * ya);
+    double a = sqrt(2 * (x2 + y2));
+    st->rb_xc = xa;
+    st->rb_yc = ya;
+    st->rb_a2 = a * a;
+    st->rb_lin = 1.0 + 2 * log(pipe_radius / a);
+    st->rb_lout = 2 * log(pipe_radius);
+    st->total_m = total;
+  }
+  const double zmin = st->zmin, dz = st->dz;
+  if (nz == 1) {
+    if (threadIdx.x == 0) lamd[0] = 0.0;
+  } else if (nz == 2) {
+    if (threadIdx.x == 0) {
+      // Grid1D::calcGradient at the midpoint (Grid1D.cc:520-534, 568-627)
+      double g0 = __dadd_rn(zmin, __dmul_rn(0.5, dz)), g1 = __dadd_rn(zmin, __dmul_rn(1.5, dz));
+      double zm = __dmul_rn(__dadd_rn(g0, g1), 0.5);
+      double d = 0.0;
+      if (!(zm < zmin || zm > st->zmax)) {
+        double ind = __dsub_rn(__ddiv_rn(__dsub_rn(zm, zmin), dz), 0.5);
+        int i0 = (int)ind, ip;
+        double gz = __dadd_rn(zmin, __dmul_rn(i0 + 0.5, dz));
+        double frac = __ddiv_rn(__dsub_rn(zm, gz), dz);
+        if (i0 == 0 && frac < 0.) { i0 = 1; ip = 0; }
+        else if (i0 == 1) { if (frac > 0.) { ip = 0; } else { ip = 1; i0 = 0; } }
+        else { ip = i0 + 1; }
+        d = __ddiv_rn(__dsub_rn(lam[ip], lam[i0]), dz);
+      }
+      lamd[0] = __ddiv_rn(d, dz);
+      lamd[1] = __ddiv_rn(d, dz);
+    }
+  } else {
+    for (int iz = threadIdx.x; iz < nz; iz += blockDim.x) lamd[iz] = rb_deriv_cell(lam, nz, navg, zmin, dz, iz);
+  }
+}
+
 // Deposit, plain form.  SMEM: block-private fixed-point grids in shared
 // memory, flushed with one 64-bit atomic per non-zero cell.  With K > 0
 // (uniform macrosize) each particle deposits unit weight in units of 2^-K
@@ -426,13 +545,15 @@ __global__ void k_deposit_fp32(const double* __restrict__ x, const double* __res
 }
 
 // Kick (SpaceChargeCalc2p5D.cc:104-119): fixed-point gradient and line
-// density (kick_fixed), FP64 routine for the particles it declines.
+// density (kick_fixed), FP64 routine for the particles it declines.  With
+// lamd (2.5Drb) also the longitudinal kick of dE.
 template <bool SMEM>
 __global__ void k_kick_plain(const double* __restrict__ x, double* __restrict__ xp, const double* __restrict__ y,
                              double* __restrict__ yp, const double* __restrict__ z, int n, const ScState* st,
                              const double* __restrict__ phi, const double* __restrict__ lam,
                              const long long* __restrict__ phi_fix, const long long* __restrict__ lam_fix,
-                             double host_factor, int nx, int ny, int nz) {
+                             double host_factor, int nx, int ny, int nz, const double* __restrict__ lamd,
+                             double rb_lsf, double* __restrict__ dE) {
   KickConst k;
   load_kick_const(k, st, host_factor, nx, ny, nz);
   if (k.skip) return;
@@ -455,6 +576,13 @@ __global__ void k_kick_plain(const double* __restrict__ x, double* __restrict__ 
     if (!kick_fixed(kf, P, Lm, xi, yi, zi, a, b)) kick_plain(k, phi, lam, xi, yi, zi, a, b);
     xp[i] = a;
     yp[i] = b;
+    if (lamd) {
+      RbConst r;
+      load_rb_const(r, st, rb_lsf);
+      double e = dE[i];
+      kick_rb_long(k, r, lamd, xi, yi, zi, e);
+      dE[i] = e;
+    }
   }
 }
 
@@ -728,6 +856,7 @@ SetupArgs sc_setup_args(const orbit_sc2p5d_t* c, const DepScales& d) {
   sa.nx = c->nx;
   sa.ny = c->ny;
   sa.nz = c->nz;
+  sa.rb = c->rb ? 1 : 0;
   sa.cond = 0;
   return sa;
 }
@@ -786,7 +915,7 @@ static int add_green_branch(orbit_sc2p5d_t* c, cudaStream_t s, cudaGraphConditio
 }
 
 int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStream_t s, bool do_extrema,
-                    bool do_kick, int* launches) {
+                    bool do_kick, int* launches, double pipe_radius) {
   int nl = 0;
   const int n = b->n;
   const double* msz = b->has_msize ? b->d_msize : nullptr;
@@ -854,6 +983,15 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
   }
   rc = plain ? enqueue_rows_fwd<double>(c, s, &nl) : enqueue_rows_fwd<float>(c, s, &nl);
   if (rc) return rc;
+  if (c->rb) {
+    // beam centre, a_bunch and the derivative grid from the finished grids
+    ORBIT_PB("rb_analysis", s);
+    k_rb_analysis<<<1, 512, 0, s>>>(c->d_st, c->d_rho, c->d_lam, c->d_lamd, c->nx, c->ny, c->nz, c->n_long_avg,
+                                     pipe_radius);
+    ORBIT_PE(s);
+    ++nl;
+    ORBIT_LAUNCH_CHECK("sc2p5drb analysis");
+  }
   if (branch_node)  // the column transforms read the Green spectrum
     ORBIT_CUDA(cudaStreamUpdateCaptureDependencies(s, &branch_node, nullptr, 1, cudaStreamAddCaptureDependencies));
   rc = plain ? enqueue_conv<double>(c, s, &nl) : enqueue_conv<float>(c, s, &nl);
@@ -871,6 +1009,8 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
   }
   if (do_kick) {
     double hf = sc_host_factor(b->sync, length);
+    const double* lamd = c->rb ? c->d_lamd : nullptr;
+    double lsf = c->rb ? sc_rb_long_factor(b->sync, length) : 0.0;
     size_t smk = (plain ? sizeof(double) : sizeof(float)) * ((size_t)c->nx * c->ny + c->nz);
     const int* mt_kick = particle_kernel_threads() + 4;
     particle_geometry(c->smem_kick ? smk : 0, n, mt_kick[(plain ? 0 : 2) + (c->smem_kick ? 0 : 1)], &blocks,
@@ -880,11 +1020,13 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
       if (c->smem_kick)
         k_kick_plain<true><<<blocks, threads, smk, s>>>(b->coord(0), b->coord(1), b->coord(2), b->coord(3),
                                                         b->coord(4), n, c->d_st, c->d_phi, c->d_lam, c->d_phi_fix,
-                                                        c->d_lam_fix, hf, c->nx, c->ny, c->nz);
+                                                        c->d_lam_fix, hf, c->nx, c->ny, c->nz, lamd, lsf,
+                                                        b->coord(5));
       else
         k_kick_plain<false><<<blocks, threads, 0, s>>>(b->coord(0), b->coord(1), b->coord(2), b->coord(3),
                                                        b->coord(4), n, c->d_st, c->d_phi, c->d_lam, c->d_phi_fix,
-                                                       c->d_lam_fix, hf, c->nx, c->ny, c->nz);
+                                                       c->d_lam_fix, hf, c->nx, c->ny, c->nz, lamd, lsf,
+                                                       b->coord(5));
     } else {
       if (c->smem_kick)
         k_kick_fp32<true><<<blocks, threads, smk, s>>>(b->coord(0), b->coord(1), b->coord(2), b->coord(3),
@@ -971,6 +1113,7 @@ int orbit_sc2p5d_create(orbit_sc2p5d_t** out, int nx, int ny, int nz, double xy_
   A((void**)&c->d_rho, sizeof(double) * ng);
   A((void**)&c->d_phi, sizeof(double) * ng);
   A((void**)&c->d_lam, sizeof(double) * nz);
+  A((void**)&c->d_lamd, sizeof(double) * nz);
   A((void**)&c->d_gbuf, sizeof(double) * (size_t)c->nx2 * c->ny2);
   if (form == ORBIT_FORM_PLAIN) {
     A((void**)&c->d_rho_q, sizeof(unsigned long long) * ng);
@@ -1032,7 +1175,7 @@ int orbit_sc2p5d_destroy(orbit_sc2p5d_t* c) {
   if (c->used) cudaEventSynchronize(c->done);
   if (c->done) cudaEventDestroy(c->done);
   if (c->aux) cudaStreamDestroy(c->aux);
-  void* ptrs[] = {c->d_st, c->d_rho_q, c->d_z_q, c->d_rho_f, c->d_z_f, c->d_rho, c->d_phi, c->d_lam,
+  void* ptrs[] = {c->d_st, c->d_rho_q, c->d_z_q, c->d_rho_f, c->d_z_f, c->d_rho, c->d_phi, c->d_lam, c->d_lamd,
                   c->d_phi_f, c->d_lam_f, c->d_hat, c->d_green, c->d_gbuf, c->d_gscratch, c->d_tw_x, c->d_tw_y,
                   c->d_phi_fix, c->d_lam_fix};
   for (void* p : ptrs)
@@ -1041,8 +1184,50 @@ int orbit_sc2p5d_destroy(orbit_sc2p5d_t* c) {
   return ORBIT_OK;
 }
 
+int orbit_sc2p5drb_create(orbit_sc2p5d_t** out, int nx, int ny, int nz, double xy_ratio) {
+  int rc = orbit_sc2p5d_create(out, nx, ny, nz, xy_ratio, ORBIT_FORM_PLAIN);
+  if (rc) return rc;
+  (*out)->rb = true;
+  (*out)->n_long_avg = 3;  // SpaceChargeCalc2p5Drb.cc:42
+  return ORBIT_OK;
+}
+
+int orbit_sc2p5drb_set_long_avg(orbit_sc2p5d_t* c, int n) {
+  if (!c || !c->rb || n < 1) return set_error(ORBIT_ERR_ARG, "orbit_sc2p5drb_set_long_avg: bad argument");
+  c->n_long_avg = n;
+  return ORBIT_OK;
+}
+
+int orbit_sc2p5drb_get_long_avg(const orbit_sc2p5d_t* c, int* n) {
+  if (!c || !c->rb || !n) return set_error(ORBIT_ERR_ARG, "orbit_sc2p5drb_get_long_avg: bad argument");
+  *n = c->n_long_avg;
+  return ORBIT_OK;
+}
+
+int orbit_sc2p5drb_track(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, double pipe_radius) {
+  if (!c || !b || !c->rb) return set_error(ORBIT_ERR_ARG, "orbit_sc2p5drb_track: null or non-2.5Drb handle");
+  if (b->n < 2) return ORBIT_OK;  // SpaceChargeCalc2p5Drb.cc:109-110
+  ORBIT_CUDA(sc_order_before(c, b->stream));
+  int rc = sc_enqueue_kick(c, b, length, b->stream, true, true, nullptr, pipe_radius);
+  if (rc) return rc;
+  ORBIT_CUDA(sc_mark_used(c, b->stream));
+  return ORBIT_OK;
+}
+
+int orbit_sc2p5drb_beam(orbit_sc2p5d_t* c, double* abx) {
+  if (!c || !c->rb || !abx) return set_error(ORBIT_ERR_ARG, "orbit_sc2p5drb_beam: bad argument");
+  if (c->used) ORBIT_CUDA(cudaEventSynchronize(c->done));
+  ScState h;
+  ORBIT_CUDA(cudaMemcpy(&h, c->d_st, sizeof(h), cudaMemcpyDeviceToHost));
+  abx[0] = std::sqrt(h.rb_a2);
+  abx[1] = h.rb_xc;
+  abx[2] = h.rb_yc;
+  return ORBIT_OK;
+}
+
 int orbit_sc2p5d_track(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length) {
   if (!c || !b) return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_track: null handle");
+  if (c->rb) return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_track: a 2.5Drb calculator needs orbit_sc2p5drb_track");
   if (b->n < 2) return ORBIT_OK;  // SpaceChargeCalc2p5D.cc:79-80
   ORBIT_CUDA(sc_order_before(c, b->stream));
   int rc = sc_enqueue_kick(c, b, length, b->stream, true, true, nullptr);
@@ -1058,6 +1243,8 @@ int orbit_sc2p5d_get_grid(orbit_sc2p5d_t* c, int which, double* host_out) {
   if (which == ORBIT_GRID_RHO) ORBIT_CUDA(cudaMemcpy(host_out, c->d_rho, sizeof(double) * ng, cudaMemcpyDeviceToHost));
   else if (which == ORBIT_GRID_PHI) ORBIT_CUDA(cudaMemcpy(host_out, c->d_phi, sizeof(double) * ng, cudaMemcpyDeviceToHost));
   else if (which == ORBIT_GRID_LONG) ORBIT_CUDA(cudaMemcpy(host_out, c->d_lam, sizeof(double) * c->nz, cudaMemcpyDeviceToHost));
+  else if (which == ORBIT_GRID_LONG_DERIV && c->rb)
+    ORBIT_CUDA(cudaMemcpy(host_out, c->d_lamd, sizeof(double) * c->nz, cudaMemcpyDeviceToHost));
   else return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_get_grid: unknown grid");
   return ORBIT_OK;
 }

@@ -27,6 +27,9 @@ struct ScState {
   unsigned long long lam_absmax;                          //  order like their bit patterns), max |lambda|
   int dep_k;                                              // fraction bits of the integer deposit (0: FP64 path)
   unsigned ext_count;                                     // blocks done with the extrema scan (last one sets up)
+  // 2.5Drb: beam centre, a_bunch^2 and the two pipe-radius terms of the
+  // longitudinal kick (SpaceChargeCalc2p5Drb.cc:124-136, 226-254)
+  double rb_xc, rb_yc, rb_a2, rb_lin, rb_lout;
   unsigned long long n_kicks, n_green;                    // kicks solved, Green spectra rebuilt
 };
 
@@ -34,6 +37,7 @@ struct ScState {
 struct SetupArgs {
   double inv_qscale;  // macrosize per unit of the fixed-point deposit (1 for the fp32 form)
   int nx, ny, nz;
+  int rb;             // SpaceChargeCalc2p5Drb set-up: fixed ratio, solver grid never reshaped
   cudaGraphConditionalHandle cond;  // inside a graph: the Green-rebuild branch of this kick (0: none)
 };
 
@@ -84,6 +88,11 @@ struct orbit_sc2p5d {
   cudaGraphConditionalHandle pending_cond = 0;
   cudaGraph_t pending_graph = nullptr;
   bool smem_deposit = false, smem_kick = false;
+  // SpaceChargeCalc2p5Drb (plain form): longitudinal kick from the smoothed
+  // derivative of the line density
+  bool rb = false;
+  int n_long_avg = 3;
+  double* d_lamd = nullptr;               // derivative grid (nz)
   int dep_threads = 512, kick_threads = 512;
 };
 
@@ -94,7 +103,7 @@ namespace orbit {
 // fused pass; `do_kick` = false when the kick is deferred to the next fused
 // pass.  Returns the number of kernel launches added through *launches.
 int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStream_t st,
-                    bool do_extrema, bool do_kick, int* launches);
+                    bool do_extrema, bool do_kick, int* launches, double pipe_radius = 0.0);
 // Cross-stream ordering of a calculator's buffers: work on stream s waits
 // for the last recorded use, then records a new one.
 cudaError_t sc_order_before(orbit_sc2p5d_t* c, cudaStream_t s);
@@ -111,6 +120,9 @@ void sc_clear_pending(orbit_sc2p5d_t* c);
 // Kick factor 2 L r_c / (beta^2 gamma^3) computed on the host exactly as
 // SpaceChargeCalc2p5D.cc:96 does (libm pow).
 double sc_host_factor(const orbit_sync_t& s, double length);
+// Longitudinal kick factor of the 2.5Drb calculator, -L r_c m / gamma^2
+// (SpaceChargeCalc2p5Drb.cc:128).
+double sc_rb_long_factor(const orbit_sync_t& s, double length);
 
 // Per-particle SC kick and extrema helpers used inside fused passes.
 struct KickArgs {
@@ -123,6 +135,8 @@ struct KickArgs {
   const long long* lam_fix;
   double host_factor;
   int nx, ny, nz, form;
+  const double* lamd;     // 2.5Drb: derivative grid, else null
+  double rb_lsf;          // 2.5Drb: -L r_c m / gamma^2
 };
 
 }  // namespace orbit

@@ -88,7 +88,22 @@ static __device__ __noinline__ void sc_setup_scalar(ScState* st, unsigned* statu
     double xy = st->xy_ratio;
     double ratio_beam = __ddiv_rn(__dsub_rn(xMax, xMin), __dsub_rn(yMax, yMin));
     int set_solver = 0;
-    if (fabs(__dsub_rn(ratio_beam, xy)) < __dmul_rn(0.25, xy)) {  // :152-168
+    if (sa.rb) {
+      // SpaceChargeCalc2p5Drb::bunchAnalysis (SpaceChargeCalc2p5Drb.cc:188-203):
+      // always stretched to the calculator's own ratio, which never changes
+      double width, center;
+      if (ratio_beam > xy) {
+        center = __ddiv_rn(__dadd_rn(yMax, yMin), 2.0);
+        width = __ddiv_rn(__dmul_rn(__dsub_rn(yMax, yMin), __ddiv_rn(ratio_beam, xy)), 2.0);
+        yMin = __dsub_rn(center, width);
+        yMax = __dadd_rn(center, width);
+      } else {
+        center = __ddiv_rn(__dadd_rn(xMax, xMin), 2.0);
+        width = __ddiv_rn(__ddiv_rn(__dsub_rn(xMax, xMin), __ddiv_rn(ratio_beam, xy)), 2.0);
+        xMin = __dsub_rn(center, width);
+        xMax = __dadd_rn(center, width);
+      }
+    } else if (fabs(__dsub_rn(ratio_beam, xy)) < __dmul_rn(0.25, xy)) {  // :152-168
       double width, center;
       if (ratio_beam > xy) {
         center = __ddiv_rn(__dadd_rn(yMax, yMin), 2.0);
@@ -113,9 +128,10 @@ static __device__ __noinline__ void sc_setup_scalar(ScState* st, unsigned* statu
     st->xmin = xMin; st->xmax = xMax; st->ymin = yMin; st->ymax = yMax;
     st->dx = dx; st->dy = dy; st->inv_dx = __drcp_rn(dx); st->inv_dy = __drcp_rn(dy);
     st->zmin = zMin; st->zmax = zMax; st->dz = dz; st->inv_dz = __drcp_rn(dz);
-    st->xy_ratio = xy;
-    // solver-shape check (SpaceChargeCalc2p5D.cc:208-216)
-    if (!set_solver) {
+    if (!sa.rb) st->xy_ratio = xy;
+    // solver-shape check (SpaceChargeCalc2p5D.cc:208-216); the 2.5Drb
+    // calculator keeps its solver grid
+    if (!set_solver && !sa.rb) {
       double sr = __ddiv_rn(__dsub_rn(st->sxmax, st->sxmin), __dsub_rn(st->symax, st->symin));
       if (fabs(__dsub_rn(sr, xy)) > 0.00000001) set_solver = 1;
     }
@@ -223,6 +239,34 @@ __device__ __forceinline__ void load_kick_const(KickConst& k, const ScState* st,
   k.fac = host_factor / (st->dz * st->total_m);
   k.nx = nx; k.ny = ny; k.nz = nz;
   k.skip = st->skip;
+}
+
+// 2.5Drb longitudinal kick (SpaceChargeCalc2p5Drb.cc:132-154):
+// dE += ez(z) * lsf * coeff(r^2), ez the smoothed derivative of the line
+// density (Grid1D::getValue), r measured from the beam centre, coeff =
+// 1 + 2 ln(R/a) - r^2/a^2 inside a = a_bunch, 2 ln R - ln r^2 outside.
+struct RbConst {
+  double xc, yc, a2, lin, lout, lsf;
+};
+
+__device__ __forceinline__ void load_rb_const(RbConst& r, const ScState* st, double lsf) {
+  r.xc = st->rb_xc; r.yc = st->rb_yc; r.a2 = st->rb_a2;
+  r.lin = st->rb_lin; r.lout = st->rb_lout; r.lsf = lsf;
+}
+
+__device__ __forceinline__ void kick_rb_long(const KickConst& k, const RbConst& r, const double* __restrict__ lamd,
+                                             double x, double y, double z, double& dE) {
+  double ez = 0.0;
+  if (!(z < k.zmin || z > k.zmax)) {
+    int i0, ip;
+    double w0, wp;
+    g1_index<double>(z, k.zmin, k.inv_dz, k.nz, i0, ip, w0, wp);
+    ez = (k.nz > 1) ? (w0 * lamd[i0] + wp * lamd[ip]) : lamd[0];
+  }
+  double ddx = x - r.xc, ddy = y - r.yc;
+  double r2 = ddx * ddx + ddy * ddy;
+  double coeff = (r2 <= r.a2) ? r.lin - r2 / r.a2 : r.lout - log(r2);
+  dE += ez * r.lsf * coeff;
 }
 
 // FP64 plain form: phi/lam may be in shared or global memory.

@@ -24,3 +24,25 @@ class SC2p5D_AccNode(SC_Base_AccNode):
             self.sc_calculator.trackBunch(bunch, self.sc_length, self.boundary)
         else:
             self.sc_calculator.trackBunch(bunch, self.sc_length)
+
+
+class SC2p5Drb_AccNode(SC_Base_AccNode):
+    """Calls SpaceChargeCalc2p5Drb.trackBunch(bunch, sc_length, pipe_radius)
+    (py/orbit/space_charge/sc2p5d/scAccNodes.py:53-84)."""
+
+    def __init__(self, sc_calculator, name="no name"):
+        SC_Base_AccNode.__init__(self, sc_calculator, name)
+        self.setType("SC2p5Drb")
+        self.pipe_radius = 1.0
+
+    def setPipeRadius(self, pipe_radius):
+        self.pipe_radius = pipe_radius
+
+    def getPipeRadius(self):
+        return self.pipe_radius
+
+    def track(self, paramsDict):
+        if self.switcher is not True:
+            return
+        bunch = paramsDict["bunch"]
+        self.sc_calculator.trackBunch(bunch, self.sc_length, self.pipe_radius)

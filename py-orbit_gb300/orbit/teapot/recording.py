@@ -35,13 +35,13 @@ class BunchRecorder:
     def _record_op(self, code, ints, dbls):
         self.ops.append((int(code), tuple(ints), tuple(dbls)))
 
-    def _record_sc(self, calc, length):
+    def _record_sc(self, calc, length, pipe_radius=0.0):
         k = self._cidx.get(id(calc))
         if k is None:
             k = len(self.calcs)
             self._cidx[id(calc)] = k
             self.calcs.append(calc)
-        self.ops.append((OP["SC"], (k,), (float(length),)))
+        self.ops.append((OP["SC"], (k,), (float(length), float(pipe_radius))))
 
     def _record_host(self, fn):
         """fn(bunch) runs on the host once per replayed turn (turn counters)."""

@@ -15,7 +15,7 @@ from . import _native
 from ._native import (FORM_FP32, FORM_PLAIN, OP, OrbitError, SpaceChargeError, Sync, call, load,
                       library_path)
 
-__all__ = ["DeviceBunch", "DeviceSC2p5D", "DeviceProgram", "OrbitError", "SpaceChargeError", "load",
+__all__ = ["DeviceBunch", "DeviceSC2p5D", "DeviceSC2p5Drb", "DeviceProgram", "OrbitError", "SpaceChargeError", "load",
            "FORM_PLAIN", "FORM_FP32", "OP", "library_path", "version"]
 
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -137,10 +137,10 @@ class DeviceSC2p5D:
         call("orbit_sc2p5d_track", self.h, bunch.h, float(length))
 
     def grid(self, which: int) -> np.ndarray:
-        n = self.nz if which == _native.GRID_LONG else self.nx * self.ny
+        n = self.nz if which in (_native.GRID_LONG, _native.GRID_LONG_DERIV) else self.nx * self.ny
         out = np.empty(n, dtype=np.float64)
         call("orbit_sc2p5d_get_grid", self.h, int(which), out.ctypes.data_as(_dp))
-        return out if which == _native.GRID_LONG else out.reshape(self.nx, self.ny)
+        return out if which in (_native.GRID_LONG, _native.GRID_LONG_DERIV) else out.reshape(self.nx, self.ny)
 
     def limits(self) -> np.ndarray:
         lim = np.empty(11, dtype=np.float64)
@@ -159,6 +159,33 @@ class DeviceSC2p5D:
         ex, ey, lam = np.empty(n), np.empty(n), np.empty(n)
         call("orbit_sc2p5d_fields", self.h, n, *[a.ctypes.data_as(_dp) for a in (x, y, z, ex, ey, lam)])
         return ex, ey, lam
+
+
+class DeviceSC2p5Drb(DeviceSC2p5D):
+    """The device SpaceChargeCalc2p5Drb (plain FP64 form)."""
+
+    def __init__(self, nx: int, ny: int, nz: int, xy_ratio: float = -1.0):
+        h = ctypes.c_void_p()
+        call("orbit_sc2p5drb_create", ctypes.byref(h), int(nx), int(ny), int(nz), float(xy_ratio))
+        self.h = h
+        self.nx, self.ny, self.nz, self.form = int(nx), int(ny), int(nz), FORM_PLAIN
+
+    def track_rb(self, bunch: DeviceBunch, length: float, pipe_radius: float):
+        call("orbit_sc2p5drb_track", self.h, bunch.h, float(length), float(pipe_radius))
+
+    def set_long_avg(self, n: int):
+        call("orbit_sc2p5drb_set_long_avg", self.h, int(n))
+
+    def get_long_avg(self) -> int:
+        v = ctypes.c_int()
+        call("orbit_sc2p5drb_get_long_avg", self.h, ctypes.byref(v))
+        return v.value
+
+    def beam(self):
+        """(a_bunch, x_center, y_center) of the last kick."""
+        out = np.zeros(3)
+        call("orbit_sc2p5drb_beam", self.h, out.ctypes.data_as(_dp))
+        return float(out[0]), float(out[1]), float(out[2])
 
 
 class DeviceProgram:

@@ -25,7 +25,7 @@ ORBIT_ERR_UNSUPPORTED = -9
 FORM_PLAIN = 0
 FORM_FP32 = 1
 
-GRID_RHO, GRID_PHI, GRID_LONG = 0, 1, 2
+GRID_RHO, GRID_PHI, GRID_LONG, GRID_LONG_DERIV = 0, 1, 2, 3
 
 # op codes (ORBIT_OP_* in include/orbit_gb300.h)
 OP = dict(DRIFT=1, QUAD1=2, QUAD2=3, QFRIN=4, QFROUT=5, BEND1=6, BEND2=7, BEND3=8, BEND4=9, BFRIN=10,
@@ -82,6 +82,12 @@ _SIGS = {
     "orbit_sc2p5d_get_limits": (ctypes.c_int, [_vp, _dp]),
     "orbit_sc2p5d_get_sizes": (ctypes.c_int, [_vp] + [ctypes.POINTER(ctypes.c_int)] * 4),
     "orbit_sc2p5d_counters": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]),
+    "orbit_sc2p5drb_create": (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_double]),
+    "orbit_sc2p5drb_track": (ctypes.c_int, [_vp, _vp, ctypes.c_double, ctypes.c_double]),
+    "orbit_sc2p5drb_set_long_avg": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "orbit_sc2p5drb_get_long_avg": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int)]),
+    "orbit_sc2p5drb_beam": (ctypes.c_int, [_vp, _dp]),
     "orbit_sc2p5d_fields": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _dp]),
     "orbit_sc2p5d_track_static": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                  ctypes.c_int, ctypes.c_double, ctypes.c_double,

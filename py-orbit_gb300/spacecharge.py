@@ -410,4 +410,73 @@ class SpaceChargeCalc2p5D:
         return self._calc.fields(x, y, z)
 
 
-__all__ = ["SpaceChargeCalc2p5D", "Grid2D", "Grid1D"]
+class SpaceChargeCalc2p5Drb(SpaceChargeCalc2p5D):
+    """``SpaceChargeCalc2p5Drb(xSize, ySize, zSize[, xy_ratio])``
+    (src/spacecharge/SpaceChargeCalc2p5Drb.cc, wrap_spacechargecalc2p5d_rb.cc:37-50):
+    the 2.5D transverse kick plus a longitudinal kick of dE from the
+    smoothed derivative of the line density and a pipe radius.  The grid
+    keeps the calculator's aspect ratio and the Poisson solver grid is never
+    reshaped.  Plain FP64 form."""
+
+    def __init__(self, xSize, ySize, zSize, xy_ratio=-1.0):
+        from orbit_gb300 import DeviceSC2p5Drb
+        if xSize < 3 or ySize < 3:
+            _finalize("Grid2D: the grid size too small (should be more than 3)")
+        if zSize < 1:
+            _finalize("Grid1D: the grid size is too small (should be more than 0)")
+        self.form = "plain"
+        self._calc = DeviceSC2p5Drb(xSize, ySize, zSize, xy_ratio)
+        self._nx, self._ny, self._nz = int(xSize), int(ySize), int(zSize)
+        self._version = 0
+        self._seen = {}
+        self._rho = Grid2D(xSize, ySize)
+        self._phi = Grid2D(xSize, ySize)
+        self._long = Grid1D(zSize)
+        self._deriv = Grid1D(zSize)
+        self._rho._bind(lambda g: self._refresh(g, 0))
+        self._phi._bind(lambda g: self._refresh(g, 1))
+        self._long._bind(lambda g: self._refresh(g, 2))
+        self._deriv._bind(lambda g: self._refresh(g, 3))
+
+    def _refresh(self, g, which):
+        if which != 3:
+            return SpaceChargeCalc2p5D._refresh(self, g, which)
+        if self._version == 0 or self._seen.get(which) == self._version:
+            return
+        self._seen[which] = self._version
+        src = g._src
+        g._src = None
+        try:
+            lim = self._calc.limits()
+            g.setGridZ(lim[4], lim[5])
+            g._dz = lim[8]
+            g._arr = np.array(self._calc.grid(3))
+        finally:
+            g._src = src
+
+    def trackBunch(self, bunch, length, pipe_radius):
+        """Transverse and longitudinal space-charge kicks of a lattice part of
+        the given length (SpaceChargeCalc2p5Drb.cc:107-155)."""
+        rec = getattr(bunch, "_record_sc", None)
+        if rec is not None:
+            rec(self, float(length), float(pipe_radius))
+            return
+        if bunch.getSizeGlobal() < 2:
+            return
+        dev = bunch._device_bunch()
+        self._calc.track_rb(dev, float(length), float(pipe_radius))
+        bunch._device_modified()
+        self._version += 1
+        dev.sync()
+
+    def getLongDerivativeGrid(self) -> Grid1D:
+        return self._deriv
+
+    def setLongAveragingPointsN(self, n_points):
+        self._calc.set_long_avg(int(n_points))
+
+    def getLongAveragingPointsN(self) -> int:
+        return self._calc.get_long_avg()
+
+
+__all__ = ["SpaceChargeCalc2p5D", "SpaceChargeCalc2p5Drb", "Grid2D", "Grid1D"]

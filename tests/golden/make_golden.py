@@ -81,6 +81,40 @@ def sc_case(name, soa, nx, ny, nz, xy_ratio, seq, ek=1.0, msize=1e9):
     print("wrote", name, "kicks", k)
 
 
+def scrb_case(name, soa, nx, ny, nz, xy_ratio, navg, pipe_radius, seq, ek=1.0, msize=1e9):
+    """SpaceChargeCalc2p5Drb: seq of ("sc", L) or maps; records the grids, the
+    derivative grid and the coordinates after each kick."""
+    b = O.RefBunch(soa, ek, msize)
+    sc = O.RefSCrb(nx, ny, nz, xy_ratio)
+    sc.setLongAveragingPointsN(navg)
+    out = {"init": soa, "nx": nx, "ny": ny, "nz": nz, "xy_ratio": xy_ratio, "ek": ek, "macrosize": msize,
+           "navg": navg, "pipe_radius": pipe_radius}
+    k = 0
+    seq_txt = []
+    for step in seq:
+        if step[0] == "sc":
+            sc.track(b, step[1], pipe_radius)
+            rho, phi, zg, zd, lim = sc.grids()
+            out["rho_%d" % k] = rho
+            out["phi_%d" % k] = phi
+            out["zg_%d" % k] = zg
+            out["zd_%d" % k] = zd
+            out["lim_%d" % k] = lim
+            out["coords_%d" % k] = b.coords()
+            k += 1
+            seq_txt.append("sc:%r" % (step[1],))
+        else:
+            b.tpb(step[0], *step[1])
+            seq_txt.append("%s:%r" % (step[0], tuple(step[1])))
+    out["final"] = b.coords()
+    out["nkicks"] = k
+    out["sequence"] = np.array(seq_txt)
+    out["kin"] = np.array([b.kinematics()[q] for q in ("beta", "gamma", "momentum", "kin_energy", "mass",
+                                                      "classical_radius", "time")])
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print("wrote", name, "kicks", k)
+
+
 def main():
     if not O.ref_available():
         if not O.build_reference():
@@ -114,6 +148,14 @@ def main():
     # 5) explicit xy_ratio and nz = 2
     sc_case("ratio2_16x16x2", gaussian(2048, 51, sx=6e-3, sy=3e-3), 16, 16, 2, 2.0,
             [("sc", 1.0), ("drift", (0.5,)), ("sc", 1.0)])
+    # 6) SpaceChargeCalc2p5Drb: longitudinal kick, default 3-point smoothing,
+    #    a 5-point case with an explicit ratio, nz = 2 and nz = 1
+    scrb_case("rb_32x32x16", gaussian(3000, 61), 32, 32, 16, -1.0, 3, 0.05,
+              [("sc", 0.5), ("drift", (0.5,)), ("sc", 0.5)])
+    scrb_case("rb_40x24x8_avg5", gaussian(3000, 71, sx=6e-3, sy=3e-3), 40, 24, 8, 1.5, 5, 0.03,
+              [("sc", 0.4), ("quad1", (0.25, 0.5)), ("sc", 0.4)])
+    scrb_case("rb_16x16x2", gaussian(2048, 81), 16, 16, 2, -1.0, 3, 0.1, [("sc", 1.0), ("sc", 1.0)])
+    scrb_case("rb_16x16x1", gaussian(2048, 91), 16, 16, 1, -1.0, 3, 0.1, [("sc", 1.0)])
 
 
 if __name__ == "__main__":

@@ -56,6 +56,36 @@ def test_sc_cases(case):
         assert rel_err(soa[c], g["final"][c]) <= TOL, (case, c)
 
 
+@pytest.mark.parametrize("case", ["rb_32x32x16", "rb_40x24x8_avg5", "rb_16x16x2", "rb_16x16x1"])
+def test_scrb_cases(case):
+    """SpaceChargeCalc2p5Drb: grids, smoothed line-density derivative and all
+    six coordinates (the longitudinal kick changes dE) after every kick."""
+    g = load_golden(case)
+    nx, ny, nz = int(g["nx"]), int(g["ny"]), int(g["nz"])
+    sc = O.OracleSCrb(nx, ny, nz, float(g["xy_ratio"]))
+    sc.setLongAveragingPointsN(int(g["navg"]))
+    s = kin_sync(g["kin"], float(g["macrosize"]))
+    soa = np.ascontiguousarray(g["init"].copy())
+    k = 0
+    for step in parse_sequence(g["sequence"]):
+        if step[0] == "sc":
+            assert sc.track(soa, s, step[1], float(g["pipe_radius"])) == 0
+            rho, phi, zg, lim = sc.grids()
+            zd = sc.extra()[0]
+            assert rel_err(rho, g["rho_%d" % k]) <= TOL
+            assert rel_err(phi, g["phi_%d" % k]) <= TOL
+            assert rel_err(zg, g["zg_%d" % k]) <= TOL
+            assert rel_err(zd, g["zd_%d" % k]) <= TOL
+            assert np.allclose(lim[:9], g["lim_%d" % k], rtol=1e-15, atol=0)
+            for c in range(6):
+                assert rel_err(soa[c], g["coords_%d" % k][c]) <= TOL, (case, k, c)
+            k += 1
+        else:
+            O.tpb(step[0], soa, s, *step[1])
+    assert k == int(g["nkicks"])
+    assert np.max(np.abs(soa[5] - g["init"][5])) > 0 or nz == 1  # the longitudinal kick acted
+
+
 def test_multithreaded_slices_match_within_summation_order():
     """The rank-sliced oracle differs from one slice only by the order of the
     grid sums (the reference's MPI decomposition)."""
