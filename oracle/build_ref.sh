@@ -21,7 +21,7 @@ for d in src/orbit src/orbit/ParticlesAttributes src/spacecharge src/teapot src/
 done
 SRCS="src/spacecharge/Grid1D.cc src/spacecharge/Grid2D.cc src/spacecharge/PoissonSolver2D.cc
 src/spacecharge/PoissonSolverFFT2D.cc src/spacecharge/SpaceChargeCalc2p5D.cc src/spacecharge/BaseBoundary2D.cc
-src/spacecharge/SpaceChargeCalc2p5Drb.cc
+src/spacecharge/SpaceChargeCalc2p5Drb.cc src/spacecharge/ShapedBoundary2D.cc
 src/teapot/teapotbase.cc src/orbit/Bunch.cc src/orbit/SyncPart.cc src/orbit/OrbitConst.cc
 src/utils/BufferStore.cc src/utils/CppPyWrapper.cc src/utils/AttributesBucket.cc src/utils/StringUtils.cc
 src/utils/bunch/BunchExtremaCalculator.cc src/mpi/orbit_mpi.cc"

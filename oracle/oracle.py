@@ -98,6 +98,21 @@ def lib():
         L.oracle_scrb_track.argtypes = [_vp, _dp, ctypes.c_int, _dp, ctypes.POINTER(OracleSync), ctypes.c_double,
                                         ctypes.c_double, ctypes.c_int]
         L.oracle_scrb_extra.argtypes = [_vp, _dp, _dp]
+        L.oracle_bnd_new.restype = _vp
+        L.oracle_bnd_new.argtypes = [ctypes.c_int, ctypes.c_int]
+        L.oracle_bnd_new_shape.restype = _vp
+        L.oracle_bnd_new_shape.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                           ctypes.c_double]
+        L.oracle_bnd_free.argtypes = [_vp]
+        L.oracle_bnd_set_point.argtypes = [_vp, ctypes.c_int, ctypes.c_double, ctypes.c_double]
+        L.oracle_bnd_initialize.restype = ctypes.c_int
+        L.oracle_bnd_initialize.argtypes = [_vp]
+        L.oracle_bnd_is_inside.restype = ctypes.c_int
+        L.oracle_bnd_is_inside.argtypes = [_vp, ctypes.c_double, ctypes.c_double]
+        L.oracle_bnd_get.argtypes = [_vp, _dp, _dp, _dp, _dp]
+        L.oracle_sc_track_bnd.restype = ctypes.c_int
+        L.oracle_sc_track_bnd.argtypes = [_vp, _dp, ctypes.c_int, _dp, ctypes.POINTER(OracleSync), ctypes.c_double,
+                                          _vp, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -168,6 +183,53 @@ class OracleSCrb(OracleSC):
         abx = np.zeros(3)
         lib().oracle_scrb_extra(self.h, _P(zd), _P(abx))
         return zd, abx[0], abx[1], abx[2]
+
+
+SHAPES = {"Circle": 1, "Ellipse": 2, "Rectangle": 3}
+
+
+class OracleBoundary:
+    """BaseBoundary2D / ShapedBoundary2D restated in C.  Boundary(np, nm) or
+    Boundary(np, nm, shape, xDim[, yDim]) as the reference's Boundary2D."""
+
+    def __init__(self, np_, nm, shape=None, xdim=0.0, ydim=None):
+        L = lib()
+        if shape is None:
+            self.h = L.oracle_bnd_new(int(np_), int(nm))
+        else:
+            self.h = L.oracle_bnd_new_shape(int(np_), int(nm), SHAPES[shape], float(xdim),
+                                            float(xdim if ydim is None else ydim))
+        if not self.h:
+            raise ValueError("bad boundary parameters")
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.oracle_bnd_free(self.h)
+            self.h = None
+
+    def setBoundaryPoint(self, i, x, y):
+        lib().oracle_bnd_set_point(self.h, int(i), float(x), float(y))
+
+    def initialize(self):
+        return lib().oracle_bnd_initialize(self.h)
+
+    def isInside(self, x, y):
+        return lib().oracle_bnd_is_inside(self.h, float(x), float(y))
+
+    def data(self):
+        head = np.zeros(7)
+        lib().oracle_bnd_get(self.h, _P(head), None, None, None)
+        np_, nm = int(head[0]), int(head[1])
+        bx, by = np.zeros(np_), np.zeros(np_)
+        lsq = np.zeros((2 * nm + 1) * np_)
+        lib().oracle_bnd_get(self.h, _P(head), _P(bx), _P(by), _P(lsq))
+        return head, bx, by, lsq.reshape(2 * nm + 1, np_)
+
+
+def sc_track_bnd(sc, soa, sync, length, bnd, msize=None, nthreads=1):
+    m = None if msize is None else _P(np.ascontiguousarray(msize, dtype=np.float64))
+    return lib().oracle_sc_track_bnd(sc.h, _P(soa), soa.shape[1], m, ctypes.byref(sync), float(length), bnd.h,
+                                     int(nthreads))
 
 
 def tpb(name: str, soa: np.ndarray, sync: OracleSync, *args):
@@ -262,6 +324,15 @@ def ref():
         L.ref_scrb_set_long_avg.argtypes = [_vp, ctypes.c_int]
         L.ref_scrb_track.argtypes = [_vp, _vp, ctypes.c_double, ctypes.c_double]
         L.ref_scrb_grids.argtypes = [_vp, _dp, _dp, _dp, _dp, _dp]
+        L.ref_bnd_new.restype = _vp
+        L.ref_bnd_new.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double]
+        L.ref_bnd_free.argtypes = [_vp]
+        L.ref_bnd_set_point.argtypes = [_vp, ctypes.c_int, ctypes.c_double, ctypes.c_double]
+        L.ref_bnd_initialize.argtypes = [_vp]
+        L.ref_bnd_is_inside.restype = ctypes.c_int
+        L.ref_bnd_is_inside.argtypes = [_vp, ctypes.c_double, ctypes.c_double]
+        L.ref_bnd_get.argtypes = [_vp, _dp, _dp, _dp]
+        L.ref_sc_track_bnd.argtypes = [_vp, _vp, ctypes.c_double, _vp]
         _ref = L
     return _ref
 
@@ -366,3 +437,37 @@ class RefSCrb:
         lim = np.zeros(9)
         ref().ref_scrb_grids(self.h, _P(rho), _P(phi), _P(zg), _P(zd), _P(lim))
         return rho.reshape(self.nx, self.ny), phi.reshape(self.nx, self.ny), zg, zd, lim
+
+
+class RefBoundary:
+    """A reference BaseBoundary2D / ShapedBoundary2D driven through the harness."""
+
+    def __init__(self, np_, nm, shape=None, xdim=0.0, ydim=None):
+        self.h = ref().ref_bnd_new(int(np_), int(nm), 0 if shape is None else SHAPES[shape], float(xdim),
+                                   float(xdim if ydim is None else ydim))
+
+    def __del__(self):
+        if getattr(self, "h", None) and _ref is not None:
+            _ref.ref_bnd_free(self.h)
+            self.h = None
+
+    def setBoundaryPoint(self, i, x, y):
+        ref().ref_bnd_set_point(self.h, int(i), float(x), float(y))
+
+    def initialize(self):
+        ref().ref_bnd_initialize(self.h)
+
+    def isInside(self, x, y):
+        return ref().ref_bnd_is_inside(self.h, float(x), float(y))
+
+    def data(self):
+        head = np.zeros(6)
+        bx = np.zeros(4096)
+        by = np.zeros(4096)
+        ref().ref_bnd_get(self.h, _P(head), _P(bx), _P(by))
+        n = int(head[0])
+        return head, bx[:n].copy(), by[:n].copy()
+
+
+def ref_sc_track_bnd(sc: "RefSC", bunch: RefBunch, length: float, bnd: RefBoundary):
+    ref().ref_sc_track_bnd(sc.h, bunch.h, float(length), bnd.h)

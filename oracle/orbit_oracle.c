@@ -629,6 +629,373 @@ void oracle_scrb_extra(const oracle_sc_t* s, double* zderiv, double* abx) {
   }
 }
 
+/* ------------------------------------------------------------------ */
+/* Conducting boundary (src/spacecharge/BaseBoundary2D.cc,            */
+/* ShapedBoundary2D.cc) and SpaceChargeCalc2p5D with a boundary       */
+/* ------------------------------------------------------------------ */
+
+struct oracle_bnd {
+  int np, nm, shape; /* shape: -1 points given by the caller, 1 circle, 2 ellipse, 3 rectangle */
+  double r_circle, a_ell, b_ell, a_rect, b_rect;
+  double xmin, xmax, ymin, ymax, rnorm;
+  int initialized;
+  double* bx;
+  double* by;
+  double* lsq;  /* (2 nm + 1) x np */
+  double* fv;   /* 2 nm + 1 */
+};
+
+static const double ORACLE_PI = 3.14159265358979323846; /* OrbitConst::PI */
+
+/* BaseBoundary2D::lsq_fuctions (BaseBoundary2D.cc:321-348): the free-space
+ * modes 1, (r/R)^j cos(j f), (r/R)^j sin(j f) at one point. */
+static void bnd_funcs(oracle_bnd_t* b, double x, double y) {
+  int nf = 2 * b->nm + 1;
+  double r2 = x * x + y * y;
+  if (r2 == 0.) {
+    b->fv[0] = 1.0;
+    for (int i = 1; i < nf; i++) b->fv[i] = 0.0;
+    return;
+  }
+  double r = sqrt(r2);
+  double sin_f = y / r, cos_f = x / r;
+  double sin_f0 = sin_f, cos_f0 = cos_f;
+  double rfac = r / b->rnorm, rj = 1.0;
+  b->fv[0] = 1.;
+  for (int i = 0; i < b->nm; i++) {
+    rj *= rfac;
+    b->fv[2 * i + 1] = rj * cos_f0;
+    b->fv[2 * i + 2] = rj * sin_f0;
+    double sin_f1 = sin_f * cos_f0 + cos_f * sin_f0;
+    double cos_f1 = cos_f * cos_f0 - sin_f * sin_f0;
+    sin_f0 = sin_f1;
+    cos_f0 = cos_f1;
+  }
+}
+
+/* BaseBoundary2D::_gaussjinv (BaseBoundary2D.cc:238-317): Gauss-Jordan
+ * inversion in place with full pivoting. Returns -1 for a singular matrix
+ * (the reference stops). */
+static int bnd_gaussj(double* a, int n) {
+  int* indxc = (int*)calloc((size_t)n, sizeof(int));
+  int* indxr = (int*)calloc((size_t)n, sizeof(int));
+  int* ipiv = (int*)calloc((size_t)n, sizeof(int));
+  int irow = 0, icol = 0, rc = 0;
+#define A(r, c) a[(size_t)(r) * n + (c)]
+  for (int i = 0; i < n && rc == 0; i++) {
+    double big = 0.0;
+    for (int j = 0; j < n; j++)
+      if (ipiv[j] != 1)
+        for (int k = 0; k < n; k++) {
+          if (ipiv[k] == 0) {
+            if (fabs(A(j, k)) >= big) {
+              big = fabs(A(j, k));
+              irow = j;
+              icol = k;
+            }
+          } else if (ipiv[k] > 1) {
+            rc = -1;
+          }
+        }
+    ++(ipiv[icol]);
+    if (irow != icol)
+      for (int l = 0; l < n; l++) {
+        double t = A(irow, l);
+        A(irow, l) = A(icol, l);
+        A(icol, l) = t;
+      }
+    indxr[i] = irow;
+    indxc[i] = icol;
+    if (A(icol, icol) == 0.0) { rc = -1; break; }
+    double pivinv = 1.0 / A(icol, icol);
+    A(icol, icol) = 1.0;
+    for (int l = 0; l < n; l++) A(icol, l) *= pivinv;
+    for (int ll = 0; ll < n; ll++)
+      if (ll != icol) {
+        double dum = A(ll, icol);
+        A(ll, icol) = 0.0;
+        for (int l = 0; l < n; l++) A(ll, l) -= A(icol, l) * dum;
+      }
+  }
+  if (rc == 0)
+    for (int l = n - 1; l >= 0; l--)
+      if (indxr[l] != indxc[l])
+        for (int k = 0; k < n; k++) {
+          double t = A(k, indxr[l]);
+          A(k, indxr[l]) = A(k, indxc[l]);
+          A(k, indxc[l]) = t;
+        }
+#undef A
+  free(indxc); free(indxr); free(ipiv);
+  return rc;
+}
+
+/* BaseBoundary2D::BaseBoundary2D (BaseBoundary2D.cc:21-97) */
+oracle_bnd_t* oracle_bnd_new(int np, int nm) {
+  if (2 * nm + 1 >= np || nm < 0) return NULL;
+  oracle_bnd_t* b = (oracle_bnd_t*)calloc(1, sizeof(oracle_bnd_t));
+  b->np = np; b->nm = nm; b->shape = -1;
+  b->xmin = DBL_MAX; b->xmax = -DBL_MAX; b->ymin = DBL_MAX; b->ymax = -DBL_MAX;
+  b->rnorm = DBL_MAX;
+  b->bx = (double*)malloc(sizeof(double) * (size_t)np);
+  b->by = (double*)malloc(sizeof(double) * (size_t)np);
+  for (int i = 0; i < np; i++) { b->bx[i] = DBL_MAX; b->by[i] = DBL_MAX; }
+  b->lsq = (double*)calloc((size_t)(2 * nm + 1) * np, sizeof(double));
+  b->fv = (double*)calloc((size_t)(2 * nm + 1), sizeof(double));
+  return b;
+}
+
+void oracle_bnd_free(oracle_bnd_t* b) {
+  if (!b) return;
+  free(b->bx); free(b->by); free(b->lsq); free(b->fv);
+  free(b);
+}
+
+void oracle_bnd_set_point(oracle_bnd_t* b, int i, double x, double y) {
+  if (i >= 0 && i < b->np) { b->bx[i] = x; b->by[i] = y; }
+  b->initialized = 0;
+}
+
+/* BaseBoundary2D::initializeBPs (BaseBoundary2D.cc:190-229): extents, the
+ * normalising radius and the least-squares matrix (F^T F)^-1 F^T. */
+int oracle_bnd_initialize(oracle_bnd_t* b) {
+  int nf = 2 * b->nm + 1, np = b->np;
+  b->xmin = DBL_MAX; b->xmax = -DBL_MAX; b->ymin = DBL_MAX; b->ymax = -DBL_MAX;
+  for (int i = 0; i < np; i++) {
+    double x = b->bx[i], y = b->by[i];
+    if (b->xmin > x) b->xmin = x;
+    if (b->xmax < x) b->xmax = x;
+    if (b->ymin > y) b->ymin = y;
+    if (b->ymax < y) b->ymax = y;
+  }
+  b->rnorm = sqrt((b->xmin - b->xmax) * (b->xmin - b->xmax) + (b->ymin - b->ymax) * (b->ymin - b->ymax));
+  double* t = (double*)calloc((size_t)nf * nf, sizeof(double));
+  for (int p = 0; p < np; p++) {
+    bnd_funcs(b, b->bx[p], b->by[p]);
+    for (int i = 0; i < nf; i++)
+      for (int j = 0; j < nf; j++) t[(size_t)i * nf + j] += b->fv[i] * b->fv[j];
+  }
+  int rc = bnd_gaussj(t, nf);
+  for (int i = 0; i < nf; i++)
+    for (int j = 0; j < np; j++) {
+      double v = 0.0;
+      bnd_funcs(b, b->bx[j], b->by[j]);
+      for (int k = 0; k < nf; k++) v += t[(size_t)i * nf + k] * b->fv[k];
+      b->lsq[(size_t)i * np + j] = v;
+    }
+  free(t);
+  b->initialized = rc == 0;
+  return rc;
+}
+
+/* ShapedBoundary2D::ShapedBoundary2D (ShapedBoundary2D.cc:18-145):
+ * shape 1 circle (diameter xDim), 2 ellipse (axes xDim, yDim), 3 rectangle
+ * (xDim x yDim); the number of points is rounded down to a multiple of 4. */
+oracle_bnd_t* oracle_bnd_new_shape(int np, int nm, int shape, double xdim, double ydim) {
+  np = 4 * (np / 4);
+  oracle_bnd_t* b = oracle_bnd_new(np, nm);
+  if (!b) return NULL;
+  b->shape = shape;
+  if (shape == 1) b->r_circle = xdim / 2;
+  else if (shape == 2) { b->a_ell = xdim / 2; b->b_ell = ydim / 2; }
+  else if (shape == 3) { b->a_rect = xdim; b->b_rect = ydim; }
+  else { oracle_bnd_free(b); return NULL; }
+  if (shape == 1 && xdim != ydim) { oracle_bnd_free(b); return NULL; }
+  if (shape == 1) {
+    for (int i = 0; i < np; i++)
+      oracle_bnd_set_point(b, i, b->r_circle * sin(2 * i * ORACLE_PI / np), b->r_circle * cos(2 * i * ORACLE_PI / np));
+  } else if (shape == 2) {
+    /* equal arc lengths by iteration on the quarter ellipse */
+    double a = b->a_ell, bb = b->b_ell;
+    double ds = 2 * ORACLE_PI * sqrt(a * bb) / np, resid = 1.0;
+    double* th_arr = (double*)calloc((size_t)np + 1, sizeof(double));
+    while (resid > 1.0e-08 || resid < -1.0e-08) {
+      double denom = bb;
+      double dtheta = ds / denom;
+      double th = dtheta / 2.;
+      th_arr[0] = 0.;
+      for (int i = 0; i < np / 4; i++) {
+        denom = bb * bb + (a * a - bb * bb) * sin(th) * sin(th);
+        denom = sqrt(denom);
+        dtheta = ds / denom;
+        th_arr[i + 1] = th_arr[i] + dtheta;
+        th += dtheta;
+      }
+      resid = th_arr[np / 4] - ORACLE_PI / 2.;
+      ds *= ORACLE_PI / (2. * th_arr[np / 4]);
+    }
+    for (int i = 0; i < np / 4; i++) th_arr[np / 2 - i] = ORACLE_PI - th_arr[i];
+    for (int i = 0; i < np / 2; i++) th_arr[np / 2 + i] = ORACLE_PI + th_arr[i];
+    for (int i = 0; i < np; i++) oracle_bnd_set_point(b, i, a * cos(th_arr[i]), bb * sin(th_arr[i]));
+    free(th_arr);
+  } else {
+    double ar = b->a_rect, br = b->b_rect;
+    double dx = ar / (np / 4), dy = br / (np / 4);
+    int c = 0;
+    for (int i = 0; i < np / 4; i++) oracle_bnd_set_point(b, c++, (-ar / 2.0) + i * dx, br / 2.0);
+    for (int i = 0; i < np / 4; i++) oracle_bnd_set_point(b, c++, ar / 2.0, br / 2.0 - i * dy);
+    for (int i = 0; i < np / 4; i++) oracle_bnd_set_point(b, c++, ar / 2.0 - i * dx, -br / 2.0);
+    for (int i = 0; i < np / 4; i++) oracle_bnd_set_point(b, c++, -ar / 2.0, (-br / 2.0) + i * dy);
+  }
+  oracle_bnd_initialize(b);
+  return b;
+}
+
+/* isInside: BaseBoundary2D.cc:144-151, ShapedBoundary2D.cc:284-304 */
+int oracle_bnd_is_inside(const oracle_bnd_t* b, double x, double y) {
+  if (b->shape == 1) return (x * x + y * y < b->r_circle * b->r_circle) ? 1 : -1;
+  if (b->shape == 2) {
+    double xx = x / b->a_ell, yy = y / b->b_ell;
+    return ((xx * xx + yy * yy) < 1.0) ? 1 : -1;
+  }
+  if (b->shape == 3) return (fabs(x / b->a_rect) < 0.5 && fabs(y / b->b_rect) < 0.5) ? 1 : -1;
+  return (x > b->xmin && x < b->xmax && y > b->ymin && y < b->ymax) ? 1 : -1;
+}
+
+/* {np, nm, xmin, xmax, ymin, ymax, rnorm} then bx[np], by[np], lsq[(2nm+1) np] */
+void oracle_bnd_get(const oracle_bnd_t* b, double* head, double* bx, double* by, double* lsq) {
+  if (head) {
+    head[0] = b->np; head[1] = b->nm; head[2] = b->xmin; head[3] = b->xmax;
+    head[4] = b->ymin; head[5] = b->ymax; head[6] = b->rnorm;
+  }
+  if (bx) memcpy(bx, b->bx, sizeof(double) * (size_t)b->np);
+  if (by) memcpy(by, b->by, sizeof(double) * (size_t)b->np);
+  if (lsq) memcpy(lsq, b->lsq, sizeof(double) * (size_t)(2 * b->nm + 1) * b->np);
+}
+
+/* Grid2D::getValue (Grid2D.cc:82-108) */
+static double g2_value(const grid2d_t* g, const double* arr, double x, double y) {
+  int iX, iY;
+  double xf, yf;
+  g2_indx(g, x, &iX, &xf);
+  g2_indy(g, y, &iY, &yf);
+  double xf2 = xf * xf, yf2 = yf * yf;
+  double Wxm = 0.5 * (0.25 - xf + xf2), Wx0 = 0.75 - xf2, Wxp = 0.5 * (0.25 + xf + xf2);
+  double Wym = 0.5 * (0.25 - yf + yf2), Wy0 = 0.75 - yf2, Wyp = 0.5 * (0.25 + yf + yf2);
+  int ny = g->ny;
+  const double* a0 = arr + (size_t)(iX - 1) * ny;
+  const double* a1 = arr + (size_t)iX * ny;
+  const double* a2 = arr + (size_t)(iX + 1) * ny;
+  return Wxm * Wym * a0[iY - 1] + Wxm * Wy0 * a0[iY] + Wxm * Wyp * a0[iY + 1] + Wx0 * Wym * a1[iY - 1] +
+         Wx0 * Wy0 * a1[iY] + Wx0 * Wyp * a1[iY + 1] + Wxp * Wym * a2[iY - 1] + Wxp * Wy0 * a2[iY] +
+         Wxp * Wyp * a2[iY + 1];
+}
+
+/* BaseBoundary2D::addBoundaryPotential (BaseBoundary2D.cc:352-460): fit the
+ * free-space modes to phi on the boundary points and subtract the fit on
+ * every grid node. Returns -1 for an uninitialized boundary or points
+ * outside the grid (the reference stops). */
+static int bnd_add_potential(oracle_bnd_t* b, oracle_sc_t* s) {
+  if (!b->initialized) return -1;
+  const grid2d_t* g = &s->grho;
+  if (g->xmin > b->xmin || g->xmax < b->xmax || g->ymin > b->ymin || g->ymax < b->ymax) return -1;
+  int nf = 2 * b->nm + 1, np = b->np;
+  double* bphi = (double*)malloc(sizeof(double) * (size_t)np);
+  double* coef = (double*)malloc(sizeof(double) * (size_t)nf);
+  for (int j = 0; j < np; j++) bphi[j] = g2_value(g, s->phi, b->bx[j], b->by[j]);
+  for (int i = 0; i < nf; i++) {
+    coef[i] = 0.0;
+    for (int j = 0; j < np; j++) coef[i] += b->lsq[(size_t)i * np + j] * bphi[j];
+  }
+  for (int i = 0; i < s->nx; i++)
+    for (int j = 0; j < s->ny; j++) {
+      double phi = 0.;
+      bnd_funcs(b, g->xmin + i * g->dx, g->ymin + j * g->dy);
+      for (int k = 0; k < nf; k++) phi += coef[k] * b->fv[k];
+      s->phi[(size_t)i * s->ny + j] -= phi;
+    }
+  free(bphi);
+  free(coef);
+  return 0;
+}
+
+typedef struct {
+  slice_t* t;
+  const oracle_bnd_t* b;
+} bslice_t;
+
+/* kick loop with the boundary test (SpaceChargeCalc2p5D.cc:104-119) */
+static void* bnd_kick_worker(void* arg) {
+  bslice_t* w = (bslice_t*)arg;
+  slice_t* t = w->t;
+  const oracle_sc_t* s = t->s;
+  double* x = t->soa;
+  double* xp = t->soa + (size_t)t->n;
+  double* y = t->soa + 2 * (size_t)t->n;
+  double* yp = t->soa + 3 * (size_t)t->n;
+  double* z = t->soa + 4 * (size_t)t->n;
+  for (int i = t->i0; i < t->i1; i++) {
+    if (oracle_bnd_is_inside(w->b, x[i], y[i]) != 1) continue;
+    double ex, ey;
+    g2_grad(&s->grho, s->phi, x[i], y[i], &ex, &ey);
+    double Lfactor = -g1_value(&s->gz, s->zarr, z[i]) * t->factor;
+    xp[i] += ex * Lfactor;
+    yp[i] += ey * Lfactor;
+  }
+  return NULL;
+}
+
+/* SpaceChargeCalc2p5D::trackBunch(bunch, length, boundary) with
+ * bunchAnalysis's boundary branch (SpaceChargeCalc2p5D.cc:77-120, 174-234). */
+int oracle_sc_track_bnd(oracle_sc_t* s, double* soa, int n, const double* msize, const oracle_sync_t* sync,
+                        double length, oracle_bnd_t* b, int nthreads) {
+  if (n < 2) return 0;
+  int nt = nthreads < 1 ? 1 : nthreads;
+  if (nt > n) nt = n;
+  slice_t* sl = (slice_t*)calloc((size_t)nt, sizeof(slice_t));
+  for (int k = 0; k < nt; k++) {
+    sl[k].s = s; sl[k].soa = soa; sl[k].msize = msize; sl[k].m0 = sync->macrosize; sl[k].n = n;
+    sl[k].i0 = (int)((long)n * k / nt);
+    sl[k].i1 = (int)((long)n * (k + 1) / nt);
+  }
+  run_phase(sl, nt, 0);  /* only z is used (getExtremaZ) */
+  double zMin = sl[0].lim[4], zMax = sl[0].lim[5];
+  for (int k = 1; k < nt; k++) {
+    if (sl[k].lim[4] < zMin) zMin = sl[k].lim[4];
+    if (sl[k].lim[5] > zMax) zMax = sl[k].lim[5];
+  }
+  double xMax = b->xmax, xMin = b->xmin, yMax = b->ymax, yMin = b->ymin;
+  s->xy_ratio = (xMax - xMin) / (yMax - yMin);
+  if (zMin >= zMax) { free(sl); return -2; }
+  g2_setx(&s->grho, xMin, xMax);
+  g2_sety(&s->grho, yMin, yMax);
+  g1_set(&s->gz, zMin, zMax);
+  if (fabs((s->sxmax - s->sxmin) / (s->symax - s->symin) - s->xy_ratio) > 0.00000001)
+    solver_set_xy(s, xMin, xMax, yMin, yMax);
+  size_t ng = (size_t)s->nx * s->ny;
+  for (int k = 0; k < nt; k++) {
+    sl[k].rho = (k == 0) ? s->rho : (double*)calloc(ng, sizeof(double));
+    sl[k].zarr = (k == 0) ? s->zarr : (double*)calloc((size_t)s->nz, sizeof(double));
+  }
+  memset(s->rho, 0, sizeof(double) * ng);
+  memset(s->zarr, 0, sizeof(double) * (size_t)s->nz);
+  run_phase(sl, nt, 1);
+  for (int k = 1; k < nt; k++) {
+    for (size_t q = 0; q < ng; q++) s->rho[q] += sl[k].rho[q];
+    for (int q = 0; q < s->nz; q++) s->zarr[q] += sl[k].zarr[q];
+    free(sl[k].rho);
+    free(sl[k].zarr);
+  }
+  double total = 0.;
+  for (int iz = 0; iz < s->nz; iz++) total += s->zarr[iz];
+  s->total_macrosize = total;
+  double z_step = s->gz.dz;
+  find_potential(s);
+  if (bnd_add_potential(b, s)) { free(sl); return -3; }
+  double factor = 2 * length * sync->classical_radius / (pow(sync->beta, 2) * pow(sync->gamma, 3));
+  factor = factor / (z_step * total);
+  bslice_t* w = (bslice_t*)calloc((size_t)nt, sizeof(bslice_t));
+  pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)nt);
+  for (int k = 0; k < nt; k++) { sl[k].factor = factor; w[k].t = &sl[k]; w[k].b = b; }
+  for (int k = 1; k < nt; k++) pthread_create(&th[k], NULL, bnd_kick_worker, &w[k]);
+  bnd_kick_worker(&w[0]);
+  for (int k = 1; k < nt; k++) pthread_join(th[k], NULL);
+  free(th);
+  free(w);
+  free(sl);
+  return 0;
+}
+
 void oracle_sc_grids(const oracle_sc_t* s, double* rho, double* phi, double* zg, double* lim) {
   size_t ng = (size_t)s->nx * s->ny;
   if (rho) memcpy(rho, s->rho, sizeof(double) * ng);

@@ -66,6 +66,24 @@ int oracle_scrb_track(oracle_sc_t* sc, double* soa, int n, const double* msize, 
 /* derivative grid [nz]; abx = {a_bunch, x_center, y_center} */
 void oracle_scrb_extra(const oracle_sc_t* sc, double* zderiv, double* abx);
 
+/* Conducting boundary: BaseBoundary2D(nPoints, nModes) with points set by
+ * the caller then initialized, or ShapedBoundary2D(nPoints, nModes, shape,
+ * xDim, yDim) with shape 1 circle, 2 ellipse, 3 rectangle
+ * (src/spacecharge/BaseBoundary2D.cc, ShapedBoundary2D.cc). */
+typedef struct oracle_bnd oracle_bnd_t;
+oracle_bnd_t* oracle_bnd_new(int np, int nm);
+oracle_bnd_t* oracle_bnd_new_shape(int np, int nm, int shape, double xdim, double ydim);
+void oracle_bnd_free(oracle_bnd_t* b);
+void oracle_bnd_set_point(oracle_bnd_t* b, int i, double x, double y);
+int oracle_bnd_initialize(oracle_bnd_t* b);
+int oracle_bnd_is_inside(const oracle_bnd_t* b, double x, double y);
+void oracle_bnd_get(const oracle_bnd_t* b, double* head, double* bx, double* by, double* lsq);
+/* SpaceChargeCalc2p5D::trackBunch(bunch, length, boundary): grid on the
+ * boundary's extents, boundary potential subtracted, particles outside the
+ * boundary not kicked.  Returns -3 when the boundary does not fit the grid. */
+int oracle_sc_track_bnd(oracle_sc_t* s, double* soa, int n, const double* msize, const oracle_sync_t* sync,
+                        double length, oracle_bnd_t* b, int nthreads);
+
 /* ---- TEAPOT maps (src/teapot/teapotbase.cc) ---- */
 void oracle_rotatexy(double* soa, int n, double angle);
 void oracle_drift(double* soa, int n, oracle_sync_t* s, double length);

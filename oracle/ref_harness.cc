@@ -13,6 +13,8 @@
 #include "SyncPart.hh"
 #include "SpaceChargeCalc2p5D.hh"
 #include "SpaceChargeCalc2p5Drb.hh"
+#include "ShapedBoundary2D.hh"
+#include <string>
 #include "Grid1D.hh"
 #include "Grid2D.hh"
 #include "teapotbase.hh"
@@ -124,6 +126,31 @@ void ref_sc_fields(void* sc, int n, const double* x, const double* y, const doub
     p->calcGradient(x[i], y[i], ex[i], ey[i]);
     lam[i] = zg->getValue(z[i]);
   }
+}
+
+// ---- boundaries (src/spacecharge/BaseBoundary2D.cc, ShapedBoundary2D.cc) ----
+// As Boundary2D_init (src/spacecharge/wrap_boundary2d.cc:37-68): shape 0
+// selects BaseBoundary2D(nPoints, nModes), 1/2/3 ShapedBoundary2D with
+// "Circle"/"Ellipse"/"Rectangle".
+void* ref_bnd_new(int np, int nm, int shape, double xdim, double ydim) {
+  if (shape == 0) return new BaseBoundary2D(np, nm);
+  const char* names[] = {"", "Circle", "Ellipse", "Rectangle"};
+  return new ShapedBoundary2D(np, nm, std::string(names[shape]), xdim, ydim);
+}
+void ref_bnd_free(void* b) { delete (BaseBoundary2D*)b; }
+void ref_bnd_set_point(void* b, int i, double x, double y) { ((BaseBoundary2D*)b)->setBoundaryPoint(i, x, y); }
+void ref_bnd_initialize(void* b) { ((BaseBoundary2D*)b)->initializeBPs(); }
+int ref_bnd_is_inside(void* b, double x, double y) { return ((BaseBoundary2D*)b)->isInside(x, y); }
+// head = {np, nm, xmin, xmax, ymin, ymax}; bx, by [np]
+void ref_bnd_get(void* b, double* head, double* bx, double* by) {
+  BaseBoundary2D* q = (BaseBoundary2D*)b;
+  int np = q->getNumberOfPoints();
+  head[0] = np; head[1] = q->getNumberOfModes();
+  head[2] = q->getMinX(); head[3] = q->getMaxX(); head[4] = q->getMinY(); head[5] = q->getMaxY();
+  for (int i = 0; i < np; ++i) { bx[i] = q->getBoundaryPointX(i); by[i] = q->getBoundaryPointY(i); }
+}
+void ref_sc_track_bnd(void* sc, void* b, double length, void* bnd) {
+  ((SpaceChargeCalc2p5D*)sc)->trackBunch((Bunch*)b, length, (BaseBoundary2D*)bnd);
 }
 
 // ---- SpaceChargeCalc2p5Drb (src/spacecharge/SpaceChargeCalc2p5Drb.cc) ----

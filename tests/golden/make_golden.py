@@ -115,6 +115,52 @@ def scrb_case(name, soa, nx, ny, nz, xy_ratio, navg, pipe_radius, seq, ek=1.0, m
     print("wrote", name, "kicks", k)
 
 
+def bnd_case(name, soa, nx, ny, nz, bnd_args, seq, points=None, ek=1.0, msize=1e9):
+    """SpaceChargeCalc2p5D with a conducting boundary: bnd_args = (nPoints,
+    nModes[, shape, xDim, yDim]); points: explicit boundary points for the
+    base class.  Records the boundary points, the grids and the coordinates
+    after each kick."""
+    b = O.RefBunch(soa, ek, msize)
+    sc = O.RefSC(nx, ny, nz, -1.0)
+    bnd = O.RefBoundary(*bnd_args)
+    if points is not None:
+        for i, (x, y) in enumerate(points):
+            bnd.setBoundaryPoint(i, x, y)
+        bnd.initialize()
+    head, bx, by = bnd.data()
+    out = {"init": soa, "nx": nx, "ny": ny, "nz": nz, "ek": ek, "macrosize": msize,
+           "bnd_np": int(bnd_args[0]), "bnd_nm": int(bnd_args[1]),
+           "bnd_shape": "" if len(bnd_args) < 3 else bnd_args[2],
+           "bnd_xdim": 0.0 if len(bnd_args) < 4 else float(bnd_args[3]),
+           "bnd_ydim": (0.0 if len(bnd_args) < 4 else float(bnd_args[3])) if len(bnd_args) < 5 else float(bnd_args[4]),
+           "bnd_head": head, "bnd_x": bx, "bnd_y": by}
+    probe = np.linspace(-0.03, 0.03, 41)
+    out["inside"] = np.array([[bnd.isInside(x, y) for y in probe] for x in probe])
+    k = 0
+    seq_txt = []
+    for step in seq:
+        if step[0] == "sc":
+            O.ref_sc_track_bnd(sc, b, step[1], bnd)
+            rho, phi, zg, lim = sc.grids()
+            out["rho_%d" % k] = rho
+            out["phi_%d" % k] = phi
+            out["zg_%d" % k] = zg
+            out["lim_%d" % k] = lim
+            out["coords_%d" % k] = b.coords()
+            k += 1
+            seq_txt.append("sc:%r" % (step[1],))
+        else:
+            b.tpb(step[0], *step[1])
+            seq_txt.append("%s:%r" % (step[0], tuple(step[1])))
+    out["final"] = b.coords()
+    out["nkicks"] = k
+    out["sequence"] = np.array(seq_txt)
+    out["kin"] = np.array([b.kinematics()[q] for q in ("beta", "gamma", "momentum", "kin_energy", "mass",
+                                                      "classical_radius", "time")])
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print("wrote", name, "kicks", k)
+
+
 def main():
     if not O.ref_available():
         if not O.build_reference():
@@ -156,6 +202,17 @@ def main():
               [("sc", 0.4), ("quad1", (0.25, 0.5)), ("sc", 0.4)])
     scrb_case("rb_16x16x2", gaussian(2048, 81), 16, 16, 2, -1.0, 3, 0.1, [("sc", 1.0), ("sc", 1.0)])
     scrb_case("rb_16x16x1", gaussian(2048, 91), 16, 16, 1, -1.0, 3, 0.1, [("sc", 1.0)])
+    # 7) conducting boundaries: circle, ellipse, rectangle and explicit points
+    #    (some particles outside the boundary are not kicked)
+    bnd_case("bnd_circle_64x64x16", gaussian(3000, 101, sx=6e-3, sy=6e-3), 64, 64, 16, (128, 10, "Circle", 0.04),
+             [("sc", 0.5), ("drift", (0.5,)), ("sc", 0.5)])
+    bnd_case("bnd_ellipse_48x40x8", gaussian(3000, 111, sx=8e-3, sy=4e-3), 48, 40, 8,
+             (120, 8, "Ellipse", 0.05, 0.03), [("sc", 0.5), ("sc", 0.5)])
+    bnd_case("bnd_rect_32x32x4", gaussian(2048, 121, sx=6e-3, sy=5e-3), 32, 32, 4,
+             (128, 12, "Rectangle", 0.05, 0.04), [("sc", 1.0)])
+    t = 2 * np.pi * np.arange(64) / 64
+    bnd_case("bnd_points_40x40x8", gaussian(2048, 131), 40, 40, 8, (64, 6), [("sc", 0.5)],
+             points=list(zip(0.03 * np.cos(t) + 0.002, 0.02 * np.sin(t))))
 
 
 if __name__ == "__main__":

@@ -86,6 +86,50 @@ def test_scrb_cases(case):
     assert np.max(np.abs(soa[5] - g["init"][5])) > 0 or nz == 1  # the longitudinal kick acted
 
 
+def oracle_boundary_of(g):
+    shape = str(g["bnd_shape"])
+    if shape:
+        return O.OracleBoundary(int(g["bnd_np"]), int(g["bnd_nm"]), shape, float(g["bnd_xdim"]),
+                                float(g["bnd_ydim"]))
+    b = O.OracleBoundary(int(g["bnd_np"]), int(g["bnd_nm"]))
+    for i, (x, y) in enumerate(zip(g["bnd_x"], g["bnd_y"])):
+        b.setBoundaryPoint(i, x, y)
+    assert b.initialize() == 0
+    return b
+
+
+@pytest.mark.parametrize("case", ["bnd_circle_64x64x16", "bnd_ellipse_48x40x8", "bnd_rect_32x32x4",
+                                  "bnd_points_40x40x8"])
+def test_boundary_cases(case):
+    """Conducting boundaries: points, extents and the inside test of the
+    shapes, and the kicks with the boundary potential subtracted."""
+    g = load_golden(case)
+    nx, ny, nz = int(g["nx"]), int(g["ny"]), int(g["nz"])
+    bnd = oracle_boundary_of(g)
+    head, bx, by, lsq = bnd.data()
+    assert np.array_equal(bx, g["bnd_x"]) and np.array_equal(by, g["bnd_y"])
+    assert np.array_equal(head[:6], g["bnd_head"][:6])
+    probe = np.linspace(-0.03, 0.03, 41)
+    assert np.array_equal(np.array([[bnd.isInside(x, y) for y in probe] for x in probe]), g["inside"])
+    sc = O.OracleSC(nx, ny, nz)
+    s = kin_sync(g["kin"], float(g["macrosize"]))
+    soa = np.ascontiguousarray(g["init"].copy())
+    k = 0
+    for step in parse_sequence(g["sequence"]):
+        if step[0] == "sc":
+            assert O.sc_track_bnd(sc, soa, s, step[1], bnd) == 0
+            rho, phi, zg, lim = sc.grids()
+            assert rel_err(rho, g["rho_%d" % k]) <= TOL
+            assert rel_err(phi, g["phi_%d" % k]) <= TOL
+            assert rel_err(zg, g["zg_%d" % k]) <= TOL
+            for c in range(6):
+                assert rel_err(soa[c], g["coords_%d" % k][c]) <= TOL, (case, k, c)
+            k += 1
+        else:
+            O.tpb(step[0], soa, s, *step[1])
+    assert k == int(g["nkicks"])
+
+
 def test_multithreaded_slices_match_within_summation_order():
     """The rank-sliced oracle differs from one slice only by the order of the
     grid sums (the reference's MPI decomposition)."""
