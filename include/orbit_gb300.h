@@ -111,6 +111,43 @@ int orbit_sc2p5d_get_grid(orbit_sc2p5d_t* c, int which, double* host_out);
 /* lim = {xmin,xmax,ymin,ymax,zmin,zmax,dx,dy,dz,xy_ratio,total_macrosize} */
 int orbit_sc2p5d_get_limits(orbit_sc2p5d_t* c, double* lim);
 int orbit_sc2p5d_get_sizes(const orbit_sc2p5d_t* c, int* nx, int* ny, int* nz, int* form);
+/* ---- conducting boundaries (Boundary2D: src/spacecharge/BaseBoundary2D.cc,
+ * ShapedBoundary2D.cc, wrap_boundary2d.cc) ---- */
+typedef struct orbit_boundary orbit_boundary_t;
+#define ORBIT_SHAPE_POINTS 0    /* points given with orbit_boundary_set_point */
+#define ORBIT_SHAPE_CIRCLE 1
+#define ORBIT_SHAPE_ELLIPSE 2
+#define ORBIT_SHAPE_RECTANGLE 3
+/* Boundary2D(nPoints, nModes): points set one by one, then initialized
+ * (BaseBoundary2D.cc:21-97, 190-229).  2*nModes+1 < nPoints; at most 63
+ * modes and 4096 points. */
+int orbit_boundary_create(orbit_boundary_t** out, int n_points, int n_modes);
+/* Boundary2D(nPoints, nModes, shape, xDim, yDim): circle of diameter xDim
+ * (xDim == yDim), ellipse with axes xDim, yDim, rectangle xDim x yDim; the
+ * number of points is rounded down to a multiple of 4; initialized
+ * (ShapedBoundary2D.cc:18-145). */
+int orbit_boundary_create_shape(orbit_boundary_t** out, int n_points, int n_modes, int shape, double xdim,
+                                double ydim);
+int orbit_boundary_destroy(orbit_boundary_t* b);
+/* setBoundaryPoint / initialize / getBoundaryPoint (BaseBoundary2D.cc:154-229) */
+int orbit_boundary_set_point(orbit_boundary_t* b, int i, double x, double y);
+int orbit_boundary_initialize(orbit_boundary_t* b);
+int orbit_boundary_get_point(const orbit_boundary_t* b, int i, double* x, double* y);
+/* n_points, n_modes, shape (ORBIT_SHAPE_*), lim = {xmin, xmax, ymin, ymax}, initialized */
+int orbit_boundary_info(const orbit_boundary_t* b, int* n_points, int* n_modes, int* shape, double* lim,
+                        int* initialized);
+/* isInside: 1 inside, -1 outside (ShapedBoundary2D.cc:284-304) */
+int orbit_boundary_is_inside(const orbit_boundary_t* b, double x, double y);
+/* The least-squares matrix ((2 n_modes + 1) x n_points, row-major) and the
+ * normalising radius, for addBoundaryPotential on host grids. */
+int orbit_boundary_lsq(const orbit_boundary_t* b, double* out);
+int orbit_boundary_rnorm(const orbit_boundary_t* b, double* rnorm);
+/* SpaceChargeCalc2p5D::trackBunch(bunch, length, boundary)
+ * (SpaceChargeCalc2p5D.cc:77-234): grid on the boundary's extents, the
+ * boundary potential subtracted from phi, particles outside the boundary
+ * not kicked.  Enqueued on the bunch's stream. */
+int orbit_sc2p5d_track_boundary(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, const orbit_boundary_t* bnd);
+
 /* SpaceChargeCalc2p5Drb(xSize, ySize, zSize[, xy_ratio]), plain FP64 form
  * (src/spacecharge/wrap_spacechargecalc2p5d_rb.cc:37-50): the 2.5D kick
  * plus a longitudinal kick of dE from the smoothed derivative of the line
@@ -208,7 +245,8 @@ int orbit_tpb_bendfringeOUT(orbit_bunch_t* b, double rho);
 #define ORBIT_OP_WEDGEROT 18  /* d0 = e, i0 = frinout */
 #define ORBIT_OP_WEDGEDRIFT 19 /* d0 = e, i0 = inout */
 #define ORBIT_OP_WEDGEBEND 20 /* d0 = e, i0 = inout, d1 = rho, i1 = nsteps */
-#define ORBIT_OP_SC 32        /* i0 = calculator index, d0 = sc length, d1 = pipe radius (2.5Drb calculators) */
+#define ORBIT_OP_SC 32        /* i0 = calculator index, d0 = sc length, d1 = pipe radius (2.5Drb calculators),
+                                 i1 = 1 + boundary index (0: none; orbit_program_set_boundaries) */
 
 typedef struct {
   int32_t code, i0, i1, i2;
@@ -223,6 +261,9 @@ typedef struct orbit_program orbit_program_t;
 int orbit_program_create(orbit_program_t** out, const orbit_op_t* ops, int nops,
                          orbit_sc2p5d_t* const* calcs, int ncalcs);
 int orbit_program_destroy(orbit_program_t* p);
+/* Boundaries for SC ops with i1 = 1 + index (the boundary passed to the
+ * node's trackBunch); the program keeps the pointers, which must outlive it. */
+int orbit_program_set_boundaries(orbit_program_t* p, orbit_boundary_t* const* bnds, int n);
 /* Runs the program `turns` times on the bunch (captured once per bunch as a
  * CUDA graph and replayed) and advances the bunch's sync time. Waits for
  * completion and reports device errors. */

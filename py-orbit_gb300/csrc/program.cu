@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(512) k_pass(double* __restrict__ cx, double* _
       p.knl = knl_buf[i];
       p.knl_ok = true;
     }
-    if (KF == 1 && !k.skip) {
+    if (KF == 1 && !k.skip && bnd_inside(kick.bnd, p.x, p.y)) {
       if (!kick_fixed(kf, P, Lm, p.x, p.y, p.z, p.xp, p.yp)) kick_plain(k, kick.phi, kick.lam, p.x, p.y, p.z, p.xp, p.yp);
       if (kick.lamd) {  // 2.5Drb: longitudinal kick; dE changed
         RbConst r;
@@ -84,7 +84,7 @@ __global__ void __launch_bounds__(512) k_pass(double* __restrict__ cx, double* _
         p.knl_ok = false;
       }
     }
-    if (KF == 2 && !k.skip) kick_fp32(k, Pf, Lf, p.x, p.y, p.z, p.xp, p.yp);
+    if (KF == 2 && !k.skip && bnd_inside(kick.bnd, p.x, p.y)) kick_fp32(k, Pf, Lf, p.x, p.y, p.z, p.xp, p.yp);
     apply_ops(p, ops, a, b, m);
     if (EXT) acc.add(p.x, p.y, p.z);
     if (km & KNL_STORE) {
@@ -136,6 +136,7 @@ using namespace orbit;
 struct orbit_program {
   std::vector<orbit_op_t> ops;
   std::vector<orbit_sc2p5d_t*> calcs;
+  std::vector<orbit_boundary_t*> bnds;   // SC ops with i1 = 1 + index
   // compiled for one bunch configuration
   orbit_bunch_t* key_bunch = nullptr;
   int key_n = -1;
@@ -180,7 +181,7 @@ static bool sync_equal(const orbit_sync_t& a, const orbit_sync_t& b) {
          a.classical_radius == b.classical_radius && a.macrosize == b.macrosize && a.mass == b.mass;
 }
 
-static KickArgs kick_args(orbit_sc2p5d_t* c, const orbit_sync_t& s, double length) {
+static KickArgs kick_args(orbit_sc2p5d_t* c, const orbit_sync_t& s, double length, const orbit_boundary* bnd) {
   KickArgs ka;
   ka.st = c->d_st;
   ka.phi = c->d_phi;
@@ -193,6 +194,7 @@ static KickArgs kick_args(orbit_sc2p5d_t* c, const orbit_sync_t& s, double lengt
   ka.nx = c->nx; ka.ny = c->ny; ka.nz = c->nz; ka.form = c->form;
   ka.lamd = c->rb ? c->d_lamd : nullptr;
   ka.rb_lsf = c->rb ? sc_rb_long_factor(s, length) : 0.0;
+  ka.bnd = bnd_shape_of(bnd);
   return ka;
 }
 
@@ -201,15 +203,15 @@ static KickArgs kick_args(orbit_sc2p5d_t* c, const orbit_sync_t& s, double lengt
 // ec_here: the kick of ec is enqueued next in this same stream (and graph),
 // so a graph branch for its Green rebuild can be set up by this pass.
 static int enqueue_pass(orbit_bunch_t* bu, cudaStream_t s, const DevOp* ops, Seg seg, const MapCtx& m,
-                        orbit_sc2p5d_t* kc, double klen, orbit_sc2p5d_t* ec, bool ec_here, double* knl_buf, int km,
-                        int* nl) {
+                        orbit_sc2p5d_t* kc, double klen, const orbit_boundary* kb, orbit_sc2p5d_t* ec,
+                        const orbit_boundary* eb, bool ec_here, double* knl_buf, int km, int* nl) {
   KickArgs ka;
   std::memset(&ka, 0, sizeof(ka));
   int kf = 0;
   size_t smem = 0;
   bool ksm = false;
   if (kc) {
-    ka = kick_args(kc, bu->sync, klen);
+    ka = kick_args(kc, bu->sync, klen, kb);
     kf = kc->form == ORBIT_FORM_PLAIN ? 1 : 2;
     smem = (kf == 1 ? 8 : 4) * ((size_t)kc->nx * kc->ny + kc->nz);
     ksm = kc->smem_kick && smem <= (size_t)kPassSmem;  // else the kick reads phi_fix, converted by the solve
@@ -220,7 +222,7 @@ static int enqueue_pass(orbit_bunch_t* bu, cudaStream_t s, const DevOp* ops, Seg
   SetupArgs sa;
   std::memset(&sa, 0, sizeof(sa));
   if (ec) {
-    sa = sc_setup_args(ec, sc_dep_scales(ec, bu));
+    sa = sc_setup_args(ec, sc_dep_scales(ec, bu), eb);
     if (ec_here) sa.cond = sc_green_cond(ec, s, true);
   }
   int rc;
@@ -326,34 +328,38 @@ static int enqueue_turn(orbit_program_t* p, orbit_bunch_t* bu, cudaStream_t s, c
     first = false;
     return km;
   };
-  double* kb = p->d_knl;
+  double* knl = p->d_knl;
+  auto bnd_of = [&](int i) -> const orbit_boundary* {
+    int k = p->ops[plan.sc_idx[i]].i1;
+    return (k >= 1 && k <= (int)p->bnds.size()) ? p->bnds[k - 1] : nullptr;
+  };
   if (nsc == 0 || !sc_active) {
     // no kicks: one pass over all maps of the turn
     for (size_t i = 0; i < plan.segs.size(); ++i) {
-      rc = enqueue_pass(bu, s, ops, plan.segs[i], m, nullptr, 0.0, nullptr, false, kb, km_of(plan.segs[i], false),
-                        nl);
+      rc = enqueue_pass(bu, s, ops, plan.segs[i], m, nullptr, 0.0, nullptr, nullptr, nullptr, false, knl,
+                        km_of(plan.segs[i], false), nl);
       if (rc) return rc;
     }
     return ORBIT_OK;
   }
   if (prologue) {
-    rc = enqueue_pass(bu, s, ops, plan.segs[0], m, nullptr, 0.0, calc_of(0), true, kb, km_of(plan.segs[0], true),
-                      nl);
+    rc = enqueue_pass(bu, s, ops, plan.segs[0], m, nullptr, 0.0, nullptr, calc_of(0), bnd_of(0), true, knl,
+                      km_of(plan.segs[0], true), nl);
     if (rc) return rc;
   }
   for (int i = 0; i < nsc; ++i) {
-    rc = sc_enqueue_kick(calc_of(i), bu, len_of(i), s, false, false, nl, pipe_of(i));
+    rc = sc_enqueue_kick(calc_of(i), bu, len_of(i), s, false, false, nl, pipe_of(i), bnd_of(i));
     if (rc) return rc;
     bool last = (i == nsc - 1);
     if (!last) {
-      rc = enqueue_pass(bu, s, ops, plan.segs[i + 1], m, calc_of(i), len_of(i), calc_of(i + 1), true, kb,
-                        km_of(plan.segs[i + 1], true, calc_of(i)), nl);
+      rc = enqueue_pass(bu, s, ops, plan.segs[i + 1], m, calc_of(i), len_of(i), bnd_of(i), calc_of(i + 1),
+                        bnd_of(i + 1), true, knl, km_of(plan.segs[i + 1], true, calc_of(i)), nl);
     } else if (wrap) {
-      rc = enqueue_pass(bu, s, ops, plan.wrap, m, calc_of(i), len_of(i), calc_of(0), false, kb,
-                        km_of(plan.wrap, true, calc_of(i)), nl);
+      rc = enqueue_pass(bu, s, ops, plan.wrap, m, calc_of(i), len_of(i), bnd_of(i), calc_of(0), bnd_of(0), false,
+                        knl, km_of(plan.wrap, true, calc_of(i)), nl);
     } else {
-      rc = enqueue_pass(bu, s, ops, plan.segs[nsc], m, calc_of(i), len_of(i), nullptr, false, kb,
-                        km_of(plan.segs[nsc], true, calc_of(i)), nl);
+      rc = enqueue_pass(bu, s, ops, plan.segs[nsc], m, calc_of(i), len_of(i), bnd_of(i), nullptr, nullptr, false,
+                        knl, km_of(plan.segs[nsc], true, calc_of(i)), nl);
     }
     if (rc) return rc;
   }
@@ -428,6 +434,22 @@ int orbit_program_create(orbit_program_t** out, const orbit_op_t* ops, int nops,
     return cuda_error(e, "orbit_program_create");
   }
   *out = p;
+  return ORBIT_OK;
+}
+
+int orbit_program_set_boundaries(orbit_program_t* p, orbit_boundary_t* const* bnds, int n) {
+  if (!p || n < 0 || (n > 0 && !bnds)) return set_error(ORBIT_ERR_ARG, "orbit_program_set_boundaries: bad argument");
+  for (int i = 0; i < n; ++i) {
+    int init = 0;
+    if (!bnds[i] || orbit_boundary_info(bnds[i], nullptr, nullptr, nullptr, nullptr, &init) || !init)
+      return set_error(ORBIT_ERR_ARG, "Boundary2D: the boundary was not initialized, call initialize()");
+    int rc = bnd_ensure_device(bnds[i]);
+    if (rc) return rc;
+  }
+  if (p->used) ORBIT_CUDA(cudaEventSynchronize(p->done));
+  p->bnds.assign(bnds, bnds + n);
+  free_graphs(p);
+  p->key_bunch = nullptr;
   return ORBIT_OK;
 }
 

@@ -553,7 +553,7 @@ __global__ void k_kick_plain(const double* __restrict__ x, double* __restrict__ 
                              const double* __restrict__ phi, const double* __restrict__ lam,
                              const long long* __restrict__ phi_fix, const long long* __restrict__ lam_fix,
                              double host_factor, int nx, int ny, int nz, const double* __restrict__ lamd,
-                             double rb_lsf, double* __restrict__ dE) {
+                             double rb_lsf, double* __restrict__ dE, BndShape bnd) {
   KickConst k;
   load_kick_const(k, st, host_factor, nx, ny, nz);
   if (k.skip) return;
@@ -573,6 +573,7 @@ __global__ void k_kick_plain(const double* __restrict__ x, double* __restrict__ 
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     double a = xp[i], b = yp[i];
     double xi = x[i], yi = y[i], zi = z[i];
+    if (!bnd_inside(bnd, xi, yi)) continue;  // SpaceChargeCalc2p5D.cc:110
     if (!kick_fixed(kf, P, Lm, xi, yi, zi, a, b)) kick_plain(k, phi, lam, xi, yi, zi, a, b);
     xp[i] = a;
     yp[i] = b;
@@ -590,7 +591,7 @@ template <bool SMEM>
 __global__ void k_kick_fp32(const double* __restrict__ x, double* __restrict__ xp, const double* __restrict__ y,
                             double* __restrict__ yp, const double* __restrict__ z, int n, const ScState* st,
                             const float* __restrict__ phi, const float* __restrict__ lam, double host_factor,
-                            int nx, int ny, int nz) {
+                            int nx, int ny, int nz, BndShape bnd) {
   KickConst k;
   load_kick_const(k, st, host_factor, nx, ny, nz);
   if (k.skip) return;
@@ -605,6 +606,7 @@ __global__ void k_kick_fp32(const double* __restrict__ x, double* __restrict__ x
     Lm = s_phif + nx * ny;
   }
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (!bnd_inside(bnd, x[i], y[i])) continue;
     double a = xp[i], b = yp[i];
     kick_fp32(k, P, Lm, x[i], y[i], z[i], a, b);
     xp[i] = a;
@@ -850,7 +852,7 @@ DepScales sc_dep_scales(const orbit_sc2p5d_t* c, const orbit_bunch_t* b) {
   return d;
 }
 
-SetupArgs sc_setup_args(const orbit_sc2p5d_t* c, const DepScales& d) {
+SetupArgs sc_setup_args(const orbit_sc2p5d_t* c, const DepScales& d, const orbit_boundary* bnd) {
   SetupArgs sa;
   sa.inv_qscale = c->form == ORBIT_FORM_PLAIN ? d.inv_q : 1.0;
   sa.nx = c->nx;
@@ -858,6 +860,15 @@ SetupArgs sc_setup_args(const orbit_sc2p5d_t* c, const DepScales& d) {
   sa.nz = c->nz;
   sa.rb = c->rb ? 1 : 0;
   sa.cond = 0;
+  sa.bnd = 0;
+  sa.bxmin = sa.bxmax = sa.bymin = sa.bymax = 0.0;
+  if (bnd) {
+    int np, nm, shape, init;
+    double lim[4];
+    orbit_boundary_info(bnd, &np, &nm, &shape, lim, &init);
+    sa.bnd = 1;
+    sa.bxmin = lim[0]; sa.bxmax = lim[1]; sa.bymin = lim[2]; sa.bymax = lim[3];
+  }
   return sa;
 }
 
@@ -915,7 +926,7 @@ static int add_green_branch(orbit_sc2p5d_t* c, cudaStream_t s, cudaGraphConditio
 }
 
 int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStream_t s, bool do_extrema,
-                    bool do_kick, int* launches, double pipe_radius) {
+                    bool do_kick, int* launches, double pipe_radius, const orbit_boundary* bnd) {
   int nl = 0;
   const int n = b->n;
   const double* msz = b->has_msize ? b->d_msize : nullptr;
@@ -927,7 +938,7 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
   // run first and return unless the spectrum is dirty.
   cudaGraphConditionalHandle cond = 0;
   if (do_extrema) {
-    SetupArgs sa = sc_setup_args(c, ds);
+    SetupArgs sa = sc_setup_args(c, ds, bnd);
     sa.cond = cond = sc_green_cond(c, s, false);
     ORBIT_PB("extrema", s);
     k_extrema<<<ext_blocks(n), 256, 0, s>>>(b->coord(0), b->coord(2), b->coord(4), n, c->d_st, b->d_status, sa);
@@ -996,6 +1007,10 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
     ORBIT_CUDA(cudaStreamUpdateCaptureDependencies(s, &branch_node, nullptr, 1, cudaStreamAddCaptureDependencies));
   rc = plain ? enqueue_conv<double>(c, s, &nl) : enqueue_conv<float>(c, s, &nl);
   if (rc) return rc;
+  if (bnd) {
+    rc = bnd_enqueue_potential(bnd, c, s, &nl);
+    if (rc) return rc;
+  }
   if (plain && !c->smem_kick) {
     // kicks that read the potential from global memory take it converted
     // once; the shared-memory kicks convert their own copy
@@ -1011,6 +1026,7 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
     double hf = sc_host_factor(b->sync, length);
     const double* lamd = c->rb ? c->d_lamd : nullptr;
     double lsf = c->rb ? sc_rb_long_factor(b->sync, length) : 0.0;
+    BndShape bshape = bnd_shape_of(bnd);
     size_t smk = (plain ? sizeof(double) : sizeof(float)) * ((size_t)c->nx * c->ny + c->nz);
     const int* mt_kick = particle_kernel_threads() + 4;
     particle_geometry(c->smem_kick ? smk : 0, n, mt_kick[(plain ? 0 : 2) + (c->smem_kick ? 0 : 1)], &blocks,
@@ -1021,21 +1037,21 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
         k_kick_plain<true><<<blocks, threads, smk, s>>>(b->coord(0), b->coord(1), b->coord(2), b->coord(3),
                                                         b->coord(4), n, c->d_st, c->d_phi, c->d_lam, c->d_phi_fix,
                                                         c->d_lam_fix, hf, c->nx, c->ny, c->nz, lamd, lsf,
-                                                        b->coord(5));
+                                                        b->coord(5), bshape);
       else
         k_kick_plain<false><<<blocks, threads, 0, s>>>(b->coord(0), b->coord(1), b->coord(2), b->coord(3),
                                                        b->coord(4), n, c->d_st, c->d_phi, c->d_lam, c->d_phi_fix,
                                                        c->d_lam_fix, hf, c->nx, c->ny, c->nz, lamd, lsf,
-                                                       b->coord(5));
+                                                       b->coord(5), bshape);
     } else {
       if (c->smem_kick)
         k_kick_fp32<true><<<blocks, threads, smk, s>>>(b->coord(0), b->coord(1), b->coord(2), b->coord(3),
                                                        b->coord(4), n, c->d_st, c->d_phi_f, c->d_lam_f, hf, c->nx,
-                                                       c->ny, c->nz);
+                                                       c->ny, c->nz, bshape);
       else
         k_kick_fp32<false><<<blocks, threads, 0, s>>>(b->coord(0), b->coord(1), b->coord(2), b->coord(3),
                                                       b->coord(4), n, c->d_st, c->d_phi_f, c->d_lam_f, hf, c->nx,
-                                                      c->ny, c->nz);
+                                                      c->ny, c->nz, bshape);
     }
     ORBIT_PE(s);
     ++nl;
@@ -1181,6 +1197,25 @@ int orbit_sc2p5d_destroy(orbit_sc2p5d_t* c) {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete c;
+  return ORBIT_OK;
+}
+
+int orbit_sc2p5d_track_boundary(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, const orbit_boundary_t* bnd) {
+  if (!c || !b) return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_track_boundary: null handle");
+  if (c->rb) return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_track_boundary: a 2.5Drb calculator has no boundary");
+  if (!bnd) return orbit_sc2p5d_track(c, b, length);
+  int np, nm, shape, init;
+  double lim[4];
+  orbit_boundary_info(bnd, &np, &nm, &shape, lim, &init);
+  if (!init)  // BaseBoundary2D.cc:354-363
+    return set_error(ORBIT_ERR_ARG, "Boundary2D: the boundary was not initialized, call initialize()");
+  if (b->n < 2) return ORBIT_OK;
+  int rc = bnd_ensure_device(const_cast<orbit_boundary_t*>(bnd));
+  if (rc) return rc;
+  ORBIT_CUDA(sc_order_before(c, b->stream));
+  rc = sc_enqueue_kick(c, b, length, b->stream, true, true, nullptr, 0.0, bnd);
+  if (rc) return rc;
+  ORBIT_CUDA(sc_mark_used(c, b->stream));
   return ORBIT_OK;
 }
 

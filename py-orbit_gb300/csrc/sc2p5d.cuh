@@ -33,11 +33,36 @@ struct ScState {
   unsigned long long n_kicks, n_green;                    // kicks solved, Green spectra rebuilt
 };
 
+// Inside test of a conducting boundary (BaseBoundary2D.cc:144-151,
+// ShapedBoundary2D.cc:284-304): type -1 none (every particle is inside),
+// 0 the extents of arbitrary points (p = xmin, xmax, ymin, ymax), 1 circle
+// (p0 = radius), 2 ellipse (p0, p1 = semi-axes), 3 rectangle (p0, p1 =
+// full sides).
+struct BndShape {
+  int type;
+  double p0, p1, p2, p3;
+};
+
+__host__ __device__ __forceinline__ bool bnd_inside(const BndShape& b, double x, double y) {
+  switch (b.type) {
+    case 0: return x > b.p0 && x < b.p1 && y > b.p2 && y < b.p3;
+    case 1: return x * x + y * y < b.p0 * b.p0;
+    case 2: {
+      double xx = x / b.p0, yy = y / b.p1;
+      return (xx * xx + yy * yy) < 1.0;
+    }
+    case 3: return fabs(x / b.p0) < 0.5 && fabs(y / b.p1) < 0.5;
+    default: return true;
+  }
+}
+
 // Arguments of the grid set-up run at the end of the extrema scan.
 struct SetupArgs {
   double inv_qscale;  // macrosize per unit of the fixed-point deposit (1 for the fp32 form)
   int nx, ny, nz;
   int rb;             // SpaceChargeCalc2p5Drb set-up: fixed ratio, solver grid never reshaped
+  int bnd;            // a conducting boundary fixes the transverse grid to its extents
+  double bxmin, bxmax, bymin, bymax;
   cudaGraphConditionalHandle cond;  // inside a graph: the Green-rebuild branch of this kick (0: none)
 };
 
@@ -56,6 +81,8 @@ struct FftPlan {
 };
 
 }  // namespace orbit
+
+struct orbit_boundary;
 
 struct orbit_sc2p5d {
   int nx = 0, ny = 0, nz = 0, form = 0;
@@ -103,13 +130,22 @@ namespace orbit {
 // fused pass; `do_kick` = false when the kick is deferred to the next fused
 // pass.  Returns the number of kernel launches added through *launches.
 int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStream_t st,
-                    bool do_extrema, bool do_kick, int* launches, double pipe_radius = 0.0);
+                    bool do_extrema, bool do_kick, int* launches, double pipe_radius = 0.0,
+                    const orbit_boundary* bnd = nullptr);
 // Cross-stream ordering of a calculator's buffers: work on stream s waits
 // for the last recorded use, then records a new one.
 cudaError_t sc_order_before(orbit_sc2p5d_t* c, cudaStream_t s);
 cudaError_t sc_mark_used(orbit_sc2p5d_t* c, cudaStream_t s);
 DepScales sc_dep_scales(const orbit_sc2p5d_t* c, const orbit_bunch_t* b);
-SetupArgs sc_setup_args(const orbit_sc2p5d_t* c, const DepScales& d);
+SetupArgs sc_setup_args(const orbit_sc2p5d_t* c, const DepScales& d, const orbit_boundary* bnd = nullptr);
+// The boundary's inside test (type -1 for none).
+BndShape bnd_shape_of(const orbit_boundary* bnd);
+// Subtracts the boundary potential from phi (BaseBoundary2D::addBoundaryPotential)
+// on stream s and recomputes max |phi|; returns launches added.
+int bnd_enqueue_potential(const orbit_boundary* bnd, orbit_sc2p5d_t* c, cudaStream_t s, int* launches);
+// Uploads the boundary's points and least-squares matrix if not yet on the
+// device (outside any stream capture).
+int bnd_ensure_device(orbit_boundary* bnd);
 // While s is being captured into a graph (and the calculator can branch):
 // a conditional handle on that graph for the Green rebuild of the kick
 // whose set-up is about to be enqueued; with `pending` it is kept for that
@@ -137,6 +173,7 @@ struct KickArgs {
   int nx, ny, nz, form;
   const double* lamd;     // 2.5Drb: derivative grid, else null
   double rb_lsf;          // 2.5Drb: -L r_c m / gamma^2
+  BndShape bnd;           // particles outside a conducting boundary are not kicked
 };
 
 }  // namespace orbit

@@ -77,6 +77,11 @@ static __device__ __noinline__ void sc_setup_scalar(ScState* st, unsigned* statu
   double yMin = dkey_inv(key[2]), yMax = dkey_inv(key[3]);
   double zMin = dkey_inv(key[4]), zMax = dkey_inv(key[5]);
   for (int c = 0; c < 3; ++c) { st->key[2 * c] = ~0ull; st->key[2 * c + 1] = 0ull; }
+  if (sa.bnd) {
+    // a boundary fixes the transverse grid to its extents; only z comes
+    // from the bunch (SpaceChargeCalc2p5D.cc:174-196)
+    xMin = sa.bxmin; xMax = sa.bxmax; yMin = sa.bymin; yMax = sa.bymax;
+  }
   int skip = 0;
   if (__ldcg(status) & ST_NAN) {
     // a non-finite coordinate was met by the extrema scan: no kick
@@ -88,7 +93,9 @@ static __device__ __noinline__ void sc_setup_scalar(ScState* st, unsigned* statu
     double xy = st->xy_ratio;
     double ratio_beam = __ddiv_rn(__dsub_rn(xMax, xMin), __dsub_rn(yMax, yMin));
     int set_solver = 0;
-    if (sa.rb) {
+    if (sa.bnd) {
+      xy = ratio_beam;  // :180
+    } else if (sa.rb) {
       // SpaceChargeCalc2p5Drb::bunchAnalysis (SpaceChargeCalc2p5Drb.cc:188-203):
       // always stretched to the calculator's own ratio, which never changes
       double width, center;

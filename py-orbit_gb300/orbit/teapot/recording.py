@@ -29,19 +29,28 @@ class BunchRecorder:
         self.ops = []
         self.calcs = []
         self._cidx = {}
+        self.boundaries = []
+        self._bidx = {}
         self.host_ops = []
 
     # --- called by teapot_base and SpaceChargeCalc2p5D
     def _record_op(self, code, ints, dbls):
         self.ops.append((int(code), tuple(ints), tuple(dbls)))
 
-    def _record_sc(self, calc, length, pipe_radius=0.0):
+    def _record_sc(self, calc, length, pipe_radius=0.0, boundary=None):
         k = self._cidx.get(id(calc))
         if k is None:
             k = len(self.calcs)
             self._cidx[id(calc)] = k
             self.calcs.append(calc)
-        self.ops.append((OP["SC"], (k,), (float(length), float(pipe_radius))))
+        b = 0
+        if boundary is not None:
+            b = self._bidx.get(id(boundary))
+            if b is None:
+                self.boundaries.append(boundary)
+                b = len(self.boundaries)
+                self._bidx[id(boundary)] = b
+        self.ops.append((OP["SC"], (k, b), (float(length), float(pipe_radius))))
 
     def _record_host(self, fn):
         """fn(bunch) runs on the host once per replayed turn (turn counters)."""
@@ -73,11 +82,12 @@ class BunchRecorder:
 class FusedProgram:
     """A recorded op list compiled for the GPU."""
 
-    def __init__(self, ops, calcs, host_ops):
+    def __init__(self, ops, calcs, host_ops, boundaries=()):
         self.ops = list(ops)
         self.calcs = list(calcs)
         self.host_ops = list(host_ops)
-        self.device = DeviceProgram(self.ops, [c._calc for c in self.calcs])
+        self.boundaries = list(boundaries)
+        self.device = DeviceProgram(self.ops, [c._calc for c in self.calcs], [b._dev for b in self.boundaries])
 
     def run(self, bunch, turns=1):
         dev = bunch._device_bunch()

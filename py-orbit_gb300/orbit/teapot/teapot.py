@@ -74,7 +74,7 @@ class TEAPOT_Lattice(AccLattice):
         if prog is None:
             if len(self._programs) > 16:
                 self._programs.clear()
-            prog = FusedProgram(rec.ops, rec.calcs, rec.host_ops)
+            prog = FusedProgram(rec.ops, rec.calcs, rec.host_ops, rec.boundaries)
             self._programs[key] = prog
         return prog
 

@@ -15,7 +15,7 @@ from . import _native
 from ._native import (FORM_FP32, FORM_PLAIN, OP, OrbitError, SpaceChargeError, Sync, call, load,
                       library_path)
 
-__all__ = ["DeviceBunch", "DeviceSC2p5D", "DeviceSC2p5Drb", "DeviceProgram", "OrbitError", "SpaceChargeError", "load",
+__all__ = ["DeviceBunch", "DeviceSC2p5D", "DeviceSC2p5Drb", "DeviceBoundary", "DeviceProgram", "OrbitError", "SpaceChargeError", "load",
            "FORM_PLAIN", "FORM_FP32", "OP", "library_path", "version"]
 
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -136,6 +136,9 @@ class DeviceSC2p5D:
     def track(self, bunch: DeviceBunch, length: float):
         call("orbit_sc2p5d_track", self.h, bunch.h, float(length))
 
+    def track_boundary(self, bunch: DeviceBunch, length: float, boundary: "DeviceBoundary"):
+        call("orbit_sc2p5d_track_boundary", self.h, bunch.h, float(length), boundary.h)
+
     def grid(self, which: int) -> np.ndarray:
         n = self.nz if which in (_native.GRID_LONG, _native.GRID_LONG_DERIV) else self.nx * self.ny
         out = np.empty(n, dtype=np.float64)
@@ -188,10 +191,63 @@ class DeviceSC2p5Drb(DeviceSC2p5D):
         return float(out[0]), float(out[1]), float(out[2])
 
 
+class DeviceBoundary:
+    """A conducting boundary (Boundary2D): points given one by one, or a
+    Circle / Ellipse / Rectangle shape."""
+
+    SHAPES = {"Circle": 1, "Ellipse": 2, "Rectangle": 3}
+
+    def __init__(self, n_points: int, n_modes: int, shape=None, xdim: float = 0.0, ydim=None):
+        h = ctypes.c_void_p()
+        if shape is None:
+            call("orbit_boundary_create", ctypes.byref(h), int(n_points), int(n_modes))
+        else:
+            if shape not in self.SHAPES:
+                raise OrbitError(_native.ORBIT_ERR_ARG, "Boundary2D: the shape should be Circle, Ellipse or Rectangle")
+            call("orbit_boundary_create_shape", ctypes.byref(h), int(n_points), int(n_modes), self.SHAPES[shape],
+                 float(xdim), float(xdim if ydim is None else ydim))
+        self.h = h
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h is not None and h.value and _native._lib is not None:
+            _native._lib.orbit_boundary_destroy(h)
+            self.h = None
+
+    def info(self):
+        npnt, nm, shape, init = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        lim = np.zeros(4)
+        call("orbit_boundary_info", self.h, ctypes.byref(npnt), ctypes.byref(nm), ctypes.byref(shape),
+             lim.ctypes.data_as(_dp), ctypes.byref(init))
+        return npnt.value, nm.value, shape.value, lim, bool(init.value)
+
+    def set_point(self, i, x, y):
+        call("orbit_boundary_set_point", self.h, int(i), float(x), float(y))
+
+    def initialize(self):
+        call("orbit_boundary_initialize", self.h)
+
+    def get_point(self, i):
+        x, y = ctypes.c_double(), ctypes.c_double()
+        call("orbit_boundary_get_point", self.h, int(i), ctypes.byref(x), ctypes.byref(y))
+        return x.value, y.value
+
+    def is_inside(self, x, y) -> int:
+        return _native.load().orbit_boundary_is_inside(self.h, float(x), float(y))
+
+    def lsq(self):
+        npnt, nm, _, _, _ = self.info()
+        out = np.empty((2 * nm + 1, npnt))
+        call("orbit_boundary_lsq", self.h, out.ctypes.data_as(_dp))
+        r = ctypes.c_double()
+        call("orbit_boundary_rnorm", self.h, ctypes.byref(r))
+        return out, r.value
+
+
 class DeviceProgram:
     """A compiled lattice program: ops (code, (i0,i1,i2), (d0..d5)) plus calculators."""
 
-    def __init__(self, ops, calcs):
+    def __init__(self, ops, calcs, boundaries=()):
         arr = (_native.Op * max(1, len(ops)))()
         for k, (code, iv, dv) in enumerate(ops):
             arr[k].code = int(code)
@@ -206,6 +262,10 @@ class DeviceProgram:
         self.h = h
         self.calcs = list(calcs)  # keep the calculators alive
         self.nops = len(ops)
+        self.boundaries = list(boundaries)  # kept alive with the program
+        if self.boundaries:
+            bh = (ctypes.c_void_p * len(self.boundaries))(*[b.h.value for b in self.boundaries])
+            call("orbit_program_set_boundaries", self.h, bh, len(self.boundaries))
 
     def __del__(self):
         h = getattr(self, "h", None)

@@ -95,6 +95,20 @@ _SIGS = {
     "orbit_program_create": (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.POINTER(Op), ctypes.c_int,
                                             ctypes.POINTER(_vp), ctypes.c_int]),
     "orbit_program_destroy": (ctypes.c_int, [_vp]),
+    "orbit_program_set_boundaries": (ctypes.c_int, [_vp, ctypes.POINTER(_vp), ctypes.c_int]),
+    "orbit_boundary_create": (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.c_int, ctypes.c_int]),
+    "orbit_boundary_create_shape": (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                   ctypes.c_double, ctypes.c_double]),
+    "orbit_boundary_destroy": (ctypes.c_int, [_vp]),
+    "orbit_boundary_set_point": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double, ctypes.c_double]),
+    "orbit_boundary_initialize": (ctypes.c_int, [_vp]),
+    "orbit_boundary_get_point": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp]),
+    "orbit_boundary_info": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                           ctypes.POINTER(ctypes.c_int), _dp, ctypes.POINTER(ctypes.c_int)]),
+    "orbit_boundary_is_inside": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_double]),
+    "orbit_boundary_lsq": (ctypes.c_int, [_vp, _dp]),
+    "orbit_boundary_rnorm": (ctypes.c_int, [_vp, _dp]),
+    "orbit_sc2p5d_track_boundary": (ctypes.c_int, [_vp, _vp, ctypes.c_double, _vp]),
     "orbit_program_run": (ctypes.c_int, [_vp, _vp, ctypes.c_int]),
     "orbit_program_enqueue": (ctypes.c_int, [_vp, _vp, ctypes.c_int]),
     "orbit_program_launches": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int)]),

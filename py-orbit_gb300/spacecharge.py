@@ -327,6 +327,84 @@ class Grid1D:
         return None
 
 
+class Boundary2D:
+    """``Boundary2D(nPoints, nModes)`` (points set with setBoundaryPoint, then
+    initialize()) or ``Boundary2D(nPoints, nModes, shape, xDim[, yDim])`` with
+    shape "Circle", "Ellipse" or "Rectangle" (src/spacecharge/wrap_boundary2d.cc,
+    BaseBoundary2D.cc, ShapedBoundary2D.cc): a conducting boundary for the
+    2.5D space-charge kick."""
+
+    IS_INSIDE = 1
+    IS_OUTSIDE = -1
+
+    def __init__(self, nPoints, nModes, shape=None, xDim=None, yDim=None):
+        from orbit_gb300 import DeviceBoundary
+        if shape is None:
+            self._dev = DeviceBoundary(nPoints, nModes)
+            self._shape = "noshape"
+        else:
+            self._dev = DeviceBoundary(nPoints, nModes, shape, xDim, yDim)
+            self._shape = shape
+
+    def _info(self):
+        return self._dev.info()
+
+    def getMaxX(self): return float(self._info()[3][1])
+    def getMinX(self): return float(self._info()[3][0])
+    def getMaxY(self): return float(self._info()[3][3])
+    def getMinY(self): return float(self._info()[3][2])
+    def getNumberOfModes(self): return self._info()[1]
+    def getNumberOfPoints(self): return self._info()[0]
+    def getShapeName(self): return self._shape
+    def isInitialized(self): return 1 if self._info()[4] else 0
+
+    def isInside(self, x, y):
+        return self._dev.is_inside(x, y)
+
+    def initialize(self):
+        self._dev.initialize()
+
+    def getBoundaryPoint(self, index):
+        return self._dev.get_point(index)
+
+    def setBoundaryPoint(self, index, x, y):
+        self._dev.set_point(index, x, y)
+
+    def addBoundaryPotential(self, rhoGrid, phiGrid):
+        """Subtracts the fitted free-space field of the boundary charges from
+        phiGrid (BaseBoundary2D::addBoundaryPotential, BaseBoundary2D.cc:352-460)."""
+        npnt, nm, _, lim, init = self._info()
+        if not init:
+            _finalize("Boundary2D: the boundary was not initialized! Call initialize() method!")
+        if (rhoGrid.getMinX() > lim[0] or rhoGrid.getMaxX() < lim[1] or rhoGrid.getMinY() > lim[2]
+                or rhoGrid.getMaxY() < lim[3]):
+            _finalize("Boundary2D: some boundary points are outside the grids")
+        lsq, rnorm = self._dev.lsq()
+        bphi = np.array([phiGrid.getValue(*self.getBoundaryPoint(j)) for j in range(npnt)])
+        coef = np.array([sum(lsq[i, j] * bphi[j] for j in range(npnt)) for i in range(2 * nm + 1)])
+        arr = phiGrid.getArray()
+        for i in range(phiGrid.getSizeX()):
+            for j in range(phiGrid.getSizeY()):
+                x, y = phiGrid.getGridX(i), phiGrid.getGridY(j)
+                r2 = x * x + y * y
+                if r2 == 0.0:
+                    f = [1.0] + [0.0] * (2 * nm)
+                else:
+                    r = math.sqrt(r2)
+                    s = y / r
+                    c = x / r
+                    s0, c0, rfac, rj = s, c, r / rnorm, 1.0
+                    f = [1.0]
+                    for _ in range(nm):
+                        rj *= rfac
+                        f += [rj * c0, rj * s0]
+                        s0, c0 = s * c0 + c * s0, c * c0 - s * s0
+                p = 0.0
+                for k in range(2 * nm + 1):
+                    p += coef[k] * f[k]
+                phiGrid.setValue(arr[i, j] - p, i, j)
+
+
 class SpaceChargeCalc2p5D:
     """``SpaceChargeCalc2p5D(xSize, ySize, zSize[, xy_ratio])``
     (src/spacecharge/SpaceChargeCalc2p5D.cc, wrap_spacechargecalc2p5d.cc:38-52).
@@ -381,17 +459,19 @@ class SpaceChargeCalc2p5D:
 
     def trackBunch(self, bunch, length, boundary=None):
         """Applies the 2.5D space-charge kick of a lattice part of the given
-        length (SpaceChargeCalc2p5D.cc:77-120)."""
-        if boundary is not None:
-            raise NotImplementedError("trackBunch with a conducting boundary is not available on the GPU path")
+        length, with an optional conducting boundary
+        (SpaceChargeCalc2p5D.cc:77-120)."""
         rec = getattr(bunch, "_record_sc", None)
         if rec is not None:
-            rec(self, float(length))
+            rec(self, float(length), 0.0, boundary)
             return
         if bunch.getSizeGlobal() < 2:
             return
         dev = bunch._device_bunch()
-        self._calc.track(dev, float(length))
+        if boundary is not None:
+            self._calc.track_boundary(dev, float(length), boundary._dev)
+        else:
+            self._calc.track(dev, float(length))
         bunch._device_modified()
         self._version += 1
         dev.sync()
@@ -479,4 +559,4 @@ class SpaceChargeCalc2p5Drb(SpaceChargeCalc2p5D):
         return self._calc.get_long_avg()
 
 
-__all__ = ["SpaceChargeCalc2p5D", "SpaceChargeCalc2p5Drb", "Grid2D", "Grid1D"]
+__all__ = ["SpaceChargeCalc2p5D", "SpaceChargeCalc2p5Drb", "Boundary2D", "Grid2D", "Grid1D"]
