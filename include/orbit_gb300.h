@@ -111,6 +111,23 @@ int orbit_sc2p5d_get_grid(orbit_sc2p5d_t* c, int which, double* host_out);
 /* lim = {xmin,xmax,ymin,ymax,zmin,zmax,dx,dy,dz,xy_ratio,total_macrosize} */
 int orbit_sc2p5d_get_limits(orbit_sc2p5d_t* c, double* lim);
 int orbit_sc2p5d_get_sizes(const orbit_sc2p5d_t* c, int* nx, int* ny, int* nz, int* form);
+/* ---- bunch diagnostics on the device (src/orbit/BunchDiagnostics) ---- */
+/* BunchTwissAnalysis::analyzeBunch (BunchTwissAnalysis.cc:49-140): out[29] =
+ * {count, total macrosize, <c_i> [6], <c_i c_j> for i >= j [21, row i holds
+ * j = 0..i]}, macrosize-weighted with per-particle macrosizes; the
+ * coordinates stay on the device.  Waits for the bunch's stream. */
+int orbit_bunch_moments(orbit_bunch_t* b, double* out);
+/* BunchTuneAnalysis::analyzeBunch (BunchTuneAnalysis.cc:36-108) with
+ * twiss = {betax, alphax, etax, etapx, betay, alphay} and etot = kinetic
+ * energy + mass: per-particle phases, tunes and actions kept on the device
+ * (zero before the first call, as the attribute the reference adds).
+ * Enqueued on the bunch's stream; the first call allocates. */
+int orbit_bunch_tune_analysis(orbit_bunch_t* b, const double* twiss, double etot);
+/* The six attribute rows {xLastPhase, yLastPhase, xLastTune, yLastTune,
+ * xAction, yAction}, each of n values, to or from the host. */
+int orbit_bunch_phase_get(orbit_bunch_t* b, double* host);
+int orbit_bunch_phase_set(orbit_bunch_t* b, const double* host);
+
 /* ---- conducting boundaries (Boundary2D: src/spacecharge/BaseBoundary2D.cc,
  * ShapedBoundary2D.cc, wrap_boundary2d.cc) ---- */
 typedef struct orbit_boundary orbit_boundary_t;

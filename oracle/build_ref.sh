@@ -16,12 +16,13 @@ fi
 mkdir -p "$OUT/obj"
 PYINC=$(python3 -c 'import sysconfig;print(sysconfig.get_paths()["include"])')
 INC="-I$HERE/fftw_shim -I$PYINC"
-for d in src/orbit src/orbit/ParticlesAttributes src/spacecharge src/teapot src/utils src/utils/bunch src/mpi; do
+for d in src/orbit src/orbit/ParticlesAttributes src/orbit/BunchDiagnostics src/spacecharge src/teapot src/utils src/utils/bunch src/mpi; do
   INC="$INC -I$REF/$d"
 done
 SRCS="src/spacecharge/Grid1D.cc src/spacecharge/Grid2D.cc src/spacecharge/PoissonSolver2D.cc
 src/spacecharge/PoissonSolverFFT2D.cc src/spacecharge/SpaceChargeCalc2p5D.cc src/spacecharge/BaseBoundary2D.cc
 src/spacecharge/SpaceChargeCalc2p5Drb.cc src/spacecharge/ShapedBoundary2D.cc
+src/orbit/BunchDiagnostics/BunchTwissAnalysis.cc src/orbit/BunchDiagnostics/BunchTuneAnalysis.cc
 src/teapot/teapotbase.cc src/orbit/Bunch.cc src/orbit/SyncPart.cc src/orbit/OrbitConst.cc
 src/utils/BufferStore.cc src/utils/CppPyWrapper.cc src/utils/AttributesBucket.cc src/utils/StringUtils.cc
 src/utils/bunch/BunchExtremaCalculator.cc src/mpi/orbit_mpi.cc"

@@ -110,6 +110,8 @@ def lib():
         L.oracle_bnd_is_inside.restype = ctypes.c_int
         L.oracle_bnd_is_inside.argtypes = [_vp, ctypes.c_double, ctypes.c_double]
         L.oracle_bnd_get.argtypes = [_vp, _dp, _dp, _dp, _dp]
+        L.oracle_twiss_moments.argtypes = [_dp, ctypes.c_int, _dp, _dp]
+        L.oracle_tune_analysis.argtypes = [_dp, ctypes.c_int, ctypes.c_double, ctypes.c_double, _dp, _dp]
         L.oracle_sc_track_bnd.restype = ctypes.c_int
         L.oracle_sc_track_bnd.argtypes = [_vp, _dp, ctypes.c_int, _dp, ctypes.POINTER(OracleSync), ctypes.c_double,
                                           _vp, ctypes.c_int]
@@ -226,6 +228,24 @@ class OracleBoundary:
         return head, bx, by, lsq.reshape(2 * nm + 1, np_)
 
 
+def twiss_moments(soa, msize=None):
+    """{count, total macrosize, <c_i>[6], <c_i c_j> i >= j [21]} as
+    BunchTwissAnalysis::analyzeBunch accumulates them."""
+    soa = np.ascontiguousarray(soa, dtype=np.float64)
+    out = np.zeros(29)
+    m = None if msize is None else _P(np.ascontiguousarray(msize, dtype=np.float64))
+    lib().oracle_twiss_moments(_P(soa), soa.shape[1], m, _P(out))
+    return out
+
+
+def tune_analysis(soa, beta, etot, twiss, ph):
+    """BunchTuneAnalysis::analyzeBunch; ph (6, n) is updated in place."""
+    soa = np.ascontiguousarray(soa, dtype=np.float64)
+    tw = np.ascontiguousarray(twiss, dtype=np.float64)
+    assert ph.dtype == np.float64 and ph.flags.c_contiguous and ph.shape == (6, soa.shape[1])
+    lib().oracle_tune_analysis(_P(soa), soa.shape[1], float(beta), float(etot), _P(tw), _P(ph))
+
+
 def sc_track_bnd(sc, soa, sync, length, bnd, msize=None, nthreads=1):
     m = None if msize is None else _P(np.ascontiguousarray(msize, dtype=np.float64))
     return lib().oracle_sc_track_bnd(sc.h, _P(soa), soa.shape[1], m, ctypes.byref(sync), float(length), bnd.h,
@@ -333,6 +353,11 @@ def ref():
         L.ref_bnd_is_inside.argtypes = [_vp, ctypes.c_double, ctypes.c_double]
         L.ref_bnd_get.argtypes = [_vp, _dp, _dp, _dp]
         L.ref_sc_track_bnd.argtypes = [_vp, _vp, ctypes.c_double, _vp]
+        L.ref_twiss.argtypes = [_vp, _dp, _dp]
+        L.ref_tune_new.restype = _vp
+        L.ref_tune_free.argtypes = [_vp]
+        L.ref_tune_assign.argtypes = [_vp, _dp]
+        L.ref_tune_analyze.argtypes = [_vp, _vp, _dp]
         _ref = L
     return _ref
 
@@ -471,3 +496,28 @@ class RefBoundary:
 
 def ref_sc_track_bnd(sc: "RefSC", bunch: RefBunch, length: float, bnd: RefBoundary):
     ref().ref_sc_track_bnd(sc.h, bunch.h, float(length), bnd.h)
+
+
+def ref_twiss(bunch: RefBunch):
+    """(moments[29], getters[27]) of the reference's BunchTwissAnalysis."""
+    out, g = np.zeros(29), np.zeros(27)
+    ref().ref_twiss(bunch.h, _P(out), _P(g))
+    return out, g
+
+
+class RefTune:
+    """A reference BunchTuneAnalysis driven through the harness."""
+
+    def __init__(self, twiss):
+        self.h = ref().ref_tune_new()
+        ref().ref_tune_assign(self.h, _P(np.ascontiguousarray(twiss, dtype=np.float64)))
+
+    def __del__(self):
+        if getattr(self, "h", None) and _ref is not None:
+            _ref.ref_tune_free(self.h)
+            self.h = None
+
+    def analyze(self, bunch: RefBunch):
+        ph = np.zeros((6, bunch.n))
+        ref().ref_tune_analyze(self.h, bunch.h, _P(ph))
+        return ph

@@ -1448,6 +1448,77 @@ int oracle_run_program(const oracle_op_t* ops, int nops, int turns, double* soa,
 
 /* BunchTwissAnalysis::analyzeBunch + getEmittance for planes 0,1
  * (BunchTwissAnalysis.cc:49-140, 372-390), equal macrosizes. */
+/* BunchTwissAnalysis::analyzeBunch (BunchTwissAnalysis.cc:49-140):
+ * out = {count, total macrosize, <c_i> [6], <c_i c_j> for i >= j [21, row i
+ * holds j = 0..i]}, macrosize-weighted when msize is given. */
+void oracle_twiss_moments(const double* soa, int n, const double* msize, double* out) {
+  double avg[6] = {0}, corr[36] = {0}, total = 0.;
+  if (msize) {
+    for (int ip = 0; ip < n; ip++) {
+      double m = msize[ip];
+      total += m;
+      for (int i = 0; i < 6; i++) avg[i] += m * soa[(size_t)i * n + ip];
+      for (int i = 0; i < 6; i++)
+        for (int j = 0; j < i + 1; j++) corr[i + 6 * j] += m * soa[(size_t)i * n + ip] * soa[(size_t)j * n + ip];
+    }
+  } else {
+    double m = 1.0;
+    for (int ip = 0; ip < n; ip++) {
+      for (int i = 0; i < 6; i++) avg[i] += soa[(size_t)i * n + ip];
+      for (int i = 0; i < 6; i++)
+        for (int j = 0; j < i + 1; j++) corr[i + 6 * j] += soa[(size_t)i * n + ip] * soa[(size_t)j * n + ip];
+    }
+    total += n * m;
+    for (int i = 0; i < 6; i++) avg[i] *= m;
+    for (int i = 0; i < 6; i++)
+      for (int j = 0; j < i + 1; j++) corr[i + 6 * j] *= m;
+  }
+  out[0] = n;
+  out[1] = total;
+  int k = 8;
+  for (int i = 0; i < 6; i++) out[2 + i] = fabs(total) > 0. ? avg[i] / total : 0.;
+  for (int i = 0; i < 6; i++)
+    for (int j = 0; j < i + 1; j++) out[k++] = fabs(total) > 0. ? corr[i + 6 * j] / total : 0.;
+}
+
+/* BunchTuneAnalysis::analyzeBunch (BunchTuneAnalysis.cc:36-108): per
+ * particle the normalised phases, the phase advance since the last call
+ * ("tune") and the actions; ph holds six SoA rows {xLastPhase, yLastPhase,
+ * xLastTune, yLastTune, xAction, yAction} of n.  twiss = {betax, alphax,
+ * etax, etapx, betay, alphay}; etot = kinetic energy + mass. */
+void oracle_tune_analysis(const double* soa, int n, double beta, double etot, const double* twiss, double* ph) {
+  const double betax = twiss[0], alphax = twiss[1], etax = twiss[2], etapx = twiss[3];
+  const double betay = twiss[4], alphay = twiss[5];
+  for (int i = 0; i < n; i++) {
+    double x = X(i), xp = XP(i), y = Y(i), yp = YP(i);
+    double dpp = 1 / (beta * beta) * DE(i) / etot;
+    double xval = (x - etax * dpp) / sqrt(betax);
+    double xpval = (xp - etapx * dpp) * sqrt(betax) + xval * alphax;
+    double yval = y / sqrt(betay);
+    double ypval = (yp + y * alphay / betay) * sqrt(betay);
+    double angle = atan2(xpval, xval);
+    if (angle < 0.) angle += (2.0 * ORACLE_PI);
+    double xPhase = angle;
+    double xTune = (ph[(size_t)0 * n + i] - xPhase) / (2.0 * ORACLE_PI);
+    if (xTune < 0.) xTune += 1.;
+    ph[(size_t)0 * n + i] = xPhase;
+    ph[(size_t)2 * n + i] = xTune;
+    angle = atan2(ypval, yval);
+    if (angle < 0.) angle += (2.0 * ORACLE_PI);
+    double yPhase = angle;
+    double yTune = (ph[(size_t)1 * n + i] - yPhase) / (2.0 * ORACLE_PI);
+    if (yTune < 0.) yTune += 1.;
+    ph[(size_t)1 * n + i] = yPhase;
+    ph[(size_t)3 * n + i] = yTune;
+    double xc = x - etax * dpp, yc = y;
+    double xpfac = xp - etapx * dpp, ypfac = yp;
+    double pxc = xpfac + xc * (alphax / betax);
+    double pyc = ypfac + yc * (alphay / betay);
+    ph[(size_t)4 * n + i] = xc * xc / betax + pxc * pxc * betax;
+    ph[(size_t)5 * n + i] = yc * yc / betay + pyc * pyc * betay;
+  }
+}
+
 void oracle_rms_emittance(const double* soa, int n, double* ex, double* ey) {
   double avg[6] = {0}, corr[36] = {0};
   for (int ip = 0; ip < n; ip++) {

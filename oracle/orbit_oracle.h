@@ -84,6 +84,14 @@ void oracle_bnd_get(const oracle_bnd_t* b, double* head, double* bx, double* by,
 int oracle_sc_track_bnd(oracle_sc_t* s, double* soa, int n, const double* msize, const oracle_sync_t* sync,
                         double length, oracle_bnd_t* b, int nthreads);
 
+/* ---- bunch diagnostics (src/orbit/BunchDiagnostics) ---- */
+/* BunchTwissAnalysis::analyzeBunch: out[29] = {count, total macrosize,
+ * <c_i> [6], <c_i c_j> i >= j [21]}. */
+void oracle_twiss_moments(const double* soa, int n, const double* msize, double* out);
+/* BunchTuneAnalysis::analyzeBunch: ph = 6 SoA rows of n {xLastPhase,
+ * yLastPhase, xLastTune, yLastTune, xAction, yAction}, updated in place. */
+void oracle_tune_analysis(const double* soa, int n, double beta, double etot, const double* twiss, double* ph);
+
 /* ---- TEAPOT maps (src/teapot/teapotbase.cc) ---- */
 void oracle_rotatexy(double* soa, int n, double angle);
 void oracle_drift(double* soa, int n, oracle_sync_t* s, double length);

@@ -14,6 +14,9 @@
 #include "SpaceChargeCalc2p5D.hh"
 #include "SpaceChargeCalc2p5Drb.hh"
 #include "ShapedBoundary2D.hh"
+#include "BunchTwissAnalysis.hh"
+#include "BunchTuneAnalysis.hh"
+#include "ParticleAttributes.hh"
 #include <string>
 #include "Grid1D.hh"
 #include "Grid2D.hh"
@@ -126,6 +129,53 @@ void ref_sc_fields(void* sc, int n, const double* x, const double* y, const doub
     p->calcGradient(x[i], y[i], ex[i], ey[i]);
     lam[i] = zg->getValue(z[i]);
   }
+}
+
+// ---- bunch diagnostics (src/orbit/BunchDiagnostics) ----
+// BunchTwissAnalysis::analyzeBunch, then out = {count, total macrosize,
+// <c_i> [6], getCorrelation(i, j) for i >= j [21]} and the
+// getters g = {emittance, normalized, alpha, beta, gamma} x {x, y, z},
+// dispersion and its derivative x, y, effective {emittance, alpha, beta,
+// gamma} x, y.
+void ref_twiss(void* b, double* out, double* g) {
+  BunchTwissAnalysis t;
+  t.analyzeBunch((Bunch*)b);
+  out[0] = t.getGlobalCount();
+  out[1] = t.getGlobalMacrosize();
+  for (int i = 0; i < 6; ++i) out[2 + i] = t.getAverage(i);
+  int k = 8;
+  for (int i = 0; i < 6; ++i)
+    for (int j = 0; j <= i; ++j) out[k++] = t.getCorrelation(i, j);
+  k = 0;
+  for (int ic = 0; ic < 3; ++ic) {
+    g[k++] = t.getEmittance(ic);
+    g[k++] = t.getEmittanceNormalized(ic);
+    g[k++] = t.getAlpha(ic);
+    g[k++] = t.getBeta(ic);
+    g[k++] = t.getGamma(ic);
+  }
+  for (int ic = 0; ic < 2; ++ic) {
+    g[k++] = t.getDispersion(ic);
+    g[k++] = t.getDispersionDerivative(ic);
+    g[k++] = t.getEffectiveEmittance(ic);
+    g[k++] = t.getEffectiveAlpha(ic);
+    g[k++] = t.getEffectiveBeta(ic);
+    g[k++] = t.getEffectiveGamma(ic);
+  }
+}
+void* ref_tune_new() { return new BunchTuneAnalysis(); }
+void ref_tune_free(void* t) { delete (BunchTuneAnalysis*)t; }
+void ref_tune_assign(void* t, const double* tw) {
+  ((BunchTuneAnalysis*)t)->assignTwiss(tw[0], tw[1], tw[2], tw[3], tw[4], tw[5]);
+}
+// analyzeBunch, then the six attribute rows (SoA of n)
+void ref_tune_analyze(void* t, void* b, double* ph) {
+  Bunch* bunch = (Bunch*)b;
+  ((BunchTuneAnalysis*)t)->analyzeBunch(bunch);
+  int n = bunch->getSize();
+  ParticleAttributes* a = bunch->getParticleAttributes("ParticlePhaseAttributes");
+  for (int k = 0; k < 6; ++k)
+    for (int i = 0; i < n; ++i) ph[(size_t)k * n + i] = a->attValue(i, k);
 }
 
 // ---- boundaries (src/spacecharge/BaseBoundary2D.cc, ShapedBoundary2D.cc) ----

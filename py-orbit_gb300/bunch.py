@@ -1,5 +1,5 @@
 """Module ``bunch``: the PyORBIT ``Bunch`` / ``SyncPart`` /
-``BunchTwissAnalysis`` interface (src/orbit/wrap_bunch.cc,
+``BunchTwissAnalysis`` / ``BunchTuneAnalysis`` interface (src/orbit/wrap_bunch.cc,
 src/orbit/wrap_syncpart.cc, src/orbit/BunchDiagnostics/) over a
 device-resident bunch.
 
@@ -22,6 +22,10 @@ _COORDS = ("x", "xp", "y", "yp", "z", "dE")
 MASS_PROTON = 0.938272013
 CLASSICAL_RADIUS_PROTON = 1.534698e-18
 CHARGE_PROTON = 1.0
+
+# ParticlePhaseAttributes.cc: six values per particle {xLastPhase,
+# yLastPhase, xLastTune, yLastTune, xAction, yAction}
+PHASE_ATTR = "ParticlePhaseAttributes"
 
 
 class SyncPart:
@@ -138,9 +142,20 @@ class Bunch:
         self._part_attr_dict = {}
         self._sync = SyncPart(self)
         self._sync_dirty = True
+        self._phase_dev = False  # device phase rows newer than the host attribute
 
     # ------------------------------------------------------------ storage
+    def _pull_attrs(self):
+        """Brings the ParticlePhaseAttributes rows that a device tune
+        analysis wrote back into the host attribute."""
+        if self._phase_dev:
+            self._phase_dev = False
+            arr = self._part_attr.get(PHASE_ATTR)
+            if arr is not None and self._n > 0:
+                arr[: self._n, :6] = self._dev.phase_get().T
+
     def _ensure_host(self):
+        self._pull_attrs()
         if not self._host_ok:
             if self._host.shape[1] < self._n:
                 self._host = np.zeros((6, max(self._n, 16)), dtype=np.float64)
@@ -231,6 +246,7 @@ class Bunch:
         self.compress()
 
     def deleteAllParticles(self):
+        self._phase_dev = False
         self._n = 0
         self._host_ok = True
         self._host_modified()
@@ -301,6 +317,7 @@ class Bunch:
         self._flag = np.ones(max(n, 16), dtype=np.int8)
         for name, arr in list(self._part_attr.items()):
             self._part_attr[name] = np.zeros((max(n, 16), arr.shape[1]))
+        self._phase_dev = False
         self._n = n
         self._host_ok = True
         self._host_modified()
@@ -399,7 +416,7 @@ class Bunch:
         return 1 if name in self._attr_int else 0
 
     # --------------------------------------- particle attributes
-    _PART_ATTR_SIZES = {"macrosize": 1, "ParticleIdNumber": 1, "TurnNumber": 1}
+    _PART_ATTR_SIZES = {"macrosize": 1, "ParticleIdNumber": 1, "TurnNumber": 1, PHASE_ATTR: 6}
 
     def addPartAttr(self, name, params=None):
         if name in self._part_attr:
@@ -413,6 +430,8 @@ class Bunch:
             self._host_modified()
 
     def removePartAttr(self, name):
+        if name == PHASE_ATTR:
+            self._phase_dev = False
         self._part_attr.pop(name, None)
         self._part_attr_dict.pop(name, None)
         if name == "macrosize":
@@ -432,6 +451,7 @@ class Bunch:
         return self._part_attr[name].shape[1]
 
     def partAttrValue(self, name, index, attr_index, value=None):
+        self._pull_attrs()
         arr = self._part_attr[name]
         if value is not None:
             arr[index, attr_index] = float(value)
@@ -545,37 +565,54 @@ class Bunch:
 
 
 class BunchTwissAnalysis:
-    """Second moments, rms emittances and Twiss parameters
-    (src/orbit/BunchDiagnostics/BunchTwissAnalysis.cc:49-140, 344-420)."""
+    """First and second moments, rms emittances, Twiss parameters and
+    dispersion (src/orbit/BunchDiagnostics/BunchTwissAnalysis.cc:49-140,
+    343-531).  analyzeBunch reduces the moments on the device where the
+    coordinates live (a deterministic two-level sum: per-block partials, then
+    the blocks in a fixed order) and reads back 29 numbers; the getters are
+    the reference's host formulas over those moments."""
 
     def __init__(self):
         self._avg = np.zeros(6)
         self._corr = np.zeros((6, 6))
         self._count = 0
         self._total_m = 0.0
+        self._momentum = 0.0
         self._beta = 0.0
         self._gamma = 1.0
+        self._kin = 0.0
+        self._mass = 0.0
 
     def analyzeBunch(self, bunch: Bunch):
         bunch.compress()
-        c = bunch.getCoordinates()
-        n = c.shape[1]
-        self._count = n
-        if "macrosize" in bunch._part_attr:
-            m = bunch._part_attr["macrosize"][:n, 0]
-        else:
-            m = np.ones(n)
-        self._total_m = float(m.sum())
-        if self._total_m != 0.0:
-            self._avg = (c * m).sum(axis=1) / self._total_m
-            self._corr = (c * m) @ c.T / self._total_m
-        s = bunch.getSyncParticle()
-        self._beta, self._gamma = s.beta(), s.gamma()
+        self._load(bunch._device_bunch().moments(), bunch.getSyncParticle())
 
+    def _load(self, mom, s):
+        """Takes the 29 moments {count, total macrosize, averages, <c_i c_j>
+        (i >= j)} and the reference particle's kinematics."""
+        self._count = int(mom[0])
+        self._total_m = float(mom[1])
+        self._avg = mom[2:8].copy()
+        corr = np.zeros((6, 6))
+        k = 8
+        for i in range(6):  # BunchTwissAnalysis.cc:126-133: symmetric fill
+            for j in range(i + 1):
+                corr[i, j] = corr[j, i] = mom[k]
+                k += 1
+        self._corr = corr
+        self._momentum, self._beta, self._gamma = s.momentum(), s.beta(), s.gamma()
+        self._kin, self._mass = s.kinEnergy(), s.mass()
+
+    # The getters compute in numpy float64 so that a zero denominator gives
+    # inf or nan as the reference's C arithmetic does, not an exception.
     def getCorrelation(self, i, j):
-        return float(self._corr[i, j] - self._avg[i] * self._avg[j])
+        if i < 0 or i > 5 or j < 0 or j > 5:
+            return 0.0
+        return float(np.float64(self._corr[i, j]) - np.float64(self._avg[i]) * np.float64(self._avg[j]))
 
     def getAverage(self, i):
+        if i < 0 or i > 5:
+            return 0.0
         return float(self._avg[i])
 
     def getGlobalCount(self):
@@ -584,34 +621,130 @@ class BunchTwissAnalysis:
     def getGlobalMacrosize(self):
         return self._total_m
 
+    def _plane(self, ic):
+        C = lambda a, b: np.float64(self.getCorrelation(a, b))  # noqa: E731
+        return (abs(C(2 * ic, 2 * ic)), abs(C(2 * ic + 1, 2 * ic + 1)), C(2 * ic, 2 * ic + 1),
+                C(2 * ic, 5), C(2 * ic + 1, 5), abs(C(5, 5)))
+
     def getEmittance(self, ic):
         if ic < 0 or ic > 2:
             return 0.0
-        C = self.getCorrelation
-        x2, xp2 = abs(C(2 * ic, 2 * ic)), abs(C(2 * ic + 1, 2 * ic + 1))
-        xxp, xdE, xpdE = C(2 * ic, 2 * ic + 1), C(2 * ic, 5), C(2 * ic + 1, 5)
-        dE2 = abs(C(5, 5))
-        if ic == 2 or dE2 == 0:
-            return math.sqrt(abs(x2 * xp2 - xxp * xxp))
-        return math.sqrt(abs((x2 - xdE * xdE / dE2) * (xp2 - xpdE * xpdE / dE2)
-                             - (xxp - xdE * xpdE / dE2) ** 2))
+        x2, xp2, xxp, xdE, xpdE, dE2 = self._plane(ic)
+        with np.errstate(all="ignore"):
+            if ic == 2 or dE2 == 0:
+                return float(np.sqrt(abs(x2 * xp2 - xxp * xxp)))
+            return float(np.sqrt(abs((x2 - xdE * xdE / dE2) * (xp2 - xpdE * xpdE / dE2)
+                                     - (xxp - xdE * xpdE / dE2) * (xxp - xdE * xpdE / dE2))))
 
     def getEmittanceNormalized(self, ic):
+        if ic < 0 or ic > 2:
+            return 0.0
         if ic == 2:
             return self.getEmittance(ic)
-        return self.getEmittance(ic) * self._gamma * self._beta
-
-    def getBeta(self, ic):
-        e = self.getEmittance(ic)
-        return abs(self.getCorrelation(2 * ic, 2 * ic)) / e if e else 0.0
+        return float(np.float64(self.getEmittance(ic)) * self._gamma * self._beta)
 
     def getAlpha(self, ic):
-        e = self.getEmittance(ic)
-        return -self.getCorrelation(2 * ic, 2 * ic + 1) / e if e else 0.0
+        if ic < 0 or ic > 2:
+            return 0.0
+        x2, xp2, xxp, xdE, xpdE, dE2 = self._plane(ic)
+        e = np.float64(self.getEmittance(ic))
+        with np.errstate(all="ignore"):
+            if ic == 2:
+                return float(-xxp / e)
+            return float(-(xxp - xdE * xpdE / dE2) / e)
+
+    def getBeta(self, ic):
+        if ic < 0 or ic > 2:
+            return 0.0
+        x2, xp2, xxp, xdE, xpdE, dE2 = self._plane(ic)
+        e = np.float64(self.getEmittance(ic))
+        with np.errstate(all="ignore"):
+            if ic == 2:
+                return float(x2 / e)
+            return float((x2 - xdE * xdE / dE2) / e)
 
     def getGamma(self, ic):
-        e = self.getEmittance(ic)
-        return abs(self.getCorrelation(2 * ic + 1, 2 * ic + 1)) / e if e else 0.0
+        if ic < 0 or ic > 2:
+            return 0.0
+        x2, xp2, xxp, xdE, xpdE, dE2 = self._plane(ic)
+        e = np.float64(self.getEmittance(ic))
+        with np.errstate(all="ignore"):
+            if ic == 2:
+                return float(xp2 / e)
+            return float((xp2 - xpdE * xpdE / dE2) / e)
+
+    def getDispersion(self, ic):
+        if ic < 0 or ic > 1:
+            return 0.0
+        x2, xp2, xxp, xdE, xpdE, dE2 = self._plane(ic)
+        with np.errstate(all="ignore"):
+            return float(xdE / dE2 * self._momentum * self._beta)
+
+    def getDispersionDerivative(self, ic):
+        if ic < 0 or ic > 1:
+            return 0.0
+        x2, xp2, xxp, xdE, xpdE, dE2 = self._plane(ic)
+        with np.errstate(all="ignore"):
+            return float(xpdE / dE2 * self._momentum * self._beta)
+
+    def _effective(self, ic):
+        x2, xp2, xxp = self._plane(ic)[:3]
+        return x2, xp2, xxp, x2 * xp2 - xxp * xxp
+
+    def getEffectiveEmittance(self, ic):
+        if ic < 0 or ic > 2:
+            return 0.0
+        e2 = self._effective(ic)[3]
+        return float(np.sqrt(abs(e2)))
+
+    def getEffectiveAlpha(self, ic):
+        if ic < 0 or ic > 2:
+            return 0.0
+        x2, xp2, xxp, e2 = self._effective(ic)
+        if e2 <= 0.0:
+            return 0.0
+        return float(-xxp / np.sqrt(e2))
+
+    def getEffectiveBeta(self, ic):
+        if ic < 0 or ic > 2:
+            return 0.0
+        x2, xp2, xxp, e2 = self._effective(ic)
+        if e2 <= 0.0:
+            return 0.0
+        return float(x2 / np.sqrt(e2))
+
+    def getEffectiveGamma(self, ic):
+        if ic < 0 or ic > 2:
+            return 0.0
+        x2, xp2, xxp, e2 = self._effective(ic)
+        if e2 <= 0.0:
+            return float(np.finfo(np.float64).max)  # DBL_MAX
+        return float(xp2 / np.sqrt(e2))
 
 
-__all__ = ["Bunch", "SyncPart", "BunchTwissAnalysis"]
+class BunchTuneAnalysis:
+    """Per-particle betatron phases, phase advances ("tunes") and actions
+    (src/orbit/BunchDiagnostics/BunchTuneAnalysis.cc:27-108).  The six
+    values per particle live in the bunch's ParticlePhaseAttributes; while
+    successive analyses run on the device they stay there, and the host
+    attribute is refreshed only when the host reads it."""
+
+    def __init__(self):
+        self._twiss = np.zeros(6)
+
+    def assignTwiss(self, betax, alphax, etax, etapx, betay, alphay):
+        self._twiss = np.array([betax, alphax, etax, etapx, betay, alphay], dtype=np.float64)
+
+    def analyzeBunch(self, bunch: Bunch):
+        bunch.compress()
+        if not bunch.hasPartAttr(PHASE_ATTR):
+            bunch.addPartAttr(PHASE_ATTR)
+        dev = bunch._device_bunch()
+        if not bunch._phase_dev:
+            dev.phase_set(np.ascontiguousarray(bunch._part_attr[PHASE_ATTR][: bunch._n, :6].T))
+        s = bunch.getSyncParticle()
+        dev.tune_analysis(self._twiss, s.kinEnergy() + s.mass())  # BunchTuneAnalysis.cc:63
+        bunch._phase_dev = True
+
+
+__all__ = ["Bunch", "SyncPart", "BunchTwissAnalysis", "BunchTuneAnalysis"]

@@ -179,6 +179,8 @@ int orbit_bunch_destroy(orbit_bunch_t* b) {
   if (b->stream) cudaStreamSynchronize(b->stream);
   if (b->d_coords) cudaFree(b->d_coords);
   if (b->d_msize) cudaFree(b->d_msize);
+  if (b->d_phase) cudaFree(b->d_phase);
+  if (b->d_diag) cudaFree(b->d_diag);
   if (b->d_status) cudaFree(b->d_status);
   if (b->h_status) cudaFreeHost(b->h_status);
   if (b->stream) cudaStreamDestroy(b->stream);

@@ -82,5 +82,10 @@ struct orbit_bunch {
   unsigned* h_status = nullptr; // pinned mirror
   cudaStream_t stream = nullptr;
   orbit_sync_t sync{};
+  // diagnostics: per-particle phase attributes (6 rows of phase_cap) and the
+  // reduction scratch of the moments
+  double* d_phase = nullptr;
+  int phase_cap = 0;
+  double* d_diag = nullptr;
   double* coord(int c) const { return d_coords + (size_t)c * cap; }
 };

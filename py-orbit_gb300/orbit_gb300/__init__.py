@@ -102,6 +102,35 @@ class DeviceBunch:
     def sync(self):
         call("orbit_bunch_sync", self.h)
 
+    # ------------------------------------------------- diagnostics
+    def moments(self) -> np.ndarray:
+        """{count, total macrosize, <c_i>[6], <c_i c_j> (i >= j)[21]}: the
+        sums of BunchTwissAnalysis::analyzeBunch reduced on the device."""
+        out = np.zeros(29)
+        call("orbit_bunch_moments", self.h, out.ctypes.data_as(_dp))
+        return out
+
+    def tune_analysis(self, twiss, etot: float):
+        """BunchTuneAnalysis::analyzeBunch on the device; twiss = {betax,
+        alphax, etax, etapx, betay, alphay}, etot = kinetic energy + mass."""
+        tw = np.ascontiguousarray(twiss, dtype=np.float64)
+        if tw.shape != (6,):
+            raise ValueError("expected six lattice functions")
+        call("orbit_bunch_tune_analysis", self.h, tw.ctypes.data_as(_dp), float(etot))
+
+    def phase_get(self) -> np.ndarray:
+        """(6, n) rows {xLastPhase, yLastPhase, xLastTune, yLastTune,
+        xAction, yAction}."""
+        out = np.zeros((6, self._n))
+        call("orbit_bunch_phase_get", self.h, out.ctypes.data_as(_dp))
+        return out
+
+    def phase_set(self, rows):
+        rows = np.ascontiguousarray(rows, dtype=np.float64)
+        if rows.shape != (6, self._n):
+            raise ValueError("expected a (6, n) array")
+        call("orbit_bunch_phase_set", self.h, rows.ctypes.data_as(_dp))
+
     def stream_ptr(self) -> int:
         """The bunch's cudaStream_t as an integer."""
         v = ctypes.c_void_p()

@@ -96,6 +96,10 @@ _SIGS = {
                                             ctypes.POINTER(_vp), ctypes.c_int]),
     "orbit_program_destroy": (ctypes.c_int, [_vp]),
     "orbit_program_set_boundaries": (ctypes.c_int, [_vp, ctypes.POINTER(_vp), ctypes.c_int]),
+    "orbit_bunch_moments": (ctypes.c_int, [_vp, _dp]),
+    "orbit_bunch_tune_analysis": (ctypes.c_int, [_vp, _dp, ctypes.c_double]),
+    "orbit_bunch_phase_get": (ctypes.c_int, [_vp, _dp]),
+    "orbit_bunch_phase_set": (ctypes.c_int, [_vp, _dp]),
     "orbit_boundary_create": (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.c_int, ctypes.c_int]),
     "orbit_boundary_create_shape": (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                    ctypes.c_double, ctypes.c_double]),

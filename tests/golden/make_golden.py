@@ -161,6 +161,29 @@ def bnd_case(name, soa, nx, ny, nz, bnd_args, seq, points=None, ek=1.0, msize=1e
     print("wrote", name, "kicks", k)
 
 
+def diag_case(name, soa, twiss, steps, ek=1.0, msize=1e9):
+    """BunchTwissAnalysis moments and getters, and BunchTuneAnalysis
+    attributes after each analysis; steps: maps applied between analyses."""
+    b = O.RefBunch(soa, ek, msize)
+    out = {"init": soa, "ek": ek, "macrosize": msize, "twiss": np.array(twiss)}
+    mom, g = O.ref_twiss(b)
+    out["moments"] = mom
+    out["getters"] = g
+    tune = O.RefTune(twiss)
+    out["phase_0"] = tune.analyze(b)
+    seq_txt = []
+    for k, step in enumerate(steps):
+        b.tpb(step[0], *step[1])
+        seq_txt.append("%s:%r" % (step[0], tuple(step[1])))
+        out["coords_%d" % (k + 1)] = b.coords()
+        out["phase_%d" % (k + 1)] = tune.analyze(b)
+    out["sequence"] = np.array(seq_txt)
+    out["kin"] = np.array([b.kinematics()[q] for q in ("beta", "gamma", "momentum", "kin_energy", "mass",
+                                                      "classical_radius", "time")])
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print("wrote", name)
+
+
 def main():
     if not O.ref_available():
         if not O.build_reference():
@@ -213,6 +236,13 @@ def main():
     t = 2 * np.pi * np.arange(64) / 64
     bnd_case("bnd_points_40x40x8", gaussian(2048, 131), 40, 40, 8, (64, 6), [("sc", 0.5)],
              points=list(zip(0.03 * np.cos(t) + 0.002, 0.02 * np.sin(t))))
+    # 8) bunch diagnostics: a correlated bunch with offsets and dispersion
+    d = gaussian(3000, 141)
+    d[0] += 1e-3
+    d[1] += 0.1 * d[0]
+    d[0] += 2.0 * d[5]
+    diag_case("diag_twiss_tune", d, [10.0, -1.2, 0.5, 0.1, 8.0, 0.7],
+              [("quad1", (0.5, 0.5)), ("drift", (1.0,)), ("quad1", (0.5, -0.5))])
 
 
 if __name__ == "__main__":

@@ -143,3 +143,66 @@ def test_multithreaded_slices_match_within_summation_order():
     s2.track(b, s, 0.5, nthreads=7)
     assert rel_err(s2.grids()[1], s1.grids()[1]) <= 1e-14
     assert rel_err(b[1] - g["init"][1], a[1] - g["init"][1]) <= 1e-12
+
+
+def centered(mom):
+    """The 29 moments with <c_i c_j> replaced by the centered correlation
+    <c_i c_j> - <c_i><c_j> (BunchTwissAnalysis::getCorrelation)."""
+    out = np.array(mom, dtype=np.float64)
+    k = 8
+    for i in range(6):
+        for j in range(i + 1):
+            out[k] = mom[k] - mom[2 + i] * mom[2 + j]
+            k += 1
+    return out
+
+
+def twiss_getters(t):
+    """The 27 getters in the order the golden fixture stores them."""
+    g = []
+    for ic in range(3):
+        g += [t.getEmittance(ic), t.getEmittanceNormalized(ic), t.getAlpha(ic), t.getBeta(ic), t.getGamma(ic)]
+    for ic in range(2):
+        g += [t.getDispersion(ic), t.getDispersionDerivative(ic), t.getEffectiveEmittance(ic),
+              t.getEffectiveAlpha(ic), t.getEffectiveBeta(ic), t.getEffectiveGamma(ic)]
+    return np.array(g)
+
+
+def test_diag_oracle_and_host_getters():
+    """BunchTwissAnalysis moments (oracle) and the product's host getters
+    over them, and the BunchTuneAnalysis phases, tunes and actions after each
+    map, bit for bit against the reference."""
+    from bunch import Bunch, BunchTwissAnalysis
+    g = load_golden("diag_twiss_tune")
+    mom = O.twiss_moments(g["init"])
+    assert np.array_equal(centered(mom), g["moments"])
+    b = Bunch()
+    b.getSyncParticle().kinEnergy(float(g["ek"]))
+    t = BunchTwissAnalysis()
+    t._load(mom, b.getSyncParticle())
+    assert np.array_equal(twiss_getters(t), g["getters"])
+    assert t.getGlobalCount() == g["init"].shape[1]
+    # tune analysis over the reference's coordinates after each map
+    s = b.getSyncParticle()
+    n = g["init"].shape[1]
+    ph = np.zeros((6, n))
+    O.tune_analysis(g["init"], s.beta(), s.kinEnergy() + s.mass(), g["twiss"], ph)
+    assert np.array_equal(ph, g["phase_0"])
+    k = 1
+    while "coords_%d" % k in g:
+        O.tune_analysis(g["coords_%d" % k], s.beta(), s.kinEnergy() + s.mass(), g["twiss"], ph)
+        assert np.array_equal(ph, g["phase_%d" % k]), k
+        k += 1
+    assert k == 4
+
+
+def test_diag_oracle_macrosize_weights():
+    """With a macrosize attribute the moments are weighted sums."""
+    g = load_golden("diag_twiss_tune")
+    soa = g["init"]
+    w = np.linspace(0.5, 1.5, soa.shape[1])
+    mom = O.twiss_moments(soa, w)
+    assert mom[1] == pytest.approx(w.sum(), rel=1e-14)
+    # the centroids are small against the coordinates: scale by <|c_i|>
+    scale = (np.abs(soa) * w).sum(axis=1) / w.sum()
+    assert np.all(np.abs(mom[2:8] - (soa * w).sum(axis=1) / w.sum()) <= 1e-13 * scale)
