@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--n", type=int, default=N_PARTICLES)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--error-turns", type=int, default=100,
+                    help="turns of the rms-emittance and tune-shift error report of a non-plain form")
     return ap.parse_args()
 
 
@@ -363,6 +365,19 @@ def run_ours(args):
     # how often the Poisson solver grid was reshaped (Green spectrum rebuilt)
     kicks_done, green_done = calc._calc.counters()
     green_rate = green_done / kicks_done if kicks_done else None
+    form_err = None
+    if args.form != "plain" and args.error_turns > 0:
+        # accuracy of the reduced-precision form against the FP64 plain form
+        # on the same bunch (outside the timed region)
+        from orbit_gb300 import workloads as W
+        from orbit_gb300.form_report import form_error
+        from spacecharge import SpaceChargeCalc2p5D
+
+        def make_lattice(form):
+            with quiet():
+                return W.fodo_lattice(None if form is None else SpaceChargeCalc2p5D(*GRID, form=form), cells=CELLS)
+
+        form_err = form_error(soa, bunch.macroSize(), make_lattice, args.form, turns=args.error_turns)
     cpu = None
     if not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -383,6 +398,8 @@ def run_ours(args):
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
         "gpu_launches": launches_per_turn * args.steps, "wall_s": wall,
     }
+    if form_err is not None:
+        line["form_error_vs_fp64"] = form_err
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

@@ -90,3 +90,26 @@ def test_fp32_emittance_over_many_kicks():
     assert growth > 1e-4  # space charge acted
     for k in range(2):
         assert abs(e32[k] / e64[k] - 1) < TOL_EMITTANCE_FP32, (k, e32, e64)
+
+
+def test_fp32_tune_shift_and_emittance_error_report():
+    """The error report of the FP32 form at the FODO benchmark's intensity
+    (1e14 protons): the beam's mean space-charge tune shift and its tune
+    spread (device tune analysis over the turns) within 1% of the FP64
+    form's mean shift, rms emittances within 1%."""
+    from orbit_gb300 import workloads as W
+    from orbit_gb300.form_report import form_error
+    from spacecharge import SpaceChargeCalc2p5D
+    soa = W.c2_coords(100_000, seed=21)
+
+    def make_lattice(form):
+        return W.fodo_lattice(None if form is None else SpaceChargeCalc2p5D(64, 64, 32, form=form), cells=10)
+
+    r = form_error(soa, 1e9, make_lattice, "fp32", turns=30)
+    for k in range(2):
+        assert 0.0 <= r["bare_tune"][k] < 1.0
+        shift = abs(r["tune_shift_fp64_mean"][k])
+        assert r["tune_shift_fp64_mean"][k] < -1e-4  # space charge depresses the tunes
+        assert r["tune_shift_mean_err"][k] < 0.01 * shift, r
+        assert r["tune_spread_err"][k] < 0.01 * shift, r
+        assert r["emittance_rel_err"][k] < TOL_EMITTANCE_FP32, r
