@@ -51,7 +51,7 @@ __global__ void __launch_bounds__(kMomThreads) k_moments(const double* __restric
     for (int w = 0; w < kMomThreads / 32; ++w) t += red[w][threadIdx.x];
     part[(size_t)blockIdx.x * kNMom + threadIdx.x] = t;
   }
-  if (last_block_done(counter) && threadIdx.x < kNMom) {
+  if (last_block_done(counter, gridDim.x) && threadIdx.x < kNMom) {
     double t = 0.0;
     for (int bk = 0; bk < (int)gridDim.x; ++bk) t += __ldcg(part + (size_t)bk * kNMom + threadIdx.x);
     out[threadIdx.x] = t;

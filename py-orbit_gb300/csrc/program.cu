@@ -15,26 +15,23 @@
 #include "sc2p5d.cuh"
 #include "sc_device.cuh"
 #include "teapot.cuh"
+#include "batch.cuh"
+#include "program.cuh"
 
 namespace orbit {
 
-int check_status(orbit_bunch_t* b);
-
 static const int kPassSmem = 220 * 1024;
 
-// Per-particle 1/(1+dp_p) kept between the passes of one program run
-// (it changes only with dE): km & KNL_STORE writes it at the end of the
-// pass, km & KNL_LOAD reads it instead of dividing.
-enum { KNL_LOAD = 1, KNL_STORE = 2 };
-
 // KF: 0 no kick, 1 plain kick, 2 fp32 kick.  EXT: accumulate extrema.
+// Blocks blk = 0..nblk-1 share the bunch's particles.
 template <int KF, bool EXT, bool KSMEM>
-__global__ void __launch_bounds__(512) k_pass(double* __restrict__ cx, double* __restrict__ cxp,
-                                              double* __restrict__ cy, double* __restrict__ cyp,
-                                              double* __restrict__ cz, double* __restrict__ cdE, int n,
-                                              const DevOp* __restrict__ ops, int a, int b, MapCtx m,
-                                              KickArgs kick, ScState* ext_st, unsigned* status, SetupArgs sa,
-                                              double* __restrict__ knl_buf, int km) {
+__device__ __forceinline__ void pass_body(double* __restrict__ cx, double* __restrict__ cxp,
+                                          double* __restrict__ cy, double* __restrict__ cyp,
+                                          double* __restrict__ cz, double* __restrict__ cdE, int n,
+                                          const DevOp* __restrict__ ops, int a, int b, const MapCtx& m,
+                                          const KickArgs& kick, ScState* ext_st, unsigned* status,
+                                          const SetupArgs& sa, double* __restrict__ knl_buf, int km, int blk,
+                                          int nblk) {
   KickConst k;
   KickFix kf;
   const long long* P = kick.phi_fix;
@@ -66,7 +63,7 @@ __global__ void __launch_bounds__(512) k_pass(double* __restrict__ cx, double* _
   }
   ExtAcc acc;
   if (EXT) acc.init();
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  for (int i = blk * blockDim.x + threadIdx.x; i < n; i += nblk * blockDim.x) {
     Part p;
     p.x = cx[i]; p.xp = cxp[i]; p.y = cy[i]; p.yp = cyp[i]; p.z = cz[i]; p.dE = cdE[i];
     p.knl_ok = false;
@@ -94,7 +91,28 @@ __global__ void __launch_bounds__(512) k_pass(double* __restrict__ cx, double* _
     cx[i] = p.x; cxp[i] = p.xp; cy[i] = p.y; cyp[i] = p.yp; cz[i] = p.z; cdE[i] = p.dE;
   }
   // the last block sets up the grids of the next kick
-  if (EXT) ext_commit_and_setup(acc, ext_st, status, sa);
+  if (EXT) ext_commit_and_setup(acc, ext_st, status, sa, nblk);
+}
+
+template <int KF, bool EXT, bool KSMEM>
+__global__ void __launch_bounds__(512) k_pass(double* __restrict__ cx, double* __restrict__ cxp,
+                                              double* __restrict__ cy, double* __restrict__ cyp,
+                                              double* __restrict__ cz, double* __restrict__ cdE, int n,
+                                              const DevOp* __restrict__ ops, int a, int b, MapCtx m,
+                                              KickArgs kick, ScState* ext_st, unsigned* status, SetupArgs sa,
+                                              double* __restrict__ knl_buf, int km) {
+  pass_body<KF, EXT, KSMEM>(cx, cxp, cy, cyp, cz, cdE, n, ops, a, b, m, kick, ext_st, status, sa, knl_buf, km,
+                            blockIdx.x, gridDim.x);
+}
+
+// The same pass for the members of a batch class; each block finds its
+// member in the block table.
+template <int KF, bool EXT, bool KSMEM>
+__global__ void __launch_bounds__(512) kb_pass(const PassJob* __restrict__ jobs,
+                                               const unsigned short* __restrict__ blk_job, int a, int b, int km) {
+  const PassJob& J = jobs[blk_job[blockIdx.x]];
+  pass_body<KF, EXT, KSMEM>(J.c[0], J.c[1], J.c[2], J.c[3], J.c[4], J.c[5], J.n, J.ops, a, b, J.m, J.ka, J.ext,
+                            J.status, J.sa, J.knl, km, blockIdx.x - J.blk0, J.nblk);
 }
 
 // Shared-memory limits are raised once, outside any stream capture.
@@ -105,6 +123,8 @@ static int init_pass_attrs() {
   ORBIT_CUDA(cudaFuncSetAttribute(k_pass<1, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kPassSmem));
   ORBIT_CUDA(cudaFuncSetAttribute(k_pass<2, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kPassSmem));
   ORBIT_CUDA(cudaFuncSetAttribute(k_pass<2, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kPassSmem));
+  ORBIT_CUDA(cudaFuncSetAttribute(kb_pass<1, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kPassSmem));
+  ORBIT_CUDA(cudaFuncSetAttribute(kb_pass<1, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kPassSmem));
   done = true;
   return ORBIT_OK;
 }
@@ -129,46 +149,33 @@ static int launch_pass(orbit_bunch_t* bu, cudaStream_t s, size_t smem, const Dev
   return ORBIT_OK;
 }
 
+size_t batch_pass_smem_limit() { return kPassSmem; }
+
+int batch_enqueue_pass(const PassJob* jobs, const unsigned short* blk_job, int nblk, int threads, int kf, bool ext,
+                       bool ksmem, size_t smem, int a, int b, int km, cudaStream_t s) {
+  int arc = init_pass_attrs();
+  if (arc) return arc;
+  ORBIT_PB(kf == 0 ? "batch_pass_maps" : "batch_pass_kick_maps", s);
+  if (kf == 0) {
+    if (ext) kb_pass<0, true, false><<<nblk, threads, 0, s>>>(jobs, blk_job, a, b, km);
+    else kb_pass<0, false, false><<<nblk, threads, 0, s>>>(jobs, blk_job, a, b, km);
+  } else if (ksmem) {
+    if (ext) kb_pass<1, true, true><<<nblk, threads, smem, s>>>(jobs, blk_job, a, b, km);
+    else kb_pass<1, false, true><<<nblk, threads, smem, s>>>(jobs, blk_job, a, b, km);
+  } else {
+    if (ext) kb_pass<1, true, false><<<nblk, threads, 0, s>>>(jobs, blk_job, a, b, km);
+    else kb_pass<1, false, false><<<nblk, threads, 0, s>>>(jobs, blk_job, a, b, km);
+  }
+  ORBIT_PE(s);
+  ORBIT_LAUNCH_CHECK("batch pass");
+  return ORBIT_OK;
+}
+
 }  // namespace orbit
 
 using namespace orbit;
 
-struct orbit_program {
-  std::vector<orbit_op_t> ops;
-  std::vector<orbit_sc2p5d_t*> calcs;
-  std::vector<orbit_boundary_t*> bnds;   // SC ops with i1 = 1 + index
-  // compiled for one bunch configuration
-  orbit_bunch_t* key_bunch = nullptr;
-  int key_n = -1;
-  double* key_coords = nullptr;
-  orbit_sync_t key_sync{};
-  int key_msize = -1;
-  DevOp* d_ops = nullptr;
-  int n_devops = 0;
-  double* d_knl = nullptr;            // per-particle 1/(1+dp_p) between passes
-  size_t knl_n = 0;
-  cudaGraphExec_t g_first = nullptr;  // prologue + turn ending with the wrap pass
-  cudaGraphExec_t g_mid = nullptr;    // turn ending with the wrap pass
-  cudaGraphExec_t g_last = nullptr;   // turn ending without the wrap
-  cudaGraphExec_t g_single = nullptr; // prologue + turn without wrap (one-turn runs)
-  std::vector<double> time_adv;       // per-op SyncPart time increments
-  int launches_per_turn = 0;
-  cudaEvent_t done = nullptr;         // recorded after the last enqueued run
-  bool used = false;
-};
-
 namespace orbit {
-
-struct Seg {
-  int a, b;
-  bool dE;  // an op of the segment changes dE (kick with dE, wedgerotate)
-};
-
-struct Plan {
-  std::vector<Seg> segs;      // m+1 map segments in the device op array
-  std::vector<int> sc_idx;    // op index of each SC op
-  Seg wrap;                   // M_m ++ M_0 in the device op array
-};
 
 static void free_graphs(orbit_program_t* p) {
   cudaGraphExec_t* gs[] = {&p->g_first, &p->g_mid, &p->g_last, &p->g_single};
@@ -181,7 +188,7 @@ static bool sync_equal(const orbit_sync_t& a, const orbit_sync_t& b) {
          a.classical_radius == b.classical_radius && a.macrosize == b.macrosize && a.mass == b.mass;
 }
 
-static KickArgs kick_args(orbit_sc2p5d_t* c, const orbit_sync_t& s, double length, const orbit_boundary* bnd) {
+KickArgs kick_args(orbit_sc2p5d_t* c, const orbit_sync_t& s, double length, const orbit_boundary* bnd) {
   KickArgs ka;
   ka.st = c->d_st;
   ka.phi = c->d_phi;
@@ -245,7 +252,7 @@ static int enqueue_pass(orbit_bunch_t* bu, cudaStream_t s, const DevOp* ops, Seg
 
 // Builds the device op array: all non-SC ops of the turn in order, then the
 // wrap segment (last segment followed by the first).
-static int compile(orbit_program_t* p, orbit_bunch_t* bu, Plan& plan) {
+int compile(orbit_program_t* p, orbit_bunch_t* bu, Plan& plan) {
   std::vector<DevOp> dev;
   p->time_adv.assign(p->ops.size(), 0.0);
   int start = 0;

@@ -10,6 +10,7 @@
 #include "fft.cuh"
 #include "sc2p5d.cuh"
 #include "sc_device.cuh"
+#include "batch.cuh"
 
 namespace orbit {
 
@@ -46,7 +47,7 @@ __global__ void k_extrema(const double* __restrict__ x, const double* __restrict
   ExtAcc a;
   a.init();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) a.add(x[i], y[i], z[i]);
-  ext_commit_and_setup(a, st, status, sa);
+  ext_commit_and_setup(a, st, status, sa, gridDim.x);
 }
 
 // Green function of the doubled grid (PoissonSolverFFT2D.cc:115-152): the
@@ -54,13 +55,14 @@ __global__ void k_extrema(const double* __restrict__ x, const double* __restrict
 // its mirror images, as the reference copies it.  gate: run only when the
 // Green spectrum is marked dirty (0 inside a graph branch taken on that
 // flag).
-__global__ void k_green_fill(const ScState* st, double* g, int nx2, int ny2, int gate) {
+__device__ __forceinline__ void green_fill_body(const ScState* st, double* g, int nx2, int ny2, int gate, int blk,
+                                                int nblk) {
   if ((gate && !st->green_dirty) || st->skip) return;
   double sdx = st->sdx, sdy = st->sdy;
   const int hx = nx2 / 2, hy = ny2 / 2;
   const int qy = hy + 1;
   int tot = (hx + 1) * qy;
-  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < tot; idx += gridDim.x * blockDim.x) {
+  for (int idx = blk * blockDim.x + threadIdx.x; idx < tot; idx += nblk * blockDim.x) {
     int iX = idx / qy, iY = idx % qy;
     double v = 0.0;
     if (iX != 0 || iY != 0) {
@@ -76,6 +78,10 @@ __global__ void k_green_fill(const ScState* st, double* g, int nx2, int ny2, int
       if (iY > 0 && mY != iY) g[(size_t)mX * ny2 + mY] = v;
     }
   }
+}
+
+__global__ void k_green_fill(const ScState* st, double* g, int nx2, int ny2, int gate) {
+  green_fill_body(st, g, nx2, ny2, gate, blockIdx.x, gridDim.x);
 }
 
 // Line density to doubles, total macrosize and the Green-rebuild flag
@@ -148,13 +154,14 @@ __device__ __noinline__ void finalize_block(ScState* st, G* zacc, int nz, double
 // deposit, and one extra block (the last) finalizes the line density.
 // gate (SRC 0): as for k_green_fill.
 template <typename T, int SRC>
-__global__ void k_rows_fwd(ScState* st, void* src, double* rho_out, typename CT<T>::t* hat,
-                           const typename CT<T>::t* __restrict__ tw, FftPlan pl, int nrows, int ncols, int H,
-                           int gate, void* zacc, int nz, double* lam, float* lam_f) {
+__device__ __forceinline__ void rows_fwd_body(ScState* st, void* src, double* rho_out, typename CT<T>::t* hat,
+                                              const typename CT<T>::t* __restrict__ tw, const FftPlan& pl,
+                                              int nrows, int ncols, int H, int gate, void* zacc, int nz,
+                                              double* lam, float* lam_f, int blk, int nblk) {
   typedef typename CT<T>::t C;
   if (SRC == 0 && gate && !st->green_dirty) return;
   if (st->skip) return;
-  if (SRC != 0 && blockIdx.x == gridDim.x - 1) {
+  if (SRC != 0 && blk == nblk - 1) {
     if (SRC == 1) finalize_block(st, (unsigned long long*)zacc, nz, lam, (float*)nullptr);
     else finalize_block(st, (float*)zacc, nz, lam, lam_f);
     return;
@@ -165,7 +172,7 @@ __global__ void k_rows_fwd(ScState* st, void* src, double* rho_out, typename CT<
   const int N = pl.n;
   C* stw = b + N;
   load_twiddles(stw, tw, N);
-  int r0 = 2 * blockIdx.x, r1 = r0 + 1;
+  int r0 = 2 * blk, r1 = r0 + 1;
   double iq = st->inv_qscale;
   for (int j = threadIdx.x; j < N; j += blockDim.x) {
     T va = (T)0, vb = (T)0;
@@ -226,6 +233,14 @@ __global__ void k_rows_fwd(ScState* st, void* src, double* rho_out, typename CT<
   }
 }
 
+template <typename T, int SRC>
+__global__ void k_rows_fwd(ScState* st, void* src, double* rho_out, typename CT<T>::t* hat,
+                           const typename CT<T>::t* __restrict__ tw, FftPlan pl, int nrows, int ncols, int H,
+                           int gate, void* zacc, int nz, double* lam, float* lam_f) {
+  rows_fwd_body<T, SRC>(st, src, rho_out, hat, tw, pl, nrows, ncols, H, gate, zacc, nz, lam, lam_f, blockIdx.x,
+                        gridDim.x);
+}
+
 // Column transforms along x (length N = nx2), one column k per block.
 // The Green spectrum is stored column by column (green[k * N + r]).
 // MODE 0: forward transform of the Green columns (when dirty), hat -> green.
@@ -233,8 +248,9 @@ __global__ void k_rows_fwd(ScState* st, void* src, double* rho_out, typename CT<
 //         correction (PoissonSolverFFT2D.cc:212-242), backward; rows >= nin
 //         are zero on input and only rows < nin are kept on output.
 template <typename T, int MODE>
-__global__ void k_cols(ScState* st, typename CT<T>::t* hat, typename CT<T>::t* __restrict__ green,
-                       const typename CT<T>::t* __restrict__ tw, FftPlan pl, int nin, int H, int ny2, int gate) {
+__device__ __forceinline__ void cols_body(ScState* st, typename CT<T>::t* hat, typename CT<T>::t* __restrict__ green,
+                                          const typename CT<T>::t* __restrict__ tw, const FftPlan& pl, int nin,
+                                          int H, int ny2, int gate, int k) {
   typedef typename CT<T>::t C;
   if (MODE == 0 && gate && !st->green_dirty) return;
   if (st->skip) return;
@@ -244,7 +260,6 @@ __global__ void k_cols(ScState* st, typename CT<T>::t* hat, typename CT<T>::t* _
   const int N = pl.n;
   C* stw = b + N;
   load_twiddles(stw, tw, N);
-  const int k = blockIdx.x;
   for (int r = threadIdx.x; r < N; r += blockDim.x) {
     C v;
     if (r < nin) v = hat[(size_t)r * H + k];
@@ -280,13 +295,20 @@ __global__ void k_cols(ScState* st, typename CT<T>::t* hat, typename CT<T>::t* _
   for (int r = threadIdx.x; r < nin; r += blockDim.x) hat[(size_t)r * H + k] = R[r];
 }
 
+template <typename T, int MODE>
+__global__ void k_cols(ScState* st, typename CT<T>::t* hat, typename CT<T>::t* __restrict__ green,
+                       const typename CT<T>::t* __restrict__ tw, FftPlan pl, int nin, int H, int ny2, int gate) {
+  cols_body<T, MODE>(st, hat, green, tw, pl, nin, H, ny2, gate, blockIdx.x);
+}
+
 // Backward row transforms (c2r, two rows per block) and the 1/(4 nx ny)
 // normalisation onto the nx x ny potential (PoissonSolverFFT2D.cc:244-255).
 // Imaginary parts at the self-conjugate k = 0 and k = N/2 are ignored.
 template <typename T>
-__global__ void k_rows_inv(ScState* st, const typename CT<T>::t* __restrict__ hat,
-                           const typename CT<T>::t* __restrict__ tw, FftPlan pl, int nrows, int ny, int H,
-                           double denom, double* phi, float* phi_f) {
+__device__ __forceinline__ void rows_inv_body(ScState* st, const typename CT<T>::t* __restrict__ hat,
+                                              const typename CT<T>::t* __restrict__ tw, const FftPlan& pl,
+                                              int nrows, int ny, int H, double denom, double* phi, float* phi_f,
+                                              int blk) {
   typedef typename CT<T>::t C;
   if (st->skip) return;
   extern __shared__ unsigned char smem_raw[];
@@ -295,7 +317,7 @@ __global__ void k_rows_inv(ScState* st, const typename CT<T>::t* __restrict__ ha
   const int N = pl.n;
   C* stw = b + N;
   load_twiddles(stw, tw, N);
-  int r0 = 2 * blockIdx.x, r1 = r0 + 1;
+  int r0 = 2 * blk, r1 = r0 + 1;
   bool has1 = r1 < nrows;
   for (int k = threadIdx.x; k < N; k += blockDim.x) {
     C A, B;
@@ -336,16 +358,29 @@ __global__ void k_rows_inv(ScState* st, const typename CT<T>::t* __restrict__ ha
   if ((threadIdx.x & 31) == 0 && amax) atomicMax(&st->phi_absmax, amax);
 }
 
+template <typename T>
+__global__ void k_rows_inv(ScState* st, const typename CT<T>::t* __restrict__ hat,
+                           const typename CT<T>::t* __restrict__ tw, FftPlan pl, int nrows, int ny, int H,
+                           double denom, double* phi, float* phi_f) {
+  rows_inv_body<T>(st, hat, tw, pl, nrows, ny, H, denom, phi, phi_f, blockIdx.x);
+}
+
 // Plain form: phi and lambda as 64-bit integers phi * 2^sphi, lambda *
 // 2^slam with the scales chosen from their maxima (below 2^61), read by the
 // fixed-point kick.
-__global__ void k_phi_fix(const ScState* st, const double* __restrict__ phi, const double* __restrict__ lam,
-                          long long* phi_fix, long long* lam_fix, int ng, int nz) {
+__device__ __forceinline__ void phi_fix_body(const ScState* st, const double* __restrict__ phi,
+                                             const double* __restrict__ lam, long long* phi_fix, long long* lam_fix,
+                                             int ng, int nz, int blk) {
   if (st->skip) return;
   int sphi = scale_bits(st->phi_absmax), slam = scale_bits(st->lam_absmax);
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blk * blockDim.x + threadIdx.x;
   if (i < ng) phi_fix[i] = phi_fixed(phi[i], sphi);
   if (i < nz) lam_fix[i] = phi_fixed(lam[i], slam);
+}
+
+__global__ void k_phi_fix(const ScState* st, const double* __restrict__ phi, const double* __restrict__ lam,
+                          long long* phi_fix, long long* lam_fix, int ng, int nz) {
+  phi_fix_body(st, phi, lam, phi_fix, lam_fix, ng, nz, blockIdx.x);
 }
 
 // 2.5Drb: one cell of the smoothed line-density derivative
@@ -471,10 +506,11 @@ __global__ void k_rb_analysis(ScState* st, const double* __restrict__ rho, const
 // latency of the shared-memory atomics; 1024 threads at 64 registers spill
 // and ran slower.
 template <bool SMEM>
-__global__ void __launch_bounds__(768) k_deposit_plain(const double* __restrict__ x, const double* __restrict__ y,
-                                const double* __restrict__ z, const double* __restrict__ msize, int n,
-                                const ScState* st, unsigned long long* g_rho, unsigned long long* g_z,
-                                double ms_uniform, double qscale, int nx, int ny, int nz, int K) {
+__device__ __forceinline__ void deposit_plain_body(const double* __restrict__ x, const double* __restrict__ y,
+                                                   const double* __restrict__ z, const double* __restrict__ msize,
+                                                   int n, const ScState* st, unsigned long long* g_rho,
+                                                   unsigned long long* g_z, double ms_uniform, double qscale, int nx,
+                                                   int ny, int nz, int K, int blk, int nblk) {
   DepConst d;
   load_dep_const(d, st, nx, ny, nz);
   if (d.skip) return;
@@ -495,7 +531,7 @@ __global__ void __launch_bounds__(768) k_deposit_plain(const double* __restrict_
     rho.p = g_rho;
     zg.p = g_z;
   }
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  for (int i = blk * blockDim.x + threadIdx.x; i < n; i += nblk * blockDim.x) {
     double xi = x[i], yi = y[i], zi = z[i];
     if (K > 0 && deposit_fixed<SMEM>(df, rho, zg, xi, yi, zi)) continue;
     double ms = msize ? msize[i] * qscale : ms_uniform;
@@ -508,6 +544,15 @@ __global__ void __launch_bounds__(768) k_deposit_plain(const double* __restrict_
       if (v) atomicAdd(i < nx * ny ? g_rho + i : g_z + (i - nx * ny), v);
     }
   }
+}
+
+template <bool SMEM>
+__global__ void __launch_bounds__(768) k_deposit_plain(const double* __restrict__ x, const double* __restrict__ y,
+                                const double* __restrict__ z, const double* __restrict__ msize, int n,
+                                const ScState* st, unsigned long long* g_rho, unsigned long long* g_z,
+                                double ms_uniform, double qscale, int nx, int ny, int nz, int K) {
+  deposit_plain_body<SMEM>(x, y, z, msize, n, st, g_rho, g_z, ms_uniform, qscale, nx, ny, nz, K, blockIdx.x,
+                           gridDim.x);
 }
 
 template <bool SMEM>
@@ -650,6 +695,52 @@ __global__ void k_fields(const ScState* st, const double* __restrict__ phi, cons
     l = (nz > 1) ? (w0 * lam[i0] + wp * lam[ip]) : lam[0];
   }
   lv[i] = l;
+}
+
+// ---------------------------------------------------------------------
+// batched kernels (plain form): the members of one grid class in one
+// launch; grid kernels take the member from blockIdx.y, particle kernels
+// from the block table
+// ---------------------------------------------------------------------
+__global__ void kb_green_fill(const SolveJob* __restrict__ jobs, int nx2, int ny2) {
+  const SolveJob& J = jobs[blockIdx.y];
+  green_fill_body(J.st, J.gbuf, nx2, ny2, 1, blockIdx.x, gridDim.x);
+}
+
+template <int SRC>
+__global__ void kb_rows_fwd(const SolveJob* __restrict__ jobs, FftPlan pl, int nrows, int ncols, int H, int nz) {
+  const SolveJob& J = jobs[blockIdx.y];
+  if (SRC == 0)
+    rows_fwd_body<double, 0>(J.st, J.gbuf, nullptr, J.hat, J.tw_y, pl, nrows, ncols, H, 1, nullptr, 0, nullptr,
+                             nullptr, blockIdx.x, gridDim.x);
+  else
+    rows_fwd_body<double, 1>(J.st, J.rho_q, J.rho, J.hat, J.tw_y, pl, nrows, ncols, H, 1, J.z_q, nz, J.lam, nullptr,
+                             blockIdx.x, gridDim.x);
+}
+
+template <int MODE>
+__global__ void kb_cols(const SolveJob* __restrict__ jobs, FftPlan pl, int nin, int H, int ny2) {
+  const SolveJob& J = jobs[blockIdx.y];
+  cols_body<double, MODE>(J.st, J.hat, J.green, J.tw_x, pl, nin, H, ny2, 1, blockIdx.x);
+}
+
+__global__ void kb_rows_inv(const SolveJob* __restrict__ jobs, FftPlan pl, int nrows, int ny, int H, double denom) {
+  const SolveJob& J = jobs[blockIdx.y];
+  rows_inv_body<double>(J.st, J.hat, J.tw_y, pl, nrows, ny, H, denom, J.phi, nullptr, blockIdx.x);
+}
+
+__global__ void kb_phi_fix(const SolveJob* __restrict__ jobs, int ng, int nz) {
+  const SolveJob& J = jobs[blockIdx.y];
+  phi_fix_body(J.st, J.phi, J.lam, J.phi_fix, J.lam_fix, ng, nz, blockIdx.x);
+}
+
+template <bool SMEM>
+__global__ void __launch_bounds__(768) kb_deposit(const DepJob* __restrict__ jobs,
+                                                  const unsigned short* __restrict__ blk_job, int nx, int ny,
+                                                  int nz) {
+  const DepJob& J = jobs[blk_job[blockIdx.x]];
+  deposit_plain_body<SMEM>(J.x, J.y, J.z, J.msize, J.n, J.st, J.g_rho, J.g_z, J.ms_uniform, J.qscale, nx, ny, nz,
+                           J.K, blockIdx.x - J.blk0, J.nblk);
 }
 
 // ---------------------------------------------------------------------
@@ -797,6 +888,96 @@ static int enqueue_green(orbit_sc2p5d_t* c, cudaStream_t s, int gate, void* scra
   ORBIT_PE(s);
   *nl += 3;
   ORBIT_LAUNCH_CHECK("sc2p5d green");
+  return ORBIT_OK;
+}
+
+// FFT block size of a batch class: power-of-two lengths N/2 threads
+// (radix-2 stages) or N/4 (radix-4 stages); other lengths the generic block.
+static int batch_fft_threads(const FftPlan& pl, int wide) {
+  if (!pl.pow2) return fft_threads(pl);
+  int t = wide ? pl.n / 2 : pl.n / 4;
+  if (t < 32) t = 32;
+  if (t > 1024) t = 1024;
+  return t;
+}
+
+bool batch_deposit_smem(const orbit_sc2p5d_t* c) {
+  return 8 * ((size_t)c->nx * c->ny + c->nz) <= (size_t)kMaxSmem;
+}
+
+int batch_init_attrs(const orbit_sc2p5d_t* c) {
+  int bytes = (int)fft_smem<double>(c->nx2 > c->ny2 ? c->nx2 : c->ny2);
+  if (bytes > 48 * 1024) {
+    ORBIT_CUDA(cudaFuncSetAttribute(kb_rows_fwd<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    ORBIT_CUDA(cudaFuncSetAttribute(kb_rows_fwd<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    ORBIT_CUDA(cudaFuncSetAttribute(kb_cols<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    ORBIT_CUDA(cudaFuncSetAttribute(kb_cols<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    ORBIT_CUDA(cudaFuncSetAttribute(kb_rows_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  }
+  size_t dep = 8 * ((size_t)c->nx * c->ny + c->nz);
+  if (dep <= (size_t)kMaxSmem && dep > 48 * 1024)
+    ORBIT_CUDA(cudaFuncSetAttribute(kb_deposit<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem));
+  return ORBIT_OK;
+}
+
+// Green spectra of the members whose solver grid changed (each member's
+// blocks return unless its spectrum is dirty); the work spectra hold the
+// row transforms, before the deposit.
+int batch_enqueue_green(const SolveJob* jobs, int nm, const orbit_sc2p5d_t* c, int fft_wide, cudaStream_t s) {
+  int thx = batch_fft_threads(c->plan_x, fft_wide), thy = batch_fft_threads(c->plan_y, fft_wide);
+  size_t smx = fft_smem<double>(c->nx2), smy = fft_smem<double>(c->ny2);
+  int quad = (c->nx + 1) * (c->ny + 1);
+  int gb = (quad + 255) / 256;
+  if (gb > 64) gb = 64;
+  ORBIT_PB("batch_green_fill", s);
+  kb_green_fill<<<dim3(gb, nm), 256, 0, s>>>(jobs, c->nx2, c->ny2);
+  ORBIT_PE(s);
+  ORBIT_PB("batch_green_rows", s);
+  kb_rows_fwd<0><<<dim3((c->nx + 2) / 2, nm), thy, smy, s>>>(jobs, c->plan_y, c->nx + 1, c->ny2, c->H, 0);
+  ORBIT_PE(s);
+  ORBIT_PB("batch_green_cols", s);
+  kb_cols<0><<<dim3(c->H, nm), thx, smx, s>>>(jobs, c->plan_x, c->nx2, c->H, c->ny2);
+  ORBIT_PE(s);
+  ORBIT_LAUNCH_CHECK("batch green");
+  return ORBIT_OK;
+}
+
+int batch_enqueue_deposit(const DepJob* jobs, const unsigned short* blk_job, int nblk, const orbit_sc2p5d_t* c,
+                          int threads, cudaStream_t s) {
+  size_t sm = 8 * ((size_t)c->nx * c->ny + c->nz);
+  ORBIT_PB("batch_deposit", s);
+  if (batch_deposit_smem(c)) kb_deposit<true><<<nblk, threads, sm, s>>>(jobs, blk_job, c->nx, c->ny, c->nz);
+  else kb_deposit<false><<<nblk, threads, 0, s>>>(jobs, blk_job, c->nx, c->ny, c->nz);
+  ORBIT_PE(s);
+  ORBIT_LAUNCH_CHECK("batch deposit");
+  return ORBIT_OK;
+}
+
+// Forward rows (+ line-density finalize), columns with the Green multiply,
+// backward rows, and the fixed-point potential for kicks that read it from
+// global memory.
+int batch_enqueue_solve(const SolveJob* jobs, int nm, const orbit_sc2p5d_t* c, int fft_wide, bool phi_fix,
+                        cudaStream_t s) {
+  int thx = batch_fft_threads(c->plan_x, fft_wide), thy = batch_fft_threads(c->plan_y, fft_wide);
+  size_t smx = fft_smem<double>(c->nx2), smy = fft_smem<double>(c->ny2);
+  ORBIT_PB("batch_rows_fwd", s);
+  kb_rows_fwd<1><<<dim3((c->nx + 1) / 2 + 1, nm), thy, smy, s>>>(jobs, c->plan_y, c->nx, c->ny, c->H, c->nz);
+  ORBIT_PE(s);
+  ORBIT_PB("batch_cols_conv", s);
+  kb_cols<1><<<dim3(c->H, nm), thx, smx, s>>>(jobs, c->plan_x, c->nx, c->H, c->ny2);
+  ORBIT_PE(s);
+  ORBIT_PB("batch_rows_inv", s);
+  kb_rows_inv<<<dim3((c->nx + 1) / 2, nm), thy, smy, s>>>(jobs, c->plan_y, c->nx, c->ny, c->H,
+                                                          1.0 / (c->nx2 * c->ny2));
+  ORBIT_PE(s);
+  if (phi_fix) {
+    int ng = c->nx * c->ny;
+    int m = ng > c->nz ? ng : c->nz;
+    ORBIT_PB("batch_phi_fix", s);
+    kb_phi_fix<<<dim3((m + 255) / 256, nm), 256, 0, s>>>(jobs, ng, c->nz);
+    ORBIT_PE(s);
+  }
+  ORBIT_LAUNCH_CHECK("batch solve");
   return ORBIT_OK;
 }
 

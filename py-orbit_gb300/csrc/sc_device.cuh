@@ -156,16 +156,17 @@ static __device__ __noinline__ void sc_setup_scalar(ScState* st, unsigned* statu
   st->skip = skip;
 }
 
-// True in exactly one block of the grid: the last to call it.  Every
-// thread's earlier global writes and atomics are fenced before the block
-// is counted; `counter` is left at zero for the next launch.
-__device__ __forceinline__ bool last_block_done(unsigned* counter) {
+// True in exactly one of the nblk blocks that share `counter` (all blocks
+// of the grid, or of one bunch of a batched launch): the last to call it.
+// Every thread's earlier global writes and atomics are fenced before the
+// block is counted; `counter` is left at zero for the next launch.
+__device__ __forceinline__ bool last_block_done(unsigned* counter, unsigned nblk) {
   __shared__ int s_last;
   __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) {
     unsigned prev = atomicAdd(counter, 1u);
-    s_last = prev == gridDim.x - 1;
+    s_last = prev == nblk - 1;
     if (s_last) {
       *counter = 0u;
       __threadfence();
@@ -175,11 +176,12 @@ __device__ __forceinline__ bool last_block_done(unsigned* counter) {
   return s_last != 0;
 }
 
-// Extrema commit followed, in the last block, by the grid set-up.
+// Extrema commit followed, in the last of the nblk blocks scanning this
+// bunch, by the grid set-up.
 __device__ __forceinline__ void ext_commit_and_setup(ExtAcc& a, ScState* st, unsigned* status,
-                                                     const SetupArgs& sa) {
+                                                     const SetupArgs& sa, unsigned nblk) {
   ext_block_commit(a, st, status);
-  if (last_block_done(&st->ext_count) && threadIdx.x == 0) sc_setup_scalar(st, status, sa);
+  if (last_block_done(&st->ext_count, nblk) && threadIdx.x == 0) sc_setup_scalar(st, status, sa);
 }
 
 // ---------------------------------------------------------------------
