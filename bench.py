@@ -55,6 +55,9 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--error-turns", type=int, default=100,
                     help="turns of the rms-emittance and tune-shift error report of a non-plain form")
+    ap.add_argument("--workload", default="fodo", choices=["fodo", "batched"],
+                    help="fodo: one 1e6-particle bunch (default); batched: the 64-bunch scan")
+    ap.add_argument("--members", type=int, default=64, help="bunches of the batched scan")
     return ap.parse_args()
 
 
@@ -422,10 +425,137 @@ class _Traffic(dict):
 TRAFFIC = _Traffic()
 
 
+def build_scan(members, cells=CELLS):
+    """The batched scan: [(soa, bunch, lattice)] per member."""
+    from orbit_gb300 import workloads as W
+    from spacecharge import SpaceChargeCalc2p5D
+    out = []
+    for k, (n, grid, k1, intensity) in enumerate(W.c3_scan(members)):
+        soa = W.c3_coords(n, seed=7000 + k)
+        b = W.make_bunch(soa, intensity / n)
+        with quiet():
+            lat = W.fodo_lattice(SpaceChargeCalc2p5D(*grid), cells=cells, kq=k1)
+        out.append((soa, b, lat))
+    return out
+
+
+def run_batched(args):
+    """The 64-bunch scan: one step = one turn of every bunch through its
+    own 40-cell FODO lattice, all bunches in one batch (orbit_batch_*)."""
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.init()
+    from orbit_gb300.batch import BunchBatch
+    scan = build_scan(args.members)
+    bb = BunchBatch([(b, lat) for _, b, lat in scan])
+    n_tot = sum(soa.shape[1] for soa, _, _ in scan)
+    bb.trackTurns(max(args.warmup, 1))  # the first turn autotunes, the rest replays the graphs
+    kicks_per_turn = sum(1 for o in scan[0][2].fusedProgram(scan[0][1]).ops if o[0] == 32)
+    stream = torch.cuda.ExternalStream(bb._batch.stream_ptr())
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    clocks = ClockSampler(local)
+    torch.cuda.synchronize()
+    bb.sync()
+    clocks.start()
+    step_ms = []
+    wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        bb.enqueueTurns(1)
+        e1.record(stream)
+        bb.sync()
+        step_ms.append(e0.elapsed_time(e1))
+    wall = time.perf_counter() - wall0
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    total_ms = sum(step_ms)
+    value = n_tot * kicks_per_turn * args.steps / (total_ms * 1e-3)
+    # the same bunches tracked one program each (each bunch on its own
+    # stream, so the programs overlap as far as the GPU lets them)
+    t0 = time.perf_counter()
+    unb_turns = 2
+    for _ in range(unb_turns):
+        for _, b, lat in scan:
+            lat.fusedProgram(b).device.enqueue(b._device_bunch(), 1)
+            b._device_modified()
+        for _, b, _ in scan:
+            b._device_bunch().sync()
+    unb_ms = (time.perf_counter() - t0) * 1e3 / unb_turns
+    # end to end: upload every bunch from pinned host memory, one turn,
+    # download every bunch
+    e2e = None
+    if not args.no_e2e:
+        pins = []
+        for soa, b, _ in scan:
+            pi = torch.empty(soa.shape, dtype=torch.float64, pin_memory=True).numpy()
+            po = torch.empty(soa.shape, dtype=torch.float64, pin_memory=True).numpy()
+            pi[...] = soa
+            pins.append((pi, po))
+        e2e_ms = []
+        for i in range(min(args.steps, 3) + 1):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for (pi, _), (_, b, _) in zip(pins, scan):
+                b.setCoordinates(pi, copy=False)
+            bb.trackTurns(1)
+            for (_, po), (_, b, _) in zip(pins, scan):
+                b.getCoordinates(out=po)
+            t1 = time.perf_counter()
+            if i > 0:  # the first call re-records the programs and recaptures the graphs
+                e2e_ms.append((t1 - t0) * 1e3)
+        tot = sum(e2e_ms)
+        e2e = {"value": n_tot * kicks_per_turn * len(e2e_ms) / (tot * 1e-3), "unit": "macroparticle-kicks/s",
+               "h2d_bytes_per_step": int(sum(p[0].nbytes for p in pins)),
+               "d2h_bytes_per_step": int(sum(p[1].nbytes for p in pins)), "ms_per_step": tot / len(e2e_ms)}
+    prof = bb.profile()
+    hbm_peak, peak_kind = measured_peaks()
+    turn_ms = sum(v[0] for v in prof.values())
+    name, (dom_ms, dom_launches) = max(prof.items(), key=lambda kv: kv[1][0])
+    alg = {"batch_pass_kick_maps": 96.0, "batch_deposit": 24.0}.get(name)
+    # every launch of a kind processes one class; over the turn the kind
+    # processed all particles once per kick
+    achieved = alg * n_tot * kicks_per_turn / (dom_ms * 1e-3) / 1e9 if alg else None
+    roofline = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak if achieved else None, "traffic": None,
+                "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_kind if peak_kind == "measured"
+                else "fallback 6.8 TB/s",
+                "share_of_turn": dom_ms / turn_ms,
+                "kernels": {k: {"ms": v[0], "launches": v[1], "share": v[0] / turn_ms} for k, v in prof.items()}}
+    cpu = None
+    if not args.no_cpu:
+        threads = os.cpu_count() or 1
+        rate, per_turn, kpt = cpu_reference_rate(CPU_SAMPLE_N, 1, 0, threads)
+        cpu = {"value": rate, "unit": "macroparticle-kicks/s", "cores": threads, "kind": "port",
+               "sample": "%d particles x 1 turn of the 128x128x64 FODO lattice (%d SC kicks), %d threads"
+                         % (CPU_SAMPLE_N, kpt, threads)}
+    classes = bb.classes()
+    line = {
+        "metric": METRIC, "value": value, "unit": "macroparticle-kicks/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Gaussian 6D bunches of the scan)",
+        "config": {"workload": "batched scan: %d bunches, %d particles in all (log-uniform 5e4-2e6), "
+                               "intensity 1e12-2e14, k1 0.3-0.7, grids 64x64x32/128x128x64/256x256x64, "
+                               "40-cell FODO x 4 SC nodes, one turn per step" % (len(scan), n_tot),
+                   "particles": n_tot, "members": len(scan), "kicks_per_step": kicks_per_turn,
+                   "classes": classes, "l2": "flushed (512 MiB write) before each timed step; inputs > L2",
+                   "unbatched_ms_per_turn": unb_ms, "parallelism": "single"},
+        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+        "gpu_launches": bb.launchesPerTurn() * args.steps, "wall_s": wall,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batched":
+        run_batched(args)
     else:
         run_ours(args)
 

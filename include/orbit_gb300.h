@@ -297,6 +297,44 @@ int orbit_program_launches(const orbit_program_t* p, int* launches);
 int orbit_program_profile(orbit_program_t* p, orbit_bunch_t* b, int max_kinds, char* names, double* total_ms,
                           int* launches, int* nkinds);
 
+/* ---- batched tracking of many bunches (scans) ----
+ * No single counterpart in the reference: a scan there is a Python loop
+ * over bunches, each tracked by its own lattice (AccLattice.trackBunch,
+ * py/orbit/lattice/AccLattice.py:243-255).  Here member i is programs[i]
+ * tracking bunches[i]; all members advance together, one kernel launch per
+ * stage per grid class, each class on its own stream in one CUDA graph per
+ * turn.  The programs must share one node structure (same op codes, SC
+ * nodes in the same places), each use one plain-form 2.5D calculator of
+ * its own (no boundary, no 2.5Drb), and every bunch needs >= 2 particles.
+ * The first run times candidate launch shapes per class (autotuner); its
+ * choice can be read and fixed with orbit_batch_class / _set_tuning. */
+typedef struct orbit_batch orbit_batch_t;
+int orbit_batch_create(orbit_batch_t** out, orbit_program_t* const* programs, orbit_bunch_t* const* bunches, int n);
+int orbit_batch_destroy(orbit_batch_t* b);
+/* Enqueues `turns` turns of every member and advances each bunch's sync
+ * time; orbit_batch_sync waits and reports the first device error of any
+ * member.  orbit_batch_run = enqueue + sync. */
+int orbit_batch_enqueue(orbit_batch_t* b, int turns);
+int orbit_batch_sync(orbit_batch_t* b);
+int orbit_batch_run(orbit_batch_t* b, int turns);
+/* Number of grid classes, and kernel launches per captured turn. */
+int orbit_batch_info(const orbit_batch_t* b, int* n_classes, int* launches_per_turn);
+/* The cudaStream_t the batch's turns are enqueued on (as void*). */
+int orbit_batch_stream(orbit_batch_t* b, void** stream);
+/* One turn without graph capture, the classes one after another on the
+ * batch stream, every launch timed by CUDA events (as
+ * orbit_program_profile); advances the members like orbit_batch_run(b, 1).
+ * Needs a first run (the autotuned shapes). */
+int orbit_batch_profile(orbit_batch_t* b, int max_kinds, char* names, double* total_ms, int* launches,
+                        int* nkinds);
+/* Class cls: grid[3] = nx, ny, nz; members; tuning[6] = deposit threads,
+ * deposit particles per block, pass threads, pass particles per block, FFT
+ * schedule (1: radix-2 stages, 0: radix-4 stages), tuned (0/1). */
+int orbit_batch_class(const orbit_batch_t* b, int cls, int* grid, int* members, int* tuning);
+/* Fixes class cls's shapes (tuning[0..4], one of the candidates); no
+ * autotuning runs afterwards. */
+int orbit_batch_set_tuning(orbit_batch_t* b, int cls, const int* tuning);
+
 #ifdef __cplusplus
 }
 #endif

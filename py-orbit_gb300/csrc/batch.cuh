@@ -14,7 +14,6 @@ namespace orbit {
 struct PassJob {
   double* c[6];
   int n;
-  int blk0, nblk;       // the member's blocks in the launch
   int pad;
   const DevOp* ops;     // the member's compiled ops (same layout for all members)
   MapCtx m;
@@ -32,7 +31,6 @@ struct DepJob {
   const double* z;
   const double* msize;
   int n;
-  int blk0, nblk;
   int K;
   const ScState* st;
   unsigned long long* g_rho;
@@ -64,14 +62,25 @@ struct ClassTuning {
   int fft_wide;                  // 1: radix-2 stages, N/2 threads; 0: radix-4 stages, N/4 threads
 };
 
-// Batched launches of one class (sc2p5d.cu); jobs and blk_job are device
-// arrays, nm members, nblk blocks for the particle kernels; `proto` is any
-// calculator of the class (sizes, plans).
+// Block layout of a batched particle launch: blk_job[block] is the member a
+// block works for, mblk[member] = {first block, number of blocks}.
+struct BlockMap {
+  unsigned short* blk_job = nullptr;  // device
+  int2* mblk = nullptr;               // device
+  int nblk = 0;
+};
+
+// Batched launches of one class (sc2p5d.cu); jobs are device arrays of nm
+// members; `proto` is any calculator of the class (sizes, plans).
 int batch_enqueue_green(const SolveJob* jobs, int nm, const orbit_sc2p5d_t* proto, int fft_wide, cudaStream_t s);
-int batch_enqueue_deposit(const DepJob* jobs, const unsigned short* blk_job, int nblk, const orbit_sc2p5d_t* proto,
-                          int threads, cudaStream_t s);
+int batch_enqueue_deposit(const DepJob* jobs, const BlockMap& bm, const orbit_sc2p5d_t* proto, int threads,
+                          cudaStream_t s);
 int batch_enqueue_solve(const SolveJob* jobs, int nm, const orbit_sc2p5d_t* proto, int fft_wide, bool phi_fix,
                         cudaStream_t s);
+// The columns (forward, Green multiply, backward) and backward rows alone,
+// for timing the FFT schedules: they write only the work spectra, the
+// potentials and max |phi|, which the next solve and grid set-up replace.
+int batch_enqueue_fft_probe(const SolveJob* jobs, int nm, const orbit_sc2p5d_t* proto, int fft_wide, cudaStream_t s);
 int batch_init_attrs(const orbit_sc2p5d_t* proto);
 // Shared-memory bytes of the plain deposit grids of the class, and whether
 // they fit in shared memory.
@@ -80,8 +89,8 @@ bool batch_deposit_smem(const orbit_sc2p5d_t* proto);
 // Batched fused pass (program.cu).  kf: 0 no kick, 1 plain kick; ksmem: the
 // kick keeps a fixed-point copy of the potential of `smem` bytes in shared
 // memory.
-int batch_enqueue_pass(const PassJob* jobs, const unsigned short* blk_job, int nblk, int threads, int kf, bool ext,
-                       bool ksmem, size_t smem, int a, int b, int km, cudaStream_t s);
+int batch_enqueue_pass(const PassJob* jobs, const BlockMap& bm, int threads, int kf, bool ext, bool ksmem,
+                       size_t smem, int a, int b, int km, cudaStream_t s);
 // Largest pass-kick copy of the potential kept in shared memory.
 size_t batch_pass_smem_limit();
 

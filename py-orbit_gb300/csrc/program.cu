@@ -109,10 +109,13 @@ __global__ void __launch_bounds__(512) k_pass(double* __restrict__ cx, double* _
 // member in the block table.
 template <int KF, bool EXT, bool KSMEM>
 __global__ void __launch_bounds__(512) kb_pass(const PassJob* __restrict__ jobs,
-                                               const unsigned short* __restrict__ blk_job, int a, int b, int km) {
-  const PassJob& J = jobs[blk_job[blockIdx.x]];
+                                               const unsigned short* __restrict__ blk_job,
+                                               const int2* __restrict__ mblk, int a, int b, int km) {
+  const int j = blk_job[blockIdx.x];
+  const PassJob& J = jobs[j];
+  const int2 mb = mblk[j];
   pass_body<KF, EXT, KSMEM>(J.c[0], J.c[1], J.c[2], J.c[3], J.c[4], J.c[5], J.n, J.ops, a, b, J.m, J.ka, J.ext,
-                            J.status, J.sa, J.knl, km, blockIdx.x - J.blk0, J.nblk);
+                            J.status, J.sa, J.knl, km, blockIdx.x - mb.x, mb.y);
 }
 
 // Shared-memory limits are raised once, outside any stream capture.
@@ -151,20 +154,21 @@ static int launch_pass(orbit_bunch_t* bu, cudaStream_t s, size_t smem, const Dev
 
 size_t batch_pass_smem_limit() { return kPassSmem; }
 
-int batch_enqueue_pass(const PassJob* jobs, const unsigned short* blk_job, int nblk, int threads, int kf, bool ext,
-                       bool ksmem, size_t smem, int a, int b, int km, cudaStream_t s) {
+int batch_enqueue_pass(const PassJob* jobs, const BlockMap& bm, int threads, int kf, bool ext, bool ksmem,
+                       size_t smem, int a, int b, int km, cudaStream_t s) {
   int arc = init_pass_attrs();
   if (arc) return arc;
+  const int nb = bm.nblk;
   ORBIT_PB(kf == 0 ? "batch_pass_maps" : "batch_pass_kick_maps", s);
   if (kf == 0) {
-    if (ext) kb_pass<0, true, false><<<nblk, threads, 0, s>>>(jobs, blk_job, a, b, km);
-    else kb_pass<0, false, false><<<nblk, threads, 0, s>>>(jobs, blk_job, a, b, km);
+    if (ext) kb_pass<0, true, false><<<nb, threads, 0, s>>>(jobs, bm.blk_job, bm.mblk, a, b, km);
+    else kb_pass<0, false, false><<<nb, threads, 0, s>>>(jobs, bm.blk_job, bm.mblk, a, b, km);
   } else if (ksmem) {
-    if (ext) kb_pass<1, true, true><<<nblk, threads, smem, s>>>(jobs, blk_job, a, b, km);
-    else kb_pass<1, false, true><<<nblk, threads, smem, s>>>(jobs, blk_job, a, b, km);
+    if (ext) kb_pass<1, true, true><<<nb, threads, smem, s>>>(jobs, bm.blk_job, bm.mblk, a, b, km);
+    else kb_pass<1, false, true><<<nb, threads, smem, s>>>(jobs, bm.blk_job, bm.mblk, a, b, km);
   } else {
-    if (ext) kb_pass<1, true, false><<<nblk, threads, 0, s>>>(jobs, blk_job, a, b, km);
-    else kb_pass<1, false, false><<<nblk, threads, 0, s>>>(jobs, blk_job, a, b, km);
+    if (ext) kb_pass<1, true, false><<<nb, threads, 0, s>>>(jobs, bm.blk_job, bm.mblk, a, b, km);
+    else kb_pass<1, false, false><<<nb, threads, 0, s>>>(jobs, bm.blk_job, bm.mblk, a, b, km);
   }
   ORBIT_PE(s);
   ORBIT_LAUNCH_CHECK("batch pass");

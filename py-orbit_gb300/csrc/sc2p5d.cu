@@ -736,11 +736,13 @@ __global__ void kb_phi_fix(const SolveJob* __restrict__ jobs, int ng, int nz) {
 
 template <bool SMEM>
 __global__ void __launch_bounds__(768) kb_deposit(const DepJob* __restrict__ jobs,
-                                                  const unsigned short* __restrict__ blk_job, int nx, int ny,
-                                                  int nz) {
-  const DepJob& J = jobs[blk_job[blockIdx.x]];
+                                                  const unsigned short* __restrict__ blk_job,
+                                                  const int2* __restrict__ mblk, int nx, int ny, int nz) {
+  const int j = blk_job[blockIdx.x];
+  const DepJob& J = jobs[j];
+  const int2 mb = mblk[j];
   deposit_plain_body<SMEM>(J.x, J.y, J.z, J.msize, J.n, J.st, J.g_rho, J.g_z, J.ms_uniform, J.qscale, nx, ny, nz,
-                           J.K, blockIdx.x - J.blk0, J.nblk);
+                           J.K, blockIdx.x - mb.x, mb.y);
 }
 
 // ---------------------------------------------------------------------
@@ -942,14 +944,26 @@ int batch_enqueue_green(const SolveJob* jobs, int nm, const orbit_sc2p5d_t* c, i
   return ORBIT_OK;
 }
 
-int batch_enqueue_deposit(const DepJob* jobs, const unsigned short* blk_job, int nblk, const orbit_sc2p5d_t* c,
-                          int threads, cudaStream_t s) {
+int batch_enqueue_deposit(const DepJob* jobs, const BlockMap& bm, const orbit_sc2p5d_t* c, int threads,
+                          cudaStream_t s) {
   size_t sm = 8 * ((size_t)c->nx * c->ny + c->nz);
   ORBIT_PB("batch_deposit", s);
-  if (batch_deposit_smem(c)) kb_deposit<true><<<nblk, threads, sm, s>>>(jobs, blk_job, c->nx, c->ny, c->nz);
-  else kb_deposit<false><<<nblk, threads, 0, s>>>(jobs, blk_job, c->nx, c->ny, c->nz);
+  if (batch_deposit_smem(c))
+    kb_deposit<true><<<bm.nblk, threads, sm, s>>>(jobs, bm.blk_job, bm.mblk, c->nx, c->ny, c->nz);
+  else
+    kb_deposit<false><<<bm.nblk, threads, 0, s>>>(jobs, bm.blk_job, bm.mblk, c->nx, c->ny, c->nz);
   ORBIT_PE(s);
   ORBIT_LAUNCH_CHECK("batch deposit");
+  return ORBIT_OK;
+}
+
+int batch_enqueue_fft_probe(const SolveJob* jobs, int nm, const orbit_sc2p5d_t* c, int fft_wide, cudaStream_t s) {
+  int thx = batch_fft_threads(c->plan_x, fft_wide), thy = batch_fft_threads(c->plan_y, fft_wide);
+  size_t smx = fft_smem<double>(c->nx2), smy = fft_smem<double>(c->ny2);
+  kb_cols<1><<<dim3(c->H, nm), thx, smx, s>>>(jobs, c->plan_x, c->nx, c->H, c->ny2);
+  kb_rows_inv<<<dim3((c->nx + 1) / 2, nm), thy, smy, s>>>(jobs, c->plan_y, c->nx, c->ny, c->H,
+                                                          1.0 / (c->nx2 * c->ny2));
+  ORBIT_LAUNCH_CHECK("batch FFT probe");
   return ORBIT_OK;
 }
 

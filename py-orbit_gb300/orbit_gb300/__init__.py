@@ -15,7 +15,7 @@ from . import _native
 from ._native import (FORM_FP32, FORM_PLAIN, OP, OrbitError, SpaceChargeError, Sync, call, load,
                       library_path)
 
-__all__ = ["DeviceBunch", "DeviceSC2p5D", "DeviceSC2p5Drb", "DeviceBoundary", "DeviceProgram", "OrbitError", "SpaceChargeError", "load",
+__all__ = ["DeviceBunch", "DeviceSC2p5D", "DeviceSC2p5Drb", "DeviceBoundary", "DeviceProgram", "DeviceBatch", "OrbitError", "SpaceChargeError", "load",
            "FORM_PLAIN", "FORM_FP32", "OP", "library_path", "version"]
 
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -271,6 +271,80 @@ class DeviceBoundary:
         r = ctypes.c_double()
         call("orbit_boundary_rnorm", self.h, ctypes.byref(r))
         return out, r.value
+
+
+class DeviceBatch:
+    """Members (program i tracking device bunch i) advanced together; one
+    kernel launch per stage per grid class (orbit_batch_*)."""
+
+    def __init__(self, programs, bunches):
+        if len(programs) != len(bunches) or not programs:
+            raise ValueError("one program per bunch")
+        n = len(programs)
+        ph = (ctypes.c_void_p * n)(*[p.h.value for p in programs])
+        bh = (ctypes.c_void_p * n)(*[b.h.value for b in bunches])
+        h = ctypes.c_void_p()
+        call("orbit_batch_create", ctypes.byref(h), ph, bh, n)
+        self.h = h
+        self.programs = list(programs)  # kept alive with the batch
+        self.bunches = list(bunches)
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h is not None and h.value and _native._lib is not None:
+            _native._lib.orbit_batch_destroy(h)
+            self.h = None
+
+    def run(self, turns: int = 1):
+        call("orbit_batch_run", self.h, int(turns))
+
+    def enqueue(self, turns: int = 1):
+        call("orbit_batch_enqueue", self.h, int(turns))
+
+    def sync(self):
+        call("orbit_batch_sync", self.h)
+
+    def info(self):
+        """(number of grid classes, kernel launches per captured turn)."""
+        nc, nl = ctypes.c_int(), ctypes.c_int()
+        call("orbit_batch_info", self.h, ctypes.byref(nc), ctypes.byref(nl))
+        return nc.value, nl.value
+
+    def classes(self):
+        """Per grid class: {grid, members, dep_threads, dep_chunk,
+        pass_threads, pass_chunk, fft_radix2, tuned}."""
+        nc, _ = self.info()
+        out = []
+        for k in range(nc):
+            g = (ctypes.c_int * 3)()
+            m = ctypes.c_int()
+            t = (ctypes.c_int * 6)()
+            call("orbit_batch_class", self.h, k, g, ctypes.byref(m), t)
+            out.append({"grid": tuple(g), "members": m.value, "dep_threads": t[0], "dep_chunk": t[1],
+                        "pass_threads": t[2], "pass_chunk": t[3], "fft_radix2": t[4], "tuned": t[5]})
+        return out
+
+    def set_tuning(self, cls, dep_threads, dep_chunk, pass_threads, pass_chunk, fft_radix2):
+        t = (ctypes.c_int * 5)(dep_threads, dep_chunk, pass_threads, pass_chunk, fft_radix2)
+        call("orbit_batch_set_tuning", self.h, int(cls), t)
+
+    def stream_ptr(self) -> int:
+        v = ctypes.c_void_p()
+        call("orbit_batch_stream", self.h, ctypes.byref(v))
+        return v.value or 0
+
+    def profile(self, max_kinds: int = 32):
+        """One eager turn with every launch timed: {kernel kind: (total ms, launches)}."""
+        names = ctypes.create_string_buffer(32 * max_kinds)
+        ms = (ctypes.c_double * max_kinds)()
+        cnt = (ctypes.c_int * max_kinds)()
+        nk = ctypes.c_int()
+        call("orbit_batch_profile", self.h, max_kinds, names, ms, cnt, ctypes.byref(nk))
+        out = {}
+        for k in range(nk.value):
+            nm = names.raw[32 * k: 32 * k + 32].split(b"\0", 1)[0].decode()
+            out[nm] = (ms[k], cnt[k])
+        return out
 
 
 class DeviceProgram:

@@ -118,6 +118,19 @@ _SIGS = {
     "orbit_program_launches": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int)]),
     "orbit_program_profile": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_char_p, _dp,
                                              ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
+    "orbit_batch_create": (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.POINTER(_vp), ctypes.POINTER(_vp),
+                                          ctypes.c_int]),
+    "orbit_batch_destroy": (ctypes.c_int, [_vp]),
+    "orbit_batch_enqueue": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "orbit_batch_sync": (ctypes.c_int, [_vp]),
+    "orbit_batch_run": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "orbit_batch_info": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
+    "orbit_batch_class": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                         ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
+    "orbit_batch_set_tuning": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+    "orbit_batch_stream": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
+    "orbit_batch_profile": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_char_p, _dp, ctypes.POINTER(ctypes.c_int),
+                                           ctypes.POINTER(ctypes.c_int)]),
 }
 
 _D, _I = ctypes.c_double, ctypes.c_int

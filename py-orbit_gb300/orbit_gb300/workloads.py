@@ -10,6 +10,11 @@ C2  FODO tracking: 1e6 protons at 1 GeV, 4D waterbag with rms 4 mm /
     cells (quads k1 = +-0.5 m^-2, 0.5 m long; 2 m drifts; 4 SC nodes per
     cell).  The configuration names no intensity; 1e14 protons
     (macrosize 1e8 at 1e6 particles) is used.
+C3  batched scan: 64 bunches, particle counts log-uniform in [5e4, 2e6],
+    Gaussian 6D (rms 4 mm / 0.8 mrad transverse, z ~ N(0, 10 m),
+    dE ~ N(0, 1 MeV)), intensities log-uniform in [1e12, 2e14] protons,
+    FODO k1 uniform in [0.3, 0.7] m^-2 (the C2 lattice otherwise), grids
+    drawn from 64x64x32, 128x128x64 and 256x256x64.
 """
 from __future__ import annotations
 
@@ -46,6 +51,34 @@ def c2_coords(n=1_000_000, seed=20240602):
 
 C1_MACROSIZE = 1e9
 C2_MACROSIZE = 1e8
+
+C3_GRIDS = ((64, 64, 32), (128, 128, 64), (256, 256, 64))
+
+
+def c3_scan(members=64, seed=20240603):
+    """[(particles, grid, k1, intensity)] of the batched scan."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for _ in range(members):
+        n = int(round(np.exp(rng.uniform(np.log(5e4), np.log(2e6)))))
+        grid = C3_GRIDS[int(rng.integers(0, len(C3_GRIDS)))]
+        k1 = float(rng.uniform(0.3, 0.7))
+        intensity = float(np.exp(rng.uniform(np.log(1e12), np.log(2e14))))
+        out.append((n, grid, k1, intensity))
+    return out
+
+
+def c3_coords(n, seed):
+    """Gaussian 6D bunch of the scan."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    soa = np.empty((6, n))
+    soa[0] = rng.normal(0.0, 4e-3, n)
+    soa[1] = rng.normal(0.0, 0.8e-3, n)
+    soa[2] = rng.normal(0.0, 4e-3, n)
+    soa[3] = rng.normal(0.0, 0.8e-3, n)
+    soa[4] = rng.normal(0.0, 10.0, n)
+    soa[5] = rng.normal(0.0, 1e-3, n)
+    return soa
 
 
 def make_bunch(soa, macrosize, kin_energy=KIN_ENERGY):

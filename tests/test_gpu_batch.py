@@ -1,0 +1,98 @@
+"""Batched tracking of a scan (orbit_batch_*): bunches of different sizes,
+intensities, quadrupole strengths and grid sizes advanced together, against
+the same bunches tracked one at a time and against the oracle.
+
+With the FFT schedule fixed to the one single-bunch tracking uses (radix-2
+stages) a batched bunch ends bit for bit where tracking it alone leaves it:
+the deposit sums integers in any block layout and the pass is per particle.
+With the schedule the autotuner picks, the FFT rounding may differ: 1e-11
+relative after the turns here.  Against the oracle: 1e-10."""
+import numpy as np
+import pytest
+
+import oracle as O
+from helpers import TOL_COORD, coord_err
+
+pytestmark = pytest.mark.gpu
+
+# (particles, grid, quadrupole k1, macrosize)
+SCAN = [(3000, (32, 32, 8), 0.35, 2e9), (20000, (64, 64, 16), 0.5, 5e8), (7000, (32, 32, 8), 0.6, 1e9),
+        (40000, (64, 64, 16), 0.45, 1e8), (2500, (32, 32, 8), 0.7, 4e9)]
+
+
+def member(k, seed_base=500):
+    from orbit_gb300 import workloads as W
+    from spacecharge import SpaceChargeCalc2p5D
+    n, grid, kq, ms = SCAN[k]
+    soa = W.c2_coords(n, seed=seed_base + k)
+    b = W.make_bunch(soa, ms)
+    lat = W.fodo_lattice(SpaceChargeCalc2p5D(*grid), cells=2, kq=kq)
+    return soa, b, lat
+
+
+def single_results(turns):
+    out = []
+    for k in range(len(SCAN)):
+        _, b, lat = member(k)
+        lat.trackBunchTurns(b, turns)
+        out.append(b.getCoordinates())
+    return out
+
+
+def test_batch_equals_single_bunch_tracking_with_the_same_fft_schedule():
+    from orbit_gb300.batch import BunchBatch
+    members = [member(k) for k in range(len(SCAN))]
+    bb = BunchBatch([(b, lat) for _, b, lat in members])
+    cls = bb.classes()
+    assert sorted(c["grid"] for c in cls) == [(32, 32, 8), (64, 64, 16)]
+    assert sorted(c["members"] for c in cls) == [2, 3]
+    for k, c in enumerate(cls):
+        bb._batch.set_tuning(k, 768, 8192, 512, 4096, 1)
+    bb.trackTurns(3)
+    ref = single_results(3)
+    for k, (_, b, _) in enumerate(members):
+        assert np.array_equal(b.getCoordinates(), ref[k]), k
+    # sync time advanced as single-bunch tracking advances it
+    _, b1, lat1 = member(0)
+    lat1.trackBunchTurns(b1, 3)
+    assert members[0][1].getSyncParticle().time() == b1.getSyncParticle().time()
+
+
+def test_batch_autotuned_against_single_and_oracle():
+    from orbit.lattice import AccActionsContainer
+    from orbit.teapot.recording import BunchRecorder
+    from orbit_gb300.batch import BunchBatch
+    members = [member(k) for k in range(len(SCAN))]
+    bb = BunchBatch([(b, lat) for _, b, lat in members])
+    bb.trackTurns(2)  # the first turn times the candidate shapes
+    bb.trackTurns(2)  # captured graphs
+    for c in bb.classes():
+        assert c["tuned"] == 1
+        assert c["fft_radix2"] in (0, 1)
+    assert bb.launchesPerTurn() > 0
+    ref = single_results(4)
+    for k, (_, b, _) in enumerate(members):
+        assert coord_err(b.getCoordinates(), ref[k]) <= 1e-11, k
+    # one member against the oracle running its recorded op list
+    soa, b0, lat0 = member(1)
+    rec = BunchRecorder(b0)
+    cont = AccActionsContainer()
+    cont.addAction(lambda p: p["node"].track(p), AccActionsContainer.BODY)
+    lat0.trackActions(cont, {"bunch": rec, "useCharge": 1})
+    s = b0.getSyncParticle()
+    sync = O.make_sync(beta=s.beta(), gamma=s.gamma(), momentum=s.momentum(), macrosize=b0.macroSize())
+    a = np.ascontiguousarray(soa.copy())
+    assert O.run_program(rec.ops, 4, a, sync, [O.OracleSC(*SCAN[1][1])], nthreads=8) == 0
+    assert coord_err(members[1][1].getCoordinates(), a) <= TOL_COORD
+
+
+def test_batch_rejects_lattices_of_different_structure():
+    from orbit_gb300 import OrbitError
+    from orbit_gb300 import workloads as W
+    from orbit_gb300.batch import BunchBatch
+    from spacecharge import SpaceChargeCalc2p5D
+    _, b0, lat0 = member(0)
+    b1 = W.make_bunch(W.c2_coords(3000, seed=9), 1e9)
+    lat1 = W.fodo_lattice(SpaceChargeCalc2p5D(32, 32, 8), cells=3)
+    with pytest.raises(OrbitError):
+        BunchBatch([(b0, lat0), (b1, lat1)]).trackTurns(1)
