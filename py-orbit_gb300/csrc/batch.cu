@@ -21,6 +21,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <string>
 #include <tuple>
 #include <vector>
 
@@ -49,6 +50,7 @@ struct BatchClass {
   std::vector<BlockMap> dep_maps;  // one per deposit candidate
   std::vector<BlockMap> pass_maps; // one per pass candidate
   int dep_sel = 0, pass_sel = 0;
+  std::string dep_tag, pass_tag;   // profile names of the class's deposit and kick passes
   cudaStream_t st = nullptr;
   cudaEvent_t joined = nullptr;
 };
@@ -323,7 +325,7 @@ static int enqueue_class_turn(orbit_batch_t* bt, int ci, cudaStream_t s, bool pr
     int rc = rec_begin(t, ci, 1, cand, s, &r);
     if (rc) return rc;
     rc = batch_enqueue_pass(c.d_pass + (size_t)table * nm, c.pass_maps[cand], kPassCand[cand][0], kick ? 1 : 0, ext,
-                            kick && c.ksmem, c.kick_smem, sg.a, sg.b, km_of(sg), s);
+                            kick && c.ksmem, c.kick_smem, sg.a, sg.b, km_of(sg), s, c.pass_tag.c_str());
     if (rc) return rc;
     ++*nl;
     return rec_end(t, s, r);
@@ -340,7 +342,7 @@ static int enqueue_class_turn(orbit_batch_t* bt, int ci, cudaStream_t s, bool pr
     int dc = tu ? i % kNDep : c.dep_sel;
     Tuner::Rec r{};
     rc = rec_begin(tu, ci, 0, dc, s, &r);
-    if (!rc) rc = batch_enqueue_deposit(c.d_dep, c.dep_maps[dc], c.proto, kDepCand[dc][0], s);
+    if (!rc) rc = batch_enqueue_deposit(c.d_dep, c.dep_maps[dc], c.proto, kDepCand[dc][0], s, c.dep_tag.c_str());
     if (!rc) rc = rec_end(tu, s, r);
     if (rc) return rc;
     ++*nl;
@@ -551,6 +553,9 @@ int orbit_batch_create(orbit_batch_t** out, orbit_program_t* const* progs, orbit
       cls->kick_smem = 8 * ((size_t)c->nx * c->ny + c->nz);
       cls->ksmem = c->smem_kick && cls->kick_smem <= batch_pass_smem_limit();
       cls->tune = ClassTuning{kDepCand[1][0], kDepCand[1][1], kPassCand[1][0], kPassCand[1][1], 1};
+      std::string g = std::to_string(c->nx) + "x" + std::to_string(c->ny) + "x" + std::to_string(c->nz);
+      cls->dep_tag = "batch_deposit_" + g;
+      cls->pass_tag = "batch_pass_" + g;
       cls->dep_sel = 1;
       cls->pass_sel = 1;
     }

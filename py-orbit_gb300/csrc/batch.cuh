@@ -73,8 +73,9 @@ struct BlockMap {
 // Batched launches of one class (sc2p5d.cu); jobs are device arrays of nm
 // members; `proto` is any calculator of the class (sizes, plans).
 int batch_enqueue_green(const SolveJob* jobs, int nm, const orbit_sc2p5d_t* proto, int fft_wide, cudaStream_t s);
+// `tag` names the launch for orbit_batch_profile.
 int batch_enqueue_deposit(const DepJob* jobs, const BlockMap& bm, const orbit_sc2p5d_t* proto, int threads,
-                          cudaStream_t s);
+                          cudaStream_t s, const char* tag);
 int batch_enqueue_solve(const SolveJob* jobs, int nm, const orbit_sc2p5d_t* proto, int fft_wide, bool phi_fix,
                         cudaStream_t s);
 // The columns (forward, Green multiply, backward) and backward rows alone,
@@ -90,7 +91,7 @@ bool batch_deposit_smem(const orbit_sc2p5d_t* proto);
 // kick keeps a fixed-point copy of the potential of `smem` bytes in shared
 // memory.
 int batch_enqueue_pass(const PassJob* jobs, const BlockMap& bm, int threads, int kf, bool ext, bool ksmem,
-                       size_t smem, int a, int b, int km, cudaStream_t s);
+                       size_t smem, int a, int b, int km, cudaStream_t s, const char* tag);
 // Largest pass-kick copy of the potential kept in shared memory.
 size_t batch_pass_smem_limit();
 

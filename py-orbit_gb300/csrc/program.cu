@@ -155,11 +155,11 @@ static int launch_pass(orbit_bunch_t* bu, cudaStream_t s, size_t smem, const Dev
 size_t batch_pass_smem_limit() { return kPassSmem; }
 
 int batch_enqueue_pass(const PassJob* jobs, const BlockMap& bm, int threads, int kf, bool ext, bool ksmem,
-                       size_t smem, int a, int b, int km, cudaStream_t s) {
+                       size_t smem, int a, int b, int km, cudaStream_t s, const char* tag) {
   int arc = init_pass_attrs();
   if (arc) return arc;
   const int nb = bm.nblk;
-  ORBIT_PB(kf == 0 ? "batch_pass_maps" : "batch_pass_kick_maps", s);
+  ORBIT_PB(kf == 0 ? "batch_pass_maps" : tag, s);
   if (kf == 0) {
     if (ext) kb_pass<0, true, false><<<nb, threads, 0, s>>>(jobs, bm.blk_job, bm.mblk, a, b, km);
     else kb_pass<0, false, false><<<nb, threads, 0, s>>>(jobs, bm.blk_job, bm.mblk, a, b, km);

@@ -945,9 +945,9 @@ int batch_enqueue_green(const SolveJob* jobs, int nm, const orbit_sc2p5d_t* c, i
 }
 
 int batch_enqueue_deposit(const DepJob* jobs, const BlockMap& bm, const orbit_sc2p5d_t* c, int threads,
-                          cudaStream_t s) {
+                          cudaStream_t s, const char* tag) {
   size_t sm = 8 * ((size_t)c->nx * c->ny + c->nz);
-  ORBIT_PB("batch_deposit", s);
+  ORBIT_PB(tag, s);
   if (batch_deposit_smem(c))
     kb_deposit<true><<<bm.nblk, threads, sm, s>>>(jobs, bm.blk_job, bm.mblk, c->nx, c->ny, c->nz);
   else
