@@ -128,14 +128,15 @@ static bool sync_same(const orbit_sync_t& a, const orbit_sync_t& b) {
          a.classical_radius == b.classical_radius && a.macrosize == b.macrosize && a.mass == b.mass;
 }
 
-// Blocks of each member for `chunk` particles per block.
-static int build_map(const orbit_batch_t* bt, const BatchClass& c, int chunk, BlockMap& out) {
+// Blocks of each member for `chunk` particles per `per` blocks.
+static int build_map(const orbit_batch_t* bt, const BatchClass& c, int chunk, int per, BlockMap& out) {
   std::vector<unsigned short> bj;
   std::vector<int2> mb(c.mem.size());
   for (size_t j = 0; j < c.mem.size(); ++j) {
     int n = bt->bunches[c.mem[j]]->n;
     int nb = (n + chunk - 1) / chunk;
     if (nb < 1) nb = 1;
+    nb *= per;
     mb[j].x = (int)bj.size();
     mb[j].y = nb;
     bj.insert(bj.end(), (size_t)nb, (unsigned short)j);
@@ -218,8 +219,9 @@ static int build_tables(orbit_batch_t* bt, BatchClass& c) {
   if (rc) return rc;
   c.dep_maps.resize(kNDep);
   c.pass_maps.resize(kNPass);
-  for (int q = 0; q < kNDep && !rc; ++q) rc = build_map(bt, c, kDepCand[q][1], c.dep_maps[q]);
-  for (int q = 0; q < kNPass && !rc; ++q) rc = build_map(bt, c, kPassCand[q][1], c.pass_maps[q]);
+  const int bands = batch_deposit_bands(c.proto);
+  for (int q = 0; q < kNDep && !rc; ++q) rc = build_map(bt, c, kDepCand[q][1], bands, c.dep_maps[q]);
+  for (int q = 0; q < kNPass && !rc; ++q) rc = build_map(bt, c, kPassCand[q][1], 1, c.pass_maps[q]);
   return rc;
 }
 

@@ -86,6 +86,9 @@ int batch_init_attrs(const orbit_sc2p5d_t* proto);
 // Shared-memory bytes of the plain deposit grids of the class, and whether
 // they fit in shared memory.
 bool batch_deposit_smem(const orbit_sc2p5d_t* proto);
+// Blocks per particle chunk of the class's deposit: the number of row bands
+// of a grid too large for one block's shared memory, else 1.
+int batch_deposit_bands(const orbit_sc2p5d_t* proto);
 
 // Batched fused pass (program.cu).  kf: 0 no kick, 1 plain kick; ksmem: the
 // kick keeps a fixed-point copy of the potential of `smem` bytes in shared

@@ -533,9 +533,9 @@ __device__ __forceinline__ void deposit_plain_body(const double* __restrict__ x,
   }
   for (int i = blk * blockDim.x + threadIdx.x; i < n; i += nblk * blockDim.x) {
     double xi = x[i], yi = y[i], zi = z[i];
-    if (K > 0 && deposit_fixed<SMEM>(df, rho, zg, xi, yi, zi)) continue;
+    if (K > 0 && deposit_fixed(df, rho, zg, xi, yi, zi)) continue;
     double ms = msize ? msize[i] * qscale : ms_uniform;
-    deposit_plain<SMEM>(d, rho, zg, xi, yi, zi, ms);
+    deposit_plain(d, rho, zg, xi, yi, zi, ms);
   }
   if constexpr (SMEM) {
     __syncthreads();
@@ -553,6 +553,63 @@ __global__ void __launch_bounds__(768) k_deposit_plain(const double* __restrict_
                                 double ms_uniform, double qscale, int nx, int ny, int nz, int K) {
   deposit_plain_body<SMEM>(x, y, z, msize, n, st, g_rho, g_z, ms_uniform, qscale, nx, ny, nz, K, blockIdx.x,
                            gridDim.x);
+}
+
+// Band deposit (plain form) for grids whose two 32-bit words per cell do
+// not fit in one block's shared memory.  Block (chunk, band) keeps rows
+// r0-1..r1 of the grid (band rows [r0, r1) plus one halo row on each side)
+// and the whole line density in shared memory, reads the chunk's
+// particles and deposits those whose centre row lies in its band (band 0
+// also those outside the transverse grid); the halo rows reach the global
+// grid through the same exact 64-bit integer adds as every other cell.
+__device__ __forceinline__ void deposit_band_body(const double* __restrict__ x, const double* __restrict__ y,
+                                                  const double* __restrict__ z, const double* __restrict__ msize,
+                                                  int n, const ScState* st, unsigned long long* g_rho,
+                                                  unsigned long long* g_z, double ms_uniform, double qscale, int nx,
+                                                  int ny, int nz, int K, int rpb, int band, int chunk, int nchunk) {
+  DepConst d;
+  load_dep_const(d, st, nx, ny, nz);
+  if (d.skip) return;
+  DepFix df;
+  if (K > 0) load_dep_fix(df, st, nx, ny, nz, K);
+  const int r0 = band * rpb, r1 = min(nx, r0 + rpb);
+  const int lr0 = max(r0 - 1, 0), lr1 = min(r1 + 1, nx);
+  const int nloc = (lr1 - lr0) * ny;
+  const int ncell = nloc + nz;
+  extern __shared__ unsigned s_band32[];
+  BandAcc rho;
+  rho.lo = s_band32;
+  rho.hi_off = ncell;
+  rho.base = lr0 * ny;
+  rho.r0 = r0;
+  rho.r1 = r1;
+  rho.first = band == 0;
+  GridAcc<true> zg;
+  zg.lo = s_band32 + nloc;
+  zg.hi_off = ncell;
+  for (int i = threadIdx.x; i < 2 * ncell; i += blockDim.x) s_band32[i] = 0u;
+  __syncthreads();
+  for (int i = chunk * blockDim.x + threadIdx.x; i < n; i += nchunk * blockDim.x) {
+    double xi = x[i], yi = y[i], zi = z[i];
+    if (K > 0 && deposit_fixed(df, rho, zg, xi, yi, zi)) continue;
+    double ms = msize ? msize[i] * qscale : ms_uniform;
+    deposit_plain(d, rho, zg, xi, yi, zi, ms);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < ncell; i += blockDim.x) {
+    unsigned long long v = ((unsigned long long)s_band32[ncell + i] << 32) | s_band32[i];
+    if (v) atomicAdd(i < nloc ? g_rho + (size_t)lr0 * ny + i : g_z + (i - nloc), v);
+  }
+}
+
+// nb bands; blocks blockIdx.x = chunk * nb + band.
+__global__ void __launch_bounds__(768) k_deposit_band(const double* __restrict__ x, const double* __restrict__ y,
+                                                      const double* __restrict__ z, const double* __restrict__ msize,
+                                                      int n, const ScState* st, unsigned long long* g_rho,
+                                                      unsigned long long* g_z, double ms_uniform, double qscale,
+                                                      int nx, int ny, int nz, int K, int rpb, int nb) {
+  deposit_band_body(x, y, z, msize, n, st, g_rho, g_z, ms_uniform, qscale, nx, ny, nz, K, rpb, blockIdx.x % nb,
+                    blockIdx.x / nb, gridDim.x / nb);
 }
 
 template <bool SMEM>
@@ -734,6 +791,19 @@ __global__ void kb_phi_fix(const SolveJob* __restrict__ jobs, int ng, int nz) {
   phi_fix_body(J.st, J.phi, J.lam, J.phi_fix, J.lam_fix, ng, nz, blockIdx.x);
 }
 
+// Members' blocks: chunk * nb + band.
+__global__ void __launch_bounds__(768) kb_deposit_band(const DepJob* __restrict__ jobs,
+                                                       const unsigned short* __restrict__ blk_job,
+                                                       const int2* __restrict__ mblk, int nx, int ny, int nz, int rpb,
+                                                       int nb) {
+  const int j = blk_job[blockIdx.x];
+  const DepJob& J = jobs[j];
+  const int2 mb = mblk[j];
+  const int lb = blockIdx.x - mb.x;
+  deposit_band_body(J.x, J.y, J.z, J.msize, J.n, J.st, J.g_rho, J.g_z, J.ms_uniform, J.qscale, nx, ny, nz, J.K, rpb,
+                    lb % nb, lb / nb, mb.y / nb);
+}
+
 template <bool SMEM>
 __global__ void __launch_bounds__(768) kb_deposit(const DepJob* __restrict__ jobs,
                                                   const unsigned short* __restrict__ blk_job,
@@ -812,6 +882,26 @@ static void particle_geometry(size_t smem, int n, int max_threads, int* blocks, 
   int b = num_sms() * bps;
   int need = (n + *threads - 1) / *threads;
   *blocks = need < b ? (need < 1 ? 1 : need) : b;
+}
+
+// Rows per band of the band deposit: shared memory (two 32-bit words per
+// cell of the band, its halo rows and the line density) within 200 KB (the
+// deposit's 80 registers at 768 threads already keep one block per SM, so
+// fewer, taller bands re-read fewer coordinates); bands of equal height.
+int band_rows(int nx, int ny, int nz, int* nbands) {
+  long long cells = 200 * 1024 / 8 - nz;
+  int rmax = (int)(cells / ny) - 2;
+  if (rmax < 1) rmax = 1;
+  int nb = (nx + rmax - 1) / rmax;
+  int rpb = (nx + nb - 1) / nb;
+  *nbands = (nx + rpb - 1) / rpb;
+  return rpb;
+}
+
+static size_t band_smem(int nx, int ny, int nz) {
+  int nb;
+  int rpb = band_rows(nx, ny, nz, &nb);
+  return 8 * ((size_t)(rpb + 2) * ny + nz);
 }
 
 // Forward row transforms of the deposit (plus one block finalizing the line
@@ -907,6 +997,13 @@ bool batch_deposit_smem(const orbit_sc2p5d_t* c) {
   return 8 * ((size_t)c->nx * c->ny + c->nz) <= (size_t)kMaxSmem;
 }
 
+int batch_deposit_bands(const orbit_sc2p5d_t* c) {
+  if (batch_deposit_smem(c) || !c->band_deposit) return 1;
+  int nb;
+  band_rows(c->nx, c->ny, c->nz, &nb);
+  return nb;
+}
+
 int batch_init_attrs(const orbit_sc2p5d_t* c) {
   int bytes = (int)fft_smem<double>(c->nx2 > c->ny2 ? c->nx2 : c->ny2);
   if (bytes > 48 * 1024) {
@@ -919,6 +1016,8 @@ int batch_init_attrs(const orbit_sc2p5d_t* c) {
   size_t dep = 8 * ((size_t)c->nx * c->ny + c->nz);
   if (dep <= (size_t)kMaxSmem && dep > 48 * 1024)
     ORBIT_CUDA(cudaFuncSetAttribute(kb_deposit<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem));
+  if (c->band_deposit && band_smem(c->nx, c->ny, c->nz) > 48 * 1024)
+    ORBIT_CUDA(cudaFuncSetAttribute(kb_deposit_band, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem));
   return ORBIT_OK;
 }
 
@@ -948,10 +1047,16 @@ int batch_enqueue_deposit(const DepJob* jobs, const BlockMap& bm, const orbit_sc
                           cudaStream_t s, const char* tag) {
   size_t sm = 8 * ((size_t)c->nx * c->ny + c->nz);
   ORBIT_PB(tag, s);
-  if (batch_deposit_smem(c))
+  if (batch_deposit_smem(c)) {
     kb_deposit<true><<<bm.nblk, threads, sm, s>>>(jobs, bm.blk_job, bm.mblk, c->nx, c->ny, c->nz);
-  else
+  } else if (c->band_deposit) {
+    int nb;
+    int rpb = band_rows(c->nx, c->ny, c->nz, &nb);
+    kb_deposit_band<<<bm.nblk, threads, band_smem(c->nx, c->ny, c->nz), s>>>(jobs, bm.blk_job, bm.mblk, c->nx, c->ny,
+                                                                           c->nz, rpb, nb);
+  } else {
     kb_deposit<false><<<bm.nblk, threads, 0, s>>>(jobs, bm.blk_job, bm.mblk, c->nx, c->ny, c->nz);
+  }
   ORBIT_PE(s);
   ORBIT_LAUNCH_CHECK("batch deposit");
   return ORBIT_OK;
@@ -1161,14 +1266,26 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
                     &threads);
   ORBIT_PB("deposit", s);
   if (plain) {
-    if (c->smem_deposit)
+    if (c->smem_deposit) {
       k_deposit_plain<true><<<blocks, threads, sm, s>>>(b->coord(0), b->coord(2), b->coord(4), msz, n, c->d_st,
                                                         c->d_rho_q, c->d_z_q, ds.ms_uniform, ds.S, c->nx, c->ny,
                                                         c->nz, ds.K);
-    else
+    } else if (c->band_deposit) {
+      // the grid in row bands, each block one band of one particle chunk
+      int nb;
+      int rpb = band_rows(c->nx, c->ny, c->nz, &nb);
+      int chunks = (n + 2047) / 2048, cap = (num_sms() + nb - 1) / nb;
+      chunks = chunks < 1 ? 1 : (chunks > cap ? cap : chunks);
+      int bt = max_threads_of(k_deposit_band);
+      bt = bt > 768 ? 768 : (bt & ~31);
+      k_deposit_band<<<chunks * nb, bt, band_smem(c->nx, c->ny, c->nz), s>>>(
+          b->coord(0), b->coord(2), b->coord(4), msz, n, c->d_st, c->d_rho_q, c->d_z_q, ds.ms_uniform, ds.S, c->nx,
+          c->ny, c->nz, ds.K, rpb, nb);
+    } else {
       k_deposit_plain<false><<<blocks, threads, 0, s>>>(b->coord(0), b->coord(2), b->coord(4), msz, n, c->d_st,
                                                         c->d_rho_q, c->d_z_q, ds.ms_uniform, ds.S, c->nx, c->ny,
                                                         c->nz, ds.K);
+    }
   } else {
     if (c->smem_deposit)
       k_deposit_fp32<true><<<blocks, threads, sm, s>>>(b->coord(0), b->coord(2), b->coord(4), msz, n, c->d_st,
@@ -1273,6 +1390,10 @@ static int init_attrs(orbit_sc2p5d_t* c) {
   c->smem_deposit = dep <= (size_t)kMaxSmem;
   c->smem_kick = kick <= (size_t)kMaxSmem;
   if (c->form == ORBIT_FORM_PLAIN) {
+    size_t bs = band_smem(c->nx, c->ny, c->nz);
+    c->band_deposit = !c->smem_deposit && bs <= (size_t)kMaxSmem;
+    if (c->band_deposit && bs > 48 * 1024)
+      ORBIT_CUDA(cudaFuncSetAttribute(k_deposit_band, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem));
     if (c->smem_deposit && dep > 48 * 1024)
       ORBIT_CUDA(cudaFuncSetAttribute(k_deposit_plain<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem));
     if (c->smem_kick && kick > 48 * 1024)

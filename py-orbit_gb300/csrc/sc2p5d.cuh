@@ -115,6 +115,7 @@ struct orbit_sc2p5d {
   cudaGraphConditionalHandle pending_cond = 0;
   cudaGraph_t pending_graph = nullptr;
   bool smem_deposit = false, smem_kick = false;
+  bool band_deposit = false;              // plain form: the grid in row bands (too large for one block)
   // SpaceChargeCalc2p5Drb (plain form): longitudinal kick from the smoothed
   // derivative of the line density
   bool rb = false;
@@ -153,6 +154,9 @@ int bnd_ensure_device(orbit_boundary* bnd);
 cudaGraphConditionalHandle sc_green_cond(orbit_sc2p5d_t* c, cudaStream_t s, bool pending);
 // Forgets a pending handle (start of a new capture).
 void sc_clear_pending(orbit_sc2p5d_t* c);
+// Band deposit of grids too large for one block's shared memory: rows per
+// band and the number of bands.
+int band_rows(int nx, int ny, int nz, int* nbands);
 // Kick factor 2 L r_c / (beta^2 gamma^3) computed on the host exactly as
 // SpaceChargeCalc2p5D.cc:96 does (libm pow).
 double sc_host_factor(const orbit_sync_t& s, double length);

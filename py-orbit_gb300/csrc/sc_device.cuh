@@ -391,6 +391,9 @@ template <bool SHARED> struct GridAcc;
 template <> struct GridAcc<false> {
   unsigned long long* p;
   __device__ __forceinline__ void add(int i, unsigned long long v) const { atomicAdd(p + i, v); }
+  // every particle is deposited by the block that reads it
+  __device__ __forceinline__ bool owns(int) const { return true; }
+  __device__ __forceinline__ bool owns_outside() const { return true; }
 };
 
 template <> struct GridAcc<true> {
@@ -405,18 +408,48 @@ template <> struct GridAcc<true> {
   __device__ __forceinline__ unsigned long long get(int i) const {
     return ((unsigned long long)lo[hi_off + i] << 32) | lo[i];
   }
+  __device__ __forceinline__ bool owns(int) const { return true; }
+  __device__ __forceinline__ bool owns_outside() const { return true; }
+};
+
+// Rows r0..r1-1 of a grid too large for one block's shared memory, plus
+// one halo row on each side (the 9-point stencil of a particle whose
+// centre row is owned).  A particle is deposited by the block that owns its
+// centre row, whole (its line-density contribution included); particles
+// outside the transverse grid belong to the first band.  Cell i of the
+// grid is local cell i - base, base = first local row * ny.
+struct BandAcc {
+  unsigned* lo;  // low words; the high words at lo + hi_off
+  int hi_off;
+  int base;
+  int r0, r1;
+  bool first;
+  __device__ __forceinline__ void add(int i, unsigned long long v) const {
+    i -= base;
+    unsigned l = (unsigned)v, h = (unsigned)(v >> 32);
+    unsigned old = atomicAdd(lo + i, l);
+    h += (old + l < old) ? 1u : 0u;
+    if (h) atomicAdd(lo + hi_off + i, h);
+  }
+  __device__ __forceinline__ unsigned long long get(int i) const {
+    return ((unsigned long long)lo[hi_off + i] << 32) | lo[i];
+  }
+  __device__ __forceinline__ bool owns(int ix) const { return ix >= r0 && ix < r1; }
+  __device__ __forceinline__ bool owns_outside() const { return first; }
 };
 
 // Plain form: contributions are rounded to a fixed-point grid of step 1/S
 // (S a power of two with S * total macrosize <= 2^62) and summed as 64-bit
 // integers, so the deposit is exact and independent of summation order.
-template <bool SHARED>
-__device__ __forceinline__ void deposit_plain(const DepConst& d, const GridAcc<SHARED>& rho,
-                                              const GridAcc<SHARED>& zg, double x, double y, double z, double ms) {
-  if (!(x < d.xmin || x > d.xmax || y < d.ymin || y > d.ymax)) {
-    int ix, iy;
-    double fx, fy;
-    tsc_index<double>((x - d.xmin) * d.inv_dx, d.nx, ix, fx);
+template <class RA, class ZA>
+__device__ __forceinline__ void deposit_plain(const DepConst& d, const RA& rho, const ZA& zg, double x, double y,
+                                              double z, double ms) {
+  const bool in2 = !(x < d.xmin || x > d.xmax || y < d.ymin || y > d.ymax);
+  int ix = 0, iy;
+  double fx, fy;
+  if (in2) tsc_index<double>((x - d.xmin) * d.inv_dx, d.nx, ix, fx);
+  if (in2 ? !rho.owns(ix) : !rho.owns_outside()) return;  // another block's particle
+  if (in2) {
     tsc_index<double>((y - d.ymin) * d.inv_dy, d.ny, iy, fy);
     double wxm, wx0, wxp, wym, wy0, wyp;
     tsc_weights<double>(fx, wxm, wx0, wxp);
@@ -557,9 +590,9 @@ __device__ __forceinline__ void load_dep_fix(DepFix& d, const ScState* st, int n
 // macrosize multiplies the grid afterwards).  Returns false when the
 // particle needs the FP64 path (never for finite coordinates in range).
 // SHARED: the grids are block-private shared memory.
-template <bool SHARED>
-__device__ __forceinline__ bool deposit_fixed(const DepFix& d, const GridAcc<SHARED>& rho,
-                                              const GridAcc<SHARED>& zg, double x, double y, double z) {
+template <class RA, class ZA>
+__device__ __forceinline__ bool deposit_fixed(const DepFix& d, const RA& rho, const ZA& zg, double x, double y,
+                                              double z) {
   unsigned long long kx = dkey(x), ky = dkey(y), kz = dkey(z);
   bool in2 = kx >= d.kxmin && kx <= d.kxmax && ky >= d.kymin && ky <= d.kymax;
   bool in1 = kz >= d.kzmin && kz <= d.kzmax;
@@ -572,6 +605,7 @@ __device__ __forceinline__ bool deposit_fixed(const DepFix& d, const GridAcc<SHA
   if (in1 && d.nz > 1) {
     if (!g1_fixed(fma(z, d.az, d.cz), d.nz, d.Fz, i0, ip, wp)) return false;
   }
+  if (in2 ? !rho.owns(ix) : !rho.owns_outside()) return true;  // another block's particle
   if (in2) {
     long long wx[3], wy[3];
     tsc_w_fixed(fx, wx);

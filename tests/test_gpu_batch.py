@@ -16,8 +16,9 @@ from helpers import TOL_COORD, coord_err
 pytestmark = pytest.mark.gpu
 
 # (particles, grid, quadrupole k1, macrosize)
+# (the 256x256 grid is too large for one block's shared memory: row-band deposit)
 SCAN = [(3000, (32, 32, 8), 0.35, 2e9), (20000, (64, 64, 16), 0.5, 5e8), (7000, (32, 32, 8), 0.6, 1e9),
-        (40000, (64, 64, 16), 0.45, 1e8), (2500, (32, 32, 8), 0.7, 4e9)]
+        (40000, (64, 64, 16), 0.45, 1e8), (2500, (32, 32, 8), 0.7, 4e9), (30000, (256, 256, 8), 0.55, 1e9)]
 
 
 def member(k, seed_base=500):
@@ -44,8 +45,8 @@ def test_batch_equals_single_bunch_tracking_with_the_same_fft_schedule():
     members = [member(k) for k in range(len(SCAN))]
     bb = BunchBatch([(b, lat) for _, b, lat in members])
     cls = bb.classes()
-    assert sorted(c["grid"] for c in cls) == [(32, 32, 8), (64, 64, 16)]
-    assert sorted(c["members"] for c in cls) == [2, 3]
+    assert sorted(c["grid"] for c in cls) == [(32, 32, 8), (64, 64, 16), (256, 256, 8)]
+    assert sorted(c["members"] for c in cls) == [1, 2, 3]
     for k, c in enumerate(cls):
         bb._batch.set_tuning(k, 768, 8192, 512, 4096, 1)
     bb.trackTurns(3)
