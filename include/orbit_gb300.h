@@ -335,6 +335,32 @@ int orbit_batch_class(const orbit_batch_t* b, int cls, int* grid, int* members, 
  * autotuning runs afterwards. */
 int orbit_batch_set_tuning(orbit_batch_t* b, int cls, const int* tuning);
 
+/* ---- learned denoising closure (no counterpart in the reference) ----
+ * A 4-level convolutional encoder-decoder (channels 16-64, 302,561
+ * parameters; BF16 convolution weights, FP32 activations and accumulation)
+ * mapping the normalised charge density of a few-macroparticle deposit to
+ * the density of a deposit with many more macroparticles on the same grid.
+ * Images are NCHW FP32 device arrays of h x w (multiples of 8). */
+typedef struct orbit_denoiser orbit_denoiser_t;
+int orbit_denoiser_create(orbit_denoiser_t** out, int max_batch, int h, int w, unsigned long long seed);
+int orbit_denoiser_destroy(orbit_denoiser_t* d);
+int orbit_denoiser_info(const orbit_denoiser_t* d, int* nparam, int* h, int* w, int* max_batch);
+/* FP32 parameters (the master copy Adam updates) to/from host memory;
+ * setting them resets the Adam moments. */
+int orbit_denoiser_get_params(orbit_denoiser_t* d, float* host);
+int orbit_denoiser_set_params(orbit_denoiser_t* d, const float* host);
+/* dev_out = network(dev_in) for nb images on `stream` (NULL: the
+ * denoiser's own stream). */
+int orbit_denoiser_forward(orbit_denoiser_t* d, const float* dev_in, float* dev_out, int nb, void* stream);
+/* One Adam step (learning rate lr) on the mean squared error of nb pairs;
+ * *loss (if not NULL) receives the loss before the step (waits). */
+int orbit_denoiser_train_step(orbit_denoiser_t* d, const float* dev_in, const float* dev_target, int nb, float lr,
+                              float* loss);
+/* Loss, parameter gradients (host, nparam floats) and, if dev_out is not
+ * NULL, the network output for nb pairs, without an update (waits). */
+int orbit_denoiser_gradients(orbit_denoiser_t* d, const float* dev_in, const float* dev_target, int nb, float* grads,
+                             float* loss, float* dev_out);
+
 #ifdef __cplusplus
 }
 #endif

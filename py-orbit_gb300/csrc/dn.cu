@@ -1,0 +1,721 @@
+// Learned denoising closure of the 2.5D space-charge kick: a 4-level
+// convolutional encoder-decoder that maps the charge density deposited by
+// few macroparticles to the density many more macroparticles of the same
+// beam give on the same grid; the plain FFT Poisson solve turns it into the
+// potential.  No counterpart in the reference (a form of this library).
+//
+// Network (H x W input, H and W multiples of 8; channels in brackets):
+//   x0[1] -> conv a1[16] -> conv s1[16] -> pool -> conv a2[32] -> conv s2[32]
+//   -> pool -> conv a3[64] -> conv s3[64] -> pool -> conv a4[64] -> conv b4[64]
+//   -> up + s3 [128] -> conv d3a[64] -> conv d3[64] -> up + s2 [96]
+//   -> conv d2a[32] -> conv d2[32] -> up + s1 [48] -> conv d1a[16]
+//   -> conv d1[16] -> 1x1 conv [1] + x0
+// Every 3x3 convolution (zero padding) is followed by a ReLU; pooling is a
+// 2x2 average, "up" a 2x nearest-neighbour upsample concatenated with the
+// skip tensor.  302,561 parameters.  Convolution weights are BF16 (an FP32
+// master copy is what Adam updates), biases FP32; activations and all
+// accumulation FP32.  Training: mean squared error, Adam.
+//
+// Tensors are NCHW FP32 in device memory.
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+
+namespace orbit {
+
+// ---------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------
+static const int kT = 16;   // output tile edge
+static const int kCo = 16;  // output channels per block
+static const int kCi = 8;   // input channels per shared-memory chunk
+
+// 3x3 convolution, zero padding, one 16x16 tile of 16 output channels per
+// block: out[n][o][y][x] = b[o] + sum_i sum_k in[n][i][y+ky-1][x+kx-1] Wt(o,i,k).
+// TRANS (data gradient): Wt(o,i,k) = W[i][o][8-k] with W stored for the
+// forward layer ([cin][cout][9] here), no bias, no ReLU.
+template <bool TRANS, bool BIAS_RELU>
+__global__ void __launch_bounds__(256) k_conv3(const float* __restrict__ in, int cin,
+                                               const __nv_bfloat16* __restrict__ w, const float* __restrict__ bias,
+                                               float* __restrict__ out, int cout, int H, int W) {
+  __shared__ float s_in[kCi][kT + 2][kT + 2];
+  __shared__ float s_w[kCo][kCi][9];
+  const int tiles_x = (W + kT - 1) / kT;
+  const int tx0 = (blockIdx.x % tiles_x) * kT, ty0 = (blockIdx.x / tiles_x) * kT;
+  const int co0 = blockIdx.y * kCo;
+  const int n = blockIdx.z;
+  const int tx = threadIdx.x % kT, ty = threadIdx.x / kT;
+  float acc[kCo];
+#pragma unroll
+  for (int o = 0; o < kCo; ++o) acc[o] = 0.f;
+  for (int ci0 = 0; ci0 < cin; ci0 += kCi) {
+    for (int idx = threadIdx.x; idx < kCi * (kT + 2) * (kT + 2); idx += blockDim.x) {
+      int c = idx / ((kT + 2) * (kT + 2)), r = idx % ((kT + 2) * (kT + 2));
+      int yy = r / (kT + 2), xx = r % (kT + 2);
+      int gy = ty0 + yy - 1, gx = tx0 + xx - 1, ci = ci0 + c;
+      float v = 0.f;
+      if (ci < cin && gy >= 0 && gy < H && gx >= 0 && gx < W) v = in[(((size_t)n * cin + ci) * H + gy) * W + gx];
+      s_in[c][yy][xx] = v;
+    }
+    for (int idx = threadIdx.x; idx < kCo * kCi * 9; idx += blockDim.x) {
+      int o = idx / (kCi * 9), r = idx % (kCi * 9);
+      int c = r / 9, k = r % 9;
+      int co = co0 + o, ci = ci0 + c;
+      float v = 0.f;
+      if (co < cout && ci < cin)
+        v = TRANS ? __bfloat162float(w[((size_t)ci * cout + co) * 9 + (8 - k)])
+                  : __bfloat162float(w[((size_t)co * cin + ci) * 9 + k]);
+      s_w[o][c][k] = v;
+    }
+    __syncthreads();
+#pragma unroll 2
+    for (int c = 0; c < kCi; ++c) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) {
+        float v = s_in[c][ty + k / 3][tx + k % 3];
+#pragma unroll
+        for (int o = 0; o < kCo; ++o) acc[o] = fmaf(v, s_w[o][c][k], acc[o]);
+      }
+    }
+    __syncthreads();
+  }
+  const int y = ty0 + ty, x = tx0 + tx;
+  if (y < H && x < W) {
+#pragma unroll
+    for (int o = 0; o < kCo; ++o) {
+      int co = co0 + o;
+      if (co < cout) {
+        float v = acc[o];
+        if (BIAS_RELU) v = fmaxf(v + bias[co], 0.f);
+        out[(((size_t)n * cout + co) * H + y) * W + x] = v;
+      }
+    }
+  }
+}
+
+// Weight and bias gradients of a 3x3 convolution:
+// dW[o][i][k] += sum_{n,y,x} dy[n][o][y][x] x[n][i][y+ky-1][x+kx-1],
+// db[o] += sum dy[n][o].  Block: 16 output x 8 input channels, the 16x16
+// tiles t = blockIdx.y, blockIdx.y + gridDim.y, ... of all images.
+__global__ void __launch_bounds__(256) k_conv3_wgrad(const float* __restrict__ x, int cin,
+                                                     const float* __restrict__ dy, int cout, int H, int W, int N,
+                                                     float* __restrict__ dw, float* __restrict__ db) {
+  __shared__ float s_dy[kCo][kT * kT];
+  __shared__ float s_x[kCi][kT + 2][kT + 2];
+  const int itiles = (cin + kCi - 1) / kCi;
+  const int co0 = (blockIdx.x / itiles) * kCo, ci0 = (blockIdx.x % itiles) * kCi;
+  const int tiles_x = (W + kT - 1) / kT, tiles_y = (H + kT - 1) / kT;
+  const int T = N * tiles_x * tiles_y;
+  const int nel = kCo * kCi * 9;  // 1152 weights per block
+  float acc[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  float bacc = 0.f;
+  for (int t = blockIdx.y; t < T; t += gridDim.y) {
+    const int n = t / (tiles_x * tiles_y), r = t % (tiles_x * tiles_y);
+    const int tx0 = (r % tiles_x) * kT, ty0 = (r / tiles_x) * kT;
+    for (int idx = threadIdx.x; idx < kCo * kT * kT; idx += blockDim.x) {
+      int o = idx / (kT * kT), p = idx % (kT * kT);
+      int yy = ty0 + p / kT, xx = tx0 + p % kT, co = co0 + o;
+      float v = 0.f;
+      if (co < cout && yy < H && xx < W) v = dy[(((size_t)n * cout + co) * H + yy) * W + xx];
+      s_dy[o][p] = v;
+    }
+    for (int idx = threadIdx.x; idx < kCi * (kT + 2) * (kT + 2); idx += blockDim.x) {
+      int c = idx / ((kT + 2) * (kT + 2)), rr = idx % ((kT + 2) * (kT + 2));
+      int yy = rr / (kT + 2), xx = rr % (kT + 2);
+      int gy = ty0 + yy - 1, gx = tx0 + xx - 1, ci = ci0 + c;
+      float v = 0.f;
+      if (ci < cin && gy >= 0 && gy < H && gx >= 0 && gx < W) v = x[(((size_t)n * cin + ci) * H + gy) * W + gx];
+      s_x[c][yy][xx] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+      int e = threadIdx.x + q * blockDim.x;
+      if (e < nel) {
+        int o = e / (kCi * 9), rr = e % (kCi * 9);
+        int c = rr / 9, k = rr % 9, ky = k / 3, kx = k % 3;
+        float s = 0.f;
+        for (int p = 0; p < kT * kT; ++p) s = fmaf(s_dy[o][p], s_x[c][p / kT + ky][p % kT + kx], s);
+        acc[q] += s;
+      }
+    }
+    if (ci0 == 0 && threadIdx.x < kCo)
+      for (int p = 0; p < kT * kT; ++p) bacc += s_dy[threadIdx.x][p];
+    __syncthreads();
+  }
+#pragma unroll
+  for (int q = 0; q < 5; ++q) {
+    int e = threadIdx.x + q * blockDim.x;
+    if (e < nel) {
+      int o = e / (kCi * 9), rr = e % (kCi * 9);
+      int c = rr / 9, k = rr % 9;
+      int co = co0 + o, ci = ci0 + c;
+      if (co < cout && ci < cin) atomicAdd(dw + ((size_t)co * cin + ci) * 9 + k, acc[q]);
+    }
+  }
+  if (ci0 == 0 && threadIdx.x < kCo && co0 + (int)threadIdx.x < cout) atomicAdd(db + co0 + threadIdx.x, bacc);
+}
+
+// dy *= (y > 0): the gradient through the ReLU that produced y.
+__global__ void k_relu_bwd(float* __restrict__ dy, const float* __restrict__ y, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    if (!(y[i] > 0.f)) dy[i] = 0.f;
+}
+
+// 2x2 average pooling of [N*C][H][W] into [N*C][H/2][W/2].
+__global__ void k_pool(const float* __restrict__ in, float* __restrict__ out, int NC, int H, int W) {
+  const int h = H / 2, w = W / 2;
+  size_t tot = (size_t)NC * h * w;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < tot; i += (size_t)gridDim.x * blockDim.x) {
+    int x = (int)(i % w), y = (int)((i / w) % h);
+    size_t nc = i / ((size_t)w * h);
+    const float* p = in + (nc * H + 2 * y) * W + 2 * x;
+    out[i] = 0.25f * (p[0] + p[1] + p[W] + p[W + 1]);
+  }
+}
+
+// din[n][c][y][x] += dout[n][c][y/2][x/2] / 4.
+__global__ void k_pool_bwd(const float* __restrict__ dout, float* __restrict__ din, int NC, int H, int W) {
+  const int h = H / 2, w = W / 2;
+  size_t tot = (size_t)NC * H * W;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < tot; i += (size_t)gridDim.x * blockDim.x) {
+    int x = (int)(i % W), y = (int)((i / W) % H);
+    size_t nc = i / ((size_t)W * H);
+    din[i] += 0.25f * dout[(nc * h + y / 2) * w + x / 2];
+  }
+}
+
+// out = [up2(a) (ca channels at H/2 x W/2), b (cb channels)] at H x W.
+__global__ void k_upcat(const float* __restrict__ a, int ca, const float* __restrict__ b, int cb,
+                        float* __restrict__ out, int N, int H, int W) {
+  const int C = ca + cb;
+  size_t tot = (size_t)N * C * H * W;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < tot; i += (size_t)gridDim.x * blockDim.x) {
+    int x = (int)(i % W), y = (int)((i / W) % H);
+    int c = (int)((i / ((size_t)W * H)) % C);
+    size_t n = i / ((size_t)W * H * C);
+    out[i] = c < ca ? a[((n * ca + c) * (H / 2) + y / 2) * (W / 2) + x / 2]
+                    : b[((n * cb + (c - ca)) * H + y) * W + x];
+  }
+}
+
+// Gradients of k_upcat: da = 2x2 sums of dout's first ca channels (written),
+// db += dout's last cb channels.
+__global__ void k_upcat_bwd(const float* __restrict__ dout, int ca, float* __restrict__ da, int cb,
+                            float* __restrict__ db, int N, int H, int W) {
+  const int C = ca + cb, h = H / 2, w = W / 2;
+  size_t ta = (size_t)N * ca * h * w, tb = (size_t)N * cb * H * W;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ta + tb; i += (size_t)gridDim.x * blockDim.x) {
+    if (i < ta) {
+      int x = (int)(i % w), y = (int)((i / w) % h);
+      int c = (int)((i / ((size_t)w * h)) % ca);
+      size_t n = i / ((size_t)w * h * ca);
+      const float* p = dout + ((n * C + c) * H + 2 * y) * W + 2 * x;
+      da[i] = p[0] + p[1] + p[W] + p[W + 1];
+    } else {
+      size_t j = i - ta;
+      int x = (int)(j % W), y = (int)((j / W) % H);
+      int c = (int)((j / ((size_t)W * H)) % cb);
+      size_t n = j / ((size_t)W * H * cb);
+      db[j] += dout[((n * C + ca + c) * H + y) * W + x];
+    }
+  }
+}
+
+// y[n][0] = x0[n][0] + b + sum_c w[c] h[n][c] (1x1 output convolution plus
+// the input: the network predicts the correction to the noisy density).
+__global__ void k_out(const float* __restrict__ h, int C, const float* __restrict__ w, const float* __restrict__ b,
+                      const float* __restrict__ x0, float* __restrict__ y, int N, int HW) {
+  size_t tot = (size_t)N * HW;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < tot; i += (size_t)gridDim.x * blockDim.x) {
+    size_t n = i / HW, p = i % HW;
+    float s = x0[i] + b[0];
+    for (int c = 0; c < C; ++c) s = fmaf(w[c], h[(n * C + c) * HW + p], s);
+    y[i] = s;
+  }
+}
+
+// Gradients of k_out: dh[n][c] = dy w[c]; dw[c] += sum dy h[c]; db += sum dy
+// (block partial sums, one atomic per block and channel).
+__global__ void k_out_bwd(const float* __restrict__ dy, const float* __restrict__ h, int C,
+                          const float* __restrict__ w, float* __restrict__ dh, float* __restrict__ dw,
+                          float* __restrict__ db, int N, int HW) {
+  __shared__ float s_red[32][17];
+  float pw[16], pb = 0.f;
+  for (int c = 0; c < 16; ++c) pw[c] = 0.f;
+  size_t tot = (size_t)N * HW;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < tot; i += (size_t)gridDim.x * blockDim.x) {
+    size_t n = i / HW, p = i % HW;
+    float g = dy[i];
+    pb += g;
+    for (int c = 0; c < C && c < 16; ++c) {
+      dh[(n * C + c) * HW + p] = g * w[c];
+      pw[c] = fmaf(g, h[(n * C + c) * HW + p], pw[c]);
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    pb += __shfl_xor_sync(0xffffffffu, pb, off);
+    for (int c = 0; c < 16; ++c) pw[c] += __shfl_xor_sync(0xffffffffu, pw[c], off);
+  }
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) {
+    for (int c = 0; c < 16; ++c) s_red[wid][c] = pw[c];
+    s_red[wid][16] = pb;
+  }
+  __syncthreads();
+  if (threadIdx.x < 17) {
+    float s = 0.f;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += s_red[q][threadIdx.x];
+    if (threadIdx.x < 16) {
+      if ((int)threadIdx.x < C) atomicAdd(dw + threadIdx.x, s);
+    } else {
+      atomicAdd(db, s);
+    }
+  }
+}
+
+// Mean squared error: loss += sum (y - t)^2 / n, dy = 2 (y - t) / n.
+__global__ void k_mse(const float* __restrict__ y, const float* __restrict__ t, float* __restrict__ dy, size_t n,
+                      float* __restrict__ loss) {
+  float s = 0.f;
+  const float inv = 1.0f / (float)n;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    float d = y[i] - t[i];
+    s = fmaf(d, d, s);
+    dy[i] = 2.f * d * inv;
+  }
+  for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+  if ((threadIdx.x & 31) == 0) atomicAdd(loss, s * inv);
+}
+
+// Adam (Kingma & Ba, 2015) on the FP32 master parameters, then the BF16
+// copies of the convolution weights; the gradients are cleared.
+__global__ void k_adam(float* __restrict__ p, float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
+                       __nv_bfloat16* __restrict__ pb, const unsigned char* __restrict__ is_w, size_t n, float lr,
+                       float b1, float b2, float eps, float c1, float c2) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    float gi = g[i];
+    float mi = b1 * m[i] + (1.f - b1) * gi;
+    float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    float w = p[i] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+    p[i] = w;
+    if (is_w[i]) pb[i] = __float2bfloat16_rn(w);
+    g[i] = 0.f;
+  }
+}
+
+__global__ void k_to_bf16(const float* __restrict__ p, __nv_bfloat16* __restrict__ pb,
+                          const unsigned char* __restrict__ is_w, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    pb[i] = is_w[i] ? __float2bfloat16_rn(p[i]) : __float2bfloat16_rn(0.f);
+}
+
+// ---------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------
+static int grid_1d(size_t n) {
+  size_t b = (n + 255) / 256;
+  size_t cap = (size_t)num_sms() * 8;
+  return (int)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
+struct Conv {
+  int cin, cout;
+  size_t w_off, b_off;  // offsets in the parameter array
+};
+
+}  // namespace orbit
+
+using namespace orbit;
+
+struct orbit_denoiser {
+  int H = 0, W = 0, maxb = 0;
+  std::vector<Conv> conv;   // 14 3x3 convolutions in network order
+  size_t out_w = 0, out_b = 0, nparam = 0;
+  float* d_p = nullptr;     // FP32 master parameters
+  __nv_bfloat16* d_pb = nullptr;  // BF16 copies (convolution weights; biases unused)
+  float* d_g = nullptr;
+  float* d_m = nullptr;
+  float* d_v = nullptr;
+  unsigned char* d_isw = nullptr;
+  long long step = 0;
+  // activations (maxb images) and their gradients
+  std::vector<float*> act, grad;
+  float* d_loss = nullptr;
+  float* d_scratch = nullptr;  // data gradient of the widest convolution input
+  cudaStream_t stream = nullptr;
+};
+
+namespace orbit {
+
+// activation indices
+enum {
+  X0, A1, S1, P1, A2, S2, P2, A3, S3, P3, A4, B4, C3, D3A, D3, C2, D2A, D2, C1, D1A, D1, Y, NACT
+};
+
+static void act_shape(const orbit_denoiser_t* d, int a, int* c, int* h, int* w) {
+  const int H = d->H, W = d->W;
+  static const int ch[NACT] = {1, 16, 16, 16, 32, 32, 32, 64, 64, 64, 64, 64, 128, 64, 64, 96, 32, 32, 48, 16, 16, 1};
+  static const int lv[NACT] = {0, 0, 0, 1, 1, 1, 2, 2, 2, 3, 3, 3, 2, 2, 2, 1, 1, 1, 0, 0, 0, 0};
+  *c = ch[a];
+  *h = H >> lv[a];
+  *w = W >> lv[a];
+}
+
+// The 3x3 layers: (input activation, output activation, conv index).
+struct Step3 {
+  int in, out, ci;
+};
+static const Step3 kSteps[14] = {{X0, A1, 0},   {A1, S1, 1},   {P1, A2, 2},   {A2, S2, 3},   {P2, A3, 4},
+                                 {A3, S3, 5},   {P3, A4, 6},   {A4, B4, 7},   {C3, D3A, 8},  {D3A, D3, 9},
+                                 {C2, D2A, 10}, {D2A, D2, 11}, {C1, D1A, 12}, {D1A, D1, 13}};
+
+static size_t act_size(const orbit_denoiser_t* d, int a, int nb) {
+  int c, h, w;
+  act_shape(d, a, &c, &h, &w);
+  return (size_t)nb * c * h * w;
+}
+
+static int conv_fwd(orbit_denoiser_t* d, const Step3& s, int nb, cudaStream_t st) {
+  const Conv& cv = d->conv[s.ci];
+  int c, h, w;
+  act_shape(d, s.out, &c, &h, &w);
+  dim3 g(((w + kT - 1) / kT) * ((h + kT - 1) / kT), (cv.cout + kCo - 1) / kCo, nb);
+  k_conv3<false, true><<<g, 256, 0, st>>>(d->act[s.in], cv.cin, d->d_pb + cv.w_off, d->d_p + cv.b_off,
+                                          d->act[s.out], cv.cout, h, w);
+  ORBIT_LAUNCH_CHECK("denoiser conv");
+  return ORBIT_OK;
+}
+
+static int forward(orbit_denoiser_t* d, int nb, cudaStream_t st) {
+  auto pool = [&](int a, int b) -> int {
+    int c, h, w;
+    act_shape(d, a, &c, &h, &w);
+    k_pool<<<grid_1d(act_size(d, b, nb)), 256, 0, st>>>(d->act[a], d->act[b], nb * c, h, w);
+    ORBIT_LAUNCH_CHECK("denoiser pool");
+    return ORBIT_OK;
+  };
+  auto upcat = [&](int a, int b, int out) -> int {
+    int ca, cb, h, w, t;
+    act_shape(d, a, &ca, &t, &t);
+    act_shape(d, b, &cb, &h, &w);
+    k_upcat<<<grid_1d(act_size(d, out, nb)), 256, 0, st>>>(d->act[a], ca, d->act[b], cb, d->act[out], nb, h, w);
+    ORBIT_LAUNCH_CHECK("denoiser upcat");
+    return ORBIT_OK;
+  };
+  int rc = 0;
+  rc = rc ? rc : conv_fwd(d, kSteps[0], nb, st);
+  rc = rc ? rc : conv_fwd(d, kSteps[1], nb, st);
+  rc = rc ? rc : pool(S1, P1);
+  rc = rc ? rc : conv_fwd(d, kSteps[2], nb, st);
+  rc = rc ? rc : conv_fwd(d, kSteps[3], nb, st);
+  rc = rc ? rc : pool(S2, P2);
+  rc = rc ? rc : conv_fwd(d, kSteps[4], nb, st);
+  rc = rc ? rc : conv_fwd(d, kSteps[5], nb, st);
+  rc = rc ? rc : pool(S3, P3);
+  rc = rc ? rc : conv_fwd(d, kSteps[6], nb, st);
+  rc = rc ? rc : conv_fwd(d, kSteps[7], nb, st);
+  rc = rc ? rc : upcat(B4, S3, C3);
+  rc = rc ? rc : conv_fwd(d, kSteps[8], nb, st);
+  rc = rc ? rc : conv_fwd(d, kSteps[9], nb, st);
+  rc = rc ? rc : upcat(D3, S2, C2);
+  rc = rc ? rc : conv_fwd(d, kSteps[10], nb, st);
+  rc = rc ? rc : conv_fwd(d, kSteps[11], nb, st);
+  rc = rc ? rc : upcat(D2, S1, C1);
+  rc = rc ? rc : conv_fwd(d, kSteps[12], nb, st);
+  rc = rc ? rc : conv_fwd(d, kSteps[13], nb, st);
+  if (rc) return rc;
+  const size_t hw = (size_t)d->H * d->W;
+  k_out<<<grid_1d(nb * hw), 256, 0, st>>>(d->act[D1], 16, d->d_p + d->out_w, d->d_p + d->out_b, d->act[X0],
+                                          d->act[Y], nb, (int)hw);
+  ORBIT_LAUNCH_CHECK("denoiser out");
+  return ORBIT_OK;
+}
+
+// Backward of one 3x3 layer: grad[out] holds dL/d(output after ReLU); it
+// becomes dL/d(pre-activation), the weight and bias gradients accumulate,
+// and the data gradient is written to grad[in] (no 3x3 layer's input has a
+// second consumer; the input image gets none).
+static int conv_bwd(orbit_denoiser_t* d, const Step3& s, int nb, cudaStream_t st) {
+  const Conv& cv = d->conv[s.ci];
+  int c, h, w;
+  act_shape(d, s.out, &c, &h, &w);
+  size_t n_out = act_size(d, s.out, nb);
+  k_relu_bwd<<<grid_1d(n_out), 256, 0, st>>>(d->grad[s.out], d->act[s.out], n_out);
+  const int tiles = ((w + kT - 1) / kT) * ((h + kT - 1) / kT);
+  const int ttot = tiles * nb;
+  const int split = ttot < 64 ? ttot : 64;
+  dim3 gw(((cv.cout + kCo - 1) / kCo) * ((cv.cin + kCi - 1) / kCi), split);
+  k_conv3_wgrad<<<gw, 256, 0, st>>>(d->act[s.in], cv.cin, d->grad[s.out], cv.cout, h, w, nb, d->d_g + cv.w_off,
+                                    d->d_g + cv.b_off);
+  if (s.in != X0) {
+    // data gradient: dy convolved with the flipped, transposed kernel
+    dim3 gd(tiles, (cv.cin + kCo - 1) / kCo, nb);
+    k_conv3<true, false><<<gd, 256, 0, st>>>(d->grad[s.out], cv.cout, d->d_pb + cv.w_off, nullptr, d->grad[s.in],
+                                             cv.cin, h, w);
+  }
+  ORBIT_LAUNCH_CHECK("denoiser conv backward");
+  return ORBIT_OK;
+}
+
+// grad[Y] holds dL/dy; every parameter gradient is accumulated into d_g.
+static int backward(orbit_denoiser_t* d, int nb, cudaStream_t st) {
+  const size_t hw = (size_t)d->H * d->W;
+  // the skip tensors collect gradients from the pooling and the decoder
+  for (int a : {S1, S2, S3}) ORBIT_CUDA(cudaMemsetAsync(d->grad[a], 0, sizeof(float) * act_size(d, a, nb), st));
+  k_out_bwd<<<grid_1d(nb * hw), 256, 0, st>>>(d->grad[Y], d->act[D1], 16, d->d_p + d->out_w, d->grad[D1],
+                                              d->d_g + d->out_w, d->d_g + d->out_b, nb, (int)hw);
+  ORBIT_LAUNCH_CHECK("denoiser out backward");
+  auto upcat_bwd = [&](int out, int a, int b) -> int {
+    int ca, cb, h, w, t;
+    act_shape(d, a, &ca, &t, &t);
+    act_shape(d, b, &cb, &h, &w);
+    k_upcat_bwd<<<grid_1d(act_size(d, out, nb)), 256, 0, st>>>(d->grad[out], ca, d->grad[a], cb, d->grad[b], nb, h,
+                                                                 w);
+    ORBIT_LAUNCH_CHECK("denoiser upcat backward");
+    return ORBIT_OK;
+  };
+  auto pool_bwd = [&](int pooled, int full) -> int {
+    int c, h, w;
+    act_shape(d, full, &c, &h, &w);
+    k_pool_bwd<<<grid_1d(act_size(d, full, nb)), 256, 0, st>>>(d->grad[pooled], d->grad[full], nb * c, h, w);
+    ORBIT_LAUNCH_CHECK("denoiser pool backward");
+    return ORBIT_OK;
+  };
+  int rc = 0;
+  rc = rc ? rc : conv_bwd(d, kSteps[13], nb, st);
+  rc = rc ? rc : conv_bwd(d, kSteps[12], nb, st);
+  rc = rc ? rc : upcat_bwd(C1, D2, S1);
+  rc = rc ? rc : conv_bwd(d, kSteps[11], nb, st);
+  rc = rc ? rc : conv_bwd(d, kSteps[10], nb, st);
+  rc = rc ? rc : upcat_bwd(C2, D3, S2);
+  rc = rc ? rc : conv_bwd(d, kSteps[9], nb, st);
+  rc = rc ? rc : conv_bwd(d, kSteps[8], nb, st);
+  rc = rc ? rc : upcat_bwd(C3, B4, S3);
+  rc = rc ? rc : conv_bwd(d, kSteps[7], nb, st);
+  rc = rc ? rc : conv_bwd(d, kSteps[6], nb, st);
+  rc = rc ? rc : pool_bwd(P3, S3);
+  rc = rc ? rc : conv_bwd(d, kSteps[5], nb, st);
+  rc = rc ? rc : conv_bwd(d, kSteps[4], nb, st);
+  rc = rc ? rc : pool_bwd(P2, S2);
+  rc = rc ? rc : conv_bwd(d, kSteps[3], nb, st);
+  rc = rc ? rc : conv_bwd(d, kSteps[2], nb, st);
+  rc = rc ? rc : pool_bwd(P1, S1);
+  rc = rc ? rc : conv_bwd(d, kSteps[1], nb, st);
+  rc = rc ? rc : conv_bwd(d, kSteps[0], nb, st);
+  return rc;
+}
+
+// Forward, loss and backward of nb pairs already in act[X0] and `target`.
+static int loss_and_grads(orbit_denoiser_t* d, const float* target, int nb, cudaStream_t st) {
+  int rc = forward(d, nb, st);
+  if (rc) return rc;
+  ORBIT_CUDA(cudaMemsetAsync(d->d_loss, 0, sizeof(float), st));
+  size_t n = (size_t)nb * d->H * d->W;
+  k_mse<<<grid_1d(n), 256, 0, st>>>(d->act[Y], target, d->grad[Y], n, d->d_loss);
+  ORBIT_LAUNCH_CHECK("denoiser loss");
+  return backward(d, nb, st);
+}
+
+// SplitMix64 (Steele, Lea, Flood 2014) and Box-Muller normals for the
+// initial weights.
+static uint64_t splitmix64(uint64_t& s) {
+  uint64_t z = (s += 0x9e3779b97f4a7c15ull);
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+static double unit_open(uint64_t& s) { return ((splitmix64(s) >> 11) + 0.5) * (1.0 / 9007199254740992.0); }
+static double normal(uint64_t& s) {
+  double u = unit_open(s), v = unit_open(s);
+  return std::sqrt(-2.0 * std::log(u)) * std::cos(6.283185307179586 * v);
+}
+
+static cudaStream_t stream_of(orbit_denoiser_t* d, void* s) { return s ? (cudaStream_t)s : d->stream; }
+
+static int check_batch(const orbit_denoiser_t* d, int nb) {
+  if (nb < 1 || nb > d->maxb) return set_error(ORBIT_ERR_ARG, "orbit_denoiser: batch size outside 1..max_batch");
+  return ORBIT_OK;
+}
+
+}  // namespace orbit
+
+extern "C" {
+
+int orbit_denoiser_create(orbit_denoiser_t** out, int max_batch, int h, int w, unsigned long long seed) {
+  if (!out || max_batch < 1 || h < 8 || w < 8 || h % 8 || w % 8)
+    return set_error(ORBIT_ERR_ARG, "orbit_denoiser_create: sizes must be multiples of 8 (three 2x2 poolings)");
+  orbit_denoiser_t* d = new orbit_denoiser_t();
+  d->H = h;
+  d->W = w;
+  d->maxb = max_batch;
+  static const int cin[14] = {1, 16, 16, 32, 32, 64, 64, 64, 128, 64, 96, 32, 48, 16};
+  static const int cout[14] = {16, 16, 32, 32, 64, 64, 64, 64, 64, 64, 32, 32, 16, 16};
+  size_t off = 0;
+  for (int k = 0; k < 14; ++k) {
+    Conv c;
+    c.cin = cin[k];
+    c.cout = cout[k];
+    c.w_off = off;
+    off += (size_t)cin[k] * cout[k] * 9;
+    c.b_off = off;
+    off += cout[k];
+    d->conv.push_back(c);
+  }
+  d->out_w = off;
+  off += 16;
+  d->out_b = off;
+  off += 1;
+  d->nparam = off;
+  // initial parameters: He normal for the 3x3 weights, zero biases, small
+  // output weights (the network starts near the identity)
+  std::vector<float> p(off, 0.f);
+  std::vector<unsigned char> isw(off, 0);
+  uint64_t rs = seed ^ 0x6a09e667f3bcc909ull;
+  for (auto& c : d->conv) {
+    double sd = std::sqrt(2.0 / (9.0 * c.cin));
+    for (size_t i = 0; i < (size_t)c.cin * c.cout * 9; ++i) {
+      p[c.w_off + i] = (float)(sd * normal(rs));
+      isw[c.w_off + i] = 1;
+    }
+  }
+  for (int c = 0; c < 16; ++c) p[d->out_w + c] = (float)(0.01 * normal(rs));
+  auto fail = [&](int code) {
+    orbit_denoiser_destroy(d);
+    return code;
+  };
+  cudaError_t e = cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&d->d_p, sizeof(float) * off);
+  if (e == cudaSuccess) e = cudaMalloc(&d->d_pb, sizeof(__nv_bfloat16) * off);
+  if (e == cudaSuccess) e = cudaMalloc(&d->d_g, sizeof(float) * off);
+  if (e == cudaSuccess) e = cudaMalloc(&d->d_m, sizeof(float) * off);
+  if (e == cudaSuccess) e = cudaMalloc(&d->d_v, sizeof(float) * off);
+  if (e == cudaSuccess) e = cudaMalloc(&d->d_isw, off);
+  if (e == cudaSuccess) e = cudaMalloc(&d->d_loss, sizeof(float));
+  if (e == cudaSuccess) e = cudaMemcpy(d->d_p, p.data(), sizeof(float) * off, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d->d_isw, isw.data(), off, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(d->d_g, 0, sizeof(float) * off);
+  if (e == cudaSuccess) e = cudaMemset(d->d_m, 0, sizeof(float) * off);
+  if (e == cudaSuccess) e = cudaMemset(d->d_v, 0, sizeof(float) * off);
+  d->act.assign(NACT, nullptr);
+  d->grad.assign(NACT, nullptr);
+  size_t widest = 0;
+  for (int a = 0; a < NACT && e == cudaSuccess; ++a) {
+    size_t n = act_size(d, a, max_batch);
+    widest = n > widest ? n : widest;
+    e = cudaMalloc(&d->act[a], sizeof(float) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&d->grad[a], sizeof(float) * n);
+  }
+  if (e != cudaSuccess) return fail(cuda_error(e, "orbit_denoiser_create"));
+  k_to_bf16<<<grid_1d(off), 256, 0, d->stream>>>(d->d_p, d->d_pb, d->d_isw, off);
+  e = cudaStreamSynchronize(d->stream);
+  if (e != cudaSuccess) return fail(cuda_error(e, "orbit_denoiser_create"));
+  *out = d;
+  return ORBIT_OK;
+}
+
+int orbit_denoiser_destroy(orbit_denoiser_t* d) {
+  if (!d) return ORBIT_OK;
+  if (d->stream) cudaStreamSynchronize(d->stream);
+  for (float* p : d->act) if (p) cudaFree(p);
+  for (float* p : d->grad) if (p) cudaFree(p);
+  void* bufs[] = {d->d_p, d->d_pb, d->d_g, d->d_m, d->d_v, d->d_isw, d->d_loss, d->d_scratch};
+  for (void* b : bufs) if (b) cudaFree(b);
+  if (d->stream) cudaStreamDestroy(d->stream);
+  delete d;
+  return ORBIT_OK;
+}
+
+int orbit_denoiser_info(const orbit_denoiser_t* d, int* nparam, int* h, int* w, int* max_batch) {
+  if (!d) return set_error(ORBIT_ERR_ARG, "orbit_denoiser_info: bad argument");
+  if (nparam) *nparam = (int)d->nparam;
+  if (h) *h = d->H;
+  if (w) *w = d->W;
+  if (max_batch) *max_batch = d->maxb;
+  return ORBIT_OK;
+}
+
+int orbit_denoiser_get_params(orbit_denoiser_t* d, float* host) {
+  if (!d || !host) return set_error(ORBIT_ERR_ARG, "orbit_denoiser_get_params: bad argument");
+  ORBIT_CUDA(cudaStreamSynchronize(d->stream));
+  ORBIT_CUDA(cudaMemcpy(host, d->d_p, sizeof(float) * d->nparam, cudaMemcpyDeviceToHost));
+  return ORBIT_OK;
+}
+
+int orbit_denoiser_set_params(orbit_denoiser_t* d, const float* host) {
+  if (!d || !host) return set_error(ORBIT_ERR_ARG, "orbit_denoiser_set_params: bad argument");
+  ORBIT_CUDA(cudaStreamSynchronize(d->stream));
+  ORBIT_CUDA(cudaMemcpy(d->d_p, host, sizeof(float) * d->nparam, cudaMemcpyHostToDevice));
+  ORBIT_CUDA(cudaMemset(d->d_m, 0, sizeof(float) * d->nparam));
+  ORBIT_CUDA(cudaMemset(d->d_v, 0, sizeof(float) * d->nparam));
+  d->step = 0;
+  k_to_bf16<<<grid_1d(d->nparam), 256, 0, d->stream>>>(d->d_p, d->d_pb, d->d_isw, d->nparam);
+  ORBIT_LAUNCH_CHECK("orbit_denoiser_set_params");
+  ORBIT_CUDA(cudaStreamSynchronize(d->stream));
+  return ORBIT_OK;
+}
+
+int orbit_denoiser_forward(orbit_denoiser_t* d, const float* dev_in, float* dev_out, int nb, void* stream) {
+  if (!d || !dev_in || !dev_out) return set_error(ORBIT_ERR_ARG, "orbit_denoiser_forward: bad argument");
+  int rc = check_batch(d, nb);
+  if (rc) return rc;
+  cudaStream_t st = stream_of(d, stream);
+  const size_t n = (size_t)nb * d->H * d->W;
+  ORBIT_CUDA(cudaMemcpyAsync(d->act[X0], dev_in, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
+  rc = forward(d, nb, st);
+  if (rc) return rc;
+  ORBIT_CUDA(cudaMemcpyAsync(dev_out, d->act[Y], sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
+  return ORBIT_OK;
+}
+
+int orbit_denoiser_train_step(orbit_denoiser_t* d, const float* dev_in, const float* dev_target, int nb, float lr,
+                              float* loss) {
+  if (!d || !dev_in || !dev_target) return set_error(ORBIT_ERR_ARG, "orbit_denoiser_train_step: bad argument");
+  int rc = check_batch(d, nb);
+  if (rc) return rc;
+  cudaStream_t st = d->stream;
+  const size_t n = (size_t)nb * d->H * d->W;
+  ORBIT_CUDA(cudaMemcpyAsync(d->act[X0], dev_in, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
+  rc = loss_and_grads(d, dev_target, nb, st);
+  if (rc) return rc;
+  d->step += 1;
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  float c1 = (float)(1.0 / (1.0 - std::pow((double)b1, (double)d->step)));
+  float c2 = (float)(1.0 / (1.0 - std::pow((double)b2, (double)d->step)));
+  k_adam<<<grid_1d(d->nparam), 256, 0, st>>>(d->d_p, d->d_g, d->d_m, d->d_v, d->d_pb, d->d_isw, d->nparam, lr, b1,
+                                              b2, eps, c1, c2);
+  ORBIT_LAUNCH_CHECK("denoiser adam");
+  if (loss) {
+    ORBIT_CUDA(cudaMemcpyAsync(loss, d->d_loss, sizeof(float), cudaMemcpyDeviceToHost, st));
+    ORBIT_CUDA(cudaStreamSynchronize(st));
+  }
+  return ORBIT_OK;
+}
+
+int orbit_denoiser_gradients(orbit_denoiser_t* d, const float* dev_in, const float* dev_target, int nb, float* grads,
+                             float* loss, float* dev_out) {
+  if (!d || !dev_in || !dev_target || !grads) return set_error(ORBIT_ERR_ARG, "orbit_denoiser_gradients: bad argument");
+  int rc = check_batch(d, nb);
+  if (rc) return rc;
+  cudaStream_t st = d->stream;
+  const size_t n = (size_t)nb * d->H * d->W;
+  ORBIT_CUDA(cudaMemsetAsync(d->d_g, 0, sizeof(float) * d->nparam, st));
+  ORBIT_CUDA(cudaMemcpyAsync(d->act[X0], dev_in, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
+  rc = loss_and_grads(d, dev_target, nb, st);
+  if (rc) return rc;
+  ORBIT_CUDA(cudaMemcpyAsync(grads, d->d_g, sizeof(float) * d->nparam, cudaMemcpyDeviceToHost, st));
+  if (loss) ORBIT_CUDA(cudaMemcpyAsync(loss, d->d_loss, sizeof(float), cudaMemcpyDeviceToHost, st));
+  if (dev_out) ORBIT_CUDA(cudaMemcpyAsync(dev_out, d->act[Y], sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
+  ORBIT_CUDA(cudaMemsetAsync(d->d_g, 0, sizeof(float) * d->nparam, st));
+  ORBIT_CUDA(cudaStreamSynchronize(st));
+  return ORBIT_OK;
+}
+
+}  // extern "C"

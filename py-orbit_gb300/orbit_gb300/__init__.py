@@ -15,7 +15,7 @@ from . import _native
 from ._native import (FORM_FP32, FORM_PLAIN, OP, OrbitError, SpaceChargeError, Sync, call, load,
                       library_path)
 
-__all__ = ["DeviceBunch", "DeviceSC2p5D", "DeviceSC2p5Drb", "DeviceBoundary", "DeviceProgram", "DeviceBatch", "OrbitError", "SpaceChargeError", "load",
+__all__ = ["DeviceBunch", "DeviceSC2p5D", "DeviceSC2p5Drb", "DeviceBoundary", "DeviceProgram", "DeviceBatch", "DeviceDenoiser", "OrbitError", "SpaceChargeError", "load",
            "FORM_PLAIN", "FORM_FP32", "OP", "library_path", "version"]
 
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -271,6 +271,55 @@ class DeviceBoundary:
         r = ctypes.c_double()
         call("orbit_boundary_rnorm", self.h, ctypes.byref(r))
         return out, r.value
+
+
+class DeviceDenoiser:
+    """The learned denoiser network (orbit_denoiser_*): images are device
+    arrays given by address (e.g. ``tensor.data_ptr()``), NCHW float32."""
+
+    def __init__(self, h: int, w: int, max_batch: int = 1, seed: int = 1):
+        hd = ctypes.c_void_p()
+        call("orbit_denoiser_create", ctypes.byref(hd), int(max_batch), int(h), int(w), int(seed))
+        self.h = hd
+        n, hh, ww, mb = (ctypes.c_int() for _ in range(4))
+        call("orbit_denoiser_info", self.h, ctypes.byref(n), ctypes.byref(hh), ctypes.byref(ww), ctypes.byref(mb))
+        self.nparam, self.height, self.width, self.max_batch = n.value, hh.value, ww.value, mb.value
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h is not None and h.value and _native._lib is not None:
+            _native._lib.orbit_denoiser_destroy(h)
+            self.h = None
+
+    def get_params(self) -> np.ndarray:
+        out = np.empty(self.nparam, dtype=np.float32)
+        call("orbit_denoiser_get_params", self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        if p.shape != (self.nparam,):
+            raise ValueError("expected %d parameters" % self.nparam)
+        call("orbit_denoiser_set_params", self.h, p.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+
+    def forward(self, dev_in: int, dev_out: int, nb: int = 1, stream: int = 0):
+        call("orbit_denoiser_forward", self.h, ctypes.c_void_p(dev_in), ctypes.c_void_p(dev_out), int(nb),
+             ctypes.c_void_p(stream) if stream else None)
+
+    def train_step(self, dev_in: int, dev_target: int, nb: int, lr: float, want_loss: bool = True):
+        loss = ctypes.c_float()
+        call("orbit_denoiser_train_step", self.h, ctypes.c_void_p(dev_in), ctypes.c_void_p(dev_target), int(nb),
+             float(lr), ctypes.byref(loss) if want_loss else None)
+        return loss.value if want_loss else None
+
+    def gradients(self, dev_in: int, dev_target: int, nb: int, dev_out: int = 0):
+        """(loss, gradient of every parameter) without an update."""
+        g = np.empty(self.nparam, dtype=np.float32)
+        loss = ctypes.c_float()
+        call("orbit_denoiser_gradients", self.h, ctypes.c_void_p(dev_in), ctypes.c_void_p(dev_target), int(nb),
+             g.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), ctypes.byref(loss),
+             ctypes.c_void_p(dev_out) if dev_out else None)
+        return loss.value, g
 
 
 class DeviceBatch:

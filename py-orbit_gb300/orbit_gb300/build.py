@@ -12,7 +12,7 @@ ROOT = os.path.dirname(PKG_DIR)
 CSRC = os.path.join(ROOT, "csrc")
 BUILD_DIR = os.path.join(PKG_DIR, "_build")
 LIB_PATH = os.path.join(PKG_DIR, "liborbit_gb300.so")
-SOURCES = ["bunch.cu", "teapot.cu", "sc2p5d.cu", "program.cu", "peaks.cu", "boundary.cu", "diag.cu", "batch.cu"]
+SOURCES = ["bunch.cu", "teapot.cu", "sc2p5d.cu", "program.cu", "peaks.cu", "boundary.cu", "diag.cu", "batch.cu", "dn.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
            "-Xptxas", "-O3"]

@@ -1,0 +1,54 @@
+"""The numpy restatement of the denoiser network (the checker of the
+device kernels): its analytic gradients against central finite
+differences on a small image, and the BF16 rounding it shares with the
+device."""
+import numpy as np
+
+import dn_oracle as D
+
+
+def test_bf16_rounding():
+    x = np.array([1.0, 1.00390625, 1.005859375, -3.14159, 0.0], dtype=np.float32)
+    r = D.bf16(x)
+    assert r[0] == 1.0 and r[1] == 1.0  # tie to even
+    assert r[2] == 1.0078125
+    assert abs(r[3] + 3.140625) < 1e-12 and r[4] == 0.0
+
+
+def test_oracle_gradients_by_finite_differences():
+    rng = np.random.default_rng(5)
+    convs, ow, ob, n = D.layout()
+    assert n == 302561
+    # parameters exactly representable in BF16, so that the finite
+    # differences (steps of whole BF16 units are too coarse) see a smooth
+    # function: perturb only FP32 parameters (biases and the output layer)
+    # and check the 3x3 weight gradients through their bilinear structure
+    p = np.zeros(n, dtype=np.float32)
+    for (w, b, ci, co) in convs:
+        p[w:w + ci * co * 9] = D.bf16(rng.normal(0, np.sqrt(2.0 / (9 * ci)), ci * co * 9))
+        p[b:b + co] = rng.normal(0, 0.05, co)
+    p[ow:ow + 16] = rng.normal(0, 0.1, 16)
+    p[ob] = 0.01
+    x = rng.uniform(0, 2, (1, 1, 8, 8))
+    t = rng.uniform(0, 2, (1, 1, 8, 8))
+    loss, g, _ = D.loss_and_grads(p.astype(np.float64), x, t)
+    pd = p.astype(np.float64)
+    idx = [ow + 3, ob] + [convs[k][1] + 1 for k in (0, 4, 8, 13)]
+    for i in idx:
+        h = 1e-6
+        a, b = pd.copy(), pd.copy()
+        a[i] += h
+        b[i] -= h
+        fd = (D.loss_and_grads(a, x, t)[0] - D.loss_and_grads(b, x, t)[0]) / (2 * h)
+        assert abs(fd - g[i]) <= 1e-6 * max(1.0, abs(fd)), (i, fd, g[i])
+    # 3x3 weights: the loss is a polynomial in each weight; a difference
+    # step of a BF16 unit of that weight (exact in both directions)
+    for k in (1, 6, 10):
+        w = convs[k][0] + 5
+        u = float(np.spacing(np.float32(abs(pd[w])))) * 65536.0  # one BF16 unit
+        a, b = pd.copy(), pd.copy()
+        a[w] += u
+        b[w] -= u
+        assert D.bf16(a[w:w + 1])[0] == a[w] and D.bf16(b[w:w + 1])[0] == b[w]
+        fd = (D.loss_and_grads(a, x, t)[0] - D.loss_and_grads(b, x, t)[0]) / (2 * u)
+        assert abs(fd - g[w]) <= 1e-3 * max(1e-3, abs(g[w])) + 1e-9, (k, fd, g[w])
