@@ -342,6 +342,17 @@ int orbit_batch_set_tuning(orbit_batch_t* b, int cls, const int* tuning);
  * the density of a deposit with many more macroparticles on the same grid.
  * Images are NCHW FP32 device arrays of h x w (multiples of 8). */
 typedef struct orbit_denoiser orbit_denoiser_t;
+/* Training beams (transverse positions): kind 0 Gaussian with rms sx, sy;
+ * 1 KV projection (uniform ellipse, semi-axes 2 sx, 2 sy); 2 waterbag
+ * projection (shadow of a uniform 4D ball, semi-axes sqrt(6) sx, sqrt(6) sy).
+ * Particle i depends only on (seed, i).  orbit_beam_sample writes n
+ * positions to device arrays; orbit_beam_deposit deposits n particles of unit
+ * weight (Grid2D's 9-point weights, FP32) on the node grid
+ * lim = {xmin, xmax, ymin, ymax} of nx x ny into dev_grid (cleared first),
+ * dropping particles outside it.  Both wait for completion. */
+int orbit_beam_sample(double* dev_x, double* dev_y, int n, int kind, double sx, double sy, unsigned long long seed);
+int orbit_beam_deposit(float* dev_grid, int nx, int ny, const double* lim, long long n, int kind, double sx,
+                       double sy, unsigned long long seed);
 int orbit_denoiser_create(orbit_denoiser_t** out, int max_batch, int h, int w, unsigned long long seed);
 int orbit_denoiser_destroy(orbit_denoiser_t* d);
 int orbit_denoiser_info(const orbit_denoiser_t* d, int* nparam, int* h, int* w, int* max_batch);
@@ -350,16 +361,19 @@ int orbit_denoiser_info(const orbit_denoiser_t* d, int* nparam, int* h, int* w, 
 int orbit_denoiser_get_params(orbit_denoiser_t* d, float* host);
 int orbit_denoiser_set_params(orbit_denoiser_t* d, const float* host);
 /* dev_out = network(dev_in) for nb images on `stream` (NULL: the
- * denoiser's own stream). */
+ * denoiser's own stream, a blocking stream ordered with the legacy default
+ * stream). */
 int orbit_denoiser_forward(orbit_denoiser_t* d, const float* dev_in, float* dev_out, int nb, void* stream);
-/* One Adam step (learning rate lr) on the mean squared error of nb pairs;
- * *loss (if not NULL) receives the loss before the step (waits). */
+/* One Adam step (learning rate lr) on the mean squared error of nb pairs,
+ * on `stream` (NULL: the denoiser's own stream; pass the stream that wrote
+ * the inputs); *loss (if not NULL) receives the loss before the step
+ * (waits). */
 int orbit_denoiser_train_step(orbit_denoiser_t* d, const float* dev_in, const float* dev_target, int nb, float lr,
-                              float* loss);
+                              float* loss, void* stream);
 /* Loss, parameter gradients (host, nparam floats) and, if dev_out is not
  * NULL, the network output for nb pairs, without an update (waits). */
 int orbit_denoiser_gradients(orbit_denoiser_t* d, const float* dev_in, const float* dev_target, int nb, float* grads,
-                             float* loss, float* dev_out);
+                             float* loss, float* dev_out, void* stream);
 
 #ifdef __cplusplus
 }

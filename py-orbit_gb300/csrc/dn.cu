@@ -318,6 +318,84 @@ __global__ void k_to_bf16(const float* __restrict__ p, __nv_bfloat16* __restrict
 }
 
 // ---------------------------------------------------------------------
+// training beams: transverse positions of Gaussian, KV and waterbag
+// beams from a counter-based generator (SplitMix64 of seed and particle
+// index), so any particle can be drawn by any thread
+// ---------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long sm64(unsigned long long& s) {
+  unsigned long long z = (s += 0x9e3779b97f4a7c15ull);
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+__device__ __forceinline__ double u01(unsigned long long& s) {  // (0, 1)
+  return ((double)(sm64(s) >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+}
+
+// kind 0: Gaussian (rms sx, sy); 1: KV projection, uniform in the ellipse of
+// semi-axes 2 sx, 2 sy; 2: waterbag projection, the 2D shadow of a uniform
+// 4D ball (density ~ 1 - r^2 inside semi-axes sqrt(6) sx, sqrt(6) sy).
+__device__ __forceinline__ void beam_xy(int kind, double sx, double sy, unsigned long long seed, long long i,
+                                        double& x, double& y) {
+  unsigned long long s = seed ^ ((unsigned long long)i * 0xd1b54a32d192ed03ull);
+  if (kind == 0) {
+    double r = sqrt(-2.0 * log(u01(s))), t = 6.283185307179586 * u01(s);
+    x = sx * r * cos(t);
+    y = sy * r * sin(t);
+  } else if (kind == 1) {
+    double r = sqrt(u01(s)), t = 6.283185307179586 * u01(s);
+    x = 2.0 * sx * r * cos(t);
+    y = 2.0 * sy * r * sin(t);
+  } else {
+    // a uniform point of the 4D unit ball: four normals scaled to radius u^(1/4)
+    double r1 = sqrt(-2.0 * log(u01(s))), t1 = 6.283185307179586 * u01(s);
+    double r2 = sqrt(-2.0 * log(u01(s))), t2 = 6.283185307179586 * u01(s);
+    double g0 = r1 * cos(t1), g1 = r1 * sin(t1), g2 = r2 * cos(t2), g3 = r2 * sin(t2);
+    double nrm = sqrt(g0 * g0 + g1 * g1 + g2 * g2 + g3 * g3);
+    double rad = sqrt(sqrt(u01(s))) / nrm;
+    x = 2.449489742783178 * sx * g0 * rad;
+    y = 2.449489742783178 * sy * g1 * rad;
+  }
+}
+
+__global__ void k_beam_sample(double* __restrict__ x, double* __restrict__ y, int n, int kind, double sx, double sy,
+                              unsigned long long seed) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) beam_xy(kind, sx, sy, seed, i, x[i], y[i]);
+}
+
+// 9-point deposit (Grid2D weights, Grid2D.cc:141-166) of n beam particles
+// with unit weight on the node grid xmin..xmax x ymin..ymax (nx x ny),
+// FP32 shared-memory accumulation; particles outside the grid are dropped.
+__global__ void k_beam_deposit(float* __restrict__ grid, int nx, int ny, double xmin, double ymin, double inv_dx,
+                               double inv_dy, double xmax, double ymax, long long n, int kind, double sx, double sy,
+                               unsigned long long seed) {
+  extern __shared__ float s_g[];
+  for (int i = threadIdx.x; i < nx * ny; i += blockDim.x) s_g[i] = 0.f;
+  __syncthreads();
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double x, y;
+    beam_xy(kind, sx, sy, seed, i, x, y);
+    if (x < xmin || x > xmax || y < ymin || y > ymax) continue;
+    double tx = (x - xmin) * inv_dx, ty = (y - ymin) * inv_dy;
+    int ix = (int)(tx + 0.5), iy = (int)(ty + 0.5);
+    ix = ix < 1 ? 1 : (ix > nx - 2 ? nx - 2 : ix);
+    iy = iy < 1 ? 1 : (iy > ny - 2 ? ny - 2 : iy);
+    float fx = (float)(tx - ix), fy = (float)(ty - iy);
+    float wx[3] = {0.5f * (0.25f - fx + fx * fx), 0.75f - fx * fx, 0.5f * (0.25f + fx + fx * fx)};
+    float wy[3] = {0.5f * (0.25f - fy + fy * fy), 0.75f - fy * fy, 0.5f * (0.25f + fy + fy * fy)};
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) atomicAdd(&s_g[(ix - 1 + a) * ny + (iy - 1 + b)], wx[a] * wy[b]);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nx * ny; i += blockDim.x) {
+    float v = s_g[i];
+    if (v != 0.f) atomicAdd(grid + i, v);
+  }
+}
+
+// ---------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------
 static int grid_1d(size_t n) {
@@ -549,6 +627,41 @@ static int check_batch(const orbit_denoiser_t* d, int nb) {
 
 extern "C" {
 
+int orbit_beam_sample(double* dev_x, double* dev_y, int n, int kind, double sx, double sy, unsigned long long seed) {
+  if (!dev_x || !dev_y || n < 0 || kind < 0 || kind > 2 || !(sx > 0) || !(sy > 0))
+    return set_error(ORBIT_ERR_ARG, "orbit_beam_sample: bad argument");
+  if (n == 0) return ORBIT_OK;
+  k_beam_sample<<<grid_1d(n), 256>>>(dev_x, dev_y, n, kind, sx, sy, seed);
+  ORBIT_LAUNCH_CHECK("orbit_beam_sample");
+  ORBIT_CUDA(cudaDeviceSynchronize());
+  return ORBIT_OK;
+}
+
+int orbit_beam_deposit(float* dev_grid, int nx, int ny, const double* lim, long long n, int kind, double sx,
+                       double sy, unsigned long long seed) {
+  if (!dev_grid || !lim || nx < 3 || ny < 3 || n < 0 || kind < 0 || kind > 2 || !(sx > 0) || !(sy > 0) ||
+      !(lim[1] > lim[0]) || !(lim[3] > lim[2]))
+    return set_error(ORBIT_ERR_ARG, "orbit_beam_deposit: bad argument");
+  size_t sm = sizeof(float) * (size_t)nx * ny;
+  if (sm > 200 * 1024) return set_error(ORBIT_ERR_UNSUPPORTED, "orbit_beam_deposit: grid above 200 KB of shared memory");
+  static bool attr = false;
+  if (!attr) {
+    ORBIT_CUDA(cudaFuncSetAttribute(k_beam_deposit, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr = true;
+  }
+  ORBIT_CUDA(cudaMemset(dev_grid, 0, sm));
+  double dx = (lim[1] - lim[0]) / (nx - 1), dy = (lim[3] - lim[2]) / (ny - 1);
+  long long blocks = (n + 8191) / 8192;
+  long long cap = (long long)num_sms() * 2;
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  k_beam_deposit<<<(int)blocks, 512, sm>>>(dev_grid, nx, ny, lim[0], lim[2], 1.0 / dx, 1.0 / dy, lim[1], lim[3], n,
+                                           kind, sx, sy, seed);
+  ORBIT_LAUNCH_CHECK("orbit_beam_deposit");
+  ORBIT_CUDA(cudaDeviceSynchronize());
+  return ORBIT_OK;
+}
+
 int orbit_denoiser_create(orbit_denoiser_t** out, int max_batch, int h, int w, unsigned long long seed) {
   if (!out || max_batch < 1 || h < 8 || w < 8 || h % 8 || w % 8)
     return set_error(ORBIT_ERR_ARG, "orbit_denoiser_create: sizes must be multiples of 8 (three 2x2 poolings)");
@@ -591,7 +704,9 @@ int orbit_denoiser_create(orbit_denoiser_t** out, int max_batch, int h, int w, u
     orbit_denoiser_destroy(d);
     return code;
   };
-  cudaError_t e = cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking);
+  // a blocking stream: work of the legacy default stream (where callers such
+  // as PyTorch usually prepare the images) is ordered before it
+  cudaError_t e = cudaStreamCreateWithFlags(&d->stream, cudaStreamDefault);
   if (e == cudaSuccess) e = cudaMalloc(&d->d_p, sizeof(float) * off);
   if (e == cudaSuccess) e = cudaMalloc(&d->d_pb, sizeof(__nv_bfloat16) * off);
   if (e == cudaSuccess) e = cudaMalloc(&d->d_g, sizeof(float) * off);
@@ -676,11 +791,11 @@ int orbit_denoiser_forward(orbit_denoiser_t* d, const float* dev_in, float* dev_
 }
 
 int orbit_denoiser_train_step(orbit_denoiser_t* d, const float* dev_in, const float* dev_target, int nb, float lr,
-                              float* loss) {
+                              float* loss, void* stream) {
   if (!d || !dev_in || !dev_target) return set_error(ORBIT_ERR_ARG, "orbit_denoiser_train_step: bad argument");
   int rc = check_batch(d, nb);
   if (rc) return rc;
-  cudaStream_t st = d->stream;
+  cudaStream_t st = stream_of(d, stream);
   const size_t n = (size_t)nb * d->H * d->W;
   ORBIT_CUDA(cudaMemcpyAsync(d->act[X0], dev_in, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
   rc = loss_and_grads(d, dev_target, nb, st);
@@ -700,11 +815,11 @@ int orbit_denoiser_train_step(orbit_denoiser_t* d, const float* dev_in, const fl
 }
 
 int orbit_denoiser_gradients(orbit_denoiser_t* d, const float* dev_in, const float* dev_target, int nb, float* grads,
-                             float* loss, float* dev_out) {
+                             float* loss, float* dev_out, void* stream) {
   if (!d || !dev_in || !dev_target || !grads) return set_error(ORBIT_ERR_ARG, "orbit_denoiser_gradients: bad argument");
   int rc = check_batch(d, nb);
   if (rc) return rc;
-  cudaStream_t st = d->stream;
+  cudaStream_t st = stream_of(d, stream);
   const size_t n = (size_t)nb * d->H * d->W;
   ORBIT_CUDA(cudaMemsetAsync(d->d_g, 0, sizeof(float) * d->nparam, st));
   ORBIT_CUDA(cudaMemcpyAsync(d->act[X0], dev_in, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));

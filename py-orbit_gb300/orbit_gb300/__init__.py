@@ -302,23 +302,25 @@ class DeviceDenoiser:
             raise ValueError("expected %d parameters" % self.nparam)
         call("orbit_denoiser_set_params", self.h, p.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
 
+    # The stream argument (a cudaStream_t as an integer) orders the network's
+    # work after whatever wrote its inputs; 0 is the denoiser's own stream.
     def forward(self, dev_in: int, dev_out: int, nb: int = 1, stream: int = 0):
         call("orbit_denoiser_forward", self.h, ctypes.c_void_p(dev_in), ctypes.c_void_p(dev_out), int(nb),
              ctypes.c_void_p(stream) if stream else None)
 
-    def train_step(self, dev_in: int, dev_target: int, nb: int, lr: float, want_loss: bool = True):
+    def train_step(self, dev_in: int, dev_target: int, nb: int, lr: float, want_loss: bool = True, stream: int = 0):
         loss = ctypes.c_float()
         call("orbit_denoiser_train_step", self.h, ctypes.c_void_p(dev_in), ctypes.c_void_p(dev_target), int(nb),
-             float(lr), ctypes.byref(loss) if want_loss else None)
+             float(lr), ctypes.byref(loss) if want_loss else None, ctypes.c_void_p(stream) if stream else None)
         return loss.value if want_loss else None
 
-    def gradients(self, dev_in: int, dev_target: int, nb: int, dev_out: int = 0):
+    def gradients(self, dev_in: int, dev_target: int, nb: int, dev_out: int = 0, stream: int = 0):
         """(loss, gradient of every parameter) without an update."""
         g = np.empty(self.nparam, dtype=np.float32)
         loss = ctypes.c_float()
         call("orbit_denoiser_gradients", self.h, ctypes.c_void_p(dev_in), ctypes.c_void_p(dev_target), int(nb),
              g.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), ctypes.byref(loss),
-             ctypes.c_void_p(dev_out) if dev_out else None)
+             ctypes.c_void_p(dev_out) if dev_out else None, ctypes.c_void_p(stream) if stream else None)
         return loss.value, g
 
 

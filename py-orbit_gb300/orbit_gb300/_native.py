@@ -132,14 +132,18 @@ _SIGS = {
     "orbit_denoiser_create": (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                              ctypes.c_ulonglong]),
     "orbit_denoiser_destroy": (ctypes.c_int, [_vp]),
+    "orbit_beam_sample": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                         ctypes.c_ulonglong]),
+    "orbit_beam_deposit": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp, ctypes.c_longlong, ctypes.c_int,
+                                          ctypes.c_double, ctypes.c_double, ctypes.c_ulonglong]),
     "orbit_denoiser_info": (ctypes.c_int, [_vp] + [ctypes.POINTER(ctypes.c_int)] * 4),
     "orbit_denoiser_get_params": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_float)]),
     "orbit_denoiser_set_params": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_float)]),
     "orbit_denoiser_forward": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, _vp]),
     "orbit_denoiser_train_step": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, ctypes.c_float,
-                                                 ctypes.POINTER(ctypes.c_float)]),
+                                                 ctypes.POINTER(ctypes.c_float), _vp]),
     "orbit_denoiser_gradients": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, ctypes.POINTER(ctypes.c_float),
-                                                ctypes.POINTER(ctypes.c_float), _vp]),
+                                                ctypes.POINTER(ctypes.c_float), _vp, _vp]),
     "orbit_batch_profile": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_char_p, _dp, ctypes.POINTER(ctypes.c_int),
                                            ctypes.POINTER(ctypes.c_int)]),
 }

@@ -1,0 +1,127 @@
+"""Learned denoising closure of the 2.5D kick: training data, training and
+evaluation of the denoiser network (orbit_denoiser_*, a 4-level
+convolutional encoder-decoder with BF16 weights).
+
+The network maps the normalised charge density that a bunch of few
+macroparticles deposits (the plain calculator's own deposit: extrema, grid
+set-up and the exact fixed-point 9-point deposit) to the density that a
+bunch of many more particles of the same beam deposits on the same grid.
+The plain FFT Poisson solve then turns the denoised density into the
+potential, so the solver stays exact and only the particle noise is
+learned away.
+
+Images are normalised to unit mean over the grid: image = rho * nx * ny /
+sum(rho).  Training pairs come from seeded Gaussian, KV and waterbag beams
+(transverse rms 2-8 mm, aspect ratio 0.5-2), the input from 1e5 and the
+target from 1e7 particles by default."""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import DeviceDenoiser, _native, call
+
+KINDS = ("gaussian", "kv", "waterbag")
+
+
+def _beam_params(rng, sizes, ratios):
+    kind = int(rng.integers(0, 3))
+    sx = math.exp(rng.uniform(math.log(sizes[0]), math.log(sizes[1])))
+    ratio = math.exp(rng.uniform(math.log(ratios[0]), math.log(ratios[1])))
+    return kind, sx, sx / ratio
+
+
+def make_pairs(n_pairs, nx=128, ny=128, nz=64, n_lo=100_000, n_hi=10_000_000, seed=1, sizes=(2e-3, 8e-3),
+               ratios=(0.5, 2.0)):
+    """(inputs, targets, beams) with inputs and targets float32 CUDA tensors
+    (n_pairs, 1, nx, ny); beams = [(kind, sx, sy)]."""
+    import ctypes
+
+    import torch
+    from spacecharge import SpaceChargeCalc2p5D
+    from .workloads import make_bunch
+    rng = np.random.default_rng(seed)
+    soa = np.zeros((6, n_lo))
+    soa[4] = rng.uniform(-100.0, 100.0, n_lo)
+    bunch = make_bunch(soa, 1.0)
+    dev = bunch._device_bunch()
+    ptrs = dev.device_pointers()
+    calc = SpaceChargeCalc2p5D(nx, ny, nz)
+    X = torch.empty((n_pairs, 1, nx, ny), dtype=torch.float32, device="cuda")
+    T = torch.empty_like(X)
+    g = torch.empty(nx * ny, dtype=torch.float32, device="cuda")
+    lim = np.zeros(4)
+    beams = []
+    for k in range(n_pairs):
+        kind, sx, sy = _beam_params(rng, sizes, ratios)
+        beams.append((kind, sx, sy))
+        s_lo, s_hi = int(rng.integers(1, 2**62)), int(rng.integers(1, 2**62))
+        call("orbit_beam_sample", ctypes.c_void_p(ptrs[0]), ctypes.c_void_p(ptrs[2]), n_lo, kind, sx, sy, s_lo)
+        calc.trackBunch(bunch, 0.0)  # the calculator's grid set-up and deposit, no kick
+        rho = calc._calc.grid(_native.GRID_RHO)
+        lim[:] = calc._calc.limits()[:4]
+        call("orbit_beam_deposit", ctypes.c_void_p(g.data_ptr()), nx, ny,
+             lim.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), int(n_hi), kind, sx, sy, s_hi)
+        X[k, 0] = torch.from_numpy(rho * (nx * ny / rho.sum())).float()
+        T[k, 0] = (g * (nx * ny / g.sum())).view(nx, ny)
+    return X, T, beams
+
+
+def _augment(x, t, code):
+    """One of the 8 symmetries of the square (flips of x, of y, transpose)."""
+    dims = []
+    if code & 1:
+        dims.append(2)
+    if code & 2:
+        dims.append(3)
+    if dims:
+        x, t = x.flip(dims), t.flip(dims)
+    if code & 4 and x.shape[2] == x.shape[3]:
+        x, t = x.transpose(2, 3), t.transpose(2, 3)
+    return x.contiguous(), t.contiguous()
+
+
+def train(net: DeviceDenoiser, X, T, epochs=4, batch=16, lr=1e-3, seed=0, log=None):
+    """Adam on minibatches with random symmetries; cosine learning-rate
+    decay.  Returns the per-epoch mean losses."""
+    import torch
+    n = X.shape[0]
+    steps = epochs * (n // batch)
+    rng = np.random.default_rng(seed)
+    stream = torch.cuda.current_stream().cuda_stream  # the stream that builds the minibatches
+    out, step = [], 0
+    for ep in range(epochs):
+        perm = torch.from_numpy(rng.permutation(n)).cuda()
+        tot = 0.0
+        for b in range(n // batch):
+            idx = perm[b * batch:(b + 1) * batch]
+            xb, tb = _augment(X.index_select(0, idx), T.index_select(0, idx), int(rng.integers(0, 8)))
+            a = lr * 0.5 * (1.0 + math.cos(math.pi * step / max(steps, 1)))
+            want = (b % 50) == 0
+            loss = net.train_step(xb.data_ptr(), tb.data_ptr(), batch, a, want_loss=want, stream=stream)
+            if want:
+                tot += loss
+            step += 1
+        out.append(tot / max(1, (n // batch + 49) // 50))
+        if log:
+            log("epoch %d: loss %.4g" % (ep, out[-1]))
+    return out
+
+
+def evaluate(net: DeviceDenoiser, X, T, batch=16):
+    """Mean squared error of the raw inputs and of the network outputs
+    against the targets, and the particle count whose raw deposit would
+    have the network's error (noise variance ~ 1/N, from the 1e5-particle
+    inputs)."""
+    import torch
+    n = X.shape[0]
+    out = torch.empty_like(X)
+    stream = torch.cuda.current_stream().cuda_stream
+    for b in range(0, n, batch):
+        m = min(batch, n - b)
+        net.forward(X[b:b + m].data_ptr(), out[b:b + m].data_ptr(), m, stream=stream)
+    torch.cuda.synchronize()
+    mse_raw = float(((X - T) ** 2).mean())
+    mse_net = float(((out - T) ** 2).mean())
+    return {"mse_raw": mse_raw, "mse_net": mse_net, "gain": mse_raw / mse_net}

@@ -51,9 +51,10 @@ def test_gradients_against_oracle():
         assert rel(g[wo:wo + ci * co * 9], g_o[wo:wo + ci * co * 9]) <= 1e-4, ("weights", k)
         assert rel(g[bo:bo + co], g_o[bo:bo + co]) <= 1e-4, ("bias", k)
     assert rel(g[ow:ow + 17], g_o[ow:ow + 17]) <= 1e-4
-    # a second call gives the same gradients (they are cleared in between)
+    # a second call gives the same gradients (they are cleared in between;
+    # the float atomic sums may round differently)
     loss2, g2 = net.gradients(xd.data_ptr(), td.data_ptr(), 2)
-    assert rel(g2, g) <= 1e-6 and loss2 == loss
+    assert rel(g2, g) <= 1e-6 and abs(loss2 - loss) <= 1e-6 * abs(loss)
 
 
 def test_forward_matches_gradients_output_and_adam_step():
@@ -76,3 +77,18 @@ def test_forward_matches_gradients_output_and_adam_step():
     for _ in range(20):
         last = net.train_step(xd.data_ptr(), td.data_ptr(), 2, lr)
     assert last < loss0
+
+
+def test_gradients_against_oracle_full_size():
+    """The same check at the 128 x 128 size the closure uses (several
+    16x16 tiles and weight-gradient splits per layer), one image."""
+    import torch
+    net, p, x, t, xd, td = _net(h=128, w=128, nb=1, seed=9)
+    loss, g = net.gradients(xd.data_ptr(), td.data_ptr(), 1)
+    loss_o, g_o, y_o = D.loss_and_grads(p.astype(np.float64), x, t)
+    assert abs(loss - loss_o) <= 1e-5 * abs(loss_o)
+    convs, ow, ob, n = D.layout()
+    for k, (wo, bo, ci, co) in enumerate(convs):
+        assert rel(g[wo:wo + ci * co * 9], g_o[wo:wo + ci * co * 9]) <= 1e-4, ("weights", k)
+        assert rel(g[bo:bo + co], g_o[bo:bo + co]) <= 1e-4, ("bias", k)
+    assert rel(g[ow:ow + 17], g_o[ow:ow + 17]) <= 1e-4
