@@ -374,6 +374,18 @@ int orbit_denoiser_train_step(orbit_denoiser_t* d, const float* dev_in, const fl
  * NULL, the network output for nb pairs, without an update (waits). */
 int orbit_denoiser_gradients(orbit_denoiser_t* d, const float* dev_in, const float* dev_target, int nb, float* grads,
                              float* loss, float* dev_out, void* stream);
+/* The learned closure of a plain 2.5D calculator (nx x ny = the network's
+ * image size; bunches with a uniform macrosize): each kick the network
+ * denoises the deposit (clamped at zero, rescaled to the deposit's total
+ * charge) before the FFT solve; every check_every-th kick the raw deposit is
+ * solved as well and, if the relative rms difference of the two potentials
+ * exceeds `bound`, the calculator falls back to the plain deposit until
+ * orbit_sc2p5d_denoiser_reset.  dn NULL removes the closure.  A denoiser
+ * serves one calculator at a time (its buffers are shared). */
+int orbit_sc2p5d_set_denoiser(orbit_sc2p5d_t* c, orbit_denoiser_t* dn, int check_every, double bound);
+int orbit_sc2p5d_denoiser_state(orbit_sc2p5d_t* c, int* fallback, long long* checks, long long* trips,
+                                double* last_err);
+int orbit_sc2p5d_denoiser_reset(orbit_sc2p5d_t* c);
 
 #ifdef __cplusplus
 }

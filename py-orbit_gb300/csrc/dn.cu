@@ -35,42 +35,53 @@ static const int kT = 16;   // output tile edge
 static const int kCo = 16;  // output channels per block
 static const int kCi = 8;   // input channels per shared-memory chunk
 
-// 3x3 convolution, zero padding, one 16x16 tile of 16 output channels per
-// block: out[n][o][y][x] = b[o] + sum_i sum_k in[n][i][y+ky-1][x+kx-1] Wt(o,i,k).
-// TRANS (data gradient): Wt(o,i,k) = W[i][o][8-k] with W stored for the
-// forward layer ([cin][cout][9] here), no bias, no ReLU.
-template <bool TRANS, bool BIAS_RELU>
+// 3x3 convolution, zero padding, one TT x TT tile of CO output channels per
+// block (one thread per pixel): out[n][o][y][x] = b[o] + sum_i sum_k
+// in[n][i][y+ky-1][x+kx-1] Wt(o,i,k).  TRANS (data gradient): Wt(o,i,k) =
+// W[i][o][8-k] with W stored for the forward layer ([cin][cout][9] here),
+// no bias, no ReLU.  Training batches fill the GPU with 16 x 16 tiles of 16
+// channels; a single image takes smaller blocks (more of them).
+// SPLIT: blockIdx.z = image * splits + part, the block sums input channels
+// [part * ci_per, (part + 1) * ci_per) and adds its partial sums to `out`
+// (zeroed before; bias and ReLU by k_bias_relu after).
+template <bool TRANS, bool BIAS_RELU, int TT = kT, int CO = kCo, bool SPLIT = false>
 __global__ void __launch_bounds__(256) k_conv3(const float* __restrict__ in, int cin,
                                                const __nv_bfloat16* __restrict__ w, const float* __restrict__ bias,
-                                               float* __restrict__ out, int cout, int H, int W) {
-  __shared__ float s_in[kCi][kT + 2][kT + 2];
-  __shared__ float s_w[kCo][kCi][9];
-  const int tiles_x = (W + kT - 1) / kT;
-  const int tx0 = (blockIdx.x % tiles_x) * kT, ty0 = (blockIdx.x / tiles_x) * kT;
-  const int co0 = blockIdx.y * kCo;
-  const int n = blockIdx.z;
-  const int tx = threadIdx.x % kT, ty = threadIdx.x / kT;
-  float acc[kCo];
+                                               float* __restrict__ out, int cout, int H, int W, int splits = 1,
+                                               int ci_per = 1 << 30) {
+  static_assert(CO % 4 == 0, "output channels per block: a multiple of 4");
+  __shared__ float s_in[kCi][TT + 2][TT + 2];
+  // weights as [input channel][tap][output channel]: four output channels
+  // per 128-bit shared load
+  __shared__ __align__(16) float s_w[kCi][9][CO];
+  const int tiles_x = (W + TT - 1) / TT;
+  const int tx0 = (blockIdx.x % tiles_x) * TT, ty0 = (blockIdx.x / tiles_x) * TT;
+  const int co0 = blockIdx.y * CO;
+  const int n = SPLIT ? (int)blockIdx.z / splits : (int)blockIdx.z;
+  const int ci_lo = SPLIT ? ((int)blockIdx.z % splits) * ci_per : 0;
+  const int ci_hi = SPLIT ? min(cin, ci_lo + ci_per) : cin;
+  const int tx = threadIdx.x % TT, ty = threadIdx.x / TT;
+  float acc[CO];
 #pragma unroll
-  for (int o = 0; o < kCo; ++o) acc[o] = 0.f;
-  for (int ci0 = 0; ci0 < cin; ci0 += kCi) {
-    for (int idx = threadIdx.x; idx < kCi * (kT + 2) * (kT + 2); idx += blockDim.x) {
-      int c = idx / ((kT + 2) * (kT + 2)), r = idx % ((kT + 2) * (kT + 2));
-      int yy = r / (kT + 2), xx = r % (kT + 2);
+  for (int o = 0; o < CO; ++o) acc[o] = 0.f;
+  for (int ci0 = ci_lo; ci0 < ci_hi; ci0 += kCi) {
+    for (int idx = threadIdx.x; idx < kCi * (TT + 2) * (TT + 2); idx += blockDim.x) {
+      int c = idx / ((TT + 2) * (TT + 2)), r = idx % ((TT + 2) * (TT + 2));
+      int yy = r / (TT + 2), xx = r % (TT + 2);
       int gy = ty0 + yy - 1, gx = tx0 + xx - 1, ci = ci0 + c;
       float v = 0.f;
-      if (ci < cin && gy >= 0 && gy < H && gx >= 0 && gx < W) v = in[(((size_t)n * cin + ci) * H + gy) * W + gx];
+      if (ci < ci_hi && gy >= 0 && gy < H && gx >= 0 && gx < W) v = in[(((size_t)n * cin + ci) * H + gy) * W + gx];
       s_in[c][yy][xx] = v;
     }
-    for (int idx = threadIdx.x; idx < kCo * kCi * 9; idx += blockDim.x) {
+    for (int idx = threadIdx.x; idx < CO * kCi * 9; idx += blockDim.x) {
       int o = idx / (kCi * 9), r = idx % (kCi * 9);
       int c = r / 9, k = r % 9;
       int co = co0 + o, ci = ci0 + c;
       float v = 0.f;
-      if (co < cout && ci < cin)
+      if (co < cout && ci < ci_hi)
         v = TRANS ? __bfloat162float(w[((size_t)ci * cout + co) * 9 + (8 - k)])
                   : __bfloat162float(w[((size_t)co * cin + ci) * 9 + k]);
-      s_w[o][c][k] = v;
+      s_w[c][k][o] = v;
     }
     __syncthreads();
 #pragma unroll 2
@@ -78,8 +89,15 @@ __global__ void __launch_bounds__(256) k_conv3(const float* __restrict__ in, int
 #pragma unroll
       for (int k = 0; k < 9; ++k) {
         float v = s_in[c][ty + k / 3][tx + k % 3];
+        const float4* wk = reinterpret_cast<const float4*>(&s_w[c][k][0]);
 #pragma unroll
-        for (int o = 0; o < kCo; ++o) acc[o] = fmaf(v, s_w[o][c][k], acc[o]);
+        for (int q = 0; q < CO / 4; ++q) {
+          float4 w4 = wk[q];
+          acc[4 * q] = fmaf(v, w4.x, acc[4 * q]);
+          acc[4 * q + 1] = fmaf(v, w4.y, acc[4 * q + 1]);
+          acc[4 * q + 2] = fmaf(v, w4.z, acc[4 * q + 2]);
+          acc[4 * q + 3] = fmaf(v, w4.w, acc[4 * q + 3]);
+        }
       }
     }
     __syncthreads();
@@ -87,15 +105,25 @@ __global__ void __launch_bounds__(256) k_conv3(const float* __restrict__ in, int
   const int y = ty0 + ty, x = tx0 + tx;
   if (y < H && x < W) {
 #pragma unroll
-    for (int o = 0; o < kCo; ++o) {
+    for (int o = 0; o < CO; ++o) {
       int co = co0 + o;
       if (co < cout) {
         float v = acc[o];
-        if (BIAS_RELU) v = fmaxf(v + bias[co], 0.f);
-        out[(((size_t)n * cout + co) * H + y) * W + x] = v;
+        if (SPLIT) {
+          atomicAdd(out + (((size_t)n * cout + co) * H + y) * W + x, v);
+        } else {
+          if (BIAS_RELU) v = fmaxf(v + bias[co], 0.f);
+          out[(((size_t)n * cout + co) * H + y) * W + x] = v;
+        }
       }
     }
   }
+}
+
+// out[n][c] = max(out[n][c] + b[c], 0) after a split convolution.
+__global__ void k_bias_relu(float* __restrict__ out, const float* __restrict__ b, int C, int HW, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = fmaxf(out[i] + b[(i / HW) % C], 0.f);
 }
 
 // Weight and bias gradients of a 3x3 convolution:
@@ -461,13 +489,38 @@ static size_t act_size(const orbit_denoiser_t* d, int a, int nb) {
   return (size_t)nb * c * h * w;
 }
 
+// Forward launch shape: 16x16 tiles of 16 channels when that already makes
+// two blocks per SM (training batches); else (a single image) 8x8 tiles of
+// 16 channels, with the input channels split over enough blocks to fill
+// the GPU and the partial sums added atomically.
 static int conv_fwd(orbit_denoiser_t* d, const Step3& s, int nb, cudaStream_t st) {
   const Conv& cv = d->conv[s.ci];
   int c, h, w;
   act_shape(d, s.out, &c, &h, &w);
-  dim3 g(((w + kT - 1) / kT) * ((h + kT - 1) / kT), (cv.cout + kCo - 1) / kCo, nb);
-  k_conv3<false, true><<<g, 256, 0, st>>>(d->act[s.in], cv.cin, d->d_pb + cv.w_off, d->d_p + cv.b_off,
-                                          d->act[s.out], cv.cout, h, w);
+  const __nv_bfloat16* W = d->d_pb + cv.w_off;
+  const float* B = d->d_p + cv.b_off;
+  long long big = (long long)((w + 15) / 16) * ((h + 15) / 16) * ((cv.cout + 15) / 16) * nb;
+  if (big >= 2LL * num_sms()) {
+    dim3 g(((w + 15) / 16) * ((h + 15) / 16), (cv.cout + 15) / 16, nb);
+    k_conv3<false, true, 16, 16><<<g, 256, 0, st>>>(d->act[s.in], cv.cin, W, B, d->act[s.out], cv.cout, h, w);
+  } else {
+    const long long base = (long long)((w + 7) / 8) * ((h + 7) / 8) * ((cv.cout + 15) / 16) * nb;
+    int chunks = (cv.cin + kCi - 1) / kCi;
+    int splits = (int)((2LL * num_sms() + base - 1) / base);
+    splits = splits < 1 ? 1 : (splits > chunks ? chunks : splits);
+    const int ci_per = ((chunks + splits - 1) / splits) * kCi;
+    splits = (cv.cin + ci_per - 1) / ci_per;
+    dim3 g(((w + 7) / 8) * ((h + 7) / 8), (cv.cout + 15) / 16, nb * splits);
+    if (splits == 1) {
+      k_conv3<false, true, 8, 16><<<g, 64, 0, st>>>(d->act[s.in], cv.cin, W, B, d->act[s.out], cv.cout, h, w);
+    } else {
+      const size_t n_out = act_size(d, s.out, nb);
+      ORBIT_CUDA(cudaMemsetAsync(d->act[s.out], 0, sizeof(float) * n_out, st));
+      k_conv3<false, true, 8, 16, true><<<g, 64, 0, st>>>(d->act[s.in], cv.cin, W, B, d->act[s.out], cv.cout, h, w,
+                                                          splits, ci_per);
+      k_bias_relu<<<grid_1d(n_out), 256, 0, st>>>(d->act[s.out], B, cv.cout, h * w, n_out);
+    }
+  }
   ORBIT_LAUNCH_CHECK("denoiser conv");
   return ORBIT_OK;
 }

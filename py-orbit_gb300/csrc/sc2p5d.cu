@@ -150,6 +150,8 @@ __device__ __noinline__ void finalize_block(ScState* st, G* zacc, int nz, double
 //        rest mirrored; nrows = nx2/2 + 1)
 // SRC 1: plain rho from the fixed-point grid (first ny columns, first nx rows)
 // SRC 2: fp32 rho
+// SRC 3: a double grid of nrows x ncols, read only (the raw density of a
+//        learned-closure check)
 // The deposit grid (SRC 1, 2) is cleared as it is read, ready for the next
 // deposit, and one extra block (the last) finalizes the line density.
 // gate (SRC 0): as for k_green_fill.
@@ -161,7 +163,7 @@ __device__ __forceinline__ void rows_fwd_body(ScState* st, void* src, double* rh
   typedef typename CT<T>::t C;
   if (SRC == 0 && gate && !st->green_dirty) return;
   if (st->skip) return;
-  if (SRC != 0 && blk == nblk - 1) {
+  if ((SRC == 1 || SRC == 2) && blk == nblk - 1) {
     if (SRC == 1) finalize_block(st, (unsigned long long*)zacc, nz, lam, (float*)nullptr);
     else finalize_block(st, (float*)zacc, nz, lam, lam_f);
     return;
@@ -181,6 +183,10 @@ __device__ __forceinline__ void rows_fwd_body(ScState* st, void* src, double* rh
         const double* g = (const double*)src;
         va = (T)g[(size_t)r0 * N + j];
         if (r1 < nrows) vb = (T)g[(size_t)r1 * N + j];
+      } else if (SRC == 3) {
+        const double* g = (const double*)src;
+        va = (T)g[(size_t)r0 * ncols + j];
+        if (r1 < nrows) vb = (T)g[(size_t)r1 * ncols + j];
       } else if (SRC == 1) {
         long long* q = (long long*)src;
         double da = (double)q[(size_t)r0 * ncols + j] * iq;
@@ -755,6 +761,97 @@ __global__ void k_fields(const ScState* st, const double* __restrict__ phi, cons
 }
 
 // ---------------------------------------------------------------------
+// learned closure (plain form)
+// ---------------------------------------------------------------------
+// The fixed-point deposit as the network's image (density * scale, scale =
+// nx ny / total macrosize: unit mean) and, on check kicks, the raw density.
+__global__ void k_learn_in(ScState* st, const unsigned long long* __restrict__ rho_q, float* __restrict__ img,
+                           double* __restrict__ raw, int n, double scale) {
+  if (st->skip) return;
+  if (blockIdx.x == 0 && threadIdx.x == 0) st->dn_sum = 0.0;
+  const double iq = st->inv_qscale;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double v = (double)(long long)rho_q[i] * iq;
+    if (raw) raw[i] = v;
+    img[i] = (float)(v * scale);
+  }
+}
+
+// Sum of the network output clamped at zero (a density is not negative).
+__global__ void k_learn_sum(ScState* st, const float* __restrict__ out, int n) {
+  if (st->skip) return;
+  __shared__ double s_part[32];
+  double s = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) s += fmaxf(out[i], 0.f);
+  for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+  if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_part[w];
+    atomicAdd(&st->dn_sum, t);
+  }
+}
+
+// The clamped network output, rescaled to the deposit's total charge (n in
+// image units), written back as the fixed-point deposit the solve reads;
+// nothing is written once the closure has fallen back.
+__global__ void k_learn_out(ScState* st, const float* __restrict__ out, unsigned long long* __restrict__ rho_q, int n,
+                            double scale) {
+  if (st->skip || st->dn_fallback) return;
+  const double sum = st->dn_sum;
+  if (!(sum > 0.0)) return;
+  const double back = ((double)n / sum) / (scale * st->inv_qscale);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    rho_q[i] = (unsigned long long)llrint((double)fmaxf(out[i], 0.f) * back);
+}
+
+// State of the check solve: the kick's skip flag and log-scale term.
+__global__ void k_learn_chk_prep(const ScState* st, ScState* chk) {
+  chk->skip = st->skip;
+  chk->scale = st->scale;
+  chk->phi_absmax = 0ull;
+}
+
+// The closure's judge: relative rms difference of the potential from the
+// denoised density and the potential from the raw deposit; above `bound`
+// the closure falls back to the plain deposit for the following kicks.
+__global__ void k_learn_compare(ScState* st, const double* __restrict__ phi, const double* __restrict__ phi_raw, int n,
+                                double bound) {
+  if (st->skip) return;
+  __shared__ double s_d[32], s_r[32];
+  double d2 = 0.0, r2 = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    double a = phi[i], b = phi_raw[i];
+    d2 += (a - b) * (a - b);
+    r2 += b * b;
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    d2 += __shfl_xor_sync(0xffffffffu, d2, off);
+    r2 += __shfl_xor_sync(0xffffffffu, r2, off);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    s_d[threadIdx.x >> 5] = d2;
+    s_r[threadIdx.x >> 5] = r2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double D = 0.0, R = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      D += s_d[w];
+      R += s_r[w];
+    }
+    double e = R > 0.0 ? sqrt(D / R) : 0.0;
+    st->dn_err = e;
+    st->dn_checks += 1;
+    if (!(e <= bound)) {
+      st->dn_fallback = 1;
+      st->dn_trips += 1;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------
 // batched kernels (plain form): the members of one grid class in one
 // launch; grid kernels take the member from blockIdx.y, particle kernels
 // from the block table
@@ -860,6 +957,7 @@ static int set_fft_attrs(int nmax) {
   ORBIT_CUDA(cudaFuncSetAttribute(k_rows_fwd<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
   ORBIT_CUDA(cudaFuncSetAttribute(k_rows_fwd<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
   ORBIT_CUDA(cudaFuncSetAttribute(k_rows_fwd<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  ORBIT_CUDA(cudaFuncSetAttribute(k_rows_fwd<T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
   ORBIT_CUDA(cudaFuncSetAttribute(k_cols<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
   ORBIT_CUDA(cudaFuncSetAttribute(k_cols<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
   ORBIT_CUDA(cudaFuncSetAttribute(k_rows_inv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
@@ -1299,6 +1397,35 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
   ORBIT_PE(s);
   ++nl;
   ORBIT_LAUNCH_CHECK("sc2p5d deposit");
+  // learned closure: the network denoises the deposit before the solve
+  bool dn_check = false;
+  double dn_scale = 0.0;
+  if (c->dn && plain && !c->rb && !bnd) {
+    if (b->has_msize)
+      return set_error(ORBIT_ERR_UNSUPPORTED, "the learned closure needs a uniform macrosize");
+    const double M = (double)n * b->sync.macrosize;
+    if (M > 0.0) {
+      const int ng = c->nx * c->ny;
+      dn_check = (c->dn_count++ % c->dn_every) == 0;
+      dn_scale = (double)ng / M;
+      int gb = (ng + 255) / 256;
+      if (gb > num_sms() * 2) gb = num_sms() * 2;
+      ORBIT_PB("learn_in", s);
+      k_learn_in<<<gb, 256, 0, s>>>(c->d_st, c->d_rho_q, c->d_dn_img, dn_check ? c->d_dn_raw : nullptr, ng,
+                                    dn_scale);
+      ORBIT_PE(s);
+      ORBIT_PB("learn_network", s);
+      rc = orbit_denoiser_forward(c->dn, c->d_dn_img, c->d_dn_out, 1, (void*)s);
+      ORBIT_PE(s);
+      if (rc) return rc;
+      ORBIT_PB("learn_out", s);
+      k_learn_sum<<<gb, 256, 0, s>>>(c->d_st, c->d_dn_out, ng);
+      k_learn_out<<<gb, 256, 0, s>>>(c->d_st, c->d_dn_out, c->d_rho_q, ng, dn_scale);
+      ORBIT_PE(s);
+      nl += 3;
+      ORBIT_LAUNCH_CHECK("sc2p5d learned closure");
+    }
+  }
   if (cond) {
     // beside the forward rows, which leave most SMs free (the deposit fills them)
     rc = add_green_branch(c, s, cond, &branch_node);
@@ -1319,6 +1446,26 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
     ORBIT_CUDA(cudaStreamUpdateCaptureDependencies(s, &branch_node, nullptr, 1, cudaStreamAddCaptureDependencies));
   rc = plain ? enqueue_conv<double>(c, s, &nl) : enqueue_conv<float>(c, s, &nl);
   if (rc) return rc;
+  if (dn_check) {
+    // the raw deposit solved beside the denoised one, and the judge
+    typedef double2 C;
+    int thx = fft_threads(c->plan_x), thy = fft_threads(c->plan_y);
+    size_t smx = fft_smem<double>(c->nx2), smy = fft_smem<double>(c->ny2);
+    ORBIT_PB("learn_check", s);
+    k_learn_chk_prep<<<1, 1, 0, s>>>(c->d_st, c->d_dn_st);
+    k_rows_fwd<double, 3><<<(c->nx + 1) / 2, thy, smy, s>>>(c->d_dn_st, c->d_dn_raw, nullptr, (C*)c->d_dn_hat,
+                                                            (const C*)c->d_tw_y, c->plan_y, c->nx, c->ny, c->H, 1,
+                                                            nullptr, 0, nullptr, nullptr);
+    k_cols<double, 1><<<c->H, thx, smx, s>>>(c->d_dn_st, (C*)c->d_dn_hat, (C*)c->d_green, (const C*)c->d_tw_x,
+                                             c->plan_x, c->nx, c->H, c->ny2, 1);
+    k_rows_inv<double><<<(c->nx + 1) / 2, thy, smy, s>>>(c->d_dn_st, (const C*)c->d_dn_hat, (const C*)c->d_tw_y,
+                                                         c->plan_y, c->nx, c->ny, c->H, 1.0 / (c->nx2 * c->ny2),
+                                                         c->d_dn_phi, nullptr);
+    k_learn_compare<<<1, 256, 0, s>>>(c->d_st, c->d_phi, c->d_dn_phi, c->nx * c->ny, c->dn_bound);
+    ORBIT_PE(s);
+    nl += 5;
+    ORBIT_LAUNCH_CHECK("sc2p5d learned closure check");
+  }
   if (bnd) {
     rc = bnd_enqueue_potential(bnd, c, s, &nl);
     if (rc) return rc;
@@ -1509,10 +1656,69 @@ int orbit_sc2p5d_destroy(orbit_sc2p5d_t* c) {
   if (c->aux) cudaStreamDestroy(c->aux);
   void* ptrs[] = {c->d_st, c->d_rho_q, c->d_z_q, c->d_rho_f, c->d_z_f, c->d_rho, c->d_phi, c->d_lam, c->d_lamd,
                   c->d_phi_f, c->d_lam_f, c->d_hat, c->d_green, c->d_gbuf, c->d_gscratch, c->d_tw_x, c->d_tw_y,
-                  c->d_phi_fix, c->d_lam_fix};
+                  c->d_phi_fix, c->d_lam_fix, c->d_dn_img, c->d_dn_out, c->d_dn_raw, c->d_dn_hat, c->d_dn_phi,
+                  c->d_dn_st};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete c;
+  return ORBIT_OK;
+}
+
+int orbit_sc2p5d_set_denoiser(orbit_sc2p5d_t* c, orbit_denoiser_t* dn, int check_every, double bound) {
+  if (!c || (dn && (check_every < 1 || !(bound > 0.0))))
+    return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_set_denoiser: bad argument");
+  if (c->used) ORBIT_CUDA(cudaEventSynchronize(c->done));
+  if (!dn) {
+    c->dn = nullptr;
+    return ORBIT_OK;
+  }
+  if (c->form != ORBIT_FORM_PLAIN || c->rb)
+    return set_error(ORBIT_ERR_UNSUPPORTED, "the learned closure is built for the plain 2.5D calculator");
+  int h = 0, w = 0, mb = 0;
+  int rc = orbit_denoiser_info(dn, nullptr, &h, &w, &mb);
+  if (rc) return rc;
+  if (h != c->nx || w != c->ny)
+    return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_set_denoiser: the network's image size differs from the grid");
+  const size_t ng = (size_t)c->nx * c->ny;
+  if (!c->d_dn_img) {
+    ORBIT_CUDA(cudaMalloc(&c->d_dn_img, sizeof(float) * ng));
+    ORBIT_CUDA(cudaMalloc(&c->d_dn_out, sizeof(float) * ng));
+    ORBIT_CUDA(cudaMalloc(&c->d_dn_raw, sizeof(double) * ng));
+    ORBIT_CUDA(cudaMalloc(&c->d_dn_hat, sizeof(double2) * (size_t)c->nx2 * c->H));
+    ORBIT_CUDA(cudaMalloc(&c->d_dn_phi, sizeof(double) * ng));
+    ORBIT_CUDA(cudaMalloc(&c->d_dn_st, sizeof(ScState)));
+    ORBIT_CUDA(cudaMemset(c->d_dn_st, 0, sizeof(ScState)));
+  }
+  c->dn = dn;
+  c->dn_every = check_every;
+  c->dn_bound = bound;
+  c->dn_count = 0;
+  return orbit_sc2p5d_denoiser_reset(c);
+}
+
+int orbit_sc2p5d_denoiser_state(orbit_sc2p5d_t* c, int* fallback, long long* checks, long long* trips,
+                                double* last_err) {
+  if (!c) return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_denoiser_state: bad argument");
+  if (c->used) ORBIT_CUDA(cudaEventSynchronize(c->done));
+  ScState h;
+  ORBIT_CUDA(cudaMemcpy(&h, c->d_st, sizeof(h), cudaMemcpyDeviceToHost));
+  if (fallback) *fallback = h.dn_fallback;
+  if (checks) *checks = (long long)h.dn_checks;
+  if (trips) *trips = (long long)h.dn_trips;
+  if (last_err) *last_err = h.dn_err;
+  return ORBIT_OK;
+}
+
+int orbit_sc2p5d_denoiser_reset(orbit_sc2p5d_t* c) {
+  if (!c) return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_denoiser_reset: bad argument");
+  if (c->used) ORBIT_CUDA(cudaEventSynchronize(c->done));
+  ScState h;
+  ORBIT_CUDA(cudaMemcpy(&h, c->d_st, sizeof(h), cudaMemcpyDeviceToHost));
+  h.dn_fallback = 0;
+  h.dn_err = 0.0;
+  h.dn_checks = 0;
+  h.dn_trips = 0;
+  ORBIT_CUDA(cudaMemcpy(c->d_st, &h, sizeof(h), cudaMemcpyHostToDevice));
   return ORBIT_OK;
 }
 

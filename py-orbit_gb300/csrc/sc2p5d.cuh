@@ -31,6 +31,13 @@ struct ScState {
   // longitudinal kick (SpaceChargeCalc2p5Drb.cc:124-136, 226-254)
   double rb_xc, rb_yc, rb_a2, rb_lin, rb_lout;
   unsigned long long n_kicks, n_green;                    // kicks solved, Green spectra rebuilt
+  // learned closure: fallen back to the plain deposit (sticky), the last
+  // check's relative rms potential difference, checks and fall-backs, and
+  // the sum of the clamped network output
+  int dn_fallback;
+  double dn_err;
+  unsigned long long dn_checks, dn_trips;
+  double dn_sum;
 };
 
 // Inside test of a conducting boundary (BaseBoundary2D.cc:144-151,
@@ -83,6 +90,7 @@ struct FftPlan {
 }  // namespace orbit
 
 struct orbit_boundary;
+struct orbit_denoiser;
 
 struct orbit_sc2p5d {
   int nx = 0, ny = 0, nz = 0, form = 0;
@@ -122,6 +130,19 @@ struct orbit_sc2p5d {
   int n_long_avg = 3;
   double* d_lamd = nullptr;               // derivative grid (nz)
   int dep_threads = 512, kick_threads = 512;
+  // learned closure (plain form): the network, the check period and bound,
+  // the host kick counter, and the image, raw-density and check-solve
+  // buffers
+  orbit_denoiser* dn = nullptr;
+  int dn_every = 10;
+  double dn_bound = 0.05;
+  long long dn_count = 0;
+  float* d_dn_img = nullptr;
+  float* d_dn_out = nullptr;
+  double* d_dn_raw = nullptr;
+  void* d_dn_hat = nullptr;
+  double* d_dn_phi = nullptr;
+  orbit::ScState* d_dn_st = nullptr;
 };
 
 namespace orbit {

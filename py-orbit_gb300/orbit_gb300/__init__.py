@@ -179,6 +179,20 @@ class DeviceSC2p5D:
         call("orbit_sc2p5d_get_limits", self.h, lim.ctypes.data_as(_dp))
         return lim
 
+    def set_denoiser(self, dn, check_every: int = 10, bound: float = 0.05):
+        """Learned closure (orbit_sc2p5d_set_denoiser); dn None removes it."""
+        call("orbit_sc2p5d_set_denoiser", self.h, dn.h if dn is not None else None, int(check_every), float(bound))
+        self._dn = dn  # kept alive while the calculator uses it
+
+    def denoiser_state(self):
+        """{fallback, checks, trips, last_err} of the learned closure."""
+        f, c, t, e = ctypes.c_int(), ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_double()
+        call("orbit_sc2p5d_denoiser_state", self.h, ctypes.byref(f), ctypes.byref(c), ctypes.byref(t), ctypes.byref(e))
+        return {"fallback": f.value, "checks": c.value, "trips": t.value, "last_err": e.value}
+
+    def denoiser_reset(self):
+        call("orbit_sc2p5d_denoiser_reset", self.h)
+
     def counters(self):
         """(kicks solved, Green spectra rebuilt) since creation."""
         k, g = ctypes.c_longlong(), ctypes.c_longlong()

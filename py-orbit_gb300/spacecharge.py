@@ -436,6 +436,21 @@ class SpaceChargeCalc2p5D:
         self._phi._bind(lambda g: self._refresh(g, 1))
         self._long._bind(lambda g: self._refresh(g, 2))
 
+    # ---- learned closure (a form of this library; no reference counterpart)
+    def setDenoiser(self, denoiser, checkEvery=10, bound=0.05):
+        """Denoise every kick's deposit with a trained network
+        (orbit_gb300.DeviceDenoiser of the grid's size) before the FFT solve;
+        every checkEvery-th kick the raw deposit is solved as well and the
+        calculator falls back to it for good when the relative rms difference
+        of the two potentials exceeds `bound`.  None removes the closure."""
+        self._calc.set_denoiser(denoiser, checkEvery, bound)
+
+    def getDenoiserState(self):
+        return self._calc.denoiser_state()
+
+    def resetDenoiser(self):
+        self._calc.denoiser_reset()
+
     def _refresh(self, g, which):
         if self._version == 0 or self._seen.get(which) == self._version:
             return
