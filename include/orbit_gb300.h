@@ -353,6 +353,10 @@ typedef struct orbit_denoiser orbit_denoiser_t;
 int orbit_beam_sample(double* dev_x, double* dev_y, int n, int kind, double sx, double sy, unsigned long long seed);
 int orbit_beam_deposit(float* dev_grid, int nx, int ny, const double* lim, long long n, int kind, double sx,
                        double sy, unsigned long long seed);
+/* The same deposit of n given positions (device arrays), e.g. a tracked
+ * bunch's x and y (waits). */
+int orbit_grid_deposit(float* dev_grid, int nx, int ny, const double* lim, const double* dev_x, const double* dev_y,
+                       long long n);
 int orbit_denoiser_create(orbit_denoiser_t** out, int max_batch, int h, int w, unsigned long long seed);
 int orbit_denoiser_destroy(orbit_denoiser_t* d);
 int orbit_denoiser_info(const orbit_denoiser_t* d, int* nparam, int* h, int* w, int* max_batch);

@@ -423,6 +423,35 @@ __global__ void k_beam_deposit(float* __restrict__ grid, int nx, int ny, double 
   }
 }
 
+// The same deposit for given positions (a tracked bunch).
+__global__ void k_grid_deposit(float* __restrict__ grid, int nx, int ny, double xmin, double ymin, double inv_dx,
+                               double inv_dy, double xmax, double ymax, const double* __restrict__ px,
+                               const double* __restrict__ py, long long n) {
+  extern __shared__ float s_g[];
+  for (int i = threadIdx.x; i < nx * ny; i += blockDim.x) s_g[i] = 0.f;
+  __syncthreads();
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double x = px[i], y = py[i];
+    if (!(x >= xmin && x <= xmax && y >= ymin && y <= ymax)) continue;
+    double tx = (x - xmin) * inv_dx, ty = (y - ymin) * inv_dy;
+    int ix = (int)(tx + 0.5), iy = (int)(ty + 0.5);
+    ix = ix < 1 ? 1 : (ix > nx - 2 ? nx - 2 : ix);
+    iy = iy < 1 ? 1 : (iy > ny - 2 ? ny - 2 : iy);
+    float fx = (float)(tx - ix), fy = (float)(ty - iy);
+    float wx[3] = {0.5f * (0.25f - fx + fx * fx), 0.75f - fx * fx, 0.5f * (0.25f + fx + fx * fx)};
+    float wy[3] = {0.5f * (0.25f - fy + fy * fy), 0.75f - fy * fy, 0.5f * (0.25f + fy + fy * fy)};
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) atomicAdd(&s_g[(ix - 1 + a) * ny + (iy - 1 + b)], wx[a] * wy[b]);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nx * ny; i += blockDim.x) {
+    float v = s_g[i];
+    if (v != 0.f) atomicAdd(grid + i, v);
+  }
+}
+
 // ---------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------
@@ -711,6 +740,31 @@ int orbit_beam_deposit(float* dev_grid, int nx, int ny, const double* lim, long 
   k_beam_deposit<<<(int)blocks, 512, sm>>>(dev_grid, nx, ny, lim[0], lim[2], 1.0 / dx, 1.0 / dy, lim[1], lim[3], n,
                                            kind, sx, sy, seed);
   ORBIT_LAUNCH_CHECK("orbit_beam_deposit");
+  ORBIT_CUDA(cudaDeviceSynchronize());
+  return ORBIT_OK;
+}
+
+int orbit_grid_deposit(float* dev_grid, int nx, int ny, const double* lim, const double* dev_x, const double* dev_y,
+                       long long n) {
+  if (!dev_grid || !lim || !dev_x || !dev_y || nx < 3 || ny < 3 || n < 0 || !(lim[1] > lim[0]) ||
+      !(lim[3] > lim[2]))
+    return set_error(ORBIT_ERR_ARG, "orbit_grid_deposit: bad argument");
+  size_t sm = sizeof(float) * (size_t)nx * ny;
+  if (sm > 200 * 1024) return set_error(ORBIT_ERR_UNSUPPORTED, "orbit_grid_deposit: grid above 200 KB of shared memory");
+  static bool attr = false;
+  if (!attr) {
+    ORBIT_CUDA(cudaFuncSetAttribute(k_grid_deposit, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr = true;
+  }
+  ORBIT_CUDA(cudaMemset(dev_grid, 0, sm));
+  double dx = (lim[1] - lim[0]) / (nx - 1), dy = (lim[3] - lim[2]) / (ny - 1);
+  long long blocks = (n + 8191) / 8192;
+  long long cap = (long long)num_sms() * 2;
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  k_grid_deposit<<<(int)blocks, 512, sm>>>(dev_grid, nx, ny, lim[0], lim[2], 1.0 / dx, 1.0 / dy, lim[1], lim[3],
+                                           dev_x, dev_y, n);
+  ORBIT_LAUNCH_CHECK("orbit_grid_deposit");
   ORBIT_CUDA(cudaDeviceSynchronize());
   return ORBIT_OK;
 }

@@ -136,6 +136,7 @@ _SIGS = {
     "orbit_sc2p5d_denoiser_state": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_longlong),
                                                    ctypes.POINTER(ctypes.c_longlong), _dp]),
     "orbit_sc2p5d_denoiser_reset": (ctypes.c_int, [_vp]),
+    "orbit_grid_deposit": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp, _vp, _vp, ctypes.c_longlong]),
     "orbit_beam_sample": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                          ctypes.c_ulonglong]),
     "orbit_beam_deposit": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp, ctypes.c_longlong, ctypes.c_int,

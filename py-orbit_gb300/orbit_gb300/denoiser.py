@@ -69,6 +69,77 @@ def make_pairs(n_pairs, nx=128, ny=128, nz=64, n_lo=100_000, n_hi=10_000_000, se
     return X, T, beams
 
 
+class _DevArray:
+    """A device array of float64 by address, for torch.as_tensor."""
+
+    def __init__(self, ptr, n):
+        self.__cuda_array_interface__ = {"shape": (int(n),), "typestr": "<f8", "data": (int(ptr), False),
+                                         "version": 3}
+
+
+def _view(ptr, n):
+    import torch
+    return torch.as_tensor(_DevArray(ptr, n), device="cuda")
+
+
+# tracked-beam set-ups: (distribution, rms scale, intensity [protons], FODO k1)
+TRACK_SETUPS = (("waterbag", 1.0, 1e14, 0.5), ("gauss", 1.0, 1e14, 0.5), ("waterbag", 0.7, 2e14, 0.4),
+                ("gauss", 1.4, 3e14, 0.6), ("waterbag", 1.2, 5e13, 0.6), ("gauss", 0.8, 1.5e14, 0.45))
+
+
+def make_tracked_pairs(setups=TRACK_SETUPS, turns=10, per_turn=40, nx=128, ny=128, nz=64, n_lo=100_000,
+                       n_hi=10_000_000, seed=3, cells=40):
+    """Pairs from beams as tracking shapes them: a bunch of n_hi particles
+    is tracked with the plain form through a FODO lattice; at the start and
+    after each turn, slices of n_lo consecutive particles (independent
+    draws of the same distribution) go through the calculator for the
+    input, and the whole bunch is deposited on each slice's grid for the
+    target."""
+    import contextlib
+    import ctypes
+    import io
+
+    import torch
+    from spacecharge import SpaceChargeCalc2p5D
+    from . import workloads as W
+    lo = W.make_bunch(np.zeros((6, n_lo)), 1.0)
+    lo_ptrs = lo._device_bunch().device_pointers()
+    lo_x, lo_y, lo_z = (_view(lo_ptrs[c], n_lo) for c in (0, 2, 4))
+    calc = SpaceChargeCalc2p5D(nx, ny, nz)
+    g = torch.empty(nx * ny, dtype=torch.float32, device="cuda")
+    lim = np.zeros(4)
+    X, T = [], []
+    for k, (dist, scale, intensity, k1) in enumerate(setups):
+        soa = W.c2_coords(n_hi, seed=seed * 100 + k) if dist == "waterbag" else W.c3_coords(n_hi, seed * 100 + k)
+        soa[:4] *= scale
+        hi = W.make_bunch(soa, intensity / n_hi)
+        del soa
+        with contextlib.redirect_stdout(io.StringIO()):
+            lat = W.fodo_lattice(SpaceChargeCalc2p5D(nx, ny, nz), cells=cells, kq=k1)
+        for t in range(turns + 1):
+            if t > 0:
+                lat.trackBunchTurns(hi, 1)
+            ptrs = hi._device_bunch().device_pointers()
+            hx, hy, hz = (_view(ptrs[c], n_hi) for c in (0, 2, 4))
+            for j in range(per_turn):
+                off = (j * n_lo) % (n_hi - n_lo + 1)
+                lo_x.copy_(hx[off:off + n_lo])
+                lo_y.copy_(hy[off:off + n_lo])
+                lo_z.copy_(hz[off:off + n_lo])
+                torch.cuda.synchronize()
+                calc.trackBunch(lo, 0.0)
+                rho = calc._calc.grid(_native.GRID_RHO)
+                lim[:] = calc._calc.limits()[:4]
+                call("orbit_grid_deposit", ctypes.c_void_p(g.data_ptr()), nx, ny,
+                     lim.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.c_void_p(ptrs[0]),
+                     ctypes.c_void_p(ptrs[2]), int(n_hi))
+                X.append(torch.from_numpy(rho * (nx * ny / rho.sum())).float().cuda())
+                T.append((g * (nx * ny / g.sum())).view(nx, ny).clone())
+        del hi, lat
+        torch.cuda.empty_cache()
+    return torch.stack(X)[:, None], torch.stack(T)[:, None]
+
+
 def _augment(x, t, code):
     """One of the 8 symmetries of the square (flips of x, of y, transpose)."""
     dims = []
@@ -133,21 +204,32 @@ DEFAULT = "denoiser_128x128.npy"
 
 
 def default_network(max_batch=1):
-    """The shipped network for 128 x 128 grids: trained by `train_default`
-    (8,000 pairs of seed 11, 10 epochs, batch 16, Adam 1e-3 with cosine
-    decay) on this library's own kernels."""
+    """The shipped network for 128 x 128 grids, trained by `train_default`
+    (6,000 synthetic-beam pairs and 2,376 tracked-beam pairs, 10 epochs,
+    batch 16, Adam 1e-3 with cosine decay) on this library's own kernels."""
     net = DeviceDenoiser(128, 128, max_batch=max_batch, seed=5)
     net.set_params(np.load(os.path.join(DATA, DEFAULT)))
     return net
 
 
-def train_default(out_path, n_train=8000, n_test=200, epochs=10, log=print):
-    """Generates the training pairs, trains the 128 x 128 network and saves
-    its parameters; returns the held-out evaluation."""
-    X, T, _ = make_pairs(n_train + n_test, seed=11)
+def train_default(out_path, n_synth=6000, epochs=10, log=print):
+    """Generates the training pairs (synthetic beams of seed 11 and the
+    tracked set-ups of seed 3), trains the 128 x 128 network and saves its
+    parameters; returns held-out evaluations on both kinds of pairs (200
+    synthetic pairs, and every tenth tracked pair, kept out of training)."""
+    import torch
+    Xs, Ts, _ = make_pairs(n_synth + 200, seed=11)
+    Xk, Tk = make_tracked_pairs()
+    test_k = torch.arange(0, Xk.shape[0], 10, device="cuda")
+    keep = torch.ones(Xk.shape[0], dtype=torch.bool, device="cuda")
+    keep[test_k] = False
+    X = torch.cat([Xs[:n_synth], Xk[keep]])
+    T = torch.cat([Ts[:n_synth], Tk[keep]])
     net = DeviceDenoiser(128, 128, max_batch=16, seed=5)
-    train(net, X[:n_train], T[:n_train], epochs=epochs, batch=16, lr=1e-3, log=log)
-    ev = evaluate(net, X[n_train:], T[n_train:])
+    train(net, X, T, epochs=epochs, batch=16, lr=1e-3, log=log)
+    ev = {"synthetic": evaluate(net, Xs[n_synth:], Ts[n_synth:]),
+          "tracked": evaluate(net, Xk[test_k].contiguous(), Tk[test_k].contiguous()),
+          "pairs": int(X.shape[0])}
     np.save(out_path, net.get_params())
     return ev
 
