@@ -49,8 +49,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--form", default="plain", choices=["plain", "fp32"])
-    ap.add_argument("--n", type=int, default=N_PARTICLES)
+    ap.add_argument("--form", default="plain", choices=["plain", "fp32", "learned"],
+                    help="learned: the plain form with the trained denoiser closure, 1e5 particles by default")
+    ap.add_argument("--n", type=int, default=None)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--error-turns", type=int, default=100,
@@ -179,10 +180,66 @@ def build_workload(n, form, seed):
     from spacecharge import SpaceChargeCalc2p5D
     soa = W.c2_coords(n, seed=seed)
     bunch = W.make_bunch(soa, W.C2_MACROSIZE * (N_PARTICLES / n))
-    calc = SpaceChargeCalc2p5D(*GRID, form=form)
+    calc = SpaceChargeCalc2p5D(*GRID, form="plain" if form == "learned" else form)
+    if form == "learned":
+        from orbit_gb300.denoiser import default_network
+        calc.setDenoiser(default_network(), 10, 1e-3)
     with quiet():
         lat = W.fodo_lattice(calc, cells=CELLS)
     return soa, bunch, calc, lat
+
+
+def learned_report(calc, ms_per_turn, n, n_equal=10_000_000, turns=10):
+    """The learned form against the plain form at the particle count of
+    equal field noise (1e7: the network's training targets): one turn's
+    time of the plain form at n_equal (CUDA graphs, bunch resident), and
+    the rms-emittance growth over `turns` turns of plain n_equal, plain n
+    and learned n on the same lattice."""
+    import numpy as np
+    import torch
+    from bunch import BunchTwissAnalysis
+    from orbit_gb300 import workloads as W
+    from orbit_gb300.denoiser import default_network
+    from spacecharge import SpaceChargeCalc2p5D
+
+    def em(b):
+        tw = BunchTwissAnalysis()
+        tw.analyzeBunch(b)
+        return np.array([tw.getEmittance(0), tw.getEmittance(1)])
+
+    def setup(npart, with_net):
+        b = W.make_bunch(W.c2_coords(npart, seed=77), W.C2_MACROSIZE * (N_PARTICLES / npart))
+        c = SpaceChargeCalc2p5D(*GRID)
+        if with_net:
+            c.setDenoiser(default_network(), 10, 1e-3)
+        with quiet():
+            lat = W.fodo_lattice(c, cells=CELLS)
+        return b, c, lat
+
+    b, c, lat = setup(n_equal, False)
+    lat.trackBunchTurns(b, 1)  # records and captures
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lat.trackBunchTurns(b, 3)
+    b._device_bunch().sync()
+    plain_equal_ms = (time.perf_counter() - t0) / 3 * 1e3
+    growth = {}
+    for name, npart, with_net in (("plain_%d" % n_equal, n_equal, False), ("plain_%d" % n, n, False),
+                                  ("learned_%d" % n, n, True)):
+        b, c, lat = setup(npart, with_net)
+        e0 = em(b)
+        lat.trackBunchTurns(b, turns)
+        growth[name] = (em(b) / e0).tolist()
+        if with_net:
+            state = c.getDenoiserState()
+    ref = np.array(growth["plain_%d" % n_equal])
+    return {"equal_noise_particles": n_equal, "plain_equal_noise_ms_per_turn": plain_equal_ms,
+            "speedup_vs_plain_equal_noise": plain_equal_ms / ms_per_turn,
+            "emittance_growth_turns": turns, "emittance_growth": growth,
+            "growth_dev_learned": (np.array(growth["learned_%d" % n]) / ref - 1).tolist(),
+            "growth_dev_plain_same_n": (np.array(growth["plain_%d" % n]) / ref - 1).tolist(),
+            "judge": state, "judge_this_run": calc.getDenoiserState(),
+            "network": "4-level conv encoder-decoder, 302,561 parameters, BF16 weights, shipped training"}
 
 
 def cpu_reference_rate(n_sample, turns, warmup, threads):
@@ -259,7 +316,7 @@ def run_ours(args):
         dist = tdist
     os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("CUDA_VISIBLE_DEVICES", ""))
     torch.cuda.init()
-    n = args.n
+    n = args.n if args.n else (100_000 if args.form == "learned" else N_PARTICLES)
     TRAFFIC.n = n
     soa, bunch, calc, lat = build_workload(n, args.form, seed=1000 + rank)
     prog = lat.fusedProgram(bunch)
@@ -368,8 +425,11 @@ def run_ours(args):
     # how often the Poisson solver grid was reshaped (Green spectrum rebuilt)
     kicks_done, green_done = calc._calc.counters()
     green_rate = green_done / kicks_done if kicks_done else None
+    learned = None
+    if args.form == "learned":
+        learned = learned_report(calc, ms_per_turn=total_ms / args.steps, n=n)
     form_err = None
-    if args.form != "plain" and args.error_turns > 0:
+    if args.form == "fp32" and args.error_turns > 0:
         # accuracy of the reduced-precision form against the FP64 plain form
         # on the same bunch (outside the timed region)
         from orbit_gb300 import workloads as W
@@ -391,7 +451,9 @@ def run_ours(args):
     line = {
         "metric": METRIC, "value": value, "unit": "macroparticle-kicks/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64" if args.form == "plain" else "f32-field/f64-coords",
+        "vs_baseline": None,
+        "dtype": {"plain": "f64", "fp32": "f32-field/f64-coords",
+                  "learned": "f64 + bf16-weight/f32 network"}[args.form],
         "data": "synthetic (seeded 4D waterbag rms 4 mm/0.8 mrad, z~N(0,10 m), dE~N(0,1 MeV))",
         "config": {"workload": "FODO 40 cells x 4 SC nodes, %d particles, grid %dx%dx%d, one turn per step"
                    % (n, *GRID), "form": args.form, "particles": n, "grid": list(GRID),
@@ -403,6 +465,8 @@ def run_ours(args):
     }
     if form_err is not None:
         line["form_error_vs_fp64"] = form_err
+    if learned is not None:
+        line["learned"] = learned
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

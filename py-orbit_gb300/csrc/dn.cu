@@ -19,6 +19,7 @@
 // Tensors are NCHW FP32 in device memory.
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -42,8 +43,9 @@ static const int kCi = 8;   // input channels per shared-memory chunk
 // no bias, no ReLU.  Training batches fill the GPU with 16 x 16 tiles of 16
 // channels; a single image takes smaller blocks (more of them).
 // SPLIT: blockIdx.z = image * splits + part, the block sums input channels
-// [part * ci_per, (part + 1) * ci_per) and adds its partial sums to `out`
-// (zeroed before; bias and ReLU by k_bias_relu after).
+// [part * ci_per, (part + 1) * ci_per) and writes its partial sums to part
+// `part` of `out` (parts of N * cout * H * W each; k_split_reduce adds them
+// in order with the bias and the ReLU).
 template <bool TRANS, bool BIAS_RELU, int TT = kT, int CO = kCo, bool SPLIT = false>
 __global__ void __launch_bounds__(256) k_conv3(const float* __restrict__ in, int cin,
                                                const __nv_bfloat16* __restrict__ w, const float* __restrict__ bias,
@@ -110,7 +112,9 @@ __global__ void __launch_bounds__(256) k_conv3(const float* __restrict__ in, int
       if (co < cout) {
         float v = acc[o];
         if (SPLIT) {
-          atomicAdd(out + (((size_t)n * cout + co) * H + y) * W + x, v);
+          const size_t part = (size_t)((int)blockIdx.z % splits);
+          const size_t nimg = gridDim.z / splits;
+          out[part * nimg * cout * H * W + (((size_t)n * cout + co) * H + y) * W + x] = v;
         } else {
           if (BIAS_RELU) v = fmaxf(v + bias[co], 0.f);
           out[(((size_t)n * cout + co) * H + y) * W + x] = v;
@@ -120,10 +124,14 @@ __global__ void __launch_bounds__(256) k_conv3(const float* __restrict__ in, int
   }
 }
 
-// out[n][c] = max(out[n][c] + b[c], 0) after a split convolution.
-__global__ void k_bias_relu(float* __restrict__ out, const float* __restrict__ b, int C, int HW, size_t n) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    out[i] = fmaxf(out[i] + b[(i / HW) % C], 0.f);
+// out = max(b + sum of the split convolution's parts (in order), 0).
+__global__ void k_split_reduce(const float* __restrict__ part, int splits, const float* __restrict__ b,
+                               float* __restrict__ out, int C, int HW, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    float v = b[(i / HW) % C];
+    for (int q = 0; q < splits; ++q) v += part[(size_t)q * n + i];
+    out[i] = fmaxf(v, 0.f);
+  }
 }
 
 // Weight and bias gradients of a 3x3 convolution:
@@ -518,37 +526,35 @@ static size_t act_size(const orbit_denoiser_t* d, int a, int nb) {
   return (size_t)nb * c * h * w;
 }
 
-// Forward launch shape: 16x16 tiles of 16 channels when that already makes
-// two blocks per SM (training batches); else (a single image) 8x8 tiles of
-// 16 channels, with the input channels split over enough blocks to fill
-// the GPU and the partial sums added atomically.
+// Forward launch plan: 16x16 tiles of 16 output channels; when that makes
+// fewer than two blocks per SM (a single image), the input channels are
+// split over enough blocks to fill the GPU, each writing partial sums to the
+// scratch, summed in order by k_split_reduce.
+static void split_plan(const Conv& cv, int h, int w, int nb, int* splits, int* ci_per) {
+  const long long base = (long long)((w + 15) / 16) * ((h + 15) / 16) * ((cv.cout + 15) / 16) * nb;
+  const int chunks = (cv.cin + kCi - 1) / kCi;
+  int sp = (int)((2LL * num_sms() + base - 1) / base);
+  sp = sp < 1 ? 1 : (sp > chunks ? chunks : sp);
+  *ci_per = ((chunks + sp - 1) / sp) * kCi;
+  *splits = (cv.cin + *ci_per - 1) / *ci_per;
+}
+
 static int conv_fwd(orbit_denoiser_t* d, const Step3& s, int nb, cudaStream_t st) {
   const Conv& cv = d->conv[s.ci];
   int c, h, w;
   act_shape(d, s.out, &c, &h, &w);
   const __nv_bfloat16* W = d->d_pb + cv.w_off;
   const float* B = d->d_p + cv.b_off;
-  long long big = (long long)((w + 15) / 16) * ((h + 15) / 16) * ((cv.cout + 15) / 16) * nb;
-  if (big >= 2LL * num_sms()) {
-    dim3 g(((w + 15) / 16) * ((h + 15) / 16), (cv.cout + 15) / 16, nb);
+  int splits, ci_per;
+  split_plan(cv, h, w, nb, &splits, &ci_per);
+  dim3 g(((w + 15) / 16) * ((h + 15) / 16), (cv.cout + 15) / 16, nb * splits);
+  if (splits == 1) {
     k_conv3<false, true, 16, 16><<<g, 256, 0, st>>>(d->act[s.in], cv.cin, W, B, d->act[s.out], cv.cout, h, w);
   } else {
-    const long long base = (long long)((w + 7) / 8) * ((h + 7) / 8) * ((cv.cout + 15) / 16) * nb;
-    int chunks = (cv.cin + kCi - 1) / kCi;
-    int splits = (int)((2LL * num_sms() + base - 1) / base);
-    splits = splits < 1 ? 1 : (splits > chunks ? chunks : splits);
-    const int ci_per = ((chunks + splits - 1) / splits) * kCi;
-    splits = (cv.cin + ci_per - 1) / ci_per;
-    dim3 g(((w + 7) / 8) * ((h + 7) / 8), (cv.cout + 15) / 16, nb * splits);
-    if (splits == 1) {
-      k_conv3<false, true, 8, 16><<<g, 64, 0, st>>>(d->act[s.in], cv.cin, W, B, d->act[s.out], cv.cout, h, w);
-    } else {
-      const size_t n_out = act_size(d, s.out, nb);
-      ORBIT_CUDA(cudaMemsetAsync(d->act[s.out], 0, sizeof(float) * n_out, st));
-      k_conv3<false, true, 8, 16, true><<<g, 64, 0, st>>>(d->act[s.in], cv.cin, W, B, d->act[s.out], cv.cout, h, w,
+    const size_t n_out = act_size(d, s.out, nb);
+    k_conv3<false, true, 16, 16, true><<<g, 256, 0, st>>>(d->act[s.in], cv.cin, W, B, d->d_scratch, cv.cout, h, w,
                                                           splits, ci_per);
-      k_bias_relu<<<grid_1d(n_out), 256, 0, st>>>(d->act[s.out], B, cv.cout, h * w, n_out);
-    }
+    k_split_reduce<<<grid_1d(n_out), 256, 0, st>>>(d->d_scratch, splits, B, d->act[s.out], cv.cout, h * w, n_out);
   }
   ORBIT_LAUNCH_CHECK("denoiser conv");
   return ORBIT_OK;
@@ -835,6 +841,17 @@ int orbit_denoiser_create(orbit_denoiser_t** out, int max_batch, int h, int w, u
     e = cudaMalloc(&d->act[a], sizeof(float) * n);
     if (e == cudaSuccess) e = cudaMalloc(&d->grad[a], sizeof(float) * n);
   }
+  if (e != cudaSuccess) return fail(cuda_error(e, "orbit_denoiser_create"));
+  // scratch of the split convolutions: the largest splits x output
+  size_t scratch = 1;
+  for (int nb = 1; nb <= max_batch; ++nb)
+    for (const Step3& stp : kSteps) {
+      int c, hh, ww, sp, cp;
+      act_shape(d, stp.out, &c, &hh, &ww);
+      split_plan(d->conv[stp.ci], hh, ww, nb, &sp, &cp);
+      if (sp > 1) scratch = std::max(scratch, (size_t)sp * act_size(d, stp.out, nb));
+    }
+  e = cudaMalloc(&d->d_scratch, sizeof(float) * scratch);
   if (e != cudaSuccess) return fail(cuda_error(e, "orbit_denoiser_create"));
   k_to_bf16<<<grid_1d(off), 256, 0, d->stream>>>(d->d_p, d->d_pb, d->d_isw, off);
   e = cudaStreamSynchronize(d->stream);
