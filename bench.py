@@ -189,6 +189,13 @@ def build_workload(n, form, seed):
     return soa, bunch, calc, lat
 
 
+# Multiply-adds x 2 of one 128 x 128 forward pass of the denoiser: the 14
+# 3x3 convolutions (H W 9 cin cout each) and the 1x1 output.
+DENOISER_GFLOP_128 = 2 * sum(h * h * 9 * ci * co for h, ci, co in (
+    (128, 1, 16), (128, 16, 16), (64, 16, 32), (64, 32, 32), (32, 32, 64), (32, 64, 64), (16, 64, 64), (16, 64, 64),
+    (32, 128, 64), (32, 64, 64), (64, 96, 32), (64, 32, 32), (128, 48, 16), (128, 16, 16))) * 1e-9 + 2 * 128 * 128 * 16e-9
+
+
 def learned_report(calc, ms_per_turn, n, n_equal=10_000_000, turns=10):
     """The learned form against the plain form at the particle count of
     equal field noise (1e7: the network's training targets): one turn's
@@ -239,7 +246,7 @@ def learned_report(calc, ms_per_turn, n, n_equal=10_000_000, turns=10):
             "growth_dev_learned": (np.array(growth["learned_%d" % n]) / ref - 1).tolist(),
             "growth_dev_plain_same_n": (np.array(growth["plain_%d" % n]) / ref - 1).tolist(),
             "judge": state, "judge_this_run": calc.getDenoiserState(),
-            "network": "4-level conv encoder-decoder, 302,561 parameters, BF16 weights, shipped training"}
+            "network_shape": "4-level conv encoder-decoder, 302,561 parameters, BF16 weights, shipped training"}
 
 
 def cpu_reference_rate(n_sample, turns, warmup, threads):
@@ -428,6 +435,13 @@ def run_ours(args):
     learned = None
     if args.form == "learned":
         learned = learned_report(calc, ms_per_turn=total_ms / args.steps, n=n)
+        # the network's arithmetic rate (FP32 CUDA-core FMAs on BF16 weights)
+        net_ms, net_l = prof.get("learn_network", (0.0, 0))
+        if net_ms > 0:
+            gflop = DENOISER_GFLOP_128
+            learned["network"] = {"gflop_per_forward": gflop, "ms_per_forward": net_ms / net_l,
+                                  "achieved_tflops": gflop / (net_ms / net_l) * 1e-3,
+                                  "note": "CUDA-core FP32 FMA; per-launch times of the eager profile"}
     form_err = None
     if args.form == "fp32" and args.error_turns > 0:
         # accuracy of the reduced-precision form against the FP64 plain form
