@@ -59,6 +59,9 @@ def parse():
     ap.add_argument("--workload", default="fodo", choices=["fodo", "batched"],
                     help="fodo: one 1e6-particle bunch (default); batched: the 64-bunch scan")
     ap.add_argument("--members", type=int, default=64, help="bunches of the batched scan")
+    ap.add_argument("--no-report", action="store_true",
+                    help="skip the secondary reports (learned form: plain at equal noise and emittance growth; "
+                         "fp32 form: error report; batched: one-program-per-bunch comparison)")
     return ap.parse_args()
 
 
@@ -434,7 +437,7 @@ def run_ours(args):
     green_rate = green_done / kicks_done if kicks_done else None
     learned = None
     if args.form == "learned":
-        learned = learned_report(calc, ms_per_turn=total_ms / args.steps, n=n)
+        learned = {} if args.no_report else learned_report(calc, ms_per_turn=total_ms / args.steps, n=n)
         # the network's arithmetic rate (FP32 CUDA-core FMAs on BF16 weights)
         net_ms, net_l = prof.get("learn_network", (0.0, 0))
         if net_ms > 0:
@@ -443,7 +446,7 @@ def run_ours(args):
                                   "achieved_tflops": gflop / (net_ms / net_l) * 1e-3,
                                   "note": "CUDA-core FP32 FMA; per-launch times of the eager profile"}
     form_err = None
-    if args.form == "fp32" and args.error_turns > 0:
+    if args.form == "fp32" and args.error_turns > 0 and not args.no_report:
         # accuracy of the reduced-precision form against the FP64 plain form
         # on the same bunch (outside the timed region)
         from orbit_gb300 import workloads as W
@@ -561,12 +564,14 @@ def run_batched(args):
         for _, b, _ in scan:
             b._device_bunch().sync()
 
-    unbatched_turn()  # records the programs and captures their graphs
-    unb_turns = 2
-    t0 = time.perf_counter()
-    for _ in range(unb_turns):
-        unbatched_turn()
-    unb_ms = (time.perf_counter() - t0) * 1e3 / unb_turns
+    unb_ms = None
+    if not args.no_report:
+        unbatched_turn()  # records the programs and captures their graphs
+        unb_turns = 2
+        t0 = time.perf_counter()
+        for _ in range(unb_turns):
+            unbatched_turn()
+        unb_ms = (time.perf_counter() - t0) * 1e3 / unb_turns
     # end to end: upload every bunch from pinned host memory, one turn,
     # download every bunch
     e2e = None
