@@ -56,8 +56,9 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--error-turns", type=int, default=100,
                     help="turns of the rms-emittance and tune-shift error report of a non-plain form")
-    ap.add_argument("--workload", default="fodo", choices=["fodo", "batched"],
-                    help="fodo: one 1e6-particle bunch (default); batched: the 64-bunch scan")
+    ap.add_argument("--workload", default="fodo", choices=["fodo", "batched", "ring"],
+                    help="fodo: one 1e6-particle bunch (default); batched: the 64-bunch scan; "
+                         "ring: the large ring, 1.6e7 particles, 256x256x128")
     ap.add_argument("--members", type=int, default=64, help="bunches of the batched scan")
     ap.add_argument("--no-report", action="store_true",
                     help="skip the secondary reports (learned form: plain at equal noise and emittance growth; "
@@ -178,17 +179,41 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# The single-bunch workloads: coordinates, lattice, intensity, description.
+WL = {"name": "fodo", "n": N_PARTICLES, "intensity": 1e14, "kicks": 160,
+      "desc": "FODO 40 cells x 4 SC nodes"}
+
+
+def wl_coords(n, seed):
+    from orbit_gb300 import workloads as W
+    return W.c5_coords(n, seed=seed) if WL["name"] == "ring" else W.c2_coords(n, seed=seed)
+
+
+def wl_lattice(calc):
+    from orbit_gb300 import workloads as W
+    with quiet():
+        return W.ring_lattice(calc) if WL["name"] == "ring" else W.fodo_lattice(calc, cells=CELLS)
+
+
+def set_workload(name):
+    global GRID
+    if name == "ring":
+        GRID = (256, 256, 128)
+        WL.update({"name": "ring", "n": 16_000_000, "intensity": 1e14, "kicks": 129,
+                   "desc": "large ring: 32 cells, 300 TEAPOT elements (sector bends 2pi/32, FODO quads, "
+                           "sextupoles k2=+-2), 129 SC nodes; KV 6 mm/1 mrad, parabolic 250 m"})
+
+
 def build_workload(n, form, seed):
     from orbit_gb300 import workloads as W
     from spacecharge import SpaceChargeCalc2p5D
-    soa = W.c2_coords(n, seed=seed)
-    bunch = W.make_bunch(soa, W.C2_MACROSIZE * (N_PARTICLES / n))
+    soa = wl_coords(n, seed)
+    bunch = W.make_bunch(soa, WL["intensity"] / n)
     calc = SpaceChargeCalc2p5D(*GRID, form="plain" if form == "learned" else form)
     if form == "learned":
         from orbit_gb300.denoiser import default_network
         calc.setDenoiser(default_network(), 10, 1e-3)
-    with quiet():
-        lat = W.fodo_lattice(calc, cells=CELLS)
+    lat = wl_lattice(calc)
     return soa, bunch, calc, lat
 
 
@@ -260,15 +285,14 @@ def cpu_reference_rate(n_sample, turns, warmup, threads):
     from orbit_gb300 import workloads as W
     from orbit.teapot.recording import BunchRecorder
     from orbit.lattice import AccActionsContainer
-    soa = W.c2_coords(n_sample, seed=99)
+    soa = wl_coords(n_sample, 99)
 
     class _Calc:  # records SC nodes without a GPU calculator
         def trackBunch(self, bunch, length, boundary=None):
             bunch._record_sc(self, length)
 
-    with quiet():
-        lat = W.fodo_lattice(_Calc(), cells=CELLS)
-    bunch = W.make_bunch(soa, W.C2_MACROSIZE * (N_PARTICLES / n_sample))
+    lat = wl_lattice(_Calc())
+    bunch = W.make_bunch(soa, WL["intensity"] / n_sample)
     rec = BunchRecorder(bunch)
     cont = AccActionsContainer()
     cont.addAction(lambda p: p["node"].track(p), AccActionsContainer.BODY)
@@ -304,8 +328,8 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded 4D waterbag, Gaussian z/dE)",
-        "config": {"workload": "FODO 40 cells, 160 SC kicks/turn, grid 128x128x64, sample %d particles"
-                   % CPU_SAMPLE_N, "particles": CPU_SAMPLE_N, "grid": list(GRID), "kicks_per_step": kpt},
+        "config": {"workload": "%s, grid %dx%dx%d, sample %d particles" % (WL["desc"], *GRID, CPU_SAMPLE_N),
+                   "particles": CPU_SAMPLE_N, "grid": list(GRID), "kicks_per_step": kpt},
         "cpu_baseline": {"value": rate, "unit": "macroparticle-kicks/s", "cores": threads, "kind": "port",
                          "sample": "%d particles x 1 turn (%d SC kicks) per step, %d threads as rank slices"
                                    % (CPU_SAMPLE_N, kpt, threads)},
@@ -326,7 +350,7 @@ def run_ours(args):
         dist = tdist
     os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("CUDA_VISIBLE_DEVICES", ""))
     torch.cuda.init()
-    n = args.n if args.n else (100_000 if args.form == "learned" else N_PARTICLES)
+    n = args.n if args.n else (100_000 if args.form == "learned" else WL["n"])
     TRAFFIC.n = n
     soa, bunch, calc, lat = build_workload(n, args.form, seed=1000 + rank)
     prog = lat.fusedProgram(bunch)
@@ -420,7 +444,7 @@ def run_ours(args):
                 else "fallback 6.8 TB/s",
                 "kernel_ms_per_launch": per_launch_ms, "share_of_turn": dom_ms / turn_ms,
                 "kernels": {k: {"ms": v[0], "launches": v[1], "share": v[0] / turn_ms} for k, v in prof.items()}}
-    if args.form == "plain":
+    if args.form == "plain" and WL["name"] == "fodo":
         # the plain form is bound by the FP64 pipe: counted FP64 instructions
         # of the fused passes and of the deposit against the live DFMA peak
         peak_inst = fp64_peak / 2 * 1e12
@@ -473,8 +497,8 @@ def run_ours(args):
         "dtype": {"plain": "f64", "fp32": "f32-field/f64-coords",
                   "learned": "f64 + bf16-weight/f32 network"}[args.form],
         "data": "synthetic (seeded 4D waterbag rms 4 mm/0.8 mrad, z~N(0,10 m), dE~N(0,1 MeV))",
-        "config": {"workload": "FODO 40 cells x 4 SC nodes, %d particles, grid %dx%dx%d, one turn per step"
-                   % (n, *GRID), "form": args.form, "particles": n, "grid": list(GRID),
+        "config": {"workload": "%s, %d particles, grid %dx%dx%d, one turn per step" % (WL["desc"], n, *GRID),
+                   "form": args.form, "particles": n, "grid": list(GRID),
                    "kicks_per_step": kicks_per_turn, "l2": "flushed (512 MiB write) before each timed step",
                    "parallelism": "replicas" if world > 1 else "single",
                    "green_rebuilds_per_kick": green_rate},
@@ -500,6 +524,8 @@ class _Traffic(dict):
     n = N_PARTICLES
 
     def get(self, key, default=None):
+        if WL["name"] != "fodo":  # captured on the FODO workload only
+            return None
         v = TRAFFIC_PER_PARTICLE.get(key)
         return None if v is None else v * self.n
 
@@ -652,6 +678,7 @@ def run_batched(args):
 
 def main():
     args = parse()
+    set_workload(args.workload)
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batched":

@@ -15,6 +15,12 @@ C3  batched scan: 64 bunches, particle counts log-uniform in [5e4, 2e6],
     dE ~ N(0, 1 MeV)), intensities log-uniform in [1e12, 2e14] protons,
     FODO k1 uniform in [0.3, 0.7] m^-2 (the C2 lattice otherwise), grids
     drawn from 64x64x32, 128x128x64 and 256x256x64.
+C5  large ring: 1.6e7 protons at 1 GeV, 4D KV with rms 6 mm / 1 mrad,
+    parabolic line density over 250 m, dE ~ N(0, 1 MeV) (not named by the
+    configuration); grid 256x256x128; 32 cells of 7.8 m (249.6 m) with FODO
+    quads, sector bends of 2 pi/32 and sextupoles of k2 = +-2 m^-3, 300
+    TEAPOT elements, 128 SC nodes.  The configuration names no intensity:
+    1e14 protons is used.
 """
 from __future__ import annotations
 
@@ -122,6 +128,73 @@ def fodo_lattice(calc, cells=40, kq=0.5, lq=0.5, ld=2.0, sc_min=0.3):
         d2 = DriftTEAPOT("d2_%d" % c)
         d2.setLength(ld)
         for node in (qf, d1, qd, d2):
+            lat.addNode(node)
+    lat.initialize()
+    if calc is not None:
+        setSC2p5DAccNodes(lat, sc_min, calc)
+    return lat
+
+
+C5_INTENSITY = 1e14
+
+
+def c5_coords(n=16_000_000, seed=20240605):
+    """4D KV beam (points on the surface of the 4D unit sphere, scaled to
+    rms 6 mm / 1 mrad: semi-axes twice the rms), parabolic line density on
+    [-125, 125] m (the median of three uniforms has the density
+    3/4 (1 - u^2)), dE ~ N(0, 1 MeV)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    soa = np.empty((6, n))
+    g = rng.normal(size=(4, n))
+    g /= np.sqrt((g * g).sum(axis=0))
+    soa[0], soa[1], soa[2], soa[3] = 12e-3 * g[0], 2e-3 * g[1], 12e-3 * g[2], 2e-3 * g[3]
+    del g
+    u = rng.uniform(-1.0, 1.0, (3, n))
+    soa[4] = 125.0 * np.median(u, axis=0)
+    del u
+    soa[5] = rng.normal(0.0, 1e-3, n)
+    return soa
+
+
+def ring_lattice(calc, cells=32, kq=0.5, k2=2.0, sc_min=1.4):
+    """cells x [QF, D, SF, D, B, D, QD, D, SD] (7.8 m), the first drift of
+    the first 12 cells in two halves: 300 TEAPOT elements for 32 cells;
+    sector bends of 2 pi/32, sextupoles of k2 = +-k2 (MultipoleTEAPOT, pole
+    2, kl = k2 * 0.2 m), 2.5D SC nodes placed by the reference rule with
+    sc_min = 1.4 m (129 nodes for 32 cells)."""
+    import math
+
+    from orbit.space_charge.sc2p5d import setSC2p5DAccNodes
+    from orbit.teapot import BendTEAPOT, DriftTEAPOT, MultipoleTEAPOT, QuadTEAPOT, TEAPOT_Lattice
+    lat = TEAPOT_Lattice("ring")
+
+    def drift(name, length):
+        d = DriftTEAPOT(name)
+        d.setLength(length)
+        return d
+
+    def quad(name, k):
+        q = QuadTEAPOT(name)
+        q.setLength(0.5)
+        q.addParam("kq", k)
+        return q
+
+    def sext(name, k):
+        m = MultipoleTEAPOT(name)
+        m.setLength(0.2)
+        m.addParam("poles", [2])
+        m.addParam("kls", [k * 0.2])
+        m.addParam("skews", [0])
+        return m
+
+    for c in range(cells):
+        b = BendTEAPOT("b%d" % c)
+        b.setLength(2.0)
+        b.addParam("theta", 2.0 * math.pi / 32)
+        first = [drift("d1a_%d" % c, 0.85), drift("d1b_%d" % c, 0.85)] if c < 12 else [drift("d1_%d" % c, 1.7)]
+        for node in [quad("qf%d" % c, kq)] + first + [sext("sf%d" % c, k2), drift("d2_%d" % c, 0.5), b,
+                                                      drift("d3_%d" % c, 0.5), quad("qd%d" % c, -kq),
+                                                      drift("d4_%d" % c, 1.7), sext("sd%d" % c, -k2)]:
             lat.addNode(node)
     lat.initialize()
     if calc is not None:
