@@ -1,7 +1,7 @@
-"""Grids too large for one block's shared memory (256x256 and a 300x180
-plain-form grid): the deposit splits the grid into row bands with halo
-rows, each block deposits the particles whose centre row it owns.  Against
-the oracle after one kick and after several, with uniform and per-particle
+"""Grids too large for one block's shared memory (256x256, 300x180,
+400x300): the deposit splits the grid into row bands with halo rows, each
+block depositing the particles whose centre row it owns.  Against the
+oracle after one kick and after several, with uniform and per-particle
 macrosizes.
 
 Tolerances (max-norm relative): rho, phi, line density and kicks 1e-12;
@@ -30,8 +30,8 @@ def oracle_sync_of(b):
                        charge=b.charge(), classical_radius=b.classicalRadius(), macrosize=b.macroSize())
 
 
-@pytest.mark.parametrize("grid,n", [((256, 256, 32), 200_000), ((300, 180, 16), 120_000)])
-def test_band_deposit_single_kick_against_oracle(grid, n):
+@pytest.mark.parametrize("grid,n", [((256, 256, 32), 200_000), ((300, 180, 16), 120_000), ((400, 300, 16), 150_000)])
+def test_large_grid_deposit_single_kick_against_oracle(grid, n):
     from orbit_gb300 import workloads as W
     from spacecharge import SpaceChargeCalc2p5D
     soa = W.c2_coords(n, seed=41)
@@ -50,7 +50,7 @@ def test_band_deposit_single_kick_against_oracle(grid, n):
         assert rel_err(got[c] - soa[c], a[c] - soa[c]) <= TOL_FIELD * 10, c
 
 
-def test_band_deposit_per_particle_macrosizes_and_many_kicks():
+def test_large_grid_deposit_per_particle_macrosizes_and_many_kicks():
     from orbit_gb300 import workloads as W
     from spacecharge import SpaceChargeCalc2p5D
     n = 100_000
