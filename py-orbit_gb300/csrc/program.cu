@@ -269,6 +269,16 @@ int compile(orbit_program_t* p, orbit_bunch_t* bu, Plan& plan) {
     }
   }
   seg_ops.push_back({start, (int)p->ops.size()});
+  // Maps that add to x, y and z a term linear in their length and change
+  // neither xp, yp nor dE (drift; quad2 = bend2) compose by adding lengths:
+  // drift(L1) drift(L2) = drift(L1+L2) and quad2(L1) quad2(L2) =
+  // quad2(L1+L2), equal in exact arithmetic (each reads only xp, yp and
+  // dp_p, which the other leaves alone), one rounding per coordinate instead
+  // of two.  The reference's quad schedule issues quad2(L) twice in a row
+  // when the element has no multipoles (teapot.py:945-960).
+  auto lengthwise = [](int code) {
+    return code == ORBIT_OP_DRIFT ? 1 : (code == ORBIT_OP_QUAD2 || code == ORBIT_OP_BEND2) ? 2 : 0;
+  };
   auto emit = [&](int a, int b) -> Seg {
     Seg s;
     s.a = (int)dev.size();
@@ -279,7 +289,12 @@ int compile(orbit_program_t* p, orbit_bunch_t* bu, Plan& plan) {
       if (!compile_op(p->ops[k], bu->sync, d, &adv)) return Seg{-1, -1, false};
       p->time_adv[k] = adv;
       if (d.code == ORBIT_OP_WEDGEROT || (d.code == ORBIT_OP_KICK && d.c[2] != 0.)) s.dE = true;
-      if (d.code != 0) dev.push_back(d);
+      if (d.code == 0) continue;
+      if (lengthwise(d.code) && (int)dev.size() > s.a && lengthwise(dev.back().code) == lengthwise(d.code)) {
+        dev.back().c[0] += d.c[0];
+        continue;
+      }
+      dev.push_back(d);
     }
     s.b = (int)dev.size();
     return s;
