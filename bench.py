@@ -61,7 +61,7 @@ def parse():
                          "ring: the large ring, 1.6e7 particles, 256x256x128")
     ap.add_argument("--members", type=int, default=64, help="bunches of the batched scan")
     ap.add_argument("--no-report", action="store_true",
-                    help="skip the secondary reports (learned form: plain at equal noise and emittance growth; "
+                    help="skip the secondary reports (learned form: plain at equal density and force noise, emittance growth; "
                          "fp32 form: error report; batched: one-program-per-bunch comparison)")
     return ap.parse_args()
 
@@ -226,16 +226,20 @@ DENOISER_GFLOP_128 = 2 * sum(h * h * 9 * ci * co for h, ci, co in (
 
 
 def learned_report(calc, ms_per_turn, n, n_equal=10_000_000, turns=10):
-    """The learned form against the plain form at the particle count of
-    equal field noise (1e7: the network's training targets): one turn's
-    time of the plain form at n_equal (CUDA graphs, bunch resident), and
-    the rms-emittance growth over `turns` turns of plain n_equal, plain n
-    and learned n on the same lattice."""
+    """The learned form against the plain form at two particle counts: equal
+    density noise (1e7, the network's training targets) and equal force
+    noise (n times the network's measured gain in force error on 96 held-out
+    synthetic beams, which is far below its gain in density error: the
+    force weights beam-scale noise by 1/k^2 and a single snapshot cannot
+    tell that noise from beam structure).  Reports one turn's time of the
+    plain form at both counts (CUDA graphs, bunch resident) and the
+    rms-emittance growth over `turns` turns of plain n_equal, plain n and
+    learned n on the same lattice."""
     import numpy as np
     import torch
     from bunch import BunchTwissAnalysis
     from orbit_gb300 import workloads as W
-    from orbit_gb300.denoiser import default_network
+    from orbit_gb300.denoiser import default_network, evaluate, make_pairs
     from spacecharge import SpaceChargeCalc2p5D
 
     def em(b):
@@ -252,13 +256,21 @@ def learned_report(calc, ms_per_turn, n, n_equal=10_000_000, turns=10):
             lat = W.fodo_lattice(c, cells=CELLS)
         return b, c, lat
 
-    b, c, lat = setup(n_equal, False)
-    lat.trackBunchTurns(b, 1)  # records and captures
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    lat.trackBunchTurns(b, 3)
-    b._device_bunch().sync()
-    plain_equal_ms = (time.perf_counter() - t0) / 3 * 1e3
+    def plain_turn_ms(npart):
+        b, c, lat = setup(npart, False)
+        lat.trackBunchTurns(b, 1)  # records and captures
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        lat.trackBunchTurns(b, 3)
+        b._device_bunch().sync()
+        return (time.perf_counter() - t0) / 3 * 1e3
+
+    X, T, _ = make_pairs(96, seed=999)
+    ev = evaluate(default_network(max_batch=16), X, T, force=True)
+    del X, T
+    n_force = int(round(n * ev["gain_force"]))
+    plain_force_ms = plain_turn_ms(n_force)
+    plain_equal_ms = plain_turn_ms(n_equal)
     growth = {}
     for name, npart, with_net in (("plain_%d" % n_equal, n_equal, False), ("plain_%d" % n, n, False),
                                   ("learned_%d" % n, n, True)):
@@ -269,8 +281,11 @@ def learned_report(calc, ms_per_turn, n, n_equal=10_000_000, turns=10):
         if with_net:
             state = c.getDenoiserState()
     ref = np.array(growth["plain_%d" % n_equal])
-    return {"equal_noise_particles": n_equal, "plain_equal_noise_ms_per_turn": plain_equal_ms,
-            "speedup_vs_plain_equal_noise": plain_equal_ms / ms_per_turn,
+    return {"equal_density_noise_particles": n_equal, "plain_equal_density_noise_ms_per_turn": plain_equal_ms,
+            "speedup_vs_plain_equal_density_noise": plain_equal_ms / ms_per_turn,
+            "network_gain": {k: ev[k] for k in ("gain", "gain_force", "gain_by_k", "k_bands")},
+            "equal_force_noise_particles": n_force, "plain_equal_force_noise_ms_per_turn": plain_force_ms,
+            "speedup_vs_plain_equal_force_noise": plain_force_ms / ms_per_turn,
             "emittance_growth_turns": turns, "emittance_growth": growth,
             "growth_dev_learned": (np.array(growth["learned_%d" % n]) / ref - 1).tolist(),
             "growth_dev_plain_same_n": (np.array(growth["plain_%d" % n]) / ref - 1).tolist(),

@@ -181,11 +181,14 @@ def train(net: DeviceDenoiser, X, T, epochs=4, batch=16, lr=1e-3, seed=0, log=No
     return out
 
 
-def evaluate(net: DeviceDenoiser, X, T, batch=16):
+def evaluate(net: DeviceDenoiser, X, T, batch=16, force=False):
     """Mean squared error of the raw inputs and of the network outputs
-    against the targets, and the particle count whose raw deposit would
-    have the network's error (noise variance ~ 1/N, from the 1e5-particle
-    inputs)."""
+    against the targets and its ratio (`gain`).  With `force`, also the
+    ratio of the force errors (`gain_force`, see `force_error`) and the
+    ratio of the error spectra per band of |k| (`gain_by_k`, K_BANDS): the
+    density error weights all wavelengths alike, the force error weights
+    them by 1/k^2, so beam-scale noise, which a single snapshot cannot tell
+    from beam structure, dominates it."""
     import torch
     n = X.shape[0]
     out = torch.empty_like(X)
@@ -196,7 +199,55 @@ def evaluate(net: DeviceDenoiser, X, T, batch=16):
     torch.cuda.synchronize()
     mse_raw = float(((X - T) ** 2).mean())
     mse_net = float(((out - T) ** 2).mean())
-    return {"mse_raw": mse_raw, "mse_net": mse_net, "gain": mse_raw / mse_net}
+    ev = {"mse_raw": mse_raw, "mse_net": mse_net, "gain": mse_raw / mse_net}
+    if force:
+        f_raw, s_raw = force_error(X, T)
+        f_net, s_net = force_error(out, T)
+        ev.update({"force_raw": f_raw, "force_net": f_net, "gain_force": f_raw / f_net,
+                   "gain_by_k": [a / b for a, b in zip(s_raw, s_net)], "k_bands": list(K_BANDS)})
+    return ev
+
+
+K_BANDS = (0.0, 0.02, 0.04, 0.08, 0.16, 0.32, 0.8)  # |k| in cycles per cell
+
+
+def force_error(Y, T, bands=K_BANDS):
+    """How far images Y are from targets T in the force they produce, the
+    quantity that moves particles (evaluation only; the kick path uses the
+    library's own solver).  Both are (n, 1, nx, ny) densities on a grid of
+    unit steps; the potential is the open-boundary convolution with
+    -ln(r) / 2 on the doubled grid (the Hockney scheme of the calculator,
+    PoissonSolverFFT2D.cc:174-256, at dx = dy), the force its central
+    difference.  Returns (force error energy / target force energy, the
+    error's power spectrum averaged over the bands of |k|)."""
+    import torch
+    dev = Y.device
+    n, _, nx, ny = Y.shape
+    i = torch.arange(2 * nx, device=dev, dtype=torch.float64)
+    j = torch.arange(2 * ny, device=dev, dtype=torch.float64)
+    i = torch.minimum(i, 2 * nx - i)
+    j = torch.minimum(j, 2 * ny - j)
+    r2 = i[:, None] ** 2 + j[None, :] ** 2
+    G = -0.5 * torch.log(r2.clamp(min=1.0))
+    G[0, 0] = 0.0
+    Gk = torch.fft.rfft2(G)
+
+    def force(rho):
+        p = torch.zeros(rho.shape[0], 2 * nx, 2 * ny, device=dev, dtype=torch.float64)
+        p[:, :nx, :ny] = rho
+        phi = torch.fft.irfft2(torch.fft.rfft2(p) * Gk, s=(2 * nx, 2 * ny))[:, :nx, :ny]
+        return phi[:, 2:, 1:-1] - phi[:, :-2, 1:-1], phi[:, 1:-1, 2:] - phi[:, 1:-1, :-2]
+
+    y, t = Y[:, 0].double(), T[:, 0].double()
+    tx, ty = force(t)
+    ex, ey = force(y)
+    rel = float(((ex - tx) ** 2 + (ey - ty) ** 2).sum() / (tx ** 2 + ty ** 2).sum())
+    P = (torch.fft.fft2(y - t).abs() ** 2).mean(0)
+    kx = torch.fft.fftfreq(nx, device=dev, dtype=torch.float64).abs()
+    ky = torch.fft.fftfreq(ny, device=dev, dtype=torch.float64).abs()
+    kr = torch.sqrt(kx[:, None] ** 2 + ky[None, :] ** 2)
+    spec = [float(P[(kr >= bands[b]) & (kr < bands[b + 1])].mean()) for b in range(len(bands) - 1)]
+    return rel, spec
 
 
 DATA = os.path.join(os.path.dirname(__file__), "data")
