@@ -40,8 +40,7 @@ __device__ __forceinline__ void pass_body(double* __restrict__ cx, double* __res
   const float* Lf = kick.lam_f;
   extern __shared__ unsigned char s_raw[];
   if (KF != 0) {
-    load_kick_const(k, kick.st, kick.host_factor, kick.nx, kick.ny, kick.nz);
-    if (KF == 1) load_kick_fix(kf, kick.st, kick.host_factor, kick.nx, kick.ny, kick.nz);
+    load_kick_block(k, KF == 1 ? &kf : nullptr, kick.st, kick.host_factor, kick.nx, kick.ny, kick.nz);
     if (KSMEM) {
       int ng = kick.nx * kick.ny;
       if (KF == 1) {
@@ -73,7 +72,8 @@ __device__ __forceinline__ void pass_body(double* __restrict__ cx, double* __res
       p.knl_ok = true;
     }
     if (KF == 1 && !k.skip && bnd_inside(kick.bnd, p.x, p.y)) {
-      if (!kick_fixed(kf, P, Lm, p.x, p.y, p.z, p.xp, p.yp)) kick_plain(k, kick.phi, kick.lam, p.x, p.y, p.z, p.xp, p.yp);
+      if (!kick_fixed(kf, P, Lm, p.x, p.y, p.z, p.xp, p.yp))
+        kick_plain(k, kick.phi, kick.lam, p.x, p.y, p.z, p.xp, p.yp);
       if (kick.lamd) {  // 2.5Drb: longitudinal kick; dE changed
         RbConst r;
         load_rb_const(r, kick.st, kick.rb_lsf);

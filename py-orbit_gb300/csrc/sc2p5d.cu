@@ -663,10 +663,9 @@ __global__ void k_kick_plain(const double* __restrict__ x, double* __restrict__ 
                              double host_factor, int nx, int ny, int nz, const double* __restrict__ lamd,
                              double rb_lsf, double* __restrict__ dE, BndShape bnd) {
   KickConst k;
-  load_kick_const(k, st, host_factor, nx, ny, nz);
-  if (k.skip) return;
   KickFix kf;
-  load_kick_fix(kf, st, host_factor, nx, ny, nz);
+  load_kick_block(k, &kf, st, host_factor, nx, ny, nz);
+  if (k.skip) return;
   extern __shared__ long long s_phix[];
   const long long* P = phi_fix;
   const long long* Lm = lam_fix;

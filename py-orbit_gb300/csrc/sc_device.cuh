@@ -670,6 +670,25 @@ __device__ __forceinline__ void load_kick_fix(KickFix& k, const ScState* st, dou
   k.skip = st->skip;
 }
 
+// The kick constants computed once per block (thread 0) and copied to every
+// thread: a thread of a 512-thread block handles only ~13 particles of a
+// 1e6-particle bunch, and the set-up holds two FP64 divisions, which on
+// GB300 occupy the FP64 pipe that bounds the fused pass.  (Reading the
+// constants from shared memory inside the particle loop instead spills
+// registers there and is slower.)  Every thread of the block must call it.
+__device__ __forceinline__ void load_kick_block(KickConst& k, KickFix* kf, const ScState* st, double host_factor,
+                                                int nx, int ny, int nz) {
+  __shared__ KickConst s_k;
+  __shared__ KickFix s_kf;
+  if (threadIdx.x == 0) {
+    load_kick_const(s_k, st, host_factor, nx, ny, nz);
+    if (kf) load_kick_fix(s_kf, st, host_factor, nx, ny, nz);
+  }
+  __syncthreads();
+  k = s_k;
+  if (kf) *kf = s_kf;
+}
+
 __device__ __forceinline__ long long phi_fixed(double v, int s) {
   long long r;
   return fix_of(v, s, r) ? r : 0;
