@@ -116,6 +116,12 @@ bool compile_op(const orbit_op_t& in, const orbit_sync_t& s, DevOp& o, double* t
       double sg = (in.code == ORBIT_OP_MPFRIN) ? -1.0 : 1.0;
       if (in.i1) { o.c[0] = 0.0 * sg; o.c[1] = sg * kf; }
       else { o.c[0] = sg * kf; o.c[1] = 0.0 * sg; }
+      double l = (double)(in.i0 + 1);  // the integer factors of the regrouped terms
+      o.c[2] = l;
+      o.c[3] = l + 2.0;
+      o.c[4] = l * (l + 1.0);
+      o.c[5] = (l + 1.0) * (l + 2.0);
+      o.c[6] = (l + 1.0) * (l - 2.0);
       return true;
     }
     case ORBIT_OP_ROTXY:

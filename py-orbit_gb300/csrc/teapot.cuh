@@ -51,53 +51,68 @@ __device__ __forceinline__ void drift_body(Part& p, const MapCtx& m, double L) {
   p.z -= L * phifac;
 }
 
-// complex helpers
-struct dcx { double re, im; };
-__device__ __forceinline__ dcx cmul(dcx a, dcx b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
-__device__ __forceinline__ dcx cadd(dcx a, dcx b) { return {a.re + b.re, a.im + b.im}; }
-__device__ __forceinline__ dcx csub(dcx a, dcx b) { return {a.re - b.re, a.im - b.im}; }
-
-// multpfringeIN/OUT body (teapotbase.cc:436-486, 549-599); the sign of
-// kterm (IN: -kterm, OUT: +kterm) is folded into c[0], c[1] on the host.
-__device__ __forceinline__ void multpfringe_body(Part& p, const MapCtx& m, int pole, double ktre, double ktim) {
+// multpfringeIN/OUT (teapotbase.cc:395-486, 508-599), with l = pole + 1,
+// z = x + i y and kt the signed kterm (IN: -kterm, OUT: +kterm, folded in
+// on the host).  The reference forms six complex products and keeps their
+// real parts; their terms satisfy, exactly,
+//   dxfxterm = l(l+1) conj(z),      dyfyterm = -l(l+1) conj(z),
+//   dyfxterm = (l+1)((l+2) y, (l-2) x),  dxfyterm = (l+1)((l-2) y, (l+2) x),
+// so with kt z^(l-1) = A + i B and kt z^l = C + i D the six real parts are
+//   dxfxcx = l(l+1)(A x + B y) = -dyfycx,
+//   dyfxcx = (l+1)(l+2) A y - (l+1)(l-2) B x,
+//   dxfycx = (l+1)(l-2) A y - (l+1)(l+2) B x,
+//   fxcx = l C x + (l+2) D y,  fycx = l C y - (l+2) D x,
+// and detM = 1 - e with e = u^2 + M12 M21 (u = dxfxcx KNL), whose inverse
+// is a short series for small e.  46 FP64 instructions instead of ~110 and
+// two divisions; the results differ from the reference's by roundings.  Every
+// sum is an explicit FMA, so every kernel that inlines it rounds alike.
+// c = {kt_re, kt_im, l, l+2, l(l+1), (l+1)(l+2), (l+1)(l-2)}, i0 = pole.
+__device__ __forceinline__ void multpfringe_body(Part& p, const MapCtx& m, const DevOp& o) {
   ensure_knl(p, m);
-  double x = p.x, y = p.y, px = p.xp, py = p.yp, KNL = p.knl;
-  dcx z = {x, y};
-  int l = pole + 1, lp2 = pole + 3;
-  dcx zlm1 = {1.0, 0.0};
-  for (int k = 0; k < pole; k++) zlm1 = cmul(zlm1, z);
-  dcx zl = cmul(zlm1, z);
-  double dl = (double)l, dlp2 = (double)lp2;
-  dcx fxterm = {dl * x, -dlp2 * y};
-  dcx dxfxterm = {dl * (fxterm.re + x), dl * (fxterm.im + y)};
-  // i * (l*fxterm - lp2*z)
-  dcx tq = {dl * fxterm.re - dlp2 * x, dl * fxterm.im - dlp2 * y};
-  dcx dyfxterm = {-tq.im, tq.re};
-  dcx fyterm = {dl * y, dlp2 * x};
-  // l*fyterm + i*lp2*z
-  dcx dxfyterm = {dl * fyterm.re - dlp2 * y, dl * fyterm.im + dlp2 * x};
-  // l*(i*fyterm + z)
-  dcx dyfyterm = {dl * (-fyterm.im + x), dl * (fyterm.re + y)};
-  dcx kt = {ktre, ktim};
-  dcx kzl = cmul(kt, zl), kzm = cmul(kt, zlm1);
-  double fxcx = cmul(kzl, fxterm).re;
-  double dxfxcx = cmul(kzm, dxfxterm).re;
-  double dyfxcx = cmul(kzm, dyfxterm).re;
-  double fycx = cmul(kzl, fyterm).re;
-  double dxfycx = cmul(kzm, dxfyterm).re;
-  double dyfycx = cmul(kzm, dyfyterm).re;
-  p.x -= fxcx * KNL;
-  p.y -= fycx * KNL;
-  double M11 = 1.0 - dxfxcx * KNL;
-  double M12 = -dxfycx * KNL;
-  double M21 = -dyfxcx * KNL;
-  double M22 = 1.0 - dyfycx * KNL;
-  double detM = M11 * M22 - M12 * M21;
-  double pxnew = (M22 * px - M12 * py) / detM;
-  double pynew = (-M21 * px + M11 * py) / detM;
+  const double x = p.x, y = p.y, px = p.xp, py = p.yp, KNL = p.knl;
+  double zr = 1.0, zi = 0.0;  // z^(l-1)
+  if (o.i0 > 0) {
+    zr = x;
+    zi = y;
+    for (int q = 1; q < o.i0; ++q) {
+      double t = fma(zr, x, -(zi * y));
+      zi = fma(zr, y, zi * x);
+      zr = t;
+    }
+  }
+  const double ktr = o.c[0], kti = o.c[1];
+  const double A = fma(ktr, zr, -(kti * zi)), B = fma(ktr, zi, kti * zr);
+  const double C = fma(A, x, -(B * y)), D = fma(A, y, B * x);
+  const double lC = o.c[2] * C, lp2D = o.c[3] * D;
+  const double fx = fma(lC, x, lp2D * y);
+  const double fy = fma(lC, y, -(lp2D * x));
+  const double dxfx = o.c[4] * fma(A, x, B * y);
+  const double dyfx = fma(o.c[5] * A, y, -((o.c[6] * B) * x));
+  const double dxfy = fma(o.c[6] * A, y, -((o.c[5] * B) * x));
+  p.x = fma(-fx, KNL, x);
+  p.y = fma(-fy, KNL, y);
+  const double u = dxfx * KNL;  // M11 = 1 - u, M22 = 1 + u
+  const double M12 = -(dxfy * KNL), M21 = -(dyfx * KNL);
+  const double e = fma(u, u, M12 * M21);  // detM = 1 - e
+  const double nxp = fma(-M12, py, fma(u, px, px));   // M22 px - M12 py
+  const double nyp = fma(-M21, px, fma(-u, py, py));  // -M21 px + M11 py
+  const long long eb = __double_as_longlong(e) & 0x7FFFFFFFFFFFFFFFll;
+  double pxnew, pynew;
+  if (eb < 0x3E40000000000000ll) {  // |e| < 2^-27: 1/(1-e) = 1 + e + O(2^-54)
+    pxnew = fma(nxp, e, nxp);
+    pynew = fma(nyp, e, nyp);
+  } else if (eb < 0x3EB0000000000000ll) {  // |e| < 2^-20: 1 + e + e^2
+    const double w = fma(e, e, e);
+    pxnew = fma(nxp, w, nxp);
+    pynew = fma(nyp, w, nyp);
+  } else {
+    const double detM = __dsub_rn(1.0, e);
+    pxnew = nxp / detM;
+    pynew = nyp / detM;
+  }
   p.xp = pxnew;
   p.yp = pynew;
-  p.z -= (pxnew * fxcx + pynew * fycx) * KNL * KNL;
+  p.z = fma(-(fma(pxnew, fx, pynew * fy) * KNL), KNL, p.z);
 }
 
 // Applies ops[a..b) to one particle.
@@ -212,23 +227,32 @@ __device__ __forceinline__ void apply_ops(Part& p, const DevOp* __restrict__ ops
       }
       case ORBIT_OP_MULTP: {  // multp (teapotbase.cc:336-374); i0 = pole, i1 = skew, c0 = kl/pole!
         if (m.charge == 0.) break;
-        dcx z = {p.x, p.y};
-        dcx zn = {1.0, 0.0};
-        for (int q = 0; q < o.i0; q++) zn = cmul(zn, z);
+        // z^pole from z (the reference starts its loop from 1), kl/pole! on
+        // the host; sums are explicit FMAs
+        double zr = 1.0, zi = 0.0;
+        if (o.i0 > 0) {
+          zr = p.x;
+          zi = p.y;
+          for (int q = 1; q < o.i0; ++q) {
+            double t = fma(zr, p.x, -(zi * p.y));
+            zi = fma(zr, p.y, zi * p.x);
+            zr = t;
+          }
+        }
         double kl1 = o.c[0];
         if (o.i1) {
-          p.xp += kl1 * zn.im;
-          p.yp += kl1 * zn.re;
+          p.xp = fma(kl1, zi, p.xp);
+          p.yp = fma(kl1, zr, p.yp);
         } else {
-          p.xp -= kl1 * zn.re;
-          p.yp += kl1 * zn.im;
+          p.xp = fma(-kl1, zr, p.xp);
+          p.yp = fma(kl1, zi, p.yp);
         }
         break;
       }
       case ORBIT_OP_MPFRIN:
       case ORBIT_OP_MPFROUT:  // c0, c1 = signed kterm (re, im)
         if (m.charge == 0.) break;
-        multpfringe_body(p, m, o.i0, o.c[0], o.c[1]);
+        multpfringe_body(p, m, o);
         break;
       case ORBIT_OP_ROTXY: {  // rotatexy (teapotbase.cc:80-101); c0 = cos, c1 = sin
         double cs = o.c[0], sn = o.c[1];

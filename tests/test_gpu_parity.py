@@ -131,6 +131,28 @@ def test_hundred_kicks_fodo():
     assert rel_err(got[1], soa[1]) > 1e-3
 
 
+def test_ring_cells_fused_program():
+    """Four cells of the large-ring lattice (sector bends with their four
+    maps and fringes, sextupoles with multp and the multipole fringes,
+    quads, drifts) fused on the GPU, two turns (32 kicks), against the
+    oracle within 1e-10."""
+    from orbit_gb300 import workloads as W
+    from spacecharge import SpaceChargeCalc2p5D
+    soa = W.c5_coords(20_000, seed=11)
+    b = gpu_bunch(soa, 5e9)
+    calc = SpaceChargeCalc2p5D(32, 32, 16)
+    lat = W.ring_lattice(calc, cells=4)
+    prog = lat.fusedProgram(b)
+    from orbit_gb300 import OP
+    inv = {v: k for k, v in OP.items()}
+    assert {"MPFRIN", "MPFROUT", "MULTP", "BEND3", "BEND4", "BFRIN", "BFROUT"} <= {inv[c] for c, _, _ in prog.ops}
+    lat.trackBunchTurns(b, 2)
+    got = b.getCoordinates()
+    ref, _ = run_oracle_program(prog.ops, soa, oracle_sync_of(b), [(32, 32, 16)], turns=2)
+    assert coord_err(got, ref) <= TOL_COORD
+    assert rel_err(got[1], soa[1]) > 1e-3
+
+
 def test_benchmark_grid_fused_program():
     """The benchmark's grid (128x128x64): shared-memory grids of 128 KiB, one
     block per SM, register-limited block sizes; fused program vs oracle."""
