@@ -86,6 +86,15 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def measured_bf16_tflops():
+    """The measured dense bf16 GEMM rate (burst), or None."""
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f).get("bf16_tflops")
+    return None
+
+
 # Algorithmic FP64 operations per particle, counted from the reference
 # formulas (each +, -, *, / is one operation; per-element constants that the
 # reference computes once per call are not counted):
@@ -483,9 +492,16 @@ def run_ours(args):
         net_ms, net_l = prof.get("learn_network", (0.0, 0))
         if net_ms > 0:
             gflop = DENOISER_GFLOP_128
+            tflops = gflop / (net_ms / net_l)
+            bf16_peak = measured_bf16_tflops()
             learned["network"] = {"gflop_per_forward": gflop, "ms_per_forward": net_ms / net_l,
-                                  "achieved_tflops": gflop / (net_ms / net_l),
-                                  "note": "CUDA-core FP32 FMA; per-launch times of the eager profile"}
+                                  "achieved_tflops": tflops,
+                                  "tensor_peak_tflops": bf16_peak / 2.0 if bf16_peak else None,
+                                  "tensor_frac": tflops / (bf16_peak / 2.0) if bf16_peak else None,
+                                  "note": "3x3 layers on the tensor cores (tcgen05 kind::tf32, FP32 accumulation "
+                                          "in TMEM), one 128 x 128 image per kick, latency-bound; peak = half the "
+                                          "measured bf16 GEMM rate (TF32 runs at half the BF16 rate); per-launch "
+                                          "times of the eager profile"}
     form_err = None
     if args.form == "fp32" and args.error_turns > 0 and not args.no_report:
         # accuracy of the reduced-precision form against the FP64 plain form

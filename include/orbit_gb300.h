@@ -368,6 +368,13 @@ int orbit_denoiser_set_params(orbit_denoiser_t* d, const float* host);
  * denoiser's own stream, a blocking stream ordered with the legacy default
  * stream). */
 int orbit_denoiser_forward(orbit_denoiser_t* d, const float* dev_in, float* dev_out, int nb, void* stream);
+/* Single-image forwards (the kick's closure) run their 3x3 layers on the
+ * tensor cores (tcgen05, TF32 operands, FP32 accumulation) unless `on` is
+ * 0; batches and training use the CUDA-core layers. */
+int orbit_denoiser_set_tensor_cores(orbit_denoiser_t* d, int on);
+/* Synchronises; *on = the setting, *err = 1 if a tensor-core layer gave up
+ * a bounded wait since the last call (then reset), else 0. */
+int orbit_denoiser_tensor_status(orbit_denoiser_t* d, int* on, int* err);
 /* One Adam step (learning rate lr) on the mean squared error of nb pairs,
  * on `stream` (NULL: the denoiser's own stream; pass the stream that wrote
  * the inputs); *loss (if not NULL) receives the loss before the step

@@ -38,6 +38,15 @@ def bf16(a):
     return v.astype(np.uint32).view(np.float32).astype(np.float64)
 
 
+def tf32(a):
+    """Round to TF32 (10 mantissa bits; to nearest, ties away from zero, as
+    cvt.rna.tf32.f32 does) through float32, as float64."""
+    a = np.asarray(a, dtype=np.float32)
+    u = a.view(np.uint32).astype(np.uint64)
+    u = ((u + 0x1000) & 0xFFFFE000).astype(np.uint32)
+    return u.view(np.float32).astype(np.float64)
+
+
 def unpack(p):
     convs, ow, ob, _ = layout()
     ws = []
@@ -85,13 +94,17 @@ def up_bwd(dy):
     return dy[:, :, 0::2, 0::2] + dy[:, :, 1::2, 0::2] + dy[:, :, 0::2, 1::2] + dy[:, :, 1::2, 1::2]
 
 
-def forward(p, x0):
-    """Network output and the activations the backward pass needs."""
+def forward(p, x0, tf32_inputs=False):
+    """Network output and the activations the backward pass needs.  With
+    tf32_inputs, the input of every 3x3 convolution is rounded to TF32 (the
+    device's tensor-core layers do so; their weights are BF16, exact in
+    TF32)."""
     ws, ow, ob = unpack(p)
     A = {"x0": np.asarray(x0, dtype=np.float64)}
 
     def c(name, src, k):
-        A[name] = np.maximum(conv3(A[src], *ws[k]), 0.0)
+        a = tf32(A[src]) if tf32_inputs else A[src]
+        A[name] = np.maximum(conv3(a, *ws[k]), 0.0)
 
     c("a1", "x0", 0); c("s1", "a1", 1); A["p1"] = pool(A["s1"])
     c("a2", "p1", 2); c("s2", "a2", 3); A["p2"] = pool(A["s2"])

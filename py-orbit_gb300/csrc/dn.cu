@@ -124,6 +124,223 @@ __global__ void __launch_bounds__(256) k_conv3(const float* __restrict__ in, int
   }
 }
 
+// ---------------------------------------------------------------------
+// Tensor-core (tcgen05) forward convolution, the inference path.
+//
+// One 3x3 layer as an implicit GEMM: D[p][o] = sum_k A[p][k] B[o][k] with p
+// a pixel, o an output channel, k = tap * cin + ci (tap = ky * 3 + kx), A
+// the zero-padded neighbourhoods of the input (im2col, built in shared
+// memory) and B the BF16 weights W[o][ci][tap], exact in TF32.  Each CTA
+// computes 128 pixels x N = cout channels (M = 128, N = 16, 32 or 64) in
+// TMEM with tcgen05.mma kind::tf32 (FP32 accumulation) over one K stage of
+// 32 (four MMAs of K = 8) staged in shared memory, the input rounded to
+// TF32 (cvt.rna) as it is staged.  Layers of more than one stage run one
+// stage per block (blockIdx.y) and write partial sums, which k_split_reduce
+// adds in order (deterministic) with the bias and the ReLU; single-stage
+// layers add those directly.
+//
+// Shared-memory operand layout (K-major, no swizzle): 8-row x 16-byte core
+// matrices; element (r, k) of a stage at (r / 8) * 1024 + (k / 4) * 128 +
+// (r % 8) * 16 + (k % 4) * 4 bytes, so the MMA over K columns 8j..8j+7
+// starts at byte 256 j with LBO = 128 (next core matrix along K) and SBO =
+// 1024 (next 8 rows).  Weights are packed into that image once per
+// parameter change (k_pack_tc) and copied to shared memory as they are.
+// ---------------------------------------------------------------------
+static const int kTcM = 128;         // pixels per CTA (MMA M)
+static const int kTcKC = 32;         // K per stage
+static const int kTcStageA = kTcM * kTcKC * 4;   // 16 KB
+static const int kTcStageB = 64 * kTcKC * 4;     // 8 KB (N <= 64)
+static const int kTcSmem = kTcStageA + kTcStageB + 1024;  // one stage + alignment slack
+static const long long kTcWaitCycles = 2000000000ll;  // ~1 s at 2 GHz: a wait that long has failed
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr) {
+  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)(128u >> 4) << 16;    // LBO: next core matrix along K
+  d |= (uint64_t)(1024u >> 4) << 32;   // SBO: next 8 rows
+  d |= (uint64_t)1 << 46;              // descriptor version of the tcgen05 family
+  return d;                            // base offset 0, no swizzle
+}
+
+// kind::tf32, D F32, A and B TF32, both K-major, M = 128, N = n.
+__host__ __device__ constexpr uint32_t tc_idesc(int n) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kTcM >> 4) << 24);
+}
+
+__device__ __forceinline__ float to_tf32(float v) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(v));
+  return __uint_as_float(r);
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Waits for phase `parity` of the barrier for at most kTcWaitCycles; false
+// (and the error flag set) when it did not complete.
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, int* err) {
+  long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity)) {
+    if (clock64() - t0 > kTcWaitCycles) {
+      atomicOr(err, 1);
+      return false;
+    }
+  }
+  return true;
+}
+
+// A stage's 32 inputs of this thread's pixel (k = 32 s .. 32 s + 31, k =
+// tap * cin + ci): base pointer and bounds test change only with the tap.
+__device__ __forceinline__ void tc_load_a(const float* __restrict__ in, int cin, int H, int W, int HW, int K,
+                                          bool pin, int py, int px, int s, float v[kTcKC]) {
+  int k = s * kTcKC;
+  int tap = k / cin, ci = k - tap * cin;
+  const float* src = nullptr;
+  bool inb = false;
+  int cur_tap = -1;
+#pragma unroll
+  for (int e = 0; e < kTcKC; ++e) {
+    if (tap != cur_tap) {
+      cur_tap = tap;
+      const int yy = py + tap / 3 - 1, xx = px + tap % 3 - 1;
+      inb = pin && tap < 9 && yy >= 0 && yy < H && xx >= 0 && xx < W;
+      src = in + (inb ? yy * W + xx : 0);
+    }
+    v[e] = (inb && k + e < K) ? __ldg(src + (size_t)ci * HW) : 0.f;
+    if (++ci == cin) {
+      ci = 0;
+      ++tap;
+    }
+  }
+}
+
+template <int N, bool SPLIT>
+__global__ void __launch_bounds__(128) k_conv3_tc(const float* __restrict__ in, int cin, int H, int W,
+                                                  const float* __restrict__ wpk, const float* __restrict__ bias,
+                                                  float* __restrict__ out, float* __restrict__ part, int* err) {
+  constexpr int BV = N * kTcKC / 4 / 128;  // float4 of the B stage per thread (1, 2 or 4)
+  extern __shared__ unsigned char tc_raw[];
+  __shared__ __align__(8) uint64_t s_bar;
+  __shared__ uint32_t s_tmem;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const uint32_t raw = smem_u32(tc_raw);
+  const uint32_t sA = (raw + 1023u) & ~1023u, sB = sA + kTcStageA;
+  unsigned char* gA = tc_raw + (sA - raw);
+  const int HW = H * W;
+  const int stage = SPLIT ? (int)blockIdx.y : 0;
+  const int p = blockIdx.x * kTcM + tid;
+  const bool pin = p < HW;
+  const int py = pin ? p / W : 0, px = pin ? p % W : 0;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" ::"r"(smem_u32(&s_tmem)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s_bar)));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  // the TMEM allocation and the barrier come before the global loads (loads
+  // issued first measured slower: 258 against 224 us per 128 x 128 forward)
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  float va[kTcKC];
+  float4 vb[BV];
+  tc_load_a(in, cin, H, W, HW, cin * 9, pin, py, px, stage, va);
+  const float4* srcB = reinterpret_cast<const float4*>(wpk + (size_t)stage * N * kTcKC);
+#pragma unroll
+  for (int i = 0; i < BV; ++i) vb[i] = __ldg(srcB + tid + 128 * i);
+  // A: row tid; B: the packed stage image, copied as it is
+  unsigned char* a_row = gA + (tid >> 3) * 1024 + (tid & 7) * 16;
+#pragma unroll
+  for (int q = 0; q < kTcKC / 4; ++q)
+    *reinterpret_cast<float4*>(a_row + q * 128) =
+        make_float4(to_tf32(va[4 * q]), to_tf32(va[4 * q + 1]), to_tf32(va[4 * q + 2]), to_tf32(va[4 * q + 3]));
+  float4* dstB = reinterpret_cast<float4*>(gA + kTcStageA);
+#pragma unroll
+  for (int i = 0; i < BV; ++i) dstB[tid + 128 * i] = vb[i];
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = s_tmem;
+  if (tid == 0) {
+#pragma unroll
+    for (int j = 0; j < kTcKC / 8; ++j) {
+      const uint64_t ad = tc_desc(sA + 256u * j), bd = tc_desc(sB + 256u * j);
+      asm volatile(
+          "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+          " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+          "l"(ad), "l"(bd), "r"(tc_idesc(N)), "r"(j > 0 ? 1u : 0u));
+    }
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     smem_u32(&s_bar))
+                 : "memory");
+  }
+  // a wait that gives up does so for the whole block
+  const bool ok = __syncthreads_and(mbar_wait_bounded(smem_u32(&s_bar), 0, err));
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  float acc[N];
+#pragma unroll
+  for (int o = 0; o < N; ++o) acc[o] = 0.f;
+  if (ok) {
+    // row tid of D: TMEM lane 32 * warp + lane, columns 0..N-1
+#pragma unroll
+    for (int c0 = 0; c0 < N; c0 += 16) {
+      uint32_t r[16];
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0));
+      asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+      for (int j = 0; j < 16; ++j) acc[c0 + j] = __uint_as_float(r[j]);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem));
+  }
+  if (!pin) return;
+  if (SPLIT) {  // part blockIdx.y of the layer's output, summed by k_split_reduce
+#pragma unroll
+    for (int o = 0; o < N; ++o) part[((size_t)blockIdx.y * N + o) * HW + p] = acc[o];
+  } else {
+#pragma unroll
+    for (int o = 0; o < N; ++o) out[(size_t)o * HW + p] = fmaxf(acc[o] + bias[o], 0.f);
+  }
+}
+
+// Packs the BF16 weights of one layer into the per-stage shared-memory
+// image of k_conv3_tc: row o, K column k = tap * cin + ci (weight
+// W[o][ci][tap]) of stage s = k / 32 at float index s * N * 32 + (o / 8) *
+// 256 + (kk / 4) * 32 + (o % 8) * 4 + kk % 4 (kk = k % 32); zero for
+// k >= 9 cin.
+__global__ void k_pack_tc(const __nv_bfloat16* __restrict__ w, int cin, int n, int nst, float* __restrict__ out) {
+  const int total = nst * n * kTcKC;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    const int s = i / (n * kTcKC), r = i % (n * kTcKC);
+    const int o = r / kTcKC, kk = r % kTcKC;
+    const int k = s * kTcKC + kk;
+    float v = 0.f;
+    if (k < 9 * cin) {
+      const int tap = k / cin, ci = k % cin;
+      v = __bfloat162float(w[((size_t)o * cin + ci) * 9 + tap]);
+    }
+    out[(size_t)s * n * kTcKC + (o >> 3) * 256 + (kk >> 2) * 32 + (o & 7) * 4 + (kk & 3)] = v;
+  }
+}
+
 // out = max(b + sum of the split convolution's parts (in order), 0).
 __global__ void k_split_reduce(const float* __restrict__ part, int splits, const float* __restrict__ b,
                                float* __restrict__ out, int C, int HW, size_t n) {
@@ -494,6 +711,13 @@ struct orbit_denoiser {
   float* d_loss = nullptr;
   float* d_scratch = nullptr;  // data gradient of the widest convolution input
   cudaStream_t stream = nullptr;
+  // tensor-core inference path (single images): packed weights per layer,
+  // repacked after any parameter change; error flag of its bounded waits
+  bool tc = true;
+  bool tc_stale = true;
+  float* d_wtc = nullptr;
+  std::vector<size_t> tc_off;
+  int* d_err = nullptr;
 };
 
 namespace orbit {
@@ -539,7 +763,7 @@ static void split_plan(const Conv& cv, int h, int w, int nb, int* splits, int* c
   *splits = (cv.cin + *ci_per - 1) / *ci_per;
 }
 
-static int conv_fwd(orbit_denoiser_t* d, const Step3& s, int nb, cudaStream_t st) {
+static int conv_fwd_cc(orbit_denoiser_t* d, const Step3& s, int nb, cudaStream_t st) {
   const Conv& cv = d->conv[s.ci];
   int c, h, w;
   act_shape(d, s.out, &c, &h, &w);
@@ -560,7 +784,78 @@ static int conv_fwd(orbit_denoiser_t* d, const Step3& s, int nb, cudaStream_t st
   return ORBIT_OK;
 }
 
-static int forward(orbit_denoiser_t* d, int nb, cudaStream_t st) {
+// Tensor-core plan of one layer: 128-pixel tiles, the K stages split over
+// blocks so that the layer fills about one block per SM.
+// One K stage per block (one MMA group of 32), parts summed in order by
+// k_split_reduce: a single image's layers are short chains of latency, and
+// running them side by side beats longer chains per block.  Measured per
+// 128 x 128 forward on GB300: 224 us, against 242 us with a few splits per
+// pixel tile summed by the tile's last block and 297 us on the CUDA-core
+// layers.
+static void tc_plan(const Conv& cv, int h, int w, int* tiles, int* nst) {
+  *tiles = (h * w + kTcM - 1) / kTcM;
+  *nst = (cv.cin * 9 + kTcKC - 1) / kTcKC;
+}
+
+static int tc_pack(orbit_denoiser_t* d, cudaStream_t st) {
+  for (size_t l = 0; l < d->conv.size(); ++l) {
+    const Conv& cv = d->conv[l];
+    const int nst = (cv.cin * 9 + kTcKC - 1) / kTcKC;
+    k_pack_tc<<<grid_1d((size_t)nst * cv.cout * kTcKC), 256, 0, st>>>(d->d_pb + cv.w_off, cv.cin, cv.cout, nst,
+                                                                      d->d_wtc + d->tc_off[l]);
+  }
+  ORBIT_LAUNCH_CHECK("denoiser tensor-core weight packing");
+  d->tc_stale = false;
+  return ORBIT_OK;
+}
+
+template <int N>
+static void launch_conv_tc(dim3 g, cudaStream_t st, bool split, const float* in, int cin, int h, int w,
+                           const float* wp, const float* bias, float* out, float* part, int nst, int* err) {
+  if (split)
+    k_conv3_tc<N, true><<<g, 128, kTcSmem, st>>>(in, cin, h, w, wp, bias, out, part, err);
+  else
+    k_conv3_tc<N, false><<<g, 128, kTcSmem, st>>>(in, cin, h, w, wp, bias, out, part, err);
+}
+
+static int conv_fwd_tc(orbit_denoiser_t* d, const Step3& s, cudaStream_t st) {
+  const Conv& cv = d->conv[s.ci];
+  int c, h, w, tiles, nst;
+  act_shape(d, s.out, &c, &h, &w);
+  tc_plan(cv, h, w, &tiles, &nst);
+  const float* wp = d->d_wtc + d->tc_off[s.ci];
+  const float* B = d->d_p + cv.b_off;
+  const bool split = nst > 1;
+  dim3 g(tiles, nst);
+  float* o = d->act[s.out];
+  float* part = d->d_scratch;
+  switch (cv.cout) {
+    case 16: launch_conv_tc<16>(g, st, split, d->act[s.in], cv.cin, h, w, wp, B, o, part, nst, d->d_err); break;
+    case 32: launch_conv_tc<32>(g, st, split, d->act[s.in], cv.cin, h, w, wp, B, o, part, nst, d->d_err); break;
+    case 64: launch_conv_tc<64>(g, st, split, d->act[s.in], cv.cin, h, w, wp, B, o, part, nst, d->d_err); break;
+    default: return set_error(ORBIT_ERR_ARG, "denoiser: tensor-core layer width not supported");
+  }
+  ORBIT_LAUNCH_CHECK("denoiser tensor-core conv");
+  if (split) {
+    const size_t n_out = (size_t)cv.cout * h * w;
+    k_split_reduce<<<grid_1d(n_out), 256, 0, st>>>(part, nst, B, o, cv.cout, h * w, n_out);
+    ORBIT_LAUNCH_CHECK("denoiser split reduce");
+  }
+  return ORBIT_OK;
+}
+
+// infer: a single image goes through the tensor-core layers (when on);
+// training keeps the CUDA-core layers, whose activations the backward
+// pass reads and whose gradients are checked against the oracle.
+static int forward(orbit_denoiser_t* d, int nb, cudaStream_t st, bool infer = false) {
+  const bool tc = infer && d->tc && nb == 1;
+  if (tc && d->tc_stale) {
+    int rc = tc_pack(d, st);
+    if (rc) return rc;
+  }
+  auto conv_fwd = [&](orbit_denoiser_t* dd, const Step3& stp, int n, cudaStream_t ss) -> int {
+    return tc ? conv_fwd_tc(dd, stp, ss) : conv_fwd_cc(dd, stp, n, ss);
+  };
   auto pool = [&](int a, int b) -> int {
     int c, h, w;
     act_shape(d, a, &c, &h, &w);
@@ -851,7 +1146,28 @@ int orbit_denoiser_create(orbit_denoiser_t** out, int max_batch, int h, int w, u
       split_plan(d->conv[stp.ci], hh, ww, nb, &sp, &cp);
       if (sp > 1) scratch = std::max(scratch, (size_t)sp * act_size(d, stp.out, nb));
     }
+  size_t wtc = 0;
+  for (size_t l = 0; l < d->conv.size(); ++l) {
+    const Conv& cv = d->conv[l];
+    d->tc_off.push_back(wtc);
+    wtc += (size_t)((cv.cin * 9 + kTcKC - 1) / kTcKC) * cv.cout * kTcKC;
+  }
+  for (const Step3& stp : kSteps) {
+    int c, hh, ww, tiles, nst;
+    act_shape(d, stp.out, &c, &hh, &ww);
+    tc_plan(d->conv[stp.ci], hh, ww, &tiles, &nst);
+    if (nst > 1) scratch = std::max(scratch, (size_t)nst * d->conv[stp.ci].cout * hh * ww);
+  }
   e = cudaMalloc(&d->d_scratch, sizeof(float) * scratch);
+  if (e == cudaSuccess) e = cudaMalloc(&d->d_wtc, sizeof(float) * wtc);
+  if (e == cudaSuccess) e = cudaMalloc(&d->d_err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(d->d_err, 0, sizeof(int));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_conv3_tc<16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_conv3_tc<16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_conv3_tc<32, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_conv3_tc<32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_conv3_tc<64, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_conv3_tc<64, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
   if (e != cudaSuccess) return fail(cuda_error(e, "orbit_denoiser_create"));
   k_to_bf16<<<grid_1d(off), 256, 0, d->stream>>>(d->d_p, d->d_pb, d->d_isw, off);
   e = cudaStreamSynchronize(d->stream);
@@ -865,7 +1181,7 @@ int orbit_denoiser_destroy(orbit_denoiser_t* d) {
   if (d->stream) cudaStreamSynchronize(d->stream);
   for (float* p : d->act) if (p) cudaFree(p);
   for (float* p : d->grad) if (p) cudaFree(p);
-  void* bufs[] = {d->d_p, d->d_pb, d->d_g, d->d_m, d->d_v, d->d_isw, d->d_loss, d->d_scratch};
+  void* bufs[] = {d->d_p, d->d_pb, d->d_g, d->d_m, d->d_v, d->d_isw, d->d_loss, d->d_scratch, d->d_wtc, d->d_err};
   for (void* b : bufs) if (b) cudaFree(b);
   if (d->stream) cudaStreamDestroy(d->stream);
   delete d;
@@ -897,6 +1213,7 @@ int orbit_denoiser_set_params(orbit_denoiser_t* d, const float* host) {
   d->step = 0;
   k_to_bf16<<<grid_1d(d->nparam), 256, 0, d->stream>>>(d->d_p, d->d_pb, d->d_isw, d->nparam);
   ORBIT_LAUNCH_CHECK("orbit_denoiser_set_params");
+  d->tc_stale = true;
   ORBIT_CUDA(cudaStreamSynchronize(d->stream));
   return ORBIT_OK;
 }
@@ -908,9 +1225,27 @@ int orbit_denoiser_forward(orbit_denoiser_t* d, const float* dev_in, float* dev_
   cudaStream_t st = stream_of(d, stream);
   const size_t n = (size_t)nb * d->H * d->W;
   ORBIT_CUDA(cudaMemcpyAsync(d->act[X0], dev_in, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
-  rc = forward(d, nb, st);
+  rc = forward(d, nb, st, true);
   if (rc) return rc;
   ORBIT_CUDA(cudaMemcpyAsync(dev_out, d->act[Y], sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
+  return ORBIT_OK;
+}
+
+int orbit_denoiser_set_tensor_cores(orbit_denoiser_t* d, int on) {
+  if (!d) return set_error(ORBIT_ERR_ARG, "orbit_denoiser_set_tensor_cores: bad argument");
+  d->tc = on != 0;
+  return ORBIT_OK;
+}
+
+int orbit_denoiser_tensor_status(orbit_denoiser_t* d, int* on, int* err) {
+  if (!d) return set_error(ORBIT_ERR_ARG, "orbit_denoiser_tensor_status: bad argument");
+  ORBIT_CUDA(cudaStreamSynchronize(d->stream));
+  ORBIT_CUDA(cudaDeviceSynchronize());
+  if (on) *on = d->tc ? 1 : 0;
+  if (err) {
+    ORBIT_CUDA(cudaMemcpy(err, d->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    ORBIT_CUDA(cudaMemset(d->d_err, 0, sizeof(int)));
+  }
   return ORBIT_OK;
 }
 
@@ -931,6 +1266,7 @@ int orbit_denoiser_train_step(orbit_denoiser_t* d, const float* dev_in, const fl
   k_adam<<<grid_1d(d->nparam), 256, 0, st>>>(d->d_p, d->d_g, d->d_m, d->d_v, d->d_pb, d->d_isw, d->nparam, lr, b1,
                                               b2, eps, c1, c2);
   ORBIT_LAUNCH_CHECK("denoiser adam");
+  d->tc_stale = true;
   if (loss) {
     ORBIT_CUDA(cudaMemcpyAsync(loss, d->d_loss, sizeof(float), cudaMemcpyDeviceToHost, st));
     ORBIT_CUDA(cudaStreamSynchronize(st));

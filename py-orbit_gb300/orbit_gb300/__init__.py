@@ -322,6 +322,26 @@ class DeviceDenoiser:
         call("orbit_denoiser_forward", self.h, ctypes.c_void_p(dev_in), ctypes.c_void_p(dev_out), int(nb),
              ctypes.c_void_p(stream) if stream else None)
 
+    @property
+    def tensor_cores(self) -> bool:
+        """Single-image forwards run their 3x3 layers on the tensor cores
+        (tcgen05, TF32 operands, FP32 accumulation); batches and training
+        use the CUDA-core layers."""
+        on = ctypes.c_int()
+        call("orbit_denoiser_tensor_status", self.h, ctypes.byref(on), None)
+        return bool(on.value)
+
+    @tensor_cores.setter
+    def tensor_cores(self, on: bool):
+        call("orbit_denoiser_set_tensor_cores", self.h, int(bool(on)))
+
+    def tensor_errors(self) -> int:
+        """1 if a tensor-core layer gave up a bounded wait since the last
+        call (the flag is then cleared), else 0."""
+        err = ctypes.c_int()
+        call("orbit_denoiser_tensor_status", self.h, None, ctypes.byref(err))
+        return err.value
+
     def train_step(self, dev_in: int, dev_target: int, nb: int, lr: float, want_loss: bool = True, stream: int = 0):
         loss = ctypes.c_float()
         call("orbit_denoiser_train_step", self.h, ctypes.c_void_p(dev_in), ctypes.c_void_p(dev_target), int(nb),
