@@ -346,8 +346,61 @@ __global__ void k_split_reduce(const float* __restrict__ part, int splits, const
                                float* __restrict__ out, int C, int HW, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     float v = b[(i / HW) % C];
-    for (int q = 0; q < splits; ++q) v += part[(size_t)q * n + i];
+    // eight parts' loads in flight at a time; the additions keep the order
+    // q = 0, 1, ... (the same sums)
+    int q = 0;
+    for (; q + 8 <= splits; q += 8) {
+      float t[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) t[u] = __ldg(part + (size_t)(q + u) * n + i);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v += t[u];
+    }
+    for (; q < splits; ++q) v += __ldg(part + (size_t)q * n + i);
     out[i] = fmaxf(v, 0.f);
+  }
+}
+
+// The sum of k_split_reduce for a layer whose output also feeds a 2x2
+// average pooling and the skip half of a concatenation, or a 2x upsample
+// into the first half of one: those copies are written here instead of by
+// k_pool and k_upcat, with the same arithmetic (the same values).  One
+// thread per 2x2 quad of one channel; cat / pool / up may be null.
+__global__ void k_split_reduce_quad(const float* __restrict__ part, int splits, const float* __restrict__ b,
+                                    float* __restrict__ out, int C, int H, int W, float* __restrict__ pool,
+                                    float* __restrict__ cat, int cat_off, float* __restrict__ up) {
+  const int h2 = H / 2, w2 = W / 2;
+  const size_t n = (size_t)C * H * W;
+  const size_t tot = (size_t)C * h2 * w2;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < tot; i += (size_t)gridDim.x * blockDim.x) {
+    const int x2 = (int)(i % w2), y2 = (int)((i / w2) % h2), c = (int)(i / ((size_t)w2 * h2));
+    float v[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int y = 2 * y2 + (k >> 1), x = 2 * x2 + (k & 1);
+      const size_t e = ((size_t)c * H + y) * W + x;
+      float sum = b[c];
+      int q = 0;
+      for (; q + 8 <= splits; q += 8) {
+        float t[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) t[u] = __ldg(part + (size_t)(q + u) * n + e);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) sum += t[u];
+      }
+      for (; q < splits; ++q) sum += __ldg(part + (size_t)q * n + e);
+      v[k] = fmaxf(sum, 0.f);
+      out[e] = v[k];
+      if (cat) cat[((size_t)(cat_off + c) * H + y) * W + x] = v[k];
+      if (up) {
+        float* u0 = up + ((size_t)c * 2 * H + 2 * y) * 2 * W + 2 * x;
+        u0[0] = v[k];
+        u0[1] = v[k];
+        u0[2 * W] = v[k];
+        u0[2 * W + 1] = v[k];
+      }
+    }
+    if (pool) pool[((size_t)c * h2 + y2) * w2 + x2] = 0.25f * (v[0] + v[1] + v[2] + v[3]);
   }
 }
 
@@ -818,7 +871,15 @@ static void launch_conv_tc(dim3 g, cudaStream_t st, bool split, const float* in,
     k_conv3_tc<N, false><<<g, 128, kTcSmem, st>>>(in, cin, h, w, wp, bias, out, part, err);
 }
 
-static int conv_fwd_tc(orbit_denoiser_t* d, const Step3& s, cudaStream_t st) {
+// What a tensor-core layer's reduction also writes (see k_split_reduce_quad).
+struct TcEpi {
+  int pool = -1;     // activation receiving the 2x2 average
+  int cat = -1;      // concatenation receiving a copy at channel cat_off
+  int cat_off = 0;
+  int up = -1;       // concatenation receiving the 2x upsample (channels 0..C-1)
+};
+
+static int conv_fwd_tc(orbit_denoiser_t* d, const Step3& s, cudaStream_t st, const TcEpi& ep = TcEpi()) {
   const Conv& cv = d->conv[s.ci];
   int c, h, w, tiles, nst;
   act_shape(d, s.out, &c, &h, &w);
@@ -836,11 +897,34 @@ static int conv_fwd_tc(orbit_denoiser_t* d, const Step3& s, cudaStream_t st) {
     default: return set_error(ORBIT_ERR_ARG, "denoiser: tensor-core layer width not supported");
   }
   ORBIT_LAUNCH_CHECK("denoiser tensor-core conv");
+  const bool epi = ep.pool >= 0 || ep.cat >= 0 || ep.up >= 0;
+  const size_t n_out = (size_t)cv.cout * h * w;
+  if (split && epi) {
+    k_split_reduce_quad<<<grid_1d(n_out / 4), 256, 0, st>>>(
+        part, nst, B, o, cv.cout, h, w, ep.pool >= 0 ? d->act[ep.pool] : nullptr, ep.cat >= 0 ? d->act[ep.cat] : nullptr,
+        ep.cat_off, ep.up >= 0 ? d->act[ep.up] : nullptr);
+    ORBIT_LAUNCH_CHECK("denoiser split reduce");
+    return ORBIT_OK;
+  }
   if (split) {
-    const size_t n_out = (size_t)cv.cout * h * w;
     k_split_reduce<<<grid_1d(n_out), 256, 0, st>>>(part, nst, B, o, cv.cout, h * w, n_out);
     ORBIT_LAUNCH_CHECK("denoiser split reduce");
   }
+  if (!epi) return ORBIT_OK;
+  // an unsplit layer with consumers: the separate kernels
+  if (ep.pool >= 0) k_pool<<<grid_1d(n_out / 4), 256, 0, st>>>(o, d->act[ep.pool], cv.cout, h, w);
+  if (ep.cat >= 0) {
+    int cc, hh, ww;
+    act_shape(d, ep.cat, &cc, &hh, &ww);
+    ORBIT_CUDA(cudaMemcpyAsync(d->act[ep.cat] + (size_t)ep.cat_off * h * w, o, sizeof(float) * n_out,
+                               cudaMemcpyDeviceToDevice, st));
+  }
+  if (ep.up >= 0) {
+    int cc, hh, ww;
+    act_shape(d, ep.up, &cc, &hh, &ww);
+    k_upcat<<<grid_1d((size_t)cv.cout * hh * ww), 256, 0, st>>>(o, cv.cout, nullptr, 0, d->act[ep.up], 1, hh, ww);
+  }
+  ORBIT_LAUNCH_CHECK("denoiser epilogue");
   return ORBIT_OK;
 }
 
@@ -854,7 +938,7 @@ static int forward(orbit_denoiser_t* d, int nb, cudaStream_t st, bool infer = fa
     if (rc) return rc;
   }
   auto conv_fwd = [&](orbit_denoiser_t* dd, const Step3& stp, int n, cudaStream_t ss) -> int {
-    return tc ? conv_fwd_tc(dd, stp, ss) : conv_fwd_cc(dd, stp, n, ss);
+    return conv_fwd_cc(dd, stp, n, ss);
   };
   auto pool = [&](int a, int b) -> int {
     int c, h, w;
@@ -872,26 +956,40 @@ static int forward(orbit_denoiser_t* d, int nb, cudaStream_t st, bool infer = fa
     return ORBIT_OK;
   };
   int rc = 0;
-  rc = rc ? rc : conv_fwd(d, kSteps[0], nb, st);
-  rc = rc ? rc : conv_fwd(d, kSteps[1], nb, st);
-  rc = rc ? rc : pool(S1, P1);
-  rc = rc ? rc : conv_fwd(d, kSteps[2], nb, st);
-  rc = rc ? rc : conv_fwd(d, kSteps[3], nb, st);
-  rc = rc ? rc : pool(S2, P2);
-  rc = rc ? rc : conv_fwd(d, kSteps[4], nb, st);
-  rc = rc ? rc : conv_fwd(d, kSteps[5], nb, st);
-  rc = rc ? rc : pool(S3, P3);
-  rc = rc ? rc : conv_fwd(d, kSteps[6], nb, st);
-  rc = rc ? rc : conv_fwd(d, kSteps[7], nb, st);
-  rc = rc ? rc : upcat(B4, S3, C3);
-  rc = rc ? rc : conv_fwd(d, kSteps[8], nb, st);
-  rc = rc ? rc : conv_fwd(d, kSteps[9], nb, st);
-  rc = rc ? rc : upcat(D3, S2, C2);
-  rc = rc ? rc : conv_fwd(d, kSteps[10], nb, st);
-  rc = rc ? rc : conv_fwd(d, kSteps[11], nb, st);
-  rc = rc ? rc : upcat(D2, S1, C1);
-  rc = rc ? rc : conv_fwd(d, kSteps[12], nb, st);
-  rc = rc ? rc : conv_fwd(d, kSteps[13], nb, st);
+  if (tc) {
+    // the layers' reductions also write the poolings and concatenations
+    TcEpi e1, e3, e5, e7, e9, e11;
+    e1.pool = P1; e1.cat = C1; e1.cat_off = 32;  // c1 = [up(d2) 32, s1 16]
+    e3.pool = P2; e3.cat = C2; e3.cat_off = 64;  // c2 = [up(d3) 64, s2 32]
+    e5.pool = P3; e5.cat = C3; e5.cat_off = 64;  // c3 = [up(b4) 64, s3 64]
+    e7.up = C3;
+    e9.up = C2;
+    e11.up = C1;
+    const TcEpi none;
+    const TcEpi* eps[14] = {&none, &e1, &none, &e3, &none, &e5, &none, &e7, &none, &e9, &none, &e11, &none, &none};
+    for (int k = 0; k < 14 && !rc; ++k) rc = conv_fwd_tc(d, kSteps[k], st, *eps[k]);
+  } else {
+    rc = rc ? rc : conv_fwd(d, kSteps[0], nb, st);
+    rc = rc ? rc : conv_fwd(d, kSteps[1], nb, st);
+    rc = rc ? rc : pool(S1, P1);
+    rc = rc ? rc : conv_fwd(d, kSteps[2], nb, st);
+    rc = rc ? rc : conv_fwd(d, kSteps[3], nb, st);
+    rc = rc ? rc : pool(S2, P2);
+    rc = rc ? rc : conv_fwd(d, kSteps[4], nb, st);
+    rc = rc ? rc : conv_fwd(d, kSteps[5], nb, st);
+    rc = rc ? rc : pool(S3, P3);
+    rc = rc ? rc : conv_fwd(d, kSteps[6], nb, st);
+    rc = rc ? rc : conv_fwd(d, kSteps[7], nb, st);
+    rc = rc ? rc : upcat(B4, S3, C3);
+    rc = rc ? rc : conv_fwd(d, kSteps[8], nb, st);
+    rc = rc ? rc : conv_fwd(d, kSteps[9], nb, st);
+    rc = rc ? rc : upcat(D3, S2, C2);
+    rc = rc ? rc : conv_fwd(d, kSteps[10], nb, st);
+    rc = rc ? rc : conv_fwd(d, kSteps[11], nb, st);
+    rc = rc ? rc : upcat(D2, S1, C1);
+    rc = rc ? rc : conv_fwd(d, kSteps[12], nb, st);
+    rc = rc ? rc : conv_fwd(d, kSteps[13], nb, st);
+  }
   if (rc) return rc;
   const size_t hw = (size_t)d->H * d->W;
   k_out<<<grid_1d(nb * hw), 256, 0, st>>>(d->act[D1], 16, d->d_p + d->out_w, d->d_p + d->out_b, d->act[X0],
