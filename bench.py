@@ -49,8 +49,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--form", default="plain", choices=["plain", "fp32", "learned"],
-                    help="learned: the plain form with the trained denoiser closure, 1e5 particles by default")
+    ap.add_argument("--form", default="plain", choices=["plain", "fp32", "learned", "learned-fp32"],
+                    help="learned: the plain form with the trained denoiser closure, 1e5 particles by default; "
+                         "learned-fp32: the same closure on the FP32 field form")
     ap.add_argument("--n", type=int, default=None)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -219,8 +220,8 @@ def build_workload(n, form, seed):
     from spacecharge import SpaceChargeCalc2p5D
     soa = wl_coords(n, seed)
     bunch = W.make_bunch(soa, WL["intensity"] / n)
-    calc = SpaceChargeCalc2p5D(*GRID, form="plain" if form == "learned" else form)
-    if form == "learned":
+    calc = SpaceChargeCalc2p5D(*GRID, form={"learned": "plain", "learned-fp32": "fp32"}.get(form, form))
+    if form in ("learned", "learned-fp32"):
         from orbit_gb300.denoiser import default_network
         calc.setDenoiser(default_network(), 10, 1e-3)
     lat = wl_lattice(calc)
@@ -234,7 +235,7 @@ DENOISER_GFLOP_128 = 2 * sum(h * h * 9 * ci * co for h, ci, co in (
     (32, 128, 64), (32, 64, 64), (64, 96, 32), (64, 32, 32), (128, 48, 16), (128, 16, 16))) * 1e-9 + 2 * 128 * 128 * 16e-9
 
 
-def learned_report(calc, ms_per_turn, n, n_equal=10_000_000, turns=10):
+def learned_report(calc, ms_per_turn, n, n_equal=10_000_000, turns=10, form="plain"):
     """The learned form against the plain form at two particle counts: equal
     density noise (1e7, the network's training targets) and equal force
     noise (n times the network's measured gain in force error on 96 held-out
@@ -258,7 +259,7 @@ def learned_report(calc, ms_per_turn, n, n_equal=10_000_000, turns=10):
 
     def setup(npart, with_net):
         b = W.make_bunch(W.c2_coords(npart, seed=77), W.C2_MACROSIZE * (N_PARTICLES / npart))
-        c = SpaceChargeCalc2p5D(*GRID)
+        c = SpaceChargeCalc2p5D(*GRID, form=form if with_net else "plain")
         if with_net:
             c.setDenoiser(default_network(), 10, 1e-3)
         with quiet():
@@ -375,7 +376,7 @@ def run_ours(args):
         dist = tdist
     os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("CUDA_VISIBLE_DEVICES", ""))
     torch.cuda.init()
-    n = args.n if args.n else (100_000 if args.form == "learned" else WL["n"])
+    n = args.n if args.n else (100_000 if args.form.startswith("learned") else WL["n"])
     TRAFFIC.n = n
     soa, bunch, calc, lat = build_workload(n, args.form, seed=1000 + rank)
     prog = lat.fusedProgram(bunch)
@@ -486,9 +487,10 @@ def run_ours(args):
     kicks_done, green_done = calc._calc.counters()
     green_rate = green_done / kicks_done if kicks_done else None
     learned = None
-    if args.form == "learned":
-        learned = {} if args.no_report else learned_report(calc, ms_per_turn=total_ms / args.steps, n=n)
-        # the network's arithmetic rate (FP32 CUDA-core FMAs on BF16 weights)
+    if args.form.startswith("learned"):
+        learned = {} if args.no_report else learned_report(calc, ms_per_turn=total_ms / args.steps, n=n,
+                                                             form="fp32" if args.form == "learned-fp32" else "plain")
+        # the network's arithmetic rate (TF32 tensor-core MMAs on BF16 weights)
         net_ms, net_l = prof.get("learn_network", (0.0, 0))
         if net_ms > 0:
             gflop = DENOISER_GFLOP_128
@@ -527,7 +529,9 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None,
         "dtype": {"plain": "f64", "fp32": "f32-field/f64-coords",
-                  "learned": "f64 + bf16-weight/f32 network"}[args.form],
+                  "learned": "f64 + bf16-weight network (tf32 tensor-core MMA, f32 accumulation)",
+                  "learned-fp32": "f32-field/f64-coords + bf16-weight network (tf32 tensor-core MMA, f32 accumulation)"
+                  }[args.form],
         "data": "synthetic (seeded 4D waterbag rms 4 mm/0.8 mrad, z~N(0,10 m), dE~N(0,1 MeV))",
         "config": {"workload": "%s, %d particles, grid %dx%dx%d, one turn per step" % (WL["desc"], n, *GRID),
                    "form": args.form, "particles": n, "grid": list(GRID),

@@ -385,8 +385,9 @@ int orbit_denoiser_train_step(orbit_denoiser_t* d, const float* dev_in, const fl
  * NULL, the network output for nb pairs, without an update (waits). */
 int orbit_denoiser_gradients(orbit_denoiser_t* d, const float* dev_in, const float* dev_target, int nb, float* grads,
                              float* loss, float* dev_out, void* stream);
-/* The learned closure of a plain 2.5D calculator (nx x ny = the network's
- * image size; bunches with a uniform macrosize): each kick the network
+/* The learned closure of a 2.5D calculator, plain or FP32 form (nx x ny =
+ * the network's image size; bunches with a uniform macrosize; not the
+ * 2.5Drb calculator, not with a boundary): each kick the network
  * denoises the deposit (clamped at zero, rescaled to the deposit's total
  * charge) before the FFT solve; every check_every-th kick the raw deposit is
  * solved as well and, if the relative rms difference of the two potentials

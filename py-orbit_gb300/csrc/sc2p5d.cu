@@ -776,6 +776,18 @@ __global__ void k_learn_in(ScState* st, const unsigned long long* __restrict__ r
   }
 }
 
+// FP32 form: the deposit is a float grid of charges.
+__global__ void k_learn_in_f(ScState* st, const float* __restrict__ rho_f, float* __restrict__ img,
+                             double* __restrict__ raw, int n, double scale) {
+  if (st->skip) return;
+  if (blockIdx.x == 0 && threadIdx.x == 0) st->dn_sum = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double v = (double)rho_f[i];
+    if (raw) raw[i] = v;
+    img[i] = (float)(v * scale);
+  }
+}
+
 // Sum of the network output clamped at zero (a density is not negative).
 __global__ void k_learn_sum(ScState* st, const float* __restrict__ out, int n) {
   if (st->skip) return;
@@ -803,6 +815,17 @@ __global__ void k_learn_out(ScState* st, const float* __restrict__ out, unsigned
   const double back = ((double)n / sum) / (scale * st->inv_qscale);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     rho_q[i] = (unsigned long long)llrint((double)fmaxf(out[i], 0.f) * back);
+}
+
+// FP32 form: the rescaled output written back as the float deposit.
+__global__ void k_learn_out_f(ScState* st, const float* __restrict__ out, float* __restrict__ rho_f, int n,
+                              double scale) {
+  if (st->skip || st->dn_fallback) return;
+  const double sum = st->dn_sum;
+  if (!(sum > 0.0)) return;
+  const double back = ((double)n / sum) / scale;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    rho_f[i] = (float)((double)fmaxf(out[i], 0.f) * back);
 }
 
 // State of the check solve: the kick's skip flag and log-scale term.
@@ -1322,6 +1345,23 @@ static int add_green_branch(orbit_sc2p5d_t* c, cudaStream_t s, cudaGraphConditio
   return ORBIT_OK;
 }
 
+// The learned closure's check: the raw deposit (FP64 copy) solved into its
+// own buffers with the calculator's Green spectrum, in its precision.
+template <typename T>
+static void enqueue_check_solve(orbit_sc2p5d_t* c, cudaStream_t s) {
+  typedef typename CT<T>::t C;
+  const int thx = fft_threads(c->plan_x), thy = fft_threads(c->plan_y);
+  const size_t smx = fft_smem<T>(c->nx2), smy = fft_smem<T>(c->ny2);
+  k_rows_fwd<T, 3><<<(c->nx + 1) / 2, thy, smy, s>>>(c->d_dn_st, c->d_dn_raw, nullptr, (C*)c->d_dn_hat,
+                                                       (const C*)c->d_tw_y, c->plan_y, c->nx, c->ny, c->H, 1,
+                                                       nullptr, 0, nullptr, nullptr);
+  k_cols<T, 1><<<c->H, thx, smx, s>>>(c->d_dn_st, (C*)c->d_dn_hat, (C*)c->d_green, (const C*)c->d_tw_x, c->plan_x,
+                                        c->nx, c->H, c->ny2, 1);
+  k_rows_inv<T><<<(c->nx + 1) / 2, thy, smy, s>>>(c->d_dn_st, (const C*)c->d_dn_hat, (const C*)c->d_tw_y,
+                                                    c->plan_y, c->nx, c->ny, c->H, 1.0 / (c->nx2 * c->ny2),
+                                                    c->d_dn_phi, nullptr);
+}
+
 int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStream_t s, bool do_extrema,
                     bool do_kick, int* launches, double pipe_radius, const orbit_boundary* bnd) {
   int nl = 0;
@@ -1399,7 +1439,7 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
   // learned closure: the network denoises the deposit before the solve
   bool dn_check = false;
   double dn_scale = 0.0;
-  if (c->dn && plain && !c->rb && !bnd) {
+  if (c->dn && !c->rb && !bnd) {
     if (b->has_msize)
       return set_error(ORBIT_ERR_UNSUPPORTED, "the learned closure needs a uniform macrosize");
     const double M = (double)n * b->sync.macrosize;
@@ -1410,8 +1450,12 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
       int gb = (ng + 255) / 256;
       if (gb > num_sms() * 2) gb = num_sms() * 2;
       ORBIT_PB("learn_in", s);
-      k_learn_in<<<gb, 256, 0, s>>>(c->d_st, c->d_rho_q, c->d_dn_img, dn_check ? c->d_dn_raw : nullptr, ng,
-                                    dn_scale);
+      if (plain)
+        k_learn_in<<<gb, 256, 0, s>>>(c->d_st, c->d_rho_q, c->d_dn_img, dn_check ? c->d_dn_raw : nullptr, ng,
+                                      dn_scale);
+      else
+        k_learn_in_f<<<gb, 256, 0, s>>>(c->d_st, c->d_rho_f, c->d_dn_img, dn_check ? c->d_dn_raw : nullptr, ng,
+                                        dn_scale);
       ORBIT_PE(s);
       ORBIT_PB("learn_network", s);
       rc = orbit_denoiser_forward(c->dn, c->d_dn_img, c->d_dn_out, 1, (void*)s);
@@ -1419,7 +1463,10 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
       if (rc) return rc;
       ORBIT_PB("learn_out", s);
       k_learn_sum<<<gb, 256, 0, s>>>(c->d_st, c->d_dn_out, ng);
-      k_learn_out<<<gb, 256, 0, s>>>(c->d_st, c->d_dn_out, c->d_rho_q, ng, dn_scale);
+      if (plain)
+        k_learn_out<<<gb, 256, 0, s>>>(c->d_st, c->d_dn_out, c->d_rho_q, ng, dn_scale);
+      else
+        k_learn_out_f<<<gb, 256, 0, s>>>(c->d_st, c->d_dn_out, c->d_rho_f, ng, dn_scale);
       ORBIT_PE(s);
       nl += 3;
       ORBIT_LAUNCH_CHECK("sc2p5d learned closure");
@@ -1446,20 +1493,14 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
   rc = plain ? enqueue_conv<double>(c, s, &nl) : enqueue_conv<float>(c, s, &nl);
   if (rc) return rc;
   if (dn_check) {
-    // the raw deposit solved beside the denoised one, and the judge
-    typedef double2 C;
-    int thx = fft_threads(c->plan_x), thy = fft_threads(c->plan_y);
-    size_t smx = fft_smem<double>(c->nx2), smy = fft_smem<double>(c->ny2);
+    // the raw deposit solved beside the denoised one (in the calculator's
+    // own precision: its Green spectrum and twiddles), and the judge
     ORBIT_PB("learn_check", s);
     k_learn_chk_prep<<<1, 1, 0, s>>>(c->d_st, c->d_dn_st);
-    k_rows_fwd<double, 3><<<(c->nx + 1) / 2, thy, smy, s>>>(c->d_dn_st, c->d_dn_raw, nullptr, (C*)c->d_dn_hat,
-                                                            (const C*)c->d_tw_y, c->plan_y, c->nx, c->ny, c->H, 1,
-                                                            nullptr, 0, nullptr, nullptr);
-    k_cols<double, 1><<<c->H, thx, smx, s>>>(c->d_dn_st, (C*)c->d_dn_hat, (C*)c->d_green, (const C*)c->d_tw_x,
-                                             c->plan_x, c->nx, c->H, c->ny2, 1);
-    k_rows_inv<double><<<(c->nx + 1) / 2, thy, smy, s>>>(c->d_dn_st, (const C*)c->d_dn_hat, (const C*)c->d_tw_y,
-                                                         c->plan_y, c->nx, c->ny, c->H, 1.0 / (c->nx2 * c->ny2),
-                                                         c->d_dn_phi, nullptr);
+    if (plain)
+      enqueue_check_solve<double>(c, s);
+    else
+      enqueue_check_solve<float>(c, s);
     k_learn_compare<<<1, 256, 0, s>>>(c->d_st, c->d_phi, c->d_dn_phi, c->nx * c->ny, c->dn_bound);
     ORBIT_PE(s);
     nl += 5;
@@ -1671,8 +1712,8 @@ int orbit_sc2p5d_set_denoiser(orbit_sc2p5d_t* c, orbit_denoiser_t* dn, int check
     c->dn = nullptr;
     return ORBIT_OK;
   }
-  if (c->form != ORBIT_FORM_PLAIN || c->rb)
-    return set_error(ORBIT_ERR_UNSUPPORTED, "the learned closure is built for the plain 2.5D calculator");
+  if (c->rb)
+    return set_error(ORBIT_ERR_UNSUPPORTED, "the learned closure is built for the 2.5D calculator (plain or FP32 form)");
   int h = 0, w = 0, mb = 0;
   int rc = orbit_denoiser_info(dn, nullptr, &h, &w, &mb);
   if (rc) return rc;

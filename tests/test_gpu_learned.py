@@ -89,6 +89,54 @@ def test_closure_denoises_inside_the_kick():
     assert st["checks"] == 1 and st["fallback"] == 0 and st["last_err"] < 1e-3
 
 
+def test_closure_with_the_fp32_form():
+    """The learned + FP32 form: the closure denoises the FP32 form's float
+    deposit (same gain bar as the plain form's), keeps its charge, and the
+    judge solves the raw deposit with the FP32 form's own Green spectrum."""
+    from orbit_gb300 import _native, call
+    from orbit_gb300 import denoiser as DN
+    from spacecharge import SpaceChargeCalc2p5D
+    import torch
+    n = 100_000
+    soa = np.zeros((6, n))
+    soa[4] = np.random.default_rng(2).uniform(-100, 100, n)
+    b = _bunch(soa, 1e9)
+    ptrs = b._device_bunch().device_pointers()
+    call("orbit_beam_sample", ctypes.c_void_p(ptrs[0]), ctypes.c_void_p(ptrs[2]), n, 1, 3e-3, 4e-3, 98)
+    net = DN.default_network()
+    raw_calc = SpaceChargeCalc2p5D(128, 128, 64, form="fp32")
+    raw_calc.trackBunch(b, 0.0)
+    raw = raw_calc._calc.grid(_native.GRID_RHO)
+    calc = SpaceChargeCalc2p5D(128, 128, 64, form="fp32")
+    calc.setDenoiser(net, 1, 1e-3)
+    calc.trackBunch(b, 0.0)
+    den = calc._calc.grid(_native.GRID_RHO)
+    lim = calc._calc.limits()[:4].copy()
+    g = torch.empty(128 * 128, dtype=torch.float32, device="cuda")
+    call("orbit_beam_deposit", ctypes.c_void_p(g.data_ptr()), 128, 128,
+         lim.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 10_000_000, 1, 3e-3, 4e-3, 124)
+    hi = g.cpu().numpy().astype(np.float64).reshape(128, 128)
+    hi *= raw.sum() / hi.sum()
+    err_raw = ((raw - hi) ** 2).mean()
+    err_den = ((den - hi) ** 2).mean()
+    assert abs(den.sum() / raw.sum() - 1) < 1e-5  # charge kept (FP32 grid)
+    assert err_raw / err_den >= 10.0, (err_raw, err_den)
+    st = calc.getDenoiserState()
+    assert st["checks"] == 1 and st["fallback"] == 0 and st["last_err"] < 1e-3
+    # a tracked lattice with both forms runs and its kicks move the beam
+    from orbit_gb300 import workloads as W
+    import contextlib
+    import io
+    b2 = W.make_bunch(W.c2_coords(n, seed=5), W.C2_MACROSIZE * 10)
+    c2 = SpaceChargeCalc2p5D(128, 128, 64, form="fp32")
+    c2.setDenoiser(net, 10, 1e-3)
+    with contextlib.redirect_stdout(io.StringIO()):
+        lat = W.fodo_lattice(c2, cells=5)
+    lat.trackBunchTurns(b2, 2)
+    st2 = c2.getDenoiserState()
+    assert st2["checks"] == 4 and st2["fallback"] == 0
+
+
 def test_judge_falls_back_on_a_beam_unlike_the_training_beams():
     """Two separated small blobs score a larger judge error (potential from
     the denoised against the raw density) than a beam like the training
