@@ -74,9 +74,11 @@ __device__ __forceinline__ void fft_stage_pow2(const typename CT<T>::t* __restri
   }
 }
 
+// lg0 > 0: the first lg0 radix-2 stages are done (the caller staged their
+// result in a); only with N/2 threads or more (all stages radix 2).
 template <typename T, bool INV>
 __device__ typename CT<T>::t* block_fft_pow2(typename CT<T>::t* a, typename CT<T>::t* b, const FftPlan& pl,
-                                             const typename CT<T>::t* __restrict__ tw) {
+                                             const typename CT<T>::t* __restrict__ tw, int lg0 = 0) {
   typedef typename CT<T>::t C;
   // FP64 runs at a fraction of a lane per cycle per SM sub-partition, so the
   // transform is bound by how many warps share it: with N/2 threads every
@@ -85,7 +87,7 @@ __device__ typename CT<T>::t* block_fft_pow2(typename CT<T>::t* a, typename CT<T
   const int N = pl.n;
   const int lgN = 31 - __clz(N);
   const bool wide = (int)blockDim.x >= N / 2;
-  int L = 1, lgL = 0;
+  int L = 1 << lg0, lgL = lg0;
   while (lgL < lgN) {
     if (!wide && lgL + 2 <= lgN) {
       fft_stage_pow2<T, 4, INV>(a, b, N, L, lgL, lgN - lgL - 2, tw);
@@ -164,6 +166,16 @@ __device__ typename CT<T>::t* block_fft(typename CT<T>::t* a, typename CT<T>::t*
     L = Lp;
   }
   return a;
+}
+
+// Forward transform of a power-of-two sequence whose second half is zero
+// (the zero-padded half of the Hockney grid), with N/2 threads or more: the
+// first radix-2 Stockham stage maps a[t], 0 to b[2t] = b[2t+1] = a[t], so
+// the caller stages its input that way into `a` (see fft_halfzero_ok) and
+// the transform starts at the second stage.
+template <typename T>
+__device__ __forceinline__ bool fft_halfzero_ok(const FftPlan& pl, int nin) {
+  return pl.pow2 && (int)blockDim.x >= pl.n / 2 && nin <= pl.n / 2;
 }
 
 // Copies the W_N twiddle table to shared memory (the caller synchronises).

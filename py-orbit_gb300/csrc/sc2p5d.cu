@@ -176,7 +176,9 @@ __device__ __forceinline__ void rows_fwd_body(ScState* st, void* src, double* rh
   load_twiddles(stw, tw, N);
   int r0 = 2 * blk, r1 = r0 + 1;
   double iq = st->inv_qscale;
-  for (int j = threadIdx.x; j < N; j += blockDim.x) {
+  // deposit rows: columns ncols..N-1 are the zero padding
+  const bool hz = SRC != 0 && fft_halfzero_ok<T>(pl, ncols);
+  for (int j = threadIdx.x; j < (hz ? N / 2 : N); j += blockDim.x) {
     T va = (T)0, vb = (T)0;
     if (j < ncols) {
       if (SRC == 0) {
@@ -216,10 +218,15 @@ __device__ __forceinline__ void rows_fwd_body(ScState* st, void* src, double* rh
     C v;
     v.x = va;
     v.y = vb;
-    a[j] = v;
+    if (hz) {
+      a[2 * j] = v;
+      a[2 * j + 1] = v;
+    } else {
+      a[j] = v;
+    }
   }
   __syncthreads();
-  C* Z = block_fft<T>(a, b, pl, stw, false);
+  C* Z = hz ? block_fft_pow2<T, false>(a, b, pl, stw, 1) : block_fft<T>(a, b, pl, stw, false);
   for (int k = threadIdx.x; k < H; k += blockDim.x) {
     C zk = Z[k], zc = c_conj(Z[(N - k) % N]);
     C A, B;
@@ -266,14 +273,20 @@ __device__ __forceinline__ void cols_body(ScState* st, typename CT<T>::t* hat, t
   const int N = pl.n;
   C* stw = b + N;
   load_twiddles(stw, tw, N);
-  for (int r = threadIdx.x; r < N; r += blockDim.x) {
+  const bool hz = MODE == 1 && fft_halfzero_ok<T>(pl, nin);
+  for (int r = threadIdx.x; r < (hz ? N / 2 : N); r += blockDim.x) {
     C v;
     if (r < nin) v = hat[(size_t)r * H + k];
     else { v.x = (T)0; v.y = (T)0; }
-    a[r] = v;
+    if (hz) {
+      a[2 * r] = v;
+      a[2 * r + 1] = v;
+    } else {
+      a[r] = v;
+    }
   }
   __syncthreads();
-  C* F = block_fft<T>(a, b, pl, stw, false);
+  C* F = hz ? block_fft_pow2<T, false>(a, b, pl, stw, 1) : block_fft<T>(a, b, pl, stw, false);
   if (MODE == 0) {
     for (int r = threadIdx.x; r < N; r += blockDim.x) green[(size_t)k * N + r] = F[r];
     if (k == 0 && threadIdx.x == 0) st->n_green += 1;
