@@ -117,11 +117,11 @@ MAP_FLOPS = {1: 22, 2: 16, 3: 25, 4: 70, 5: 70, 6: 18, 7: 25, 8: 20, 9: 14, 10: 
 # (smsp__sass_thread_inst_executed_op_{dfma,dmul,dadd}_pred_on, 4e6
 # particles): the fused pass alternates the {kick, quad1, quad2 (the two
 # back-to-back quad2 of the reference schedule merged), quad1, fringe-out}
-# segment (79.6) and the {kick, drift, fringe-in} segment (60.6); the deposit
+# segment (73.0) and the {kick, drift, fringe-in} segment (54.0); the deposit
 # runs 6.3 (one FMA per coordinate and the fixed-point conversions; weights
 # and sums are integer).  Conversions and compares also occupy the FP64 pipe
 # and are not in these counts.
-FP64_INST_PER_PARTICLE = {"pass_kick_maps": (79.6 + 60.6) / 2, "deposit": 6.26}
+FP64_INST_PER_PARTICLE = {"pass_kick_maps": (73.0 + 54.0) / 2, "deposit": 6.26}
 
 
 def pass_flops_per_turn(ops):
