@@ -123,6 +123,13 @@ int orbit_bunch_moments(orbit_bunch_t* b, double* out);
  * (zero before the first call, as the attribute the reference adds).
  * Enqueued on the bunch's stream; the first call allocates. */
 int orbit_bunch_tune_analysis(orbit_bunch_t* b, const double* twiss, double etot);
+/* BunchTwissAnalysis::computeBunchMoments (BunchTwissAnalysis.cc:146-340)
+ * summed on the device: out[(order+1)^2] = the moment table getBunchMoment
+ * (i, j) reads (row i: power of x), with the reference's recurrences,
+ * normalisation and fixed cells; params = {D, E_kin + mass, beta^2, xAvg,
+ * yAvg, xbetaterm, ybetaterm} from analyzeBunch's getters (D = 0 without the
+ * dispersion term).  2 <= order <= 16.  Waits for the bunch's stream. */
+int orbit_bunch_xy_moments(orbit_bunch_t* b, int order, const double* params, double* out);
 /* The six attribute rows {xLastPhase, yLastPhase, xLastTune, yLastTune,
  * xAction, yAction}, each of n values, to or from the host. */
 int orbit_bunch_phase_get(orbit_bunch_t* b, double* host);

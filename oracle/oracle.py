@@ -354,6 +354,7 @@ def ref():
         L.ref_bnd_get.argtypes = [_vp, _dp, _dp, _dp]
         L.ref_sc_track_bnd.argtypes = [_vp, _vp, ctypes.c_double, _vp]
         L.ref_twiss.argtypes = [_vp, _dp, _dp]
+        L.ref_bunch_moments.argtypes = [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp]
         L.ref_tune_new.restype = _vp
         L.ref_tune_free.argtypes = [_vp]
         L.ref_tune_assign.argtypes = [_vp, _dp]
@@ -496,6 +497,17 @@ class RefBoundary:
 
 def ref_sc_track_bnd(sc: "RefSC", bunch: RefBunch, length: float, bnd: RefBoundary):
     ref().ref_sc_track_bnd(sc.h, bunch.h, float(length), bnd.h)
+
+
+def ref_bunch_moments(bunch: RefBunch, order, dispersion=0, emitnorm=0):
+    """getBunchMoment(i, j), i, j = 0..order, after the reference's
+    BunchTwissAnalysis::computeBunchMoments(bunch, order, dispersion,
+    emitnorm) (order >= 2)."""
+    if order < 2:
+        raise ValueError("order >= 2: for order 1 the reference writes outside its moment table")
+    out = np.zeros((order + 1) * (order + 1))
+    ref().ref_bunch_moments(bunch.h, int(order), int(dispersion), int(emitnorm), _P(out))
+    return out.reshape(order + 1, order + 1)
 
 
 def ref_twiss(bunch: RefBunch):

@@ -163,6 +163,15 @@ void ref_twiss(void* b, double* out, double* g) {
     g[k++] = t.getEffectiveGamma(ic);
   }
 }
+// BunchTwissAnalysis::computeBunchMoments then getBunchMoment(i, j) for
+// i, j = 0..order into out[i * (order + 1) + j] (order >= 2: for order 1 the
+// reference writes outside its table).
+void ref_bunch_moments(void* b, int order, int dispersion, int emitnorm, double* out) {
+  BunchTwissAnalysis t;
+  t.computeBunchMoments((Bunch*)b, order, dispersion, emitnorm);
+  for (int i = 0; i <= order; ++i)
+    for (int j = 0; j <= order; ++j) out[i * (order + 1) + j] = t.getBunchMoment(i, j);
+}
 void* ref_tune_new() { return new BunchTuneAnalysis(); }
 void ref_tune_free(void* t) { delete (BunchTuneAnalysis*)t; }
 void ref_tune_assign(void* t, const double* tw) {

@@ -587,6 +587,40 @@ class BunchTwissAnalysis:
         bunch.compress()
         self._load(bunch._device_bunch().moments(), bunch.getSyncParticle())
 
+    def computeBunchMoments(self, bunch: Bunch, order, dispersionflag=0, emitnormflag=0):
+        """The x-y moment table of BunchTwissAnalysis::computeBunchMoments
+        (BunchTwissAnalysis.cc:146-340), summed on the device with the
+        reference's recurrences, normalisation and fixed cells: centred on
+        the averages of analyzeBunch (its dispersion-corrected average is
+        never taken: dispterm is zero where the reference tests it), divided
+        by sqrt(beta) (emitnormflag: sqrt(beta * emittance)) per power, x
+        corrected by D dE / (E_kin + m) / beta^2 with dispersionflag.  The
+        reference's uniform-macrosize loop also adds momX[2] momY[order]
+        once per particle after its loops (cell [2][order], not
+        normalised), reproduced here.  order >= 2 (for order 1 that write
+        falls outside the reference's table)."""
+        order = int(order)
+        if order < 2:
+            raise ValueError("computeBunchMoments: order >= 2")
+        self.analyzeBunch(bunch)
+        D = self.getDispersion(0) if dispersionflag > 0 else 0.0
+        if emitnormflag > 0:
+            xb = math.sqrt(self.getBeta(0) * self.getEmittance(0))
+            yb = math.sqrt(self.getBeta(1) * self.getEmittance(1))
+        else:
+            xb = math.sqrt(self.getBeta(0))
+            yb = math.sqrt(self.getBeta(1))
+        params = [D, self._kin + self._mass, self._beta * self._beta, self.getAverage(0), self.getAverage(2), xb, yb]
+        self._order = order
+        self._mom_xy = bunch._device_bunch().xy_moments(order, params)
+
+    def getBunchMoment(self, i, j):
+        """(BunchTwissAnalysis.cc:350-353)"""
+        order = getattr(self, "_order", -1)
+        if i < 0 or i > order or j < 0 or j > order:
+            return 0.0
+        return float(self._mom_xy[i, j])
+
     def _load(self, mom, s):
         """Takes the 29 moments {count, total macrosize, averages, <c_i c_j>
         (i >= j)} and the reference particle's kinematics."""

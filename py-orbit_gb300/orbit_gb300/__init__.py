@@ -110,6 +110,16 @@ class DeviceBunch:
         call("orbit_bunch_moments", self.h, out.ctypes.data_as(_dp))
         return out
 
+    def xy_moments(self, order: int, params) -> np.ndarray:
+        """The (order+1) x (order+1) table of BunchTwissAnalysis::
+        computeBunchMoments summed on the device; params = {D, E_kin + mass,
+        beta^2, xAvg, yAvg, xbetaterm, ybetaterm} (D = 0 without the
+        dispersion term)."""
+        out = np.zeros((order + 1) * (order + 1))
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        call("orbit_bunch_xy_moments", self.h, int(order), p.ctypes.data_as(_dp), out.ctypes.data_as(_dp))
+        return out.reshape(order + 1, order + 1)
+
     def tune_analysis(self, twiss, etot: float):
         """BunchTuneAnalysis::analyzeBunch on the device; twiss = {betax,
         alphax, etax, etapx, betay, alphay}, etot = kinetic energy + mass."""

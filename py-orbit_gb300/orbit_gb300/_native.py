@@ -97,6 +97,7 @@ _SIGS = {
     "orbit_program_destroy": (ctypes.c_int, [_vp]),
     "orbit_program_set_boundaries": (ctypes.c_int, [_vp, ctypes.POINTER(_vp), ctypes.c_int]),
     "orbit_bunch_moments": (ctypes.c_int, [_vp, _dp]),
+    "orbit_bunch_xy_moments": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp]),
     "orbit_bunch_tune_analysis": (ctypes.c_int, [_vp, _dp, ctypes.c_double]),
     "orbit_bunch_phase_get": (ctypes.c_int, [_vp, _dp]),
     "orbit_bunch_phase_set": (ctypes.c_int, [_vp, _dp]),

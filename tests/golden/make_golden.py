@@ -243,6 +243,20 @@ def main():
     d[0] += 2.0 * d[5]
     diag_case("diag_twiss_tune", d, [10.0, -1.2, 0.5, 0.1, 8.0, 0.7],
               [("quad1", (0.5, 0.5)), ("drift", (1.0,)), ("quad1", (0.5, -0.5))])
+    # 9) BunchTwissAnalysis::computeBunchMoments / getBunchMoment on the same
+    # bunch (orders 2-4, with and without the dispersion and emittance flags)
+    moments_case("diag_moments", d)
+
+
+def moments_case(name, soa, ek=1.0, msize=1e9):
+    b = O.RefBunch(soa, ek, msize)
+    out = {"init": soa, "ek": ek, "macrosize": msize}
+    for order in (2, 3, 4):
+        for disp in (0, 1):
+            for norm in (0, 1):
+                out["m_%d_%d_%d" % (order, disp, norm)] = O.ref_bunch_moments(b, order, disp, norm)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print("wrote", name)
 
 
 if __name__ == "__main__":

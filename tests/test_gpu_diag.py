@@ -202,3 +202,79 @@ def test_tune_analysis_large_bunch_matches_oracle():
     O.tune_analysis(soa, s.beta(), s.kinEnergy() + s.mass(), tw, ph)
     O.tune_analysis(b.getCoordinates(), s.beta(), s.kinEnergy() + s.mass(), tw, ph)
     check_phase(b._dev.phase_get(), ph)
+
+
+def _moment_table_close(got, ref, tol=1e-9):
+    """Cell by cell: zeros exactly, the others within tol relative (the
+    table spans many orders of magnitude; sums differ in order only)."""
+    got, ref = np.asarray(got), np.asarray(ref)
+    zero = ref == 0.0
+    assert np.array_equal(got[zero], ref[zero])
+    nz = ~zero
+    rel = np.abs(got[nz] - ref[nz]) / np.abs(ref[nz])
+    return float(rel.max()) if rel.size else 0.0
+
+
+def test_bunch_moments_against_golden():
+    """BunchTwissAnalysis.computeBunchMoments / getBunchMoment against the
+    compiled reference: orders 2-4, with and without the dispersion and the
+    emittance-normalisation flags (the reference's stray cell [2][order]
+    included)."""
+    from bunch import BunchTwissAnalysis
+    g = load_golden("diag_moments")
+    b = gpu_bunch(g["init"], float(g["macrosize"]), float(g["ek"]))
+    tw = BunchTwissAnalysis()
+    for order in (2, 3, 4):
+        for disp in (0, 1):
+            for norm in (0, 1):
+                tw.computeBunchMoments(b, order, disp, norm)
+                got = np.array([[tw.getBunchMoment(i, j) for j in range(order + 1)] for i in range(order + 1)])
+                err = _moment_table_close(got, g["m_%d_%d_%d" % (order, disp, norm)])
+                assert err <= 1e-9, (order, disp, norm, err)
+    assert tw.getBunchMoment(5, 0) == 0.0 and tw.getBunchMoment(-1, 0) == 0.0
+
+
+def _moments_msize_restated(soa, m, order, D, ekm, b2, xa, ya, xb, yb):
+    """The per-particle-macrosize branch of computeBunchMoments
+    (BunchTwissAnalysis.cc:229-262, 325-336) restated in numpy."""
+    disp = D * soa[5] / ekm / b2 if D != 0.0 else 0.0
+    dx, dy = (soa[0] - disp) - xa, soa[2] - ya
+    w = order + 1
+    out = np.zeros((w, w))
+    mx = [np.ones_like(dx)]
+    my = [np.ones_like(dy)]
+    for k in range(order):
+        mx.append(mx[-1] * m * dx)
+        my.append(my[-1] * m * dy)
+    for j in range(order):
+        for i in range(order + 1 - j):
+            out[i, j] = np.sum(mx[i] / xb ** i * my[j] / yb ** j + mx[i] * my[j])
+    tot = m.sum()
+    for i in range(w):
+        for j in range(w - i):
+            out[i, j] /= tot
+    out[0, 0], out[1, 0], out[0, 1] = 1.0, xa, ya
+    return out
+
+
+def test_bunch_moments_with_macrosize_attribute():
+    from bunch import BunchTwissAnalysis
+    g = load_golden("diag_moments")
+    soa = g["init"]
+    m = np.random.default_rng(5).uniform(0.5, 1.5, soa.shape[1])
+    b = gpu_bunch(soa, 1e9)
+    b.addPartAttr("macrosize")
+    b._part_attr["macrosize"][: soa.shape[1], 0] = m
+    b._host_modified()
+    tw = BunchTwissAnalysis()
+    for order, disp, norm in ((2, 0, 0), (3, 1, 1), (4, 0, 1)):
+        tw.computeBunchMoments(b, order, disp, norm)
+        got = np.array([[tw.getBunchMoment(i, j) for j in range(order + 1)] for i in range(order + 1)])
+        D = tw.getDispersion(0) if disp else 0.0
+        xb = np.sqrt(tw.getBeta(0) * tw.getEmittance(0)) if norm else np.sqrt(tw.getBeta(0))
+        yb = np.sqrt(tw.getBeta(1) * tw.getEmittance(1)) if norm else np.sqrt(tw.getBeta(1))
+        s = b.getSyncParticle()
+        ref = _moments_msize_restated(soa, m, order, D, s.kinEnergy() + b.mass(), s.beta() ** 2,
+                                      tw.getAverage(0), tw.getAverage(2), xb, yb)
+        err = _moment_table_close(got, ref)
+        assert err <= 1e-9, (order, disp, norm, err)

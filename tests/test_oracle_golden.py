@@ -206,3 +206,56 @@ def test_diag_oracle_macrosize_weights():
     # the centroids are small against the coordinates: scale by <|c_i|>
     scale = (np.abs(soa) * w).sum(axis=1) / w.sum()
     assert np.all(np.abs(mom[2:8] - (soa * w).sum(axis=1) / w.sum()) <= 1e-13 * scale)
+
+
+def _moments_uniform_restated(soa, order, D, ekm, b2, xa, ya, xb, yb):
+    """The uniform-macrosize branch of BunchTwissAnalysis::computeBunchMoments
+    (BunchTwissAnalysis.cc:264-336) restated in numpy: the normalised term
+    for j < order, i <= order - j; the raw product momX[i] momY[j] that the
+    reference adds once per particle after its loops (i = 2, j = order: its
+    braces close the loops before that statement), left unnormalised."""
+    disp = D * soa[5] / ekm / b2 if D != 0.0 else 0.0
+    dx, dy = (soa[0] - disp) - xa, soa[2] - ya
+    w = order + 1
+    out = np.zeros((w, w))
+    mx, my = [np.ones_like(dx)], [np.ones_like(dy)]
+    for _ in range(order):
+        mx.append(mx[-1] * dx)
+        my.append(my[-1] * dy)
+    for j in range(order):
+        for i in range(order + 1 - j):
+            out[i, j] = np.sum(mx[i] / xb ** i * my[j] / yb ** j)
+    out[2, order] += np.sum(mx[2] * my[order])
+    n = soa.shape[1]
+    for i in range(w):
+        for j in range(w - i):
+            out[i, j] /= n
+    out[0, 0], out[1, 0], out[0, 1] = 1.0, xa, ya
+    return out
+
+
+def test_bunch_moments_restatement_against_golden():
+    """The restated computeBunchMoments (its stray cell included) against
+    the compiled reference's tables, cell by cell to 1e-9 (zeros exactly):
+    the semantics the device kernel reproduces."""
+    from bunch import Bunch, BunchTwissAnalysis
+    g = load_golden("diag_moments")
+    soa = g["init"]
+    b = Bunch()
+    b.getSyncParticle().kinEnergy(float(g["ek"]))
+    t = BunchTwissAnalysis()
+    t._load(O.twiss_moments(soa), b.getSyncParticle())
+    s = b.getSyncParticle()
+    for order in (2, 3, 4):
+        for disp in (0, 1):
+            for norm in (0, 1):
+                D = t.getDispersion(0) if disp else 0.0
+                xb = np.sqrt(t.getBeta(0) * t.getEmittance(0)) if norm else np.sqrt(t.getBeta(0))
+                yb = np.sqrt(t.getBeta(1) * t.getEmittance(1)) if norm else np.sqrt(t.getBeta(1))
+                got = _moments_uniform_restated(soa, order, D, s.kinEnergy() + s.mass(), s.beta() ** 2,
+                                                t.getAverage(0), t.getAverage(2), xb, yb)
+                ref = g["m_%d_%d_%d" % (order, disp, norm)]
+                zero = ref == 0.0
+                assert np.array_equal(got[zero], ref[zero])
+                rel = np.abs(got[~zero] - ref[~zero]) / np.abs(ref[~zero])
+                assert rel.max() <= 1e-9, (order, disp, norm, rel.max())
