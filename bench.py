@@ -470,6 +470,17 @@ def run_ours(args):
                 else "fallback 6.8 TB/s",
                 "kernel_ms_per_launch": per_launch_ms, "share_of_turn": dom_ms / turn_ms,
                 "kernels": {k: {"ms": v[0], "launches": v[1], "share": v[0] / turn_ms} for k, v in prof.items()}}
+    if name == "learn_network":
+        # the learned forms: the network's 3x3 layers run on the tensor cores
+        # (TF32, half the BF16 rate); the bound is its FLOPs per forward over
+        # the forward's time (one 128 x 128 image per kick: latency-bound)
+        bf16 = measured_bf16_tflops()
+        tf32_peak = bf16 / 2.0 if bf16 else 1900.0 / 2.0
+        tflops = DENOISER_GFLOP_128 * 1e-3 / (per_launch_ms * 1e-3)
+        roofline.update({"bound": "tensor", "achieved": tflops, "peak": tf32_peak, "unit": "TFLOP/s",
+                         "frac": tflops / tf32_peak, "traffic": None,
+                         "peak_source": "half the measured bf16 GEMM rate (MEASURED_PEAKS.json bf16_tflops)"
+                         if bf16 else "half the fallback 1.9 PFLOP/s bf16"})
     if args.form == "plain" and WL["name"] == "fodo":
         # the plain form is bound by the FP64 pipe: counted FP64 instructions
         # of the fused passes and of the deposit against the live DFMA peak
