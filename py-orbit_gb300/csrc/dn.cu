@@ -14,7 +14,9 @@
 // 2x2 average, "up" a 2x nearest-neighbour upsample concatenated with the
 // skip tensor.  302,561 parameters.  Convolution weights are BF16 (an FP32
 // master copy is what Adam updates), biases FP32; activations and all
-// accumulation FP32.  Training: mean squared error, Adam.
+// accumulation FP32.  Training: mean squared error, Adam, on CUDA-core
+// layers.  Single-image inference (the kick's closure) runs the 3x3 layers
+// on the tensor cores (k_conv3_tc: tcgen05.mma kind::tf32 into TMEM).
 //
 // Tensors are NCHW FP32 in device memory.
 #include <cuda_bf16.h>
