@@ -1424,7 +1424,9 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
       // the grid in row bands, each block one band of one particle chunk
       int nb;
       int rpb = band_rows(c->nx, c->ny, c->nz, &nb);
-      int chunks = (n + 2047) / 2048, cap = (num_sms() + nb - 1) / nb;
+      // one block per SM (each holds a band of the grid): at most one wave,
+      // so that no block starts after the others have finished
+      int chunks = (n + 2047) / 2048, cap = num_sms() / nb > 0 ? num_sms() / nb : 1;
       chunks = chunks < 1 ? 1 : (chunks > cap ? cap : chunks);
       int bt = max_threads_of(k_deposit_band);
       bt = bt > 768 ? 768 : (bt & ~31);
