@@ -35,7 +35,11 @@ N_PARTICLES = 1_000_000
 GRID = (128, 128, 64)
 CELLS = 40
 METRIC = "2.5D SC macroparticle-kicks/s, 1M particles 128x128 grid, vs FP64 plain form"
-CPU_SAMPLE_N = 250_000
+# CPU legs (the oracle on the host cores): the whole FODO bunch, one turn per
+# step (the same configuration as the GPU arm); the large ring's 1.6e7
+# particles take minutes per turn on the host, so it times a 1e6 sample.
+CPU_SAMPLE_RING = 1_000_000
+L2_NOTE = "GPU arm: flushed (512 MiB write) before each timed step"
 
 # Algorithmic HBM bytes per particle of each particle kernel: the fused pass
 # reads and writes x, xp, y, yp, z, dE; the deposit and the extrema scan
@@ -342,23 +346,38 @@ def cpu_reference_rate(n_sample, turns, warmup, threads):
     return n_sample * kicks_per_turn * turns / total, total / turns, kicks_per_turn
 
 
+def cpu_sample_n(n):
+    """Particles of the CPU legs: the GPU arm's whole bunch, except on the
+    large ring (a 1e6 sample of its 1.6e7)."""
+    return min(n, CPU_SAMPLE_RING) if WL["name"] == "ring" else n
+
+
+def bench_config(n, kicks_per_turn, form, world):
+    """The workload description shared by both arms (same keys, same values
+    where both run the same configuration)."""
+    return {"workload": "%s, %d particles, grid %dx%dx%d, one turn per step" % (WL["desc"], n, *GRID),
+            "form": form, "particles": n, "grid": list(GRID), "kicks_per_step": kicks_per_turn, "l2": L2_NOTE,
+            "parallelism": "replicas" if world > 1 else "single"}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    rate, per_turn, kpt = cpu_reference_rate(CPU_SAMPLE_N, args.steps, args.warmup, threads)
+    n = cpu_sample_n(WL["n"])
+    rate, per_turn, kpt = cpu_reference_rate(n, args.steps, args.warmup, threads)
     ms_per_step = per_turn * 1e3
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": "macroparticle-kicks/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded 4D waterbag, Gaussian z/dE)",
-        "config": {"workload": "%s, grid %dx%dx%d, sample %d particles" % (WL["desc"], *GRID, CPU_SAMPLE_N),
-                   "particles": CPU_SAMPLE_N, "grid": list(GRID), "kicks_per_step": kpt},
+        "data": "synthetic (seeded 4D waterbag rms 4 mm/0.8 mrad, z~N(0,10 m), dE~N(0,1 MeV))",
+        "config": bench_config(n, kpt, "plain", 1),
         "cpu_baseline": {"value": rate, "unit": "macroparticle-kicks/s", "cores": threads, "kind": "port",
-                         "sample": "%d particles x 1 turn (%d SC kicks) per step, %d threads as rank slices"
-                                   % (CPU_SAMPLE_N, kpt, threads)},
+                         "sample": "%d particles x 1 turn (%d SC kicks) per step, %d threads as rank slices "
+                                   "(the reference's MPI decomposition); the restatement reproduces the compiled "
+                                   "reference bit for bit at one thread" % (n, kpt, threads)},
         "e2e": {"value": rate, "unit": "macroparticle-kicks/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -481,16 +500,40 @@ def run_ours(args):
                          "frac": tflops / tf32_peak, "traffic": None,
                          "peak_source": "half the measured bf16 GEMM rate (MEASURED_PEAKS.json bf16_tflops)"
                          if bf16 else "half the fallback 1.9 PFLOP/s bf16"})
-    if args.form == "plain" and WL["name"] == "fodo":
-        # the plain form is bound by the FP64 pipe: counted FP64 instructions
-        # of the fused passes and of the deposit against the live DFMA peak
+    if args.form in ("plain", "fp32") and name in ("pass_kick_maps", "pass_maps"):
+        # The fused pass keeps the maps in FP64 (both forms) and is bound by
+        # the FP64 pipe, not by HBM: its roof is the FP64 rate.  Algorithmic
+        # work = the reference's FP64 operation count of every map and SC
+        # kick the passes of one turn apply (FLOP-counting each +, -, *, /
+        # of teapotbase.cc and of the kick formulas), over the passes' time,
+        # against the DFMA rate measured in this process (2 FLOP per DFMA;
+        # MEASURED_PEAKS.json has no FP64 figure).  The deposit, gradient
+        # and extrema run on the integer pipes here, so the pass does the
+        # reference's work in fewer FP64 instructions than its count / 2
+        # and can read above 1.0.
+        hbm = dict(roofline)
+        hbm.pop("kernels", None)
+        pass_ms = sum(v[0] for k, v in prof.items() if k in ("pass_kick_maps", "pass_maps"))
+        flops_turn = pass_flops_per_turn(prog.ops) * float(n)
+        tflops = flops_turn / (pass_ms * 1e-3) / 1e12
+        roofline.update({
+            "bound": "fp64", "kernel": "fused pass (kick + maps + extrema), all launches of one turn",
+            "achieved": tflops, "peak": fp64_peak, "unit": "TFLOP/s", "frac": tflops / fp64_peak,
+            "peak_source": "measured in this run (orbit_device_peaks: independent DFMA chains on every SM, "
+                           "2 FLOP per DFMA); MEASURED_PEAKS.json carries no FP64 figure",
+            "alg_flops_per_particle_turn": pass_flops_per_turn(prog.ops),
+            "alg_count": "reference operation count of the SC kick (113 per particle) and of each map "
+                         "(teapotbase.cc), bench.py MAP_FLOPS",
+            "hbm": {"achieved": hbm["achieved"], "peak": hbm["peak"], "unit": "GB/s", "frac": hbm["frac"],
+                    "traffic": hbm["traffic"], "alg_bytes_per_particle": ALG_BYTES[name],
+                    "peak_source": hbm["peak_source"]}})
+        # counted FP64 instructions (ncu) of the passes and of the deposit
+        # against the live DFMA instruction rate
         peak_inst = fp64_peak / 2 * 1e12
-        fp = {"peak_tflops": fp64_peak, "peak_source": "measured in this run (orbit_device_peaks: DFMA chains)",
-              "peak_inst_per_s": peak_inst,
-              "reference_flops_per_particle_turn": pass_flops_per_turn(prog.ops) + DEPOSIT_FLOPS * kicks_per_turn}
+        fp = {"peak_inst_per_s": peak_inst}
         for kname, ipp in FP64_INST_PER_PARTICLE.items():
             k_ms, k_l = prof.get(kname, (0.0, 0))
-            if k_ms > 0:
+            if k_ms > 0 and args.form == "plain" and WL["name"] == "fodo":
                 rate = ipp * n * k_l / (k_ms * 1e-3)
                 fp[kname] = {"fp64_inst_per_particle": ipp, "achieved_inst_per_s": rate, "frac": rate / peak_inst}
         roofline["fp64_pipe"] = fp
@@ -529,12 +572,13 @@ def run_ours(args):
 
         form_err = form_error(soa, bunch.macroSize(), make_lattice, args.form, turns=args.error_turns)
     cpu = None
-    if not args.no_cpu:
+    if not args.no_cpu and world == 1:
         threads = os.cpu_count() or 1
-        rate, per_turn, kpt = cpu_reference_rate(CPU_SAMPLE_N, 1, 0, threads)
+        ncpu = cpu_sample_n(n)
+        rate, per_turn, kpt = cpu_reference_rate(ncpu, 1, 0, threads)
         cpu = {"value": rate, "unit": "macroparticle-kicks/s", "cores": threads, "kind": "port",
-               "sample": "%d particles x 1 turn (%d SC kicks), %d threads as rank slices" % (CPU_SAMPLE_N, kpt,
-                                                                                         threads)}
+               "sample": "%d particles x 1 turn (%d SC kicks), %d threads as rank slices" % (ncpu, kpt, threads),
+               "same_config": ncpu == n}
     line = {
         "metric": METRIC, "value": value, "unit": "macroparticle-kicks/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -544,11 +588,8 @@ def run_ours(args):
                   "learned-fp32": "f32-field/f64-coords + bf16-weight network (tf32 tensor-core MMA, f32 accumulation)"
                   }[args.form],
         "data": "synthetic (seeded 4D waterbag rms 4 mm/0.8 mrad, z~N(0,10 m), dE~N(0,1 MeV))",
-        "config": {"workload": "%s, %d particles, grid %dx%dx%d, one turn per step" % (WL["desc"], n, *GRID),
-                   "form": args.form, "particles": n, "grid": list(GRID),
-                   "kicks_per_step": kicks_per_turn, "l2": "flushed (512 MiB write) before each timed step",
-                   "parallelism": "replicas" if world > 1 else "single",
-                   "green_rebuilds_per_kick": green_rate},
+        "config": bench_config(n, kicks_per_turn, args.form, world),
+        "green_rebuilds_per_kick": green_rate,
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
         "gpu_launches": launches_per_turn * args.steps, "wall_s": wall,
     }
@@ -702,10 +743,10 @@ def run_batched(args):
     cpu = None
     if not args.no_cpu:
         threads = os.cpu_count() or 1
-        rate, per_turn, kpt = cpu_reference_rate(CPU_SAMPLE_N, 1, 0, threads)
+        rate, per_turn, kpt = cpu_reference_rate(N_PARTICLES, 1, 0, threads)
         cpu = {"value": rate, "unit": "macroparticle-kicks/s", "cores": threads, "kind": "port",
                "sample": "%d particles x 1 turn of the 128x128x64 FODO lattice (%d SC kicks), %d threads"
-                         % (CPU_SAMPLE_N, kpt, threads)}
+                         % (N_PARTICLES, kpt, threads)}
     classes = bb.classes()
     line = {
         "metric": METRIC, "value": value, "unit": "macroparticle-kicks/s", "n_gpus": 1, "steps": args.steps,

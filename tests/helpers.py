@@ -29,6 +29,22 @@ def coord_err(a, b):
     return max(rel_err(a[c], b[c]) for c in range(6))
 
 
+def kick_delta_tol(p_after, dp_ref):
+    """Tolerance on a kick read back from coordinates, dp = p_after - p_before.
+
+    The kick itself is held to TOL_FIELD, but the coordinate stores
+    fl(p_before + kick): that addition rounds by up to half an ulp of
+    p_after, in this code and in the reference alike, and the subtraction
+    that recovers the kick keeps that rounding.  Relative to max |kick| the
+    two roundings add 2 * 2^-53 max|p_after| / max|kick|; for a 1 mrad
+    angle kicked by 1e-5 that is 2.2e-14.  The bound is that term plus
+    TOL_FIELD."""
+    den = float(np.max(np.abs(dp_ref)))
+    if den == 0.0:
+        return TOL_FIELD
+    return TOL_FIELD + 2.0 * 2.0 ** -53 * float(np.max(np.abs(p_after))) / den
+
+
 def load_golden(name):
     return dict(np.load(os.path.join(GOLDEN, name + ".npz"), allow_pickle=False))
 

@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from helpers import TOL_COORD, TOL_FIELD, coord_err, load_golden, parse_sequence, rel_err
+from helpers import TOL_COORD, TOL_FIELD, coord_err, kick_delta_tol, load_golden, parse_sequence, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -56,7 +56,8 @@ def test_boundary_against_golden(case):
             ref = g["coords_%d" % k]
             if k == 0:
                 for c in (1, 3):
-                    assert rel_err(got[c] - before[c], ref[c] - before[c]) <= TOL_FIELD * 10, (case, c)
+                    dk = ref[c] - before[c]
+                    assert rel_err(got[c] - before[c], dk) <= kick_delta_tol(ref[c], dk), (case, c)
                 outside = np.array([bnd.isInside(x, y) != 1 for x, y in zip(before[0], before[2])])
                 assert np.array_equal(got[1][outside], before[1][outside])  # not kicked
             assert coord_err(got, ref) <= TOL_COORD

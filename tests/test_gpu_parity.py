@@ -7,8 +7,8 @@ import numpy as np
 import pytest
 
 import oracle as O
-from helpers import (TOL_COORD, TOL_FIELD, coord_err, golden_maps, kin_sync, load_golden, parse_sequence,
-                     rel_err)
+from helpers import (TOL_COORD, TOL_FIELD, coord_err, golden_maps, kick_delta_tol, kin_sync, load_golden,
+                     parse_sequence, rel_err)
 
 pytestmark = pytest.mark.gpu
 
@@ -79,7 +79,8 @@ def test_sc_against_golden(case):
                 assert rel_err(ey, g["ey_0"]) <= TOL_FIELD
                 assert rel_err(lam, g["lam_0"]) <= TOL_FIELD
                 # the kick itself: xp, yp changes
-                assert rel_err(c[1] - g["init"][1], g["coords_0"][1] - g["init"][1]) <= TOL_FIELD * 10
+                dk = g["coords_0"][1] - g["init"][1]
+                assert rel_err(c[1] - g["init"][1], dk) <= kick_delta_tol(g["coords_0"][1], dk)
             k += 1
         else:
             getattr(TPB, step[0])(b, *step[1])
@@ -176,7 +177,7 @@ def test_benchmark_grid_fused_program():
     s2 = O.OracleSC(128, 128, 64)
     a = np.ascontiguousarray(soa.copy())
     assert s2.track(a, oracle_sync_of(b2), 0.5, nthreads=8) == 0
-    assert rel_err(b2.getCoordinates()[1] - soa[1], a[1] - soa[1]) <= TOL_FIELD * 10
+    assert rel_err(b2.getCoordinates()[1] - soa[1], a[1] - soa[1]) <= kick_delta_tol(a[1], a[1] - soa[1])
 
 
 def test_fused_equals_eager():
@@ -260,7 +261,7 @@ def test_large_grid_global_path():
     rho, phi, zg, lim = sc.grids()
     assert rel_err(calc.getRhoGrid().getArray(), rho) <= TOL_FIELD
     assert rel_err(calc.getPhiGrid().getArray(), phi) <= TOL_FIELD
-    assert rel_err(got[1] - soa[1], a[1] - soa[1]) <= TOL_FIELD * 10
+    assert rel_err(got[1] - soa[1], a[1] - soa[1]) <= kick_delta_tol(a[1], a[1] - soa[1])
     assert coord_err(got, a) <= TOL_COORD
 
 
