@@ -212,10 +212,12 @@ int orbit_sc2p5d_fields(orbit_sc2p5d_t* c, int n, const double* x, const double*
  * nx, ny <= 128 and nz <= 256 (larger sizes return ORBIT_ERR_UNSUPPORTED).
  * dev_coords: device SoA, coordinate c (x, xp, y, yp, z, dE) at
  * dev_coords + c*stride, stride >= n; xp and yp are updated in place.
- * stream: a cudaStream_t (NULL = default stream); the call waits for it.
- * The first call on a device looks up the array's device address, so make
- * that first call before any stream capture.  Calls share the array:
- * calls that overlap on the GPU race. */
+ * stream: a cudaStream_t (NULL = default stream).  Every call copies the
+ * fresh calculator's state from host memory into the array and waits for
+ * the stream before it returns.  The first call on a device looks up the
+ * array's device address (once per device, under a lock), so make that
+ * first call before any stream capture.  Calls share the array: calls that
+ * overlap on the GPU race. */
 int orbit_sc2p5d_track_static(double* dev_coords, int n, int stride, int nx, int ny, int nz, double xy_ratio,
                               double length, const orbit_sync_t* sync, void* stream);
 
@@ -379,9 +381,20 @@ int orbit_denoiser_forward(orbit_denoiser_t* d, const float* dev_in, float* dev_
  * tensor cores (tcgen05, TF32 operands, FP32 accumulation) unless `on` is
  * 0; batches and training use the CUDA-core layers. */
 int orbit_denoiser_set_tensor_cores(orbit_denoiser_t* d, int on);
-/* Synchronises; *on = the setting, *err = 1 if a tensor-core layer gave up
- * a bounded wait since the last call (then reset), else 0. */
+/* Synchronises; *on = whether single-image forwards use the tensor cores
+ * now; *err = the error bits of the tensor-core layers since the last call
+ * (then reset): 1 = a bounded wait on an MMA gave up, 2 = the MMA had not
+ * completed after a second wait either and its tensor memory was released
+ * all the same.  After any error this network runs its single-image
+ * forwards on the CUDA-core layers; after bit 2 no network of the process
+ * uses the tensor cores again.  A learned closure whose network reported
+ * an error falls back to the plain deposit. */
 int orbit_denoiser_tensor_status(orbit_denoiser_t* d, int* on, int* err);
+/* The tensor-core layers' bounded waits: each gives up after `cycles` SM
+ * clock cycles (default 2e9, about one second).  withhold_mma != 0 (for
+ * testing the failure path only) issues no MMA, so every wait runs out
+ * with nothing in flight.  No counterpart in the reference. */
+int orbit_denoiser_set_wait_limit(orbit_denoiser_t* d, long long cycles, int withhold_mma);
 /* One Adam step (learning rate lr) on the mean squared error of nb pairs,
  * on `stream` (NULL: the denoiser's own stream; pass the stream that wrote
  * the inputs); *loss (if not NULL) receives the loss before the step

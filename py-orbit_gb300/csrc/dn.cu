@@ -186,15 +186,12 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Waits for phase `parity` of the barrier for at most kTcWaitCycles; false
-// (and the error flag set) when it did not complete.
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, int* err) {
+// Waits for phase `parity` of the barrier for at most `limit` clock cycles;
+// false when it did not complete.
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, long long limit) {
   long long t0 = clock64();
   while (!mbar_try_wait(bar, parity)) {
-    if (clock64() - t0 > kTcWaitCycles) {
-      atomicOr(err, 1);
-      return false;
-    }
+    if (clock64() - t0 > limit) return false;
   }
   return true;
 }
@@ -224,10 +221,24 @@ __device__ __forceinline__ void tc_load_a(const float* __restrict__ in, int cin,
   }
 }
 
+// The bounded waits of a tensor-core layer: `cycles` per wait; `withhold`
+// (test only) issues no MMA, so that the wait runs out with nothing in
+// flight and the failure path can be exercised.
+struct TcWait {
+  long long cycles;
+  int withhold;
+};
+
+// Error flag bits: 1 = a wait gave up; 2 = the MMA had still not completed
+// after a second wait of the same length, and its TMEM was released all the
+// same (the results and the state of that SM's tensor memory are then not
+// to be trusted: the network must not run on the tensor cores again in
+// this process).
 template <int N, bool SPLIT>
 __global__ void __launch_bounds__(128) k_conv3_tc(const float* __restrict__ in, int cin, int H, int W,
                                                   const float* __restrict__ wpk, const float* __restrict__ bias,
-                                                  float* __restrict__ out, float* __restrict__ part, int* err) {
+                                                  float* __restrict__ out, float* __restrict__ part, int* err,
+                                                  TcWait tw) {
   constexpr int BV = N * kTcKC / 4 / 128;  // float4 of the B stage per thread (1, 2 or 4)
   extern __shared__ unsigned char tc_raw[];
   __shared__ __align__(8) uint64_t s_bar;
@@ -273,7 +284,7 @@ __global__ void __launch_bounds__(128) k_conv3_tc(const float* __restrict__ in, 
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = s_tmem;
-  if (tid == 0) {
+  if (tid == 0 && !tw.withhold) {
 #pragma unroll
     for (int j = 0; j < kTcKC / 8; ++j) {
       const uint64_t ad = tc_desc(sA + 256u * j), bd = tc_desc(sB + 256u * j);
@@ -287,7 +298,14 @@ __global__ void __launch_bounds__(128) k_conv3_tc(const float* __restrict__ in, 
                  : "memory");
   }
   // a wait that gives up does so for the whole block
-  const bool ok = __syncthreads_and(mbar_wait_bounded(smem_u32(&s_bar), 0, err));
+  const bool ok = __syncthreads_and(mbar_wait_bounded(smem_u32(&s_bar), 0, tw.cycles));
+  if (!ok) {
+    if (tid == 0) atomicOr(err, 1);
+    // an MMA that was issued may still write the accumulators and arrive on
+    // the barrier: wait once more before the TMEM is released
+    if (!tw.withhold && !__syncthreads_and(mbar_wait_bounded(smem_u32(&s_bar), 0, tw.cycles)) && tid == 0)
+      atomicOr(err, 2);
+  }
   asm volatile("tcgen05.fence::after_thread_sync;");
   float acc[N];
 #pragma unroll
@@ -773,9 +791,14 @@ struct orbit_denoiser {
   float* d_wtc = nullptr;
   std::vector<size_t> tc_off;
   int* d_err = nullptr;
+  long long tc_wait_cycles = kTcWaitCycles;
+  int tc_withhold = 0;
+  bool tc_failed = false;  // a tensor-core layer reported a failed wait
 };
 
 namespace orbit {
+
+int* dn_error_flag(orbit_denoiser_t* d) { return d->d_err; }
 
 // activation indices
 enum {
@@ -866,11 +889,12 @@ static int tc_pack(orbit_denoiser_t* d, cudaStream_t st) {
 
 template <int N>
 static void launch_conv_tc(dim3 g, cudaStream_t st, bool split, const float* in, int cin, int h, int w,
-                           const float* wp, const float* bias, float* out, float* part, int nst, int* err) {
+                           const float* wp, const float* bias, float* out, float* part, int nst, int* err,
+                           TcWait tw) {
   if (split)
-    k_conv3_tc<N, true><<<g, 128, kTcSmem, st>>>(in, cin, h, w, wp, bias, out, part, err);
+    k_conv3_tc<N, true><<<g, 128, kTcSmem, st>>>(in, cin, h, w, wp, bias, out, part, err, tw);
   else
-    k_conv3_tc<N, false><<<g, 128, kTcSmem, st>>>(in, cin, h, w, wp, bias, out, part, err);
+    k_conv3_tc<N, false><<<g, 128, kTcSmem, st>>>(in, cin, h, w, wp, bias, out, part, err, tw);
 }
 
 // What a tensor-core layer's reduction also writes (see k_split_reduce_quad).
@@ -892,10 +916,11 @@ static int conv_fwd_tc(orbit_denoiser_t* d, const Step3& s, cudaStream_t st, con
   dim3 g(tiles, nst);
   float* o = d->act[s.out];
   float* part = d->d_scratch;
+  const TcWait tw = {d->tc_wait_cycles, d->tc_withhold};
   switch (cv.cout) {
-    case 16: launch_conv_tc<16>(g, st, split, d->act[s.in], cv.cin, h, w, wp, B, o, part, nst, d->d_err); break;
-    case 32: launch_conv_tc<32>(g, st, split, d->act[s.in], cv.cin, h, w, wp, B, o, part, nst, d->d_err); break;
-    case 64: launch_conv_tc<64>(g, st, split, d->act[s.in], cv.cin, h, w, wp, B, o, part, nst, d->d_err); break;
+    case 16: launch_conv_tc<16>(g, st, split, d->act[s.in], cv.cin, h, w, wp, B, o, part, nst, d->d_err, tw); break;
+    case 32: launch_conv_tc<32>(g, st, split, d->act[s.in], cv.cin, h, w, wp, B, o, part, nst, d->d_err, tw); break;
+    case 64: launch_conv_tc<64>(g, st, split, d->act[s.in], cv.cin, h, w, wp, B, o, part, nst, d->d_err, tw); break;
     default: return set_error(ORBIT_ERR_ARG, "denoiser: tensor-core layer width not supported");
   }
   ORBIT_LAUNCH_CHECK("denoiser tensor-core conv");
@@ -933,8 +958,14 @@ static int conv_fwd_tc(orbit_denoiser_t* d, const Step3& s, cudaStream_t st, con
 // infer: a single image goes through the tensor-core layers (when on);
 // training keeps the CUDA-core layers, whose activations the backward
 // pass reads and whose gradients are checked against the oracle.
+// Set when a tensor-core layer reported an MMA that had not completed after
+// two bounded waits (error bit 2): that SM's tensor memory may still have
+// been written after its release, so no network of this process uses the
+// tensor-core layers again.
+static bool g_tc_untrusted = false;
+
 static int forward(orbit_denoiser_t* d, int nb, cudaStream_t st, bool infer = false) {
-  const bool tc = infer && d->tc && nb == 1;
+  const bool tc = infer && d->tc && !d->tc_failed && !g_tc_untrusted && nb == 1;
   if (tc && d->tc_stale) {
     int rc = tc_pack(d, st);
     if (rc) return rc;
@@ -1341,11 +1372,22 @@ int orbit_denoiser_tensor_status(orbit_denoiser_t* d, int* on, int* err) {
   if (!d) return set_error(ORBIT_ERR_ARG, "orbit_denoiser_tensor_status: bad argument");
   ORBIT_CUDA(cudaStreamSynchronize(d->stream));
   ORBIT_CUDA(cudaDeviceSynchronize());
-  if (on) *on = d->tc ? 1 : 0;
+  if (on) *on = (d->tc && !d->tc_failed && !g_tc_untrusted) ? 1 : 0;
   if (err) {
     ORBIT_CUDA(cudaMemcpy(err, d->d_err, sizeof(int), cudaMemcpyDeviceToHost));
     ORBIT_CUDA(cudaMemset(d->d_err, 0, sizeof(int)));
+    // after a failed wait this network runs its single-image forwards on
+    // the CUDA-core layers; after an MMA that never completed no network does
+    if (*err) d->tc_failed = true;
+    if (*err & 2) g_tc_untrusted = true;
   }
+  return ORBIT_OK;
+}
+
+int orbit_denoiser_set_wait_limit(orbit_denoiser_t* d, long long cycles, int withhold_mma) {
+  if (!d || cycles <= 0) return set_error(ORBIT_ERR_ARG, "orbit_denoiser_set_wait_limit: bad argument");
+  d->tc_wait_cycles = cycles;
+  d->tc_withhold = withhold_mma != 0;
   return ORBIT_OK;
 }
 

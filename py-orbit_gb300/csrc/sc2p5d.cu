@@ -4,6 +4,7 @@
 // PoissonSolverFFT2D.cc:115-256, Grid2D.cc, Grid1D.cc).
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -802,8 +803,17 @@ __global__ void k_learn_in_f(ScState* st, const float* __restrict__ rho_f, float
 }
 
 // Sum of the network output clamped at zero (a density is not negative).
-__global__ void k_learn_sum(ScState* st, const float* __restrict__ out, int n) {
+// A network that reported a failed tensor-core wait (net_err != 0) produced
+// no valid output: the closure falls back to the plain deposit for good.
+__global__ void k_learn_sum(ScState* st, const float* __restrict__ out, int n, const int* __restrict__ net_err) {
   if (st->skip) return;
+  if (*net_err) {
+    if (blockIdx.x == 0 && threadIdx.x == 0 && !st->dn_fallback) {
+      st->dn_fallback = 1;
+      st->dn_trips += 1;
+    }
+    return;
+  }
   __shared__ double s_part[32];
   double s = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) s += fmaxf(out[i], 0.f);
@@ -950,16 +960,16 @@ __global__ void __launch_bounds__(768) kb_deposit(const DepJob* __restrict__ job
 // ---------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------
+// W_N^e = exp(-2 pi i e / N), e = 0..n-1, from long-double cos/sin, with the
+// quadrant points exact.
 template <typename T>
-static void* make_twiddles(int n, cudaError_t* err) {
-  typedef typename CT<T>::t C;
-  std::vector<C> h(n);
+static void fill_twiddles_host(int n, typename CT<T>::t* h) {
   for (int e = 0; e < n; ++e) {
     long double a = 2.0L * 3.141592653589793238462643383279502884L * (long double)e / (long double)n;
     h[e].x = (T)cosl(a);
     h[e].y = (T)(-sinl(a));
   }
-  if (n % 4 == 0) {  // exact quadrant points
+  if (n % 4 == 0) {
     h[0].x = 1; h[0].y = 0;
     h[n / 4].x = 0; h[n / 4].y = -1;
     h[n / 2].x = -1; h[n / 2].y = 0;
@@ -967,6 +977,13 @@ static void* make_twiddles(int n, cudaError_t* err) {
   } else if (n % 2 == 0) {
     h[n / 2].x = -1; h[n / 2].y = 0;
   }
+}
+
+template <typename T>
+static void* make_twiddles(int n, cudaError_t* err) {
+  typedef typename CT<T>::t C;
+  std::vector<C> h(n);
+  fill_twiddles_host<T>(n, h.data());
   void* d = nullptr;
   *err = cudaMalloc(&d, sizeof(C) * n);
   if (*err == cudaSuccess) *err = cudaMemcpy(d, h.data(), sizeof(C) * n, cudaMemcpyHostToDevice);
@@ -1477,7 +1494,7 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
       ORBIT_PE(s);
       if (rc) return rc;
       ORBIT_PB("learn_out", s);
-      k_learn_sum<<<gb, 256, 0, s>>>(c->d_st, c->d_dn_out, ng);
+      k_learn_sum<<<gb, 256, 0, s>>>(c->d_st, c->d_dn_out, ng, dn_error_flag(c->dn));
       if (plain)
         k_learn_out<<<gb, 256, 0, s>>>(c->d_st, c->d_dn_out, c->d_rho_q, ng, dn_scale);
       else
@@ -1948,12 +1965,17 @@ static constexpr size_t kStaticScratchBytes =
 // (about 2.1 MB).  Shared by all calls: calls that overlap on the GPU race.
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
 
-static unsigned char* g_static_ptr[256];  // device address per device ordinal, set up once
+// Device address of the array per device ordinal, looked up once per device
+// (with that device current) under a lock, so that host threads calling
+// concurrently do not race on the table.
+static unsigned char* g_static_ptr[256];
+static std::mutex g_static_lock;
 
 static int static_scratch_ptr(unsigned char** out) {
   int dev = 0;
   ORBIT_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 256) return set_error(ORBIT_ERR_UNSUPPORTED, "orbit_sc2p5d_track_static: device ordinal");
+  std::lock_guard<std::mutex> guard(g_static_lock);
   if (!g_static_ptr[dev]) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
@@ -1962,23 +1984,6 @@ static int static_scratch_ptr(unsigned char** out) {
   }
   *out = g_static_ptr[dev];
   return ORBIT_OK;
-}
-
-template <typename T>
-static void fill_twiddles_host(int n, typename CT<T>::t* h) {
-  for (int e = 0; e < n; ++e) {
-    long double a = 2.0L * 3.141592653589793238462643383279502884L * (long double)e / (long double)n;
-    h[e].x = (T)cosl(a);
-    h[e].y = (T)(-sinl(a));
-  }
-  if (n % 4 == 0) {
-    h[0].x = 1; h[0].y = 0;
-    h[n / 4].x = 0; h[n / 4].y = -1;
-    h[n / 2].x = -1; h[n / 2].y = 0;
-    h[3 * n / 4].x = 0; h[3 * n / 4].y = 1;
-  } else if (n % 2 == 0) {
-    h[n / 2].x = -1; h[n / 2].y = 0;
-  }
 }
 
 }  // namespace orbit

@@ -92,6 +92,11 @@ struct FftPlan {
 struct orbit_boundary;
 struct orbit_denoiser;
 
+namespace orbit {
+// The denoiser's device error flag (tensor-core waits that gave up).
+int* dn_error_flag(orbit_denoiser* d);
+}  // namespace orbit
+
 struct orbit_sc2p5d {
   int nx = 0, ny = 0, nz = 0, form = 0;
   int nx2 = 0, ny2 = 0, H = 0;   // doubled grid, H = ny2/2 + 1

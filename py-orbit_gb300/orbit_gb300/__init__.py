@@ -346,11 +346,19 @@ class DeviceDenoiser:
         call("orbit_denoiser_set_tensor_cores", self.h, int(bool(on)))
 
     def tensor_errors(self) -> int:
-        """1 if a tensor-core layer gave up a bounded wait since the last
-        call (the flag is then cleared), else 0."""
+        """Error bits of the tensor-core layers since the last call (then
+        cleared): 1 = a bounded wait gave up, 2 = an MMA had not completed
+        after a second wait either.  After any error this network's
+        single-image forwards run on the CUDA-core layers."""
         err = ctypes.c_int()
         call("orbit_denoiser_tensor_status", self.h, None, ctypes.byref(err))
         return err.value
+
+    def set_wait_limit(self, cycles: int, withhold_mma: bool = False):
+        """Clock-cycle limit of each bounded wait of the tensor-core layers
+        (default 2e9); withhold_mma issues no MMA, so the waits run out with
+        nothing in flight (for testing the failure path)."""
+        call("orbit_denoiser_set_wait_limit", self.h, ctypes.c_longlong(int(cycles)), int(bool(withhold_mma)))
 
     def train_step(self, dev_in: int, dev_target: int, nb: int, lr: float, want_loss: bool = True, stream: int = 0):
         loss = ctypes.c_float()

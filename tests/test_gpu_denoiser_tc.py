@@ -89,3 +89,44 @@ def test_tensor_core_gain_on_held_out_beams():
     assert net.tensor_errors() == 0
     assert gains[True] > 20
     assert abs(gains[True] / gains[False] - 1) < 0.02
+
+
+def test_bounded_wait_runs_out_and_the_closure_falls_back():
+    """The failure path of the tensor-core layers, without a GPU fault: the
+    network issues no MMA (test hook), so every bounded wait runs out after
+    its limit (2e6 cycles, about a millisecond) with nothing in flight.  The
+    layers set the error flag, release their tensor memory and return; the
+    closure reads the flag and falls back to the plain deposit (the kick
+    then equals the calculator's without a closure, bit for bit); the
+    network reports the error and runs its single-image forwards on the
+    CUDA-core layers from then on."""
+    import contextlib
+    import io
+    from orbit_gb300 import denoiser as DN
+    from orbit_gb300 import workloads as W
+    from spacecharge import SpaceChargeCalc2p5D
+    net = DN.default_network()
+    assert net.tensor_cores
+    net.set_wait_limit(2_000_000, withhold_mma=True)
+    soa = W.c2_coords(100_000, seed=9)
+    b1 = W.make_bunch(soa, 1e9)
+    b2 = W.make_bunch(soa, 1e9)
+    calc = SpaceChargeCalc2p5D(128, 128, 64)
+    calc.setDenoiser(net, 10, 1e-3)
+    calc.trackBunch(b1, 0.5)
+    st = calc.getDenoiserState()
+    assert st["fallback"] == 1 and st["trips"] == 1, st
+    plain = SpaceChargeCalc2p5D(128, 128, 64)
+    plain.trackBunch(b2, 0.5)
+    assert np.array_equal(calc.getRhoGrid().getArray(), plain.getRhoGrid().getArray())
+    assert np.array_equal(b1.getCoordinates(), b2.getCoordinates())
+    assert net.tensor_errors() == 1
+    assert not net.tensor_cores
+    # a fresh network is unaffected (nothing was left in flight)
+    net2 = DN.default_network()
+    assert net2.tensor_cores
+    # and the calculator keeps tracking with the plain deposit
+    with contextlib.redirect_stdout(io.StringIO()):
+        lat = W.fodo_lattice(calc, cells=2)
+    lat.trackBunch(b1)
+    assert calc.getDenoiserState()["fallback"] == 1

@@ -65,6 +65,28 @@ def test_static_kick_matches_allocating_entry_points_twice():
         assert coord_err(got, ref) <= TOL_FIELD
 
 
+def test_static_kick_allocates_no_device_memory():
+    """The entry point's promise: after a first call (which looks up the
+    array's address), a call leaves the device's free memory unchanged
+    (cudaMemGetInfo before and after, nothing else running in between)."""
+    import torch
+    from orbit_gb300 import DeviceBunch
+    soa = _inputs(50_000, seed=3)
+    grid = (128, 128, 64)
+    sync = _sync(1e9)
+    dev = DeviceBunch()
+    dev.upload(soa)
+    dev.set_sync(sync)
+    assert _static_call(dev, soa.shape[1], grid, 0.5, sync) == 0
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        assert _static_call(dev, soa.shape[1], grid, 0.5, sync) == 0
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+
+
 def test_static_kick_rejects_grids_above_its_scratch():
     from orbit_gb300 import DeviceBunch, _native
     soa = _inputs(1000)
