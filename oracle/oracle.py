@@ -359,6 +359,22 @@ def ref():
         L.ref_tune_free.argtypes = [_vp]
         L.ref_tune_assign.argtypes = [_vp, _dp]
         L.ref_tune_analyze.argtypes = [_vp, _vp, _dp]
+        _cp = ctypes.c_char_p
+        L.ref_bunch_dump.argtypes = [_vp, _cp]
+        L.ref_bunch_read.argtypes = [_vp, _cp]
+        L.ref_bunch_add_attr.argtypes = [_vp, _cp, ctypes.c_int]
+        L.ref_bunch_attr_size.restype = ctypes.c_int
+        L.ref_bunch_attr_size.argtypes = [_vp, _cp]
+        L.ref_bunch_attr_set.argtypes = [_vp, _cp, ctypes.c_int, ctypes.c_int, ctypes.c_double]
+        L.ref_bunch_attr_get.restype = ctypes.c_double
+        L.ref_bunch_attr_get.argtypes = [_vp, _cp, ctypes.c_int, ctypes.c_int]
+        L.ref_bunch_set_int_attr.argtypes = [_vp, _cp, ctypes.c_int]
+        L.ref_bunch_set_double_attr.argtypes = [_vp, _cp, ctypes.c_double]
+        L.ref_bunch_get_int_attr.restype = ctypes.c_int
+        L.ref_bunch_get_int_attr.argtypes = [_vp, _cp]
+        L.ref_bunch_get_double_attr.restype = ctypes.c_double
+        L.ref_bunch_get_double_attr.argtypes = [_vp, _cp]
+        L.ref_bunch_set_time.argtypes = [_vp, ctypes.c_double]
         _ref = L
     return _ref
 
@@ -381,9 +397,42 @@ class RefBunch:
             self.h = None
 
     def coords(self) -> np.ndarray:
+        self.n = ref().ref_bunch_size(self.h)
         out = np.zeros((6, self.n))
         ref().ref_bunch_get(self.h, _P(out))
         return out
+
+    # text I/O (Bunch::print / readBunch) and attributes
+    def dump(self, path: str):
+        ref().ref_bunch_dump(self.h, path.encode())
+
+    def read(self, path: str):
+        ref().ref_bunch_read(self.h, path.encode())
+        self.n = ref().ref_bunch_size(self.h)
+
+    def add_attr(self, name: str, size: int = 0):
+        ref().ref_bunch_add_attr(self.h, name.encode(), int(size))
+
+    def attr_size(self, name: str) -> int:
+        return ref().ref_bunch_attr_size(self.h, name.encode())
+
+    def attr(self, name: str, i: int, j: int, value=None) -> float:
+        if value is not None:
+            ref().ref_bunch_attr_set(self.h, name.encode(), int(i), int(j), float(value))
+        return ref().ref_bunch_attr_get(self.h, name.encode(), int(i), int(j))
+
+    def bunch_attr_int(self, name: str, value=None) -> int:
+        if value is not None:
+            ref().ref_bunch_set_int_attr(self.h, name.encode(), int(value))
+        return ref().ref_bunch_get_int_attr(self.h, name.encode())
+
+    def bunch_attr_double(self, name: str, value=None) -> float:
+        if value is not None:
+            ref().ref_bunch_set_double_attr(self.h, name.encode(), float(value))
+        return ref().ref_bunch_get_double_attr(self.h, name.encode())
+
+    def set_time(self, t: float):
+        ref().ref_bunch_set_time(self.h, float(t))
 
     def kinematics(self):
         k = np.zeros(7)

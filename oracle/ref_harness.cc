@@ -17,6 +17,7 @@
 #include "BunchTwissAnalysis.hh"
 #include "BunchTuneAnalysis.hh"
 #include "ParticleAttributes.hh"
+#include <map>
 #include <string>
 #include "Grid1D.hh"
 #include "Grid2D.hh"
@@ -89,6 +90,42 @@ void ref_bunch_set(void* b, const double* soa) {
   for (int i = 0; i < n; ++i)
     for (int c = 0; c < 6; ++c) a[i][c] = soa[c * n + i];
 }
+
+// Bunch text I/O as the Python wrapper drives it (src/orbit/wrap_bunch.cc:
+// dumpBunch -> Bunch::print(fileName), readBunch -> initBunchAttributes,
+// readParticleAttributes, readBunchCoords), and the attribute calls a
+// golden bunch file needs.
+void ref_bunch_dump(void* b, const char* fn) { ((Bunch*)b)->print(fn); }
+void ref_bunch_read(void* b, const char* fn) {
+  Bunch* bb = (Bunch*)b;
+  bb->initBunchAttributes(fn);
+  bb->readParticleAttributes(fn);
+  bb->readBunchCoords(fn);
+}
+void ref_bunch_add_attr(void* b, const char* name, int size) {
+  std::map<std::string, double> d;
+  if (size > 0) d["size"] = size;
+  ((Bunch*)b)->addParticleAttributes(std::string(name), d);
+}
+int ref_bunch_attr_size(void* b, const char* name) {
+  ParticleAttributes* a = ((Bunch*)b)->getParticleAttributes(std::string(name));
+  return a ? a->getAttSize() : -1;
+}
+void ref_bunch_attr_set(void* b, const char* name, int i, int j, double v) {
+  ((Bunch*)b)->getParticleAttributes(std::string(name))->attValue(i, j) = v;
+}
+double ref_bunch_attr_get(void* b, const char* name, int i, int j) {
+  return ((Bunch*)b)->getParticleAttributes(std::string(name))->attValue(i, j);
+}
+void ref_bunch_set_int_attr(void* b, const char* name, int v) { ((Bunch*)b)->setBunchAttribute(std::string(name), v); }
+void ref_bunch_set_double_attr(void* b, const char* name, double v) {
+  ((Bunch*)b)->setBunchAttribute(std::string(name), v);
+}
+int ref_bunch_get_int_attr(void* b, const char* name) { return ((Bunch*)b)->getBunchAttributeInt(std::string(name)); }
+double ref_bunch_get_double_attr(void* b, const char* name) {
+  return ((Bunch*)b)->getBunchAttributeDouble(std::string(name));
+}
+void ref_bunch_set_time(void* b, double t) { ((Bunch*)b)->getSyncPart()->setTime(t); }
 
 // Same constructor choice as SpaceChargeCalc2p5D_init
 // (src/spacecharge/wrap_spacechargecalc2p5d.cc:38-52).

@@ -37,6 +37,7 @@ class SyncPart:
         self._time = 0.0
         self._xyz = [0.0, 0.0, 0.0]
         self._pxyz = [0.0, 0.0, 0.0]
+        self._nx = [1.0, 0.0, 0.0]  # x-axis ort (SyncPart.cc: normal vector, printed and read only)
         self._p_abs = 0.0
         self._energy = 0.0
         self._beta = 0.0
@@ -492,32 +493,56 @@ class Bunch:
         other._host_modified()
 
     # ----------------------------------------------------- I/O
+    # Column descriptions the reference's attribute classes print
+    # (attrDescr in src/orbit/ParticlesAttributes/*.cc), by factory name
+    # (ParticleAttributesFactory.cc).
+    _ATTR_DESCR = {"empty": "no attributes", "macrosize": "macro_size", "ParticleIdNumber": "Particle_Id_Number",
+                   "LostParticleAttributes": "Pos (m)", PHASE_ATTR: "PhaseVars", "Amplitudes": "Ampls",
+                   "Populations": "Pops", "pq_coords": "Coords", "part_time": "time", "Evolution": "Evol",
+                   "TurnNumber": "TurnNumber"}
+
+    @staticmethod
+    def _g(v, prec):
+        """A double as a C++ ostream prints it with setprecision(prec)."""
+        return "%.*g" % (prec, v)
+
     def dumpBunch(self, fileName=None):
-        """Text dump in the layout of Bunch::print (Bunch.cc:894-980)."""
+        """Text dump in the layout of Bunch::print (Bunch.cc:894-980) and
+        SyncPart::print (SyncPart.cc:465-536): attribute controller names
+        and their parameter dictionaries (keys in std::map order), bunch
+        attributes by name, the synchronous particle at 14 digits, then one
+        line per live particle at 8 digits."""
         self._ensure_host()
-        lines = ["% PARTICLE_ATTRIBUTES_CONTROLLERS_NAMES " + " ".join(self._part_attr.keys()) + " "]
-        for name, v in self._attr_int.items():
-            lines.append("%% BUNCH_ATTRIBUTE_INT %s   %d " % (name, v))
-        for name, v in self._attr_double.items():
-            lines.append("%% BUNCH_ATTRIBUTE_DOUBLE %s   %.8g " % (name, v))
+        g = self._g
+        names = list(self._part_attr.keys())
+        lines = ["% PARTICLE_ATTRIBUTES_CONTROLLERS_NAMES " + "".join(n + " " for n in names)]
+        for n in names:
+            d = dict(self._part_attr_dict.get(n) or {})
+            d["size"] = float(self._part_attr[n].shape[1])
+            lines.append("% PARTICLE_ATTRIBUTES_CONTROLLER_DICT " + n + " " +
+                         "".join("%s %s " % (k, g(d[k], 6)) for k in sorted(d)))
+        for name in sorted(self._attr_int):
+            lines.append("%% BUNCH_ATTRIBUTE_INT %s   %d " % (name, self._attr_int[name]))
+        for name in sorted(self._attr_double):
+            lines.append("%% BUNCH_ATTRIBUTE_DOUBLE %s   %s " % (name, g(self._attr_double[name], 6)))
         s = self._sync
-        lines.append("% SYNC_PART_COORDS " + " ".join("%.8g" % v for v in s._xyz) + "  x, y, z positions in [m]")
-        lines.append("% SYNC_PART_MOMENTUM " + " ".join("%.8g" % v for v in s._pxyz) + "  px, py, pz momentum component in GeV/c")
-        lines.append("% SYNC_PART_X_AXIS 1 0 0  nxx, nxy, nxz - x-axis ort coordinates")
-        lines.append("% info only: energy of the synchronous particle [GeV] = %.8g" % s.kinEnergy())
-        lines.append("% info only: momentum of the synchronous particle [GeV/c] = %.8g" % s.momentum())
-        lines.append("% info only: beta of the synchronous particle = %.8g" % s.beta())
-        lines.append("% info only: gamma of the synchronous particle = %.8g" % s.gamma())
-        lines.append("% SYNC_PART_TIME %.8g  time in [sec]" % s.time())
-        lines.append("% x[m] px[rad] y[m] py[rad] z[m]  (pz or dE [GeV]) ")
-        body = []
-        attrs = [self._part_attr[k] for k in self._part_attr]
-        for i in range(self._n):
-            if self._flag[i] > 0:
-                vals = ["%.8g" % v for v in self._host[:, i]]
-                for a in attrs:
-                    vals += ["%.8g" % v for v in a[i]]
-                body.append(" ".join(vals) + " ")
+        t = s.time()
+        lines += [
+            "%%  SYNC_PART_COORDS %s %s %s  x, y, z positions in [m]" % tuple(g(v, 14) for v in s._xyz),
+            "%%  SYNC_PART_MOMENTUM %s %s %s  px, py, pz momentum component in GeV/c" % tuple(g(v, 14) for v in s._pxyz),
+            "%%  SYNC_PART_X_AXIS %s %s %s  nxx, nxy, pxz - x-axis ort coordinates" % tuple(g(v, 14) for v in s._nx),
+            "%%  info only: energy of the synchronous particle [GeV] = %s " % g(s.kinEnergy(), 14),
+            "%%  info only: momentum of the synchronous particle [GeV/c] = %s " % g(s.momentum(), 14),
+            "%%  info only: beta=v/c of the synchronous particle = %s " % g(s.beta(), 14),
+            "%%  info only: gamma=1/sqrt(1-(v/c)**2) of the synchronous particle = %s " % g(s.gamma(), 14),
+            "%%  SYNC_PART_TIME %s  time in [sec]" % g(t, 14),
+            "% x[m] px[rad] y[m] py[rad] z[m]  (pz or dE [GeV]) " +
+            "".join(self._ATTR_DESCR.get(n, "no attributes") + " " for n in names),
+        ]
+        live = np.nonzero(self._flag[: self._n] > 0)[0]
+        cols = [self._host[:, : self._n]] + [self._part_attr[n][: self._n].T for n in names]
+        table = np.vstack(cols)[:, live].T
+        body = ["".join("%.8g " % v for v in row) for row in table]
         text = "\n".join(lines + body) + "\n"
         if fileName is None:
             print(text, end="")
@@ -526,41 +551,70 @@ class Bunch:
                 f.write(text)
 
     def readBunch(self, fileName, nParts=-1):
-        """Reads a file written by dumpBunch (Bunch.cc:1116-1300)."""
-        rows = []
-        attr_names = []
+        """Reads a bunch text file as the reference's readBunch does
+        (wrap_bunch.cc:1087-1119): bunch attributes and the synchronous
+        particle from the header (Bunch::initBunchAttributes,
+        SyncPart.cc:360-460), the particle attribute controllers with their
+        parameter dictionaries (Bunch.cc:1287-1420: every existing attribute
+        is removed first), then the particle lines appended to the bunch
+        (Bunch.cc:1116-1264: 6 or 6 + attribute-width numbers per line, at
+        most nParts particles).  Returns the bunch size."""
+        names, dicts = [], {}
+        header = []
         with open(fileName) as f:
-            for line in f:
-                line = line.strip()
-                if not line:
-                    continue
-                if line.startswith("%"):
-                    tok = line.split()
-                    if len(tok) >= 2 and tok[1] == "PARTICLE_ATTRIBUTES_CONTROLLERS_NAMES":
-                        attr_names = tok[2:]
-                    elif len(tok) >= 4 and tok[1] == "BUNCH_ATTRIBUTE_DOUBLE":
-                        self.bunchAttrDouble(tok[2], float(tok[3]))
-                    elif len(tok) >= 4 and tok[1] == "BUNCH_ATTRIBUTE_INT":
-                        self.bunchAttrInt(tok[2], int(tok[3]))
-                    elif len(tok) >= 5 and tok[1] == "SYNC_PART_MOMENTUM":
-                        self._sync.pVector([float(t) for t in tok[2:5]])
-                    elif len(tok) >= 5 and tok[1] == "SYNC_PART_COORDS":
-                        self._sync.rVector([float(t) for t in tok[2:5]])
-                    elif len(tok) >= 3 and tok[1] == "SYNC_PART_TIME":
-                        self._sync.time(float(tok[2]))
-                    continue
-                rows.append([float(t) for t in line.split()])
-                if 0 < nParts <= len(rows):
-                    break
-        for name in attr_names:
-            self.addPartAttr(name)
-        arr = np.array(rows, dtype=np.float64).reshape(-1, max(6, len(rows[0]) if rows else 6))
-        self.setCoordinates(arr[:, :6].T)
-        col = 6
-        for name in attr_names:
-            k = self._part_attr[name].shape[1]
-            self._part_attr[name][: self._n] = arr[:, col:col + k]
-            col += k
+            lines = f.read().splitlines()
+        k = 0
+        while k < len(lines) and lines[k].startswith("%"):
+            tok = lines[k].split()
+            header.append(tok)
+            if len(tok) > 2 and tok[1] == "PARTICLE_ATTRIBUTES_CONTROLLERS_NAMES":
+                names = tok[2:]
+            elif len(tok) > 2 and tok[1] == "PARTICLE_ATTRIBUTES_CONTROLLER_DICT":
+                dicts[tok[2]] = {tok[i]: float(tok[i + 1]) for i in range(3, len(tok) - 1, 2)}
+            k += 1
+        for tok in header:
+            if len(tok) > 3 and tok[1] == "BUNCH_ATTRIBUTE_INT":
+                self.bunchAttrInt(tok[2], int(tok[3]))
+            elif len(tok) > 3 and tok[1] == "BUNCH_ATTRIBUTE_DOUBLE":
+                self.bunchAttrDouble(tok[2], float(tok[3]))
+            elif len(tok) > 4 and tok[1] == "SYNC_PART_COORDS":
+                self._sync.rVector([float(t) for t in tok[2:5]])
+            elif len(tok) > 4 and tok[1] == "SYNC_PART_MOMENTUM":
+                self._sync.pVector([float(t) for t in tok[2:5]])
+            elif len(tok) > 4 and tok[1] == "SYNC_PART_X_AXIS":
+                self._sync._nx = [float(t) for t in tok[2:5]]
+            elif len(tok) > 2 and tok[1] == "SYNC_PART_TIME":
+                self._sync.time(float(tok[2]))
+        self.removeAllPartAttr()
+        for n in names:
+            self.addPartAttr(n, dicts.get(n))
+        width = 6 + sum(self._part_attr[n].shape[1] for n in names)
+        rows = []
+        for ln in lines[k:]:
+            tok = ln.split()
+            if not tok or tok[0].startswith("%"):
+                continue
+            if len(tok) != width and len(tok) != 6:
+                raise ValueError("readBunch: %s: a particle line has %d numbers, expected 6 or %d"
+                                 % (fileName, len(tok), width))
+            rows.append([float(t) for t in tok] + [0.0] * (width - len(tok)))
+            if 0 <= nParts <= len(rows):
+                break
+        self._ensure_host()
+        base = self._n
+        m = len(rows)
+        self._grow(base + m)
+        if m:
+            arr = np.array(rows, dtype=np.float64)
+            self._host[:, base:base + m] = arr[:, :6].T
+            self._flag[base:base + m] = 1
+            col = 6
+            for n in names:
+                w = self._part_attr[n].shape[1]
+                self._part_attr[n][base:base + m] = arr[:, col:col + w]
+                col += w
+        self._n = base + m
+        self._host_modified()
         return self._n
 
 

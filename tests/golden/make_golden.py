@@ -184,7 +184,40 @@ def diag_case(name, soa, twiss, steps, ek=1.0, msize=1e9):
     print("wrote", name)
 
 
+def bunch_io_case():
+    """Bunch::print of a bunch with particle attributes (macrosize, the
+    particle id and a 3-wide "Amplitudes" set, whose size goes into its
+    PARTICLE_ATTRIBUTES_CONTROLLER_DICT line), bunch attributes and a sync
+    particle time: the reference's own text file, plus its coordinates and
+    attributes as the reference holds them."""
+    soa = gaussian(40, 151)
+    b = O.RefBunch(soa, 1.3, 2.5e9)
+    b.add_attr("macrosize")
+    b.add_attr("ParticleIdNumber")
+    b.add_attr("Amplitudes", 3)
+    for i in range(soa.shape[1]):
+        b.attr("macrosize", i, 0, 1e9 * (1.0 + 0.01 * i))
+        b.attr("ParticleIdNumber", i, 0, 1000 + i)
+        for j in range(3):
+            b.attr("Amplitudes", i, j, 0.1 * j - 0.003 * i)
+    b.bunch_attr_int("TurnNumber", 7)
+    b.bunch_attr_double("beam_current", 0.0123456789)
+    b.set_time(1.234567890123e-6)
+    path = os.path.join(HERE, "bunch_dump_ref.txt")
+    b.dump(path)
+    # the reference reading its own file into a new bunch and writing it
+    # again (the mass comes back at the 6 digits the file holds, which moves
+    # the kinematics lines)
+    r = O.RefBunch(np.zeros((6, 0)), 1.0, 1.0)
+    r.read(path)
+    r.dump(os.path.join(HERE, "bunch_dump_ref_reread.txt"))
+    print("wrote bunch_dump_ref.txt, bunch_dump_ref_reread.txt")
+
+
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "bunch_io":
+        bunch_io_case()
+        return
     if not O.ref_available():
         if not O.build_reference():
             raise SystemExit("the compiled reference is not available")
@@ -246,6 +279,8 @@ def main():
     # 9) BunchTwissAnalysis::computeBunchMoments / getBunchMoment on the same
     # bunch (orders 2-4, with and without the dispersion and emittance flags)
     moments_case("diag_moments", d)
+    # 10) the bunch text file (Bunch::print) with attributes
+    bunch_io_case()
 
 
 def moments_case(name, soa, ek=1.0, msize=1e9):
