@@ -3,6 +3,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "softf64.cuh"
 #include "sc2p5d.cuh"
 
 namespace orbit {
@@ -729,9 +730,9 @@ __device__ __forceinline__ bool kick_fixed(const KickFix& k, const long long* __
     gx += __mul64hi(dwx[i] << 3, s);  // Q(sphi-5)
     gy += __mul64hi(wx[i] << 4, t);   // Q(sphi-5)
   }
-  double lf = (double)lv * k.lfs;  // -lambda(z) * factor
-  xp = fma((double)gx, k.gxs * lf, xp);
-  yp = fma((double)gy, k.gys * lf, yp);
+  const double lf = dmul<ORBIT_SOFT_MUL>((double)lv, k.lfs);  // -lambda(z) * factor
+  xp = fma((double)gx, dmul<ORBIT_SOFT_MUL>(k.gxs, lf), xp);
+  yp = fma((double)gy, dmul<ORBIT_SOFT_MUL>(k.gys, lf), yp);
   return true;
 }
 

@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(256) k_apply_one(double* __restrict__ cx, doub
     Part p;
     p.x = cx[i]; p.xp = cxp[i]; p.y = cy[i]; p.yp = cyp[i]; p.z = cz[i]; p.dE = cdE[i];
     p.knl_ok = false;
-    apply_ops(p, &op, 0, 1, m);
+    apply_ops<ORBIT_SOFT_MUL>(p, &op, 0, 1, m);
     cx[i] = p.x; cxp[i] = p.xp; cy[i] = p.y; cyp[i] = p.yp; cz[i] = p.z; cdE[i] = p.dE;
   }
 }

@@ -11,6 +11,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "softf64.cuh"
 
 namespace orbit {
 
@@ -31,24 +32,33 @@ struct Part {
   bool knl_ok;
 };
 
+// Every operation of the maps below is written out (fma, dmul<S>, __dadd_rn,
+// __dsub_rn), so that no kernel contracts them differently from another and
+// the choice of S changes no bit of the result: S = 1 routes the maps'
+// multiplies to the integer pipes (sf::mul, the same correctly rounded
+// product), which frees the FP64 pipe that bounds the fused pass on GB300.
+template <int S>
 __device__ __forceinline__ void ensure_knl(Part& p, const MapCtx& m) {
   if (!p.knl_ok) {
-    p.dp_p = p.dE * m.dp_p_coeff;
-    p.knl = __drcp_rn(1.0 + p.dp_p);
+    p.dp_p = dmul<S>(p.dE, m.dp_p_coeff);
+    p.knl = __drcp_rn(__dadd_rn(1.0, p.dp_p));
     p.knl_ok = true;
   }
 }
 
 // drifti body (teapotbase.cc:132-139)
+template <int S>
 __device__ __forceinline__ void drift_body(Part& p, const MapCtx& m, double L) {
-  ensure_knl(p, m);
-  double dp_p = p.dp_p, knl = p.knl;
-  double kl = knl * L;
-  p.x += kl * p.xp;
-  p.y += kl * p.yp;
-  double phifac = (p.xp * p.xp + p.yp * p.yp + dp_p * dp_p * m.gamma2i) * 0.5;
-  phifac = (phifac * knl - dp_p * m.gamma2i) * knl;
-  p.z -= L * phifac;
+  ensure_knl<S>(p, m);
+  const double dp_p = p.dp_p, knl = p.knl;
+  const double kl = dmul<S>(knl, L);
+  p.x = fma(kl, p.xp, p.x);
+  p.y = fma(kl, p.yp, p.y);
+  // phifac = (xp^2 + yp^2 + dp_p^2 / gamma^2) / 2
+  const double d2g = dmul<S>(dmul<S>(dp_p, dp_p), m.gamma2i);
+  double phifac = dhalf<S>(fma(p.xp, p.xp, fma(p.yp, p.yp, d2g)));
+  phifac = dmul<S>(fma(phifac, knl, -dmul<S>(dp_p, m.gamma2i)), knl);
+  p.z = fma(-L, phifac, p.z);
 }
 
 // multpfringeIN/OUT (teapotbase.cc:395-486, 508-599), with l = pole + 1,
@@ -63,37 +73,37 @@ __device__ __forceinline__ void drift_body(Part& p, const MapCtx& m, double L) {
 //   dxfycx = (l+1)(l-2) A y - (l+1)(l+2) B x,
 //   fxcx = l C x + (l+2) D y,  fycx = l C y - (l+2) D x,
 // and detM = 1 - e with e = u^2 + M12 M21 (u = dxfxcx KNL), whose inverse
-// is a short series for small e.  46 FP64 instructions instead of ~110 and
-// two divisions; the results differ from the reference's by roundings.  Every
-// sum is an explicit FMA, so every kernel that inlines it rounds alike.
+// is a short series for small e.  46 FP64 operations instead of ~110 and
+// two divisions; the results differ from the reference's by roundings.
 // c = {kt_re, kt_im, l, l+2, l(l+1), (l+1)(l+2), (l+1)(l-2)}, i0 = pole.
+template <int S>
 __device__ __forceinline__ void multpfringe_body(Part& p, const MapCtx& m, const DevOp& o) {
-  ensure_knl(p, m);
+  ensure_knl<S>(p, m);
   const double x = p.x, y = p.y, px = p.xp, py = p.yp, KNL = p.knl;
   double zr = 1.0, zi = 0.0;  // z^(l-1)
   if (o.i0 > 0) {
     zr = x;
     zi = y;
     for (int q = 1; q < o.i0; ++q) {
-      double t = fma(zr, x, -(zi * y));
-      zi = fma(zr, y, zi * x);
+      const double t = fma(zr, x, -dmul<S>(zi, y));
+      zi = fma(zr, y, dmul<S>(zi, x));
       zr = t;
     }
   }
   const double ktr = o.c[0], kti = o.c[1];
-  const double A = fma(ktr, zr, -(kti * zi)), B = fma(ktr, zi, kti * zr);
-  const double C = fma(A, x, -(B * y)), D = fma(A, y, B * x);
-  const double lC = o.c[2] * C, lp2D = o.c[3] * D;
-  const double fx = fma(lC, x, lp2D * y);
-  const double fy = fma(lC, y, -(lp2D * x));
-  const double dxfx = o.c[4] * fma(A, x, B * y);
-  const double dyfx = fma(o.c[5] * A, y, -((o.c[6] * B) * x));
-  const double dxfy = fma(o.c[6] * A, y, -((o.c[5] * B) * x));
+  const double A = fma(ktr, zr, -dmul<S>(kti, zi)), B = fma(ktr, zi, dmul<S>(kti, zr));
+  const double C = fma(A, x, -dmul<S>(B, y)), D = fma(A, y, dmul<S>(B, x));
+  const double lC = dmul<S>(o.c[2], C), lp2D = dmul<S>(o.c[3], D);
+  const double fx = fma(lC, x, dmul<S>(lp2D, y));
+  const double fy = fma(lC, y, -dmul<S>(lp2D, x));
+  const double dxfx = dmul<S>(o.c[4], fma(A, x, dmul<S>(B, y)));
+  const double dyfx = fma(dmul<S>(o.c[5], A), y, -dmul<S>(dmul<S>(o.c[6], B), x));
+  const double dxfy = fma(dmul<S>(o.c[6], A), y, -dmul<S>(dmul<S>(o.c[5], B), x));
   p.x = fma(-fx, KNL, x);
   p.y = fma(-fy, KNL, y);
-  const double u = dxfx * KNL;  // M11 = 1 - u, M22 = 1 + u
-  const double M12 = -(dxfy * KNL), M21 = -(dyfx * KNL);
-  const double e = fma(u, u, M12 * M21);  // detM = 1 - e
+  const double u = dmul<S>(dxfx, KNL);  // M11 = 1 - u, M22 = 1 + u
+  const double M12 = -dmul<S>(dxfy, KNL), M21 = -dmul<S>(dyfx, KNL);
+  const double e = fma(u, u, dmul<S>(M12, M21));  // detM = 1 - e
   const double nxp = fma(-M12, py, fma(u, px, px));   // M22 px - M12 py
   const double nyp = fma(-M21, px, fma(-u, py, py));  // -M21 px + M11 py
   const long long eb = __double_as_longlong(e) & 0x7FFFFFFFFFFFFFFFll;
@@ -107,139 +117,138 @@ __device__ __forceinline__ void multpfringe_body(Part& p, const MapCtx& m, const
     pynew = fma(nyp, w, nyp);
   } else {
     const double detM = __dsub_rn(1.0, e);
-    pxnew = nxp / detM;
-    pynew = nyp / detM;
+    pxnew = __ddiv_rn(nxp, detM);
+    pynew = __ddiv_rn(nyp, detM);
   }
   p.xp = pxnew;
   p.yp = pynew;
-  p.z = fma(-(fma(pxnew, fx, pynew * fy) * KNL), KNL, p.z);
+  p.z = fma(-dmul<S>(fma(pxnew, fx, dmul<S>(pynew, fy)), KNL), KNL, p.z);
 }
 
 // Applies ops[a..b) to one particle.
+template <int S>
 __device__ __forceinline__ void apply_ops(Part& p, const DevOp* __restrict__ ops, int a, int b,
                                           const MapCtx& m) {
   for (int k = a; k < b; ++k) {
     const DevOp& o = ops[k];
     switch (o.code) {
       case ORBIT_OP_DRIFT:  // drift (teapotbase.cc:158-184)
-        drift_body(p, m, o.c[0]);
+        drift_body<S>(p, m, o.c[0]);
         break;
       case ORBIT_OP_QUAD1: {  // quad1 (teapotbase.cc:620-701); c = m11,m12,m21,m22,m33,m34,m43,m44,g2i*L
-        ensure_knl(p, m);
-        double x0 = p.x, xp0 = p.xp, y0 = p.y, yp0 = p.yp;
-        p.x = x0 * o.c[0] + xp0 * o.c[1];
-        p.xp = x0 * o.c[2] + xp0 * o.c[3];
-        p.y = y0 * o.c[4] + yp0 * o.c[5];
-        p.yp = y0 * o.c[6] + yp0 * o.c[7];
-        p.z += p.dp_p * o.c[8];
+        ensure_knl<S>(p, m);
+        const double x0 = p.x, xp0 = p.xp, y0 = p.y, yp0 = p.yp;
+        p.x = fma(x0, o.c[0], dmul<S>(xp0, o.c[1]));
+        p.xp = fma(x0, o.c[2], dmul<S>(xp0, o.c[3]));
+        p.y = fma(y0, o.c[4], dmul<S>(yp0, o.c[5]));
+        p.yp = fma(y0, o.c[6], dmul<S>(yp0, o.c[7]));
+        p.z = fma(p.dp_p, o.c[8], p.z);
         break;
       }
       case ORBIT_OP_QUAD2:
       case ORBIT_OP_BEND2: {  // quad2 / bend2 (teapotbase.cc:719-744, 1164-1189); c0 = L
-        ensure_knl(p, m);
-        double L = o.c[0], dp_p = p.dp_p, knl = p.knl;
-        double kld = knl * L * dp_p;
-        p.x -= kld * p.xp;
-        p.y -= kld * p.yp;
-        double d2g = dp_p * dp_p * m.gamma2i;
-        double phifac = (p.xp * p.xp + p.yp * p.yp + d2g) * 0.5;
-        phifac = (phifac * knl + d2g) * knl;
-        p.z -= L * phifac;
+        ensure_knl<S>(p, m);
+        const double L = o.c[0], dp_p = p.dp_p, knl = p.knl;
+        const double kld = dmul<S>(dmul<S>(knl, L), dp_p);
+        p.x = fma(-kld, p.xp, p.x);
+        p.y = fma(-kld, p.yp, p.y);
+        const double d2g = dmul<S>(dmul<S>(dp_p, dp_p), m.gamma2i);
+        double phifac = dhalf<S>(fma(p.xp, p.xp, fma(p.yp, p.yp, d2g)));
+        phifac = dmul<S>(fma(phifac, knl, d2g), knl);
+        p.z = fma(-L, phifac, p.z);
         break;
       }
       case ORBIT_OP_QFRIN:
       case ORBIT_OP_QFROUT: {  // quadfringeIN/OUT (teapotbase.cc:784-904); c0 = +-kq/4, c1 = +-kq/12
-        ensure_knl(p, m);
-        // Regrouped for the FP64 pipe (29 instructions instead of 33, one
-        // rounding more or less per term): k4 folded into r^2 and x y, the
+        ensure_knl<S>(p, m);
+        // Regrouped for the FP64 pipe: k4 folded into r^2 and x y, the
         // products k12 x0 a and k12 y0 b shared by x, y and z, and the
-        // test on u made on its bits (u >= 0) on the integer pipe.  Sums
-        // are explicitly rounded (__dadd_rn) so that no kernel contracts
-        // them into FMAs differently from another.
-        double KNL = p.knl;
-        double x0 = p.x, xp0 = p.xp, y0 = p.y, yp0 = p.yp;
-        double x2 = x0 * x0, y2 = y0 * y0;
-        double k4 = o.c[0] * KNL, k12 = o.c[1] * KNL;
-        double a = fma(3., y2, x2), b = fma(3., x2, y2);  // x^2+3y^2, y^2+3x^2
-        double t = k4 * __dsub_rn(x2, y2);
-        double u = t * t;                                  // detM = 1 - u
-        double kr = k4 * __dadd_rn(x2, y2), kxy = (2.0 * k4) * (x0 * y0);
-        double nxp = fma(kxy, yp0, fma(-kr, xp0, xp0));   // xp0 - k4 (xp0 r^2 - 2 yp0 x y)
-        double nyp = fma(-kxy, xp0, fma(kr, yp0, yp0));   // yp0 - k4 (-yp0 r^2 + 2 xp0 x y)
-        long long ub = __double_as_longlong(u);
+        // test on u made on its bits (u >= 0) on the integer pipe.
+        const double KNL = p.knl;
+        const double x0 = p.x, xp0 = p.xp, y0 = p.y, yp0 = p.yp;
+        const double x2 = dmul<S>(x0, x0), y2 = dmul<S>(y0, y0);
+        const double k4 = dmul<S>(o.c[0], KNL), k12 = dmul<S>(o.c[1], KNL);
+        const double a = fma(3., y2, x2), b = fma(3., x2, y2);  // x^2+3y^2, y^2+3x^2
+        const double t = dmul<S>(k4, __dsub_rn(x2, y2));
+        const double u = dmul<S>(t, t);  // detM = 1 - u
+        const double kr = dmul<S>(k4, __dadd_rn(x2, y2)), kxy = dmul<S>(dtwice<S>(k4), dmul<S>(x0, y0));
+        const double nxp = fma(kxy, yp0, fma(-kr, xp0, xp0));  // xp0 - k4 (xp0 r^2 - 2 yp0 x y)
+        const double nyp = fma(-kxy, xp0, fma(kr, yp0, yp0));  // yp0 - k4 (-yp0 r^2 + 2 xp0 x y)
+        const long long ub = __double_as_longlong(u);
         if (ub < 0x3E40000000000000ll) {
           // u < 2^-27: 1/(1-u) = 1 + u + O(2^-54)
           p.xp = fma(nxp, u, nxp);
           p.yp = fma(nyp, u, nyp);
         } else if (ub < 0x3EB0000000000000ll) {
           // u < 2^-20: 1/(1-u) = 1 + u + u^2 + O(2^-60)
-          double w = fma(u, u, u);
+          const double w = fma(u, u, u);
           p.xp = fma(nxp, w, nxp);
           p.yp = fma(nyp, w, nyp);
         } else {
-          double detM = 1.0 - u;
-          p.xp = nxp / detM;
-          p.yp = nyp / detM;
+          const double detM = __dsub_rn(1.0, u);
+          p.xp = __ddiv_rn(nxp, detM);
+          p.yp = __ddiv_rn(nyp, detM);
         }
-        double X = (k12 * x0) * a, Y = (k12 * y0) * b;
+        const double X = dmul<S>(dmul<S>(k12, x0), a), Y = dmul<S>(dmul<S>(k12, y0), b);
         p.x = __dadd_rn(x0, X);
         p.y = __dsub_rn(y0, Y);
-        p.z = fma(KNL, fma(xp0, X, -(yp0 * Y)), p.z);
+        p.z = fma(KNL, fma(xp0, X, -dmul<S>(yp0, Y)), p.z);
         break;
       }
       case ORBIT_OP_BEND1: {  // bend1 (teapotbase.cc:1099-1146); c = m11,m12,m16,m21,m22,m26,m51,m52,m56,L
-        ensure_knl(p, m);
-        double x0 = p.x, xp0 = p.xp, dp_p = p.dp_p;
-        p.x = x0 * o.c[0] + xp0 * o.c[1] + dp_p * o.c[2];
-        p.xp = x0 * o.c[3] + xp0 * o.c[4] + dp_p * o.c[5];
-        p.y += o.c[9] * p.yp;
-        p.z += x0 * o.c[6] + xp0 * o.c[7] + dp_p * o.c[8];
+        ensure_knl<S>(p, m);
+        const double x0 = p.x, xp0 = p.xp, dp_p = p.dp_p;
+        p.x = fma(x0, o.c[0], fma(xp0, o.c[1], dmul<S>(dp_p, o.c[2])));
+        p.xp = fma(x0, o.c[3], fma(xp0, o.c[4], dmul<S>(dp_p, o.c[5])));
+        p.y = fma(o.c[9], p.yp, p.y);
+        p.z = __dadd_rn(p.z, fma(x0, o.c[6], fma(xp0, o.c[7], dmul<S>(dp_p, o.c[8]))));
         break;
       }
       case ORBIT_OP_BEND3: {  // bend3 (teapotbase.cc:1208-1232); c0 = th
-        ensure_knl(p, m);
-        double th = o.c[0], dp_p = p.dp_p, KNL = p.knl;
-        double phifac = (p.yp * p.yp + dp_p * dp_p * m.gamma2i) * 0.5;
-        p.xp -= phifac * KNL * th;
-        p.y += KNL * p.yp * p.x * th;
-        phifac = (phifac * KNL - dp_p * m.gamma2i) * KNL;
-        p.z -= th * phifac * p.x;
+        ensure_knl<S>(p, m);
+        const double th = o.c[0], dp_p = p.dp_p, KNL = p.knl;
+        double phifac = dhalf<S>(fma(p.yp, p.yp, dmul<S>(dmul<S>(dp_p, dp_p), m.gamma2i)));
+        p.xp = fma(-dmul<S>(phifac, KNL), th, p.xp);
+        p.y = fma(dmul<S>(dmul<S>(KNL, p.yp), p.x), th, p.y);
+        phifac = dmul<S>(fma(phifac, KNL, -dmul<S>(dp_p, m.gamma2i)), KNL);
+        p.z = fma(-dmul<S>(th, phifac), p.x, p.z);
         break;
       }
       case ORBIT_OP_BEND4: {  // bend4 (teapotbase.cc:1251-1274); c0 = th
-        ensure_knl(p, m);
-        double th = o.c[0], KNL = p.knl;
-        double xfac = 1.0 + KNL * p.xp * th * 0.5;
-        double phifac = KNL * KNL * p.xp * p.xp * 0.5;
-        p.x *= xfac * xfac;
-        p.xp /= xfac;
-        p.z -= th * phifac * p.x;
+        ensure_knl<S>(p, m);
+        const double th = o.c[0], KNL = p.knl;
+        const double xfac = fma(dhalf<S>(dmul<S>(KNL, p.xp)), th, 1.0);
+        const double kxp = dmul<S>(KNL, p.xp);
+        const double phifac = dhalf<S>(dmul<S>(kxp, kxp));
+        p.x = dmul<S>(p.x, dmul<S>(xfac, xfac));
+        p.xp = __ddiv_rn(p.xp, xfac);
+        p.z = fma(-dmul<S>(th, phifac), p.x, p.z);
         break;
       }
       case ORBIT_OP_BFRIN:
       case ORBIT_OP_BFROUT: {  // bendfringeIN/OUT (teapotbase.cc:1292-1348); c0 = +-1/(2 rho), c1 = +-1/rho
-        ensure_knl(p, m);
-        double KNL = p.knl, y2 = p.y * p.y;
-        p.x += KNL * y2 * o.c[0];
-        p.yp -= KNL * p.xp * p.y * o.c[1];
-        p.z += KNL * KNL * p.xp * y2 * o.c[0];
+        ensure_knl<S>(p, m);
+        const double KNL = p.knl, y2 = dmul<S>(p.y, p.y), xp0 = p.xp;
+        p.x = fma(dmul<S>(KNL, y2), o.c[0], p.x);
+        p.yp = fma(-dmul<S>(dmul<S>(KNL, xp0), p.y), o.c[1], p.yp);
+        p.z = fma(dmul<S>(dmul<S>(dmul<S>(KNL, KNL), xp0), y2), o.c[0], p.z);
         break;
       }
       case ORBIT_OP_MULTP: {  // multp (teapotbase.cc:336-374); i0 = pole, i1 = skew, c0 = kl/pole!
         if (m.charge == 0.) break;
         // z^pole from z (the reference starts its loop from 1), kl/pole! on
-        // the host; sums are explicit FMAs
+        // the host
         double zr = 1.0, zi = 0.0;
         if (o.i0 > 0) {
           zr = p.x;
           zi = p.y;
           for (int q = 1; q < o.i0; ++q) {
-            double t = fma(zr, p.x, -(zi * p.y));
-            zi = fma(zr, p.y, zi * p.x);
+            const double t = fma(zr, p.x, -dmul<S>(zi, p.y));
+            zi = fma(zr, p.y, dmul<S>(zi, p.x));
             zr = t;
           }
         }
-        double kl1 = o.c[0];
+        const double kl1 = o.c[0];
         if (o.i1) {
           p.xp = fma(kl1, zi, p.xp);
           p.yp = fma(kl1, zr, p.yp);
@@ -252,83 +261,85 @@ __device__ __forceinline__ void apply_ops(Part& p, const DevOp* __restrict__ ops
       case ORBIT_OP_MPFRIN:
       case ORBIT_OP_MPFROUT:  // c0, c1 = signed kterm (re, im)
         if (m.charge == 0.) break;
-        multpfringe_body(p, m, o);
+        multpfringe_body<S>(p, m, o);
         break;
       case ORBIT_OP_ROTXY: {  // rotatexy (teapotbase.cc:80-101); c0 = cos, c1 = sin
-        double cs = o.c[0], sn = o.c[1];
-        double xt = p.x, pxt = p.xp, yt = p.y, pyt = p.yp;
-        p.x = cs * xt - sn * yt;
-        p.xp = cs * pxt - sn * pyt;
-        p.y = sn * xt + cs * yt;
-        p.yp = sn * pxt + cs * pyt;
+        const double cs = o.c[0], sn = o.c[1];
+        const double xt = p.x, pxt = p.xp, yt = p.y, pyt = p.yp;
+        p.x = fma(cs, xt, -dmul<S>(sn, yt));
+        p.xp = fma(cs, pxt, -dmul<S>(sn, pyt));
+        p.y = fma(sn, xt, dmul<S>(cs, yt));
+        p.yp = fma(sn, pxt, dmul<S>(cs, pyt));
         break;
       }
       case ORBIT_OP_WRAP:  // wrapbunch (teapotbase.cc:202-212); c0 = L, c1 = L/2
-        if (p.z < -o.c[1]) p.z += o.c[0];
-        if (p.z > o.c[1]) p.z -= o.c[0];
+        if (p.z < -o.c[1]) p.z = __dadd_rn(p.z, o.c[0]);
+        if (p.z > o.c[1]) p.z = __dsub_rn(p.z, o.c[0]);
         break;
       case ORBIT_OP_KICK:  // kick (teapotbase.cc:232-258)
-        if (o.c[0] != 0.) p.xp += o.c[0];
-        if (o.c[1] != 0.) p.yp += o.c[1];
-        if (o.c[2] != 0.) { p.dE += o.c[2]; p.knl_ok = false; }
+        if (o.c[0] != 0.) p.xp = __dadd_rn(p.xp, o.c[0]);
+        if (o.c[1] != 0.) p.yp = __dadd_rn(p.yp, o.c[1]);
+        if (o.c[2] != 0.) { p.dE = __dadd_rn(p.dE, o.c[2]); p.knl_ok = false; }
         break;
       case ORBIT_OP_WEDGEROT: {  // wedgerotate (teapotbase.cc:923-967); c0 = cos, c1 = sin, i0 = frinout
         // dE = (p0 - 1)/coeff cancels, so this rare map keeps the
         // reference's unfused rounding (explicit _rn operations).
-        double cs = o.c[0], sn = o.c[1], dp_p;
-        double dpc = m.dp_p_coeff;
+        const double cs = o.c[0], sn = o.c[1];
+        const double dpc = m.dp_p_coeff;
+        double dp_p;
         if (o.i0 == 0) {
           dp_p = __dmul_rn(p.dE, dpc);
-          double xp_t = p.xp, p0_t = __dadd_rn(1.0, dp_p);
-          p.x /= cs;
+          const double xp_t = p.xp, p0_t = __dadd_rn(1.0, dp_p);
+          p.x = __ddiv_rn(p.x, cs);
           p.xp = __dadd_rn(__dmul_rn(xp_t, cs), __dmul_rn(p0_t, sn));
-          double p0 = __dadd_rn(__dmul_rn(-xp_t, sn), __dmul_rn(p0_t, cs));
+          const double p0 = __dadd_rn(__dmul_rn(-xp_t, sn), __dmul_rn(p0_t, cs));
           dp_p = __dsub_rn(p0, 1.0);
           p.z = __dmul_rn(__dadd_rn(__dmul_rn(-p.x, sn), p.z), cs);
         } else {
           dp_p = __dmul_rn(p.dE, dpc);
-          double p0 = __dadd_rn(1.0, dp_p);
-          p.z = __dadd_rn(__dmul_rn(p.x, sn), p.z / cs);
+          const double p0 = __dadd_rn(1.0, dp_p);
+          p.z = __dadd_rn(__dmul_rn(p.x, sn), __ddiv_rn(p.z, cs));
           p.x = __dmul_rn(p.x, cs);
-          double xp_t = __dsub_rn(__dmul_rn(p.xp, cs), __dmul_rn(p0, sn));
-          double p0_t = __dadd_rn(__dmul_rn(p.xp, sn), __dmul_rn(p0, cs));
+          const double xp_t = __dsub_rn(__dmul_rn(p.xp, cs), __dmul_rn(p0, sn));
+          const double p0_t = __dadd_rn(__dmul_rn(p.xp, sn), __dmul_rn(p0, cs));
           p.xp = xp_t;
           dp_p = __dsub_rn(p0_t, 1.0);
         }
-        p.dE = dp_p / dpc;
+        p.dE = __ddiv_rn(dp_p, dpc);
         p.knl_ok = false;
         break;
       }
       case ORBIT_OP_WEDGEDRIFT: {  // wedgedrift (teapotbase.cc:986-1016); c0 = ct, i0 = inout
         double s;
         if (o.i0 == 0) {
-          ensure_knl(p, m);
-          double tn = p.xp / (1.0 + p.dp_p);
-          s = p.x / (o.c[0] - tn);
+          ensure_knl<S>(p, m);
+          const double tn = __ddiv_rn(p.xp, __dadd_rn(1.0, p.dp_p));
+          s = __ddiv_rn(p.x, __dsub_rn(o.c[0], tn));
         } else {
-          s = p.x / o.c[0];
+          s = __ddiv_rn(p.x, o.c[0]);
         }
-        drift_body(p, m, s);
+        drift_body<S>(p, m, s);
         break;
       }
       case ORBIT_OP_WEDGEBEND: {  // wedgebend (teapotbase.cc:1037-1080); c0 = ct, c1 = rho, i0 = inout, i1 = nst
         double s;
         if (o.i0 == 0) {
-          s = -p.x / o.c[0];
+          s = __ddiv_rn(-p.x, o.c[0]);
         } else {
-          ensure_knl(p, m);
-          double tn = p.xp / (1.0 + p.dp_p);
-          s = -p.x / (o.c[0] + tn);
+          ensure_knl<S>(p, m);
+          const double tn = __ddiv_rn(p.xp, __dadd_rn(1.0, p.dp_p));
+          s = __ddiv_rn(-p.x, __dadd_rn(o.c[0], tn));
         }
-        int nst = o.i1;
-        double sm = s / nst, sm2 = sm / 2.0;
-        drift_body(p, m, sm2);
-        p.xp -= sm / o.c[1];
+        const int nst = o.i1;
+        const double sm = __ddiv_rn(s, (double)nst), sm2 = __ddiv_rn(sm, 2.0);
+        const double kick = __ddiv_rn(sm, o.c[1]);
+        drift_body<S>(p, m, sm2);
+        p.xp = __dsub_rn(p.xp, kick);
         for (int j = 1; j < nst; j++) {
-          drift_body(p, m, sm);
-          p.xp -= sm / o.c[1];
+          drift_body<S>(p, m, sm);
+          p.xp = __dsub_rn(p.xp, kick);
         }
-        drift_body(p, m, sm2);
+        drift_body<S>(p, m, sm2);
         break;
       }
       default:
