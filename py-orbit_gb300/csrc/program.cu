@@ -67,7 +67,7 @@ __device__ __forceinline__ void pass_body(double* __restrict__ cx, double* __res
     p.x = cx[i]; p.xp = cxp[i]; p.y = cy[i]; p.yp = cyp[i]; p.z = cz[i]; p.dE = cdE[i];
     p.knl_ok = false;
     if (km & KNL_LOAD) {  // 1/(1+dp_p) as an earlier pass of this run computed it from the same dE
-      p.dp_p = dmul<ORBIT_SOFT_MUL>(p.dE, m.dp_p_coeff);
+      p.dp_p = dmul<ORBIT_SOFT_MUL & 1>(p.dE, m.dp_p_coeff);
       p.knl = knl_buf[i];
       p.knl_ok = true;
     }
@@ -85,7 +85,7 @@ __device__ __forceinline__ void pass_body(double* __restrict__ cx, double* __res
     apply_ops<ORBIT_SOFT_MUL>(p, ops, a, b, m);
     if (EXT) acc.add(p.x, p.y, p.z);
     if (km & KNL_STORE) {
-      ensure_knl<ORBIT_SOFT_MUL>(p, m);
+      ensure_knl<ORBIT_SOFT_MUL & 1>(p, m);
       knl_buf[i] = p.knl;
     }
     cx[i] = p.x; cxp[i] = p.xp; cy[i] = p.y; cyp[i] = p.yp; cz[i] = p.z; cdE[i] = p.dE;

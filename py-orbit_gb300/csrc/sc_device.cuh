@@ -730,9 +730,9 @@ __device__ __forceinline__ bool kick_fixed(const KickFix& k, const long long* __
     gx += __mul64hi(dwx[i] << 3, s);  // Q(sphi-5)
     gy += __mul64hi(wx[i] << 4, t);   // Q(sphi-5)
   }
-  const double lf = dmul<ORBIT_SOFT_MUL>((double)lv, k.lfs);  // -lambda(z) * factor
-  xp = fma((double)gx, dmul<ORBIT_SOFT_MUL>(k.gxs, lf), xp);
-  yp = fma((double)gy, dmul<ORBIT_SOFT_MUL>(k.gys, lf), yp);
+  const double lf = dmul<(ORBIT_SOFT_MUL >> 4) & 1>((double)lv, k.lfs);  // -lambda(z) * factor
+  xp = fma((double)gx, dmul<(ORBIT_SOFT_MUL >> 4) & 1>(k.gxs, lf), xp);
+  yp = fma((double)gy, dmul<(ORBIT_SOFT_MUL >> 4) & 1>(k.gys, lf), yp);
   return true;
 }
 

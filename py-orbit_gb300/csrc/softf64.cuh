@@ -276,10 +276,15 @@ SF_HD double scale2(double x, int k) {
 
 }  // namespace sf
 
-// Which pipe the maps' and the kick's multiplies use (1: integer, 0: FP64);
-// the results are the same either way.
+// Which pipe the maps' and the kick's multiplies use, one bit per family
+// (1: integer, 0: FP64; bits as in apply_ops, bit 4 the SC kick); the
+// results are the same for every value.  Measured on the FODO turn (1e6
+// particles, fused pass per turn): all on the FP64 pipe 26.2 ms, all on the
+// integer pipes 23.5 ms, drift and quad fringe on the integer pipes 23.1
+// ms (quad1 indifferent; the kick's on the integer pipes 0.4 ms slower, the
+// fringe's on the FP64 pipe 1.9 ms slower).
 #ifndef ORBIT_SOFT_MUL
-#define ORBIT_SOFT_MUL 1
+#define ORBIT_SOFT_MUL 0x0D
 #endif
 
 #ifdef __CUDACC__

@@ -129,49 +129,54 @@ __device__ __forceinline__ void multpfringe_body(Part& p, const MapCtx& m, const
 template <int S>
 __device__ __forceinline__ void apply_ops(Part& p, const DevOp* __restrict__ ops, int a, int b,
                                           const MapCtx& m) {
+  // S: a bit per map family selects its multiplies' pipe (1 = integer):
+  // bit 0 drift, quad2 / bend2 and the wedges; bit 1 quad1; bit 2 the quad
+  // fringes; bit 3 bends, bend fringes, multipoles and their fringes,
+  // rotations.  The results are the same for every S.
+  constexpr int SD = S & 1, SQ = (S >> 1) & 1, SF = (S >> 2) & 1, SB = (S >> 3) & 1;
   for (int k = a; k < b; ++k) {
     const DevOp& o = ops[k];
     switch (o.code) {
       case ORBIT_OP_DRIFT:  // drift (teapotbase.cc:158-184)
-        drift_body<S>(p, m, o.c[0]);
+        drift_body<SD>(p, m, o.c[0]);
         break;
       case ORBIT_OP_QUAD1: {  // quad1 (teapotbase.cc:620-701); c = m11,m12,m21,m22,m33,m34,m43,m44,g2i*L
-        ensure_knl<S>(p, m);
+        ensure_knl<SQ>(p, m);
         const double x0 = p.x, xp0 = p.xp, y0 = p.y, yp0 = p.yp;
-        p.x = fma(x0, o.c[0], dmul<S>(xp0, o.c[1]));
-        p.xp = fma(x0, o.c[2], dmul<S>(xp0, o.c[3]));
-        p.y = fma(y0, o.c[4], dmul<S>(yp0, o.c[5]));
-        p.yp = fma(y0, o.c[6], dmul<S>(yp0, o.c[7]));
+        p.x = fma(x0, o.c[0], dmul<SQ>(xp0, o.c[1]));
+        p.xp = fma(x0, o.c[2], dmul<SQ>(xp0, o.c[3]));
+        p.y = fma(y0, o.c[4], dmul<SQ>(yp0, o.c[5]));
+        p.yp = fma(y0, o.c[6], dmul<SQ>(yp0, o.c[7]));
         p.z = fma(p.dp_p, o.c[8], p.z);
         break;
       }
       case ORBIT_OP_QUAD2:
       case ORBIT_OP_BEND2: {  // quad2 / bend2 (teapotbase.cc:719-744, 1164-1189); c0 = L
-        ensure_knl<S>(p, m);
+        ensure_knl<SD>(p, m);
         const double L = o.c[0], dp_p = p.dp_p, knl = p.knl;
-        const double kld = dmul<S>(dmul<S>(knl, L), dp_p);
+        const double kld = dmul<SD>(dmul<SD>(knl, L), dp_p);
         p.x = fma(-kld, p.xp, p.x);
         p.y = fma(-kld, p.yp, p.y);
-        const double d2g = dmul<S>(dmul<S>(dp_p, dp_p), m.gamma2i);
-        double phifac = dhalf<S>(fma(p.xp, p.xp, fma(p.yp, p.yp, d2g)));
-        phifac = dmul<S>(fma(phifac, knl, d2g), knl);
+        const double d2g = dmul<SD>(dmul<SD>(dp_p, dp_p), m.gamma2i);
+        double phifac = dhalf<SD>(fma(p.xp, p.xp, fma(p.yp, p.yp, d2g)));
+        phifac = dmul<SD>(fma(phifac, knl, d2g), knl);
         p.z = fma(-L, phifac, p.z);
         break;
       }
       case ORBIT_OP_QFRIN:
       case ORBIT_OP_QFROUT: {  // quadfringeIN/OUT (teapotbase.cc:784-904); c0 = +-kq/4, c1 = +-kq/12
-        ensure_knl<S>(p, m);
+        ensure_knl<SF>(p, m);
         // Regrouped for the FP64 pipe: k4 folded into r^2 and x y, the
         // products k12 x0 a and k12 y0 b shared by x, y and z, and the
         // test on u made on its bits (u >= 0) on the integer pipe.
         const double KNL = p.knl;
         const double x0 = p.x, xp0 = p.xp, y0 = p.y, yp0 = p.yp;
-        const double x2 = dmul<S>(x0, x0), y2 = dmul<S>(y0, y0);
-        const double k4 = dmul<S>(o.c[0], KNL), k12 = dmul<S>(o.c[1], KNL);
+        const double x2 = dmul<SF>(x0, x0), y2 = dmul<SF>(y0, y0);
+        const double k4 = dmul<SF>(o.c[0], KNL), k12 = dmul<SF>(o.c[1], KNL);
         const double a = fma(3., y2, x2), b = fma(3., x2, y2);  // x^2+3y^2, y^2+3x^2
-        const double t = dmul<S>(k4, __dsub_rn(x2, y2));
-        const double u = dmul<S>(t, t);  // detM = 1 - u
-        const double kr = dmul<S>(k4, __dadd_rn(x2, y2)), kxy = dmul<S>(dtwice<S>(k4), dmul<S>(x0, y0));
+        const double t = dmul<SF>(k4, __dsub_rn(x2, y2));
+        const double u = dmul<SF>(t, t);  // detM = 1 - u
+        const double kr = dmul<SF>(k4, __dadd_rn(x2, y2)), kxy = dmul<SF>(dtwice<SF>(k4), dmul<SF>(x0, y0));
         const double nxp = fma(kxy, yp0, fma(-kr, xp0, xp0));  // xp0 - k4 (xp0 r^2 - 2 yp0 x y)
         const double nyp = fma(-kxy, xp0, fma(kr, yp0, yp0));  // yp0 - k4 (-yp0 r^2 + 2 xp0 x y)
         const long long ub = __double_as_longlong(u);
@@ -189,49 +194,49 @@ __device__ __forceinline__ void apply_ops(Part& p, const DevOp* __restrict__ ops
           p.xp = __ddiv_rn(nxp, detM);
           p.yp = __ddiv_rn(nyp, detM);
         }
-        const double X = dmul<S>(dmul<S>(k12, x0), a), Y = dmul<S>(dmul<S>(k12, y0), b);
+        const double X = dmul<SF>(dmul<SF>(k12, x0), a), Y = dmul<SF>(dmul<SF>(k12, y0), b);
         p.x = __dadd_rn(x0, X);
         p.y = __dsub_rn(y0, Y);
-        p.z = fma(KNL, fma(xp0, X, -dmul<S>(yp0, Y)), p.z);
+        p.z = fma(KNL, fma(xp0, X, -dmul<SF>(yp0, Y)), p.z);
         break;
       }
       case ORBIT_OP_BEND1: {  // bend1 (teapotbase.cc:1099-1146); c = m11,m12,m16,m21,m22,m26,m51,m52,m56,L
-        ensure_knl<S>(p, m);
+        ensure_knl<SB>(p, m);
         const double x0 = p.x, xp0 = p.xp, dp_p = p.dp_p;
-        p.x = fma(x0, o.c[0], fma(xp0, o.c[1], dmul<S>(dp_p, o.c[2])));
-        p.xp = fma(x0, o.c[3], fma(xp0, o.c[4], dmul<S>(dp_p, o.c[5])));
+        p.x = fma(x0, o.c[0], fma(xp0, o.c[1], dmul<SB>(dp_p, o.c[2])));
+        p.xp = fma(x0, o.c[3], fma(xp0, o.c[4], dmul<SB>(dp_p, o.c[5])));
         p.y = fma(o.c[9], p.yp, p.y);
-        p.z = __dadd_rn(p.z, fma(x0, o.c[6], fma(xp0, o.c[7], dmul<S>(dp_p, o.c[8]))));
+        p.z = __dadd_rn(p.z, fma(x0, o.c[6], fma(xp0, o.c[7], dmul<SB>(dp_p, o.c[8]))));
         break;
       }
       case ORBIT_OP_BEND3: {  // bend3 (teapotbase.cc:1208-1232); c0 = th
-        ensure_knl<S>(p, m);
+        ensure_knl<SB>(p, m);
         const double th = o.c[0], dp_p = p.dp_p, KNL = p.knl;
-        double phifac = dhalf<S>(fma(p.yp, p.yp, dmul<S>(dmul<S>(dp_p, dp_p), m.gamma2i)));
-        p.xp = fma(-dmul<S>(phifac, KNL), th, p.xp);
-        p.y = fma(dmul<S>(dmul<S>(KNL, p.yp), p.x), th, p.y);
-        phifac = dmul<S>(fma(phifac, KNL, -dmul<S>(dp_p, m.gamma2i)), KNL);
-        p.z = fma(-dmul<S>(th, phifac), p.x, p.z);
+        double phifac = dhalf<SB>(fma(p.yp, p.yp, dmul<SB>(dmul<SB>(dp_p, dp_p), m.gamma2i)));
+        p.xp = fma(-dmul<SB>(phifac, KNL), th, p.xp);
+        p.y = fma(dmul<SB>(dmul<SB>(KNL, p.yp), p.x), th, p.y);
+        phifac = dmul<SB>(fma(phifac, KNL, -dmul<SB>(dp_p, m.gamma2i)), KNL);
+        p.z = fma(-dmul<SB>(th, phifac), p.x, p.z);
         break;
       }
       case ORBIT_OP_BEND4: {  // bend4 (teapotbase.cc:1251-1274); c0 = th
-        ensure_knl<S>(p, m);
+        ensure_knl<SB>(p, m);
         const double th = o.c[0], KNL = p.knl;
-        const double xfac = fma(dhalf<S>(dmul<S>(KNL, p.xp)), th, 1.0);
-        const double kxp = dmul<S>(KNL, p.xp);
-        const double phifac = dhalf<S>(dmul<S>(kxp, kxp));
-        p.x = dmul<S>(p.x, dmul<S>(xfac, xfac));
+        const double xfac = fma(dhalf<SB>(dmul<SB>(KNL, p.xp)), th, 1.0);
+        const double kxp = dmul<SB>(KNL, p.xp);
+        const double phifac = dhalf<SB>(dmul<SB>(kxp, kxp));
+        p.x = dmul<SB>(p.x, dmul<SB>(xfac, xfac));
         p.xp = __ddiv_rn(p.xp, xfac);
-        p.z = fma(-dmul<S>(th, phifac), p.x, p.z);
+        p.z = fma(-dmul<SB>(th, phifac), p.x, p.z);
         break;
       }
       case ORBIT_OP_BFRIN:
       case ORBIT_OP_BFROUT: {  // bendfringeIN/OUT (teapotbase.cc:1292-1348); c0 = +-1/(2 rho), c1 = +-1/rho
-        ensure_knl<S>(p, m);
-        const double KNL = p.knl, y2 = dmul<S>(p.y, p.y), xp0 = p.xp;
-        p.x = fma(dmul<S>(KNL, y2), o.c[0], p.x);
-        p.yp = fma(-dmul<S>(dmul<S>(KNL, xp0), p.y), o.c[1], p.yp);
-        p.z = fma(dmul<S>(dmul<S>(dmul<S>(KNL, KNL), xp0), y2), o.c[0], p.z);
+        ensure_knl<SB>(p, m);
+        const double KNL = p.knl, y2 = dmul<SB>(p.y, p.y), xp0 = p.xp;
+        p.x = fma(dmul<SB>(KNL, y2), o.c[0], p.x);
+        p.yp = fma(-dmul<SB>(dmul<SB>(KNL, xp0), p.y), o.c[1], p.yp);
+        p.z = fma(dmul<SB>(dmul<SB>(dmul<SB>(KNL, KNL), xp0), y2), o.c[0], p.z);
         break;
       }
       case ORBIT_OP_MULTP: {  // multp (teapotbase.cc:336-374); i0 = pole, i1 = skew, c0 = kl/pole!
@@ -243,8 +248,8 @@ __device__ __forceinline__ void apply_ops(Part& p, const DevOp* __restrict__ ops
           zr = p.x;
           zi = p.y;
           for (int q = 1; q < o.i0; ++q) {
-            const double t = fma(zr, p.x, -dmul<S>(zi, p.y));
-            zi = fma(zr, p.y, dmul<S>(zi, p.x));
+            const double t = fma(zr, p.x, -dmul<SB>(zi, p.y));
+            zi = fma(zr, p.y, dmul<SB>(zi, p.x));
             zr = t;
           }
         }
@@ -261,15 +266,15 @@ __device__ __forceinline__ void apply_ops(Part& p, const DevOp* __restrict__ ops
       case ORBIT_OP_MPFRIN:
       case ORBIT_OP_MPFROUT:  // c0, c1 = signed kterm (re, im)
         if (m.charge == 0.) break;
-        multpfringe_body<S>(p, m, o);
+        multpfringe_body<SB>(p, m, o);
         break;
       case ORBIT_OP_ROTXY: {  // rotatexy (teapotbase.cc:80-101); c0 = cos, c1 = sin
         const double cs = o.c[0], sn = o.c[1];
         const double xt = p.x, pxt = p.xp, yt = p.y, pyt = p.yp;
-        p.x = fma(cs, xt, -dmul<S>(sn, yt));
-        p.xp = fma(cs, pxt, -dmul<S>(sn, pyt));
-        p.y = fma(sn, xt, dmul<S>(cs, yt));
-        p.yp = fma(sn, pxt, dmul<S>(cs, pyt));
+        p.x = fma(cs, xt, -dmul<SB>(sn, yt));
+        p.xp = fma(cs, pxt, -dmul<SB>(sn, pyt));
+        p.y = fma(sn, xt, dmul<SB>(cs, yt));
+        p.yp = fma(sn, pxt, dmul<SB>(cs, pyt));
         break;
       }
       case ORBIT_OP_WRAP:  // wrapbunch (teapotbase.cc:202-212); c0 = L, c1 = L/2
@@ -312,13 +317,13 @@ __device__ __forceinline__ void apply_ops(Part& p, const DevOp* __restrict__ ops
       case ORBIT_OP_WEDGEDRIFT: {  // wedgedrift (teapotbase.cc:986-1016); c0 = ct, i0 = inout
         double s;
         if (o.i0 == 0) {
-          ensure_knl<S>(p, m);
+          ensure_knl<SD>(p, m);
           const double tn = __ddiv_rn(p.xp, __dadd_rn(1.0, p.dp_p));
           s = __ddiv_rn(p.x, __dsub_rn(o.c[0], tn));
         } else {
           s = __ddiv_rn(p.x, o.c[0]);
         }
-        drift_body<S>(p, m, s);
+        drift_body<SD>(p, m, s);
         break;
       }
       case ORBIT_OP_WEDGEBEND: {  // wedgebend (teapotbase.cc:1037-1080); c0 = ct, c1 = rho, i0 = inout, i1 = nst
@@ -326,20 +331,20 @@ __device__ __forceinline__ void apply_ops(Part& p, const DevOp* __restrict__ ops
         if (o.i0 == 0) {
           s = __ddiv_rn(-p.x, o.c[0]);
         } else {
-          ensure_knl<S>(p, m);
+          ensure_knl<SD>(p, m);
           const double tn = __ddiv_rn(p.xp, __dadd_rn(1.0, p.dp_p));
           s = __ddiv_rn(-p.x, __dadd_rn(o.c[0], tn));
         }
         const int nst = o.i1;
         const double sm = __ddiv_rn(s, (double)nst), sm2 = __ddiv_rn(sm, 2.0);
         const double kick = __ddiv_rn(sm, o.c[1]);
-        drift_body<S>(p, m, sm2);
+        drift_body<SD>(p, m, sm2);
         p.xp = __dsub_rn(p.xp, kick);
         for (int j = 1; j < nst; j++) {
-          drift_body<S>(p, m, sm);
+          drift_body<SD>(p, m, sm);
           p.xp = __dsub_rn(p.xp, kick);
         }
-        drift_body<S>(p, m, sm2);
+        drift_body<SD>(p, m, sm2);
         break;
       }
       default:
