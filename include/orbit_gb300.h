@@ -344,6 +344,16 @@ int orbit_batch_class(const orbit_batch_t* b, int cls, int* grid, int* members, 
  * autotuning runs afterwards. */
 int orbit_batch_set_tuning(orbit_batch_t* b, int cls, const int* tuning);
 
+/* ---- NVTX ranges (no counterpart in the reference) ----
+ * A named NVTX range pushed and popped by the host layer: with
+ * ORBIT_NVTX=1 in the environment the Python lattice walk
+ * (AccNode.trackActions) opens one per node, so Nsight Systems timelines and
+ * ncu --nvtx filters show the lattice structure; the C entry points
+ * (teapot_base maps, trackBunch, program and batch turns) always open their
+ * own.  Without an attached tool a range costs a branch. */
+int orbit_nvtx_push(const char* name);
+int orbit_nvtx_pop(void);
+
 /* ---- learned denoising closure (no counterpart in the reference) ----
  * A 4-level convolutional encoder-decoder (channels 16-64, 302,561
  * parameters; BF16 convolution weights, FP32 activations and accumulation)

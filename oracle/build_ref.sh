@@ -5,9 +5,11 @@
 # oracle/_ref/libpyorbit_ref.so.  Flags follow the reference's
 # conf/Linux/make_root_config (-O3) with MPI off (-DUSE_MPI=0: no MPI here).
 # Runs only where the reference tree exists; outputs only into oracle/_ref/.
+# Usage: build_ref.sh [REFERENCE_ROOT]; the root defaults to $PYORBIT_REF,
+# else to a directory named "reference" beside the repository.
 set -euo pipefail
-REF=${PYORBIT_REF:-/root/reference}
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
+REF=${1:-${PYORBIT_REF:-$(dirname "$(dirname "$HERE")")/reference}}
 OUT="$HERE/_ref"
 if [ ! -d "$REF/src/spacecharge" ]; then
   echo "reference tree not found at $REF; skipping" >&2

@@ -600,6 +600,7 @@ int orbit_batch_destroy(orbit_batch_t* bt) {
 }
 
 int orbit_batch_enqueue(orbit_batch_t* bt, int turns) {
+  ORBIT_NVTX("batch turns");
   if (!bt || turns < 0) return set_error(ORBIT_ERR_ARG, "orbit_batch_enqueue: bad argument");
   if (turns == 0) return ORBIT_OK;
   for (auto b : bt->bunches)

@@ -270,3 +270,15 @@ int orbit_bunch_stream(orbit_bunch_t* b, void** stream) {
 }
 
 }  // extern "C"
+
+// NVTX ranges opened and closed by the host layer (the lattice walk names
+// each node); no counterpart in the reference.
+extern "C" int orbit_nvtx_push(const char* name) {
+  nvtxRangePushA(name ? name : "");
+  return ORBIT_OK;
+}
+
+extern "C" int orbit_nvtx_pop(void) {
+  nvtxRangePop();
+  return ORBIT_OK;
+}

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <cstdint>
 #include <string>
 
@@ -45,6 +46,18 @@ void prof_begin(const char* tag, cudaStream_t s);
 void prof_end(cudaStream_t s);
 Profiler* prof_install();
 int prof_collect(Profiler* p, int max_kinds, char* names, double* total_ms, int* launches, int* nkinds);
+// Host-side NVTX range around one reference-level call (a teapot_base map,
+// an SC kick, the turns of a lattice program or of a batch), so that
+// Nsight Systems timelines and ncu's --nvtx filters show the node structure.
+// nvtx3 is header-only: without an attached tool a range costs a branch.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
+#define ORBIT_NVTX(name) ::orbit::NvtxRange orbit_nvtx_range_(name)
+
 #define ORBIT_PB(tag, s) do { if (::orbit::g_prof) ::orbit::prof_begin(tag, s); } while (0)
 #define ORBIT_PE(s) do { if (::orbit::g_prof) ::orbit::prof_end(s); } while (0)
 

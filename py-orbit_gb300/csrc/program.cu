@@ -497,6 +497,7 @@ int orbit_program_run(orbit_program_t* p, orbit_bunch_t* b, int turns) {
 }
 
 int orbit_program_enqueue(orbit_program_t* p, orbit_bunch_t* b, int turns) {
+  ORBIT_NVTX("lattice program turns");
   if (!p || !b || turns < 0) return set_error(ORBIT_ERR_ARG, "orbit_program_enqueue: bad argument");
   if (turns == 0) return ORBIT_OK;
   // work already queued on a calculator by another bunch comes first

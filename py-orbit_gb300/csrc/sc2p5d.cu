@@ -1795,6 +1795,7 @@ int orbit_sc2p5d_denoiser_reset(orbit_sc2p5d_t* c) {
 }
 
 int orbit_sc2p5d_track_boundary(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, const orbit_boundary_t* bnd) {
+  ORBIT_NVTX("SpaceChargeCalc2p5D.trackBunch(boundary)");
   if (!c || !b) return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_track_boundary: null handle");
   if (c->rb) return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_track_boundary: a 2.5Drb calculator has no boundary");
   if (!bnd) return orbit_sc2p5d_track(c, b, length);
@@ -1834,6 +1835,7 @@ int orbit_sc2p5drb_get_long_avg(const orbit_sc2p5d_t* c, int* n) {
 }
 
 int orbit_sc2p5drb_track(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, double pipe_radius) {
+  ORBIT_NVTX("SpaceChargeCalc2p5Drb.trackBunch");
   if (!c || !b || !c->rb) return set_error(ORBIT_ERR_ARG, "orbit_sc2p5drb_track: null or non-2.5Drb handle");
   if (b->n < 2) return ORBIT_OK;  // SpaceChargeCalc2p5Drb.cc:109-110
   ORBIT_CUDA(sc_order_before(c, b->stream));
@@ -1855,6 +1857,7 @@ int orbit_sc2p5drb_beam(orbit_sc2p5d_t* c, double* abx) {
 }
 
 int orbit_sc2p5d_track(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length) {
+  ORBIT_NVTX("SpaceChargeCalc2p5D.trackBunch");
   if (!c || !b) return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_track: null handle");
   if (c->rb) return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_track: a 2.5Drb calculator needs orbit_sc2p5drb_track");
   if (b->n < 2) return ORBIT_OK;  // SpaceChargeCalc2p5D.cc:79-80

@@ -169,7 +169,35 @@ __global__ void __launch_bounds__(256) k_apply_one(double* __restrict__ cx, doub
   }
 }
 
+// teapot_base function names (src/teapot/wrap_teapotbase.cc:488-512) by op code.
+static const char* tpb_name(int code) {
+  switch (code) {
+    case ORBIT_OP_DRIFT: return "teapot_base.drift";
+    case ORBIT_OP_QUAD1: return "teapot_base.quad1";
+    case ORBIT_OP_QUAD2: return "teapot_base.quad2";
+    case ORBIT_OP_QFRIN: return "teapot_base.quadfringeIN";
+    case ORBIT_OP_QFROUT: return "teapot_base.quadfringeOUT";
+    case ORBIT_OP_BEND1: return "teapot_base.bend1";
+    case ORBIT_OP_BEND2: return "teapot_base.bend2";
+    case ORBIT_OP_BEND3: return "teapot_base.bend3";
+    case ORBIT_OP_BEND4: return "teapot_base.bend4";
+    case ORBIT_OP_BFRIN: return "teapot_base.bendfringeIN";
+    case ORBIT_OP_BFROUT: return "teapot_base.bendfringeOUT";
+    case ORBIT_OP_MULTP: return "teapot_base.multp";
+    case ORBIT_OP_MPFRIN: return "teapot_base.multpfringeIN";
+    case ORBIT_OP_MPFROUT: return "teapot_base.multpfringeOUT";
+    case ORBIT_OP_ROTXY: return "teapot_base.rotatexy";
+    case ORBIT_OP_WRAP: return "teapot_base.wrapbunch";
+    case ORBIT_OP_KICK: return "teapot_base.kick";
+    case ORBIT_OP_WEDGEROT: return "teapot_base.wedgerotate";
+    case ORBIT_OP_WEDGEDRIFT: return "teapot_base.wedgedrift";
+    case ORBIT_OP_WEDGEBEND: return "teapot_base.wedgebend";
+    default: return "teapot_base";
+  }
+}
+
 static int launch_one(orbit_bunch_t* b, const orbit_op_t& op) {
+  ORBIT_NVTX(tpb_name(op.code));
   if (!b) return set_error(ORBIT_ERR_ARG, "null bunch");
   DevOp d;
   double tadv = 0.0;

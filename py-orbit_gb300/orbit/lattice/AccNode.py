@@ -6,9 +6,24 @@ the reference's order (AccNode.py:302-350); the space-charge nodes sit as
 BODY/BEFORE children, so the order of maps and kicks is fixed here.
 """
 import math
+import os
 
 from orbit.lattice.AccActionsContainer import AccActionsContainer
 from orbit.utils import NamedObject, ParamsDictObject, TypedObject, orbitFinalize
+
+# ORBIT_NVTX=1: one NVTX range per node walked (orbit_nvtx_push/pop), shown
+# by Nsight Systems and usable as an ncu --nvtx filter.
+_NVTX = os.environ.get("ORBIT_NVTX", "0") == "1"
+
+
+def _nvtx_push(name):
+    from orbit_gb300 import call
+    call("orbit_nvtx_push", str(name).encode())
+
+
+def _nvtx_pop():
+    from orbit_gb300 import call
+    call("orbit_nvtx_pop")
 
 
 class AccNode(NamedObject, TypedObject, ParamsDictObject):
@@ -159,6 +174,8 @@ class AccNode(NamedObject, TypedObject, ParamsDictObject):
         actions (AccNode.py:302-350)."""
         if paramsDict is None:
             paramsDict = {}
+        if _NVTX:
+            _nvtx_push(self.getName())
         paramsDict["node"] = self
         parentNode = paramsDict.get("parentNode")
         if "path_length" not in paramsDict:
@@ -193,3 +210,5 @@ class AccNode(NamedObject, TypedObject, ParamsDictObject):
         paramsDict["node"] = self
         paramsDict["parentNode"] = parentNode
         actionsContainer.performActions(paramsDict, AccNode.EXIT)
+        if _NVTX:
+            _nvtx_pop()

@@ -4,44 +4,43 @@ from orbit.lattice import AccNode
 
 
 def setSC_General_AccNodes(lattice, sc_path_length_min, space_charge_calculator, SC_NodeConstructor):
-    """Walks all parts of the first-level nodes; a node is placed at the start
-    of a part once the path since the previous node exceeds
-    sc_path_length_min, as a BODY/BEFORE child.  Each node's kick length is
-    the path to the next node; the first node (at the lattice start) covers
-    the rest of the lattice.  Returns the list of SC nodes."""
-    accNodes = lattice.getNodes()
-    if len(accNodes) == 0:
+    """Places SC nodes as BODY/BEFORE children of the first-level nodes and
+    returns them in lattice order.
+
+    The rule (which decides the maps between kicks, so it is kept exactly):
+    the parts of the first-level nodes are walked in order; a part that
+    starts once the path walked since the previous placement exceeds
+    sc_path_length_min gets a node.  One more node sits at the start of the
+    lattice.  Each node kicks for the path up to the next node (the path
+    summed part by part since that placement), the last one for the path
+    from its position to the end of the lattice.  Parts longer than 1 m get
+    a warning.  Nodes are named "<node name>:<part index>:"."""
+    nodes = lattice.getNodes()
+    if len(nodes) == 0:
         return
-    nodes_arr = []
-    length_total = 0.0
-    running_path = 0.0
-    for accNode in accNodes:
-        for ip in range(accNode.getnParts()):
-            part_length = accNode.getLength(ip)
+    # placements found by the walk: (node, part index, path from the lattice
+    # start to the part, path walked since the previous placement)
+    found = []
+    since_previous = 0.0
+    walked = 0.0
+    for node in nodes:
+        for part in range(node.getnParts()):
+            part_length = node.getLength(part)
             if part_length > 1.0:
-                print("Warning! Node ", accNode.getName(), " has length ", part_length,
-                      "m which is great than 1 m.  Space charge algorithm may be innacurate!")
-            if running_path > sc_path_length_min:
-                nodes_arr.append((accNode, ip, length_total, running_path))
-                running_path = 0.0
-            running_path += part_length
-            length_total += part_length
-    if len(nodes_arr) > 0:
-        rest_length = length_total - nodes_arr[len(nodes_arr) - 1][2]
-    else:
-        rest_length = length_total
-    nodes_arr.insert(0, (accNodes[0], 0, 0.0, rest_length))
-    scNodes_arr = []
-    for inode in range(len(nodes_arr) - 1):
-        (accNode, part_index, position, path_length) = nodes_arr[inode]
-        (_, _, _, path_lengthNext) = nodes_arr[inode + 1]
-        scNode = SC_NodeConstructor(space_charge_calculator, accNode.getName() + ":" + str(part_index) + ":")
-        scNode.setLengthOfSC(path_lengthNext)
-        scNodes_arr.append(scNode)
-        accNode.addChildNode(scNode, AccNode.BODY, part_index, AccNode.BEFORE)
-    (accNode, part_index, position, path_length) = nodes_arr[len(nodes_arr) - 1]
-    scNode = SC_NodeConstructor(space_charge_calculator, accNode.getName() + ":" + str(part_index) + ":")
-    scNode.setLengthOfSC(rest_length)
-    scNodes_arr.append(scNode)
-    accNode.addChildNode(scNode, AccNode.BODY, part_index, AccNode.BEFORE)
-    return scNodes_arr
+                print("Warning: part %d of node %s is %s m long (more than 1 m); the space-charge kicks may be "
+                      "inaccurate" % (part, node.getName(), part_length))
+            if since_previous > sc_path_length_min:
+                found.append((node, part, walked, since_previous))
+                since_previous = 0.0
+            since_previous += part_length
+            walked += part_length
+    last_position = found[-1][2] if found else 0.0
+    placements = [(nodes[0], 0)] + [(node, part) for node, part, _, _ in found]
+    kick_lengths = [path for _, _, _, path in found] + [walked - last_position]
+    sc_nodes = []
+    for (node, part), kick_length in zip(placements, kick_lengths):
+        sc_node = SC_NodeConstructor(space_charge_calculator, node.getName() + ":" + str(part) + ":")
+        sc_node.setLengthOfSC(kick_length)
+        node.addChildNode(sc_node, AccNode.BODY, part, AccNode.BEFORE)
+        sc_nodes.append(sc_node)
+    return sc_nodes

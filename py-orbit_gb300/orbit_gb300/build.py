@@ -3,7 +3,9 @@ sm_103a (one -gencode, translation units compiled in parallel)."""
 from __future__ import annotations
 
 import concurrent.futures as cf
+import hashlib
 import os
+import platform
 import shutil
 import subprocess
 
@@ -25,11 +27,31 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found")
 
 
-def _stale(target: str, deps) -> bool:
-    if not os.path.exists(target):
+def _digest(paths, flags) -> str:
+    """SHA-256 of the compiler flags and the contents of the given files."""
+    h = hashlib.sha256(" ".join(flags).encode())
+    for p in paths:
+        h.update(p.encode())
+        with open(p, "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()
+
+
+def _stale(target: str, digest: str) -> bool:
+    """A build output is stale unless it exists beside a stamp holding the
+    digest of what it was built from (contents, not modification times: a
+    copied tree with fresh times or an output carried over from another
+    machine is rebuilt exactly when its inputs differ)."""
+    stamp = target + ".sha256"
+    if not (os.path.exists(target) and os.path.exists(stamp)):
         return True
-    t = os.path.getmtime(target)
-    return any(os.path.getmtime(d) > t for d in deps)
+    with open(stamp) as f:
+        return f.read().strip() != digest
+
+
+def _stamp(target: str, digest: str):
+    with open(target + ".sha256", "w") as f:
+        f.write(digest + "\n")
 
 
 def _headers():
@@ -46,11 +68,14 @@ def build_library(force: bool = False, verbose: bool = False, extra_flags=None) 
     flags = NVFLAGS + list(extra_flags or [])
     jobs = []
     objs = []
+    digests = []
     for src in SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(BUILD_DIR, src.replace(".cu", ".o"))
         objs.append(o)
-        if force or _stale(o, [s] + hdrs):
+        d = _digest([s] + sorted(hdrs), ARCH + flags + [platform.machine()])
+        digests.append((o, d))
+        if force or _stale(o, d):
             jobs.append([cc] + ARCH + flags + ["-c", s, "-o", o])
 
     def run(cmd):
@@ -64,10 +89,14 @@ def build_library(force: bool = False, verbose: bool = False, extra_flags=None) 
             for out in ex.map(run, jobs):
                 if verbose and out.strip():
                     print(out)
-    if force or jobs or _stale(LIB_PATH, objs):
+    for o, d in digests:
+        _stamp(o, d)
+    lib_digest = hashlib.sha256("".join(d for _, d in digests).encode()).hexdigest()
+    if force or jobs or _stale(LIB_PATH, lib_digest):
         tmp = LIB_PATH + ".tmp%d" % os.getpid()
         run([cc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart_static", "-lrt", "-ldl", "-lpthread"])
         os.replace(tmp, LIB_PATH)
+        _stamp(LIB_PATH, lib_digest)
     return LIB_PATH
 
 
