@@ -530,7 +530,12 @@ def run_ours(args):
         # counted FP64 instructions (ncu) of the passes and of the deposit
         # against the live DFMA instruction rate
         peak_inst = fp64_peak / 2 * 1e12
-        fp = {"peak_inst_per_s": peak_inst}
+        from orbit_gb300 import device_mul_rates
+        m_fp64, m_int, m_mix = device_mul_rates()
+        fp = {"peak_inst_per_s": peak_inst,
+              "mul_rates_gmul_s": {"fp64_pipe": m_fp64, "integer_pipes": m_int, "both": m_mix,
+                                   "note": "correctly rounded binary64 multiplies measured in this run; the maps' "
+                                           "drift, quad-fringe and bend multiplies run on the integer pipes"}}
         for kname, ipp in FP64_INST_PER_PARTICLE.items():
             k_ms, k_l = prof.get(kname, (0.0, 0))
             if k_ms > 0 and args.form == "plain" and WL["name"] == "fodo":

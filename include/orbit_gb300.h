@@ -49,6 +49,10 @@ const char* orbit_version(void);
  * chains) and streaming copy bandwidth (GB/s, read + write), the roofs the
  * benchmark reports against.  No counterpart in the reference. */
 int orbit_device_peaks(double* fp64_tflops, double* copy_gbs);
+/* Binary64 multiply rates in G multiplies/s over all SMs: on the FP64 pipe
+ * alone, on the integer pipes alone (the library's correctly rounded
+ * integer multiply) and half on each; no counterpart in the reference. */
+int orbit_device_mul_rates(double* fp64_gmul, double* int_gmul, double* mixed_gmul);
 
 /* ------------------------------------------------------------------ */
 /* Bunch: device-resident SoA macroparticle container                 */

@@ -4,6 +4,7 @@
 #include <cstring>
 
 #include "common.cuh"
+#include "softf64.cuh"
 
 namespace orbit {
 
@@ -19,6 +20,43 @@ __global__ void k_dfma_chain(double* out, int iters, double a, double b) {
 #pragma unroll
   for (int k = 0; k < 8; ++k) s += r[k];
   if (s == 123456.789) out[0] = s;  // keeps the chains alive
+}
+
+// HW chains of hardware binary64 multiplies and SW chains of integer-pipe
+// ones (sf::mul), all independent, per thread.
+template <int HW, int SW>
+__global__ void k_dmul_chains(double* out, int iters, double a) {
+  double r[HW + SW + 1];
+#pragma unroll
+  for (int q = 0; q < HW + SW; ++q) r[q] = 1.0 + threadIdx.x * 1e-9 + q * 1e-7;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int q = 0; q < HW; ++q) r[q] = __dmul_rn(r[q], a);
+#pragma unroll
+    for (int q = HW; q < HW + SW; ++q) r[q] = sf::mul(r[q], a);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int q = 0; q < HW + SW; ++q) s += r[q];
+  if (s == 123456.789) out[0] = s;  // keeps the chains alive
+}
+
+template <int HW, int SW>
+static double dmul_rate(double* out, cudaEvent_t e0, cudaEvent_t e1) {
+  const int blocks = num_sms() * 2, threads = 512, iters = 1000;
+  k_dmul_chains<HW, SW><<<blocks, threads>>>(out, 10, 1.0000001);
+  if (cudaDeviceSynchronize() != cudaSuccess) return -1.0;
+  float best = 1e30f;
+  for (int rep = 0; rep < 3; ++rep) {
+    cudaEventRecord(e0);
+    k_dmul_chains<HW, SW><<<blocks, threads>>>(out, iters, 1.0000001);
+    cudaEventRecord(e1);
+    if (cudaEventSynchronize(e1) != cudaSuccess) return -1.0;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) best = ms;
+  }
+  return (double)blocks * threads * iters * (HW + SW) / (best * 1e-3) / 1e9;
 }
 
 __global__ void k_copy(const double2* __restrict__ a, double2* __restrict__ b, size_t n) {
@@ -79,5 +117,31 @@ extern "C" int orbit_device_peaks(double* fp64_tflops, double* copy_gbs) {
   cudaFree(b);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  return ORBIT_OK;
+}
+
+// Binary64 multiply rates (G multiplies/s, correctly rounded, all SMs): on
+// the FP64 pipe alone, on the integer pipes alone (sf::mul) and half on
+// each, which run at the same time.
+extern "C" int orbit_device_mul_rates(double* fp64_gmul, double* int_gmul, double* mixed_gmul) {
+  if (!fp64_gmul || !int_gmul || !mixed_gmul) return set_error(ORBIT_ERR_ARG, "orbit_device_mul_rates: bad argument");
+  cudaEvent_t e0, e1;
+  ORBIT_CUDA(cudaEventCreate(&e0));
+  ORBIT_CUDA(cudaEventCreate(&e1));
+  double* out = nullptr;
+  cudaError_t e = cudaMalloc(&out, sizeof(double));
+  if (e != cudaSuccess) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return cuda_error(e, "orbit_device_mul_rates");
+  }
+  *fp64_gmul = dmul_rate<12, 0>(out, e0, e1);
+  *int_gmul = dmul_rate<0, 12>(out, e0, e1);
+  *mixed_gmul = dmul_rate<6, 6>(out, e0, e1);
+  cudaFree(out);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (*fp64_gmul < 0 || *int_gmul < 0 || *mixed_gmul < 0)
+    return set_error(ORBIT_ERR_CUDA, "orbit_device_mul_rates: kernel failed");
   return ORBIT_OK;
 }

@@ -32,6 +32,15 @@ def device_peaks():
     return f.value, g.value
 
 
+def device_mul_rates():
+    """Binary64 multiply rates (G multiplies/s) on the current GPU: FP64 pipe
+    alone, integer pipes alone (the correctly rounded integer multiply of
+    the maps), half on each."""
+    a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    call("orbit_device_mul_rates", ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+    return a.value, b.value, c.value
+
+
 def _ptr_array(arrs):
     return (_dp * 6)(*[a.ctypes.data_as(_dp) for a in arrs])
 

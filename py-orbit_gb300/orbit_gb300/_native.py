@@ -62,6 +62,7 @@ _SIGS = {
     "orbit_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
     "orbit_version": (ctypes.c_char_p, []),
     "orbit_device_peaks": (ctypes.c_int, [_dp, _dp]),
+    "orbit_device_mul_rates": (ctypes.c_int, [_dp, _dp, _dp]),
     "orbit_bunch_create": (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.c_int]),
     "orbit_bunch_destroy": (ctypes.c_int, [_vp]),
     "orbit_bunch_upload": (ctypes.c_int, [_vp, ctypes.POINTER(_dp), ctypes.c_int]),
