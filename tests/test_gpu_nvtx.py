@@ -12,7 +12,10 @@ pytestmark = pytest.mark.gpu
 
 
 def test_nvtx_ranges_leave_tracking_unchanged(monkeypatch):
-    import orbit.lattice.AccNode as accnode
+    import sys
+
+    import orbit.lattice.AccNode  # noqa: F401  (the package re-exports the class under the same name)
+    accnode = sys.modules["orbit.lattice.AccNode"]
     from orbit_gb300 import workloads as W
     from spacecharge import SpaceChargeCalc2p5D
     soa = W.c2_coords(5000, seed=71)
