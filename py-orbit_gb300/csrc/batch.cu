@@ -34,7 +34,11 @@ namespace orbit {
 // Candidate launch shapes of the particle kernels.
 static const int kDepCand[][2] = {{768, 4096}, {768, 8192}, {768, 16384}, {768, 32768}, {512, 8192}};
 static const int kNDep = 5;
-static const int kPassCand[][2] = {{512, 2048}, {512, 4096}, {512, 8192}, {512, 16384}};
+#ifndef ORBIT_PASS_THREADS
+#define ORBIT_PASS_THREADS 512
+#endif
+static const int kPassCand[][2] = {{ORBIT_PASS_THREADS, 2048}, {ORBIT_PASS_THREADS, 4096}, {ORBIT_PASS_THREADS, 8192},
+                                   {ORBIT_PASS_THREADS, 16384}};
 static const int kNPass = 4;
 
 struct BatchClass {

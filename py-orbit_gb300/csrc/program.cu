@@ -22,6 +22,13 @@ namespace orbit {
 
 static const int kPassSmem = 220 * 1024;
 
+// Threads per block of the fused pass (one block per SM when the kick keeps
+// its potential in shared memory); the register budget per thread is
+// 65536 / ORBIT_PASS_THREADS.
+#ifndef ORBIT_PASS_THREADS
+#define ORBIT_PASS_THREADS 512
+#endif
+
 // KF: 0 no kick, 1 plain kick, 2 fp32 kick.  EXT: accumulate extrema.
 // Blocks blk = 0..nblk-1 share the bunch's particles.
 template <int KF, bool EXT, bool KSMEM>
@@ -95,7 +102,7 @@ __device__ __forceinline__ void pass_body(double* __restrict__ cx, double* __res
 }
 
 template <int KF, bool EXT, bool KSMEM>
-__global__ void __launch_bounds__(512) k_pass(double* __restrict__ cx, double* __restrict__ cxp,
+__global__ void __launch_bounds__(ORBIT_PASS_THREADS) k_pass(double* __restrict__ cx, double* __restrict__ cxp,
                                               double* __restrict__ cy, double* __restrict__ cyp,
                                               double* __restrict__ cz, double* __restrict__ cdE, int n,
                                               const DevOp* __restrict__ ops, int a, int b, MapCtx m,
@@ -108,7 +115,7 @@ __global__ void __launch_bounds__(512) k_pass(double* __restrict__ cx, double* _
 // The same pass for the members of a batch class; each block finds its
 // member in the block table.
 template <int KF, bool EXT, bool KSMEM>
-__global__ void __launch_bounds__(512) kb_pass(const PassJob* __restrict__ jobs,
+__global__ void __launch_bounds__(ORBIT_PASS_THREADS) kb_pass(const PassJob* __restrict__ jobs,
                                                const unsigned short* __restrict__ blk_job,
                                                const int2* __restrict__ mblk, int a, int b, int km) {
   const int j = blk_job[blockIdx.x];
@@ -136,7 +143,7 @@ template <int KF, bool EXT, bool KSMEM>
 static int launch_pass(orbit_bunch_t* bu, cudaStream_t s, size_t smem, const DevOp* ops, int a, int b,
                        const MapCtx& m, const KickArgs& ka, ScState* ext, const SetupArgs& sa, double* knl_buf,
                        int km) {
-  int threads = 512;
+  int threads = ORBIT_PASS_THREADS;
   int bps = KSMEM ? (int)(kPassSmem / (smem > 0 ? smem : 1)) : 4;
   if (bps < 1) bps = 1;
   if (bps > 4) bps = 4;

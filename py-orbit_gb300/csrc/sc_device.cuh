@@ -237,6 +237,11 @@ __device__ __forceinline__ void g1_index(T z, T zmin, T inv_dz, int nz, int& i0,
 // ---------------------------------------------------------------------
 struct KickConst {
   double xmin, ymin, inv_dx, inv_dy, zmin, zmax, inv_dz, fac;
+  // FP32 form: grid coordinates as one FMA, t = x inv_dx + c; the z range
+  // test on order-preserving integer keys; the float constants
+  double cx, cy, cz;
+  unsigned long long kzmin, kzmax;
+  float inv_dx_f, inv_dy_f, fac_f;
   int nx, ny, nz;
   int skip;
 };
@@ -247,6 +252,14 @@ __device__ __forceinline__ void load_kick_const(KickConst& k, const ScState* st,
   k.zmin = st->zmin; k.zmax = st->zmax; k.inv_dz = st->inv_dz;
   // factor = 2 L r_c/(beta^2 gamma^3) / (z_step * totalMacrosize)  (:96-100)
   k.fac = host_factor / (st->dz * st->total_m);
+  k.cx = -k.xmin * k.inv_dx;
+  k.cy = -k.ymin * k.inv_dy;
+  k.cz = -k.zmin * k.inv_dz;
+  k.kzmin = dkey(k.zmin);
+  k.kzmax = dkey(k.zmax);
+  k.inv_dx_f = (float)k.inv_dx;
+  k.inv_dy_f = (float)k.inv_dy;
+  k.fac_f = (float)k.fac;
   k.nx = nx; k.ny = ny; k.nz = nz;
   k.skip = st->skip;
 }
@@ -325,8 +338,10 @@ __device__ __forceinline__ void kick_plain(const KickConst& k, const double* __r
 __device__ __forceinline__ void kick_fp32(const KickConst& k, const float* __restrict__ phi,
                                           const float* __restrict__ lam, double x, double y, double z,
                                           double& xp, double& yp) {
-  float tx = (float)((x - k.xmin) * k.inv_dx);
-  float ty = (float)((y - k.ymin) * k.inv_dy);
+  // the FP64 pipe bounds the pass: one FMA and one conversion per
+  // coordinate, the z range test on the integer pipes
+  float tx = (float)fma(x, k.inv_dx, k.cx);
+  float ty = (float)fma(y, k.inv_dy, k.cy);
   int ix, iy;
   float fx, fy;
   tsc_index<float>(tx, k.nx, ix, fx);
@@ -351,16 +366,17 @@ __device__ __forceinline__ void kick_fp32(const KickConst& k, const float* __res
   float gx = dxm * s0 + dx0 * s1 + dxp * s2;
   float gy = wxm * t0 + wx0 * t1 + wxp * t2;
   float lv = 0.0f;
-  if (!(z < k.zmin || z > k.zmax)) {
-    float zt = (float)((z - k.zmin) * k.inv_dz);
+  const unsigned long long kz = dkey(z);
+  if (kz >= k.kzmin && kz <= k.kzmax) {
+    float zt = (float)fma(z, k.inv_dz, k.cz);
     int i0, ip;
     float w0, wp;
     g1_index<float>(zt, 0.0f, 1.0f, k.nz, i0, ip, w0, wp);
     lv = (k.nz > 1) ? (w0 * lam[i0] + wp * lam[ip]) : lam[0];
   }
-  float lf = -lv * (float)k.fac;
-  xp += (double)(gx * (float)k.inv_dx * lf);
-  yp += (double)(gy * (float)k.inv_dy * lf);
+  float lf = -lv * k.fac_f;
+  xp += (double)(gx * k.inv_dx_f * lf);
+  yp += (double)(gy * k.inv_dy_f * lf);
 }
 
 // ---------------------------------------------------------------------
@@ -369,6 +385,10 @@ __device__ __forceinline__ void kick_fp32(const KickConst& k, const float* __res
 // ---------------------------------------------------------------------
 struct DepConst {
   double xmin, xmax, ymin, ymax, inv_dx, inv_dy, zmin, zmax, inv_dz;
+  // FP32 form: grid coordinates as one FMA and the range tests on
+  // order-preserving integer keys (the FP64 pipe is the scarce one)
+  double cx, cy, cz;
+  unsigned long long kxmin, kxmax, kymin, kymax, kzmin, kzmax;
   int nx, ny, nz;
   int skip;
 };
@@ -377,6 +397,12 @@ __device__ __forceinline__ void load_dep_const(DepConst& d, const ScState* st, i
   d.xmin = st->xmin; d.xmax = st->xmax; d.ymin = st->ymin; d.ymax = st->ymax;
   d.inv_dx = st->inv_dx; d.inv_dy = st->inv_dy;
   d.zmin = st->zmin; d.zmax = st->zmax; d.inv_dz = st->inv_dz;
+  d.cx = -d.xmin * d.inv_dx;
+  d.cy = -d.ymin * d.inv_dy;
+  d.cz = -d.zmin * d.inv_dz;
+  d.kxmin = dkey(d.xmin); d.kxmax = dkey(d.xmax);
+  d.kymin = dkey(d.ymin); d.kymax = dkey(d.ymax);
+  d.kzmin = dkey(d.zmin); d.kzmax = dkey(d.zmax);
   d.nx = nx; d.ny = ny; d.nz = nz;
   d.skip = st->skip;
 }
@@ -738,9 +764,10 @@ __device__ __forceinline__ bool kick_fixed(const KickFix& k, const long long* __
 
 __device__ __forceinline__ void deposit_fp32(const DepConst& d, float* rho, float* zg, double x, double y,
                                              double z, float m) {
-  if (!(x < d.xmin || x > d.xmax || y < d.ymin || y > d.ymax)) {
-    float tx = (float)((x - d.xmin) * d.inv_dx);
-    float ty = (float)((y - d.ymin) * d.inv_dy);
+  const unsigned long long kx = dkey(x), ky = dkey(y), kz = dkey(z);
+  if (kx >= d.kxmin && kx <= d.kxmax && ky >= d.kymin && ky <= d.kymax) {
+    float tx = (float)fma(x, d.inv_dx, d.cx);
+    float ty = (float)fma(y, d.inv_dy, d.cy);
     int ix, iy;
     float fx, fy;
     tsc_index<float>(tx, d.nx, ix, fx);
@@ -756,8 +783,8 @@ __device__ __forceinline__ void deposit_fp32(const DepConst& d, float* rho, floa
 #pragma unroll
       for (int j = 0; j < 3; ++j) atomicAdd(base + i * d.ny + j, ax[i] * wy[j]);
   }
-  if (!(z < d.zmin || z > d.zmax)) {
-    float zt = (float)((z - d.zmin) * d.inv_dz);
+  if (kz >= d.kzmin && kz <= d.kzmax) {
+    float zt = (float)fma(z, d.inv_dz, d.cz);
     int i0, ip;
     float w0, wp;
     g1_index<float>(zt, 0.0f, 1.0f, d.nz, i0, ip, w0, wp);
