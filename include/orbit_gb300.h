@@ -404,6 +404,14 @@ int orbit_denoiser_set_tensor_cores(orbit_denoiser_t* d, int on);
  * uses the tensor cores again.  A learned closure whose network reported
  * an error falls back to the plain deposit. */
 int orbit_denoiser_tensor_status(orbit_denoiser_t* d, int* on, int* err);
+/* Training loss (no counterpart in the reference): levels = 0, the mean
+ * squared error of the output against the target (the default); levels L
+ * in 1..7, the multi-scale loss sum_{s=0..L} weights[s] mean((P^s y -
+ * P^s t)^2) with P the 2x2 average pooling (h and w divisible by 2^L).
+ * Weights 4^s make it a stand-in for the force error (the squared error of
+ * the field of y - t), which weights an error of wavenumber k by 1/k^2:
+ * pooling s times keeps the modes below k_max / 2^s.  Waits for the device. */
+int orbit_denoiser_set_loss(orbit_denoiser_t* d, int levels, const float* weights);
 /* The tensor-core layers' bounded waits: each gives up after `cycles` SM
  * clock cycles (default 2e9, about one second).  withhold_mma != 0 (for
  * testing the failure path only) issues no MMA, so every wait runs out

@@ -120,14 +120,31 @@ def forward(p, x0, tf32_inputs=False):
     return A["y"], A
 
 
-def loss_and_grads(p, x0, t):
-    """Mean squared error, the flat parameter gradient and the output."""
+def loss_and_grads(p, x0, t, weights=None):
+    """The loss, the flat parameter gradient and the output.  Loss: the mean
+    squared error, or with `weights` (w_0..w_L) the multi-scale loss
+    sum_s w_s mean((P^s y - P^s t)^2), P the 2x2 average pooling, whose
+    gradient is sum_s w_s (P^T)^s 2 (P^s y - P^s t) / n_s."""
     ws, ow, ob = unpack(p)
     y, A = forward(p, x0)
     t = np.asarray(t, dtype=np.float64)
     n = y.size
-    loss = float(((y - t) ** 2).sum() / n)
-    dy = 2.0 * (y - t) / n
+    if not weights:
+        loss = float(((y - t) ** 2).sum() / n)
+        dy = 2.0 * (y - t) / n
+    else:
+        loss = 0.0
+        dy = np.zeros_like(y)
+        ys, ts = y, t
+        for s, w in enumerate(weights):
+            if s > 0:
+                ys, ts = pool(ys), pool(ts)
+            e = ys - ts
+            loss += float(w * (e ** 2).sum() / e.size)
+            g = 2.0 * w * e / e.size
+            for _ in range(s):
+                g = pool_bwd(g)
+            dy = dy + g
     convs, owo, obo, total = layout()
     g = np.zeros(total)
     g[owo:owo + 16] = np.einsum("nyx,ncyx->c", dy[:, 0], A["d1"])

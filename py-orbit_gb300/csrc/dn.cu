@@ -619,6 +619,22 @@ __global__ void k_mse(const float* __restrict__ y, const float* __restrict__ t, 
   if ((threadIdx.x & 31) == 0) atomicAdd(loss, s * inv);
 }
 
+// Weighted squared error of one level of the multi-scale loss: loss += w
+// mean((y - t)^2), dy (=, or += with acc) 2 w (y - t) / n.
+__global__ void k_mse_w(const float* __restrict__ y, const float* __restrict__ t, float* __restrict__ dy, size_t n,
+                        float* __restrict__ loss, float w, int acc) {
+  float s = 0.f;
+  const float inv = 1.0f / (float)n;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    float d = y[i] - t[i];
+    s = fmaf(d, d, s);
+    const float g = 2.f * w * d * inv;
+    dy[i] = acc ? dy[i] + g : g;
+  }
+  for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+  if ((threadIdx.x & 31) == 0) atomicAdd(loss, w * s * inv);
+}
+
 // Adam (Kingma & Ba, 2015) on the FP32 master parameters, then the BF16
 // copies of the convolution weights; the gradients are cleared.
 __global__ void k_adam(float* __restrict__ p, float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
@@ -791,6 +807,12 @@ struct orbit_denoiser {
   float* d_wtc = nullptr;
   std::vector<size_t> tc_off;
   int* d_err = nullptr;
+  // training loss: 0 levels = mean squared error; L levels = the
+  // multi-scale loss sum_s w_s mean((P^s y - P^s t)^2), P = 2x2 average
+  // pooling, with its pooled outputs, targets and gradients per level
+  int loss_levels = 0;
+  float loss_w[8] = {1.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  std::vector<float*> ms_y, ms_t, ms_g;
   long long tc_wait_cycles = kTcWaitCycles;
   int tc_withhold = 0;
   bool tc_failed = false;  // a tensor-core layer reported a failed wait
@@ -1111,8 +1133,33 @@ static int loss_and_grads(orbit_denoiser_t* d, const float* target, int nb, cuda
   if (rc) return rc;
   ORBIT_CUDA(cudaMemsetAsync(d->d_loss, 0, sizeof(float), st));
   size_t n = (size_t)nb * d->H * d->W;
-  k_mse<<<grid_1d(n), 256, 0, st>>>(d->act[Y], target, d->grad[Y], n, d->d_loss);
-  ORBIT_LAUNCH_CHECK("denoiser loss");
+  if (d->loss_levels == 0) {
+    k_mse<<<grid_1d(n), 256, 0, st>>>(d->act[Y], target, d->grad[Y], n, d->d_loss);
+    ORBIT_LAUNCH_CHECK("denoiser loss");
+    return backward(d, nb, st);
+  }
+  // multi-scale loss: the squared error of the output, then of its 2x2
+  // poolings level by level (each level weighted); the gradients of the
+  // pooled levels flow back through the pooling to the output
+  const int L = d->loss_levels;
+  k_mse_w<<<grid_1d(n), 256, 0, st>>>(d->act[Y], target, d->grad[Y], n, d->d_loss, d->loss_w[0], 0);
+  const float* yp = d->act[Y];
+  const float* tp = target;
+  for (int s = 1; s <= L; ++s) {
+    const int H = d->H >> (s - 1), W = d->W >> (s - 1);
+    const size_t ns = (size_t)nb * (H / 2) * (W / 2);
+    k_pool<<<grid_1d(ns), 256, 0, st>>>(yp, d->ms_y[s], nb, H, W);
+    k_pool<<<grid_1d(ns), 256, 0, st>>>(tp, d->ms_t[s], nb, H, W);
+    k_mse_w<<<grid_1d(ns), 256, 0, st>>>(d->ms_y[s], d->ms_t[s], d->ms_g[s], ns, d->d_loss, d->loss_w[s], 0);
+    yp = d->ms_y[s];
+    tp = d->ms_t[s];
+  }
+  for (int s = L; s >= 1; --s) {
+    float* din = s > 1 ? d->ms_g[s - 1] : d->grad[Y];
+    const int H = d->H >> (s - 1), W = d->W >> (s - 1);
+    k_pool_bwd<<<grid_1d((size_t)nb * H * W), 256, 0, st>>>(d->ms_g[s], din, nb, H, W);
+  }
+  ORBIT_LAUNCH_CHECK("denoiser multi-scale loss");
   return backward(d, nb, st);
 }
 
@@ -1312,6 +1359,9 @@ int orbit_denoiser_destroy(orbit_denoiser_t* d) {
   if (d->stream) cudaStreamSynchronize(d->stream);
   for (float* p : d->act) if (p) cudaFree(p);
   for (float* p : d->grad) if (p) cudaFree(p);
+  for (auto v : {&d->ms_y, &d->ms_t, &d->ms_g})
+    for (float* p : *v)
+      if (p) cudaFree(p);
   void* bufs[] = {d->d_p, d->d_pb, d->d_g, d->d_m, d->d_v, d->d_isw, d->d_loss, d->d_scratch, d->d_wtc, d->d_err};
   for (void* b : bufs) if (b) cudaFree(b);
   if (d->stream) cudaStreamDestroy(d->stream);
@@ -1381,6 +1431,28 @@ int orbit_denoiser_tensor_status(orbit_denoiser_t* d, int* on, int* err) {
     if (*err) d->tc_failed = true;
     if (*err & 2) g_tc_untrusted = true;
   }
+  return ORBIT_OK;
+}
+
+int orbit_denoiser_set_loss(orbit_denoiser_t* d, int levels, const float* weights) {
+  if (!d || levels < 0 || levels > 7 || (levels > 0 && !weights))
+    return set_error(ORBIT_ERR_ARG, "orbit_denoiser_set_loss: bad argument");
+  if (levels > 0 && ((d->H >> levels) < 1 || (d->W >> levels) < 1 || (d->H % (1 << levels)) || (d->W % (1 << levels))))
+    return set_error(ORBIT_ERR_ARG, "orbit_denoiser_set_loss: the image does not halve that many times");
+  ORBIT_CUDA(cudaDeviceSynchronize());  // training work in flight may use the level buffers
+  for (auto v : {&d->ms_y, &d->ms_t, &d->ms_g}) {
+    for (float* p : *v)
+      if (p) cudaFree(p);
+    v->assign(levels + 1, nullptr);
+  }
+  for (int s = 1; s <= levels; ++s) {
+    const size_t bytes = sizeof(float) * (size_t)d->maxb * (d->H >> s) * (d->W >> s);
+    ORBIT_CUDA(cudaMalloc(&d->ms_y[s], bytes));
+    ORBIT_CUDA(cudaMalloc(&d->ms_t[s], bytes));
+    ORBIT_CUDA(cudaMalloc(&d->ms_g[s], bytes));
+  }
+  d->loss_levels = levels;
+  for (int s = 0; s < 8; ++s) d->loss_w[s] = s <= levels ? (levels ? weights[s] : 1.f) : 0.f;
   return ORBIT_OK;
 }
 

@@ -363,6 +363,17 @@ class DeviceDenoiser:
         call("orbit_denoiser_tensor_status", self.h, None, ctypes.byref(err))
         return err.value
 
+    def set_loss(self, weights=None):
+        """Training loss: None, the mean squared error; a list of L + 1
+        weights, the multi-scale loss sum_s w_s mean((P^s y - P^s t)^2)
+        over s = 0..L 2x2 poolings (weights 4^s: a stand-in for the force
+        error)."""
+        if not weights:
+            call("orbit_denoiser_set_loss", self.h, 0, None)
+            return
+        w = (ctypes.c_float * len(weights))(*[float(v) for v in weights])
+        call("orbit_denoiser_set_loss", self.h, len(weights) - 1, w)
+
     def set_wait_limit(self, cycles: int, withhold_mma: bool = False):
         """Clock-cycle limit of each bounded wait of the tensor-core layers
         (default 2e9); withhold_mma issues no MMA, so the waits run out with

@@ -150,6 +150,7 @@ _SIGS = {
     "orbit_denoiser_set_tensor_cores": (ctypes.c_int, [_vp, ctypes.c_int]),
     "orbit_denoiser_tensor_status": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
     "orbit_denoiser_set_wait_limit": (ctypes.c_int, [_vp, ctypes.c_longlong, ctypes.c_int]),
+    "orbit_denoiser_set_loss": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
     "orbit_nvtx_push": (ctypes.c_int, [ctypes.c_char_p]),
     "orbit_nvtx_pop": (ctypes.c_int, []),
     "orbit_denoiser_train_step": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, ctypes.c_float,

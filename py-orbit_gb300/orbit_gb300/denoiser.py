@@ -154,10 +154,19 @@ def _augment(x, t, code):
     return x.contiguous(), t.contiguous()
 
 
-def train(net: DeviceDenoiser, X, T, epochs=4, batch=16, lr=1e-3, seed=0, log=None):
+# Multi-scale loss weights 4^s over the output and five 2x2 poolings: a
+# stand-in for the force error (the field of the density error weights
+# wavenumber k by 1/k^2; pooling s times keeps the modes below k_max / 2^s).
+FORCE_LOSS_WEIGHTS = [4.0 ** s for s in range(6)]
+
+
+def train(net: DeviceDenoiser, X, T, epochs=4, batch=16, lr=1e-3, seed=0, log=None, loss_weights=None):
     """Adam on minibatches with random symmetries; cosine learning-rate
-    decay.  Returns the per-epoch mean losses."""
+    decay.  loss_weights: None, the mean squared error; a list, the
+    multi-scale loss (DeviceDenoiser.set_loss).  Returns the per-epoch mean
+    losses."""
     import torch
+    net.set_loss(loss_weights)
     n = X.shape[0]
     steps = epochs * (n // batch)
     rng = np.random.default_rng(seed)
@@ -263,11 +272,13 @@ def default_network(max_batch=1):
     return net
 
 
-def train_default(out_path, n_synth=6000, epochs=10, log=print):
+def train_default(out_path, n_synth=6000, epochs=10, log=print, loss_weights=None, init=None, lr=1e-3):
     """Generates the training pairs (synthetic beams of seed 11 and the
-    tracked set-ups of seed 3), trains the 128 x 128 network and saves its
-    parameters; returns held-out evaluations on both kinds of pairs (200
-    synthetic pairs, and every tenth tracked pair, kept out of training)."""
+    tracked set-ups of seed 3), trains the 128 x 128 network (from the
+    parameters `init` if given, else from a seeded initialisation) and
+    saves its parameters; returns held-out evaluations, density and force
+    errors, on both kinds of pairs (200 synthetic pairs, and every tenth
+    tracked pair, kept out of training)."""
     import torch
     Xs, Ts, _ = make_pairs(n_synth + 200, seed=11)
     Xk, Tk = make_tracked_pairs()
@@ -277,9 +288,11 @@ def train_default(out_path, n_synth=6000, epochs=10, log=print):
     X = torch.cat([Xs[:n_synth], Xk[keep]])
     T = torch.cat([Ts[:n_synth], Tk[keep]])
     net = DeviceDenoiser(128, 128, max_batch=16, seed=5)
-    train(net, X, T, epochs=epochs, batch=16, lr=1e-3, log=log)
-    ev = {"synthetic": evaluate(net, Xs[n_synth:], Ts[n_synth:]),
-          "tracked": evaluate(net, Xk[test_k].contiguous(), Tk[test_k].contiguous()),
+    if init is not None:
+        net.set_params(np.asarray(init, dtype=np.float32))
+    train(net, X, T, epochs=epochs, batch=16, lr=lr, log=log, loss_weights=loss_weights)
+    ev = {"synthetic": evaluate(net, Xs[n_synth:], Ts[n_synth:], force=True),
+          "tracked": evaluate(net, Xk[test_k].contiguous(), Tk[test_k].contiguous(), force=True),
           "pairs": int(X.shape[0])}
     np.save(out_path, net.get_params())
     return ev
@@ -289,5 +302,12 @@ if __name__ == "__main__":
     import argparse
     ap = argparse.ArgumentParser(description="train the 128 x 128 denoiser and save its parameters")
     ap.add_argument("--out", default=os.path.join(DATA, DEFAULT))
+    ap.add_argument("--loss", choices=["mse", "force"], default="mse",
+                    help="mse: squared density error; force: the multi-scale stand-in for the force error")
+    ap.add_argument("--init", default=None, help="start from these parameters (.npy) instead of a fresh network")
+    ap.add_argument("--epochs", type=int, default=10)
+    ap.add_argument("--lr", type=float, default=1e-3)
     a = ap.parse_args()
-    print(train_default(a.out))
+    init = np.load(a.init) if a.init else None
+    print(train_default(a.out, epochs=a.epochs, loss_weights=FORCE_LOSS_WEIGHTS if a.loss == "force" else None,
+                        init=init, lr=a.lr))

@@ -52,3 +52,35 @@ def test_oracle_gradients_by_finite_differences():
         assert D.bf16(a[w:w + 1])[0] == a[w] and D.bf16(b[w:w + 1])[0] == b[w]
         fd = (D.loss_and_grads(a, x, t)[0] - D.loss_and_grads(b, x, t)[0]) / (2 * u)
         assert abs(fd - g[w]) <= 1e-3 * max(1e-3, abs(g[w])) + 1e-9, (k, fd, g[w])
+
+
+def test_oracle_multiscale_loss_gradient_by_finite_differences():
+    """The multi-scale loss (squared errors of the output and of its 2x2
+    poolings, weighted 4^s): its gradient with respect to the output bias
+    and output weights against central differences, on a 16x16 image (three
+    pooling levels)."""
+    rng = np.random.default_rng(6)
+    convs, ow, ob, n = D.layout()
+    p = np.zeros(n)
+    for (w, b, ci, co) in convs:
+        p[w:w + ci * co * 9] = D.bf16(rng.normal(0, np.sqrt(2.0 / (9 * ci)), ci * co * 9))
+        p[b:b + co] = rng.normal(0, 0.05, co)
+    p[ow:ow + 16] = rng.normal(0, 0.1, 16)
+    x = rng.uniform(0, 2, (2, 1, 16, 16))
+    t = rng.uniform(0, 2, (2, 1, 16, 16))
+    wts = [1.0, 4.0, 16.0, 64.0]
+    loss, g, y = D.loss_and_grads(p, x, t, weights=wts)
+    # the loss itself, from its definition
+    ref, ys, ts = 0.0, y, t
+    for s, w in enumerate(wts):
+        if s:
+            ys, ts = D.pool(ys), D.pool(ts)
+        ref += w * np.mean((ys - ts) ** 2)
+    assert abs(loss - ref) <= 1e-12 * ref
+    for i in [ob, ow, ow + 7, convs[13][1] + 2, convs[2][1]]:
+        h = 1e-6
+        a, b = p.copy(), p.copy()
+        a[i] += h
+        b[i] -= h
+        fd = (D.loss_and_grads(a, x, t, wts)[0] - D.loss_and_grads(b, x, t, wts)[0]) / (2 * h)
+        assert abs(fd - g[i]) <= 1e-6 * max(1.0, abs(fd)), (i, fd, g[i])

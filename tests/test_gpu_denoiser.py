@@ -97,3 +97,26 @@ def test_gradients_against_oracle_full_size():
         assert rel(g[wo:wo + ci * co * 9], g_o[wo:wo + ci * co * 9]) <= 1e-4, ("weights", k)
         assert rel(g[bo:bo + co], g_o[bo:bo + co]) <= 1e-4, ("bias", k)
     assert rel(g[ow:ow + 17], g_o[ow:ow + 17]) <= 1e-4
+
+
+def test_multiscale_loss_gradients_against_oracle():
+    """The multi-scale training loss (weights 4^s over the output and three
+    2x2 poolings) on the device against the oracle: loss 1e-5, gradients
+    1e-4, as the mean-squared-error test."""
+    import torch
+    net, p, x, t, xd, td = _net()
+    wts = [1.0, 4.0, 16.0, 64.0]
+    net.set_loss(wts)
+    loss, g = net.gradients(xd.data_ptr(), td.data_ptr(), 2)
+    loss_o, g_o, _ = D.loss_and_grads(p.astype(np.float64), x, t, weights=wts)
+    assert abs(loss - loss_o) <= 1e-5 * abs(loss_o)
+    convs, ow, ob, n = D.layout()
+    for k, (wo, bo, ci, co) in enumerate(convs):
+        assert rel(g[wo:wo + ci * co * 9], g_o[wo:wo + ci * co * 9]) <= 1e-4, ("weights", k)
+        assert rel(g[bo:bo + co], g_o[bo:bo + co]) <= 1e-4, ("bias", k)
+    assert rel(g[ow:ow + 17], g_o[ow:ow + 17]) <= 1e-4
+    # back to the mean squared error
+    net.set_loss(None)
+    loss_m, _ = net.gradients(xd.data_ptr(), td.data_ptr(), 2)
+    loss_mo, _, _ = D.loss_and_grads(p.astype(np.float64), x, t)
+    assert abs(loss_m - loss_mo) <= 1e-5 * abs(loss_mo)
