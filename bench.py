@@ -227,7 +227,7 @@ def build_workload(n, form, seed):
     calc = SpaceChargeCalc2p5D(*GRID, form={"learned": "plain", "learned-fp32": "fp32"}.get(form, form))
     if form in ("learned", "learned-fp32"):
         from orbit_gb300.denoiser import default_network
-        calc.setDenoiser(default_network(), 10, 1e-3)
+        calc.setDenoiser(default_network(size=GRID[0]), 10, 1e-3)
     lat = wl_lattice(calc)
     return soa, bunch, calc, lat
 
@@ -305,6 +305,59 @@ def learned_report(calc, ms_per_turn, n, n_equal=10_000_000, turns=10, form="pla
             "growth_dev_plain_same_n": (np.array(growth["plain_%d" % n]) / ref - 1).tolist(),
             "judge": state, "judge_this_run": calc.getDenoiserState(),
             "network_shape": "4-level conv encoder-decoder, 302,561 parameters, BF16 weights, shipped training"}
+
+
+def ring_learned_report(calc, ms_per_turn, n, turns=100, form="fp32"):
+    """The learned form on the large ring (the shipped convolutional
+    network on the 256 x 256 grid) against the plain form at the ring's
+    1.6e7 particles: one turn's time of each, and the rms-emittance growth
+    over `turns` turns of plain 1.6e7, plain n and learned n (same beam,
+    same lattice)."""
+    import numpy as np
+    import torch
+    from bunch import BunchTwissAnalysis
+    from orbit_gb300 import workloads as W
+    from orbit_gb300.denoiser import default_network
+    from spacecharge import SpaceChargeCalc2p5D
+
+    def em(b):
+        tw = BunchTwissAnalysis()
+        tw.analyzeBunch(b)
+        return np.array([tw.getEmittance(0), tw.getEmittance(1)])
+
+    def setup(npart, with_net):
+        b = W.make_bunch(W.c5_coords(npart, seed=78), WL["intensity"] / npart)
+        c = SpaceChargeCalc2p5D(*GRID, form=form if with_net else "plain")
+        if with_net:
+            c.setDenoiser(default_network(size=GRID[0]), 10, 1e-3)
+        with quiet():
+            lat = W.ring_lattice(c)
+        return b, c, lat
+
+    b, c, lat = setup(WL["n"], False)
+    lat.trackBunchTurns(b, 1)  # records and captures
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lat.trackBunchTurns(b, 2)
+    b._device_bunch().sync()
+    plain_ms = (time.perf_counter() - t0) / 2 * 1e3
+    growth, state = {}, None
+    for name, npart, with_net in (("plain_%d" % WL["n"], WL["n"], False), ("plain_%d" % n, n, False),
+                                  ("learned_%d" % n, n, True)):
+        b, c, lat = setup(npart, with_net)
+        e0 = em(b)
+        lat.trackBunchTurns(b, turns)
+        growth[name] = (em(b) / e0).tolist()
+        if with_net:
+            state = c.getDenoiserState()
+    ref = np.array(growth["plain_%d" % WL["n"]])
+    return {"plain_particles": WL["n"], "plain_ms_per_turn": plain_ms,
+            "speedup_vs_plain_same_beam": plain_ms / ms_per_turn,
+            "emittance_growth_turns": turns, "emittance_growth": growth,
+            "growth_dev_learned": (np.array(growth["learned_%d" % n]) / ref - 1).tolist(),
+            "growth_dev_plain_same_n": (np.array(growth["plain_%d" % n]) / ref - 1).tolist(),
+            "judge": state, "judge_this_run": calc.getDenoiserState(),
+            "network_shape": "the shipped 128 x 128-trained convolutional network run on the 256 x 256 grid"}
 
 
 def cpu_reference_rate(n_sample, turns, warmup, threads):
@@ -395,7 +448,11 @@ def run_ours(args):
         dist = tdist
     os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("CUDA_VISIBLE_DEVICES", ""))
     torch.cuda.init()
-    n = args.n if args.n else (100_000 if args.form.startswith("learned") else WL["n"])
+    # the learned forms run at 1/100 (FODO, the network's training ratio) or
+    # 1/40 (the ring's 256 x 256 grid: the same particles per cell as the
+    # 1e5 training inputs on 128 x 128) of the plain form's particles
+    n_learned = 100_000 if WL["name"] == "fodo" else WL["n"] // 40
+    n = args.n if args.n else (n_learned if args.form.startswith("learned") else WL["n"])
     TRAFFIC.n = n
     soa, bunch, calc, lat = build_workload(n, args.form, seed=1000 + rank)
     prog = lat.fusedProgram(bunch)
@@ -495,7 +552,7 @@ def run_ours(args):
         # the forward's time (one 128 x 128 image per kick: latency-bound)
         bf16 = measured_bf16_tflops()
         tf32_peak = bf16 / 2.0 if bf16 else 1900.0 / 2.0
-        tflops = DENOISER_GFLOP_128 * 1e-3 / (per_launch_ms * 1e-3)
+        tflops = DENOISER_GFLOP_128 * (GRID[0] * GRID[1] / 16384.0) * 1e-3 / (per_launch_ms * 1e-3)
         roofline.update({"bound": "tensor", "achieved": tflops, "peak": tf32_peak, "unit": "TFLOP/s",
                          "frac": tflops / tf32_peak, "traffic": None,
                          "peak_source": "half the measured bf16 GEMM rate (MEASURED_PEAKS.json bf16_tflops)"
@@ -546,13 +603,16 @@ def run_ours(args):
     kicks_done, green_done = calc._calc.counters()
     green_rate = green_done / kicks_done if kicks_done else None
     learned = None
-    if args.form.startswith("learned"):
+    if args.form.startswith("learned") and WL["name"] == "ring":
+        learned = {} if args.no_report else ring_learned_report(calc, ms_per_turn=total_ms / args.steps, n=n,
+                                                                  form="fp32" if args.form == "learned-fp32" else "plain")
+    elif args.form.startswith("learned"):
         learned = {} if args.no_report else learned_report(calc, ms_per_turn=total_ms / args.steps, n=n,
                                                              form="fp32" if args.form == "learned-fp32" else "plain")
         # the network's arithmetic rate (TF32 tensor-core MMAs on BF16 weights)
         net_ms, net_l = prof.get("learn_network", (0.0, 0))
         if net_ms > 0:
-            gflop = DENOISER_GFLOP_128
+            gflop = DENOISER_GFLOP_128 * (GRID[0] * GRID[1] / 16384.0)
             tflops = gflop / (net_ms / net_l)
             bf16_peak = measured_bf16_tflops()
             learned["network"] = {"gflop_per_forward": gflop, "ms_per_forward": net_ms / net_l,

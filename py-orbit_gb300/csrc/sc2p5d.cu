@@ -17,6 +17,12 @@ namespace orbit {
 
 static const int kMaxSmem = 220 * 1024;
 
+// Thread bound of the single-bunch shared-memory deposit (one block per SM
+// holds the 128x128 grid): 65536 / ORBIT_DEP_THREADS registers per thread.
+#ifndef ORBIT_DEP_THREADS
+#define ORBIT_DEP_THREADS 768
+#endif
+
 bool make_fft_plan(int n, FftPlan& pl) {
   pl.n = n;
   pl.nst = 0;
@@ -567,7 +573,7 @@ __device__ __forceinline__ void deposit_plain_body(const double* __restrict__ x,
 }
 
 template <bool SMEM>
-__global__ void __launch_bounds__(768) k_deposit_plain(const double* __restrict__ x, const double* __restrict__ y,
+__global__ void __launch_bounds__(ORBIT_DEP_THREADS) k_deposit_plain(const double* __restrict__ x, const double* __restrict__ y,
                                 const double* __restrict__ z, const double* __restrict__ msize, int n,
                                 const ScState* st, unsigned long long* g_rho, unsigned long long* g_z,
                                 double ms_uniform, double qscale, int nx, int ny, int nz, int K) {

@@ -263,11 +263,15 @@ DATA = os.path.join(os.path.dirname(__file__), "data")
 DEFAULT = "denoiser_128x128.npy"
 
 
-def default_network(max_batch=1):
-    """The shipped network for 128 x 128 grids, trained by `train_default`
+def default_network(max_batch=1, size=128):
+    """The shipped network, trained by `train_default` on 128 x 128 images
     (6,000 synthetic-beam pairs and 2,376 tracked-beam pairs, 10 epochs,
-    batch 16, Adam 1e-3 with cosine decay) on this library's own kernels."""
-    net = DeviceDenoiser(128, 128, max_batch=max_batch, seed=5)
+    batch 16, Adam 1e-3 with cosine decay) on this library's own kernels.
+    The network is convolutional, so the same weights run on a size x size
+    grid (size a multiple of 8); they were trained at about 6 input
+    particles per cell (1e5 particles on 128 x 128), so a larger grid wants
+    proportionally more particles (4e5 on 256 x 256)."""
+    net = DeviceDenoiser(size, size, max_batch=max_batch, seed=5)
     net.set_params(np.load(os.path.join(DATA, DEFAULT)))
     return net
 
