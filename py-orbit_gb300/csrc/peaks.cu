@@ -59,6 +59,60 @@ static double dmul_rate(double* out, cudaEvent_t e0, cudaEvent_t e1) {
   return (double)blocks * threads * iters * (HW + SW) / (best * 1e-3) / 1e9;
 }
 
+// Operand classes of the device check of sf::mul / add / fma / scale2,
+// drawn from a counter hash (splitmix64) of the case index.
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ double normal_operand(uint64_t r, uint64_t r2, int spread) {
+  const int e = (int)(r2 % (uint64_t)(2 * spread + 1)) - spread;
+  const double x = sf::from_bits((r >> 12) | ((uint64_t)(1023 + e) << 52));
+  return (r2 >> 63) ? -x : x;
+}
+
+// One case per thread and loop step; counts[0..3] = mismatches of mul, add,
+// fma and scale2 against the FP64 instructions (__dmul_rn, __dadd_rn,
+// __fma_rn, and a multiply by the power of two), NaN matching any NaN.
+__global__ void k_softf64_check(long long n, uint64_t seed, unsigned long long* counts) {
+  unsigned long long bad[4] = {0, 0, 0, 0};
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const uint64_t h = mix64(seed ^ (uint64_t)i);
+    uint64_t r[6];
+    for (int q = 0; q < 6; ++q) r[q] = mix64(h + (uint64_t)q);
+    const int cls = (int)(i % 10), sp = (int)((i / 10) % 4);
+    const int spread = sp == 0 ? 1000 : (sp == 1 ? 60 : (sp == 2 ? 5 : 0));
+    double a = normal_operand(r[0], r[1], spread), b = normal_operand(r[2], r[3], spread),
+           c = normal_operand(r[4], r[5], spread);
+    switch (cls) {
+      case 1: c = -__dmul_rn(a, b); break;                                               // total cancellation
+      case 2: c = sf::from_bits(sf::bits(-__dmul_rn(a, b)) ^ (r[5] & 0xFF)); break;     // near cancellation
+      case 3: b = sf::from_bits(sf::bits(-a) ^ (r[3] & 0xFFF)); break;                   // add cancellation
+      case 4: b = sf::from_bits(sf::bits(a) ^ (r[3] & 0xF)); break;                      // close significands
+      case 5: a = sf::from_bits(r[0] | (1ull << 52)); b = sf::from_bits((r[2] & 0x3FFFFFF000ull) | 0x3FF0000000000000ull); break;  // short b: ties
+      case 6: b = sf::from_bits(sf::bits(b) & ~((1ull << ((r[3] >> 58) % 52)) - 1)); break;
+      case 7: c = __dmul_rn(__dmul_rn(a, b), 0x1p-53) * ((r[5] & 1) ? 1.5 : 0.5); break;  // fma ties
+      case 8: a = sf::from_bits(r[0]); b = sf::from_bits(r[2]); c = sf::from_bits(r[4]); break;
+      case 9: a = (r[0] & 1) ? 0.0 : -0.0; break;
+      default: break;
+    }
+    const double m1 = __dmul_rn(a, b), m2 = sf::mul(a, b);
+    const double s1 = __dadd_rn(a, b), s2 = sf::add(a, b);
+    const double f1 = __fma_rn(a, b, c), f2 = sf::fma(a, b, c);
+    const int k = (r[5] & 2) ? 1 : -1;
+    const double k1 = __dmul_rn(a, k > 0 ? 2.0 : 0.5), k2 = sf::scale2(a, k);
+    bad[0] += !(sf::bits(m1) == sf::bits(m2) || (m1 != m1 && m2 != m2));
+    bad[1] += !(sf::bits(s1) == sf::bits(s2) || (s1 != s1 && s2 != s2));
+    bad[2] += !(sf::bits(f1) == sf::bits(f2) || (f1 != f1 && f2 != f2));
+    bad[3] += !(sf::bits(k1) == sf::bits(k2) || (k1 != k1 && k2 != k2));
+  }
+  for (int q = 0; q < 4; ++q)
+    if (bad[q]) atomicAdd(counts + q, bad[q]);
+}
+
 __global__ void k_copy(const double2* __restrict__ a, double2* __restrict__ b, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     b[i] = a[i];
@@ -143,5 +197,24 @@ extern "C" int orbit_device_mul_rates(double* fp64_gmul, double* int_gmul, doubl
   cudaEventDestroy(e1);
   if (*fp64_gmul < 0 || *int_gmul < 0 || *mixed_gmul < 0)
     return set_error(ORBIT_ERR_CUDA, "orbit_device_mul_rates: kernel failed");
+  return ORBIT_OK;
+}
+
+// Device check of the integer-pipe binary64 routines against the FP64
+// instructions on n generated cases (operand classes in k_softf64_check).
+extern "C" int orbit_softf64_check(long long n, unsigned long long seed, long long* mismatches) {
+  if (n < 0 || !mismatches) return set_error(ORBIT_ERR_ARG, "orbit_softf64_check: bad argument");
+  unsigned long long* d = nullptr;
+  ORBIT_CUDA(cudaMalloc(&d, 4 * sizeof(unsigned long long)));
+  cudaError_t e = cudaMemset(d, 0, 4 * sizeof(unsigned long long));
+  if (e == cudaSuccess) {
+    k_softf64_check<<<num_sms() * 4, 256>>>(n, (uint64_t)seed, d);
+    e = cudaGetLastError();
+  }
+  unsigned long long h[4] = {0, 0, 0, 0};
+  if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_error(e, "orbit_softf64_check");
+  for (int q = 0; q < 4; ++q) mismatches[q] = (long long)h[q];
   return ORBIT_OK;
 }

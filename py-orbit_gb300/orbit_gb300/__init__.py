@@ -41,6 +41,14 @@ def device_mul_rates():
     return a.value, b.value, c.value
 
 
+def softf64_check(n, seed=1):
+    """Mismatch counts (mul, add, fma, scale2) of the integer-pipe binary64
+    routines against the FP64 instructions on n generated device cases."""
+    out = (ctypes.c_longlong * 4)()
+    call("orbit_softf64_check", ctypes.c_longlong(n), ctypes.c_ulonglong(seed), out)
+    return tuple(out)
+
+
 def _ptr_array(arrs):
     return (_dp * 6)(*[a.ctypes.data_as(_dp) for a in arrs])
 

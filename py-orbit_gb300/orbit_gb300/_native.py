@@ -63,6 +63,7 @@ _SIGS = {
     "orbit_version": (ctypes.c_char_p, []),
     "orbit_device_peaks": (ctypes.c_int, [_dp, _dp]),
     "orbit_device_mul_rates": (ctypes.c_int, [_dp, _dp, _dp]),
+    "orbit_softf64_check": (ctypes.c_int, [ctypes.c_longlong, ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_longlong)]),
     "orbit_bunch_create": (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.c_int]),
     "orbit_bunch_destroy": (ctypes.c_int, [_vp]),
     "orbit_bunch_upload": (ctypes.c_int, [_vp, ctypes.POINTER(_dp), ctypes.c_int]),
