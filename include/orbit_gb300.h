@@ -122,6 +122,21 @@ int orbit_sc2p5d_get_grid(orbit_sc2p5d_t* c, int which, double* host_out);
 /* lim = {xmin,xmax,ymin,ymax,zmin,zmax,dx,dy,dz,xy_ratio,total_macrosize} */
 int orbit_sc2p5d_get_limits(orbit_sc2p5d_t* c, double* lim);
 int orbit_sc2p5d_get_sizes(const orbit_sc2p5d_t* c, int* nx, int* ny, int* nz, int* form);
+/* The Green rebuild and the convolution of each kick (forward rows with the
+ * line-density finalization, columns with the Green multiply, backward
+ * rows) as one cooperative launch with two grid-wide barriers (on = 1, the
+ * default where the device supports cooperative launches), or as separate
+ * kernels (on = 0; always for SpaceChargeCalc2p5Drb).  *active (optional)
+ * receives whether the fused launch will run.  Applies to kicks enqueued
+ * afterwards: a program keeps the form its graph was recorded with.  The
+ * same results either way.  No counterpart in the reference (the solve of
+ * PoissonSolverFFT2D.cc:174-256). */
+int orbit_sc2p5d_set_fused_conv(orbit_sc2p5d_t* c, int on, int* active);
+/* The fused convolution's barrier waits: the limit in polls (>= 1; default
+ * 2^20, about 0.1 s), and a block withheld from the first barrier (-1:
+ * none), a test hook with which the other blocks' waits run out: they
+ * return, and the next status check of the bunch reports ORBIT_ERR_DEVICE. */
+int orbit_sc2p5d_set_conv_wait(orbit_sc2p5d_t* c, long long polls, int withhold);
 /* ---- bunch diagnostics on the device (src/orbit/BunchDiagnostics) ---- */
 /* BunchTwissAnalysis::analyzeBunch (BunchTwissAnalysis.cc:49-140): out[29] =
  * {count, total macrosize, <c_i> [6], <c_i c_j> for i >= j [21, row i holds

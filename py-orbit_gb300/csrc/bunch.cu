@@ -131,6 +131,9 @@ int check_status(orbit_bunch_t* b) {
   ORBIT_CUDA(cudaMemsetAsync(b->d_status, 0, sizeof(unsigned), b->stream));
   ORBIT_CUDA(cudaStreamSynchronize(b->stream));
   if (st & ST_NAN) return set_error(ORBIT_ERR_NAN, "non-finite particle coordinate found by the extrema scan");
+  if (st & ST_SYNC)
+    return set_error(ORBIT_ERR_DEVICE,
+                     "fused convolution: a grid-wide barrier ran out of its wait limit; the kick's potential is invalid");
   if (st & ST_EXTENT)
     return set_error(ORBIT_ERR_EXTENT,
                      "SpaceChargeCalc2p5D: the bunch min and max sizes are wrong (zero extent); kick skipped");

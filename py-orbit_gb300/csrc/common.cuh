@@ -33,6 +33,7 @@ enum : unsigned {
   ST_EXTENT = 1u,   // zero beam extent at an SC kick
   ST_NAN = 2u,      // non-finite coordinate
   ST_RANGE = 4u,    // grid index out of range (should not happen)
+  ST_SYNC = 8u,     // a grid-wide barrier of the fused convolution ran out of its wait limit
 };
 
 int num_sms();

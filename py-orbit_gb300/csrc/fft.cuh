@@ -21,11 +21,18 @@ template <typename T> struct CT;
 template <> struct CT<double> { typedef double2 t; };
 template <> struct CT<float> { typedef float2 t; };
 
-template <typename C>
-__device__ __forceinline__ C c_mul(C a, C b) {
-  C r;
-  r.x = a.x * b.x - a.y * b.y;
-  r.y = a.x * b.y + a.y * b.x;
+// Complex product with explicit roundings (the same bits in every kernel
+// that inlines it): re = fma(a.x, b.x, -(a.y b.y)), im = fma(a.x, b.y, a.y b.x).
+__device__ __forceinline__ double2 c_mul(double2 a, double2 b) {
+  double2 r;
+  r.x = __fma_rn(a.x, b.x, -__dmul_rn(a.y, b.y));
+  r.y = __fma_rn(a.x, b.y, __dmul_rn(a.y, b.x));
+  return r;
+}
+__device__ __forceinline__ float2 c_mul(float2 a, float2 b) {
+  float2 r;
+  r.x = __fmaf_rn(a.x, b.x, -__fmul_rn(a.y, b.y));
+  r.y = __fmaf_rn(a.x, b.y, __fmul_rn(a.y, b.x));
   return r;
 }
 template <typename C>
@@ -100,6 +107,46 @@ __device__ typename CT<T>::t* block_fft_pow2(typename CT<T>::t* a, typename CT<T
     C* tmp = a;
     a = b;
     b = tmp;
+  }
+  return a;
+}
+
+// Power-of-two length N = 2^LOGN fixed at compile time, one radix-2
+// butterfly per thread (threads >= N/2; the others only synchronise):
+// unrolled stages with constant strides, each thread's twiddle of every
+// stage read once into registers (W_{2L}^j = tw[j << (LOGN-1-s)], j = t mod
+// L), stages from lg0 on (lg0 = 1 when the caller staged the half-zero
+// input as for block_fft_pow2).  The same operations per butterfly as
+// fft_stage_pow2<T, 2, INV>, so the same results.
+template <typename T, bool INV, int LOGN>
+__device__ __forceinline__ typename CT<T>::t* block_fft_fixed(typename CT<T>::t* a, typename CT<T>::t* b,
+                                                              const typename CT<T>::t* __restrict__ tw, int lg0) {
+  typedef typename CT<T>::t C;
+  constexpr int N = 1 << LOGN, H2 = N / 2;
+  const int t = threadIdx.x;
+  C w[LOGN];
+#pragma unroll
+  for (int s = 1; s < LOGN; ++s) {
+    w[s] = tw[(t & ((1 << s) - 1)) << (LOGN - 1 - s)];
+    if (INV) w[s].y = -w[s].y;
+  }
+#pragma unroll
+  for (int s = 0; s < LOGN; ++s) {
+    if (s >= lg0) {
+      if (t < H2) {
+        const int L = 1 << s;
+        const int j = t & (L - 1);
+        C x0 = a[t], x1 = a[t + H2];
+        if (s > 0) x1 = c_mul(x1, w[s]);
+        C* out = b + ((t - j) << 1) + j;
+        out[0] = c_add(x0, x1);
+        out[L] = c_sub(x0, x1);
+      }
+      __syncthreads();
+      C* tmp = a;
+      a = b;
+      b = tmp;
+    }
   }
   return a;
 }

@@ -96,9 +96,10 @@ __global__ void k_green_fill(const ScState* st, double* g, int nx2, int ny2, int
 // is complete; an eager Green rebuild ran before it, a graph branch reads
 // no flag).  The line density accumulator is cleared for the next deposit.
 template <typename G>
-__device__ __noinline__ void finalize_block(ScState* st, G* zacc, int nz, double* lam, float* lam_f) {
+__device__ __noinline__ void finalize_block(ScState* st, G* zacc, int nz, double* lam, float* lam_f,
+                                            bool reset_dirty = true) {
   if (threadIdx.x == 0) {
-    st->green_dirty = 0;
+    if (reset_dirty) st->green_dirty = 0;
     st->n_kicks += 1;
   }
   __shared__ double s_part[32];
@@ -151,6 +152,25 @@ __device__ __noinline__ void finalize_block(ScState* st, G* zacc, int nz, double
   }
 }
 
+// Loads of data that other blocks of the same launch wrote (the fused
+// convolution): from L2, never from a stale L1 line.
+template <bool CG, typename C>
+__device__ __forceinline__ C ldx(const C* p) {
+  if (CG) return __ldcg(p);
+  return *p;
+}
+
+// Green function value of the doubled grid at row iX <= nx2/2, column j
+// (mirrored as green_fill_body writes it): the same operations, so the
+// same bits.
+__device__ __forceinline__ double green_value(double sdx, double sdy, int iX, int j, int ny2) {
+  const int iY = j <= ny2 / 2 ? j : ny2 - j;
+  if (iX == 0 && iY == 0) return 0.0;
+  double rX = __dmul_rn((double)iX, sdx), rY = __dmul_rn((double)iY, sdy);
+  double r2 = __dadd_rn(__dmul_rn(rX, rX), __dmul_rn(rY, rY));
+  return __ddiv_rn(-log(r2), 2.0);
+}
+
 // Row transforms along y (length N = ny2) of two real rows per block:
 // z = a + i b, Z = FFT(z), A_k = (Z_k + conj Z_{N-k})/2, B_k = (Z_k - conj Z_{N-k})/(2i).
 // SRC 0: Green rows (double, full length; rows 0..nx2/2 transformed, the
@@ -159,32 +179,46 @@ __device__ __noinline__ void finalize_block(ScState* st, G* zacc, int nz, double
 // SRC 2: fp32 rho
 // SRC 3: a double grid of nrows x ncols, read only (the raw density of a
 //        learned-closure check)
+// SRC 4: Green rows as SRC 0, the function evaluated in place (the fused
+//        convolution)
 // The deposit grid (SRC 1, 2) is cleared as it is read, ready for the next
 // deposit, and one extra block (the last) finalizes the line density.
-// gate (SRC 0): as for k_green_fill.
-template <typename T, int SRC>
+// gate (SRC 0): as for k_green_fill.  sa, stw_in: the block's work buffers
+// and its staged twiddles (the fused convolution stages them once);
+// otherwise the dynamic shared memory and a copy made here.
+template <typename T, int SRC, int LOGN = 0>
 __device__ __forceinline__ void rows_fwd_body(ScState* st, void* src, double* rho_out, typename CT<T>::t* hat,
                                               const typename CT<T>::t* __restrict__ tw, const FftPlan& pl,
                                               int nrows, int ncols, int H, int gate, void* zacc, int nz,
-                                              double* lam, float* lam_f, int blk, int nblk) {
+                                              double* lam, float* lam_f, int blk, int nblk,
+                                              typename CT<T>::t* sa = nullptr,
+                                              const typename CT<T>::t* stw_in = nullptr, bool reset_dirty = true) {
   typedef typename CT<T>::t C;
   if (SRC == 0 && gate && !st->green_dirty) return;
   if (st->skip) return;
   if ((SRC == 1 || SRC == 2) && blk == nblk - 1) {
-    if (SRC == 1) finalize_block(st, (unsigned long long*)zacc, nz, lam, (float*)nullptr);
-    else finalize_block(st, (float*)zacc, nz, lam, lam_f);
+    if (SRC == 1) finalize_block(st, (unsigned long long*)zacc, nz, lam, (float*)nullptr, reset_dirty);
+    else finalize_block(st, (float*)zacc, nz, lam, lam_f, reset_dirty);
     return;
   }
   extern __shared__ unsigned char smem_raw[];
-  C* a = reinterpret_cast<C*>(smem_raw);
+  C* a = sa ? sa : reinterpret_cast<C*>(smem_raw);
   C* b = a + pl.n;
   const int N = pl.n;
-  C* stw = b + N;
-  load_twiddles(stw, tw, N);
+  const C* stw = stw_in;
+  if (!stw) {
+    load_twiddles(b + N, tw, N);
+    stw = b + N;
+  }
   int r0 = 2 * blk, r1 = r0 + 1;
   double iq = st->inv_qscale;
+  double gsx = 0.0, gsy = 0.0;
+  if (SRC == 4) {
+    gsx = st->sdx;
+    gsy = st->sdy;
+  }
   // deposit rows: columns ncols..N-1 are the zero padding
-  const bool hz = SRC != 0 && fft_halfzero_ok<T>(pl, ncols);
+  const bool hz = SRC != 0 && SRC != 4 && fft_halfzero_ok<T>(pl, ncols);
   for (int j = threadIdx.x; j < (hz ? N / 2 : N); j += blockDim.x) {
     T va = (T)0, vb = (T)0;
     if (j < ncols) {
@@ -196,6 +230,9 @@ __device__ __forceinline__ void rows_fwd_body(ScState* st, void* src, double* rh
         const double* g = (const double*)src;
         va = (T)g[(size_t)r0 * ncols + j];
         if (r1 < nrows) vb = (T)g[(size_t)r1 * ncols + j];
+      } else if (SRC == 4) {
+        va = (T)green_value(gsx, gsy, r0, j, N);
+        if (r1 < nrows) vb = (T)green_value(gsx, gsy, r1, j, N);
       } else if (SRC == 1) {
         long long* q = (long long*)src;
         double da = (double)q[(size_t)r0 * ncols + j] * iq;
@@ -233,7 +270,9 @@ __device__ __forceinline__ void rows_fwd_body(ScState* st, void* src, double* rh
     }
   }
   __syncthreads();
-  C* Z = hz ? block_fft_pow2<T, false>(a, b, pl, stw, 1) : block_fft<T>(a, b, pl, stw, false);
+  C* Z;
+  if constexpr (LOGN > 0) Z = block_fft_fixed<T, false, LOGN>(a, b, stw, hz ? 1 : 0);
+  else Z = hz ? block_fft_pow2<T, false>(a, b, pl, stw, 1) : block_fft<T>(a, b, pl, stw, false);
   for (int k = threadIdx.x; k < H; k += blockDim.x) {
     C zk = Z[k], zc = c_conj(Z[(N - k) % N]);
     C A, B;
@@ -244,7 +283,7 @@ __device__ __forceinline__ void rows_fwd_body(ScState* st, void* src, double* rh
     B.y = -(zk.x - zc.x) * (T)0.5;
     hat[(size_t)r0 * H + k] = A;
     if (r1 < nrows) hat[(size_t)r1 * H + k] = B;
-    if (SRC == 0) {
+    if (SRC == 0 || SRC == 4) {
       // Green rows 0..nrows-1 = 0..nx2/2; row nx2 - r repeats row r
       const int nfull = 2 * (nrows - 1);
       if (r0 > 0 && r0 < nrows - 1) hat[(size_t)(nfull - r0) * H + k] = A;
@@ -267,23 +306,29 @@ __global__ void k_rows_fwd(ScState* st, void* src, double* rho_out, typename CT<
 // MODE 1: forward, multiply by the Green spectrum with the log-scale
 //         correction (PoissonSolverFFT2D.cc:212-242), backward; rows >= nin
 //         are zero on input and only rows < nin are kept on output.
-template <typename T, int MODE>
+// CG: hat and green were written by other blocks of the same launch (the
+// fused convolution); sa, stw_in as for rows_fwd_body.
+template <typename T, int MODE, bool CG = false, int LOGN = 0>
 __device__ __forceinline__ void cols_body(ScState* st, typename CT<T>::t* hat, typename CT<T>::t* __restrict__ green,
                                           const typename CT<T>::t* __restrict__ tw, const FftPlan& pl, int nin,
-                                          int H, int ny2, int gate, int k) {
+                                          int H, int ny2, int gate, int k, typename CT<T>::t* sa = nullptr,
+                                          const typename CT<T>::t* stw_in = nullptr) {
   typedef typename CT<T>::t C;
   if (MODE == 0 && gate && !st->green_dirty) return;
   if (st->skip) return;
   extern __shared__ unsigned char smem_raw[];
-  C* a = reinterpret_cast<C*>(smem_raw);
+  C* a = sa ? sa : reinterpret_cast<C*>(smem_raw);
   C* b = a + pl.n;
   const int N = pl.n;
-  C* stw = b + N;
-  load_twiddles(stw, tw, N);
+  const C* stw = stw_in;
+  if (!stw) {
+    load_twiddles(b + N, tw, N);
+    stw = b + N;
+  }
   const bool hz = MODE == 1 && fft_halfzero_ok<T>(pl, nin);
   for (int r = threadIdx.x; r < (hz ? N / 2 : N); r += blockDim.x) {
     C v;
-    if (r < nin) v = hat[(size_t)r * H + k];
+    if (r < nin) v = ldx<CG>(hat + (size_t)r * H + k);
     else { v.x = (T)0; v.y = (T)0; }
     if (hz) {
       a[2 * r] = v;
@@ -293,7 +338,9 @@ __device__ __forceinline__ void cols_body(ScState* st, typename CT<T>::t* hat, t
     }
   }
   __syncthreads();
-  C* F = hz ? block_fft_pow2<T, false>(a, b, pl, stw, 1) : block_fft<T>(a, b, pl, stw, false);
+  C* F;
+  if constexpr (LOGN > 0) F = block_fft_fixed<T, false, LOGN>(a, b, stw, hz ? 1 : 0);
+  else F = hz ? block_fft_pow2<T, false>(a, b, pl, stw, 1) : block_fft<T>(a, b, pl, stw, false);
   if (MODE == 0) {
     for (int r = threadIdx.x; r < N; r += blockDim.x) green[(size_t)k * N + r] = F[r];
     if (k == 0 && threadIdx.x == 0) st->n_green += 1;
@@ -301,7 +348,7 @@ __device__ __forceinline__ void cols_body(ScState* st, typename CT<T>::t* hat, t
   }
   double s = st->scale;
   for (int r = threadIdx.x; r < N; r += blockDim.x) {
-    C g = green[(size_t)k * N + r];
+    C g = ldx<CG>(green + (size_t)k * N + r);
     T gr;
     if (r == 0 && k == 0) {
       double re00 = (double)g.x;
@@ -317,7 +364,9 @@ __device__ __forceinline__ void cols_body(ScState* st, typename CT<T>::t* hat, t
   }
   __syncthreads();
   C* other = (F == a) ? b : a;
-  C* R = block_fft<T>(F, other, pl, stw, true);
+  C* R;
+  if constexpr (LOGN > 0) R = block_fft_fixed<T, true, LOGN>(F, other, stw, 0);
+  else R = block_fft<T>(F, other, pl, stw, true);
   for (int r = threadIdx.x; r < nin; r += blockDim.x) hat[(size_t)r * H + k] = R[r];
 }
 
@@ -330,30 +379,34 @@ __global__ void k_cols(ScState* st, typename CT<T>::t* hat, typename CT<T>::t* _
 // Backward row transforms (c2r, two rows per block) and the 1/(4 nx ny)
 // normalisation onto the nx x ny potential (PoissonSolverFFT2D.cc:244-255).
 // Imaginary parts at the self-conjugate k = 0 and k = N/2 are ignored.
-template <typename T>
+template <typename T, bool CG = false, int LOGN = 0>
 __device__ __forceinline__ void rows_inv_body(ScState* st, const typename CT<T>::t* __restrict__ hat,
                                               const typename CT<T>::t* __restrict__ tw, const FftPlan& pl,
                                               int nrows, int ny, int H, double denom, double* phi, float* phi_f,
-                                              int blk) {
+                                              int blk, typename CT<T>::t* sa = nullptr,
+                                              const typename CT<T>::t* stw_in = nullptr) {
   typedef typename CT<T>::t C;
   if (st->skip) return;
   extern __shared__ unsigned char smem_raw[];
-  C* a = reinterpret_cast<C*>(smem_raw);
+  C* a = sa ? sa : reinterpret_cast<C*>(smem_raw);
   C* b = a + pl.n;
   const int N = pl.n;
-  C* stw = b + N;
-  load_twiddles(stw, tw, N);
+  const C* stw = stw_in;
+  if (!stw) {
+    load_twiddles(b + N, tw, N);
+    stw = b + N;
+  }
   int r0 = 2 * blk, r1 = r0 + 1;
   bool has1 = r1 < nrows;
   for (int k = threadIdx.x; k < N; k += blockDim.x) {
     C A, B;
     if (k < H) {
-      A = hat[(size_t)r0 * H + k];
-      B = has1 ? hat[(size_t)r1 * H + k] : C{(T)0, (T)0};
+      A = ldx<CG>(hat + (size_t)r0 * H + k);
+      B = has1 ? ldx<CG>(hat + (size_t)r1 * H + k) : C{(T)0, (T)0};
       if (k == 0 || 2 * k == N) { A.y = (T)0; B.y = (T)0; }
     } else {
-      A = c_conj(hat[(size_t)r0 * H + (N - k)]);
-      B = has1 ? c_conj(hat[(size_t)r1 * H + (N - k)]) : C{(T)0, (T)0};
+      A = c_conj(ldx<CG>(hat + (size_t)r0 * H + (N - k)));
+      B = has1 ? c_conj(ldx<CG>(hat + (size_t)r1 * H + (N - k))) : C{(T)0, (T)0};
     }
     C z;  // A + i B
     z.x = A.x - B.y;
@@ -361,7 +414,9 @@ __device__ __forceinline__ void rows_inv_body(ScState* st, const typename CT<T>:
     a[k] = z;
   }
   __syncthreads();
-  C* R = block_fft<T>(a, b, pl, stw, true);
+  C* R;
+  if constexpr (LOGN > 0) R = block_fft_fixed<T, true, LOGN>(a, b, stw, 0);
+  else R = block_fft<T>(a, b, pl, stw, true);
   unsigned long long amax = 0ull;  // bits of max |phi| (non-negative doubles order like their bits)
   for (int j = threadIdx.x; j < ny; j += blockDim.x) {
     double va = denom * (double)R[j].x;
@@ -389,6 +444,118 @@ __global__ void k_rows_inv(ScState* st, const typename CT<T>::t* __restrict__ ha
                            const typename CT<T>::t* __restrict__ tw, FftPlan pl, int nrows, int ny, int H,
                            double denom, double* phi, float* phi_f) {
   rows_inv_body<T>(st, hat, tw, pl, nrows, ny, H, denom, phi, phi_f, blockIdx.x);
+}
+
+// ---------------------------------------------------------------------
+// Fused convolution: the Green rebuild (when the set-up marked it), the
+// forward rows of the deposit with the line-density finalization, the
+// column transforms with the Green multiply and the backward rows in one
+// cooperative launch (all blocks resident), the phases separated by two
+// grid-wide barriers.  Every block stages both twiddle tables once.
+// ---------------------------------------------------------------------
+struct ConvArgs {
+  ScState* st;
+  unsigned* status;         // the bunch's status word (ST_SYNC)
+  void* src;                // the deposit grid (fixed point or FP32)
+  double* rho;
+  void* hat;                // nx2 x H complex work spectrum
+  void* green;              // nx2 x H complex Green spectrum
+  void* gscr;               // nx2 x H complex: the Green row spectra
+  const void* twx;
+  const void* twy;
+  FftPlan plx, ply;
+  int nx, ny, nz, H, nx2, ny2;
+  void* zacc;               // line-density accumulator
+  double* lam;
+  float* lam_f;
+  double* phi;
+  float* phi_f;
+  double denom;             // 1 / (nx2 ny2)
+  long long wait_polls;     // barrier wait limit
+  int withhold;             // test hook: this block skips the first barrier (-1: none)
+};
+
+// Grid-wide barrier on a counter zeroed by the kick's set-up: every block
+// arrives once (its earlier writes fenced) and waits until all have; the
+// wait is bounded by `polls`, after which the block sets ST_SYNC and
+// returns false.
+__device__ __forceinline__ bool conv_barrier(unsigned* cnt, unsigned nblk, long long polls, unsigned* status) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(cnt, 1u);
+    int ok = 1;
+    long long i = 0;
+    for (;;) {
+      unsigned v;
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(cnt) : "memory");
+      if (v >= nblk) break;
+      if (++i > polls) {
+        ok = 0;
+        break;
+      }
+      __nanosleep(32);
+    }
+    if (!ok) atomicOr(status, (unsigned)ST_SYNC);
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// T double: plain form (fixed-point deposit); float: FP32 form.  LOGN > 0:
+// square power-of-two doubled grid nx2 = ny2 = 2^LOGN, transforms
+// specialised at compile time (block_fft_fixed); 0: any supported size.
+template <typename T, int LOGN>
+__global__ void k_conv_fused(ConvArgs A) {
+  typedef typename CT<T>::t C;
+  constexpr int SRC = sizeof(T) == 8 ? 1 : 2;
+  extern __shared__ unsigned char smem_raw[];
+  ScState* st = A.st;
+  if (st->skip) return;  // set by the set-up: the same in every block
+  const int nmax = A.nx2 > A.ny2 ? A.nx2 : A.ny2;
+  C* a = reinterpret_cast<C*>(smem_raw);  // a, b: nmax each
+  C* stx = a + 2 * nmax;
+  C* sty = stx + A.nx2;
+  load_twiddles(stx, (const C*)A.twx, A.nx2);
+  load_twiddles(sty, (const C*)A.twy, A.ny2);
+  const int dirty = st->green_dirty;  // read before the first barrier, reset after it
+  __syncthreads();
+  C* hat = (C*)A.hat;
+  C* green = (C*)A.green;
+  C* gscr = (C*)A.gscr;
+  // phase 1: deposit rows (+ the finalization item), Green rows
+  const int nrp = (A.nx + 1) / 2, ngp = dirty ? (A.nx + 2) / 2 : 0;
+  for (int it = blockIdx.x; it < nrp + 1 + ngp; it += gridDim.x) {
+    if (it <= nrp)
+      rows_fwd_body<T, SRC, LOGN>(st, A.src, A.rho, hat, nullptr, A.ply, A.nx, A.ny, A.H, 1, A.zacc, A.nz, A.lam,
+                                  A.lam_f, it, nrp + 1, a, sty, false);
+    else
+      rows_fwd_body<T, 4, LOGN>(st, nullptr, nullptr, gscr, nullptr, A.ply, A.nx + 1, A.ny2, A.H, 0, nullptr, 0,
+                                nullptr, nullptr, it - nrp - 1, ngp, a, sty);
+    __syncthreads();
+  }
+  if ((int)blockIdx.x == A.withhold) return;
+  if (!conv_barrier(&st->conv_bar[0], gridDim.x, A.wait_polls, A.status)) return;
+  if (blockIdx.x == 0 && threadIdx.x == 0 && dirty) st->green_dirty = 0;
+  // phase 2: per column, the Green column (when rebuilt), then the deposit's
+  // forward transform, the multiply and the backward transform
+  for (int k = blockIdx.x; k < A.H; k += gridDim.x) {
+    if (dirty) {
+      cols_body<T, 0, true, LOGN>(st, gscr, green, nullptr, A.plx, A.nx2, A.H, A.ny2, 0, k, a, stx);
+      __syncthreads();
+    }
+    cols_body<T, 1, true, LOGN>(st, hat, green, nullptr, A.plx, A.nx, A.H, A.ny2, 1, k, a, stx);
+    __syncthreads();
+  }
+  if (!conv_barrier(&st->conv_bar[1], gridDim.x, A.wait_polls, A.status)) return;
+  // phase 3: backward rows onto phi
+  for (int it = blockIdx.x; it < nrp; it += gridDim.x) {
+    rows_inv_body<T, true, LOGN>(st, hat, nullptr, A.ply, A.nx, A.ny, A.H, A.denom, A.phi, A.phi_f, it, a, sty);
+    __syncthreads();
+  }
 }
 
 // Plain form: phi and lambda as 64-bit integers phi * 2^sphi, lambda *
@@ -1060,6 +1227,114 @@ static size_t band_smem(int nx, int ny, int nz) {
   return 8 * ((size_t)(rpb + 2) * ny + nz);
 }
 
+// Fused convolution geometry: threads for the longer transform, shared
+// memory for two work buffers and both twiddle tables, and the largest
+// number of work items of a phase (deposit rows + finalization + Green
+// rows; columns; backward rows).
+static int conv_threads(const orbit_sc2p5d_t* c) {
+  int tx = fft_threads(c->plan_x), ty = fft_threads(c->plan_y);
+  return tx > ty ? tx : ty;
+}
+
+template <typename T>
+static size_t conv_smem(const orbit_sc2p5d_t* c) {
+  int nmax = c->nx2 > c->ny2 ? c->nx2 : c->ny2;
+  return sizeof(typename CT<T>::t) * (size_t)(2 * nmax + c->nx2 + c->ny2);
+}
+
+static int conv_items(const orbit_sc2p5d_t* c) {
+  int rows = (c->nx + 1) / 2 + 1 + (c->nx + 2) / 2;
+  return rows > c->H ? rows : c->H;
+}
+
+// The fused kernel for the calculator's grid: specialised transforms for
+// square power-of-two doubled grids of 128 to 1024 points, else generic.
+template <typename T>
+static void (*conv_kernel(const orbit_sc2p5d_t* c))(ConvArgs) {
+  if (c->nx2 == c->ny2 && c->plan_x.pow2) {
+    switch (c->nx2) {
+      case 128: return k_conv_fused<T, 7>;
+      case 256: return k_conv_fused<T, 8>;
+      case 512: return k_conv_fused<T, 9>;
+      case 1024: return k_conv_fused<T, 10>;
+      default: break;
+    }
+  }
+  return k_conv_fused<T, 0>;
+}
+
+// The co-resident block count of the fused convolution (0: it cannot run
+// and the separate kernels are used).
+template <typename T>
+static int init_conv_fused(orbit_sc2p5d_t* c) {
+  const void* fn = (const void*)conv_kernel<T>(c);
+  size_t sm = conv_smem<T>(c);
+  c->conv_blocks = 0;
+  int coop = 0;
+  ORBIT_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, 0));
+  if (!coop || sm > (size_t)kMaxSmem) return ORBIT_OK;
+  if (sm > 48 * 1024) ORBIT_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  int per_sm = 0;
+  ORBIT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, conv_threads(c), sm));
+  c->conv_blocks = per_sm * num_sms();
+  return ORBIT_OK;
+}
+
+static bool use_conv_fused(const orbit_sc2p5d_t* c) {
+  return c->fused_conv && c->conv_blocks > 0 && !c->rb && c->d_gscratch && c->d_hat && c->d_green;
+}
+
+// The Green rebuild, the forward rows, the convolution and the backward
+// rows as one cooperative launch (k_conv_fused).
+template <typename T>
+static int enqueue_conv_fused(orbit_sc2p5d_t* c, orbit_bunch_t* b, cudaStream_t s, int* nl) {
+  ConvArgs A;
+  std::memset(&A, 0, sizeof(A));
+  A.st = c->d_st;
+  A.status = b->d_status;
+  A.rho = c->d_rho;
+  A.hat = c->d_hat;
+  A.green = c->d_green;
+  A.gscr = c->d_gscratch;
+  A.twx = c->d_tw_x;
+  A.twy = c->d_tw_y;
+  A.plx = c->plan_x;
+  A.ply = c->plan_y;
+  A.nx = c->nx; A.ny = c->ny; A.nz = c->nz; A.H = c->H; A.nx2 = c->nx2; A.ny2 = c->ny2;
+  A.lam = c->d_lam;
+  A.phi = c->d_phi;
+  A.denom = 1.0 / (c->nx2 * c->ny2);
+  A.wait_polls = c->conv_wait_polls;
+  A.withhold = c->conv_withhold;
+  const bool plain = c->form == ORBIT_FORM_PLAIN;
+  if (plain) {
+    A.src = c->d_rho_q;
+    A.zacc = c->d_z_q;
+  } else {
+    A.src = c->d_rho_f;
+    A.zacc = c->d_z_f;
+    A.lam_f = c->d_lam_f;
+    A.phi_f = c->d_phi_f;
+  }
+  int items = conv_items(c);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(items < c->conv_blocks ? items : c->conv_blocks);
+  cfg.blockDim = dim3(conv_threads(c));
+  cfg.dynamicSmemBytes = conv_smem<T>(c);
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  ORBIT_PB("fft_conv_fused", s);
+  cudaError_t e = cudaLaunchKernelEx(&cfg, conv_kernel<T>(c), A);
+  ORBIT_PE(s);
+  if (e != cudaSuccess) return cuda_error(e, "sc2p5d fused convolution");
+  ++*nl;
+  return ORBIT_OK;
+}
+
 // Forward row transforms of the deposit (plus one block finalizing the line
 // density).
 template <typename T>
@@ -1329,7 +1604,7 @@ SetupArgs sc_setup_args(const orbit_sc2p5d_t* c, const DepScales& d, const orbit
 }
 
 cudaGraphConditionalHandle sc_green_cond(orbit_sc2p5d_t* c, cudaStream_t s, bool pending) {
-  if (!c->aux || !c->d_gscratch) return 0;
+  if (!c->aux || !c->d_gscratch || use_conv_fused(c)) return 0;  // the fused convolution rebuilds in place
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   cudaGraph_t g = nullptr;
   if (cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, nullptr, nullptr, nullptr) != cudaSuccess) return 0;
@@ -1426,7 +1701,8 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
   sc_clear_pending(c);
   cudaGraphNode_t branch_node = nullptr;
   int rc;
-  if (!cond) {
+  const bool fused = use_conv_fused(c);
+  if (!cond && !fused) {
     // before the deposit: the work spectrum is free to hold the row spectra
     rc = plain ? enqueue_green<double>(c, s, 1, c->d_hat, &nl) : enqueue_green<float>(c, s, 1, c->d_hat, &nl);
     if (rc) return rc;
@@ -1515,8 +1791,13 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
     rc = add_green_branch(c, s, cond, &branch_node);
     if (rc) return rc;
   }
-  rc = plain ? enqueue_rows_fwd<double>(c, s, &nl) : enqueue_rows_fwd<float>(c, s, &nl);
-  if (rc) return rc;
+  if (fused) {
+    rc = plain ? enqueue_conv_fused<double>(c, b, s, &nl) : enqueue_conv_fused<float>(c, b, s, &nl);
+    if (rc) return rc;
+  } else {
+    rc = plain ? enqueue_rows_fwd<double>(c, s, &nl) : enqueue_rows_fwd<float>(c, s, &nl);
+    if (rc) return rc;
+  }
   if (c->rb) {
     // beam centre, a_bunch and the derivative grid from the finished grids
     ORBIT_PB("rb_analysis", s);
@@ -1528,8 +1809,10 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
   }
   if (branch_node)  // the column transforms read the Green spectrum
     ORBIT_CUDA(cudaStreamUpdateCaptureDependencies(s, &branch_node, nullptr, 1, cudaStreamAddCaptureDependencies));
-  rc = plain ? enqueue_conv<double>(c, s, &nl) : enqueue_conv<float>(c, s, &nl);
-  if (rc) return rc;
+  if (!fused) {
+    rc = plain ? enqueue_conv<double>(c, s, &nl) : enqueue_conv<float>(c, s, &nl);
+    if (rc) return rc;
+  }
   if (dn_check) {
     // the raw deposit solved beside the denoised one (in the calculator's
     // own precision: its Green spectrum and twiddles), and the judge
@@ -1624,14 +1907,16 @@ static int init_attrs(orbit_sc2p5d_t* c) {
     if (c->smem_kick && kick > 48 * 1024)
       ORBIT_CUDA(cudaFuncSetAttribute(k_kick_plain<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem));
     int nmax = c->nx2 > c->ny2 ? c->nx2 : c->ny2;
-    return set_fft_attrs<double>(nmax);
+    int rc = set_fft_attrs<double>(nmax);
+    return rc ? rc : init_conv_fused<double>(c);
   }
   if (c->smem_deposit && dep > 48 * 1024)
     ORBIT_CUDA(cudaFuncSetAttribute(k_deposit_fp32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem));
   if (c->smem_kick && kick > 48 * 1024)
     ORBIT_CUDA(cudaFuncSetAttribute(k_kick_fp32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem));
   int nmax = c->nx2 > c->ny2 ? c->nx2 : c->ny2;
-  return set_fft_attrs<float>(nmax);
+  int rc = set_fft_attrs<float>(nmax);
+  return rc ? rc : init_conv_fused<float>(c);
 }
 
 }  // namespace orbit
@@ -1916,6 +2201,20 @@ int orbit_sc2p5d_get_sizes(const orbit_sc2p5d_t* c, int* nx, int* ny, int* nz, i
   return ORBIT_OK;
 }
 
+int orbit_sc2p5d_set_fused_conv(orbit_sc2p5d_t* c, int on, int* active) {
+  if (!c) return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_set_fused_conv: null handle");
+  c->fused_conv = on != 0;
+  if (active) *active = use_conv_fused(c) ? 1 : 0;
+  return ORBIT_OK;
+}
+
+int orbit_sc2p5d_set_conv_wait(orbit_sc2p5d_t* c, long long polls, int withhold) {
+  if (!c || polls < 1 || withhold < -1) return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_set_conv_wait: bad argument");
+  c->conv_wait_polls = polls;
+  c->conv_withhold = withhold;
+  return ORBIT_OK;
+}
+
 int orbit_sc2p5d_fields(orbit_sc2p5d_t* c, int n, const double* x, const double* y, const double* z, double* ex,
                         double* ey, double* lam) {
   if (!c || n < 0 || (n > 0 && (!x || !y || !z || !ex || !ey || !lam)))
@@ -2008,6 +2307,7 @@ extern "C" int orbit_sc2p5d_track_static(double* dev_coords, int n, int stride, 
     return set_error(ORBIT_ERR_UNSUPPORTED,
                      "orbit_sc2p5d_track_static: grid above the static scratch limit (nx, ny <= 128, nz <= 256)");
   orbit_sc2p5d_t c;
+  c.fused_conv = false;  // the separate solve kernels: no Green scratch is carved here
   c.nx = nx; c.ny = ny; c.nz = nz; c.form = ORBIT_FORM_PLAIN;
   c.nx2 = 2 * nx; c.ny2 = 2 * ny; c.H = ny + 1;
   c.xy_ratio0 = xy_ratio > 0. ? xy_ratio : 1.0;

@@ -38,6 +38,9 @@ struct ScState {
   double dn_err;
   unsigned long long dn_checks, dn_trips;
   double dn_sum;
+  // arrival counters of the fused convolution's two grid-wide barriers,
+  // zeroed by every kick's set-up
+  unsigned conv_bar[2];
 };
 
 // Inside test of a conducting boundary (BaseBoundary2D.cc:144-151,
@@ -129,6 +132,13 @@ struct orbit_sc2p5d {
   cudaGraph_t pending_graph = nullptr;
   bool smem_deposit = false, smem_kick = false;
   bool band_deposit = false;              // plain form: the grid in row bands (too large for one block)
+  // the Green rebuild and the convolution in one cooperative launch (0
+  // blocks: the separate kernels), the barrier wait limit in polls and a
+  // block withheld from the first barrier (test hook, -1: none)
+  bool fused_conv = true;
+  int conv_blocks = 0;
+  long long conv_wait_polls = 1ll << 20;
+  int conv_withhold = -1;
   // SpaceChargeCalc2p5Drb (plain form): longitudinal kick from the smoothed
   // derivative of the line density
   bool rb = false;

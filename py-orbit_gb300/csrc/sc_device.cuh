@@ -78,6 +78,8 @@ static __device__ __noinline__ void sc_setup_scalar(ScState* st, unsigned* statu
   double yMin = dkey_inv(key[2]), yMax = dkey_inv(key[3]);
   double zMin = dkey_inv(key[4]), zMax = dkey_inv(key[5]);
   for (int c = 0; c < 3; ++c) { st->key[2 * c] = ~0ull; st->key[2 * c + 1] = 0ull; }
+  st->conv_bar[0] = 0u;
+  st->conv_bar[1] = 0u;
   if (sa.bnd) {
     // a boundary fixes the transverse grid to its extents; only z comes
     // from the bunch (SpaceChargeCalc2p5D.cc:174-196)

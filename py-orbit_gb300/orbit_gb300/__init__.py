@@ -206,6 +206,19 @@ class DeviceSC2p5D:
         call("orbit_sc2p5d_get_limits", self.h, lim.ctypes.data_as(_dp))
         return lim
 
+    def set_fused_conv(self, on: bool) -> bool:
+        """The convolution of each kick as one cooperative launch (True, the
+        default) or as separate kernels; returns whether the fused launch
+        will run (orbit_sc2p5d_set_fused_conv)."""
+        act = ctypes.c_int()
+        call("orbit_sc2p5d_set_fused_conv", self.h, int(bool(on)), ctypes.byref(act))
+        return bool(act.value)
+
+    def set_conv_wait(self, polls: int, withhold: int = -1):
+        """Barrier wait limit of the fused convolution and its test hook
+        (orbit_sc2p5d_set_conv_wait)."""
+        call("orbit_sc2p5d_set_conv_wait", self.h, int(polls), int(withhold))
+
     def set_denoiser(self, dn, check_every: int = 10, bound: float = 0.05):
         """Learned closure (orbit_sc2p5d_set_denoiser); dn None removes it."""
         call("orbit_sc2p5d_set_denoiser", self.h, dn.h if dn is not None else None, int(check_every), float(bound))

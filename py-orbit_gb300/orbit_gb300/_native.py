@@ -83,6 +83,8 @@ _SIGS = {
     "orbit_sc2p5d_get_grid": (ctypes.c_int, [_vp, ctypes.c_int, _dp]),
     "orbit_sc2p5d_get_limits": (ctypes.c_int, [_vp, _dp]),
     "orbit_sc2p5d_get_sizes": (ctypes.c_int, [_vp] + [ctypes.POINTER(ctypes.c_int)] * 4),
+    "orbit_sc2p5d_set_fused_conv": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+    "orbit_sc2p5d_set_conv_wait": (ctypes.c_int, [_vp, ctypes.c_longlong, ctypes.c_int]),
     "orbit_sc2p5d_counters": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]),
     "orbit_sc2p5drb_create": (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                              ctypes.c_double]),
