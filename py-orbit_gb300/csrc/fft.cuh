@@ -37,6 +37,24 @@ __device__ __forceinline__ float2 c_mul(float2 a, float2 b) {
 }
 template <typename C>
 __device__ __forceinline__ C c_add(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+
+// Radix-2 butterfly with a twiddle, o0 = x0 + w x1, o1 = x0 - w x1, in six
+// fused multiply-adds instead of a product and four additions:
+// o0 = fma(x1.x, w.x, fma(-x1.y, w.y, x0.x)) (and the imaginary part
+// likewise), o1 = fma(2, x0, -o0) = 2 x0 - o0, one rounding each.  The FP64
+// pipe bounds the transforms on GB300.
+__device__ __forceinline__ void bfly2_tw(double2 x0, double2 x1, double2 w, double2& o0, double2& o1) {
+  o0.x = __fma_rn(x1.x, w.x, __fma_rn(-x1.y, w.y, x0.x));
+  o0.y = __fma_rn(x1.x, w.y, __fma_rn(x1.y, w.x, x0.y));
+  o1.x = __fma_rn(2.0, x0.x, -o0.x);
+  o1.y = __fma_rn(2.0, x0.y, -o0.y);
+}
+__device__ __forceinline__ void bfly2_tw(float2 x0, float2 x1, float2 w, float2& o0, float2& o1) {
+  o0.x = __fmaf_rn(x1.x, w.x, __fmaf_rn(-x1.y, w.y, x0.x));
+  o0.y = __fmaf_rn(x1.x, w.y, __fmaf_rn(x1.y, w.x, x0.y));
+  o1.x = __fmaf_rn(2.0f, x0.x, -o0.x);
+  o1.y = __fmaf_rn(2.0f, x0.y, -o0.y);
+}
 template <typename C>
 __device__ __forceinline__ C c_sub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
 template <typename C>
@@ -56,6 +74,13 @@ __device__ __forceinline__ void fft_stage_pow2(const typename CT<T>::t* __restri
     C x[P];
 #pragma unroll
     for (int q = 0; q < P; ++q) x[q] = a[t + q * Np];
+    if (P == 2 && L > 1) {
+      C w = tw[j << lgtw];
+      if (INV) w.y = -w.y;
+      C* out = b + ((t - j) * 2) + j;
+      bfly2_tw(x[0], x[1], w, out[0], out[L]);
+      continue;
+    }
     if (L > 1) {  // the first stage has only W^0 = 1
 #pragma unroll
       for (int q = 1; q < P; ++q) {
@@ -116,8 +141,8 @@ __device__ typename CT<T>::t* block_fft_pow2(typename CT<T>::t* a, typename CT<T
 // unrolled stages with constant strides, each thread's twiddle of every
 // stage read once into registers (W_{2L}^j = tw[j << (LOGN-1-s)], j = t mod
 // L), stages from lg0 on (lg0 = 1 when the caller staged the half-zero
-// input as for block_fft_pow2).  The same operations per butterfly as
-// fft_stage_pow2<T, 2, INV>, so the same results.
+// input as for block_fft_pow2).  The same butterflies as
+// fft_stage_pow2<T, 2, INV> (bfly2_tw), so the same results.
 template <typename T, bool INV, int LOGN>
 __device__ __forceinline__ typename CT<T>::t* block_fft_fixed(typename CT<T>::t* a, typename CT<T>::t* b,
                                                               const typename CT<T>::t* __restrict__ tw, int lg0) {
@@ -137,10 +162,13 @@ __device__ __forceinline__ typename CT<T>::t* block_fft_fixed(typename CT<T>::t*
         const int L = 1 << s;
         const int j = t & (L - 1);
         C x0 = a[t], x1 = a[t + H2];
-        if (s > 0) x1 = c_mul(x1, w[s]);
         C* out = b + ((t - j) << 1) + j;
-        out[0] = c_add(x0, x1);
-        out[L] = c_sub(x0, x1);
+        if (s > 0) {
+          bfly2_tw(x0, x1, w[s], out[0], out[L]);
+        } else {
+          out[0] = c_add(x0, x1);
+          out[L] = c_sub(x0, x1);
+        }
       }
       __syncthreads();
       C* tmp = a;
