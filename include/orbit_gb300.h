@@ -53,12 +53,12 @@ int orbit_device_peaks(double* fp64_tflops, double* copy_gbs);
  * alone, on the integer pipes alone (the library's correctly rounded
  * integer multiply) and half on each; no counterpart in the reference. */
 int orbit_device_mul_rates(double* fp64_gmul, double* int_gmul, double* mixed_gmul);
-/* Checks the integer-pipe binary64 multiply, add, fused multiply-add and
- * x 2^+-1 against the FP64 instructions on n generated cases (random
- * normal operands over several exponent spreads, cancellations, rounding
- * ties, zeros and random bit patterns); mismatches[0..3] receives the
- * number of results whose bits differ, per operation.  No counterpart in
- * the reference. */
+/* Checks the integer-pipe binary64 multiply, add, fused multiply-add,
+ * x 2^+-1 and the double-to-float and float-to-double conversions against
+ * the hardware instructions on n generated cases (random normal operands
+ * over several exponent spreads, cancellations, rounding ties, zeros and
+ * random bit patterns); mismatches[0..5] receives the number of results
+ * whose bits differ, per operation.  No counterpart in the reference. */
 int orbit_softf64_check(long long n, unsigned long long seed, long long* mismatches);
 
 /* ------------------------------------------------------------------ */

@@ -74,11 +74,12 @@ __device__ __forceinline__ double normal_operand(uint64_t r, uint64_t r2, int sp
   return (r2 >> 63) ? -x : x;
 }
 
-// One case per thread and loop step; counts[0..3] = mismatches of mul, add,
-// fma and scale2 against the FP64 instructions (__dmul_rn, __dadd_rn,
-// __fma_rn, and a multiply by the power of two), NaN matching any NaN.
+// One case per thread and loop step; counts[0..5] = mismatches of mul, add,
+// fma, scale2, to_float and from_float against the hardware instructions
+// (__dmul_rn, __dadd_rn, __fma_rn, a multiply by the power of two,
+// __double2float_rn, the float-to-double conversion), NaN matching any NaN.
 __global__ void k_softf64_check(long long n, uint64_t seed, unsigned long long* counts) {
-  unsigned long long bad[4] = {0, 0, 0, 0};
+  unsigned long long bad[6] = {0, 0, 0, 0, 0, 0};
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const uint64_t h = mix64(seed ^ (uint64_t)i);
     uint64_t r[6];
@@ -108,8 +109,16 @@ __global__ void k_softf64_check(long long n, uint64_t seed, unsigned long long* 
     bad[1] += !(sf::bits(s1) == sf::bits(s2) || (s1 != s1 && s2 != s2));
     bad[2] += !(sf::bits(f1) == sf::bits(f2) || (f1 != f1 && f2 != f2));
     bad[3] += !(sf::bits(k1) == sf::bits(k2) || (k1 != k1 && k2 != k2));
+    // conversions: a over the float range (and exact ties), a random float
+    double t = (cls & 1) ? a : __dmul_rn(a, __longlong_as_double((long long)((uint64_t)(1023 + (int)(r[1] % 300) - 150) << 52)));
+    if (cls == 5) t = sf::from_bits((sf::bits(t) & ~((1ull << 29) - 1)) | (1ull << 28));
+    const float c1 = __double2float_rn(t), c2 = sf::to_float(t);
+    bad[4] += !(sf::fbits(c1) == sf::fbits(c2) || (c1 != c1 && c2 != c2));
+    const float rf = sf::from_fbits((uint32_t)r[4]);
+    const double e1 = (double)rf, e2 = sf::from_float(rf);
+    bad[5] += !(sf::bits(e1) == sf::bits(e2) || (e1 != e1 && e2 != e2));
   }
-  for (int q = 0; q < 4; ++q)
+  for (int q = 0; q < 6; ++q)
     if (bad[q]) atomicAdd(counts + q, bad[q]);
 }
 
@@ -205,16 +214,16 @@ extern "C" int orbit_device_mul_rates(double* fp64_gmul, double* int_gmul, doubl
 extern "C" int orbit_softf64_check(long long n, unsigned long long seed, long long* mismatches) {
   if (n < 0 || !mismatches) return set_error(ORBIT_ERR_ARG, "orbit_softf64_check: bad argument");
   unsigned long long* d = nullptr;
-  ORBIT_CUDA(cudaMalloc(&d, 4 * sizeof(unsigned long long)));
-  cudaError_t e = cudaMemset(d, 0, 4 * sizeof(unsigned long long));
+  ORBIT_CUDA(cudaMalloc(&d, 6 * sizeof(unsigned long long)));
+  cudaError_t e = cudaMemset(d, 0, 6 * sizeof(unsigned long long));
   if (e == cudaSuccess) {
     k_softf64_check<<<num_sms() * 4, 256>>>(n, (uint64_t)seed, d);
     e = cudaGetLastError();
   }
-  unsigned long long h[4] = {0, 0, 0, 0};
+  unsigned long long h[6] = {0, 0, 0, 0, 0, 0};
   if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
   cudaFree(d);
   if (e != cudaSuccess) return cuda_error(e, "orbit_softf64_check");
-  for (int q = 0; q < 4; ++q) mismatches[q] = (long long)h[q];
+  for (int q = 0; q < 6; ++q) mismatches[q] = (long long)h[q];
   return ORBIT_OK;
 }

@@ -175,13 +175,13 @@ __device__ __forceinline__ double green_value(double sdx, double sdy, int iX, in
 // z = a + i b, Z = FFT(z), A_k = (Z_k + conj Z_{N-k})/2, B_k = (Z_k - conj Z_{N-k})/(2i).
 // SRC 0: Green rows (double, full length; rows 0..nx2/2 transformed, the
 //        rest mirrored; nrows = nx2/2 + 1)
-// SRC 1: plain rho from the fixed-point grid (first ny columns, first nx rows)
-// SRC 2: fp32 rho
+// SRC 1: rho from the fixed-point grid (first ny columns, first nx rows;
+//        both forms)
 // SRC 3: a double grid of nrows x ncols, read only (the raw density of a
 //        learned-closure check)
 // SRC 4: Green rows as SRC 0, the function evaluated in place (the fused
 //        convolution)
-// The deposit grid (SRC 1, 2) is cleared as it is read, ready for the next
+// The deposit grid (SRC 1) is cleared as it is read, ready for the next
 // deposit, and one extra block (the last) finalizes the line density.
 // gate (SRC 0): as for k_green_fill.  sa, stw_in: the block's work buffers
 // and its staged twiddles (the fused convolution stages them once);
@@ -196,9 +196,8 @@ __device__ __forceinline__ void rows_fwd_body(ScState* st, void* src, double* rh
   typedef typename CT<T>::t C;
   if (SRC == 0 && gate && !st->green_dirty) return;
   if (st->skip) return;
-  if ((SRC == 1 || SRC == 2) && blk == nblk - 1) {
-    if (SRC == 1) finalize_block(st, (unsigned long long*)zacc, nz, lam, (float*)nullptr, reset_dirty);
-    else finalize_block(st, (float*)zacc, nz, lam, lam_f, reset_dirty);
+  if (SRC == 1 && blk == nblk - 1) {
+    finalize_block(st, (unsigned long long*)zacc, nz, lam, lam_f, reset_dirty);
     return;
   }
   extern __shared__ unsigned char smem_raw[];
@@ -244,18 +243,6 @@ __device__ __forceinline__ void rows_fwd_body(ScState* st, void* src, double* rh
           q[(size_t)r1 * ncols + j] = 0;
           rho_out[(size_t)r1 * ncols + j] = db;
           vb = (T)db;
-        }
-      } else {
-        float* q = (float*)src;
-        float fa = q[(size_t)r0 * ncols + j];
-        q[(size_t)r0 * ncols + j] = 0.0f;
-        rho_out[(size_t)r0 * ncols + j] = (double)fa;
-        va = (T)fa;
-        if (r1 < nrows) {
-          float fb = q[(size_t)r1 * ncols + j];
-          q[(size_t)r1 * ncols + j] = 0.0f;
-          rho_out[(size_t)r1 * ncols + j] = (double)fb;
-          vb = (T)fb;
         }
       }
     }
@@ -505,13 +492,14 @@ __device__ __forceinline__ bool conv_barrier(unsigned* cnt, unsigned nblk, long 
   return s_ok != 0;
 }
 
-// T double: plain form (fixed-point deposit); float: FP32 form.  LOGN > 0:
+// T double: plain form; float: FP32 form (both read the fixed-point
+// deposit).  LOGN > 0:
 // square power-of-two doubled grid nx2 = ny2 = 2^LOGN, transforms
 // specialised at compile time (block_fft_fixed); 0: any supported size.
 template <typename T, int LOGN>
 __global__ void k_conv_fused(ConvArgs A) {
   typedef typename CT<T>::t C;
-  constexpr int SRC = sizeof(T) == 8 ? 1 : 2;
+  constexpr int SRC = 1;  // both forms deposit in fixed point
   extern __shared__ unsigned char smem_raw[];
   ScState* st = A.st;
   if (st->skip) return;  // set by the set-up: the same in every block
@@ -805,40 +793,6 @@ __global__ void __launch_bounds__(768) k_deposit_band(const double* __restrict__
                     blockIdx.x / nb, gridDim.x / nb);
 }
 
-template <bool SMEM>
-__global__ void k_deposit_fp32(const double* __restrict__ x, const double* __restrict__ y,
-                               const double* __restrict__ z, const double* __restrict__ msize, int n,
-                               const ScState* st, float* g_rho, float* g_z, float m_uniform, int nx, int ny,
-                               int nz) {
-  DepConst d;
-  load_dep_const(d, st, nx, ny, nz);
-  if (d.skip) return;
-  extern __shared__ float s_accf[];
-  float* rho = g_rho;
-  float* zg = g_z;
-  if (SMEM) {
-    rho = s_accf;
-    zg = s_accf + nx * ny;
-    for (int i = threadIdx.x; i < nx * ny + nz; i += blockDim.x) s_accf[i] = 0.0f;
-    __syncthreads();
-  }
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    float m = msize ? (float)msize[i] : m_uniform;
-    deposit_fp32(d, rho, zg, x[i], y[i], z[i], m);
-  }
-  if (SMEM) {
-    __syncthreads();
-    for (int i = threadIdx.x; i < nx * ny; i += blockDim.x) {
-      float v = s_accf[i];
-      if (v != 0.0f) atomicAdd(g_rho + i, v);
-    }
-    for (int i = threadIdx.x; i < nz; i += blockDim.x) {
-      float v = s_accf[nx * ny + i];
-      if (v != 0.0f) atomicAdd(g_z + i, v);
-    }
-  }
-}
-
 // Kick (SpaceChargeCalc2p5D.cc:104-119): fixed-point gradient and line
 // density (kick_fixed), FP64 routine for the particles it declines.  With
 // lamd (2.5Drb) also the longitudinal kick of dE.
@@ -963,18 +917,6 @@ __global__ void k_learn_in(ScState* st, const unsigned long long* __restrict__ r
   }
 }
 
-// FP32 form: the deposit is a float grid of charges.
-__global__ void k_learn_in_f(ScState* st, const float* __restrict__ rho_f, float* __restrict__ img,
-                             double* __restrict__ raw, int n, double scale) {
-  if (st->skip) return;
-  if (blockIdx.x == 0 && threadIdx.x == 0) st->dn_sum = 0.0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    double v = (double)rho_f[i];
-    if (raw) raw[i] = v;
-    img[i] = (float)(v * scale);
-  }
-}
-
 // Sum of the network output clamped at zero (a density is not negative).
 // A network that reported a failed tensor-core wait (net_err != 0) produced
 // no valid output: the closure falls back to the plain deposit for good.
@@ -1011,17 +953,6 @@ __global__ void k_learn_out(ScState* st, const float* __restrict__ out, unsigned
   const double back = ((double)n / sum) / (scale * st->inv_qscale);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     rho_q[i] = (unsigned long long)llrint((double)fmaxf(out[i], 0.f) * back);
-}
-
-// FP32 form: the rescaled output written back as the float deposit.
-__global__ void k_learn_out_f(ScState* st, const float* __restrict__ out, float* __restrict__ rho_f, int n,
-                              double scale) {
-  if (st->skip || st->dn_fallback) return;
-  const double sum = st->dn_sum;
-  if (!(sum > 0.0)) return;
-  const double back = ((double)n / sum) / scale;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    rho_f[i] = (float)((double)fmaxf(out[i], 0.f) * back);
 }
 
 // State of the check solve: the kick's skip flag and log-scale term.
@@ -1181,7 +1112,6 @@ static int set_fft_attrs(int nmax) {
   if (bytes <= 48 * 1024) return ORBIT_OK;
   ORBIT_CUDA(cudaFuncSetAttribute(k_rows_fwd<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
   ORBIT_CUDA(cudaFuncSetAttribute(k_rows_fwd<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-  ORBIT_CUDA(cudaFuncSetAttribute(k_rows_fwd<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
   ORBIT_CUDA(cudaFuncSetAttribute(k_rows_fwd<T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
   ORBIT_CUDA(cudaFuncSetAttribute(k_cols<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
   ORBIT_CUDA(cudaFuncSetAttribute(k_cols<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
@@ -1306,16 +1236,10 @@ static int enqueue_conv_fused(orbit_sc2p5d_t* c, orbit_bunch_t* b, cudaStream_t 
   A.denom = 1.0 / (c->nx2 * c->ny2);
   A.wait_polls = c->conv_wait_polls;
   A.withhold = c->conv_withhold;
-  const bool plain = c->form == ORBIT_FORM_PLAIN;
-  if (plain) {
-    A.src = c->d_rho_q;
-    A.zacc = c->d_z_q;
-  } else {
-    A.src = c->d_rho_f;
-    A.zacc = c->d_z_f;
-    A.lam_f = c->d_lam_f;
-    A.phi_f = c->d_phi_f;
-  }
+  A.src = c->d_rho_q;
+  A.zacc = c->d_z_q;
+  A.lam_f = c->d_lam_f;  // FP32 form: float copies for its kick (null otherwise)
+  A.phi_f = c->d_phi_f;
   int items = conv_items(c);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(items < c->conv_blocks ? items : c->conv_blocks);
@@ -1346,13 +1270,8 @@ static int enqueue_rows_fwd(orbit_sc2p5d_t* c, cudaStream_t s, int* nl) {
   size_t smy = fft_smem<T>(c->ny2);
   int blocks = (c->nx + 1) / 2 + 1;
   ORBIT_PB("fft_rows_fwd", s);
-  if (c->form == ORBIT_FORM_PLAIN) {
-    k_rows_fwd<T, 1><<<blocks, thy, smy, s>>>(c->d_st, c->d_rho_q, c->d_rho, hat, twy, c->plan_y, c->nx, c->ny,
-                                              c->H, 1, c->d_z_q, c->nz, c->d_lam, nullptr);
-  } else {
-    k_rows_fwd<T, 2><<<blocks, thy, smy, s>>>(c->d_st, c->d_rho_f, c->d_rho, hat, twy, c->plan_y, c->nx, c->ny,
-                                              c->H, 1, c->d_z_f, c->nz, c->d_lam, c->d_lam_f);
-  }
+  k_rows_fwd<T, 1><<<blocks, thy, smy, s>>>(c->d_st, c->d_rho_q, c->d_rho, hat, twy, c->plan_y, c->nx, c->ny,
+                                            c->H, 1, c->d_z_q, c->nz, c->d_lam, c->d_lam_f);
   ORBIT_PE(s);
   ++*nl;
   ORBIT_LAUNCH_CHECK("sc2p5d rows");
@@ -1539,12 +1458,11 @@ static int max_threads_of(K kernel) {
   return a.maxThreadsPerBlock;
 }
 
-// Block-size limits of the particle kernels: deposit plain (shared, global),
-// deposit fp32 (shared, global), kick plain (shared, global), kick fp32.
-// Queried once, outside any stream capture (init_attrs).
+// Block-size limits of the particle kernels: deposit (shared, global), kick
+// plain (shared, global), kick fp32 (shared, global).  Queried once,
+// outside any stream capture (init_attrs).
 static const int* particle_kernel_threads() {
-  static const int mt[8] = {max_threads_of(k_deposit_plain<true>), max_threads_of(k_deposit_plain<false>),
-                            max_threads_of(k_deposit_fp32<true>), max_threads_of(k_deposit_fp32<false>),
+  static const int mt[6] = {max_threads_of(k_deposit_plain<true>), max_threads_of(k_deposit_plain<false>),
                             max_threads_of(k_kick_plain<true>), max_threads_of(k_kick_plain<false>),
                             max_threads_of(k_kick_fp32<true>), max_threads_of(k_kick_fp32<false>)};
   return mt;
@@ -1585,7 +1503,7 @@ DepScales sc_dep_scales(const orbit_sc2p5d_t* c, const orbit_bunch_t* b) {
 
 SetupArgs sc_setup_args(const orbit_sc2p5d_t* c, const DepScales& d, const orbit_boundary* bnd) {
   SetupArgs sa;
-  sa.inv_qscale = c->form == ORBIT_FORM_PLAIN ? d.inv_q : 1.0;
+  sa.inv_qscale = d.inv_q;  // both forms deposit in fixed point
   sa.nx = c->nx;
   sa.ny = c->ny;
   sa.nz = c->nz;
@@ -1707,14 +1625,13 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
     rc = plain ? enqueue_green<double>(c, s, 1, c->d_hat, &nl) : enqueue_green<float>(c, s, 1, c->d_hat, &nl);
     if (rc) return rc;
   }
-  size_t esz = plain ? sizeof(unsigned long long) : sizeof(float);
-  size_t sm = esz * ((size_t)c->nx * c->ny + c->nz);
+  // both forms: the exact fixed-point deposit
+  size_t sm = sizeof(unsigned long long) * ((size_t)c->nx * c->ny + c->nz);
   int blocks, threads;
   const int* mt_dep = particle_kernel_threads();
-  particle_geometry(c->smem_deposit ? sm : 0, n, mt_dep[(plain ? 0 : 2) + (c->smem_deposit ? 0 : 1)], &blocks,
-                    &threads);
+  particle_geometry(c->smem_deposit ? sm : 0, n, mt_dep[c->smem_deposit ? 0 : 1], &blocks, &threads);
   ORBIT_PB("deposit", s);
-  if (plain) {
+  {
     if (c->smem_deposit) {
       k_deposit_plain<true><<<blocks, threads, sm, s>>>(b->coord(0), b->coord(2), b->coord(4), msz, n, c->d_st,
                                                         c->d_rho_q, c->d_z_q, ds.ms_uniform, ds.S, c->nx, c->ny,
@@ -1737,15 +1654,6 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
                                                         c->d_rho_q, c->d_z_q, ds.ms_uniform, ds.S, c->nx, c->ny,
                                                         c->nz, ds.K);
     }
-  } else {
-    if (c->smem_deposit)
-      k_deposit_fp32<true><<<blocks, threads, sm, s>>>(b->coord(0), b->coord(2), b->coord(4), msz, n, c->d_st,
-                                                       c->d_rho_f, c->d_z_f, (float)b->sync.macrosize, c->nx,
-                                                       c->ny, c->nz);
-    else
-      k_deposit_fp32<false><<<blocks, threads, 0, s>>>(b->coord(0), b->coord(2), b->coord(4), msz, n, c->d_st,
-                                                       c->d_rho_f, c->d_z_f, (float)b->sync.macrosize, c->nx,
-                                                       c->ny, c->nz);
   }
   ORBIT_PE(s);
   ++nl;
@@ -1764,12 +1672,8 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
       int gb = (ng + 255) / 256;
       if (gb > num_sms() * 2) gb = num_sms() * 2;
       ORBIT_PB("learn_in", s);
-      if (plain)
-        k_learn_in<<<gb, 256, 0, s>>>(c->d_st, c->d_rho_q, c->d_dn_img, dn_check ? c->d_dn_raw : nullptr, ng,
-                                      dn_scale);
-      else
-        k_learn_in_f<<<gb, 256, 0, s>>>(c->d_st, c->d_rho_f, c->d_dn_img, dn_check ? c->d_dn_raw : nullptr, ng,
-                                        dn_scale);
+      k_learn_in<<<gb, 256, 0, s>>>(c->d_st, c->d_rho_q, c->d_dn_img, dn_check ? c->d_dn_raw : nullptr, ng,
+                                    dn_scale);
       ORBIT_PE(s);
       ORBIT_PB("learn_network", s);
       rc = orbit_denoiser_forward(c->dn, c->d_dn_img, c->d_dn_out, 1, (void*)s);
@@ -1777,10 +1681,7 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
       if (rc) return rc;
       ORBIT_PB("learn_out", s);
       k_learn_sum<<<gb, 256, 0, s>>>(c->d_st, c->d_dn_out, ng, dn_error_flag(c->dn));
-      if (plain)
-        k_learn_out<<<gb, 256, 0, s>>>(c->d_st, c->d_dn_out, c->d_rho_q, ng, dn_scale);
-      else
-        k_learn_out_f<<<gb, 256, 0, s>>>(c->d_st, c->d_dn_out, c->d_rho_f, ng, dn_scale);
+      k_learn_out<<<gb, 256, 0, s>>>(c->d_st, c->d_dn_out, c->d_rho_q, ng, dn_scale);
       ORBIT_PE(s);
       nl += 3;
       ORBIT_LAUNCH_CHECK("sc2p5d learned closure");
@@ -1848,7 +1749,7 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
     double lsf = c->rb ? sc_rb_long_factor(b->sync, length) : 0.0;
     BndShape bshape = bnd_shape_of(bnd);
     size_t smk = (plain ? sizeof(double) : sizeof(float)) * ((size_t)c->nx * c->ny + c->nz);
-    const int* mt_kick = particle_kernel_threads() + 4;
+    const int* mt_kick = particle_kernel_threads() + 2;
     particle_geometry(c->smem_kick ? smk : 0, n, mt_kick[(plain ? 0 : 2) + (c->smem_kick ? 0 : 1)], &blocks,
                       &threads);
     ORBIT_PB("kick", s);
@@ -1893,25 +1794,25 @@ cudaError_t sc_mark_used(orbit_sc2p5d_t* c, cudaStream_t s) {
 
 static int init_attrs(orbit_sc2p5d_t* c) {
   particle_kernel_threads();
-  size_t dep = (c->form == ORBIT_FORM_PLAIN ? 8 : 4) * ((size_t)c->nx * c->ny + c->nz);
+  // both forms deposit into the exact fixed-point grids (two 32-bit words
+  // per cell in shared memory); the FP32 form's kick reads a float copy
+  size_t dep = 8 * ((size_t)c->nx * c->ny + c->nz);
   size_t kick = (c->form == ORBIT_FORM_PLAIN ? 8 : 4) * ((size_t)c->nx * c->ny + c->nz);
   c->smem_deposit = dep <= (size_t)kMaxSmem;
   c->smem_kick = kick <= (size_t)kMaxSmem;
+  size_t bs = band_smem(c->nx, c->ny, c->nz);
+  c->band_deposit = !c->smem_deposit && bs <= (size_t)kMaxSmem;
+  if (c->band_deposit && bs > 48 * 1024)
+    ORBIT_CUDA(cudaFuncSetAttribute(k_deposit_band, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem));
+  if (c->smem_deposit && dep > 48 * 1024)
+    ORBIT_CUDA(cudaFuncSetAttribute(k_deposit_plain<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem));
   if (c->form == ORBIT_FORM_PLAIN) {
-    size_t bs = band_smem(c->nx, c->ny, c->nz);
-    c->band_deposit = !c->smem_deposit && bs <= (size_t)kMaxSmem;
-    if (c->band_deposit && bs > 48 * 1024)
-      ORBIT_CUDA(cudaFuncSetAttribute(k_deposit_band, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem));
-    if (c->smem_deposit && dep > 48 * 1024)
-      ORBIT_CUDA(cudaFuncSetAttribute(k_deposit_plain<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem));
     if (c->smem_kick && kick > 48 * 1024)
       ORBIT_CUDA(cudaFuncSetAttribute(k_kick_plain<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem));
     int nmax = c->nx2 > c->ny2 ? c->nx2 : c->ny2;
     int rc = set_fft_attrs<double>(nmax);
     return rc ? rc : init_conv_fused<double>(c);
   }
-  if (c->smem_deposit && dep > 48 * 1024)
-    ORBIT_CUDA(cudaFuncSetAttribute(k_deposit_fp32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem));
   if (c->smem_kick && kick > 48 * 1024)
     ORBIT_CUDA(cudaFuncSetAttribute(k_kick_fp32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem));
   int nmax = c->nx2 > c->ny2 ? c->nx2 : c->ny2;
@@ -1957,9 +1858,10 @@ int orbit_sc2p5d_create(orbit_sc2p5d_t** out, int nx, int ny, int nz, double xy_
   A((void**)&c->d_lam, sizeof(double) * nz);
   A((void**)&c->d_lamd, sizeof(double) * nz);
   A((void**)&c->d_gbuf, sizeof(double) * (size_t)c->nx2 * c->ny2);
+  // both forms: the fixed-point deposit grids
+  A((void**)&c->d_rho_q, sizeof(unsigned long long) * ng);
+  A((void**)&c->d_z_q, sizeof(unsigned long long) * nz);
   if (form == ORBIT_FORM_PLAIN) {
-    A((void**)&c->d_rho_q, sizeof(unsigned long long) * ng);
-    A((void**)&c->d_z_q, sizeof(unsigned long long) * nz);
     A((void**)&c->d_phi_fix, sizeof(long long) * ng);
     A((void**)&c->d_lam_fix, sizeof(long long) * nz);
     A(&c->d_hat, sizeof(double2) * nhat);
@@ -1968,8 +1870,6 @@ int orbit_sc2p5d_create(orbit_sc2p5d_t** out, int nx, int ny, int nz, double xy_
     if (e == cudaSuccess) c->d_tw_x = make_twiddles<double>(c->nx2, &e);
     if (e == cudaSuccess) c->d_tw_y = make_twiddles<double>(c->ny2, &e);
   } else {
-    A((void**)&c->d_rho_f, sizeof(float) * ng);
-    A((void**)&c->d_z_f, sizeof(float) * nz);
     A((void**)&c->d_phi_f, sizeof(float) * ng);
     A((void**)&c->d_lam_f, sizeof(float) * nz);
     A(&c->d_hat, sizeof(float2) * nhat);
@@ -2017,7 +1917,7 @@ int orbit_sc2p5d_destroy(orbit_sc2p5d_t* c) {
   if (c->used) cudaEventSynchronize(c->done);
   if (c->done) cudaEventDestroy(c->done);
   if (c->aux) cudaStreamDestroy(c->aux);
-  void* ptrs[] = {c->d_st, c->d_rho_q, c->d_z_q, c->d_rho_f, c->d_z_f, c->d_rho, c->d_phi, c->d_lam, c->d_lamd,
+  void* ptrs[] = {c->d_st, c->d_rho_q, c->d_z_q, c->d_rho, c->d_phi, c->d_lam, c->d_lamd,
                   c->d_phi_f, c->d_lam_f, c->d_hat, c->d_green, c->d_gbuf, c->d_gscratch, c->d_tw_x, c->d_tw_y,
                   c->d_phi_fix, c->d_lam_fix, c->d_dn_img, c->d_dn_out, c->d_dn_raw, c->d_dn_hat, c->d_dn_phi,
                   c->d_dn_st};

@@ -105,10 +105,8 @@ struct orbit_sc2p5d {
   int nx2 = 0, ny2 = 0, H = 0;   // doubled grid, H = ny2/2 + 1
   double xy_ratio0 = 1.0;
   orbit::ScState* d_st = nullptr;
-  unsigned long long* d_rho_q = nullptr;  // fixed-point deposit (plain form)
+  unsigned long long* d_rho_q = nullptr;  // fixed-point deposit (both forms)
   unsigned long long* d_z_q = nullptr;
-  float* d_rho_f = nullptr;               // FP32 deposit (fp32 form)
-  float* d_z_f = nullptr;
   double* d_rho = nullptr;                // user-visible rho (nx*ny)
   double* d_phi = nullptr;                // user-visible phi (nx*ny)
   double* d_lam = nullptr;                // user-visible line density (nz)

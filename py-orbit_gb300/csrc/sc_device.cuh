@@ -239,14 +239,42 @@ __device__ __forceinline__ void g1_index(T z, T zmin, T inv_dz, int nz, int& i0,
 // ---------------------------------------------------------------------
 struct KickConst {
   double xmin, ymin, inv_dx, inv_dy, zmin, zmax, inv_dz, fac;
-  // FP32 form: grid coordinates as one FMA, t = x inv_dx + c; the z range
-  // test on order-preserving integer keys; the float constants
+  // FP32 form: grid coordinates t = x inv_dx + c; the z range test on
+  // order-preserving integer keys; the float constants.  f32: the grid
+  // origin lies within four grid extents of the coordinate origin, so t is
+  // formed in float from the coordinate converted on the integer pipes:
+  // t = fma(xf, ih, ch) + fma(xf, il, cl), 1/dx = ih + il and c = ch + cl
+  // as float pairs, so that no rounding of a per-kick constant shifts or
+  // stretches the whole grid (the kick would then sample the field away
+  // from where the deposit put the charge); what is left are the unbiased
+  // roundings of x and of the two operations, a few 2^-24 x n cells.
+  // Otherwise one FP64 FMA and a conversion per coordinate.
   double cx, cy, cz;
   unsigned long long kzmin, kzmax;
   float inv_dx_f, inv_dy_f, fac_f;
+  float ihx, ilx, chx, clx, ihy, ily, chy, cly, ihz, ilz, chz, clz;
+  int f32;
   int nx, ny, nz;
   int skip;
 };
+
+// v as a float pair hi + lo (hi = float(v), lo = float(v - hi)).
+__device__ __forceinline__ void split_f(double v, float& hi, float& lo) {
+  hi = (float)v;
+  lo = (float)(v - (double)hi);
+}
+
+// Grid coordinate of the FP32 form from a float coordinate and the float
+// pairs of 1/dx and the offset.
+__device__ __forceinline__ float grid_t_f32(float xf, float ih, float il, float ch, float cl) {
+  return fmaf(xf, ih, ch) + fmaf(xf, il, cl);
+}
+
+// Whether the FP32 form's grid coordinates can be formed in float (see
+// KickConst::f32).
+__device__ __forceinline__ int grid_f32_ok(double cx, double cy, double cz, int nx, int ny, int nz) {
+  return fabs(cx) <= 4.0 * nx && fabs(cy) <= 4.0 * ny && fabs(cz) <= 4.0 * nz + 4.0;
+}
 
 __device__ __forceinline__ void load_kick_const(KickConst& k, const ScState* st, double host_factor,
                                                 int nx, int ny, int nz) {
@@ -262,6 +290,13 @@ __device__ __forceinline__ void load_kick_const(KickConst& k, const ScState* st,
   k.inv_dx_f = (float)k.inv_dx;
   k.inv_dy_f = (float)k.inv_dy;
   k.fac_f = (float)k.fac;
+  split_f(k.inv_dx, k.ihx, k.ilx);
+  split_f(k.cx, k.chx, k.clx);
+  split_f(k.inv_dy, k.ihy, k.ily);
+  split_f(k.cy, k.chy, k.cly);
+  split_f(k.inv_dz, k.ihz, k.ilz);
+  split_f(k.cz, k.chz, k.clz);
+  k.f32 = grid_f32_ok(k.cx, k.cy, k.cz, nx, ny, nz);
   k.nx = nx; k.ny = ny; k.nz = nz;
   k.skip = st->skip;
 }
@@ -340,10 +375,17 @@ __device__ __forceinline__ void kick_plain(const KickConst& k, const double* __r
 __device__ __forceinline__ void kick_fp32(const KickConst& k, const float* __restrict__ phi,
                                           const float* __restrict__ lam, double x, double y, double z,
                                           double& xp, double& yp) {
-  // the FP64 pipe bounds the pass: one FMA and one conversion per
-  // coordinate, the z range test on the integer pipes
-  float tx = (float)fma(x, k.inv_dx, k.cx);
-  float ty = (float)fma(y, k.inv_dy, k.cy);
+  // the FP64 pipe bounds the pass: the coordinates converted to float on
+  // the integer pipes (or one FMA and a conversion each, far from the
+  // origin), the z range test on integer keys
+  float tx, ty;
+  if (k.f32) {
+    tx = grid_t_f32(sf::to_float(x), k.ihx, k.ilx, k.chx, k.clx);
+    ty = grid_t_f32(sf::to_float(y), k.ihy, k.ily, k.chy, k.cly);
+  } else {
+    tx = (float)fma(x, k.inv_dx, k.cx);
+    ty = (float)fma(y, k.inv_dy, k.cy);
+  }
   int ix, iy;
   float fx, fy;
   tsc_index<float>(tx, k.nx, ix, fx);
@@ -370,15 +412,15 @@ __device__ __forceinline__ void kick_fp32(const KickConst& k, const float* __res
   float lv = 0.0f;
   const unsigned long long kz = dkey(z);
   if (kz >= k.kzmin && kz <= k.kzmax) {
-    float zt = (float)fma(z, k.inv_dz, k.cz);
+    float zt = k.f32 ? grid_t_f32(sf::to_float(z), k.ihz, k.ilz, k.chz, k.clz) : (float)fma(z, k.inv_dz, k.cz);
     int i0, ip;
     float w0, wp;
     g1_index<float>(zt, 0.0f, 1.0f, k.nz, i0, ip, w0, wp);
     lv = (k.nz > 1) ? (w0 * lam[i0] + wp * lam[ip]) : lam[0];
   }
   float lf = -lv * k.fac_f;
-  xp += (double)(gx * k.inv_dx_f * lf);
-  yp += (double)(gy * k.inv_dy_f * lf);
+  xp += sf::from_float(gx * k.inv_dx_f * lf);
+  yp += sf::from_float(gy * k.inv_dy_f * lf);
 }
 
 // ---------------------------------------------------------------------
@@ -387,10 +429,6 @@ __device__ __forceinline__ void kick_fp32(const KickConst& k, const float* __res
 // ---------------------------------------------------------------------
 struct DepConst {
   double xmin, xmax, ymin, ymax, inv_dx, inv_dy, zmin, zmax, inv_dz;
-  // FP32 form: grid coordinates as one FMA and the range tests on
-  // order-preserving integer keys (the FP64 pipe is the scarce one)
-  double cx, cy, cz;
-  unsigned long long kxmin, kxmax, kymin, kymax, kzmin, kzmax;
   int nx, ny, nz;
   int skip;
 };
@@ -399,12 +437,6 @@ __device__ __forceinline__ void load_dep_const(DepConst& d, const ScState* st, i
   d.xmin = st->xmin; d.xmax = st->xmax; d.ymin = st->ymin; d.ymax = st->ymax;
   d.inv_dx = st->inv_dx; d.inv_dy = st->inv_dy;
   d.zmin = st->zmin; d.zmax = st->zmax; d.inv_dz = st->inv_dz;
-  d.cx = -d.xmin * d.inv_dx;
-  d.cy = -d.ymin * d.inv_dy;
-  d.cz = -d.zmin * d.inv_dz;
-  d.kxmin = dkey(d.xmin); d.kxmax = dkey(d.xmax);
-  d.kymin = dkey(d.ymin); d.kymax = dkey(d.ymax);
-  d.kzmin = dkey(d.zmin); d.kzmax = dkey(d.zmax);
   d.nx = nx; d.ny = ny; d.nz = nz;
   d.skip = st->skip;
 }
@@ -762,41 +794,6 @@ __device__ __forceinline__ bool kick_fixed(const KickFix& k, const long long* __
   xp = fma((double)gx, dmul<(ORBIT_SOFT_MUL >> 4) & 1>(k.gxs, lf), xp);
   yp = fma((double)gy, dmul<(ORBIT_SOFT_MUL >> 4) & 1>(k.gys, lf), yp);
   return true;
-}
-
-__device__ __forceinline__ void deposit_fp32(const DepConst& d, float* rho, float* zg, double x, double y,
-                                             double z, float m) {
-  const unsigned long long kx = dkey(x), ky = dkey(y), kz = dkey(z);
-  if (kx >= d.kxmin && kx <= d.kxmax && ky >= d.kymin && ky <= d.kymax) {
-    float tx = (float)fma(x, d.inv_dx, d.cx);
-    float ty = (float)fma(y, d.inv_dy, d.cy);
-    int ix, iy;
-    float fx, fy;
-    tsc_index<float>(tx, d.nx, ix, fx);
-    tsc_index<float>(ty, d.ny, iy, fy);
-    float wxm, wx0, wxp, wym, wy0, wyp;
-    tsc_weights<float>(fx, wxm, wx0, wxp);
-    tsc_weights<float>(fy, wym, wy0, wyp);
-    float ax[3] = {wxm * m, wx0 * m, wxp * m};
-    float wy[3] = {wym, wy0, wyp};
-    float* base = rho + (ix - 1) * d.ny + (iy - 1);
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int j = 0; j < 3; ++j) atomicAdd(base + i * d.ny + j, ax[i] * wy[j]);
-  }
-  if (kz >= d.kzmin && kz <= d.kzmax) {
-    float zt = (float)fma(z, d.inv_dz, d.cz);
-    int i0, ip;
-    float w0, wp;
-    g1_index<float>(zt, 0.0f, 1.0f, d.nz, i0, ip, w0, wp);
-    if (d.nz > 1) {
-      atomicAdd(zg + i0, w0 * m);
-      atomicAdd(zg + ip, wp * m);
-    } else {
-      atomicAdd(zg, m);
-    }
-  }
 }
 
 }  // namespace orbit

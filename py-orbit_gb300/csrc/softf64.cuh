@@ -264,6 +264,77 @@ SF_HD double fma(double a, double b, double c) {
   return out;
 }
 
+#ifdef __CUDACC__
+static __host__ __device__ __noinline__
+#else
+inline
+#endif
+float hw_d2f(double x) {
+#ifdef __CUDA_ARCH__
+  return __double2float_rn(x);
+#else
+  return (float)x;
+#endif
+}
+
+#ifdef __CUDACC__
+static __host__ __device__ __noinline__
+#else
+inline
+#endif
+double hw_f2d(float f) {
+  return (double)f;
+}
+
+SF_HD uint32_t fbits(float v) {
+#ifdef __CUDA_ARCH__
+  return (uint32_t)__float_as_uint(v);
+#else
+  uint32_t u;
+  std::memcpy(&u, &v, 4);
+  return u;
+#endif
+}
+
+SF_HD float from_fbits(uint32_t u) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(u);
+#else
+  float v;
+  std::memcpy(&v, &u, 4);
+  return v;
+#endif
+}
+
+// (float)x rounded to nearest even: for x whose float exponent is in
+// [-126, 126] the top 24 significand bits are kept, bit 28 rounds and the
+// 28 bits below it are sticky; the rounding carry may step the exponent
+// (to at most 127, still finite).  Zeros, subnormal results, overflow,
+// infinities and NaN take the hardware conversion.
+SF_HD float to_float(double x) {
+  const uint64_t X = bits(x);
+  const int ef = (int)((X >> 52) & 0x7FF) - 1023 + 127;  // biased float exponent
+  if ((unsigned)(ef - 1) >= 253u) return hw_d2f(x);
+  const uint64_t m = X & ((1ull << 52) - 1);
+  uint32_t r = ((uint32_t)ef << 23) | (uint32_t)(m >> 29);
+  const uint32_t rest = (uint32_t)m & ((1u << 29) - 1), half = 1u << 28;
+  r += (rest > half || (rest == half && (r & 1u))) ? 1u : 0u;
+  return from_fbits(r | ((uint32_t)(X >> 32) & 0x80000000u));
+}
+
+// (double)f, exact: the exponent rebased and the significand widened;
+// subnormal floats, infinities and NaN take the hardware conversion.
+SF_HD double from_float(float f) {
+  const uint32_t F = fbits(f);
+  const uint32_t e = (F >> 23) & 0xFFu;
+  if (e - 1u >= 254u) {
+    if ((F & 0x7FFFFFFFu) == 0u) return from_bits((uint64_t)F << 32);  // signed zero
+    return hw_f2d(f);
+  }
+  return from_bits(((uint64_t)(F & 0x80000000u) << 32) | ((uint64_t)(e + 896u) << 52) |
+                   ((uint64_t)(F & 0x7FFFFFu) << 29));
+}
+
 // x * 2^k for k = -1 or +1 (exact) as an exponent change; the hardware
 // multiply where x is zero, subnormal, not finite or the result leaves the
 // normal range.

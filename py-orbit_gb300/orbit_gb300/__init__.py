@@ -42,9 +42,10 @@ def device_mul_rates():
 
 
 def softf64_check(n, seed=1):
-    """Mismatch counts (mul, add, fma, scale2) of the integer-pipe binary64
-    routines against the FP64 instructions on n generated device cases."""
-    out = (ctypes.c_longlong * 4)()
+    """Mismatch counts (mul, add, fma, scale2, to_float, from_float) of the
+    integer-pipe binary64 routines against the hardware instructions on n
+    generated device cases."""
+    out = (ctypes.c_longlong * 6)()
     call("orbit_softf64_check", ctypes.c_longlong(n), ctypes.c_ulonglong(seed), out)
     return tuple(out)
 

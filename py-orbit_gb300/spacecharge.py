@@ -410,8 +410,8 @@ class SpaceChargeCalc2p5D:
     (src/spacecharge/SpaceChargeCalc2p5D.cc, wrap_spacechargecalc2p5d.cc:38-52).
 
     ``form`` selects the arithmetic: ``"plain"`` (FP64 throughout, the
-    drop-in) or ``"fp32"`` (deposit, FFT and gradient in FP32; coordinates
-    and kick accumulation FP64).
+    drop-in) or ``"fp32"`` (the plain form's exact fixed-point deposit, FFT
+    and gradient in FP32; coordinates and kick accumulation FP64).
     """
 
     _FORMS = {"plain": 0, "fp32": 1}

@@ -1,7 +1,8 @@
 // Host check of the integer-pipe binary64 routines (py-orbit_gb300/csrc/
 // softf64.cuh) against the host's IEEE arithmetic: sf::mul, sf::add,
 // sf::fma and sf::scale2 must return the same bits as a * b, a + b,
-// fma(a, b, c) and a * 2^k on random normal operands over wide and narrow
+// fma(a, b, c) and a * 2^k, and sf::to_float / sf::from_float the same as
+// the casts, on random normal operands over wide and narrow
 // exponent spreads, near-cancellations, exact ties, zeros and random bit
 // patterns (subnormals, infinities, NaN).  Prints the mismatch count.
 #include <cmath>
@@ -44,6 +45,15 @@ int main(int argc, char** argv) {
     if (!same(a + b, sf::add(a, b))) ++bad;
     if (!same(std::fma(a, b, c), sf::fma(a, b, c))) ++bad;
     if (!same(a * 0.5, sf::scale2(a, -1)) || !same(a * 2.0, sf::scale2(a, 1))) ++bad;
+    // conversions: doubles near float ties and over the float range, and
+    // random float bit patterns
+    double t = (i % 3 == 0) ? a : std::ldexp(a, (int)(g() % 300) - 150);
+    if (i % 5 == 0) t = sf::from_bits((sf::bits(t) & ~((1ull << 29) - 1)) | (1ull << 28));  // exact tie
+    const float tf = (float)t, sf32 = sf::to_float(t);
+    if (!(sf::fbits(tf) == sf::fbits(sf32) || (std::isnan(tf) && std::isnan(sf32)))) ++bad;
+    const float r = sf::from_fbits((uint32_t)g());
+    const double rd = (double)r, sd = sf::from_float(r);
+    if (!same(rd, sd)) ++bad;
   }
   std::printf("%ld\n", bad);
   return bad != 0;

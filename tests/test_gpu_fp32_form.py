@@ -1,19 +1,22 @@
-"""The FP32 field form (deposit, FFT and gradient in FP32; coordinates, maps
-and kick accumulation in FP64) against the FP64 oracle and the plain form.
+"""The FP32 field form (the plain form's exact fixed-point deposit; FFT and
+gradient in FP32; coordinates, maps and kick accumulation in FP64) against
+the FP64 oracle and the plain form.
 
-Tolerances: potential within 1e-5 and kicks within 2e-4 (max-norm relative)
-of the FP64 oracle after one kick; rms emittances within 1% of the plain
-form after 200 kicks.  The kick bound is the FP32 noise floor: the grid
-coordinate rounded to float (half an ulp at 64-128 cells, 4-8e-6 of a
-cell, moves the 9-point weights) and the potential's FP32 error (about
-1e-6 of its maximum, amplified some 50 times by the gradient's
-differences over one cell) each reach a few 1e-5 of the largest kick;
-measured 0.99-1.00e-4 on this test's bunch."""
+Tolerances: density within 1e-12 (the deposit is the plain form's),
+potential within 1e-5 and kicks within 2e-4 (max-norm relative) of the
+FP64 oracle after one kick; rms emittances within 1% of the plain form
+after 200 kicks.  The kick bound is the FP32 noise floor: the grid
+coordinate formed in float (the coordinate, 1/dx and the offset each
+rounded to float, a few ulps at 64-128 cells, about 1e-5 of a cell, move
+the 9-point weights) and the potential's FP32 error (about 1e-6 of its
+maximum, amplified some 50 times by the gradient's differences over one
+cell) each reach a few 1e-5 of the largest kick; measured 0.99-1.00e-4 on
+this test's bunch."""
 import numpy as np
 import pytest
 
 import oracle as O
-from helpers import rel_err
+from helpers import TOL_FIELD, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -53,7 +56,7 @@ def test_fp32_single_kick_accuracy():
     assert np.array_equal(got[0], soa[0]) and np.array_equal(got[2], soa[2]) and np.array_equal(got[4], soa[4])
     rho, phi, zg, lim = sc.grids()
     assert rel_err(calc.getPhiGrid().getArray(), phi) < TOL_PHI_FP32
-    assert rel_err(calc.getRhoGrid().getArray(), rho) < TOL_PHI_FP32
+    assert rel_err(calc.getRhoGrid().getArray(), rho) <= TOL_FIELD
 
 
 def test_fp32_fused_program_matches_eager():

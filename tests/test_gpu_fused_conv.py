@@ -2,21 +2,17 @@
 Green rebuild, the forward rows with the line-density finalization, the
 columns with the Green multiply and the backward rows in one cooperative
 launch) against the separate kernels it replaces.  It runs the same
-operations in the same order, so grids and coordinates are bit-identical
-(plain form): eagerly with Green rebuilds on reshaped beams, in the
-recorded FODO program (CUDA graphs) and on a non-square grid of mixed
-radices.  The FP32 form's deposit adds floats in no fixed order, so two of
-its runs agree to its rounding only: grids within 1e-5, and coordinates
-within 1e-5 after six kicks (the kicks inherit the grids' relative
-difference; the coordinates that the kicks move most change by a few
-times the kick).
+operations in the same order, so grids and coordinates are bit-identical,
+in both forms (the deposit is exact in both): eagerly with Green rebuilds
+on reshaped beams, in the recorded FODO program (CUDA graphs) and on a
+non-square grid of mixed radices.
 Its barrier waits are bounded: with a block withheld from the first
 barrier, the other blocks' waits run out, the bunch's status reports it,
 and the next kick runs normally."""
 import numpy as np
 import pytest
 
-from helpers import TOL_FIELD, coord_err, rel_err
+from helpers import TOL_FIELD, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -55,14 +51,8 @@ def test_eager_kicks_bit_identical_with_rebuilds(form, grid):
         fused.trackBunch(ba, 0.5)
         sep.trackBunch(bb, 0.5)
         for g1, g2 in zip(_grids(fused), _grids(sep)):
-            if form == "plain":
-                assert np.array_equal(g1, g2), k
-            else:
-                assert rel_err(g1, g2) <= 1e-5, k
-    if form == "plain":
-        assert np.array_equal(ba.getCoordinates(), bb.getCoordinates())
-    else:
-        assert coord_err(ba.getCoordinates(), bb.getCoordinates()) <= 1e-5
+            assert np.array_equal(g1, g2), k
+    assert np.array_equal(ba.getCoordinates(), bb.getCoordinates())
     kf, gf = fused._calc.counters()
     ks, gs = sep._calc.counters()
     assert (kf, gf) == (ks, gs) and kf == 6 and gf >= 3
