@@ -78,6 +78,17 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(v, dist, device="cuda"):
+    """The largest v over the ranks (the slowest replica sets the job's
+    time); v itself without a process group."""
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def quiet():
     return contextlib.redirect_stdout(io.StringIO())
 
@@ -496,11 +507,7 @@ def run_ours(args):
     barrier()
     clk = clocks.stop()
     bunch._device_modified()
-    total_ms = sum(step_ms)
-    if dist is not None:
-        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(sum(step_ms), dist)
     kicks = world * n * kicks_per_turn * args.steps
     value = kicks / (total_ms * 1e-3)
 
@@ -521,11 +528,7 @@ def run_ours(args):
             t1 = time.perf_counter()
             if i > 0:  # the first call re-records and re-captures the graphs
                 e2e_ms.append((t1 - t0) * 1e3)
-        tot = sum(e2e_ms)
-        if dist is not None:
-            t = torch.tensor([tot], dtype=torch.float64, device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            tot = float(t.item())
+        tot = max_over_ranks(sum(e2e_ms), dist)
         e2e = {"value": world * n * kicks_per_turn * len(e2e_ms) / (tot * 1e-3), "unit": "macroparticle-kicks/s",
                "h2d_bytes_per_step": int(pin_in.nbytes), "d2h_bytes_per_step": int(pin_out.nbytes),
                "ms_per_step": tot / len(e2e_ms)}
@@ -705,6 +708,12 @@ def run_batched(args):
     own 40-cell FODO lattice, all bunches in one batch (orbit_batch_*)."""
     import torch
     rank, world, local = dist_env()
+    dist = None
+    if world > 1:  # replicas: every rank runs the whole scan on its own GPU
+        import torch.distributed as tdist
+        torch.cuda.set_device(local)
+        tdist.init_process_group("nccl")
+        dist = tdist
     torch.cuda.init()
     from orbit_gb300.batch import BunchBatch
     scan = build_scan(args.members)
@@ -717,6 +726,8 @@ def run_batched(args):
     clocks = ClockSampler(local)
     torch.cuda.synchronize()
     bb.sync()
+    if dist is not None:
+        dist.barrier()
     clocks.start()
     step_ms = []
     wall0 = time.perf_counter()
@@ -732,9 +743,11 @@ def run_batched(args):
         step_ms.append(e0.elapsed_time(e1))
     wall = time.perf_counter() - wall0
     torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
     clk = clocks.stop()
-    total_ms = sum(step_ms)
-    value = n_tot * kicks_per_turn * args.steps / (total_ms * 1e-3)
+    total_ms = max_over_ranks(sum(step_ms), dist)
+    value = world * n_tot * kicks_per_turn * args.steps / (total_ms * 1e-3)
     # the same bunches tracked one program each (each bunch on its own
     # stream, so the programs overlap as far as the GPU lets them)
     def unbatched_turn():
@@ -775,10 +788,15 @@ def run_batched(args):
             t1 = time.perf_counter()
             if i > 0:  # the first call re-records the programs and recaptures the graphs
                 e2e_ms.append((t1 - t0) * 1e3)
-        tot = sum(e2e_ms)
-        e2e = {"value": n_tot * kicks_per_turn * len(e2e_ms) / (tot * 1e-3), "unit": "macroparticle-kicks/s",
+        tot = max_over_ranks(sum(e2e_ms), dist)
+        e2e = {"value": world * n_tot * kicks_per_turn * len(e2e_ms) / (tot * 1e-3), "unit": "macroparticle-kicks/s",
                "h2d_bytes_per_step": int(sum(p[0].nbytes for p in pins)),
                "d2h_bytes_per_step": int(sum(p[1].nbytes for p in pins)), "ms_per_step": tot / len(e2e_ms)}
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank != 0:
+        return
     prof = bb.profile()
     hbm_peak, peak_kind = measured_peaks()
     turn_ms = sum(v[0] for v in prof.values())
@@ -806,7 +824,7 @@ def run_batched(args):
                 "share_of_turn": pass_ms / turn_ms, "per_class": kinds,
                 "kernels": {k: {"ms": v[0], "launches": v[1], "share": v[0] / turn_ms} for k, v in prof.items()}}
     cpu = None
-    if not args.no_cpu:
+    if not args.no_cpu and world == 1:
         threads = os.cpu_count() or 1
         rate, per_turn, kpt = cpu_reference_rate(N_PARTICLES, 1, 0, threads)
         cpu = {"value": rate, "unit": "macroparticle-kicks/s", "cores": threads, "kind": "port",
@@ -814,7 +832,7 @@ def run_batched(args):
                          % (N_PARTICLES, kpt, threads)}
     classes = bb.classes()
     line = {
-        "metric": METRIC, "value": value, "unit": "macroparticle-kicks/s", "n_gpus": 1, "steps": args.steps,
+        "metric": METRIC, "value": value, "unit": "macroparticle-kicks/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Gaussian 6D bunches of the scan)",
         "config": {"workload": "batched scan: %d bunches, %d particles in all (log-uniform 5e4-2e6), "
@@ -822,7 +840,7 @@ def run_batched(args):
                                "40-cell FODO x 4 SC nodes, one turn per step" % (len(scan), n_tot),
                    "particles": n_tot, "members": len(scan), "kicks_per_step": kicks_per_turn,
                    "classes": classes, "l2": "flushed (512 MiB write) before each timed step; inputs > L2",
-                   "unbatched_ms_per_turn": unb_ms, "parallelism": "single"},
+                   "unbatched_ms_per_turn": unb_ms, "parallelism": "replicas" if world > 1 else "single"},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
         "gpu_launches": bb.launchesPerTurn() * args.steps, "wall_s": wall,
     }
