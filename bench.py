@@ -127,16 +127,16 @@ MAP_FLOPS = {1: 22, 2: 16, 3: 25, 4: 70, 5: 70, 6: 18, 7: 25, 8: 20, 9: 14, 10: 
              14: 60, 15: 12, 16: 2, 17: 3, 18: 20, 19: 30, 20: 60}
 
 
-# FP64 instructions per particle (DFMA + DMUL + DADD, thread level) that the
-# kernels execute on this workload, counted by ncu
-# (smsp__sass_thread_inst_executed_op_{dfma,dmul,dadd}_pred_on, 4e6
-# particles): the fused pass alternates the {kick, quad1, quad2 (the two
-# back-to-back quad2 of the reference schedule merged), quad1, fringe-out}
-# segment (73.0) and the {kick, drift, fringe-in} segment (54.0); the deposit
-# runs 6.3 (one FMA per coordinate and the fixed-point conversions; weights
-# and sums are integer).  Conversions and compares also occupy the FP64 pipe
-# and are not in these counts.
-FP64_INST_PER_PARTICLE = {"pass_kick_maps": (73.0 + 54.0) / 2, "deposit": 6.26}
+# FP64-pipe instructions per particle (thread level: DFMA, DMUL, DADD, the
+# conversions and compares) that the kernels execute on this workload,
+# counted by ncu (sm__inst_executed_pipe_fp64.sum x 32 / particles, 4e6
+# particles, the multiplies of the drift, quad fringe and bend maps on the
+# integer pipes): the fused pass alternates the {kick, quad1, quad2 (the
+# two back-to-back quad2 of the reference schedule merged), quad1,
+# fringe-out} segment (56.1) and the {kick, drift, fringe-in} segment
+# (38.1); the deposit runs 6.3 (one FMA per coordinate and the fixed-point
+# conversions; weights and sums are integer).
+FP64_INST_PER_PARTICLE = {"pass_kick_maps": (56.09 + 38.09) / 2, "deposit": 6.26}
 
 
 def pass_flops_per_turn(ops):

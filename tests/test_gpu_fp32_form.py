@@ -121,3 +121,26 @@ def test_fp32_tune_shift_and_emittance_error_report():
         assert r["tune_shift_mean_err"][k] < 0.01 * shift, r
         assert r["tune_spread_err"][k] < 0.01 * shift, r
         assert r["emittance_rel_err"][k] < TOL_EMITTANCE_FP32, r
+
+
+@pytest.mark.parametrize("offset", [0.03, 2.0])
+def test_fp32_offset_beam(offset):
+    """A beam displaced from the coordinate origin: by 0.03 m the grid origin
+    stays within four grid extents and the kick's grid coordinates are formed
+    in float from the converted coordinates; by 2 m (a hundred extents) the
+    kick forms them with one FP64 FMA each.  Both within the single-kick
+    tolerance of the oracle."""
+    from orbit_gb300 import workloads as W
+    from spacecharge import SpaceChargeCalc2p5D
+    soa = W.c2_coords(100_000, seed=6)
+    soa[0] += offset
+    soa[2] -= 0.5 * offset
+    b = gpu_bunch(soa, 1e9)
+    calc = SpaceChargeCalc2p5D(128, 128, 64, form="fp32")
+    calc.trackBunch(b, 1.0)
+    got = b.getCoordinates()
+    sc = O.OracleSC(128, 128, 64)
+    a = np.ascontiguousarray(soa.copy())
+    assert sc.track(a, oracle_sync_of(b), 1.0, nthreads=8) == 0
+    assert rel_err(got[1] - soa[1], a[1] - soa[1]) < TOL_KICK_FP32
+    assert rel_err(got[3] - soa[3], a[3] - soa[3]) < TOL_KICK_FP32
