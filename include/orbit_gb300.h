@@ -241,9 +241,8 @@ int orbit_sc2p5d_fields(orbit_sc2p5d_t* c, int n, const double* x, const double*
  * stream: a cudaStream_t (NULL = default stream).  Every call copies the
  * fresh calculator's state from host memory into the array and waits for
  * the stream before it returns.  The first call on a device looks up the
- * array's device address (once per device, under a lock), so make that
- * first call before any stream capture.  Calls share the array: calls that
- * overlap on the GPU race. */
+ * array's device address (once per device, under a lock).  Calls share the
+ * array: calls that overlap on the GPU race. */
 int orbit_sc2p5d_track_static(double* dev_coords, int n, int stride, int nx, int ny, int nz, double xy_ratio,
                               double length, const orbit_sync_t* sync, void* stream);
 
