@@ -1200,8 +1200,9 @@ static int init_conv_fused(orbit_sc2p5d_t* c) {
   const void* fn = (const void*)conv_kernel<T>(c);
   size_t sm = conv_smem<T>(c);
   c->conv_blocks = 0;
-  int coop = 0;
-  ORBIT_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, 0));
+  int coop = 0, dev = 0;
+  ORBIT_CUDA(cudaGetDevice(&dev));
+  ORBIT_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
   if (!coop || sm > (size_t)kMaxSmem) return ORBIT_OK;
   if (sm > 48 * 1024) ORBIT_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   int per_sm = 0;
