@@ -29,6 +29,54 @@ static const int kPassSmem = 220 * 1024;
 #define ORBIT_PASS_THREADS 512
 #endif
 
+// Copies n values of global memory (written by an earlier kernel) into
+// shared memory through f, with V-wide vector loads (16 bytes), U of them
+// in flight per thread: one at a time, each load would wait for the shared
+// store before it (which the compiler cannot prove does not alias it), a
+// full L2 round trip per value, and all blocks read the same values at
+// once.  Threads t0.. of the block take part (t0 = 32 leaves warp 0 free).
+// Out of line, so that its registers do not weigh on the particle loop's.
+// g and s are 16-byte aligned; the caller synchronises the block.
+template <int U, typename VT, typename Tin, typename Tout, typename F>
+__device__ __noinline__ void fill_smem(Tout* s, const Tin* g, int n, F f, int t0) {
+  constexpr int V = (int)(sizeof(VT) / sizeof(Tin));
+  const int t = (int)threadIdx.x - t0, nt = (int)blockDim.x - t0;
+  if (t < 0) return;
+  const int nv = n / V;
+  const VT* gv = reinterpret_cast<const VT*>(g);
+  // each block starts at its own offset, so that the blocks do not all ask
+  // the same L2 lines at the same moment
+  const int off = nv > 0 ? (int)(((long long)blockIdx.x * 1031) % nv) : 0;
+  for (int i0 = t; i0 < nv; i0 += U * nt) {
+    VT v[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int i = i0 + u * nt;
+      int j = i + off;
+      j = j >= nv ? j - nv : j;
+      if (i < nv) v[u] = __ldcg(gv + j);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int i = i0 + u * nt;
+      int j = i + off;
+      j = j >= nv ? j - nv : j;
+      if (i < nv) {
+        const Tin* e = reinterpret_cast<const Tin*>(&v[u]);
+#pragma unroll
+        for (int q = 0; q < V; ++q) s[j * V + q] = f(e[q]);
+      }
+    }
+  }
+  for (int i = nv * V + t; i < n; i += nt) s[i] = f(__ldcg(g + i));
+}
+
+// The kick constants of a pass (one thread), out of line like fill_smem.
+__device__ __noinline__ void kick_consts_into(KickConst* k, KickFix* kf, const KickArgs& kick) {
+  load_kick_const(*k, kick.st, kick.host_factor, kick.nx, kick.ny, kick.nz, kf == nullptr);
+  if (kf) load_kick_fix(*kf, kick.st, k->fac, kick.nx, kick.ny, kick.nz);
+}
+
 // KF: 0 no kick, 1 plain kick, 2 fp32 kick.  EXT: accumulate extrema.
 // Blocks blk = 0..nblk-1 share the bunch's particles.
 template <int KF, bool EXT, bool KSMEM>
@@ -47,25 +95,34 @@ __device__ __forceinline__ void pass_body(double* __restrict__ cx, double* __res
   const float* Lf = kick.lam_f;
   extern __shared__ unsigned char s_raw[];
   if (KF != 0) {
-    load_kick_block(k, KF == 1 ? &kf : nullptr, kick.st, kick.host_factor, kick.nx, kick.ny, kick.nz);
+    // thread 0 computes the kick constants (two FP64 divisions among
+    // them) while warps 1.. fill the block's copy of the potential and the
+    // line density; one barrier completes both
+    __shared__ KickConst s_k;
+    __shared__ KickFix s_kf;
+    if (threadIdx.x == 0) kick_consts_into(&s_k, KF == 1 ? &s_kf : nullptr, kick);
     if (KSMEM) {
-      int ng = kick.nx * kick.ny;
+      const int ng = kick.nx * kick.ny, t0 = blockDim.x > 64 ? 32 : 0;
       if (KF == 1) {
-        // fixed-point copy converted here from the FP64 potential
+        // fixed-point copy converted here from the FP64 potential, at the
+        // scales the kick constants use
+        const int sphi = scale_bits(kick.st->phi_absmax), slam = scale_bits(kick.st->lam_absmax);
         long long* s = reinterpret_cast<long long*>(s_raw);
-        for (int i = threadIdx.x; i < ng; i += blockDim.x) s[i] = phi_fixed(kick.phi[i], kf.sphi);
-        for (int i = threadIdx.x; i < kick.nz; i += blockDim.x) s[ng + i] = phi_fixed(kick.lam[i], kf.slam);
+        fill_smem<4, double2>(s, kick.phi, ng, [sphi](double v) { return phi_fixed(v, sphi); }, t0);
+        fill_smem<4, double2>(s + ng, kick.lam, kick.nz, [slam](double v) { return phi_fixed(v, slam); }, t0);
         P = s;
         Lm = s + ng;
       } else {
         float* s = reinterpret_cast<float*>(s_raw);
-        for (int i = threadIdx.x; i < ng; i += blockDim.x) s[i] = kick.phi_f[i];
-        for (int i = threadIdx.x; i < kick.nz; i += blockDim.x) s[ng + i] = kick.lam_f[i];
+        fill_smem<4, float4>(s, kick.phi_f, ng, [](float v) { return v; }, t0);
+        fill_smem<4, float4>(s + ng, kick.lam_f, kick.nz, [](float v) { return v; }, t0);
         Pf = s;
         Lf = s + ng;
       }
-      __syncthreads();
     }
+    __syncthreads();
+    k = s_k;
+    if (KF == 1) kf = s_kf;
   }
   ExtAcc acc;
   if (EXT) acc.init();

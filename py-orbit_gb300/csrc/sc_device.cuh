@@ -276,12 +276,17 @@ __device__ __forceinline__ int grid_f32_ok(double cx, double cy, double cz, int 
   return fabs(cx) <= 4.0 * nx && fabs(cy) <= 4.0 * ny && fabs(cz) <= 4.0 * nz + 4.0;
 }
 
+// f32: also the FP32 form's constants (a dozen FP64 operations the plain
+// form does not need; one thread computes them while the block waits).
 __device__ __forceinline__ void load_kick_const(KickConst& k, const ScState* st, double host_factor,
-                                                int nx, int ny, int nz) {
+                                                int nx, int ny, int nz, bool f32 = true) {
   k.xmin = st->xmin; k.ymin = st->ymin; k.inv_dx = st->inv_dx; k.inv_dy = st->inv_dy;
   k.zmin = st->zmin; k.zmax = st->zmax; k.inv_dz = st->inv_dz;
   // factor = 2 L r_c/(beta^2 gamma^3) / (z_step * totalMacrosize)  (:96-100)
   k.fac = host_factor / (st->dz * st->total_m);
+  k.nx = nx; k.ny = ny; k.nz = nz;
+  k.skip = st->skip;
+  if (!f32) return;
   k.cx = -k.xmin * k.inv_dx;
   k.cy = -k.ymin * k.inv_dy;
   k.cz = -k.zmin * k.inv_dz;
@@ -297,8 +302,6 @@ __device__ __forceinline__ void load_kick_const(KickConst& k, const ScState* st,
   split_f(k.inv_dz, k.ihz, k.ilz);
   split_f(k.cz, k.chz, k.clz);
   k.f32 = grid_f32_ok(k.cx, k.cy, k.cz, nx, ny, nz);
-  k.nx = nx; k.ny = ny; k.nz = nz;
-  k.skip = st->skip;
 }
 
 // 2.5Drb longitudinal kick (SpaceChargeCalc2p5Drb.cc:132-154):
@@ -714,8 +717,8 @@ __device__ __forceinline__ int scale_bits(unsigned long long absmax_bits) {
   return absmax_bits == 0 ? 0 : 1083 - e;  // max * 2^s < 2^61
 }
 
-__device__ __forceinline__ void load_kick_fix(KickFix& k, const ScState* st, double host_factor, int nx, int ny,
-                                              int nz) {
+// fac: the kick factor of load_kick_const (the same division).
+__device__ __forceinline__ void load_kick_fix(KickFix& k, const ScState* st, double fac, int nx, int ny, int nz) {
   k.ax = st->inv_dx; k.cx = 0.5 - st->xmin * st->inv_dx;
   k.ay = st->inv_dy; k.cy = 0.5 - st->ymin * st->inv_dy;
   k.az = st->inv_dz; k.cz = 0.5 - st->zmin * st->inv_dz;
@@ -724,7 +727,6 @@ __device__ __forceinline__ void load_kick_fix(KickFix& k, const ScState* st, dou
   k.slam = scale_bits(st->lam_absmax);
   k.gxs = ldexp(st->inv_dx, 5 - k.sphi);
   k.gys = ldexp(st->inv_dy, 5 - k.sphi);
-  double fac = host_factor / (st->dz * st->total_m);
   k.lfs = ldexp(-fac, 2 - k.slam);
   k.nx = nx; k.ny = ny; k.nz = nz;
   k.Fx = fix_bits(nx); k.Fy = fix_bits(ny); k.Fz = fix_bits(nz);
@@ -743,7 +745,7 @@ __device__ __forceinline__ void load_kick_block(KickConst& k, KickFix* kf, const
   __shared__ KickFix s_kf;
   if (threadIdx.x == 0) {
     load_kick_const(s_k, st, host_factor, nx, ny, nz);
-    if (kf) load_kick_fix(s_kf, st, host_factor, nx, ny, nz);
+    if (kf) load_kick_fix(s_kf, st, s_k.fac, nx, ny, nz);
   }
   __syncthreads();
   k = s_k;
