@@ -23,6 +23,11 @@ class AccActionsContainer(NamedObject):
     def getActions(self, place):
         return self.__actions[place]
 
+    def actionLists(self):
+        """The (entrance, body, exit) action lists themselves (run in place
+        by AccNode.trackActions)."""
+        return self.__actions
+
     def performActions(self, paramsDict, place):
         for action in self.__actions[place]:
             action(paramsDict)

@@ -171,44 +171,68 @@ class AccNode(NamedObject, TypedObject, ParamsDictObject):
     def trackActions(self, actionsContainer, paramsDict=None):
         """Entrance actions, entrance children, then per part: BEFORE
         children, body actions, AFTER children; then exit children and exit
-        actions (AccNode.py:302-350)."""
+        actions (AccNode.py:302-350).  The lattice walk records a device
+        program on every trackBunch, so the common case is kept short: a
+        plain AccActionsContainer's action lists are run in place (a
+        subclass's performActions is called as usual), and the node and
+        parent entries are rewritten only where a child walk changed them."""
         if paramsDict is None:
             paramsDict = {}
         if _NVTX:
             _nvtx_push(self.getName())
+        plain = type(actionsContainer) is AccActionsContainer
+        if plain:
+            ent_a, body_a, exit_a = actionsContainer.actionLists()
         paramsDict["node"] = self
         parentNode = paramsDict.get("parentNode")
         if "path_length" not in paramsDict:
             paramsDict["path_length"] = 0.0
         has_length = self.getLength() > 0.0
         self.__activePartIndex = -1
-        actionsContainer.performActions(paramsDict, AccNode.ENTRANCE)
-        for node in self.__children[AccNode.ENTRANCE]:
+        if plain:
+            for action in ent_a:
+                action(paramsDict)
+        else:
+            actionsContainer.performActions(paramsDict, AccNode.ENTRANCE)
+        children = self.__children
+        for node in children[AccNode.ENTRANCE]:
             paramsDict["node"] = node
             paramsDict["parentNode"] = self
             node.trackActions(actionsContainer, paramsDict)
+        body_children = children[AccNode.BODY]
         for i in range(self.__nParts):
             paramsDict["node"] = self
             paramsDict["parentNode"] = parentNode
             self.__activePartIndex = i
-            for node in self.__children[AccNode.BODY][i][AccNode.BEFORE]:
-                paramsDict["parentNode"] = self
-                node.trackActions(actionsContainer, paramsDict)
-            paramsDict["node"] = self
-            paramsDict["parentNode"] = parentNode
-            actionsContainer.performActions(paramsDict, AccNode.BODY)
+            part = body_children[i]
+            before = part[AccNode.BEFORE]
+            if before:
+                for node in before:
+                    paramsDict["parentNode"] = self
+                    node.trackActions(actionsContainer, paramsDict)
+                paramsDict["node"] = self
+                paramsDict["parentNode"] = parentNode
+            if plain:
+                for action in body_a:
+                    action(paramsDict)
+            else:
+                actionsContainer.performActions(paramsDict, AccNode.BODY)
             if has_length:
                 paramsDict["path_length"] += self.getLength(i)
-            for node in self.__children[AccNode.BODY][i][AccNode.AFTER]:
+            for node in part[AccNode.AFTER]:
                 paramsDict["parentNode"] = self
                 node.trackActions(actionsContainer, paramsDict)
         self.__activePartIndex = -1
-        for node in self.__children[AccNode.EXIT]:
+        for node in children[AccNode.EXIT]:
             paramsDict["node"] = node
             paramsDict["parentNode"] = self
             node.trackActions(actionsContainer, paramsDict)
         paramsDict["node"] = self
         paramsDict["parentNode"] = parentNode
-        actionsContainer.performActions(paramsDict, AccNode.EXIT)
+        if plain:
+            for action in exit_a:
+                action(paramsDict)
+        else:
+            actionsContainer.performActions(paramsDict, AccNode.EXIT)
         if _NVTX:
             _nvtx_pop()

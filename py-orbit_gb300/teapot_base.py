@@ -21,9 +21,17 @@ _OPS = {
 }
 
 
+# the maps whose parameters are all doubles (most of them): their program
+# tuples are built without the per-argument type dispatch (the lattice walk
+# records every map call on every trackBunch)
+_ALL_D = {name for name, (_, types) in _OPS.items() if "i" not in types}
+
+
 def op_tuple(name, args):
     """(code, ints, doubles) of one map call in the program format."""
     code, types = _OPS[name]
+    if name in _ALL_D:
+        return code, (), tuple(map(float, args))
     ints, dbls = [], []
     for t, a in zip(types, args):
         (ints if t == "i" else dbls).append(int(a) if t == "i" else float(a))
