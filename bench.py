@@ -314,7 +314,7 @@ def learned_report(calc, ms_per_turn, n, n_equal=10_000_000, turns=10, form="pla
             "emittance_growth_turns": turns, "emittance_growth": growth,
             "growth_dev_learned": (np.array(growth["learned_%d" % n]) / ref - 1).tolist(),
             "growth_dev_plain_same_n": (np.array(growth["plain_%d" % n]) / ref - 1).tolist(),
-            "judge": state, "judge_this_run": calc.getDenoiserState(),
+            "check": state, "check_this_run": calc.getDenoiserState(),
             "network_shape": "4-level conv encoder-decoder, 302,561 parameters, BF16 weights, shipped training"}
 
 
@@ -367,7 +367,7 @@ def ring_learned_report(calc, ms_per_turn, n, turns=100, form="fp32"):
             "emittance_growth_turns": turns, "emittance_growth": growth,
             "growth_dev_learned": (np.array(growth["learned_%d" % n]) / ref - 1).tolist(),
             "growth_dev_plain_same_n": (np.array(growth["plain_%d" % n]) / ref - 1).tolist(),
-            "judge": state, "judge_this_run": calc.getDenoiserState(),
+            "check": state, "check_this_run": calc.getDenoiserState(),
             "network_shape": "the shipped 128 x 128-trained convolutional network run on the 256 x 256 grid"}
 
 

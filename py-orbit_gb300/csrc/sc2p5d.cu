@@ -962,7 +962,7 @@ __global__ void k_learn_chk_prep(const ScState* st, ScState* chk) {
   chk->phi_absmax = 0ull;
 }
 
-// The closure's judge: relative rms difference of the potential from the
+// The closure's check: relative rms difference of the potential from the
 // denoised density and the potential from the raw deposit; above `bound`
 // the closure falls back to the plain deposit for the following kicks.
 __global__ void k_learn_compare(ScState* st, const double* __restrict__ phi, const double* __restrict__ phi_raw, int n,
@@ -1717,7 +1717,7 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
   }
   if (dn_check) {
     // the raw deposit solved beside the denoised one (in the calculator's
-    // own precision: its Green spectrum and twiddles), and the judge
+    // own precision: its Green spectrum and twiddles), and the check
     ORBIT_PB("learn_check", s);
     k_learn_chk_prep<<<1, 1, 0, s>>>(c->d_st, c->d_dn_st);
     if (plain)

@@ -1,6 +1,6 @@
 """The learned denoising closure: what the trained network gains over the
 deposit without it, training from scratch on the library's own kernels,
-the closure's judge and fall-back inside the 2.5D kick, and tracking
+the closure's check and fall-back inside the 2.5D kick, and tracking
 against the plain form with many more macroparticles.
 
 Figures: the shipped network's mean squared error against 1e7-particle
@@ -92,7 +92,7 @@ def test_closure_denoises_inside_the_kick():
 def test_closure_with_the_fp32_form():
     """The learned + FP32 form: the closure denoises the FP32 form's float
     deposit (same gain bar as the plain form's), keeps its charge, and the
-    judge solves the raw deposit with the FP32 form's own Green spectrum."""
+    check solves the raw deposit with the FP32 form's own Green spectrum."""
     from orbit_gb300 import _native, call
     from orbit_gb300 import denoiser as DN
     from spacecharge import SpaceChargeCalc2p5D
@@ -137,8 +137,8 @@ def test_closure_with_the_fp32_form():
     assert st2["checks"] == 4 and st2["fallback"] == 0
 
 
-def test_judge_falls_back_on_a_beam_unlike_the_training_beams():
-    """Two separated small blobs score a larger judge error (potential from
+def test_check_falls_back_on_a_beam_unlike_the_training_beams():
+    """Two separated small blobs score a larger check error (potential from
     the denoised against the raw density) than a beam like the training
     beams; with a bound between the two, the calculator falls back on the
     blobs (not on the other beam), and its next deposit is the plain one
@@ -155,19 +155,19 @@ def test_judge_falls_back_on_a_beam_unlike_the_training_beams():
     blobs[4] = rng.normal(0, 10, n)
     usual = W.c2_coords(n, seed=8)
 
-    def judge(soa, bound):
+    def run_check(soa, bound):
         b = _bunch(soa, 1e9)
         calc = SpaceChargeCalc2p5D(128, 128, 64)
         calc.setDenoiser(net, 1, bound)
         calc.trackBunch(b, 0.5)
         return b, calc, calc.getDenoiserState()
 
-    e_usual = judge(usual, 1e9)[2]["last_err"]
-    e_blobs = judge(blobs, 1e9)[2]["last_err"]
+    e_usual = run_check(usual, 1e9)[2]["last_err"]
+    e_blobs = run_check(blobs, 1e9)[2]["last_err"]
     assert e_blobs > 3 * e_usual, (e_blobs, e_usual)
     bound = float(np.sqrt(e_usual * e_blobs))
-    assert judge(usual, bound)[2]["fallback"] == 0
-    b, calc, st = judge(blobs, bound)
+    assert run_check(usual, bound)[2]["fallback"] == 0
+    b, calc, st = run_check(blobs, bound)
     assert st["fallback"] == 1 and st["trips"] == 1, st
     before = b.getCoordinates()
     calc.trackBunch(b, 0.5)
