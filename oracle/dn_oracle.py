@@ -1,7 +1,7 @@
 """Test infrastructure only: a float64 numpy restatement of the learned
 denoiser network of the library (py-orbit_gb300/csrc/dn.cu), its loss and
-its gradients, used as the checker of the device forward and backward
-kernels.  The network has no counterpart in the reference.
+its gradients, against which the tests hold the device forward and
+backward kernels.  The network has no counterpart in the reference.
 
 Parameters are one flat array in the library's order: for each of the 14
 3x3 convolutions W[cout][cin][3][3] then b[cout]; then the 16 weights and

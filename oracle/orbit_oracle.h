@@ -2,7 +2,7 @@
  * ORACLE / TEST INFRASTRUCTURE ONLY.
  *
  * Plain-C restatement of the PyORBIT 2.5D space-charge + TEAPOT hot path,
- * used as the CPU checker for the CUDA path and as the timed CPU baseline
+ * used as the CPU reference of the CUDA path's tests and as the timed CPU baseline
  * ("port").  Every function cites the reference file:line it restates.
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline and
  * reference legs may load it.  It is never linked into the product library.

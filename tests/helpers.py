@@ -1,5 +1,5 @@
 """Shared helpers of the test-suite: tolerances, golden fixtures and the
-oracle runners used as the checker."""
+oracle runners."""
 import os
 
 import numpy as np

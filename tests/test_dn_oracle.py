@@ -1,4 +1,4 @@
-"""The numpy restatement of the denoiser network (the checker of the
+"""The numpy restatement of the denoiser network (the oracle of the
 device kernels): its analytic gradients against central finite
 differences on a small image, and the BF16 rounding it shares with the
 device."""

@@ -1,6 +1,6 @@
 """The C restatement (oracle) against golden vectors produced by the
 reference's own C++ (tests/golden/make_golden.py).  This pins the oracle
-before it is trusted as the GPU checker."""
+before the GPU tests compare against it."""
 import numpy as np
 import pytest
 
