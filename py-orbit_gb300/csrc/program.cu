@@ -29,49 +29,37 @@ static const int kPassSmem = 220 * 1024;
 #define ORBIT_PASS_THREADS 512
 #endif
 
-// Copies n values of global memory (written by an earlier kernel) into
-// shared memory through f, with V-wide vector loads (16 bytes), U of them
-// in flight per thread: one at a time, each load would wait for the shared
-// store before it (which the compiler cannot prove does not alias it), a
-// full L2 round trip per value, and all blocks read the same values at
-// once.  Threads t0.. of the block take part (t0 = 32 leaves warp 0 free).
-// Out of line, so that its registers do not weigh on the particle loop's.
-// g and s are 16-byte aligned; the caller synchronises the block.
-template <int U, typename VT, typename Tin, typename Tout, typename F>
-__device__ __noinline__ void fill_smem(Tout* s, const Tin* g, int n, F f, int t0) {
-  constexpr int V = (int)(sizeof(VT) / sizeof(Tin));
+// Copies n elements of global memory (written by an earlier kernel) into
+// shared memory with asynchronous 16-byte copies (cp.async.cg: no
+// registers held, every copy of the thread in flight at once), then applies
+// f in place to the elements this thread copied, once they have landed
+// (cp.async.wait_all waits for the thread's own copies).  Threads t0.. of
+// the block take part.  Where either address is not 16-byte aligned the
+// thread copies element by element instead.  Returns with this thread's
+// elements final; the caller synchronises the block.
+template <typename T, typename F>
+__device__ __forceinline__ void copy_smem_async(T* s, const T* g, int n, F f, int t0) {
   const int t = (int)threadIdx.x - t0, nt = (int)blockDim.x - t0;
   if (t < 0) return;
-  const int nv = n / V;
-  const VT* gv = reinterpret_cast<const VT*>(g);
-  // each block starts at its own offset, so that the blocks do not all ask
-  // the same L2 lines at the same moment
-  const int off = nv > 0 ? (int)(((long long)blockIdx.x * 1031) % nv) : 0;
-  for (int i0 = t; i0 < nv; i0 += U * nt) {
-    VT v[U];
+  constexpr int E = 16 / (int)sizeof(T);  // elements per 16-byte copy
+  const uint32_t sb = (uint32_t)__cvta_generic_to_shared(s);
+  const bool aligned = ((sb | (uint32_t)(size_t)g) & 15u) == 0u;
+  const int nb = aligned ? n / E : 0;
+  for (int i = t; i < nb; i += nt)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sb + 16u * (uint32_t)i),
+                 "l"(reinterpret_cast<const char*>(g) + 16 * (size_t)i)
+                 : "memory");
+  asm volatile("cp.async.commit_group;" ::: "memory");
+  asm volatile("cp.async.wait_all;" ::: "memory");
+  for (int i = t; i < nb; i += nt) {
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const int i = i0 + u * nt;
-      int j = i + off;
-      j = j >= nv ? j - nv : j;
-      if (i < nv) v[u] = __ldcg(gv + j);
-    }
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const int i = i0 + u * nt;
-      int j = i + off;
-      j = j >= nv ? j - nv : j;
-      if (i < nv) {
-        const Tin* e = reinterpret_cast<const Tin*>(&v[u]);
-#pragma unroll
-        for (int q = 0; q < V; ++q) s[j * V + q] = f(e[q]);
-      }
-    }
+    for (int q = 0; q < E; ++q) s[i * E + q] = f(s[i * E + q]);
   }
-  for (int i = nv * V + t; i < n; i += nt) s[i] = f(__ldcg(g + i));
+  for (int i = nb * E + t; i < n; i += nt) s[i] = f(__ldcg(g + i));
 }
 
-// The kick constants of a pass (one thread), out of line like fill_smem.
+// The kick constants of a pass (one thread), out of line so that their
+// registers do not weigh on the particle loop's.
 __device__ __noinline__ void kick_consts_into(KickConst* k, KickFix* kf, const KickArgs& kick) {
   load_kick_const(*k, kick.st, kick.host_factor, kick.nx, kick.ny, kick.nz, kf == nullptr);
   if (kf) load_kick_fix(*kf, kick.st, k->fac, kick.nx, kick.ny, kick.nz);
@@ -93,7 +81,7 @@ __device__ __forceinline__ void pass_body(double* __restrict__ cx, double* __res
   const long long* Lm = kick.lam_fix;
   const float* Pf = kick.phi_f;
   const float* Lf = kick.lam_f;
-  extern __shared__ unsigned char s_raw[];
+  extern __shared__ __align__(16) unsigned char s_raw[];
   if (KF != 0) {
     // thread 0 computes the kick constants (two FP64 divisions among
     // them) while warps 1.. fill the block's copy of the potential and the
@@ -108,14 +96,18 @@ __device__ __forceinline__ void pass_body(double* __restrict__ cx, double* __res
         // scales the kick constants use
         const int sphi = scale_bits(kick.st->phi_absmax), slam = scale_bits(kick.st->lam_absmax);
         long long* s = reinterpret_cast<long long*>(s_raw);
-        fill_smem<4, double2>(s, kick.phi, ng, [sphi](double v) { return phi_fixed(v, sphi); }, t0);
-        fill_smem<4, double2>(s + ng, kick.lam, kick.nz, [slam](double v) { return phi_fixed(v, slam); }, t0);
+        // the FP64 values land in place and become 64-bit integers there
+        double* sd = reinterpret_cast<double*>(s_raw);
+        copy_smem_async(sd, kick.phi, ng,
+                        [sphi](double v) { return __longlong_as_double(phi_fixed(v, sphi)); }, t0);
+        copy_smem_async(sd + ng, kick.lam, kick.nz,
+                        [slam](double v) { return __longlong_as_double(phi_fixed(v, slam)); }, t0);
         P = s;
         Lm = s + ng;
       } else {
         float* s = reinterpret_cast<float*>(s_raw);
-        fill_smem<4, float4>(s, kick.phi_f, ng, [](float v) { return v; }, t0);
-        fill_smem<4, float4>(s + ng, kick.lam_f, kick.nz, [](float v) { return v; }, t0);
+        copy_smem_async(s, kick.phi_f, ng, [](float v) { return v; }, t0);
+        copy_smem_async(s + ng, kick.lam_f, kick.nz, [](float v) { return v; }, t0);
         Pf = s;
         Lf = s + ng;
       }
