@@ -132,6 +132,7 @@ class Bunch:
         self._host_ok = True     # host copy holds the current coordinates
         self._dev_ok = False     # device copy holds the current coordinates
         self._dev = None         # orbit_gb300.DeviceBunch, created on first device use
+        self._upload_pending = False  # an enqueued upload may still read the host rows
         self._mass = MASS_PROTON
         self._charge = CHARGE_PROTON
         self._classical_radius = CLASSICAL_RADIUS_PROTON
@@ -156,6 +157,10 @@ class Bunch:
                 arr[: self._n, :6] = self._dev.phase_get().T
 
     def _ensure_host(self):
+        if self._upload_pending:
+            # an upload may still read the host rows: let it finish first
+            self._dev.sync()
+            self._upload_pending = False
         self._pull_attrs()
         if not self._host_ok:
             if self._host.shape[1] < self._n:
@@ -182,8 +187,11 @@ class Bunch:
             a[: self._n] = arr[: self._n]
             self._part_attr[name] = a
 
-    def _device_bunch(self):
-        """Device copy with current coordinates and reference-particle data."""
+    def _device_bunch(self, wait=True):
+        """Device copy with current coordinates and reference-particle data.
+        wait=False: an upload is only enqueued on the bunch's stream (so that
+        host work can overlap it); the next host access to the coordinates
+        (_ensure_host) waits for it first."""
         from orbit_gb300 import DeviceBunch, Sync  # noqa: WPS433
         if self._dev is None:
             self._dev = DeviceBunch()
@@ -198,7 +206,10 @@ class Bunch:
                 self._dev.set_macrosizes(self._part_attr["macrosize"][: self._n, 0])
             else:
                 self._dev.set_macrosizes(None)
-            self._dev.sync()
+            if wait:
+                self._dev.sync()
+            else:
+                self._upload_pending = True
             self._dev_ok = True
         if self._sync_dirty:
             s = self._sync

@@ -84,6 +84,7 @@ class TEAPOT_Lattice(AccLattice):
         if paramsDict is None:
             paramsDict = {}
         if actionContainer is None and self._fused and is_device_bunch(bunch):
+            bunch._device_bunch(wait=False)  # the upload overlaps the walk
             prog = self._program(bunch, paramsDict, index_start, index_stop)
             if prog is not None:
                 prog.run(bunch, 1)
@@ -107,6 +108,7 @@ class TEAPOT_Lattice(AccLattice):
         if paramsDict is None:
             paramsDict = {}
         if self._fused and is_device_bunch(bunch):
+            bunch._device_bunch(wait=False)  # the upload overlaps the walk
             prog = self._program(bunch, paramsDict, -1, -1)
             if prog is not None:
                 prog.run(bunch, int(turns))
