@@ -315,7 +315,10 @@ class Bunch:
     def setCoordinates(self, soa, copy=True):
         """Replaces all particles by the (6, n) array.  With copy=False a
         C-contiguous float64 array (e.g. in pinned memory) becomes the host
-        storage itself, so uploads read it directly."""
+        storage itself, so uploads read it directly; an upload that
+        trackBunch enqueued may still read it until the next host access to
+        the coordinates, so write new values into it only after such an
+        access (e.g. getCoordinates) and pass it here again."""
         soa = np.asarray(soa, dtype=np.float64)
         if soa.ndim != 2 or soa.shape[0] != 6:
             raise ValueError("expected a (6, n) array")

@@ -118,3 +118,30 @@ def test_barrier_wait_runs_out_and_is_reported():
     b._device_bunch().sync()
     assert np.array_equal(fused.getPhiGrid().getArray(), sep.getPhiGrid().getArray())
     assert np.array_equal(b.getCoordinates(), b2.getCoordinates())
+
+
+def test_host_edits_after_an_overlapped_upload():
+    """trackBunch enqueues the bunch's upload before the lattice walk and
+    does not wait for it; host reads and edits of the coordinates afterwards
+    wait for that upload first.  The same sequence with every upload waited
+    for beforehand gives the same coordinates."""
+    from orbit_gb300 import workloads as W
+    from spacecharge import SpaceChargeCalc2p5D
+    soa = W.c2_coords(50_000, seed=36)
+    edited = soa.copy()
+    edited[0, :10] += 1e-4
+    out = []
+    for wait in (False, True):
+        calc = SpaceChargeCalc2p5D(64, 64, 16)
+        lat = W.fodo_lattice(calc, cells=4)
+        b = W.make_bunch(soa.copy(), 1e9)
+        steps = [lambda: None,
+                 lambda: b.setCoordinates(edited.copy()),
+                 lambda: [b.x(i, b.x(i) + 1e-5) for i in range(10)]]
+        for edit in steps:
+            edit()
+            if wait:
+                b._device_bunch()        # upload now and wait for it
+            lat.trackBunch(b)
+        out.append(b.getCoordinates())
+    assert np.array_equal(out[0], out[1])
