@@ -470,7 +470,10 @@ static int capture(orbit_program_t* p, orbit_bunch_t* bu, const Plan& plan, bool
 
 static int prepare(orbit_program_t* p, orbit_bunch_t* bu) {
   bool same = p->key_bunch == bu && p->key_n == bu->n && p->key_coords == bu->d_coords &&
-              p->key_msize == bu->has_msize && sync_equal(p->key_sync, bu->sync) && p->g_mid;
+              p->key_msize == bu->has_msize && sync_equal(p->key_sync, bu->sync) && p->g_mid &&
+              p->key_gen.size() == p->calcs.size();
+  for (size_t i = 0; same && i < p->calcs.size(); ++i)
+    same = p->key_gen[i] == (p->calcs[i] ? p->calcs[i]->cfg_gen : 0ull);
   if (same) return ORBIT_OK;
   free_graphs(p);
   Plan plan;
@@ -487,6 +490,8 @@ static int prepare(orbit_program_t* p, orbit_bunch_t* bu) {
   p->key_coords = bu->d_coords;
   p->key_sync = bu->sync;
   p->key_msize = bu->has_msize;
+  p->key_gen.resize(p->calcs.size());
+  for (size_t i = 0; i < p->calcs.size(); ++i) p->key_gen[i] = p->calcs[i] ? p->calcs[i]->cfg_gen : 0ull;
   return ORBIT_OK;
 }
 

@@ -18,6 +18,7 @@ struct orbit_program {
   double* key_coords = nullptr;
   orbit_sync_t key_sync{};
   int key_msize = -1;
+  std::vector<unsigned long long> key_gen;  // the calculators' cfg_gen
   orbit::DevOp* d_ops = nullptr;
   int n_devops = 0;
   double* d_knl = nullptr;            // per-particle 1/(1+dp_p) between passes

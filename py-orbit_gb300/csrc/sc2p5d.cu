@@ -1932,6 +1932,7 @@ int orbit_sc2p5d_set_denoiser(orbit_sc2p5d_t* c, orbit_denoiser_t* dn, int check
   if (!c || (dn && (check_every < 1 || !(bound > 0.0))))
     return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_set_denoiser: bad argument");
   if (c->used) ORBIT_CUDA(cudaEventSynchronize(c->done));
+  ++c->cfg_gen;
   if (!dn) {
     c->dn = nullptr;
     return ORBIT_OK;
@@ -2105,6 +2106,7 @@ int orbit_sc2p5d_get_sizes(const orbit_sc2p5d_t* c, int* nx, int* ny, int* nz, i
 int orbit_sc2p5d_set_fused_conv(orbit_sc2p5d_t* c, int on, int* active) {
   if (!c) return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_set_fused_conv: null handle");
   c->fused_conv = on != 0;
+  ++c->cfg_gen;
   if (active) *active = use_conv_fused(c) ? 1 : 0;
   return ORBIT_OK;
 }
@@ -2113,6 +2115,7 @@ int orbit_sc2p5d_set_conv_wait(orbit_sc2p5d_t* c, long long polls, int withhold)
   if (!c || polls < 1 || withhold < -1) return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_set_conv_wait: bad argument");
   c->conv_wait_polls = polls;
   c->conv_withhold = withhold;
+  ++c->cfg_gen;
   return ORBIT_OK;
 }
 

@@ -156,6 +156,10 @@ struct orbit_sc2p5d {
   void* d_dn_hat = nullptr;
   double* d_dn_phi = nullptr;
   orbit::ScState* d_dn_st = nullptr;
+  // bumped by every setter that changes what an enqueued kick launches or
+  // reads (closure, fused convolution and its waits): lattice programs
+  // captured before it are captured again
+  unsigned long long cfg_gen = 0;
 };
 
 namespace orbit {

@@ -214,3 +214,32 @@ def test_learned_tracking_close_to_plain_with_twenty_times_the_particles():
     assert np.all(np.abs(g_l / g_hi - 1) < 0.02), (g_l, g_hi)
     st = calc.getDenoiserState()
     assert st["fallback"] == 0 and st["checks"] >= 30
+
+
+def test_closure_removed_after_capture_is_captured_again():
+    """A lattice program captured with the closure, then the closure
+    removed: the next run is captured again and runs without it, as a
+    program captured afresh does (bit for bit), and unlike a run that kept
+    the closure."""
+    from orbit_gb300 import denoiser as DN
+    from orbit_gb300 import workloads as W
+    from spacecharge import SpaceChargeCalc2p5D
+    net = DN.default_network()
+    soa = W.c2_coords(100_000, seed=44)
+    out = []
+    for mode in ("removed", "fresh", "kept"):
+        calc = SpaceChargeCalc2p5D(128, 128, 64)
+        calc.setDenoiser(net, 10, 1e-3)
+        with contextlib.redirect_stdout(io.StringIO()):
+            lat = W.fodo_lattice(calc, cells=3)
+        b = W.make_bunch(soa.copy(), W.C2_MACROSIZE * 10)
+        lat.trackBunch(b)
+        if mode != "kept":
+            calc.setDenoiser(None)
+        if mode == "fresh":
+            with contextlib.redirect_stdout(io.StringIO()):
+                lat = W.fodo_lattice(calc, cells=3)
+        lat.trackBunch(b)
+        out.append(b.getCoordinates())
+    assert np.array_equal(out[0], out[1])
+    assert not np.array_equal(out[0], out[2])
