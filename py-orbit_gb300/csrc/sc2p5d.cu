@@ -4,7 +4,6 @@
 // PoissonSolverFFT2D.cc:115-256, Grid2D.cc, Grid1D.cc).
 #include <cmath>
 #include <cstring>
-#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -2177,24 +2176,14 @@ static constexpr size_t kStaticScratchBytes =
 // (about 2.1 MB).  Shared by all calls: calls that overlap on the GPU race.
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
 
-// Device address of the array per device ordinal, looked up once per device
-// (with that device current) under a lock, so that host threads calling
-// concurrently do not race on the table.
-static unsigned char* g_static_ptr[256];
-static std::mutex g_static_lock;
-
+// Device address of the array in the current context, looked up on every
+// call (a runtime table lookup): nothing is cached, so a new primary
+// context after a device reset is seen and host threads share no state.
 static int static_scratch_ptr(unsigned char** out) {
-  int dev = 0;
-  ORBIT_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 256) return set_error(ORBIT_ERR_UNSUPPORTED, "orbit_sc2p5d_track_static: device ordinal");
-  std::lock_guard<std::mutex> guard(g_static_lock);
-  if (!g_static_ptr[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
-    if (e != cudaSuccess) return cuda_error(e, "orbit_sc2p5d_track_static: cudaGetSymbolAddress");
-    g_static_ptr[dev] = (unsigned char*)p;
-  }
-  *out = g_static_ptr[dev];
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+  if (e != cudaSuccess) return cuda_error(e, "orbit_sc2p5d_track_static: cudaGetSymbolAddress");
+  *out = (unsigned char*)p;
   return ORBIT_OK;
 }
 
