@@ -34,7 +34,7 @@ extern "C" {
 #define ORBIT_ERR_GRID (-3)     /* grid too small (Grid2D.cc:40-51, Grid1D.cc:70-82) */
 #define ORBIT_ERR_CUDA (-4)     /* CUDA runtime error */
 #define ORBIT_ERR_NAN (-5)      /* non-finite coordinate met by the extrema scan */
-#define ORBIT_ERR_DEVICE (-6)   /* device-side range check failed */
+#define ORBIT_ERR_DEVICE (-6)   /* device-side check failed (range check, bounded barrier wait ran out) */
 #define ORBIT_ERR_NOMEM (-8)    /* device allocation failed */
 #define ORBIT_ERR_UNSUPPORTED (-9)
 
