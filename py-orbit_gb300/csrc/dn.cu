@@ -555,14 +555,30 @@ __global__ void k_upcat_bwd(const float* __restrict__ dout, int ca, float* __res
 
 // y[n][0] = x0[n][0] + b + sum_c w[c] h[n][c] (1x1 output convolution plus
 // the input: the network predicts the correction to the noisy density).
+// With `parts`, block k also writes the sum of its outputs clamped at zero
+// to parts[k] (a fixed order within the block: the learned closure sums
+// the parts in block order, so its charge scale is the same on every run).
 __global__ void k_out(const float* __restrict__ h, int C, const float* __restrict__ w, const float* __restrict__ b,
-                      const float* __restrict__ x0, float* __restrict__ y, int N, int HW) {
+                      const float* __restrict__ x0, float* __restrict__ y, int N, int HW,
+                      double* __restrict__ parts) {
   size_t tot = (size_t)N * HW;
+  double acc = 0.0;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < tot; i += (size_t)gridDim.x * blockDim.x) {
     size_t n = i / HW, p = i % HW;
     float s = x0[i] + b[0];
     for (int c = 0; c < C; ++c) s = fmaf(w[c], h[(n * C + c) * HW + p], s);
     y[i] = s;
+    acc += fmaxf(s, 0.f);
+  }
+  if (!parts) return;
+  __shared__ double s_part[32];
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+  if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += s_part[q];
+    parts[blockIdx.x] = t;
   }
 }
 
@@ -986,7 +1002,7 @@ static int conv_fwd_tc(orbit_denoiser_t* d, const Step3& s, cudaStream_t st, con
 // tensor-core layers again.
 static bool g_tc_untrusted = false;
 
-static int forward(orbit_denoiser_t* d, int nb, cudaStream_t st, bool infer = false) {
+static int forward(orbit_denoiser_t* d, int nb, cudaStream_t st, bool infer = false, double* parts = nullptr) {
   const bool tc = infer && d->tc && !d->tc_failed && !g_tc_untrusted && nb == 1;
   if (tc && d->tc_stale) {
     int rc = tc_pack(d, st);
@@ -1048,7 +1064,7 @@ static int forward(orbit_denoiser_t* d, int nb, cudaStream_t st, bool infer = fa
   if (rc) return rc;
   const size_t hw = (size_t)d->H * d->W;
   k_out<<<grid_1d(nb * hw), 256, 0, st>>>(d->act[D1], 16, d->d_p + d->out_w, d->d_p + d->out_b, d->act[X0],
-                                          d->act[Y], nb, (int)hw);
+                                          d->act[Y], nb, (int)hw, parts);
   ORBIT_LAUNCH_CHECK("denoiser out");
   return ORBIT_OK;
 }
@@ -1182,6 +1198,19 @@ static cudaStream_t stream_of(orbit_denoiser_t* d, void* s) { return s ? (cudaSt
 static int check_batch(const orbit_denoiser_t* d, int nb) {
   if (nb < 1 || nb > d->maxb) return set_error(ORBIT_ERR_ARG, "orbit_denoiser: batch size outside 1..max_batch");
   return ORBIT_OK;
+}
+
+int dn_closure_io(orbit_denoiser_t* d, float** in, const float** out, int* nparts) {
+  if (!d) return set_error(ORBIT_ERR_ARG, "dn_closure_io: null network");
+  *in = d->act[X0];
+  *out = d->act[Y];
+  *nparts = grid_1d((size_t)d->H * d->W);
+  return ORBIT_OK;
+}
+
+int dn_forward_inplace(orbit_denoiser_t* d, cudaStream_t st, double* parts) {
+  if (!d) return set_error(ORBIT_ERR_ARG, "dn_forward_inplace: null network");
+  return forward(d, 1, st, true, parts);
 }
 
 }  // namespace orbit

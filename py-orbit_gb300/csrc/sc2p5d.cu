@@ -904,10 +904,9 @@ __global__ void k_fields(const ScState* st, const double* __restrict__ phi, cons
 // ---------------------------------------------------------------------
 // The fixed-point deposit as the network's image (density * scale, scale =
 // nx ny / total macrosize: unit mean) and, on check kicks, the raw density.
-__global__ void k_learn_in(ScState* st, const unsigned long long* __restrict__ rho_q, float* __restrict__ img,
-                           double* __restrict__ raw, int n, double scale) {
+__global__ void k_learn_in(const ScState* st, const unsigned long long* __restrict__ rho_q,
+                           float* __restrict__ img, double* __restrict__ raw, int n, double scale) {
   if (st->skip) return;
-  if (blockIdx.x == 0 && threadIdx.x == 0) st->dn_sum = 0.0;
   const double iq = st->inv_qscale;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     double v = (double)(long long)rho_q[i] * iq;
@@ -916,10 +915,16 @@ __global__ void k_learn_in(ScState* st, const unsigned long long* __restrict__ r
   }
 }
 
-// Sum of the network output clamped at zero (a density is not negative).
-// A network that reported a failed tensor-core wait (net_err != 0) produced
-// no valid output: the closure falls back to the plain deposit for good.
-__global__ void k_learn_sum(ScState* st, const float* __restrict__ out, int n, const int* __restrict__ net_err) {
+// The network output clamped at zero (a density is not negative), rescaled
+// to the deposit's total charge (n in image units) and written back as the
+// fixed-point deposit the solve reads.  The output's sum is the network's
+// per-block sums (`parts`) added in block order by warp 0 of every block:
+// the same on every run.  A network that reported a failed tensor-core wait
+// (net_err != 0) produced no valid output: the closure falls back to the
+// plain deposit for good; nothing is written once it has fallen back.
+__global__ void k_learn_out(ScState* st, const float* __restrict__ out, unsigned long long* __restrict__ rho_q, int n,
+                            double scale, const double* __restrict__ parts, int nparts,
+                            const int* __restrict__ net_err) {
   if (st->skip) return;
   if (*net_err) {
     if (blockIdx.x == 0 && threadIdx.x == 0 && !st->dn_fallback) {
@@ -928,26 +933,16 @@ __global__ void k_learn_sum(ScState* st, const float* __restrict__ out, int n, c
     }
     return;
   }
-  __shared__ double s_part[32];
-  double s = 0.0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) s += fmaxf(out[i], 0.f);
-  for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-  if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = s;
-  __syncthreads();
-  if (threadIdx.x == 0) {
+  if (st->dn_fallback) return;
+  __shared__ double s_sum;
+  if (threadIdx.x < 32) {
     double t = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_part[w];
-    atomicAdd(&st->dn_sum, t);
+    for (int k = threadIdx.x; k < nparts; k += 32) t += parts[k];
+    for (int off = 16; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+    if (threadIdx.x == 0) s_sum = t;
   }
-}
-
-// The clamped network output, rescaled to the deposit's total charge (n in
-// image units), written back as the fixed-point deposit the solve reads;
-// nothing is written once the closure has fallen back.
-__global__ void k_learn_out(ScState* st, const float* __restrict__ out, unsigned long long* __restrict__ rho_q, int n,
-                            double scale) {
-  if (st->skip || st->dn_fallback) return;
-  const double sum = st->dn_sum;
+  __syncthreads();
+  const double sum = s_sum;
   if (!(sum > 0.0)) return;
   const double back = ((double)n / sum) / (scale * st->inv_qscale);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -964,7 +959,7 @@ __global__ void k_learn_chk_prep(const ScState* st, ScState* chk) {
 // The closure's check: relative rms difference of the potential from the
 // denoised density and the potential from the raw deposit; above `bound`
 // the closure falls back to the plain deposit for the following kicks.
-__global__ void k_learn_compare(ScState* st, const double* __restrict__ phi, const double* __restrict__ phi_raw, int n,
+__global__ void __launch_bounds__(1024) k_learn_compare(ScState* st, const double* __restrict__ phi, const double* __restrict__ phi_raw, int n,
                                 double bound) {
   if (st->skip) return;
   __shared__ double s_d[32], s_r[32];
@@ -1672,18 +1667,23 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
       int gb = (ng + 255) / 256;
       if (gb > num_sms() * 2) gb = num_sms() * 2;
       ORBIT_PB("learn_in", s);
-      k_learn_in<<<gb, 256, 0, s>>>(c->d_st, c->d_rho_q, c->d_dn_img, dn_check ? c->d_dn_raw : nullptr, ng,
-                                    dn_scale);
+      float* img = nullptr;
+      const float* out = nullptr;
+      int nparts = 0;
+      rc = dn_closure_io(c->dn, &img, &out, &nparts);
+      if (rc) return rc;
+      if (nparts > kDnMaxParts) return set_error(ORBIT_ERR_UNSUPPORTED, "the learned closure's grid is too large");
+      k_learn_in<<<gb, 256, 0, s>>>(c->d_st, c->d_rho_q, img, dn_check ? c->d_dn_raw : nullptr, ng, dn_scale);
       ORBIT_PE(s);
       ORBIT_PB("learn_network", s);
-      rc = orbit_denoiser_forward(c->dn, c->d_dn_img, c->d_dn_out, 1, (void*)s);
+      rc = dn_forward_inplace(c->dn, s, c->d_dn_parts);
       ORBIT_PE(s);
       if (rc) return rc;
       ORBIT_PB("learn_out", s);
-      k_learn_sum<<<gb, 256, 0, s>>>(c->d_st, c->d_dn_out, ng, dn_error_flag(c->dn));
-      k_learn_out<<<gb, 256, 0, s>>>(c->d_st, c->d_dn_out, c->d_rho_q, ng, dn_scale);
+      k_learn_out<<<gb, 256, 0, s>>>(c->d_st, out, c->d_rho_q, ng, dn_scale, c->d_dn_parts, nparts,
+                                     dn_error_flag(c->dn));
       ORBIT_PE(s);
-      nl += 3;
+      nl += 2;
       ORBIT_LAUNCH_CHECK("sc2p5d learned closure");
     }
   }
@@ -1723,7 +1723,7 @@ int sc_enqueue_kick(orbit_sc2p5d_t* c, orbit_bunch_t* b, double length, cudaStre
       enqueue_check_solve<double>(c, s);
     else
       enqueue_check_solve<float>(c, s);
-    k_learn_compare<<<1, 256, 0, s>>>(c->d_st, c->d_phi, c->d_dn_phi, c->nx * c->ny, c->dn_bound);
+    k_learn_compare<<<1, 1024, 0, s>>>(c->d_st, c->d_phi, c->d_dn_phi, c->nx * c->ny, c->dn_bound);
     ORBIT_PE(s);
     nl += 5;
     ORBIT_LAUNCH_CHECK("sc2p5d learned closure check");
@@ -1919,7 +1919,7 @@ int orbit_sc2p5d_destroy(orbit_sc2p5d_t* c) {
   if (c->aux) cudaStreamDestroy(c->aux);
   void* ptrs[] = {c->d_st, c->d_rho_q, c->d_z_q, c->d_rho, c->d_phi, c->d_lam, c->d_lamd,
                   c->d_phi_f, c->d_lam_f, c->d_hat, c->d_green, c->d_gbuf, c->d_gscratch, c->d_tw_x, c->d_tw_y,
-                  c->d_phi_fix, c->d_lam_fix, c->d_dn_img, c->d_dn_out, c->d_dn_raw, c->d_dn_hat, c->d_dn_phi,
+                  c->d_phi_fix, c->d_lam_fix, c->d_dn_parts, c->d_dn_raw, c->d_dn_hat, c->d_dn_phi,
                   c->d_dn_st};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -1944,9 +1944,8 @@ int orbit_sc2p5d_set_denoiser(orbit_sc2p5d_t* c, orbit_denoiser_t* dn, int check
   if (h != c->nx || w != c->ny)
     return set_error(ORBIT_ERR_ARG, "orbit_sc2p5d_set_denoiser: the network's image size differs from the grid");
   const size_t ng = (size_t)c->nx * c->ny;
-  if (!c->d_dn_img) {
-    ORBIT_CUDA(cudaMalloc(&c->d_dn_img, sizeof(float) * ng));
-    ORBIT_CUDA(cudaMalloc(&c->d_dn_out, sizeof(float) * ng));
+  if (!c->d_dn_parts) {
+    ORBIT_CUDA(cudaMalloc(&c->d_dn_parts, sizeof(double) * kDnMaxParts));
     ORBIT_CUDA(cudaMalloc(&c->d_dn_raw, sizeof(double) * ng));
     ORBIT_CUDA(cudaMalloc(&c->d_dn_hat, sizeof(double2) * (size_t)c->nx2 * c->H));
     ORBIT_CUDA(cudaMalloc(&c->d_dn_phi, sizeof(double) * ng));

@@ -32,12 +32,10 @@ struct ScState {
   double rb_xc, rb_yc, rb_a2, rb_lin, rb_lout;
   unsigned long long n_kicks, n_green;                    // kicks solved, Green spectra rebuilt
   // learned closure: fallen back to the plain deposit (sticky), the last
-  // check's relative rms potential difference, checks and fall-backs, and
-  // the sum of the clamped network output
+  // check's relative rms potential difference, checks and fall-backs
   int dn_fallback;
   double dn_err;
   unsigned long long dn_checks, dn_trips;
-  double dn_sum;
   // arrival counters of the fused convolution's two grid-wide barriers,
   // zeroed by every kick's set-up
   unsigned conv_bar[2];
@@ -98,6 +96,13 @@ struct orbit_denoiser;
 namespace orbit {
 // The denoiser's device error flag (tensor-core waits that gave up).
 int* dn_error_flag(orbit_denoiser* d);
+// Forward of one image in place for the learned closure: the caller writes
+// the image into *in and reads the output from *out (the network's own
+// input and output activations: no copies); dn_forward_inplace also writes
+// *nparts per-block sums of the output clamped at zero into parts.
+int dn_closure_io(orbit_denoiser* d, float** in, const float** out, int* nparts);
+int dn_forward_inplace(orbit_denoiser* d, cudaStream_t st, double* parts);
+constexpr int kDnMaxParts = 4096;  // sums the closure's buffer holds
 }  // namespace orbit
 
 struct orbit_sc2p5d {
@@ -143,15 +148,14 @@ struct orbit_sc2p5d {
   int n_long_avg = 3;
   double* d_lamd = nullptr;               // derivative grid (nz)
   int dep_threads = 512, kick_threads = 512;
-  // learned closure (plain form): the network, the check period and bound,
-  // the host kick counter, and the image, raw-density and check-solve
-  // buffers
+  // learned closure (both forms): the network, the check period and bound,
+  // the host kick counter, and the output-sum, raw-density and check-solve
+  // buffers (the image and the output are the network's own)
   orbit_denoiser* dn = nullptr;
   int dn_every = 10;
   double dn_bound = 0.05;
   long long dn_count = 0;
-  float* d_dn_img = nullptr;
-  float* d_dn_out = nullptr;
+  double* d_dn_parts = nullptr;  // the network's per-block sums of its clamped output
   double* d_dn_raw = nullptr;
   void* d_dn_hat = nullptr;
   double* d_dn_phi = nullptr;
