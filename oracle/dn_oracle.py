@@ -120,13 +120,18 @@ def forward(p, x0, tf32_inputs=False):
     return A["y"], A
 
 
-def loss_and_grads(p, x0, t, weights=None):
+def loss_and_grads(p, x0, t, weights=None, tf32_operands=False):
     """The loss, the flat parameter gradient and the output.  Loss: the mean
     squared error, or with `weights` (w_0..w_L) the multi-scale loss
     sum_s w_s mean((P^s y - P^s t)^2), P the 2x2 average pooling, whose
-    gradient is sum_s w_s (P^T)^s 2 (P^s y - P^s t) / n_s."""
+    gradient is sum_s w_s (P^T)^s 2 (P^s y - P^s t) / n_s.  With
+    tf32_operands, the operands the device's batched tensor-core layers
+    round to TF32 are rounded here too: the input of every 3x3 convolution
+    in the forward pass and the output gradient entering every data
+    gradient (the weight gradients use the unrounded values, as the
+    device's CUDA-core weight-gradient kernel does)."""
     ws, ow, ob = unpack(p)
-    y, A = forward(p, x0)
+    y, A = forward(p, x0, tf32_inputs=tf32_operands)
     t = np.asarray(t, dtype=np.float64)
     n = y.size
     if not weights:
@@ -156,6 +161,8 @@ def loss_and_grads(p, x0, t, weights=None):
     def cb(k):
         dpre = D[outs[k]] * (A[outs[k]] > 0)
         dW, db, dx = conv3_bwd(A[srcs[k]], ws[k][0], dpre)
+        if tf32_operands:
+            dx = conv3_bwd(A[srcs[k]], ws[k][0], tf32(dpre))[2]
         w, b, ci, co = convs[k]
         g[w:w + ci * co * 9] = dW.ravel()
         g[b:b + co] = db

@@ -341,6 +341,154 @@ __global__ void __launch_bounds__(128) k_conv3_tc(const float* __restrict__ in, 
   }
 }
 
+// Batched 3x3 layer on the tensor cores (training and batched forwards):
+// a CTA computes 128 consecutive pixels of the nb images (pixel p of image
+// p / HW) x N output channels and loops over every K stage of 32 (k = tap
+// * cin + ci) with the accumulators in TMEM: per stage the im2col rows and
+// the packed weight stage are staged in shared memory (the single-image
+// layout), one thread issues four MMAs, and the block waits on their
+// commit (phase s of the barrier) before the next stage reuses the buffers.
+// MODE 0: out = max(acc + bias, 0) (forward); MODE 1: out = acc (the data
+// gradient: `in` is the output gradient, the weights packed flipped and
+// transposed by k_pack_tc_t).  The waits are bounded as in k_conv3_tc; a
+// block whose wait gives up writes nothing.
+static const int kTcbSmem = kTcStageA + 128 * kTcKC * 4 + 1024;  // N <= 128
+
+template <int N, int MODE>
+__global__ void __launch_bounds__(128) k_conv3_tcb(const float* __restrict__ in, int cin, int H, int W, int nb,
+                                                   const float* __restrict__ wpk, int nst,
+                                                   const float* __restrict__ bias, float* __restrict__ out,
+                                                   int* err, TcWait tw) {
+  static_assert(N % 16 == 0 && N >= 16 && N <= 128, "MMA N");
+  constexpr int BV = N * kTcKC / 4 / 128;                          // float4 of a B stage per thread
+  constexpr uint32_t COLS = N <= 32 ? 32u : (N <= 64 ? 64u : 128u);  // TMEM columns (a power of two)
+  extern __shared__ unsigned char tc_raw[];
+  __shared__ __align__(8) uint64_t s_bar;
+  __shared__ uint32_t s_tmem;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const uint32_t raw = smem_u32(tc_raw);
+  const uint32_t sA = (raw + 1023u) & ~1023u, sB = sA + kTcStageA;
+  unsigned char* gA = tc_raw + (sA - raw);
+  const int HW = H * W;
+  const long long P = (long long)nb * HW;
+  const long long p = (long long)blockIdx.x * kTcM + tid;
+  const bool pin = p < P;
+  const int img = pin ? (int)(p / HW) : 0;
+  const int q = pin ? (int)(p % HW) : 0;
+  const int py = q / W, px = q % W;
+  const float* src = in + (size_t)img * cin * HW;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&s_tmem)),
+                 "r"(COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s_bar)));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = s_tmem;
+  unsigned char* a_row = gA + (tid >> 3) * 1024 + (tid & 7) * 16;
+  float4* dstB = reinterpret_cast<float4*>(gA + kTcStageA);
+  bool ok = true;
+  int s = 0;
+  // the next stage's global loads are issued before the wait on this
+  // stage's MMAs, so their latency overlaps the tensor-core work
+  float va[kTcKC];
+  float4 vb[BV];
+  auto load_stage = [&](int st) {
+    tc_load_a(src, cin, H, W, HW, cin * 9, pin, py, px, st, va);
+    const float4* srcB = reinterpret_cast<const float4*>(wpk + (size_t)st * N * kTcKC);
+#pragma unroll
+    for (int i = 0; i < BV; ++i) vb[i] = __ldg(srcB + tid + 128 * i);
+  };
+  load_stage(0);
+  for (; s < nst; ++s) {
+#pragma unroll
+    for (int u = 0; u < kTcKC / 4; ++u)
+      *reinterpret_cast<float4*>(a_row + u * 128) =
+          make_float4(to_tf32(va[4 * u]), to_tf32(va[4 * u + 1]), to_tf32(va[4 * u + 2]), to_tf32(va[4 * u + 3]));
+#pragma unroll
+    for (int i = 0; i < BV; ++i) dstB[tid + 128 * i] = vb[i];
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (tid == 0 && !tw.withhold) {
+#pragma unroll
+      for (int j = 0; j < kTcKC / 8; ++j) {
+        const uint64_t ad = tc_desc(sA + 256u * j), bd = tc_desc(sB + 256u * j);
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(tc_idesc(N)), "r"((s > 0 || j > 0) ? 1u : 0u));
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       smem_u32(&s_bar))
+                   : "memory");
+    }
+    if (s + 1 < nst) load_stage(s + 1);
+    // the MMAs of this stage read the buffers the next stage overwrites
+    ok = __syncthreads_and(mbar_wait_bounded(smem_u32(&s_bar), (uint32_t)(s & 1), tw.cycles));
+    if (!ok) break;
+  }
+  if (!ok) {
+    if (tid == 0) atomicOr(err, 1);
+    if (!tw.withhold &&
+        !__syncthreads_and(mbar_wait_bounded(smem_u32(&s_bar), (uint32_t)(s & 1), tw.cycles)) && tid == 0)
+      atomicOr(err, 2);
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  if (ok) {
+    // row tid of D: TMEM lane 32 * warp + lane, columns 0..N-1
+    float* dst = out + (size_t)img * N * HW + q;
+#pragma unroll
+    for (int c0 = 0; c0 < N; c0 += 16) {
+      uint32_t r[16];
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0));
+      asm volatile("tcgen05.wait::ld.sync.aligned;");
+      if (pin) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const float v = __uint_as_float(r[j]);
+          dst[(size_t)(c0 + j) * HW] = MODE == 0 ? fmaxf(v + bias[c0 + j], 0.f) : v;
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(COLS));
+  }
+}
+
+// The data-gradient weights of one layer (cout x cin x 3 x 3, BF16) packed
+// for k_conv3_tcb<cin, 1>: output row ci, K column k = tap' * cout + o with
+// the flipped tap (weight W[o][ci][8 - tap']), stages of 32 in the layout of
+// k_pack_tc; zero for k >= 9 cout.
+__global__ void k_pack_tc_t(const __nv_bfloat16* __restrict__ w, int cout, int cin, int nst, float* __restrict__ out) {
+  const int total = nst * cin * kTcKC;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    const int st = i / (cin * kTcKC), r = i % (cin * kTcKC);
+    const int ci = r / kTcKC, kk = r % kTcKC;
+    const int k = st * kTcKC + kk;
+    float v = 0.f;
+    if (k < 9 * cout) {
+      const int tap = k / cout, o = k % cout;
+      v = __bfloat162float(w[((size_t)o * cin + ci) * 9 + (8 - tap)]);
+    }
+    out[(size_t)st * cin * kTcKC + (ci >> 3) * 256 + (kk >> 2) * 32 + (ci & 7) * 4 + (kk & 3)] = v;
+  }
+}
+
 // Packs the BF16 weights of one layer into the per-stage shared-memory
 // image of k_conv3_tc: row o, K column k = tap * cin + ci (weight
 // W[o][ci][tap]) of stage s = k / 32 at float index s * N * 32 + (o / 8) *
@@ -823,6 +971,12 @@ struct orbit_denoiser {
   float* d_wtc = nullptr;
   std::vector<size_t> tc_off;
   int* d_err = nullptr;
+  // batches (training and batched forwards) on the tensor cores: forward
+  // layers from d_wtc, data gradients from the flipped, transposed packing
+  bool tcb = false;
+  bool tct_stale = true;
+  float* d_wtct = nullptr;
+  std::vector<size_t> tct_off;
   // training loss: 0 levels = mean squared error; L levels = the
   // multi-scale loss sum_s w_s mean((P^s y - P^s t)^2), P = 2x2 average
   // pooling, with its pooled outputs, targets and gradients per level
@@ -925,6 +1079,69 @@ static int tc_pack(orbit_denoiser_t* d, cudaStream_t st) {
   return ORBIT_OK;
 }
 
+static int tc_pack_t(orbit_denoiser_t* d, cudaStream_t st) {
+  for (size_t l = 0; l < d->conv.size(); ++l) {
+    const Conv& cv = d->conv[l];
+    if (cv.cin < 16) continue;  // the first layer's input gets no gradient
+    const int nst = (cv.cout * 9 + kTcKC - 1) / kTcKC;
+    k_pack_tc_t<<<grid_1d((size_t)nst * cv.cin * kTcKC), 256, 0, st>>>(d->d_pb + cv.w_off, cv.cout, cv.cin, nst,
+                                                                        d->d_wtct + d->tct_off[l]);
+  }
+  ORBIT_LAUNCH_CHECK("denoiser tensor-core data-gradient weight packing");
+  d->tct_stale = false;
+  return ORBIT_OK;
+}
+
+template <int N, int MODE>
+static void launch_tcb(const orbit_denoiser_t* d, cudaStream_t st, const float* in, int cin, int h, int w, int nb,
+                       const float* wp, int nst, const float* bias, float* out) {
+  const long long P = (long long)nb * h * w;
+  const int blocks = (int)((P + kTcM - 1) / kTcM);
+  const TcWait tw = {d->tc_wait_cycles, d->tc_withhold};
+  k_conv3_tcb<N, MODE><<<blocks, 128, kTcbSmem, st>>>(in, cin, h, w, nb, wp, nst, bias, out, d->d_err, tw);
+}
+
+// Forward of one 3x3 layer for nb images on the tensor cores.
+static int conv_fwd_tcb(orbit_denoiser_t* d, const Step3& s, int nb, cudaStream_t st) {
+  const Conv& cv = d->conv[s.ci];
+  int c, h, w;
+  act_shape(d, s.out, &c, &h, &w);
+  const int nst = (cv.cin * 9 + kTcKC - 1) / kTcKC;
+  const float* wp = d->d_wtc + d->tc_off[s.ci];
+  const float* B = d->d_p + cv.b_off;
+  switch (cv.cout) {
+    case 16: launch_tcb<16, 0>(d, st, d->act[s.in], cv.cin, h, w, nb, wp, nst, B, d->act[s.out]); break;
+    case 32: launch_tcb<32, 0>(d, st, d->act[s.in], cv.cin, h, w, nb, wp, nst, B, d->act[s.out]); break;
+    case 64: launch_tcb<64, 0>(d, st, d->act[s.in], cv.cin, h, w, nb, wp, nst, B, d->act[s.out]); break;
+    default: return set_error(ORBIT_ERR_ARG, "denoiser: tensor-core layer width not supported");
+  }
+  ORBIT_LAUNCH_CHECK("denoiser tensor-core batched conv");
+  return ORBIT_OK;
+}
+
+// Data gradient of one 3x3 layer for nb images on the tensor cores:
+// grad[in] = grad[out] convolved with the flipped, transposed kernel.
+static int conv_dgrad_tcb(orbit_denoiser_t* d, const Step3& s, int nb, cudaStream_t st) {
+  const Conv& cv = d->conv[s.ci];
+  int c, h, w;
+  act_shape(d, s.out, &c, &h, &w);
+  const int nst = (cv.cout * 9 + kTcKC - 1) / kTcKC;
+  const float* wp = d->d_wtct + d->tct_off[s.ci];
+  const float* gi = d->grad[s.out];
+  float* go = d->grad[s.in];
+  switch (cv.cin) {
+    case 16: launch_tcb<16, 1>(d, st, gi, cv.cout, h, w, nb, wp, nst, nullptr, go); break;
+    case 32: launch_tcb<32, 1>(d, st, gi, cv.cout, h, w, nb, wp, nst, nullptr, go); break;
+    case 48: launch_tcb<48, 1>(d, st, gi, cv.cout, h, w, nb, wp, nst, nullptr, go); break;
+    case 64: launch_tcb<64, 1>(d, st, gi, cv.cout, h, w, nb, wp, nst, nullptr, go); break;
+    case 96: launch_tcb<96, 1>(d, st, gi, cv.cout, h, w, nb, wp, nst, nullptr, go); break;
+    case 128: launch_tcb<128, 1>(d, st, gi, cv.cout, h, w, nb, wp, nst, nullptr, go); break;
+    default: return set_error(ORBIT_ERR_ARG, "denoiser: tensor-core data-gradient width not supported");
+  }
+  ORBIT_LAUNCH_CHECK("denoiser tensor-core data gradient");
+  return ORBIT_OK;
+}
+
 template <int N>
 static void launch_conv_tc(dim3 g, cudaStream_t st, bool split, const float* in, int cin, int h, int w,
                            const float* wp, const float* bias, float* out, float* part, int nst, int* err,
@@ -1002,14 +1219,17 @@ static int conv_fwd_tc(orbit_denoiser_t* d, const Step3& s, cudaStream_t st, con
 // tensor-core layers again.
 static bool g_tc_untrusted = false;
 
+static bool use_tcb(const orbit_denoiser_t* d) { return d->tcb && !d->tc_failed && !g_tc_untrusted; }
+
 static int forward(orbit_denoiser_t* d, int nb, cudaStream_t st, bool infer = false, double* parts = nullptr) {
   const bool tc = infer && d->tc && !d->tc_failed && !g_tc_untrusted && nb == 1;
-  if (tc && d->tc_stale) {
+  const bool tcb = !tc && use_tcb(d);
+  if ((tc || tcb) && d->tc_stale) {
     int rc = tc_pack(d, st);
     if (rc) return rc;
   }
   auto conv_fwd = [&](orbit_denoiser_t* dd, const Step3& stp, int n, cudaStream_t ss) -> int {
-    return conv_fwd_cc(dd, stp, n, ss);
+    return tcb ? conv_fwd_tcb(dd, stp, n, ss) : conv_fwd_cc(dd, stp, n, ss);
   };
   auto pool = [&](int a, int b) -> int {
     int c, h, w;
@@ -1087,9 +1307,18 @@ static int conv_bwd(orbit_denoiser_t* d, const Step3& s, int nb, cudaStream_t st
                                     d->d_g + cv.b_off);
   if (s.in != X0) {
     // data gradient: dy convolved with the flipped, transposed kernel
-    dim3 gd(tiles, (cv.cin + kCo - 1) / kCo, nb);
-    k_conv3<true, false><<<gd, 256, 0, st>>>(d->grad[s.out], cv.cout, d->d_pb + cv.w_off, nullptr, d->grad[s.in],
-                                             cv.cin, h, w);
+    if (use_tcb(d)) {
+      if (d->tct_stale) {
+        int rc = tc_pack_t(d, st);
+        if (rc) return rc;
+      }
+      int rc = conv_dgrad_tcb(d, s, nb, st);
+      if (rc) return rc;
+    } else {
+      dim3 gd(tiles, (cv.cin + kCo - 1) / kCo, nb);
+      k_conv3<true, false><<<gd, 256, 0, st>>>(d->grad[s.out], cv.cout, d->d_pb + cv.w_off, nullptr,
+                                               d->grad[s.in], cv.cin, h, w);
+    }
   }
   ORBIT_LAUNCH_CHECK("denoiser conv backward");
   return ORBIT_OK;
@@ -1198,6 +1427,20 @@ static cudaStream_t stream_of(orbit_denoiser_t* d, void* s) { return s ? (cudaSt
 static int check_batch(const orbit_denoiser_t* d, int nb) {
   if (nb < 1 || nb > d->maxb) return set_error(ORBIT_ERR_ARG, "orbit_denoiser: batch size outside 1..max_batch");
   return ORBIT_OK;
+}
+
+// After a synchronised batched step on the tensor cores: a bounded wait
+// that gave up (error bits set) makes the network run on the CUDA cores
+// from now on, and the step reports the error.
+static int tcb_status(orbit_denoiser_t* d) {
+  if (!d->tcb || d->tc_failed) return ORBIT_OK;
+  int err = 0;
+  ORBIT_CUDA(cudaMemcpy(&err, d->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (!err) return ORBIT_OK;
+  ORBIT_CUDA(cudaMemset(d->d_err, 0, sizeof(int)));
+  d->tc_failed = true;
+  if (err & 2) g_tc_untrusted = true;
+  return set_error(ORBIT_ERR_DEVICE, "denoiser: a tensor-core wait gave up; the network now runs on the CUDA cores");
 }
 
 int dn_closure_io(orbit_denoiser_t* d, float** in, const float** out, int* nparts) {
@@ -1353,11 +1596,13 @@ int orbit_denoiser_create(orbit_denoiser_t** out, int max_batch, int h, int w, u
       split_plan(d->conv[stp.ci], hh, ww, nb, &sp, &cp);
       if (sp > 1) scratch = std::max(scratch, (size_t)sp * act_size(d, stp.out, nb));
     }
-  size_t wtc = 0;
+  size_t wtc = 0, wtct = 0;
   for (size_t l = 0; l < d->conv.size(); ++l) {
     const Conv& cv = d->conv[l];
     d->tc_off.push_back(wtc);
     wtc += (size_t)((cv.cin * 9 + kTcKC - 1) / kTcKC) * cv.cout * kTcKC;
+    d->tct_off.push_back(wtct);
+    if (cv.cin >= 16) wtct += (size_t)((cv.cout * 9 + kTcKC - 1) / kTcKC) * cv.cin * kTcKC;
   }
   for (const Step3& stp : kSteps) {
     int c, hh, ww, tiles, nst;
@@ -1367,6 +1612,7 @@ int orbit_denoiser_create(orbit_denoiser_t** out, int max_batch, int h, int w, u
   }
   e = cudaMalloc(&d->d_scratch, sizeof(float) * scratch);
   if (e == cudaSuccess) e = cudaMalloc(&d->d_wtc, sizeof(float) * wtc);
+  if (e == cudaSuccess) e = cudaMalloc(&d->d_wtct, sizeof(float) * (wtct ? wtct : 1));
   if (e == cudaSuccess) e = cudaMalloc(&d->d_err, sizeof(int));
   if (e == cudaSuccess) e = cudaMemset(d->d_err, 0, sizeof(int));
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_conv3_tc<16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
@@ -1391,7 +1637,8 @@ int orbit_denoiser_destroy(orbit_denoiser_t* d) {
   for (auto v : {&d->ms_y, &d->ms_t, &d->ms_g})
     for (float* p : *v)
       if (p) cudaFree(p);
-  void* bufs[] = {d->d_p, d->d_pb, d->d_g, d->d_m, d->d_v, d->d_isw, d->d_loss, d->d_scratch, d->d_wtc, d->d_err};
+  void* bufs[] = {d->d_p,       d->d_pb,  d->d_g,    d->d_m,  d->d_v, d->d_isw,
+                  d->d_loss,    d->d_scratch, d->d_wtc, d->d_wtct, d->d_err};
   for (void* b : bufs) if (b) cudaFree(b);
   if (d->stream) cudaStreamDestroy(d->stream);
   delete d;
@@ -1424,6 +1671,7 @@ int orbit_denoiser_set_params(orbit_denoiser_t* d, const float* host) {
   k_to_bf16<<<grid_1d(d->nparam), 256, 0, d->stream>>>(d->d_p, d->d_pb, d->d_isw, d->nparam);
   ORBIT_LAUNCH_CHECK("orbit_denoiser_set_params");
   d->tc_stale = true;
+  d->tct_stale = true;
   ORBIT_CUDA(cudaStreamSynchronize(d->stream));
   return ORBIT_OK;
 }
@@ -1438,6 +1686,13 @@ int orbit_denoiser_forward(orbit_denoiser_t* d, const float* dev_in, float* dev_
   rc = forward(d, nb, st, true);
   if (rc) return rc;
   ORBIT_CUDA(cudaMemcpyAsync(dev_out, d->act[Y], sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
+  return ORBIT_OK;
+}
+
+int orbit_denoiser_set_batch_tensor_cores(orbit_denoiser_t* d, int on) {
+  if (!d) return set_error(ORBIT_ERR_ARG, "orbit_denoiser_set_batch_tensor_cores: bad argument");
+  if (d->stream) ORBIT_CUDA(cudaStreamSynchronize(d->stream));
+  d->tcb = on != 0;
   return ORBIT_OK;
 }
 
@@ -1510,9 +1765,11 @@ int orbit_denoiser_train_step(orbit_denoiser_t* d, const float* dev_in, const fl
                                               b2, eps, c1, c2);
   ORBIT_LAUNCH_CHECK("denoiser adam");
   d->tc_stale = true;
+  d->tct_stale = true;
   if (loss) {
     ORBIT_CUDA(cudaMemcpyAsync(loss, d->d_loss, sizeof(float), cudaMemcpyDeviceToHost, st));
     ORBIT_CUDA(cudaStreamSynchronize(st));
+    return tcb_status(d);
   }
   return ORBIT_OK;
 }
@@ -1533,7 +1790,7 @@ int orbit_denoiser_gradients(orbit_denoiser_t* d, const float* dev_in, const flo
   if (dev_out) ORBIT_CUDA(cudaMemcpyAsync(dev_out, d->act[Y], sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
   ORBIT_CUDA(cudaMemsetAsync(d->d_g, 0, sizeof(float) * d->nparam, st));
   ORBIT_CUDA(cudaStreamSynchronize(st));
-  return ORBIT_OK;
+  return tcb_status(d);
 }
 
 }  // extern "C"

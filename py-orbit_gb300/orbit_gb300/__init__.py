@@ -376,6 +376,13 @@ class DeviceDenoiser:
     def tensor_cores(self, on: bool):
         call("orbit_denoiser_set_tensor_cores", self.h, int(bool(on)))
 
+    def set_batch_tensor_cores(self, on: bool = True):
+        """Batches (training steps, gradients, batched forwards): the 3x3
+        layers' forward and data gradient on the tensor cores (TF32
+        operands, FP32 accumulation); the weight gradients stay on the CUDA
+        cores.  Off by default."""
+        call("orbit_denoiser_set_batch_tensor_cores", self.h, int(bool(on)))
+
     def tensor_errors(self) -> int:
         """Error bits of the tensor-core layers since the last call (then
         cleared): 1 = a bounded wait gave up, 2 = an MMA had not completed

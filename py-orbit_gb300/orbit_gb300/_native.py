@@ -151,6 +151,7 @@ _SIGS = {
     "orbit_denoiser_set_params": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_float)]),
     "orbit_denoiser_forward": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, _vp]),
     "orbit_denoiser_set_tensor_cores": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "orbit_denoiser_set_batch_tensor_cores": (ctypes.c_int, [_vp, ctypes.c_int]),
     "orbit_denoiser_tensor_status": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
     "orbit_denoiser_set_wait_limit": (ctypes.c_int, [_vp, ctypes.c_longlong, ctypes.c_int]),
     "orbit_denoiser_set_loss": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
