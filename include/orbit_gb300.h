@@ -417,10 +417,9 @@ int orbit_denoiser_forward(orbit_denoiser_t* d, const float* dev_in, float* dev_
  * 0; batches and training use the CUDA-core layers. */
 int orbit_denoiser_set_tensor_cores(orbit_denoiser_t* d, int on);
 /* Batches (training steps, gradients and batched forwards) run their 3x3
- * layers' forward and data gradient on the tensor cores when `on` (TF32
- * operands, FP32 accumulation, every K stage of a 128-pixel tile
- * accumulated in tensor memory); the weight gradients stay on the CUDA
- * cores.  Off by default.  A synchronised step that finds a tensor-core
+ * layers' forward, data gradient and weight gradient on the tensor cores
+ * when `on` (TF32 operands, FP32 accumulation in tensor memory).  Off by
+ * default.  A synchronised step that finds a tensor-core
  * wait gave up returns ORBIT_ERR_DEVICE and the network falls back to the
  * CUDA cores (see orbit_denoiser_tensor_status). */
 int orbit_denoiser_set_batch_tensor_cores(orbit_denoiser_t* d, int on);

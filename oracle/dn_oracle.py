@@ -127,9 +127,9 @@ def loss_and_grads(p, x0, t, weights=None, tf32_operands=False):
     gradient is sum_s w_s (P^T)^s 2 (P^s y - P^s t) / n_s.  With
     tf32_operands, the operands the device's batched tensor-core layers
     round to TF32 are rounded here too: the input of every 3x3 convolution
-    in the forward pass and the output gradient entering every data
-    gradient (the weight gradients use the unrounded values, as the
-    device's CUDA-core weight-gradient kernel does)."""
+    in the forward pass, and in the backward pass the layer input and the
+    output gradient entering the weight and data gradients (the bias
+    gradient sums the unrounded output gradient)."""
     ws, ow, ob = unpack(p)
     y, A = forward(p, x0, tf32_inputs=tf32_operands)
     t = np.asarray(t, dtype=np.float64)
@@ -162,7 +162,7 @@ def loss_and_grads(p, x0, t, weights=None, tf32_operands=False):
         dpre = D[outs[k]] * (A[outs[k]] > 0)
         dW, db, dx = conv3_bwd(A[srcs[k]], ws[k][0], dpre)
         if tf32_operands:
-            dx = conv3_bwd(A[srcs[k]], ws[k][0], tf32(dpre))[2]
+            dW, _, dx = conv3_bwd(tf32(A[srcs[k]]), ws[k][0], tf32(dpre))
         w, b, ci, co = convs[k]
         g[w:w + ci * co * 9] = dW.ravel()
         g[b:b + co] = db

@@ -470,6 +470,161 @@ __global__ void __launch_bounds__(128) k_conv3_tcb(const float* __restrict__ in,
   }
 }
 
+// Weight and bias gradients of a 3x3 layer on the tensor cores:
+// dW[o][k] = sum_p dy[o][p] X[k][p] over the batch's pixels p (X the im2col
+// of the layer's input, k = tap * cin + ci): an M = 128 (rows o < cout, the
+// rest zero) x N = 64 (a chunk of k) product whose K runs over a slice of
+// 32-pixel stages, accumulated in TMEM; the next stage's loads overlap the
+// MMAs.  CTA (chunk, slice) adds its sums to dW with atomics, and the CTAs
+// of chunk 0 also the bias gradient sum_p dy[o][p].  TF32 operands, FP32
+// accumulation; bounded waits as in k_conv3_tc (a CTA whose wait gives up
+// adds nothing).
+static const int kWgNC = 64;  // columns of k per CTA
+
+__global__ void __launch_bounds__(128) k_conv3_wgrad_tc(const float* __restrict__ x, int cin,
+                                                        const float* __restrict__ dy, int cout, int H, int W,
+                                                        int nb, int spc, float* __restrict__ dw,
+                                                        float* __restrict__ db, int* err, TcWait tw) {
+  extern __shared__ unsigned char tc_raw[];
+  __shared__ __align__(8) uint64_t s_bar;
+  __shared__ uint32_t s_tmem;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const uint32_t raw = smem_u32(tc_raw);
+  const uint32_t sA = (raw + 1023u) & ~1023u, sB = sA + kTcStageA;
+  unsigned char* gA = tc_raw + (sA - raw);
+  const int HW = H * W, P = nb * HW, K9 = 9 * cin;
+  const int k0 = blockIdx.x * kWgNC;
+  const int p_begin = blockIdx.y * spc * kTcKC;
+  const int nst = min(spc, (P - p_begin + kTcKC - 1) / kTcKC);
+  // B row of this thread: k = k0 + (tid >> 1), pixels 16 (tid & 1) .. + 15
+  const int kb = k0 + (tid >> 1), half = tid & 1;
+  const bool kvalid = kb < K9;
+  const int tap = kvalid ? kb / cin : 0, ci = kvalid ? kb % cin : 0;
+  const int ky = tap / 3 - 1, kx = tap % 3 - 1;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&s_tmem)),
+                 "r"((uint32_t)kWgNC));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s_bar)));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = s_tmem;
+  float va[kTcKC], vb[16];
+  float bsum = 0.f;
+  auto load_stage = [&](int st) {
+    const int p0 = p_begin + st * kTcKC;
+    if (tid < cout) {  // A row o = tid: dy[o] at the stage's 32 pixels
+      int p = p0, img = p0 / HW, q = p0 - img * HW;
+#pragma unroll
+      for (int e = 0; e < kTcKC; ++e) {
+        va[e] = p < P ? __ldg(dy + ((size_t)img * cout + tid) * HW + q) : 0.f;
+        ++p;
+        if (++q == HW) {
+          q = 0;
+          ++img;
+        }
+      }
+    } else {
+#pragma unroll
+      for (int e = 0; e < kTcKC; ++e) va[e] = 0.f;
+    }
+    int p = p0 + 16 * half, img = p / HW, q = p - img * HW, py = q / W, px = q - py * W;
+#pragma unroll
+    for (int e = 0; e < 16; ++e) {
+      const int yy = py + ky, xx = px + kx;
+      const bool inb = kvalid && p < P && yy >= 0 && yy < H && xx >= 0 && xx < W;
+      vb[e] = inb ? __ldg(x + ((size_t)img * cin + ci) * HW + yy * W + xx) : 0.f;
+      ++p;
+      if (++px == W) {
+        px = 0;
+        if (++py == H) {
+          py = 0;
+          ++img;
+        }
+      }
+    }
+  };
+  unsigned char* a_row = gA + (tid >> 3) * 1024 + (tid & 7) * 16;
+  const int rb = tid >> 1;
+  unsigned char* b_row = gA + kTcStageA + (rb >> 3) * 1024 + (rb & 7) * 16 + half * 4 * 128;
+  bool ok = true;
+  int s = 0;
+  load_stage(0);
+  for (; s < nst; ++s) {
+    if (blockIdx.x == 0 && tid < cout) {
+#pragma unroll
+      for (int e = 0; e < kTcKC; ++e) bsum += va[e];
+    }
+#pragma unroll
+    for (int u = 0; u < kTcKC / 4; ++u)
+      *reinterpret_cast<float4*>(a_row + u * 128) =
+          make_float4(to_tf32(va[4 * u]), to_tf32(va[4 * u + 1]), to_tf32(va[4 * u + 2]), to_tf32(va[4 * u + 3]));
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      *reinterpret_cast<float4*>(b_row + u * 128) =
+          make_float4(to_tf32(vb[4 * u]), to_tf32(vb[4 * u + 1]), to_tf32(vb[4 * u + 2]), to_tf32(vb[4 * u + 3]));
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (tid == 0 && !tw.withhold) {
+#pragma unroll
+      for (int j = 0; j < kTcKC / 8; ++j) {
+        const uint64_t ad = tc_desc(sA + 256u * j), bd = tc_desc(sB + 256u * j);
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(tc_idesc(kWgNC)), "r"((s > 0 || j > 0) ? 1u : 0u));
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       smem_u32(&s_bar))
+                   : "memory");
+    }
+    if (s + 1 < nst) load_stage(s + 1);
+    ok = __syncthreads_and(mbar_wait_bounded(smem_u32(&s_bar), (uint32_t)(s & 1), tw.cycles));
+    if (!ok) break;
+  }
+  if (!ok) {
+    if (tid == 0) atomicOr(err, 1);
+    if (!tw.withhold &&
+        !__syncthreads_and(mbar_wait_bounded(smem_u32(&s_bar), (uint32_t)(s & 1), tw.cycles)) && tid == 0)
+      atomicOr(err, 2);
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  if (ok) {
+    // row o = tid of D: TMEM lane 32 * warp + lane, columns 0..63 = k0..k0+63
+#pragma unroll
+    for (int c0 = 0; c0 < kWgNC; c0 += 16) {
+      uint32_t r[16];
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0));
+      asm volatile("tcgen05.wait::ld.sync.aligned;");
+      if (tid < cout) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int k = k0 + c0 + j;
+          if (k < K9) atomicAdd(dw + ((size_t)tid * cin + k % cin) * 9 + k / cin, __uint_as_float(r[j]));
+        }
+      }
+    }
+    if (blockIdx.x == 0 && tid < cout) atomicAdd(db + tid, bsum);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)kWgNC));
+  }
+}
+
 // The data-gradient weights of one layer (cout x cin x 3 x 3, BF16) packed
 // for k_conv3_tcb<cin, 1>: output row ci, K column k = tap' * cout + o with
 // the flipped tap (weight W[o][ci][8 - tap']), stages of 32 in the layout of
@@ -1300,11 +1455,26 @@ static int conv_bwd(orbit_denoiser_t* d, const Step3& s, int nb, cudaStream_t st
   size_t n_out = act_size(d, s.out, nb);
   k_relu_bwd<<<grid_1d(n_out), 256, 0, st>>>(d->grad[s.out], d->act[s.out], n_out);
   const int tiles = ((w + kT - 1) / kT) * ((h + kT - 1) / kT);
-  const int ttot = tiles * nb;
-  const int split = ttot < 64 ? ttot : 64;
-  dim3 gw(((cv.cout + kCo - 1) / kCo) * ((cv.cin + kCi - 1) / kCi), split);
-  k_conv3_wgrad<<<gw, 256, 0, st>>>(d->act[s.in], cv.cin, d->grad[s.out], cv.cout, h, w, nb, d->d_g + cv.w_off,
-                                    d->d_g + cv.b_off);
+  if (use_tcb(d)) {
+    // chunks of 64 weight columns x slices of the batch's pixels, about
+    // four CTAs per SM in all
+    const int chunks = (cv.cin * 9 + kWgNC - 1) / kWgNC;
+    const int stages = (int)(((long long)nb * h * w + kTcKC - 1) / kTcKC);
+    int want = 4 * num_sms() / chunks;
+    want = want < 1 ? 1 : want;
+    const int spc = (stages + want - 1) / want;
+    const int slices = (stages + spc - 1) / spc;
+    const TcWait tw = {d->tc_wait_cycles, d->tc_withhold};
+    k_conv3_wgrad_tc<<<dim3(chunks, slices), 128, kTcSmem, st>>>(d->act[s.in], cv.cin, d->grad[s.out], cv.cout, h,
+                                                                w, nb, spc, d->d_g + cv.w_off, d->d_g + cv.b_off,
+                                                                d->d_err, tw);
+  } else {
+    const int ttot = tiles * nb;
+    const int split = ttot < 64 ? ttot : 64;
+    dim3 gw(((cv.cout + kCo - 1) / kCo) * ((cv.cin + kCi - 1) / kCi), split);
+    k_conv3_wgrad<<<gw, 256, 0, st>>>(d->act[s.in], cv.cin, d->grad[s.out], cv.cout, h, w, nb, d->d_g + cv.w_off,
+                                      d->d_g + cv.b_off);
+  }
   if (s.in != X0) {
     // data gradient: dy convolved with the flipped, transposed kernel
     if (use_tcb(d)) {

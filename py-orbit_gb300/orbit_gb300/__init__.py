@@ -378,9 +378,8 @@ class DeviceDenoiser:
 
     def set_batch_tensor_cores(self, on: bool = True):
         """Batches (training steps, gradients, batched forwards): the 3x3
-        layers' forward and data gradient on the tensor cores (TF32
-        operands, FP32 accumulation); the weight gradients stay on the CUDA
-        cores.  Off by default."""
+        layers' forward, data gradient and weight gradient on the tensor
+        cores (TF32 operands, FP32 accumulation).  Off by default."""
         call("orbit_denoiser_set_batch_tensor_cores", self.h, int(bool(on)))
 
     def tensor_errors(self) -> int:

@@ -11,6 +11,8 @@ benchmark, for profiling its kernels (ncu summaries) and for timing them:
             kick), 128x128x64, 4e6 particles
   train     denoiser training steps (CUDA-core convolution forward, data and
             weight gradients, Adam) on batches of 16 128x128 images
+  train_tc  the same steps with the 3x3 layers on the tensor cores
+            (k_conv3_tcb forward and data gradient, k_conv3_wgrad_tc)
   batch     a 6-bunch batched scan (grids 64x64x32, 128x128x64, 256x256x64)
 
 Usage: python py-orbit_gb300/orbit_gb300/cases.py CASE [--n N] [--repeat R]
@@ -90,10 +92,11 @@ def case_fp32(n):
     return step
 
 
-def case_train(n):
+def case_train(n, tensor_cores=False):
     import torch
     from orbit_gb300 import DeviceDenoiser
     net = DeviceDenoiser(128, 128, max_batch=16, seed=1)
+    net.set_batch_tensor_cores(tensor_cores)
     g = torch.Generator(device="cuda").manual_seed(0)
     x = torch.rand((16, 1, 128, 128), device="cuda", generator=g)
     t = torch.rand((16, 1, 128, 128), device="cuda", generator=g)
@@ -124,7 +127,8 @@ def case_batch(n):
 
 
 CASES = {"diag": (case_diag, 4_000_000), "boundary": (case_boundary, 2_000_000), "rb": (case_rb, 2_000_000),
-         "fp32": (case_fp32, 4_000_000), "train": (case_train, 0), "batch": (case_batch, 400_000)}
+         "fp32": (case_fp32, 4_000_000), "train": (case_train, 0),
+         "train_tc": (lambda n: case_train(n, tensor_cores=True), 0), "batch": (case_batch, 400_000)}
 
 
 def main(argv=None):

@@ -1,12 +1,13 @@
 """Batches on the tensor cores (orbit_denoiser_set_batch_tensor_cores): the
-denoiser's 3x3 layers, forward and data gradient, as tcgen05 MMAs (TF32
-operands, FP32 accumulation, every K stage of a 128-pixel tile of the
-batch accumulated in tensor memory); the weight gradients stay on the
-CUDA cores.
+denoiser's 3x3 layers, forward, data gradient and weight gradient, as
+tcgen05 MMAs (TF32 operands, FP32 accumulation in tensor memory: every K
+stage of a 128-pixel tile for the forward and data gradient, a slice of
+the batch's pixels for the weight gradient).
 
 Against the float64 oracle that rounds the same operands to TF32 (every
-3x3 convolution's input in the forward pass, the output gradient entering
-every data gradient) and against the CUDA-core layers; a short training
+3x3 convolution's input in the forward pass; the layer input and the
+output gradient entering the weight and data gradients) and against the
+CUDA-core layers; a short training
 run on the tensor cores gains as much as one on the CUDA cores; a bounded
 wait that runs out (no MMA issued, a test hook) makes the step report the
 error and the network fall back to the CUDA cores.
@@ -101,9 +102,7 @@ def test_training_on_tensor_cores_gains_like_cuda_cores():
     gains = {}
     for tcb in (True, False):
         net = DeviceDenoiser(128, 128, max_batch=16, seed=3)
-        net.set_batch_tensor_cores(tcb)
-        DN.train(net, X[:512], T[:512], epochs=4, batch=16, lr=1e-3)
-        net.set_batch_tensor_cores(False)
+        DN.train(net, X[:512], T[:512], epochs=4, batch=16, lr=1e-3, tensor_cores=tcb)
         gains[tcb] = DN.evaluate(net, X[512:], T[512:])["gain"]
     print("held-out gain: tensor cores %.2f, CUDA cores %.2f" % (gains[True], gains[False]))
     assert gains[True] >= 2.0
