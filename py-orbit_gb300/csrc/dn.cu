@@ -1123,6 +1123,7 @@ struct orbit_denoiser {
   // repacked after any parameter change; error flag of its bounded waits
   bool tc = true;
   bool tc_stale = true;
+  unsigned long long version = 1;  // bumped by every parameter change
   float* d_wtc = nullptr;
   std::vector<size_t> tc_off;
   int* d_err = nullptr;
@@ -1380,6 +1381,12 @@ static int forward(orbit_denoiser_t* d, int nb, cudaStream_t st, bool infer = fa
   const bool tc = infer && d->tc && !d->tc_failed && !g_tc_untrusted && nb == 1;
   const bool tcb = !tc && use_tcb(d);
   if ((tc || tcb) && d->tc_stale) {
+    // a packing captured into a graph would run only where that graph is
+    // replayed: captures find the weights packed (dn_prepare_capture)
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    ORBIT_CUDA(cudaStreamIsCapturing(st, &cs));
+    if (cs != cudaStreamCaptureStatusNone)
+      return set_error(ORBIT_ERR_UNSUPPORTED, "denoiser: parameters changed without dn_prepare_capture before a capture");
     int rc = tc_pack(d, st);
     if (rc) return rc;
   }
@@ -1613,6 +1620,18 @@ static int tcb_status(orbit_denoiser_t* d) {
   return set_error(ORBIT_ERR_DEVICE, "denoiser: a tensor-core wait gave up; the network now runs on the CUDA cores");
 }
 
+unsigned long long dn_version(const orbit_denoiser_t* d) { return d ? d->version : 0ull; }
+
+int dn_prepare_capture(orbit_denoiser_t* d) {
+  if (!d || !d->tc_stale) return ORBIT_OK;
+  // forwards in flight may still read the packed weights
+  ORBIT_CUDA(cudaDeviceSynchronize());
+  int rc = tc_pack(d, d->stream);
+  if (rc) return rc;
+  ORBIT_CUDA(cudaStreamSynchronize(d->stream));
+  return ORBIT_OK;
+}
+
 int dn_closure_io(orbit_denoiser_t* d, float** in, const float** out, int* nparts) {
   if (!d) return set_error(ORBIT_ERR_ARG, "dn_closure_io: null network");
   *in = d->act[X0];
@@ -1842,6 +1861,7 @@ int orbit_denoiser_set_params(orbit_denoiser_t* d, const float* host) {
   ORBIT_LAUNCH_CHECK("orbit_denoiser_set_params");
   d->tc_stale = true;
   d->tct_stale = true;
+  ++d->version;
   ORBIT_CUDA(cudaStreamSynchronize(d->stream));
   return ORBIT_OK;
 }
@@ -1936,6 +1956,7 @@ int orbit_denoiser_train_step(orbit_denoiser_t* d, const float* dev_in, const fl
   ORBIT_LAUNCH_CHECK("denoiser adam");
   d->tc_stale = true;
   d->tct_stale = true;
+  ++d->version;
   if (loss) {
     ORBIT_CUDA(cudaMemcpyAsync(loss, d->d_loss, sizeof(float), cudaMemcpyDeviceToHost, st));
     ORBIT_CUDA(cudaStreamSynchronize(st));

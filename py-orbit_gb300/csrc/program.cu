@@ -469,13 +469,19 @@ static int capture(orbit_program_t* p, orbit_bunch_t* bu, const Plan& plan, bool
 }
 
 static int prepare(orbit_program_t* p, orbit_bunch_t* bu) {
+  auto dnv = [](const orbit_sc2p5d_t* c) { return c && c->dn ? dn_version(c->dn) : 0ull; };
   bool same = p->key_bunch == bu && p->key_n == bu->n && p->key_coords == bu->d_coords &&
               p->key_msize == bu->has_msize && sync_equal(p->key_sync, bu->sync) && p->g_mid &&
-              p->key_gen.size() == p->calcs.size();
+              p->key_gen.size() == p->calcs.size() && p->key_dnv.size() == p->calcs.size();
   for (size_t i = 0; same && i < p->calcs.size(); ++i)
-    same = p->key_gen[i] == (p->calcs[i] ? p->calcs[i]->cfg_gen : 0ull);
+    same = p->key_gen[i] == (p->calcs[i] ? p->calcs[i]->cfg_gen : 0ull) && p->key_dnv[i] == dnv(p->calcs[i]);
   if (same) return ORBIT_OK;
   free_graphs(p);
+  for (auto c : p->calcs)
+    if (c && c->dn) {
+      int prc = dn_prepare_capture(c->dn);
+      if (prc) return prc;
+    }
   Plan plan;
   int rc = compile(p, bu, plan);
   if (rc) return rc;
@@ -491,7 +497,11 @@ static int prepare(orbit_program_t* p, orbit_bunch_t* bu) {
   p->key_sync = bu->sync;
   p->key_msize = bu->has_msize;
   p->key_gen.resize(p->calcs.size());
-  for (size_t i = 0; i < p->calcs.size(); ++i) p->key_gen[i] = p->calcs[i] ? p->calcs[i]->cfg_gen : 0ull;
+  p->key_dnv.resize(p->calcs.size());
+  for (size_t i = 0; i < p->calcs.size(); ++i) {
+    p->key_gen[i] = p->calcs[i] ? p->calcs[i]->cfg_gen : 0ull;
+    p->key_dnv[i] = dnv(p->calcs[i]);
+  }
   return ORBIT_OK;
 }
 

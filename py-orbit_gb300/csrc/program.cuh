@@ -19,6 +19,7 @@ struct orbit_program {
   orbit_sync_t key_sync{};
   int key_msize = -1;
   std::vector<unsigned long long> key_gen;  // the calculators' cfg_gen
+  std::vector<unsigned long long> key_dnv;  // their networks' parameter versions
   orbit::DevOp* d_ops = nullptr;
   int n_devops = 0;
   double* d_knl = nullptr;            // per-particle 1/(1+dp_p) between passes

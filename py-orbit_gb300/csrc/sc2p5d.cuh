@@ -102,6 +102,12 @@ int* dn_error_flag(orbit_denoiser* d);
 // *nparts per-block sums of the output clamped at zero into parts.
 int dn_closure_io(orbit_denoiser* d, float** in, const float** out, int* nparts);
 int dn_forward_inplace(orbit_denoiser* d, cudaStream_t st, double* parts);
+// The network's parameter version (bumped by every change) and, before a
+// stream capture that runs it, the packing of its tensor-core weights done
+// eagerly when a change left them stale (a packing captured into one graph
+// would not run where another graph is replayed).
+unsigned long long dn_version(const orbit_denoiser* d);
+int dn_prepare_capture(orbit_denoiser* d);
 constexpr int kDnMaxParts = 4096;  // sums the closure's buffer holds
 }  // namespace orbit
 

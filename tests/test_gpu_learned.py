@@ -243,3 +243,37 @@ def test_closure_removed_after_capture_is_captured_again():
         out.append(b.getCoordinates())
     assert np.array_equal(out[0], out[1])
     assert not np.array_equal(out[0], out[2])
+
+
+def test_closure_first_used_inside_a_one_turn_program():
+    """A network whose parameters just changed, first run inside a captured
+    one-turn lattice program: its tensor-core weights are packed before the
+    capture (a packing captured into the program's multi-turn graph would
+    not run in the one-turn graph).  Against the eager walk of the same turn
+    (within the coordinate tolerance of the program's fused maps) and
+    unlike the turn without the closure."""
+    from orbit_gb300 import denoiser as DN
+    from orbit_gb300 import workloads as W
+    from spacecharge import SpaceChargeCalc2p5D
+    from helpers import TOL_COORD, coord_err
+    soa = W.c2_coords(100_000, seed=45)
+    rng = np.random.default_rng(45)
+    out = {}
+    for mode in ("program", "eager", "none"):
+        net = DN.default_network()
+        p = net.get_params()
+        net.set_params(p * (1.0 + 1e-3 * rng.standard_normal(p.shape)).astype(np.float32) if mode != "none" else p)
+        rng = np.random.default_rng(45)  # the same perturbation for both closures
+        calc = SpaceChargeCalc2p5D(128, 128, 64)
+        if mode != "none":
+            calc.setDenoiser(net, 10, 1e-3)
+        with contextlib.redirect_stdout(io.StringIO()):
+            lat = W.fodo_lattice(calc, cells=3)
+        lat.setFusedTracking(mode != "eager")
+        b = W.make_bunch(soa.copy(), W.C2_MACROSIZE * 10)
+        lat.trackBunch(b)
+        out[mode] = b.getCoordinates()
+        if mode != "none":
+            assert calc.getDenoiserState()["fallback"] == 0
+    assert coord_err(out["program"], out["eager"]) <= TOL_COORD
+    assert coord_err(out["program"], out["none"]) > 1e3 * TOL_COORD
