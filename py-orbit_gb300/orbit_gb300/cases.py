@@ -6,8 +6,9 @@ benchmark, for profiling its kernels (ncu summaries) and for timing them:
   boundary  trackBunch with a 128-point circular conducting boundary,
             128x128x32 grid, 2e6 particles
   rb        SpaceChargeCalc2p5Drb.trackBunch, 128x128x64, 2e6 particles
-  fp32      the FP32 field form: eager trackBunch (k_deposit_fp32,
-            k_kick_fp32) and a 4-cell FODO program (fused pass with the FP32
+  fp32      the FP32 field form: eager trackBunch (k_deposit_plain, the
+            fixed-point deposit both forms use, and k_kick_fp32) and a
+            4-cell FODO program (fused pass with the FP32
             kick), 128x128x64, 4e6 particles
   train     denoiser training steps (CUDA-core convolution forward, data and
             weight gradients, Adam) on batches of 16 128x128 images
