@@ -40,8 +40,14 @@ void prof_begin(const char* tag, cudaStream_t s) {
   g_prof->recs.push_back(r);
 }
 
+// The host waits for each timed launch, so that every bracket times its own
+// launch alone: without the wait, the brackets of the large ring's eager
+// turn (1.6e7 particles, launches of milliseconds) each read about one kick
+// longer than the launch they enclose, their sum six times the turn.
 void prof_end(cudaStream_t s) {
-  if (!g_prof->recs.empty()) cudaEventRecord(g_prof->recs.back().b, s);
+  if (g_prof->recs.empty()) return;
+  cudaEventRecord(g_prof->recs.back().b, s);
+  cudaEventSynchronize(g_prof->recs.back().b);
 }
 
 Profiler* prof_install() {
