@@ -84,3 +84,32 @@ def test_oracle_multiscale_loss_gradient_by_finite_differences():
         b[i] -= h
         fd = (D.loss_and_grads(a, x, t, wts)[0] - D.loss_and_grads(b, x, t, wts)[0]) / (2 * h)
         assert abs(fd - g[i]) <= 1e-6 * max(1.0, abs(fd)), (i, fd, g[i])
+
+
+def test_tf32_rounding_and_the_rounded_operand_model():
+    """TF32 rounding (10 mantissa bits, to nearest, ties away from zero) and
+    the oracle's model of the batched tensor-core layers: its output is the
+    forward pass with TF32 conv inputs, and its gradients differ from the
+    unrounded ones by about the TF32 rounding, not more."""
+    x = np.array([1.0, 1.0 + 2.0 ** -11, 1.0 + 3 * 2.0 ** -11, -2.5, 0.0], dtype=np.float32)
+    r = D.tf32(x)
+    assert r[0] == 1.0 and r[4] == 0.0 and r[3] == -2.5
+    assert r[1] == 1.0 + 2.0 ** -10          # a tie rounds away from zero
+    assert r[2] == 1.0 + 2.0 ** -9
+    rng = np.random.default_rng(8)
+    convs, ow, ob, n = D.layout()
+    p = np.zeros(n, dtype=np.float32)
+    for (w, b, ci, co) in convs:
+        p[w:w + ci * co * 9] = D.bf16(rng.normal(0, np.sqrt(2.0 / (9 * ci)), ci * co * 9))
+        p[b:b + co] = rng.normal(0, 0.05, co)
+    p[ow:ow + 16] = rng.normal(0, 0.1, 16)
+    x0 = rng.uniform(0.0, 2.0, (1, 1, 16, 16)).astype(np.float32)
+    t = (x0 + rng.normal(0, 0.1, x0.shape)).astype(np.float32)
+    pd = p.astype(np.float64)
+    loss_r, g_r, y_r = D.loss_and_grads(pd, x0, t, tf32_operands=True)
+    y_f, _ = D.forward(pd, x0, tf32_inputs=True)
+    assert np.array_equal(y_r, y_f)
+    loss, g, y = D.loss_and_grads(pd, x0, t)
+    assert 0 < np.abs(y_r - y).max() <= 1e-2 * np.abs(y).max()
+    assert np.abs(g_r - g).max() <= 5e-2 * np.abs(g).max()
+    assert not np.array_equal(g_r, g)
